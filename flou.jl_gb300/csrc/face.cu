@@ -1,0 +1,30 @@
+// Face kernels (traces, boundary states, numerical fluxes) for every dimension and equation.
+#include "flou_internal.cuh"
+namespace flou {
+template <int DIM, int EQ>
+static cudaError_t launch_face_t(bool lgl, const FaceParams& P, cudaStream_t s) {
+    int64_t nthreads = (int64_t)P.nfaces * P.nfd;
+    if (nthreads == 0) return cudaSuccess;
+    int grid = (int)((nthreads + 255) / 256);
+    if (lgl) face_kernel<DIM, EQ, true><<<grid, 256, 0, s>>>(P);
+    else face_kernel<DIM, EQ, false><<<grid, 256, 0, s>>>(P);
+    return cudaGetLastError();
+}
+cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s) {
+    if (eq == FLOU_EQ_EULER) {
+        if (dim == 1) return launch_face_t<1, FLOU_EQ_EULER>(lgl, P, s);
+        if (dim == 2) return launch_face_t<2, FLOU_EQ_EULER>(lgl, P, s);
+        return launch_face_t<3, FLOU_EQ_EULER>(lgl, P, s);
+    }
+    if (eq == FLOU_EQ_BURGERS) return launch_face_t<1, FLOU_EQ_BURGERS>(lgl, P, s);
+    if (dim == 1) return launch_face_t<1, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
+    if (dim == 2) return launch_face_t<2, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
+    return launch_face_t<3, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
+}
+cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
+    if (L.eq != FLOU_EQ_EULER) return launch_elem_scalar(L, P, s);
+    if (L.dim == 1) return launch_elem_euler1d(L, P, s);
+    if (L.dim == 2) return launch_elem_euler2d(L, P, s);
+    return L.vol == FLOU_OP_STRONG ? launch_elem_euler3d_strong(L, P, s) : launch_elem_euler3d_split(L, P, s);
+}
+}  // namespace flou

@@ -1,0 +1,640 @@
+// flou_api.cu -- the C ABI of libflou_cuda (include/flou_cuda.h): context lifecycle,
+// host-side validation and compression of the set-up arrays, the residual, SSP-RK3
+// stepping replayed as a CUDA graph, the CFL time step and the FP64 peak probe.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "flou_internal.cuh"
+
+using namespace flou;
+
+struct flou_ctx {
+    flou_config cfg;
+    int nv = 0, n = 0, npe = 0, nfd = 0;
+    bool lgl = false;
+    std::string err;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    bool have_ops = false, have_mesh = false, have_geom = false;
+    int nelem = 0, nfaces = 0;
+    int64_t ndofs = 0, nfdofs = 0;
+    std::vector<double> omega;              // quadrature weights (1D)
+    std::vector<double> h_invJ, h_J;        // per element
+    int nbcs = 0;
+    int bc_kind[MAXBC] = {0};
+    double bc_state[MAXBC][5] = {{0}};
+    std::vector<int8_t> h_face_bc;
+    // device buffers
+    double* d_ops = nullptr;        // Ds, D♯, l_l, l_r, dg_l, dg_r
+    int32_t* d_elem_face = nullptr;
+    int32_t* d_face_elem = nullptr;
+    int8_t* d_face_bc = nullptr;
+    double* d_faceJ = nullptr;
+    double* d_invJ = nullptr;
+    double* d_Ja = nullptr;
+    double* d_dx = nullptr;         // per-element CFL length (vol / n^d)^(1/d)
+    double* d_Fn = nullptr;         // face-flux scratch
+    double* d_U = nullptr;          // RK stage scratch
+    double* d_Qh = nullptr;         // staging for host-pointer calls
+    double* d_dQh = nullptr;
+    int32_t* d_status = nullptr;    // [flags, lowest element]
+    unsigned long long* d_dtmin = nullptr;
+    // graph cache for flou_step
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    double* g_Q = nullptr;
+    double g_dt = 0.0;
+};
+
+namespace {
+
+int fail(flou_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+int cuda_fail(flou_ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) return fail(c, FLOU_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(c, FLOU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t _e = (call);                        \
+        if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+    } while (0)
+
+template <class T>
+int upload(flou_ctx* c, T** dst, const T* src, size_t count, const char* what) {
+    if (*dst) { cudaFree(*dst); *dst = nullptr; }
+    if (count == 0) return FLOU_OK;
+    CK(cudaMalloc((void**)dst, count * sizeof(T)), what);
+    CK(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice), what);
+    return FLOU_OK;
+}
+
+int ensure(flou_ctx* c, double** buf, size_t count, const char* what) {
+    if (*buf) return FLOU_OK;
+    CK(cudaMalloc((void**)buf, count * sizeof(double)), what);
+    return FLOU_OK;
+}
+
+void drop_graph(flou_ctx* c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+    c->g_Q = nullptr;
+}
+
+int ready(flou_ctx* c) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators has not been called");
+    if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh has not been called");
+    if (!c->have_geom) return fail(c, FLOU_ERR_STATE, "flou_set_geometry has not been called");
+    for (int f = 0; f < c->nfaces; ++f) {
+        int b = c->h_face_bc[f];
+        if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
+            return fail(c, FLOU_ERR_STATE, "boundary index %d of face %d has no boundary condition", b + 1, f + 1);
+    }
+    int e = ensure(c, &c->d_Fn, (size_t)c->nfdofs * c->nv, "face-flux buffer");
+    return e;
+}
+
+FaceParams face_params(const flou_ctx* c, const double* Q) {
+    FaceParams P;
+    memset(&P, 0, sizeof(P));
+    P.Q = Q;
+    P.Fn = c->d_Fn;
+    P.face_elem = c->d_face_elem;
+    P.faceJ = c->d_faceJ;
+    P.face_bc = c->d_face_bc;
+    P.l = c->d_ops + 2 * c->n * c->n;
+    P.ndofs = c->ndofs;
+    P.nfdofs = c->nfdofs;
+    P.nfaces = c->nfaces;
+    P.n = c->n;
+    P.npe = c->npe;
+    P.nfd = c->nfd;
+    P.numflux = c->cfg.numflux;
+    P.lxf_avg = c->cfg.numflux_avg;
+    P.intensity = c->cfg.numflux_intensity;
+    P.gamma = c->cfg.gamma;
+    for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
+    for (int b = 0; b < MAXBC; ++b) {
+        P.bc_kind[b] = c->bc_kind[b];
+        for (int k = 0; k < 5; ++k) P.bc_state[b][k] = c->bc_state[b][k];
+    }
+    return P;
+}
+
+ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, double* out, int mode, double dt,
+                       double a0, double a1) {
+    ElemParams P;
+    memset(&P, 0, sizeof(P));
+    P.Q = Q;
+    P.Q0 = Q0;
+    P.out = out;
+    P.Fn = c->d_Fn;
+    P.elem_face = c->d_elem_face;
+    P.elem_invJ = c->d_invJ;
+    P.elem_Ja = c->d_Ja;
+    P.ops = c->d_ops;
+    P.ndofs = c->ndofs;
+    P.nfdofs = c->nfdofs;
+    P.nelem = c->nelem;
+    P.mode = mode;
+    P.dt = dt;
+    P.a0 = a0;
+    P.a1 = a1;
+    P.gamma = c->cfg.gamma;
+    for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
+    P.status = c->d_status;
+    return P;
+}
+
+ElemLaunch elem_launch(const flou_ctx* c) {
+    ElemLaunch L;
+    L.dim = c->cfg.dim;
+    L.eq = c->cfg.equation;
+    L.n = c->n;
+    L.vol = c->cfg.volume_op;
+    L.tp = c->cfg.twopoint_flux;
+    L.lgl = c->lgl;
+    L.prepare = false;
+    return L;
+}
+
+// One residual evaluation followed by the stage combination selected by `mode`.
+int stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
+          double a0, double a1) {
+    cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
+    e = launch_elem(elem_launch(c), elem_params(c, Q, Q0, out, mode, dt, a0, a1), s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "element kernel launch");
+    return FLOU_OK;
+}
+
+int rk3_step(flou_ctx* c, cudaStream_t s, double* Q, double dt) {
+    int r;
+    if ((r = stage(c, s, Q, Q, c->d_U, 1, dt, 0.0, 1.0))) return r;
+    if ((r = stage(c, s, c->d_U, Q, c->d_U, 2, dt, 0.75, 0.25))) return r;
+    if ((r = stage(c, s, c->d_U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;
+    return FLOU_OK;
+}
+
+int check_status(flou_ctx* c) {
+    int32_t st[2];
+    CK(cudaMemcpyAsync(st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "status read");
+    CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    if (st[0]) {
+        int32_t init[2] = {0, 0x7fffffff};
+        cudaMemcpy(c->d_status, init, sizeof(init), cudaMemcpyHostToDevice);
+        return fail(c, FLOU_ERR_NONPHYSICAL, "non-physical or non-finite state in element %d", st[1]);
+    }
+    return FLOU_OK;
+}
+
+__global__ void max_dt_kernel(const double* Q, const double* dx, int64_t ndofs, int npe, int dim, int eq,
+                              double gamma, double a0, double a1, double a2, double cfl,
+                              unsigned long long* out) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = INFINITY;
+    if (g < ndofs) {
+        double h = dx[g / npe];
+        if (eq == FLOU_EQ_LINEAR_ADVECTION) {
+            v = cfl * h / sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+        } else if (eq == FLOU_EQ_BURGERS) {
+            v = cfl * h / Q[g];   // no abs, as Burgers.jl:35-37
+        } else {
+            double rho = Q[g];
+            double m[3] = {Q[ndofs + g], dim > 1 ? Q[2 * ndofs + g] : 0.0, dim > 2 ? Q[3 * ndofs + g] : 0.0};
+            double E = Q[(dim + 1) * ndofs + g];
+            double s = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+            double p = (gamma - 1.0) * (E - s / (2.0 * rho));
+            double a = sqrt(gamma * p / rho);
+            double u = m[0] / rho, vv = m[1] / rho, w = m[2] / rho;
+            double speed = dim == 1 ? fabs(u) : sqrt(u * u + vv * vv + w * w);
+            v = cfl * h / (speed + a);
+        }
+        if (!(v == v)) v = 0.0;   // NaN -> report 0 so the caller sees a broken state
+    }
+    // warp/block min of positive doubles through their ordered bit patterns
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = (threadIdx.x < (blockDim.x + 31) / 32) ? sm[threadIdx.x] : INFINITY;
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) {
+            double w = v < 0.0 ? 0.0 : v;
+            atomicMin(out, (unsigned long long)__double_as_longlong(w));
+        }
+    }
+}
+
+// Throughput probe: independent FMA chains per thread, eight per thread for ILP.
+__global__ void fma_probe_kernel(double* sink, int iters, double x) {
+    double a0 = x, a1 = x + 1, a2 = x + 2, a3 = x + 3, a4 = x + 4, a5 = x + 5, a6 = x + 6, a7 = x + 7;
+    const double m = 0.999999999, b = 1e-9;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, m, b); a1 = fma(a1, m, b); a2 = fma(a2, m, b); a3 = fma(a3, m, b);
+        a4 = fma(a4, m, b); a5 = fma(a5, m, b); a6 = fma(a6, m, b); a7 = fma(a7, m, b);
+    }
+    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 1234.5678) sink[threadIdx.x] = s;   // never true; keeps the chains alive
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* flou_last_error(const flou_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int32_t flou_create(const flou_config* cfg, flou_ctx** out) {
+    if (!cfg || !out) return FLOU_ERR_ARG;
+    *out = nullptr;
+    if (cfg->dim < 1 || cfg->dim > 3) return FLOU_ERR_ARG;
+    if (cfg->nnodes < 2 || cfg->nnodes > MAXN) return FLOU_ERR_ARG;
+    if (cfg->equation < 0 || cfg->equation > 2) return FLOU_ERR_ARG;
+    if (cfg->equation == FLOU_EQ_BURGERS && cfg->dim != 1) return FLOU_ERR_ARG;
+    if (cfg->volume_op != FLOU_OP_STRONG && cfg->volume_op != FLOU_OP_SPLIT) return FLOU_ERR_ARG;
+    if (cfg->numflux < 0 || cfg->numflux > 4) return FLOU_ERR_ARG;
+    if (cfg->equation != FLOU_EQ_EULER && cfg->numflux != FLOU_NF_STD_AVERAGE && cfg->numflux != FLOU_NF_LXF)
+        return FLOU_ERR_UNSUPPORTED;
+    if (cfg->equation == FLOU_EQ_EULER && !(cfg->gamma > 1.0)) return FLOU_ERR_ARG;
+    flou_ctx* c = new flou_ctx();
+    c->cfg = *cfg;
+    c->n = cfg->nnodes;
+    c->nv = cfg->equation == FLOU_EQ_EULER ? cfg->dim + 2 : 1;
+    c->npe = ipow(c->n, cfg->dim);
+    c->nfd = ipow(c->n, cfg->dim - 1);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return FLOU_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    e = cudaMalloc((void**)&c->d_status, 2 * sizeof(int32_t));
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(c->own_stream);
+        delete c;
+        return FLOU_ERR_OOM;
+    }
+    int32_t init[2] = {0, 0x7fffffff};
+    cudaMemcpy(c->d_status, init, sizeof(init), cudaMemcpyHostToDevice);
+    *out = c;
+    return FLOU_OK;
+}
+
+int32_t flou_destroy(flou_ctx* c) {
+    if (!c) return FLOU_ERR_ARG;
+    drop_graph(c);
+    void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
+                    c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return FLOU_OK;
+}
+
+int32_t flou_set_stream(flou_ctx* c, void* stream) {
+    if (!c) return FLOU_ERR_ARG;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return FLOU_OK;
+}
+
+int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const double* Dsharp, const double* omega,
+                           const double* l_l, const double* l_r, const double* dg_l, const double* dg_r) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!D || !Ds || !Dsharp || !omega || !l_l || !l_r || !dg_l || !dg_r)
+        return fail(c, FLOU_ERR_ARG, "null operator pointer");
+    int n = c->n;
+    std::vector<double> ops(2 * n * n + 4 * n);
+    std::copy(Ds, Ds + n * n, ops.begin());
+    std::copy(Dsharp, Dsharp + n * n, ops.begin() + n * n);
+    std::copy(l_l, l_l + n, ops.begin() + 2 * n * n);
+    std::copy(l_r, l_r + n, ops.begin() + 2 * n * n + n);
+    std::copy(dg_l, dg_l + n, ops.begin() + 2 * n * n + 2 * n);
+    std::copy(dg_r, dg_r + n, ops.begin() + 2 * n * n + 3 * n);
+    for (double v : ops)
+        if (!std::isfinite(v)) return fail(c, FLOU_ERR_ARG, "non-finite operator entry");
+    // A basis with boundary nodes (Gauss-Lobatto) injects the end nodes: l_l = e_1,
+    // l_r = e_n and ∂g vanishes off the ends, exactly.  Then the kernels skip the zero terms
+    // (bitwise the same result); any other basis takes the general interpolation path.
+    bool lgl = l_l[0] == 1.0 && l_r[n - 1] == 1.0;
+    for (int i = 0; i < n; ++i) {
+        if (i != 0 && (l_l[i] != 0.0 || dg_l[i] != 0.0)) lgl = false;
+        if (i != n - 1 && (l_r[i] != 0.0 || dg_r[i] != 0.0)) lgl = false;
+    }
+    if (c->cfg.volume_op == FLOU_OP_SPLIT && !lgl)
+        return fail(c, FLOU_ERR_UNSUPPORTED,
+                    "the split-form operator needs a basis with boundary nodes (the subcell path of "
+                    "OpDivergence.jl:301-437 is not implemented)");
+    int r = upload(c, &c->d_ops, ops.data(), ops.size(), "operator upload");
+    if (r) return r;
+    c->lgl = lgl;
+    c->omega.assign(omega, omega + n);
+    c->have_ops = true;
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_mesh(flou_ctx* c, int32_t nelem, int32_t nfaces, const int32_t* faceinds, const int32_t* facepos,
+                      const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
+                      const int32_t* bdface_index) {
+    if (!c) return FLOU_ERR_ARG;
+    int dim = c->cfg.dim, nfpe = 2 * dim;
+    if (nelem <= 0 || nfaces <= 0 || nelem >= (1 << 27))
+        return fail(c, FLOU_ERR_ARG, "invalid sizes nelem=%d nfaces=%d", nelem, nfaces);
+    if (!faceinds || !facepos || !eleminds || !elempos || !orientation || !bdface_index)
+        return fail(c, FLOU_ERR_ARG, "null connectivity pointer");
+    std::vector<int32_t> ef((size_t)nelem * nfpe), fe((size_t)nfaces * 2);
+    std::vector<int8_t> fb(nfaces, -1);
+    for (int f = 0; f < nfaces; ++f) {
+        if (orientation[f] != 0)
+            return fail(c, FLOU_ERR_UNSUPPORTED, "face %d has orientation %d; only conforming Cartesian faces "
+                        "(orientation 0) are supported", f + 1, (int)orientation[f]);
+        for (int s = 0; s < 2; ++s) {
+            int e = eleminds[2 * f + s], p = elempos[2 * f + s];
+            if (s == 1 && e == 0) { fe[2 * f + 1] = -1; continue; }
+            if (e < 1 || e > nelem || p < 1 || p > nfpe)
+                return fail(c, FLOU_ERR_ARG, "face %d side %d: element %d / position %d out of range", f + 1, s + 1, e, p);
+            if (faceinds[(size_t)(e - 1) * nfpe + p - 1] != f + 1 || facepos[(size_t)(e - 1) * nfpe + p - 1] != s + 1)
+                return fail(c, FLOU_ERR_ARG, "face %d side %d is not face %d of element %d in faceinds/facepos",
+                            f + 1, s + 1, p, e);
+            fe[2 * f + s] = ((e - 1) << 3) | (p - 1);
+        }
+        int b = bdface_index[f];
+        if (eleminds[2 * f + 1] == 0) {
+            if (b < 1 || b > MAXBC) return fail(c, FLOU_ERR_ARG, "boundary face %d has boundary index %d", f + 1, b);
+            fb[f] = (int8_t)(b - 1);
+        } else if (b != 0) {
+            return fail(c, FLOU_ERR_ARG, "interior face %d has boundary index %d", f + 1, b);
+        }
+    }
+    for (int e = 0; e < nelem; ++e)
+        for (int k = 0; k < nfpe; ++k) {
+            int f = faceinds[(size_t)e * nfpe + k], s = facepos[(size_t)e * nfpe + k];
+            if (f < 1 || f > nfaces || s < 1 || s > 2)
+                return fail(c, FLOU_ERR_ARG, "element %d face %d: face %d / side %d out of range", e + 1, k + 1, f, s);
+            if (eleminds[2 * (f - 1) + s - 1] != e + 1 || elempos[2 * (f - 1) + s - 1] != k + 1)
+                return fail(c, FLOU_ERR_ARG, "element %d face %d does not point back through eleminds/elempos",
+                            e + 1, k + 1);
+            ef[(size_t)e * nfpe + k] = ((f - 1) << 1) | (s - 1);
+        }
+    int r;
+    if ((r = upload(c, &c->d_elem_face, ef.data(), ef.size(), "mesh upload"))) return r;
+    if ((r = upload(c, &c->d_face_elem, fe.data(), fe.size(), "mesh upload"))) return r;
+    if ((r = upload(c, &c->d_face_bc, fb.data(), fb.size(), "mesh upload"))) return r;
+    // sizes changed: drop size-dependent buffers
+    double** sized[] = {&c->d_Fn, &c->d_U, &c->d_Qh, &c->d_dQh};
+    for (double** b : sized)
+        if (*b) { cudaFree(*b); *b = nullptr; }
+    c->h_face_bc = fb;
+    c->nelem = nelem;
+    c->nfaces = nfaces;
+    c->ndofs = (int64_t)nelem * c->npe;
+    c->nfdofs = (int64_t)nfaces * c->nfd;
+    c->have_mesh = true;
+    c->have_geom = false;
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_bcs(flou_ctx* c, int32_t nbcs, const int32_t* kinds, const double* states) {
+    if (!c) return FLOU_ERR_ARG;
+    if (nbcs < 0 || nbcs > MAXBC) return fail(c, FLOU_ERR_ARG, "at most %d boundary conditions", MAXBC);
+    if (nbcs > 0 && !kinds) return fail(c, FLOU_ERR_ARG, "null kinds");
+    for (int b = 0; b < nbcs; ++b) {
+        int k = kinds[b];
+        if (k != FLOU_BC_OUTFLOW && k != FLOU_BC_INFLOW && k != FLOU_BC_SLIP)
+            return fail(c, FLOU_ERR_ARG, "unknown boundary condition kind %d", k);
+        if (k == FLOU_BC_SLIP && c->cfg.equation != FLOU_EQ_EULER)
+            return fail(c, FLOU_ERR_ARG, "slip walls apply to the Euler equations only");
+        if (k == FLOU_BC_INFLOW && !states) return fail(c, FLOU_ERR_ARG, "inflow condition without a state");
+    }
+    c->nbcs = nbcs;
+    for (int b = 0; b < MAXBC; ++b) {
+        c->bc_kind[b] = b < nbcs ? kinds[b] : 0;
+        for (int k = 0; k < 5; ++k) c->bc_state[b][k] = (b < nbcs && states) ? states[b * 5 + k] : 0.0;
+    }
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const double* frames, const double* face_J) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh must come before flou_set_geometry");
+    if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators must come before flou_set_geometry");
+    if (!J || !Ja || !frames || !face_J) return fail(c, FLOU_ERR_ARG, "null geometry pointer");
+    int dim = c->cfg.dim, npe = c->npe, nfd = c->nfd;
+    std::vector<double> invJ(c->nelem), Jd((size_t)c->nelem * dim), fJ(c->nfaces), dx(c->nelem);
+    std::vector<int32_t> fe((size_t)c->nfaces * 2);
+    CK(cudaMemcpy(fe.data(), c->d_face_elem, fe.size() * sizeof(int32_t), cudaMemcpyDeviceToHost), "mesh readback");
+    for (int e = 0; e < c->nelem; ++e) {
+        const double* Je = J + (size_t)e * npe;
+        const double* Me = Ja + (size_t)e * npe * dim * dim;
+        for (int i = 0; i < npe; ++i) {
+            if (Je[i] != Je[0])
+                return fail(c, FLOU_ERR_UNSUPPORTED, "element %d: the Jacobian varies within the element "
+                            "(curvilinear geometry is not supported)", e + 1);
+            for (int q = 0; q < dim * dim; ++q) {
+                double v = Me[(size_t)i * dim * dim + q];
+                bool diag = (q % (dim + 1)) == 0;
+                if ((!diag && v != 0.0) || v != Me[q])
+                    return fail(c, FLOU_ERR_UNSUPPORTED, "element %d: the metric is not diagonal and constant "
+                                "(curvilinear geometry is not supported)", e + 1);
+            }
+        }
+        if (!(Je[0] > 0.0) || !std::isfinite(Je[0])) return fail(c, FLOU_ERR_ARG, "element %d: J <= 0", e + 1);
+        invJ[e] = 1.0 / Je[0];
+        for (int d = 0; d < dim; ++d) Jd[(size_t)e * dim + d] = Me[d * (dim + 1)];
+        // get_max_dt length scale: (Σ J ω / n^d)^(1/d), MultielementDiscontinuous.jl:169-171
+        double vol = 0.0;
+        for (int i = 0; i < npe; ++i) {
+            double w = 1.0;
+            int r = i;
+            for (int d = 0; d < dim; ++d) { w *= c->omega[r % c->n]; r /= c->n; }
+            vol += Je[i] * w;
+        }
+        double h = vol / npe;
+        dx[e] = dim == 1 ? h : (dim == 2 ? std::sqrt(h) : std::cbrt(h));
+    }
+    for (int f = 0; f < c->nfaces; ++f) {
+        FrameTab T = frame_of(dim, fe[2 * f] & 7);
+        for (int m = 0; m < nfd; ++m) {
+            size_t idx = (size_t)f * nfd + m;
+            if (face_J[idx] != face_J[(size_t)f * nfd])
+                return fail(c, FLOU_ERR_UNSUPPORTED, "face %d: the surface Jacobian varies along the face", f + 1);
+            const double* fr = frames + idx * 9;
+            for (int q = 0; q < 3; ++q) {
+                bool ok = (q >= dim || (fr[q] == T.n[q] && fr[3 + q] == T.t[q] && (dim < 3 || fr[6 + q] == T.b[q])));
+                if (!ok)
+                    return fail(c, FLOU_ERR_UNSUPPORTED, "face %d: the frame is not the Cartesian frame of its master "
+                                "side (curvilinear geometry is not supported)", f + 1);
+            }
+        }
+        fJ[f] = face_J[(size_t)f * nfd];
+    }
+    int r;
+    if ((r = upload(c, &c->d_invJ, invJ.data(), invJ.size(), "geometry upload"))) return r;
+    if ((r = upload(c, &c->d_Ja, Jd.data(), Jd.size(), "geometry upload"))) return r;
+    if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;
+    if ((r = upload(c, &c->d_dx, dx.data(), dx.size(), "geometry upload"))) return r;
+    c->have_geom = true;
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_sizes(const flou_ctx* c, int64_t* ndofs, int32_t* nvars, int32_t* nelem, int32_t* nfaces) {
+    if (!c) return FLOU_ERR_ARG;
+    if (ndofs) *ndofs = c->ndofs;
+    if (nvars) *nvars = c->nv;
+    if (nelem) *nelem = c->nelem;
+    if (nfaces) *nfaces = c->nfaces;
+    return FLOU_OK;
+}
+
+int32_t flou_rhs(flou_ctx* c, double* dQ, const double* Q, double t, int32_t ptr_kind) {
+    (void)t;   // no time-dependent boundary condition on this path
+    int r = ready(c);
+    if (r) return r;
+    if (!dQ || !Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
+    size_t bytes = (size_t)c->ndofs * c->nv * sizeof(double);
+    if (ptr_kind == FLOU_PTR_HOST) {
+        if ((r = ensure(c, &c->d_Qh, (size_t)c->ndofs * c->nv, "staging buffer"))) return r;
+        if ((r = ensure(c, &c->d_dQh, (size_t)c->ndofs * c->nv, "staging buffer"))) return r;
+        CK(cudaMemcpyAsync(c->d_Qh, Q, bytes, cudaMemcpyHostToDevice, c->stream), "state upload");
+        if ((r = stage(c, c->stream, c->d_Qh, c->d_Qh, c->d_dQh, 0, 0.0, 0.0, 0.0))) return r;
+        CK(cudaMemcpyAsync(dQ, c->d_dQh, bytes, cudaMemcpyDeviceToHost, c->stream), "residual download");
+    } else if (ptr_kind == FLOU_PTR_DEVICE) {
+        if ((r = stage(c, c->stream, Q, Q, dQ, 0, 0.0, 0.0, 0.0))) return r;
+    } else {
+        return fail(c, FLOU_ERR_ARG, "unknown pointer kind %d", ptr_kind);
+    }
+    return check_status(c);
+}
+
+int32_t flou_step(flou_ctx* c, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind) {
+    (void)t0;
+    int r = ready(c);
+    if (r) return r;
+    if (!Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
+    if (nsteps < 0 || !std::isfinite(dt)) return fail(c, FLOU_ERR_ARG, "invalid nsteps/dt");
+    if (nsteps == 0) return FLOU_OK;
+    if ((r = ensure(c, &c->d_U, (size_t)c->ndofs * c->nv, "stage buffer"))) return r;
+    size_t bytes = (size_t)c->ndofs * c->nv * sizeof(double);
+    double* Qd = Q;
+    if (ptr_kind == FLOU_PTR_HOST) {
+        if ((r = ensure(c, &c->d_Qh, (size_t)c->ndofs * c->nv, "staging buffer"))) return r;
+        CK(cudaMemcpyAsync(c->d_Qh, Q, bytes, cudaMemcpyHostToDevice, c->stream), "state upload");
+        Qd = c->d_Qh;
+    } else if (ptr_kind != FLOU_PTR_DEVICE) {
+        return fail(c, FLOU_ERR_ARG, "unknown pointer kind %d", ptr_kind);
+    }
+    if (!c->gexec || c->g_Q != Qd || c->g_dt != dt) {
+        drop_graph(c);
+        ElemLaunch L = elem_launch(c);
+        L.prepare = true;
+        cudaError_t pe = launch_elem(L, elem_params(c, Qd, Qd, c->d_U, 1, dt, 0.0, 1.0), c->own_stream);
+        if (pe != cudaSuccess) return cuda_fail(c, pe, "element kernel set-up");
+        CK(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        int rr = rk3_step(c, c->own_stream, Qd, dt);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(c->own_stream, &g);
+        if (rr) { if (g) cudaGraphDestroy(g); return rr; }
+        if (ce != cudaSuccess) return cuda_fail(c, ce, "graph capture");
+        c->graph = g;
+        CK(cudaGraphInstantiate(&c->gexec, g, 0), "graph instantiate");
+        c->g_Q = Qd;
+        c->g_dt = dt;
+    }
+    for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+    if (ptr_kind == FLOU_PTR_HOST)
+        CK(cudaMemcpyAsync(Q, c->d_Qh, bytes, cudaMemcpyDeviceToHost, c->stream), "state download");
+    return check_status(c);
+}
+
+int32_t flou_max_dt(flou_ctx* c, const double* Q, double cfl, double* dt, int32_t ptr_kind) {
+    int r = ready(c);
+    if (r) return r;
+    if (!Q || !dt) return fail(c, FLOU_ERR_ARG, "null pointer");
+    const double* Qd = Q;
+    size_t bytes = (size_t)c->ndofs * c->nv * sizeof(double);
+    if (ptr_kind == FLOU_PTR_HOST) {
+        if ((r = ensure(c, &c->d_Qh, (size_t)c->ndofs * c->nv, "staging buffer"))) return r;
+        CK(cudaMemcpyAsync(c->d_Qh, Q, bytes, cudaMemcpyHostToDevice, c->stream), "state upload");
+        Qd = c->d_Qh;
+    }
+    if (!c->d_dtmin) CK(cudaMalloc((void**)&c->d_dtmin, sizeof(unsigned long long)), "dt buffer");
+    double inf = INFINITY;
+    unsigned long long init;
+    memcpy(&init, &inf, sizeof(init));
+    CK(cudaMemcpyAsync(c->d_dtmin, &init, sizeof(init), cudaMemcpyHostToDevice, c->stream), "dt init");
+    int grid = (int)((c->ndofs + 255) / 256);
+    const double* a = c->cfg.advection;
+    max_dt_kernel<<<grid, 256, 0, c->stream>>>(Qd, c->d_dx, c->ndofs, c->npe, c->cfg.dim, c->cfg.equation,
+                                               c->cfg.gamma, a[0], a[1], a[2], cfl, c->d_dtmin);
+    CK(cudaGetLastError(), "dt kernel");
+    unsigned long long res;
+    CK(cudaMemcpyAsync(&res, c->d_dtmin, sizeof(res), cudaMemcpyDeviceToHost, c->stream), "dt read");
+    CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    memcpy(dt, &res, sizeof(double));
+    return FLOU_OK;
+}
+
+int32_t flou_take_status(flou_ctx* c, int32_t* flags, int32_t* elem) {
+    if (!c) return FLOU_ERR_ARG;
+    int32_t st[2];
+    CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    CK(cudaMemcpy(st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost), "status read");
+    int32_t init[2] = {0, 0x7fffffff};
+    CK(cudaMemcpy(c->d_status, init, sizeof(init), cudaMemcpyHostToDevice), "status reset");
+    if (flags) *flags = st[0];
+    if (elem) *elem = st[0] ? st[1] : 0;
+    return FLOU_OK;
+}
+
+int32_t flou_fp64_peak(double* gflops) {
+    if (!gflops) return FLOU_ERR_ARG;
+    flou_ctx* c = nullptr;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    double* sink = nullptr;
+    CK(cudaMalloc((void**)&sink, 1024 * sizeof(double)), "probe buffer");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int iters = 1 << 14, threads = 256, blocks = sms * 8;
+    fma_probe_kernel<<<blocks, threads>>>(sink, 64, 1.0);   // warm-up
+    cudaEventRecord(a);
+    fma_probe_kernel<<<blocks, threads>>>(sink, iters, 1.0);
+    cudaEventRecord(b);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return FLOU_ERR_CUDA;
+    double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+    *gflops = flops / (ms * 1e-3) / 1e9;
+    return FLOU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,17 @@
+"""flou_cuda: Flou.jl's DGSEM residual and SSP-RK3 stepping on GB300 (sm_103a, FP64).
+
+The Python side mirrors Flou's set-up API (CartesianMesh, apply_periodicBCs!, LagrangeBasis,
+DGSEMrec, StdSegment/StdQuad/StdHex, equations, fluxes, operators, MultielementDisc,
+EquationConfig, rhs!, timeintegrate, get_max_dt); all arithmetic runs in libflou_cuda.
+"""
+from ._lib import DomainError, FlouError, load
+from .disc import Context, DofHandler, EquationConfig, MultielementDisc, get_max_dt, rhs_
+from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, EulerEquation, EulerInflowBC,
+                        EulerOutflowBC, EulerSlipBC, HLL, HLLC, KennedyGruberAverage, LinearAdvection, LxF,
+                        OutflowBC, SplitDivOperator, StdAverage, StrongDivOperator)
+from .mesh import CartesianMesh, apply_periodicBCs
+from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
+from .timeint import SSPRK33, timeintegrate
+from . import initial
+
+rhs = rhs_

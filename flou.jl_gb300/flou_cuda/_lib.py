@@ -1,0 +1,122 @@
+"""ctypes binding of libflou_cuda (include/flou_cuda.h).
+
+The shared library is built in-tree (flou.jl_gb300/lib/libflou_cuda.so).  There is no CPU
+fallback: if the library is missing, every call raises FlouError.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libflou_cuda.so")
+
+FLOU_OK = 0
+FLOU_ERR_ARG = 1
+FLOU_ERR_CUDA = 2
+FLOU_ERR_NONPHYSICAL = 3
+FLOU_ERR_TIMEOUT = 4
+FLOU_ERR_OOM = 5
+FLOU_ERR_UNSUPPORTED = 6
+FLOU_ERR_STATE = 7
+
+EQ_LINEAR_ADVECTION, EQ_BURGERS, EQ_EULER = 0, 1, 2
+OP_STRONG, OP_SPLIT = 0, 1
+TP_STD_AVERAGE, TP_CHANDRASHEKAR, TP_KENNEDY_GRUBER = 0, 1, 2
+NF_STD_AVERAGE, NF_LXF, NF_CHANDRASHEKAR, NF_HLL, NF_HLLC = 0, 1, 2, 3, 4
+BC_OUTFLOW, BC_INFLOW, BC_SLIP = 1, 2, 3
+PTR_HOST, PTR_DEVICE = 0, 1
+
+STATUS_NAMES = {
+    FLOU_ERR_ARG: "FLOU_ERR_ARG",
+    FLOU_ERR_CUDA: "FLOU_ERR_CUDA",
+    FLOU_ERR_NONPHYSICAL: "FLOU_ERR_NONPHYSICAL",
+    FLOU_ERR_TIMEOUT: "FLOU_ERR_TIMEOUT",
+    FLOU_ERR_OOM: "FLOU_ERR_OOM",
+    FLOU_ERR_UNSUPPORTED: "FLOU_ERR_UNSUPPORTED",
+    FLOU_ERR_STATE: "FLOU_ERR_STATE",
+}
+
+
+class FlouError(RuntimeError):
+    """A libflou_cuda call returned a non-zero status."""
+
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class DomainError(FlouError):
+    """Non-physical state (rho <= 0, p <= 0, NaN), Flou's DomainError."""
+
+
+class FlouConfig(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("equation", ctypes.c_int32),
+        ("gamma", ctypes.c_double),
+        ("advection", ctypes.c_double * 3),
+        ("volume_op", ctypes.c_int32),
+        ("twopoint_flux", ctypes.c_int32),
+        ("numflux", ctypes.c_int32),
+        ("numflux_avg", ctypes.c_int32),
+        ("numflux_intensity", ctypes.c_double),
+        ("nnodes", ctypes.c_int32),
+    ]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_U8 = ctypes.POINTER(ctypes.c_uint8)
+_I64 = ctypes.POINTER(ctypes.c_int64)
+
+# Every symbol the header declares, with its argument types.
+PROTOTYPES = {
+    "flou_create": [ctypes.POINTER(FlouConfig), ctypes.POINTER(_P)],
+    "flou_destroy": [_P],
+    "flou_last_error": [_P],
+    "flou_set_stream": [_P, _P],
+    "flou_set_operators": [_P, _D, _D, _D, _D, _D, _D, _D, _D],
+    "flou_set_mesh": [_P, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32, _I32, _U8, _I32],
+    "flou_set_bcs": [_P, ctypes.c_int32, _I32, _D],
+    "flou_set_geometry": [_P, _D, _D, _D, _D],
+    "flou_rhs": [_P, _P, _P, ctypes.c_double, ctypes.c_int32],
+    "flou_step": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32],
+    "flou_max_dt": [_P, _P, ctypes.c_double, _D, ctypes.c_int32],
+    "flou_sizes": [_P, _I64, _I32, _I32, _I32],
+    "flou_take_status": [_P, _I32, _I32],
+    "flou_fp64_peak": [_D],
+}
+
+_lib = None
+
+
+def load():
+    """Load libflou_cuda.so (raises FlouError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FlouError(FLOU_ERR_STATE, "libflou_cuda.so not built (%s); run build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, args in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_char_p if name == "flou_last_error" else ctypes.c_int32
+    _lib = lib
+    return lib
+
+
+def check(status, ctx=None):
+    if status == FLOU_OK:
+        return
+    msg = ""
+    if ctx is not None:
+        raw = load().flou_last_error(ctx)
+        msg = raw.decode() if raw else ""
+    cls = DomainError if status == FLOU_ERR_NONPHYSICAL else FlouError
+    raise cls(status, msg)
+
+
+def dptr(a):
+    """ctypes double* of a C- or Fortran-contiguous float64 numpy array."""
+    return a.ctypes.data_as(_D)

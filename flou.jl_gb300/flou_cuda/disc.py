@@ -1,0 +1,259 @@
+"""MultielementDisc / EquationConfig / rhs! / get_max_dt on top of libflou_cuda.
+
+Reference: src/FlouSpatial/MultielementDiscontinuous.jl:29-92 (MultielementDisc),
+src/FlouCommon/FlouCommon.jl:92-102 (EquationConfig, rhs!),
+src/FlouSpatial/Equations/Hyperbolic.jl:31-69 (the residual), MultielementDiscontinuous.jl:162-178
+(get_max_dt), src/FlouSpatial/PhysicalRegions.jl:370-408,541-696 (Cartesian geometry).
+
+States are Flou's (ndofs, nvars) column-major matrices: a numpy array in Fortran order
+(host memory) or a CUDA tensor laid out as (nvars, ndofs) row-major, which is the same
+memory.  Every residual runs on the GPU; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, HLL, HLLC, LinearAdvection, LxF,
+                        SplitDivOperator, StdAverage, StrongDivOperator)
+
+
+class DofHandler:
+    def __init__(self, nelem, nfaces, npe, nfd):
+        self.nelements = nelem
+        self.nfaces = nfaces
+        self.elem_dofs = npe
+        self.face_dofs = nfd
+
+    @property
+    def ndofs(self):
+        return self.nelements * self.elem_dofs
+
+
+def cartesian_geometry(mesh, std):
+    """Per-node J and metric, per-face-node frame and surface Jacobian of a CartesianMesh
+    (PhysicalRegions.jl:370-408 and :541-696), plus node coordinates."""
+    d, n = mesh.dim, std.n
+    dx = mesh.dx
+    npe, nfd = n ** d, n ** (d - 1)
+    nd = mesh.nelements * npe
+    nfd_tot = mesh.nfaces * nfd
+    if d == 1:
+        jac, M = dx[0] / 2, np.array([[1.0]])
+    elif d == 2:
+        jac = (dx[0] * dx[1]) / 4
+        M = np.array([[dx[1] / 2, 0.0], [0.0, dx[0] / 2]])
+    else:
+        jac = (dx[0] * dx[1] * dx[2]) / 8
+        M = np.diag([dx[1] * dx[2] / 4, dx[0] * dx[2] / 4, dx[0] * dx[1] / 4])
+    J = np.full(nd, jac)
+    Ja = np.broadcast_to(M.ravel(order="F"), (nd, d * d)).copy()
+    # frames and surface Jacobians from the master side's local face position
+    tab = {
+        1: {1: ((-1, 0, 0), (0, 0, 0), (0, 0, 0)), 2: ((1, 0, 0), (0, 0, 0), (0, 0, 0))},
+        2: {1: ((-1, 0, 0), (0, -1, 0), (0, 0, 0)), 2: ((1, 0, 0), (0, 1, 0), (0, 0, 0)),
+            3: ((0, -1, 0), (1, 0, 0), (0, 0, 0)), 4: ((0, 1, 0), (-1, 0, 0), (0, 0, 0))},
+        3: {1: ((-1, 0, 0), (0, -1, 0), (0, 0, 1)), 2: ((1, 0, 0), (0, 1, 0), (0, 0, 1)),
+            3: ((0, -1, 0), (0, 0, -1), (1, 0, 0)), 4: ((0, 1, 0), (0, 0, 1), (1, 0, 0)),
+            5: ((0, 0, -1), (-1, 0, 0), (0, 1, 0)), 6: ((0, 0, 1), (1, 0, 0), (0, 1, 0))},
+    }[d]
+    if d == 1:
+        fj = {1: 1.0, 2: 1.0}
+    elif d == 2:
+        fj = {1: dx[1] / 2, 2: dx[1] / 2, 3: dx[0] / 2, 4: dx[0] / 2}
+    else:
+        fj = {1: dx[1] * dx[2] / 4, 2: dx[1] * dx[2] / 4, 3: dx[0] * dx[2] / 4, 4: dx[0] * dx[2] / 4,
+              5: dx[0] * dx[1] / 4, 6: dx[0] * dx[1] / 4}
+    pos = mesh.elempos[:, 0]
+    frames_f = np.array([np.array(tab[p], dtype=np.float64).ravel() for p in range(1, 2 * d + 1)])[pos - 1]
+    frames = np.repeat(frames_f, nfd, axis=0)
+    faceJ = np.repeat(np.array([fj[p] for p in range(1, 2 * d + 1)])[pos - 1], nfd)
+    # node coordinates (x fastest within an element)
+    org = mesh.element_origin()
+    r = (std.xi1d + 1.0) / 2.0
+    idx = np.array(np.unravel_index(np.arange(npe), (n,) * d, order="F"))   # (d, npe)
+    coords = np.zeros((nd, 3))
+    for k in range(d):
+        local = r[idx[k]] * dx[k]
+        coords[:, k] = (org[:, k][:, None] + local[None, :]).ravel()
+    return J, Ja, frames, faceJ, coords
+
+
+class MultielementDisc:
+    """MultielementDisc(mesh, std, equation, operator, bcs) on the GPU.
+
+    `bcs` maps boundary names ("1".."2d") to EulerInflowBC / EulerOutflowBC / EulerSlipBC.
+    """
+
+    def __init__(self, mesh, std, equation, operator, bcs=None):
+        bcs = dict(bcs or {})
+        if mesh.dim != std.dim or mesh.dim != equation.dim:
+            raise ValueError("mesh, standard region and equation dimensions differ")
+        if len(bcs) != mesh.nboundaries:
+            raise ValueError("The number of BCs does not match the number of boundaries.")
+        self.mesh, self.std, self.equation, self.operator = mesh, std, equation, operator
+        self.bcs = [None] * mesh.nboundaries
+        for key, value in bcs.items():
+            self.bcs[mesh.bdmap[int(key)] - 1] = value
+        n, d = std.n, mesh.dim
+        self.dofhandler = DofHandler(mesh.nelements, mesh.nfaces, n ** d, n ** (d - 1))
+        self.J, self.Ja, self.frames, self.faceJ, self.coords = cartesian_geometry(mesh, std)
+        self.config = self._config()
+        self._ctx = None
+
+    # -- C ABI configuration ------------------------------------------------------------
+    def _config(self):
+        eq, op = self.equation, self.operator
+        cfg = L.FlouConfig()
+        cfg.dim = self.mesh.dim
+        cfg.equation = eq.kind
+        cfg.gamma = getattr(eq, "gamma", 1.4)
+        adv = getattr(eq, "a", np.zeros(0))
+        for k in range(3):
+            cfg.advection[k] = float(adv[k]) if k < len(adv) else 0.0
+        cfg.volume_op = op.code
+        cfg.twopoint_flux = op.tpflux.tpcode if op.code == L.OP_SPLIT else L.TP_STD_AVERAGE
+        nf = op.numflux
+        if nf.code is None:
+            raise ValueError("%s is not a numerical flux" % type(nf).__name__)
+        cfg.numflux = nf.code
+        avg = getattr(nf, "avg", StdAverage())
+        cfg.numflux_avg = L.NF_CHANDRASHEKAR if isinstance(avg, ChandrasekharAverage) else L.NF_STD_AVERAGE
+        cfg.numflux_intensity = getattr(nf, "intensity", 1.0)
+        cfg.nnodes = self.std.n
+        return cfg
+
+    def abi_arrays(self):
+        """The set-up arrays exactly as the C ABI receives them."""
+        m, s = self.mesh, self.std
+        kinds = np.array([b.kind for b in self.bcs], dtype=np.int32)
+        states = np.zeros((max(len(self.bcs), 1), 5))
+        for i, b in enumerate(self.bcs):
+            if b.state is not None:
+                states[i, :len(b.state)] = b.state
+        return dict(
+            D=np.asfortranarray(s.D), Ds=np.asfortranarray(s.Ds), Dsharp=np.asfortranarray(s.Dsharp),
+            omega=s.omega1d.copy(), l_l=s.l[0].copy(), l_r=s.l[1].copy(), dg_l=s.dg[0].copy(), dg_r=s.dg[1].copy(),
+            faceinds=np.ascontiguousarray(m.faceinds, dtype=np.int32),
+            facepos=np.ascontiguousarray(m.facepos, dtype=np.int32),
+            eleminds=np.ascontiguousarray(m.eleminds, dtype=np.int32),
+            elempos=np.ascontiguousarray(m.elempos, dtype=np.int32),
+            orientation=np.ascontiguousarray(m.orientation, dtype=np.uint8),
+            bdface_index=np.ascontiguousarray(m.bdface_index, dtype=np.int32),
+            bc_kinds=kinds, bc_states=np.ascontiguousarray(states),
+            J=self.J, Ja=np.ascontiguousarray(self.Ja), frames=np.ascontiguousarray(self.frames), faceJ=self.faceJ,
+        )
+
+    @property
+    def ctx(self):
+        if self._ctx is None:
+            self._ctx = Context(self.config, self.abi_arrays(), self.mesh.nelements, self.mesh.nfaces)
+        return self._ctx
+
+    @property
+    def ndofs(self):
+        return self.dofhandler.ndofs
+
+    @property
+    def nvariables(self):
+        return self.equation.nvariables
+
+    def new_state(self):
+        return np.zeros((self.ndofs, self.nvariables), order="F")
+
+
+class Context:
+    """Owns one flou_ctx (create + uploads); destroyed with the object."""
+
+    def __init__(self, cfg, a, nelem, nfaces):
+        lib = L.load()
+        self._lib = lib
+        h = ctypes.c_void_p()
+        st = lib.flou_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != L.FLOU_OK:
+            raise L.FlouError(st, "flou_create rejected the configuration")
+        self.h = h
+        self.cfg = cfg
+        d = L.dptr
+        i32 = lambda x: x.ctypes.data_as(L._I32)
+        L.check(lib.flou_set_operators(h, d(a["D"]), d(a["Ds"]), d(a["Dsharp"]), d(a["omega"]), d(a["l_l"]),
+                                       d(a["l_r"]), d(a["dg_l"]), d(a["dg_r"])), h)
+        L.check(lib.flou_set_mesh(h, nelem, nfaces, i32(a["faceinds"]), i32(a["facepos"]), i32(a["eleminds"]),
+                                  i32(a["elempos"]), a["orientation"].ctypes.data_as(L._U8),
+                                  i32(a["bdface_index"])), h)
+        L.check(lib.flou_set_bcs(h, len(a["bc_kinds"]), i32(a["bc_kinds"]), d(a["bc_states"])), h)
+        L.check(lib.flou_set_geometry(h, d(a["J"]), d(a["Ja"]), d(a["frames"]), d(a["faceJ"])), h)
+        nd = ctypes.c_int64()
+        nv = ctypes.c_int32()
+        L.check(lib.flou_sizes(h, ctypes.byref(nd), ctypes.byref(nv), None, None), h)
+        self.ndofs, self.nvars = nd.value, nv.value
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            self._lib.flou_destroy(h)
+            self.h = None
+
+    def _ptr(self, a, writable=False):
+        """(pointer, kind) of a state array: numpy (host) or CUDA tensor (device)."""
+        if isinstance(a, np.ndarray):
+            if a.dtype != np.float64 or a.size != self.ndofs * self.nvars:
+                raise ValueError("state must be float64 with %d x %d entries" % (self.ndofs, self.nvars))
+            if a.ndim == 2 and a.shape == (self.ndofs, self.nvars):
+                if not a.flags.f_contiguous:
+                    raise ValueError("host state must be a column-major (ndofs, nvars) matrix")
+            elif not a.flags.c_contiguous:
+                raise ValueError("host state must be contiguous")
+            if writable and not a.flags.writeable:
+                raise ValueError("state is read-only")
+            return ctypes.c_void_p(a.ctypes.data), L.PTR_HOST
+        # torch tensor on the GPU
+        if not getattr(a, "is_cuda", False):
+            raise TypeError("state must be a numpy array or a CUDA tensor")
+        if a.numel() != self.ndofs * self.nvars or not a.is_contiguous() or str(a.dtype) != "torch.float64":
+            raise ValueError("device state must be a contiguous float64 tensor (nvars, ndofs)")
+        return ctypes.c_void_p(a.data_ptr()), L.PTR_DEVICE
+
+    def set_stream(self, stream_ptr):
+        L.check(self._lib.flou_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
+
+    def rhs(self, dQ, Q, t=0.0):
+        pd, kd = self._ptr(dQ, True)
+        pq, kq = self._ptr(Q)
+        if kd != kq:
+            raise ValueError("dQ and Q must both live on the host or both on the device")
+        L.check(self._lib.flou_rhs(self.h, pd, pq, float(t), kd), self.h)
+
+    def step(self, Q, dt, nsteps, t0=0.0):
+        pq, kq = self._ptr(Q, True)
+        L.check(self._lib.flou_step(self.h, pq, float(dt), float(t0), int(nsteps), kq), self.h)
+
+    def max_dt(self, Q, cfl):
+        pq, kq = self._ptr(Q)
+        out = ctypes.c_double()
+        L.check(self._lib.flou_max_dt(self.h, pq, float(cfl), ctypes.byref(out), kq), self.h)
+        return out.value
+
+    def take_status(self):
+        f, e = ctypes.c_int32(), ctypes.c_int32()
+        L.check(self._lib.flou_take_status(self.h, ctypes.byref(f), ctypes.byref(e)), self.h)
+        return f.value, e.value
+
+
+class EquationConfig:
+    """EquationConfig(disc, equation)."""
+
+    def __init__(self, disc, equation):
+        self.disc = disc
+        self.equation = equation
+
+
+def rhs_(dQ, Q, p, time=0.0):
+    """rhs!(dQ, Q, p::EquationConfig, t): overwrites dQ with the semidiscrete residual."""
+    p.disc.ctx.rhs(dQ, Q, time)
+    return None
+
+
+def get_max_dt(q, disc, equation, cfl):
+    """get_max_dt(q, disc, eq, cfl) (MultielementDiscontinuous.jl:162-178)."""
+    return disc.ctx.max_dt(q, cfl)

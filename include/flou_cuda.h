@@ -1,0 +1,165 @@
+/*
+ * flou_cuda.h -- C ABI of libflou_cuda, the GB300 (sm_103a) FP64 implementation of Flou.jl's
+ * DGSEM semidiscrete residual and explicit SSP-RK3 stepping.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns an int32
+ * status (FLOU_OK = 0).  flou_last_error(ctx) gives a message for the last failure on ctx.
+ *
+ * Conventions (those of Flou's own containers, so a Julia caller passes its arrays as is):
+ *   - The state is a column-major (ndofs_total x nvars) Float64 matrix: each variable is one
+ *     contiguous column; element e (1-based) owns rows (e-1)*n^d+1 .. e*n^d; element nodes are
+ *     ordered i fastest (src/FlouSpatial/GlobalContainers.jl:19-50, DofHandler.jl:62-68,
+ *     StdRegions/StdRegions.jl:60-62).
+ *   - Square operator matrices are n x n column-major (Julia Matrix{Float64}).
+ *   - Mesh connectivity uses the reference's 1-based indices (src/FlouCommon/Mesh.jl:26-133).
+ *   - Pointers to state arrays may be host or device memory, chosen by `ptr_kind`.
+ *
+ * Threading: a context is used by one host thread at a time; distinct contexts may be used
+ * concurrently.  Each context launches on one CUDA stream (its own, or the caller's after
+ * flou_set_stream).
+ */
+#ifndef FLOU_CUDA_H
+#define FLOU_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------- */
+#define FLOU_OK 0
+#define FLOU_ERR_ARG 1          /* invalid argument or inconsistent sizes                  */
+#define FLOU_ERR_CUDA 2         /* a CUDA runtime call failed                                */
+#define FLOU_ERR_NONPHYSICAL 3  /* rho <= 0, p <= 0 or a non-finite value was produced       */
+#define FLOU_ERR_TIMEOUT 4      /* a bounded device-side wait ran out                        */
+#define FLOU_ERR_OOM 5          /* device allocation failed                                   */
+#define FLOU_ERR_UNSUPPORTED 6  /* valid in Flou but outside this library (e.g. curvilinear) */
+#define FLOU_ERR_STATE 7        /* call order violated (e.g. rhs before set_mesh)            */
+
+/* ---- enumerations --------------------------------------------------------------------- */
+/* Equations: LinearAdvection (src/FlouCommon/LinearAdvection.jl:16-26), BurgersEquation
+ * (src/FlouCommon/Burgers.jl:16), EulerEquation{ND}(γ) (src/FlouCommon/Euler.jl:16-24). */
+#define FLOU_EQ_LINEAR_ADVECTION 0
+#define FLOU_EQ_BURGERS 1
+#define FLOU_EQ_EULER 2
+
+/* Volume operators: StrongDivOperator (OpDivergence.jl:105-160; weak == strong on LGL),
+ * SplitDivOperator (OpDivergence.jl:184-282, LGL nodes only). */
+#define FLOU_OP_STRONG 0
+#define FLOU_OP_SPLIT 1
+
+/* Two-point volume fluxes of the split form: StdAverage (Euler.jl:385-472),
+ * ChandrasekharAverage (Euler.jl:474-536), Kennedy-Gruber (no Flou counterpart). */
+#define FLOU_TP_STD_AVERAGE 0
+#define FLOU_TP_CHANDRASHEKAR 1
+#define FLOU_TP_KENNEDY_GRUBER 2
+
+/* Interface (numerical) fluxes: StdAverage (Euler.jl:99-136), LxF(avg, intensity) =
+ * Rusanov (Euler.jl:138-165), ChandrasekharAverage (Euler.jl:167-226), HLL and HLLC (no Flou
+ * counterpart; Toro's formulation with Davis wave speeds). */
+#define FLOU_NF_STD_AVERAGE 0
+#define FLOU_NF_LXF 1
+#define FLOU_NF_CHANDRASHEKAR 2
+#define FLOU_NF_HLL 3
+#define FLOU_NF_HLLC 4
+
+/* Boundary conditions applied on boundary faces (periodic faces are interior faces after
+ * apply_periodicBCs!): EulerOutflowBC, EulerInflowBC(Qext), EulerSlipBC
+ * (src/FlouSpatial/Equations/Euler.jl:69-94).  Inflow/outflow also serve the scalar
+ * equations (a constant Dirichlet state / zero-gradient copy). */
+#define FLOU_BC_OUTFLOW 1
+#define FLOU_BC_INFLOW 2
+#define FLOU_BC_SLIP 3
+
+/* Pointer kinds for state arrays. */
+#define FLOU_PTR_HOST 0
+#define FLOU_PTR_DEVICE 1
+
+typedef struct flou_ctx flou_ctx;
+
+/* Replaces the set-up of EquationConfig(MultielementDisc(mesh, std, equation, operator,
+ * bcs), equation) (src/FlouCommon/FlouCommon.jl:92-95,
+ * src/FlouSpatial/MultielementDiscontinuous.jl:29-92). */
+typedef struct flou_config {
+    int32_t dim;               /* 1, 2 or 3                                                 */
+    int32_t equation;          /* FLOU_EQ_*                                                 */
+    double gamma;              /* EulerEquation γ                                           */
+    double advection[3];       /* LinearAdvection velocity (unused entries 0)               */
+    int32_t volume_op;         /* FLOU_OP_*                                                 */
+    int32_t twopoint_flux;     /* FLOU_TP_* (split form only)                               */
+    int32_t numflux;           /* FLOU_NF_*                                                 */
+    int32_t numflux_avg;       /* averaging flux inside LxF: FLOU_NF_STD_AVERAGE or _CHANDRASHEKAR */
+    double numflux_intensity;  /* LxF intensity (1.0 = Rusanov)                             */
+    int32_t nnodes;            /* nodes per direction n = p + 1, 2 <= n <= 8                */
+} flou_config;
+
+/* ---- context lifecycle ------------------------------------------------------------------ */
+int32_t flou_create(const flou_config* cfg, flou_ctx** out);
+int32_t flou_destroy(flou_ctx* ctx);
+const char* flou_last_error(const flou_ctx* ctx);
+/* Launch on the caller's stream (a cudaStream_t); NULL restores the context's own stream. */
+int32_t flou_set_stream(flou_ctx* ctx, void* stream);
+
+/* ---- set-up uploads (deep copies; the caller keeps ownership) -------------------------- */
+/* Std-region operators of StdSegment (src/FlouSpatial/StdRegions/StdSegment.jl:77-89):
+ * D, Ds = D - B, D♯ = 2D - B (n x n), ω, l_l, l_r, ∂g_l, ∂g_r (n).  StdQuad/StdHex reuse the
+ * segment's matrices (StdQuad.jl:61-67, StdHex.jl:79-85). */
+int32_t flou_set_operators(flou_ctx* ctx, const double* D, const double* Ds, const double* Dsharp,
+                           const double* omega, const double* l_l, const double* l_r, const double* dg_l,
+                           const double* dg_r);
+
+/* Connectivity of the mesh after apply_periodicBCs! (src/FlouCommon/Mesh.jl:236-322):
+ *   faceinds/facepos: nelem x 2d, element-major (mesh.elements[e].faceinds/.facepos);
+ *   eleminds/elempos: nfaces x 2 (mesh.faces[f].eleminds/.elempos), eleminds[.,2] = 0 on
+ *   boundary faces; orientation: nfaces (mesh.faces[f].orientation);
+ *   bdface_index: nfaces, the boundary index (1-based, position in mesh.bdfaces) of each
+ *   boundary face, 0 for interior faces. */
+int32_t flou_set_mesh(flou_ctx* ctx, int32_t nelem, int32_t nfaces, const int32_t* faceinds, const int32_t* facepos,
+                      const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
+                      const int32_t* bdface_index);
+
+/* Boundary conditions per boundary index (MultielementDisc's _bcs tuple,
+ * MultielementDiscontinuous.jl:40-51): kinds[nbcs] (FLOU_BC_*), states[nbcs x 5]
+ * (the Qext of inflow conditions, row per boundary). */
+int32_t flou_set_bcs(flou_ctx* ctx, int32_t nbcs, const int32_t* kinds, const double* states);
+
+/* Geometry (Geometry, src/FlouSpatial/PhysicalRegions.jl:982-991): per node J (ndofs),
+ * metric Ja (ndofs x d x d, column-major per node); per face node the frame
+ * (nfacedofs x 3 x 3: n, t, b with 3 components each) and the surface Jacobian
+ * (nfacedofs).  Only Cartesian geometry is supported: J and a diagonal Ja constant per
+ * element, one frame and one surface Jacobian per face. */
+int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, const double* frames,
+                          const double* face_J);
+
+/* ---- residual and stepping ------------------------------------------------------------- */
+/* FlouCommon.rhs!(dQ, Q, p::EquationConfig{<:MultielementDisc,<:HyperbolicEquation}, t)
+ * (src/FlouSpatial/Equations/Hyperbolic.jl:31-69): dQ is overwritten.  Synchronous. */
+int32_t flou_rhs(flou_ctx* ctx, double* dQ, const double* Q, double t, int32_t ptr_kind);
+
+/* `nsteps` Shu-Osher SSP-RK3 steps of size dt, in place on Q (the SSPRK33 solver that
+ * timeintegrate hands to OrdinaryDiffEq, src/FlouTime/FlouTime.jl:34-54).  Each stage's
+ * combination is fused into the residual kernel; the step is replayed as a CUDA graph.
+ * Returns FLOU_ERR_NONPHYSICAL when any stage produced rho <= 0, p <= 0 or a non-finite
+ * value (Flou raises a DomainError there, FlouTime.jl:37-51). */
+int32_t flou_step(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind);
+
+/* get_max_dt(q, disc, eq, cfl) (src/FlouSpatial/MultielementDiscontinuous.jl:162-178). */
+int32_t flou_max_dt(flou_ctx* ctx, const double* Q, double cfl, double* dt, int32_t ptr_kind);
+
+/* Number of nodes (DOFs in Flou's sense, DofHandler.jl:53) and of variables. */
+int32_t flou_sizes(const flou_ctx* ctx, int64_t* ndofs, int32_t* nvars, int32_t* nelem, int32_t* nfaces);
+
+/* Status word of the last device work on ctx: bit 0 = non-physical state seen; *elem = the
+ * lowest element index (1-based) that raised it, 0 if none.  Clears the word. */
+int32_t flou_take_status(flou_ctx* ctx, int32_t* flags, int32_t* elem);
+
+/* Measured FP64 fused-multiply-add throughput of the current device in GFLOP/s (2 flops per
+ * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
+int32_t flou_fp64_peak(double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOU_CUDA_H */

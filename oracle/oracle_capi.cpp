@@ -1,0 +1,290 @@
+// oracle_capi.cpp -- TEST INFRASTRUCTURE ONLY: C entry points over flou_oracle.hpp so the
+// Python tests can drive the CPU restatement of Flou.jl through ctypes.  Not part of the
+// product; the CUDA library never links or calls it.
+#include <omp.h>
+
+#include <cstdio>
+
+#include "flou_oracle.hpp"
+
+using namespace oracle;
+
+// ---------------------------------------------------------------------------------------
+// Counting scalar: every + - * is one flop, divisions / sqrt / log tallied separately.
+// Used to measure the algorithmic operation count of the reference's residual.
+// ---------------------------------------------------------------------------------------
+struct OpCount { long long add = 0, mul = 0, div = 0, sqrt = 0, log = 0, cmp = 0; };
+static OpCount g_count;
+
+struct CD {
+    double v = 0;
+    CD() = default;
+    CD(double x) : v(x) {}
+};
+static inline CD operator+(CD a, CD b) { g_count.add++; return CD(a.v + b.v); }
+static inline CD operator-(CD a, CD b) { g_count.add++; return CD(a.v - b.v); }
+static inline CD operator*(CD a, CD b) { g_count.mul++; return CD(a.v * b.v); }
+static inline CD operator/(CD a, CD b) { g_count.div++; return CD(a.v / b.v); }
+static inline CD operator-(CD a) { return CD(-a.v); }
+static inline CD operator+(CD a, double b) { return a + CD(b); }
+static inline CD operator-(CD a, double b) { return a - CD(b); }
+static inline CD operator*(CD a, double b) { return a * CD(b); }
+static inline CD operator/(CD a, double b) { return a / CD(b); }
+static inline CD operator+(double a, CD b) { return CD(a) + b; }
+static inline CD operator-(double a, CD b) { return CD(a) - b; }
+static inline CD operator*(double a, CD b) { return CD(a) * b; }
+static inline CD operator/(double a, CD b) { return CD(a) / b; }
+static inline bool operator<(CD a, CD b) { g_count.cmp++; return a.v < b.v; }
+static inline bool operator<(CD a, double b) { g_count.cmp++; return a.v < b; }
+static inline bool operator>=(CD a, double b) { g_count.cmp++; return a.v >= b; }
+static inline bool operator<=(CD a, double b) { g_count.cmp++; return a.v <= b; }
+static inline CD sqrt(CD a) { g_count.sqrt++; return CD(std::sqrt(a.v)); }
+static inline CD log(CD a) { g_count.log++; return CD(std::log(a.v)); }
+static inline CD fabs(CD a) { return CD(std::fabs(a.v)); }
+namespace std {
+static inline CD min(CD a, CD b) { g_count.cmp++; return a.v < b.v ? a : b; }
+static inline CD max(CD a, CD b) { g_count.cmp++; return a.v < b.v ? b : a; }
+}  // namespace std
+
+extern "C" {
+
+void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+int oracle_max_threads() { return omp_get_max_threads(); }
+
+// ------------------------------- mesh ------------------------------------------------
+void* oracle_mesh_new(int dim, const double* start, const double* finish, const int* n, int nperiodic,
+                      const int* pairs) {
+    try {
+        Mesh* m = new Mesh(cartesian_mesh(dim, start, finish, n));
+        std::vector<std::pair<int, int>> p;
+        for (int i = 0; i < nperiodic; ++i) p.push_back({pairs[2 * i], pairs[2 * i + 1]});
+        if (nperiodic) apply_periodic(*m, p);
+        return m;
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "oracle_mesh_new: %s\n", e.what());
+        return nullptr;
+    }
+}
+void oracle_mesh_free(void* h) { delete (Mesh*)h; }
+void oracle_mesh_sizes(void* h, int* nelem, int* nfaces, int* nint, int* nbd_lists) {
+    Mesh* m = (Mesh*)h;
+    *nelem = m->nelem();
+    *nfaces = m->nfaces();
+    *nint = (int)m->intfaces.size();
+    *nbd_lists = (int)m->bdfaces.size();
+}
+// Connectivity in the reference's own 1-based form, plus bdid[f] = boundary index (1-based)
+// for boundary faces, 0 otherwise, and bdindex_of_id[id-1] = bdmap[id] (0 when periodic).
+void oracle_mesh_get(void* h, int* faceinds, int* facepos, int* eleminds, int* elempos, unsigned char* orient,
+                     int* bdid, int* intfaces, int* bdindex_of_id) {
+    Mesh* m = (Mesh*)h;
+    std::copy(m->e_faceinds.begin(), m->e_faceinds.end(), faceinds);
+    std::copy(m->e_facepos.begin(), m->e_facepos.end(), facepos);
+    std::copy(m->f_eleminds.begin(), m->f_eleminds.end(), eleminds);
+    std::copy(m->f_elempos.begin(), m->f_elempos.end(), elempos);
+    std::copy(m->f_orient.begin(), m->f_orient.end(), orient);
+    std::copy(m->intfaces.begin(), m->intfaces.end(), intfaces);
+    for (int f = 0; f < m->nfaces(); ++f) bdid[f] = 0;
+    for (size_t b = 0; b < m->bdfaces.size(); ++b)
+        for (int f : m->bdfaces[b]) bdid[f - 1] = (int)b + 1;
+    for (int id = 1; id <= 2 * m->dim; ++id) bdindex_of_id[id - 1] = m->bdmap.count(id) ? m->bdmap[id] : 0;
+}
+
+// Cartesian geometry (PhysicalRegions.jl:370-408 elements, :541-696 faces, Mesh.jl:364-487
+// coordinates).  Outputs per node: J, Ja (dim x dim column-major), coords (3 per node);
+// per face node: frames (n, t, b; 3 x 3 doubles), faceJ.
+void oracle_geometry(void* h, int n, const double* xi, double* J, double* Ja, double* coords, double* frames,
+                     double* faceJ) {
+    Mesh* m = (Mesh*)h;
+    int dim = m->dim;
+    int npe = 1, nfd = 1;
+    for (int d = 0; d < dim; ++d) npe *= n;
+    for (int d = 0; d < dim - 1; ++d) nfd *= n;
+    const double* dx = m->dx;
+    double jac = dim == 1 ? dx[0] / 2 : (dim == 2 ? (dx[0] * dx[1]) / 4 : (dx[0] * dx[1] * dx[2]) / 8);
+    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (dim == 1) M[0] = 1.0;
+    else if (dim == 2) { M[0] = dx[1] / 2; M[3] = dx[0] / 2; }
+    else { M[0] = dx[1] * dx[2] / 4; M[4] = dx[0] * dx[2] / 4; M[8] = dx[0] * dx[1] / 4; }
+    for (int e = 0; e < m->nelem(); ++e) {
+        const int* nodes = &m->e_nodeinds[e * m->nvert_e];
+        for (int i = 0; i < npe; ++i) {
+            long g = (long)e * npe + i;
+            J[g] = jac;
+            for (int q = 0; q < dim * dim; ++q) Ja[g * dim * dim + q] = M[q];
+            int ix = i % n, iy = (i / n) % n, iz = i / (n * n);
+            double r[3] = {(xi[ix] + 1) / 2, dim > 1 ? (xi[iy] + 1) / 2 : 0.0, dim > 2 ? (xi[iz] + 1) / 2 : 0.0};
+            for (int c = 0; c < 3; ++c) {
+                auto X = [&](int v) { return m->nodes[nodes[v] - 1][c]; };
+                double x;
+                if (dim == 1) x = X(0) * (1 - r[0]) + X(1) * r[0];
+                else if (dim == 2)
+                    x = X(0) * (1 - r[0]) * (1 - r[1]) + X(1) * r[0] * (1 - r[1]) + X(2) * r[0] * r[1] +
+                        X(3) * (1 - r[0]) * r[1];
+                else
+                    x = X(0) * (1 - r[0]) * (1 - r[1]) * (1 - r[2]) + X(1) * r[0] * (1 - r[1]) * (1 - r[2]) +
+                        X(2) * r[0] * r[1] * (1 - r[2]) + X(3) * (1 - r[0]) * r[1] * (1 - r[2]) +
+                        X(4) * (1 - r[0]) * (1 - r[1]) * r[2] + X(5) * r[0] * (1 - r[1]) * r[2] +
+                        X(6) * r[0] * r[1] * r[2] + X(7) * (1 - r[0]) * r[1] * r[2];
+                coords[g * 3 + c] = c < dim ? x : 0.0;
+            }
+        }
+    }
+    for (int f = 0; f < m->nfaces(); ++f) {
+        int pos = m->elempos(f + 1, 1);
+        double fr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // n, t, b
+        double fj = 1.0;
+        auto set = [&](std::array<double, 3> nn, std::array<double, 3> tt, std::array<double, 3> bb) {
+            for (int q = 0; q < 3; ++q) { fr[q] = nn[q]; fr[3 + q] = tt[q]; fr[6 + q] = bb[q]; }
+        };
+        if (dim == 1) {
+            set({pos == 1 ? -1.0 : 1.0, 0, 0}, {0, 0, 0}, {0, 0, 0});
+        } else if (dim == 2) {
+            if (pos == 1) { fj = dx[1] / 2; set({-1, 0, 0}, {0, -1, 0}, {0, 0, 0}); }
+            else if (pos == 2) { fj = dx[1] / 2; set({1, 0, 0}, {0, 1, 0}, {0, 0, 0}); }
+            else if (pos == 3) { fj = dx[0] / 2; set({0, -1, 0}, {1, 0, 0}, {0, 0, 0}); }
+            else { fj = dx[0] / 2; set({0, 1, 0}, {-1, 0, 0}, {0, 0, 0}); }
+        } else {
+            if (pos == 1) { fj = dx[1] * dx[2] / 4; set({-1, 0, 0}, {0, -1, 0}, {0, 0, 1}); }
+            else if (pos == 2) { fj = dx[1] * dx[2] / 4; set({1, 0, 0}, {0, 1, 0}, {0, 0, 1}); }
+            else if (pos == 3) { fj = dx[0] * dx[2] / 4; set({0, -1, 0}, {0, 0, -1}, {1, 0, 0}); }
+            else if (pos == 4) { fj = dx[0] * dx[2] / 4; set({0, 1, 0}, {0, 0, 1}, {1, 0, 0}); }
+            else if (pos == 5) { fj = dx[0] * dx[1] / 4; set({0, 0, -1}, {-1, 0, 0}, {0, 1, 0}); }
+            else { fj = dx[0] * dx[1] / 4; set({0, 0, 1}, {1, 0, 0}, {0, 1, 0}); }
+        }
+        for (int q = 0; q < nfd; ++q) {
+            long idx = (long)f * nfd + q;
+            for (int c = 0; c < 9; ++c) frames[idx * 9 + c] = fr[c];
+            faceJ[idx] = fj;
+        }
+    }
+}
+
+// ------------------------------- operators -------------------------------------------
+void oracle_std_operators(int n, int lobatto, double* xi, double* omega, double* D, double* Ds, double* Dsharp,
+                          double* ll, double* lr, double* dgl, double* dgr) {
+    StdOps s = std_operators(n, lobatto != 0);
+    std::copy(s.xi.begin(), s.xi.end(), xi);
+    std::copy(s.omega.begin(), s.omega.end(), omega);
+    std::copy(s.D.begin(), s.D.end(), D);
+    std::copy(s.Ds.begin(), s.Ds.end(), Ds);
+    std::copy(s.Dsharp.begin(), s.Dsharp.end(), Dsharp);
+    std::copy(s.ll.begin(), s.ll.end(), ll);
+    std::copy(s.lr.begin(), s.lr.end(), lr);
+    std::copy(s.dgl.begin(), s.dgl.end(), dgl);
+    std::copy(s.dgr.begin(), s.dgr.end(), dgr);
+}
+
+// ------------------------------- discretization --------------------------------------
+struct Handle {
+    Disc g;
+    Workspace<double> ws;
+    std::vector<double> U, L;
+};
+
+void* oracle_disc_new(int dim, int eq, double gamma, const double* adv, int volop, int tpflux, int numflux,
+                      int lxf_avg, double intensity, int n, const double* Ds, const double* Dsharp, const double* ll,
+                      const double* lr, const double* dgl, const double* dgr, int nelem, int nfaces,
+                      const int* faceinds, const int* facepos, const int* eleminds, const int* elempos,
+                      const unsigned char* orient, const int* bdid, int nbcs, const int* bc_kinds,
+                      const double* bc_states, const double* J, const double* Ja, const double* frames,
+                      const double* faceJ) {
+    Handle* h = new Handle();
+    Disc& g = h->g;
+    Config& c = g.cfg;
+    c.dim = dim;
+    c.eq = eq;
+    c.nv = eq == EQ_EULER ? dim + 2 : 1;
+    c.gamma = gamma;
+    for (int d = 0; d < 3; ++d) c.a[d] = adv ? adv[d] : 0.0;
+    c.volop = volop;
+    c.tpflux = tpflux;
+    c.numflux = numflux;
+    c.lxf_avg = lxf_avg;
+    c.intensity = intensity;
+    g.n = n;
+    g.npe = 1;
+    g.nfd = 1;
+    for (int d = 0; d < dim; ++d) g.npe *= n;
+    for (int d = 0; d < dim - 1; ++d) g.nfd *= n;
+    g.nelem = nelem;
+    g.nfaces = nfaces;
+    g.Ds.assign(Ds, Ds + n * n);
+    g.Dsharp.assign(Dsharp, Dsharp + n * n);
+    g.ll.assign(ll, ll + n);
+    g.lr.assign(lr, lr + n);
+    g.dgl.assign(dgl, dgl + n);
+    g.dgr.assign(dgr, dgr + n);
+    g.faceinds.assign(faceinds, faceinds + nelem * 2 * dim);
+    g.facepos.assign(facepos, facepos + nelem * 2 * dim);
+    g.eleminds.assign(eleminds, eleminds + nfaces * 2);
+    g.elempos.assign(elempos, elempos + nfaces * 2);
+    g.orient.assign(orient, orient + nfaces);
+    g.bdid.assign(bdid, bdid + nfaces);
+    g.bcs.resize(nbcs);
+    for (int b = 0; b < nbcs; ++b) {
+        g.bcs[b].kind = bc_kinds[b];
+        for (int k = 0; k < 5; ++k) g.bcs[b].state[k] = bc_states[b * 5 + k];
+    }
+    long nd = g.ndofs(), nf = g.nfdofs();
+    g.J.assign(J, J + nd);
+    g.Ja.assign(Ja, Ja + nd * dim * dim);
+    g.frames.resize(nf);
+    for (long i = 0; i < nf; ++i)
+        for (int q = 0; q < 3; ++q) {
+            g.frames[i].n[q] = frames[i * 9 + q];
+            g.frames[i].t[q] = frames[i * 9 + 3 + q];
+            g.frames[i].b[q] = frames[i * 9 + 6 + q];
+        }
+    g.faceJ.assign(faceJ, faceJ + nf);
+    return h;
+}
+
+void oracle_disc_free(void* h) { delete (Handle*)h; }
+
+int oracle_rhs(void* hp, double* dQ, const double* Q, double t) {
+    Handle* h = (Handle*)hp;
+    try {
+        rhs(h->g, dQ, Q, t, h->ws);
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "oracle_rhs: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+int oracle_ssprk3(void* hp, double* Q, double dt, int nsteps, double t0) {
+    Handle* h = (Handle*)hp;
+    try {
+        for (int s = 0; s < nsteps; ++s) ssprk3_step(h->g, Q, dt, t0 + s * dt, h->ws, h->U, h->L);
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "oracle_ssprk3: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+double oracle_max_dt(void* hp, const double* Q, double cfl, const double* omega_tp) {
+    Handle* h = (Handle*)hp;
+    std::vector<double> w(omega_tp, omega_tp + h->g.npe);
+    return get_max_dt(h->g, Q, cfl, w);
+}
+
+// Operation count of one residual evaluation (single thread).  out = {add, mul, div, sqrt,
+// log, cmp}.
+void oracle_count_rhs(void* hp, const double* Q, double t, long long* out) {
+    Handle* h = (Handle*)hp;
+    int nt = omp_get_max_threads();
+    omp_set_num_threads(1);
+    long N = h->g.ndofs() * h->g.cfg.nv;
+    std::vector<CD> q(N), dq(N);
+    for (long i = 0; i < N; ++i) q[i] = CD(Q[i]);
+    Workspace<CD> ws;
+    g_count = OpCount();
+    rhs(h->g, dq.data(), q.data(), t, ws);
+    out[0] = g_count.add; out[1] = g_count.mul; out[2] = g_count.div;
+    out[3] = g_count.sqrt; out[4] = g_count.log; out[5] = g_count.cmp;
+    omp_set_num_threads(nt);
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+"""GPU parity: libflou_cuda against the CPU oracle on the same inputs, through the C ABI.
+
+Bars (north-star): one residual to <= 1e-12 relative L-inf per variable, N SSP-RK3 steps to
+<= 1e-10; connectivity/index work is bit-exact (set-up tests).  Relative L-inf is
+max_v max_i |a - b| / max_i |b| per variable.
+"""
+import numpy as np
+import pytest
+
+import flou_cuda as F
+import oracle_ref
+from cases import build, oracle_for, rel_linf, smooth_euler_state
+
+pytestmark = pytest.mark.gpu
+
+RES_TOL = 1e-12
+STEP_TOL = 1e-10
+
+
+def _euler(dim):
+    return F.EulerEquation(dim, 1.4)
+
+
+def _ops():
+    return {
+        "strong_lxf": lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+        "strong_lxf_half": lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 0.5)),
+        "strong_hllc": lambda: F.StrongDivOperator(F.HLLC()),
+        "strong_hll": lambda: F.StrongDivOperator(F.HLL()),
+        "strong_std": lambda: F.StrongDivOperator(F.StdAverage()),
+        "split_chandra_hllc": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()),
+        "split_chandra_chandra": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.ChandrasekharAverage()),
+        "split_chandra_lxfc": lambda: F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)),
+        "split_kg_lxf": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
+        "split_std_lxf": lambda: F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)),
+    }
+
+
+EULER_CASES = [
+    (1, 6, (7,), "split_chandra_lxfc"),
+    (1, 4, (5,), "strong_lxf"),
+    (1, 5, (6,), "strong_hllc"),
+    (2, 5, (4, 4), "strong_lxf"),
+    (2, 5, (3, 4), "strong_hllc"),
+    (2, 4, (3, 3), "strong_hll"),
+    (2, 3, (4, 3), "strong_std"),
+    (2, 5, (3, 3), "split_chandra_lxfc"),
+    (2, 6, (3, 2), "split_chandra_chandra"),
+    (2, 4, (3, 3), "split_kg_lxf"),
+    (2, 4, (3, 3), "split_std_lxf"),
+    (2, 5, (3, 3), "strong_lxf_half"),
+    (3, 4, (3, 3, 3), "split_chandra_hllc"),
+    (3, 8, (2, 2, 2), "split_chandra_hllc"),
+    (3, 3, (3, 2, 3), "strong_lxf"),
+    (3, 3, (2, 3, 2), "split_chandra_chandra"),
+    (3, 5, (2, 2, 2), "split_kg_lxf"),
+    (3, 4, (2, 2, 2), "split_std_lxf"),
+]
+
+
+def _check(disc, Q, nsteps=5, res_tol=RES_TOL, step_tol=STEP_TOL, arrays=None):
+    o = oracle_for(disc, arrays)
+    ref = o.rhs(Q)
+    dQ = disc.new_state()
+    disc.ctx.rhs(dQ, Q)
+    e_res = rel_linf(dQ, ref)
+    assert e_res <= res_tol, "residual rel err %.3e" % e_res
+    dt = 0.3 * disc.ctx.max_dt(Q, 1.0)
+    Qg = Q.copy(order="F")
+    disc.ctx.step(Qg, dt, nsteps)
+    e_step = rel_linf(Qg, o.ssprk3(Q, dt, nsteps))
+    assert e_step <= step_tol, "%d-step rel err %.3e" % (nsteps, e_step)
+    return e_res, e_step
+
+
+@pytest.mark.parametrize("dim,n,ne,op", EULER_CASES)
+def test_euler_periodic(dim, n, ne, op):
+    disc = build(dim, n, ne, _euler(dim), _ops()[op]())
+    _check(disc, smooth_euler_state(disc, seed=dim * 10 + n))
+
+
+@pytest.mark.parametrize("n", range(2, 9))
+def test_euler2d_strong_all_orders(n):
+    disc = build(2, n, (3, 2), _euler(2), _ops()["strong_lxf"]())
+    _check(disc, smooth_euler_state(disc, seed=n))
+
+
+@pytest.mark.parametrize("n", range(2, 9))
+def test_euler3d_split_all_orders(n):
+    disc = build(3, n, (2, 2, 2), _euler(3), _ops()["split_chandra_hllc"]())
+    _check(disc, smooth_euler_state(disc, seed=100 + n), nsteps=3)
+
+
+@pytest.mark.parametrize("dim,op", [(2, "strong_lxf"), (2, "split_chandra_hllc"), (3, "split_chandra_hllc"),
+                                    (1, "strong_hllc")])
+def test_euler_walls_inflow_outflow(dim, op):
+    eq = _euler(dim)
+    # x: slip walls; y: inflow / outflow; z: periodic
+    per = (2,) if dim == 3 else ()
+    mesh_bcs = {"1": F.EulerSlipBC(), "2": F.EulerSlipBC()}
+    if dim >= 2:
+        Pin = np.zeros(dim + 2)
+        Pin[0], Pin[2], Pin[-1] = 1.1, 0.3, 1.05
+        mesh_bcs["3"] = F.EulerInflowBC(eq.vars_prim2cons(Pin))
+        mesh_bcs["4"] = F.EulerOutflowBC()
+    disc = build(dim, 4, (3,) * dim, eq, _ops()[op](), periodic=per, bcs=mesh_bcs)
+    _check(disc, smooth_euler_state(disc, seed=7))
+
+
+def test_oracle_built_operators_general_path():
+    """Flou-style fitted operators (tiny non-zero off-end entries) take the general
+    interpolation path on the GPU."""
+    disc = build(2, 5, (3, 3), _euler(2), _ops()["strong_lxf"]())
+    a = disc.abi_arrays()
+    o = oracle_ref.operators(5, True)
+    for k in ("D", "Ds", "Dsharp", "omega", "l_l", "l_r", "dg_l", "dg_r"):
+        a[k] = o[k]
+    disc._ctx = F.Context(disc.config, a, disc.mesh.nelements, disc.mesh.nfaces)
+    _check(disc, smooth_euler_state(disc, seed=5), arrays=a)
+
+
+@pytest.mark.parametrize("dim,basis,op", [(1, "GL", "strong"), (2, "GL", "strong"), (3, "GLL", "strong"),
+                                          (2, "GLL", "split"), (3, "GLL", "split"), (1, "GLL", "strong")])
+def test_linear_advection(dim, basis, op):
+    eq = F.LinearAdvection(*[1.0, -0.7, 0.4][:dim])
+    o = (F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)) if op == "strong"
+         else F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    disc = build(dim, 5, (3,) * dim, eq, o, basis=basis)
+    Q = np.asfortranarray(1.0 + 0.3 * np.sin(np.pi * disc.coords[:, :1]).prod(axis=1, keepdims=True))
+    _check(disc, Q)
+
+
+def test_linear_advection_dirichlet():
+    eq = F.LinearAdvection(1.0, 0.5)
+    bcs = {"1": F.DirichletBC([0.5]), "2": F.OutflowBC(), "3": F.DirichletBC([0.25]), "4": F.OutflowBC()}
+    disc = build(2, 4, (3, 3), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), periodic=(), bcs=bcs)
+    Q = np.asfortranarray(1.0 + 0.2 * np.cos(disc.coords[:, :1]))
+    _check(disc, Q)
+
+
+@pytest.mark.parametrize("op", ["strong", "split"])
+def test_burgers(op):
+    eq = F.BurgersEquation()
+    o = (F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)) if op == "strong"
+         else F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    disc = build(1, 6, (8,), eq, o)
+    Q = np.asfortranarray(1.5 + 0.5 * np.sin(np.pi * disc.coords[:, :1]))
+    _check(disc, Q)
+
+
+def test_max_dt_matches_oracle():
+    eq = _euler(2)
+    disc = build(2, 5, (8, 8), eq, _ops()["strong_lxf"](), box=((-5.0, -5.0), (5.0, 5.0)))
+    Q = np.asfortranarray(F.initial.isentropic_vortex(eq, disc.coords, (1.0, 2.0), period=(10, 10)))
+    dt = disc.ctx.max_dt(Q, 0.5)
+    ref = oracle_for(disc).max_dt(Q, 0.5, disc.std.omega)
+    assert abs(dt - ref) <= 4e-16 * ref
+
+
+def test_nonphysical_state_raises_domain_error():
+    eq = _euler(2)
+    disc = build(2, 4, (3, 3), eq, _ops()["strong_lxf"]())
+    Q = smooth_euler_state(disc, seed=2)
+    Q[17, 0] = -1.0   # negative density, planted on the host
+    with pytest.raises(F.DomainError) as ei:
+        disc.ctx.rhs(disc.new_state(), Q)
+    assert "element 1" in str(ei.value)
+    # the context stays usable
+    Q[17, 0] = 1.0
+    disc.ctx.rhs(disc.new_state(), Q)
+
+
+def test_device_pointers_and_determinism():
+    torch = pytest.importorskip("torch")
+    eq = _euler(3)
+    disc = build(3, 4, (3, 3, 3), eq, _ops()["split_chandra_hllc"]())
+    Q = smooth_euler_state(disc, seed=9)
+    Qd = torch.from_numpy(np.ascontiguousarray(Q.T)).cuda()
+    dQd = torch.empty_like(Qd)
+    disc.ctx.rhs(dQd, Qd)
+    ref = oracle_for(disc).rhs(Q)
+    assert rel_linf(dQd.cpu().numpy().T, ref) <= RES_TOL
+    again = torch.empty_like(Qd)
+    disc.ctx.rhs(again, Qd)
+    assert torch.equal(again, dQd)   # bitwise reproducible (no atomics on the data path)
+    a, b = Qd.clone(), Qd.clone()
+    disc.ctx.step(a, 1e-3, 4)
+    disc.ctx.step(b, 1e-3, 2)
+    disc.ctx.step(b, 1e-3, 2)
+    assert torch.equal(a, b)   # graph replays are deterministic

@@ -1,0 +1,118 @@
+"""The oracle against the reference's own known-answer tests and the invariants of the
+scheme.  Pins: the Advection1D / Advection2D period property (test/tests.jl:16-88,
+test/runtests.jl:23-32: u(T) ≈ u(0), rtol 1e-3) re-run with SSP-RK3 at the reference's dt;
+freestream preservation; discrete conservation; entropy conservation of the split form
+with entropy-conserving fluxes; the convergence order of examples/src/Convergence.jl."""
+import numpy as np
+import pytest
+
+import flou_cuda as F
+import oracle_ref
+from cases import build, oracle_for, smooth_euler_state
+
+
+def _norm_close(a, b, rtol):   # Julia's isapprox for arrays: norm(a-b) <= rtol*max(norm(a), norm(b))
+    return np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b))
+
+
+def _oracle_disc(disc, lobatto):
+    """Oracle fed with the operators built by its own (reference) construction."""
+    a = disc.abi_arrays()
+    o = oracle_ref.operators(disc.std.n, lobatto)
+    for k in ("D", "Ds", "Dsharp", "omega", "l_l", "l_r", "dg_l", "dg_r"):
+        a[k] = o[k]
+    return oracle_for(disc, a)
+
+
+def test_advection1d_period():
+    """Advection1D: GL n=5, 20 elements on [0,1], a=2, LxF(StdAverage,1), dt=1e-3, t=0.5."""
+    eq = F.LinearAdvection(2.0)
+    disc = build(1, 5, (20,), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), basis="GL",
+                 box=((0.0,), (1.0,)))
+    Q0 = np.asfortranarray(F.initial.gaussian_bump(disc.coords, (0.5,), (0.1,), 1.0)[:, None])
+    o = _oracle_disc(disc, lobatto=False)
+    Q = o.ssprk3(Q0, 1e-3, 500)
+    assert _norm_close(Q, Q0, 1e-3)
+    assert not np.allclose(o.ssprk3(Q0, 1e-3, 250), Q0, rtol=1e-3)   # it did move
+
+
+def test_advection2d_period():
+    """Advection2D: GL n=5, 20x10 elements on [0,1.5]x[0,2], a=(3,4), dt=1e-3, t=0.5."""
+    eq = F.LinearAdvection(3.0, 4.0)
+    disc = build(2, 5, (20, 10), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), basis="GL",
+                 box=((0.0, 0.0), (1.5, 2.0)))
+    Q0 = np.asfortranarray(F.initial.gaussian_bump(disc.coords[:, :2], (0.75, 1.0), (0.2, 0.2), 1.0)[:, None])
+    o = _oracle_disc(disc, lobatto=False)
+    Q = o.ssprk3(Q0, 1e-3, 500)
+    assert _norm_close(Q, Q0, 1e-3)
+
+
+@pytest.mark.parametrize("dim,n,vol", [(1, 5, "strong"), (2, 4, "strong"), (2, 5, "split"), (3, 3, "split"),
+                                       (3, 4, "strong")])
+def test_freestream_and_conservation(dim, n, vol):
+    eq = F.EulerEquation(dim, 1.4)
+    if vol == "strong":
+        op = F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
+    else:
+        op = F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC())
+    disc = build(dim, n, (3,) * dim, eq, op)
+    o = oracle_for(disc)
+    P = np.zeros((disc.ndofs, dim + 2))
+    P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.3, 0.4, 2.0
+    Qf = np.asfortranarray(eq.vars_prim2cons(P))
+    assert np.max(np.abs(o.rhs(Qf))) < 1e-12
+    Q = smooth_euler_state(disc, seed=1)
+    dQ = o.rhs(Q)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    for v in range(dim + 2):
+        assert abs(w @ dQ[:, v]) < 1e-12 * np.sum(w * np.abs(dQ[:, v]))
+
+
+def test_entropy_conservation_split_form():
+    """Split form with Chandrashekar volume and interface fluxes conserves entropy (2D)."""
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 5, (3, 3), eq, F.SplitDivOperator(F.ChandrasekharAverage(), F.ChandrasekharAverage()))
+    o = oracle_for(disc)
+    Q = smooth_euler_state(disc, seed=3, amp=0.2)
+    dQ = o.rhs(Q)
+    g = eq.gamma
+    p = eq.pressure(Q)
+    s = np.log(p) - g * np.log(Q[:, 0])
+    W = np.stack([(g - s) / (g - 1) - (Q[:, 1] ** 2 + Q[:, 2] ** 2) / Q[:, 0] / (2 * p), Q[:, 1] / p, Q[:, 2] / p,
+                  -Q[:, 0] / p], axis=1)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    dS = w @ np.sum(W * dQ, axis=1)
+    scale = w @ np.sum(np.abs(W * dQ), axis=1)
+    # exact up to the truncated log-mean series (relative error <= u^4/9 for u < 0.01)
+    assert abs(dS) < 1e-10 * scale
+
+
+def test_convergence_order():
+    """1D Euler, smooth solution 2 + sin(π(x - t)) with u = p = 1 (examples/src/Convergence.jl),
+    LGL p=3, split form with LxF(Chandrashekar): the error falls like h^(p+1)."""
+    eq = F.EulerEquation(1, 1.4)
+    errs = []
+    for ne in (8, 16):
+        disc = build(1, 4, (ne,), eq, F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)))
+        x = disc.coords[:, 0]
+        sol = lambda t: np.asfortranarray(eq.vars_prim2cons(np.stack([2 + np.sin(np.pi * (x - t)),
+                                                                      np.ones_like(x), np.ones_like(x)], 1)))
+        o = oracle_for(disc)
+        dt, T = 1e-3, 0.2
+        Q = o.ssprk3(sol(0.0), dt, int(round(T / dt)))
+        errs.append(np.sqrt(np.mean((Q - sol(T)) ** 2)))
+    rate = np.log2(errs[0] / errs[1])
+    assert rate > 3.3, (errs, rate)
+
+
+def test_oracle_max_dt_formula():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 5, (4, 4), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+                 box=((-5.0, -5.0), (5.0, 5.0)))
+    Q = np.asfortranarray(F.initial.isentropic_vortex(eq, disc.coords, (0.3, -0.2), period=(10, 10)))
+    o = oracle_for(disc)
+    dt = o.max_dt(Q, 0.5, disc.std.omega)
+    P = eq.vars_cons2prim(Q)
+    c = np.sqrt(1.4 * P[:, 3] / P[:, 0])
+    ref = np.min(0.5 * np.sqrt(2.5 ** 2 / 25) / (np.hypot(P[:, 1], P[:, 2]) + c))
+    assert abs(dt - ref) < 1e-14 * ref
