@@ -1,0 +1,326 @@
+"""Benchmark: FP64 DOF·stage-updates/s of the DGSEM residual + SSP-RK3 on one GB300.
+
+Workload (3D compressible Euler Taylor-Green vortex, Mach 0.1, ρ0 = 1, p0 = 1/(γM²), periodic
+[0, 2π]³, split-form flux differencing with the Chandrashekar two-point flux, HLLC interface
+flux, SSP-RK3):  mesh A = 32³ elements at p = 3, mesh B = 16³ elements at p = 7
+(2,097,152 nodes each).  One bench step = one SSP-RK3 step of A and one of B.
+A DOF is a solution node (all 5 variables); one DOF·stage-update advances one node through
+one RK stage (residual + stage combination).
+
+  value   device-resident throughput (states already in HBM), CUDA events on the launching
+          stream, K steps between synchronised barriers, max over ranks
+  e2e     the same metric through the public API with pinned host buffers: every step copies
+          the state host->device, advances it and copies it back
+  --impl reference   the CPU oracle (the C++ restatement of Flou's residual), all host
+          threads, on a bounded sample mesh of the same configuration
+
+Under torchrun (N > 1) every rank runs its own replica of the workload (the path has no
+exchange step); value = total DOF·stage-updates of all ranks / max time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "flou.jl_gb300"))
+
+import numpy as np
+
+METRIC = "FP64 DOF·stage-updates/s (residual + SSP-RK3 stage), 3D Euler TGV split-form"
+UNIT = "DOF·stage-updates/s"
+NV = 5
+BYTES_PER_DOF_STAGE = (8.0 / 3.0) * NV * 8   # compulsory state traffic, fused SSP-RK3
+
+
+def make_tgv(nel, n, mach=0.1):
+    import flou_cuda as F
+    eq = F.EulerEquation(3, 1.4)
+    mesh = F.CartesianMesh((0.0, 0.0, 0.0), (2 * math.pi,) * 3, (nel,) * 3)
+    F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
+    b = F.LagrangeBasis("GLL", n)
+    std = F.StdHex(b, F.DGSEMrec(b), eq.nvariables)
+    disc = F.MultielementDisc(mesh, std, eq, F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), {})
+    Q0 = np.asfortranarray(F.initial.taylor_green(eq, disc.coords, mach=mach))
+    return disc, Q0
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def load_profile_summary():
+    """Per-DOF DRAM traffic and executed FP64 operations of the element kernels, from the
+    committed ncu summary (profiles/)."""
+    p = os.path.join(ROOT, "profiles", "tgv3d_split_elem_kernel.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def cpu_oracle_rate(steps, warmup, threads):
+    """The CPU oracle on a bounded sample of the workload: one SSP-RK3 step on a 16³ p=3 mesh
+    and one on an 8³ p=7 mesh (262,144 nodes each) per step.  Returns (rate, seconds, ndofs)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_ref
+    from cases import oracle_for
+    L = oracle_ref.lib()
+    L.oracle_set_threads(threads)
+    samples = []
+    for nel, n in ((16, 4), (8, 8)):
+        disc, Q0 = make_tgv(nel, n)
+        o = oracle_for(disc)
+        dt = 0.5 * o.max_dt(Q0, 1.0, disc.std.omega)
+        samples.append((o, Q0, dt, disc.ndofs))
+    for _ in range(warmup):
+        for o, Q0, dt, _n in samples:
+            o.ssprk3(Q0, dt, 1)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o, Q0, dt, _n in samples:
+            o.ssprk3(Q0, dt, 1)
+    sec = time.perf_counter() - t0
+    ndofs = sum(s[3] for s in samples)
+    return ndofs * 3 * steps / sec, sec, ndofs
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    steps = max(args.steps, 1)
+    rate, sec, ndofs = cpu_oracle_rate(steps, args.warmup, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sec / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "tgv3d_split_chandrashekar_hllc_sample_16c_p3+8c_p7", "sample_ndofs": ndofs,
+                   "note": "Flou's Julia path cannot run here (no julia); the C++ restatement of its residual"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "1 SSP-RK3 step on a 16^3 p=3 and an 8^3 p=7 TGV mesh per step"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_profile(which):
+    """Two SSP-RK3 steps of one mesh on the device (the case the ncu captures use)."""
+    import torch
+    nel, n = (32, 4) if which == "A" else (16, 8)
+    disc, Q0 = make_tgv(nel, n)
+    Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+    dt = 0.5 * disc.ctx.max_dt(Qd, 1.0)
+    disc.ctx.step(Qd, dt, 2)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "tgv3d %d^3 p=%d" % (nel, n - 1), "ndofs": disc.ndofs, "steps": 2}))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["A", "B"], default=None,
+                    help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3) or B (16^3 p=7) only")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile:
+        return run_profile(args.profile)
+
+    import torch
+    import flou_cuda as F
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    steps, warmup = args.steps, max(args.warmup, 3)
+    meshes = []
+    for nel, n in ((32, 4), (16, 8)):
+        disc, Q0 = make_tgv(nel, n)
+        ctx = disc.ctx
+        Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+        dt = 0.5 * ctx.max_dt(Qd, 1.0)
+        meshes.append(dict(name="%dc_p%d" % (nel, n - 1), disc=disc, ctx=ctx, Q0=Q0, Qd=Qd, dt=dt, ndofs=disc.ndofs))
+    stream = torch.cuda.current_stream()
+    for m in meshes:
+        m["ctx"].set_stream(stream.cuda_stream)
+    ndofs = sum(m["ndofs"] for m in meshes)
+
+    fp64_peak = None
+    try:
+        import ctypes
+        g = ctypes.c_double()
+        if F.load().flou_fp64_peak(ctypes.byref(g)) == 0:
+            fp64_peak = g.value
+    except Exception:
+        pass
+
+    # ---- value: device-resident ----
+    for _ in range(warmup):
+        for m in meshes:
+            m["ctx"].step(m["Qd"], m["dt"], 1)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        for m in meshes:
+            m["ctx"].step(m["Qd"], m["dt"], 1)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ndofs * 3 * steps / (ms * 1e-3)
+
+    # ---- per-kernel timing for the roofline (CUDA events around single launches) ----
+    kern = {}
+    for m in meshes:
+        fms, ems = m["ctx"].time_kernels(m["Qd"], nrep=3)
+        kern[m["name"]] = {"face_ms": fms, "elem_ms": ems, "ndofs": m["ndofs"]}
+    tot = {k: 3 * (v["face_ms"] + v["elem_ms"]) for k, v in kern.items()}
+    dom = max(kern, key=lambda k: kern[k]["elem_ms"])
+    dk = kern[dom]
+    algo_bytes = BYTES_PER_DOF_STAGE * dk["ndofs"]
+    achieved = algo_bytes / (dk["elem_ms"] * 1e-3) / 1e9
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peaks = json.load(open(pp))
+    hbm_peak = peaks.get("hbm_gbs")
+    prof = load_profile_summary().get(dom, {})
+    traffic = prof.get("dram_bytes_per_dof_stage")
+    fp64_ops = prof.get("fp64_flops_per_dof_stage")
+    roofline = {
+        "kernel": "elem_split_kernel<3,%d,Euler,Chandrashekar> (%s)" % (int(dom[-1]) + 1, dom),
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": (achieved / hbm_peak) if hbm_peak else None,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None,
+        "traffic": (traffic * dk["ndofs"]) if traffic else None,
+        "algorithmic_bytes_per_launch": algo_bytes,
+        "launch_ms": dk["elem_ms"],
+        "fp64": {
+            "peak_gflops": fp64_peak, "peak_source": "DFMA throughput probe (flou_fp64_peak), this run",
+            "executed_flops_per_dof_stage": fp64_ops,
+            "achieved_gflops": (fp64_ops * dk["ndofs"] / (dk["elem_ms"] * 1e-3) / 1e9) if fp64_ops else None,
+        },
+        "kernels": kern,
+    }
+    if fp64_ops and fp64_peak:
+        roofline["fp64"]["frac"] = roofline["fp64"]["achieved_gflops"] / fp64_peak
+
+    # ---- e2e: through the public API with pinned host buffers ----
+    hosts = []
+    for m in meshes:
+        m["ctx"].set_stream(0)
+        h = torch.from_numpy(np.ascontiguousarray(m["Q0"].T)).pin_memory()
+        hosts.append(h)
+        m["ctx"].step(h, m["dt"], 1)   # warm the host-pointer path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for m, h in zip(meshes, hosts):
+            m["ctx"].step(h, m["dt"], 1)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    state_bytes = sum(m["ndofs"] * NV * 8 for m in meshes)
+    e2e = {"value": world * ndofs * 3 * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+           "d2h_bytes_per_step": state_bytes}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, sec, nd = cpu_oracle_rate(4, 1, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "4 SSP-RK3 steps on a 16^3 p=3 and an 8^3 p=7 TGV mesh (%d nodes), %.1f s wall" % (nd, sec)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tgv3d_M0.1_split_chandrashekar_hllc_ssprk3: 32^3 p=3 + 16^3 p=7",
+                       "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -609,6 +609,43 @@ int32_t flou_take_status(flou_ctx* c, int32_t* flags, int32_t* elem) {
     return FLOU_OK;
 }
 
+int32_t flou_time_kernels(flou_ctx* c, const double* Q, int32_t nrep, double* face_ms, double* elem_ms) {
+    int r = ready(c);
+    if (r) return r;
+    if (!Q || nrep <= 0 || !face_ms || !elem_ms) return fail(c, FLOU_ERR_ARG, "invalid arguments");
+    if ((r = ensure(c, &c->d_U, (size_t)c->ndofs * c->nv, "stage buffer"))) return r;
+    if ((r = ensure(c, &c->d_dQh, (size_t)c->ndofs * c->nv, "stage buffer"))) return r;
+    cudaEvent_t ev[4];
+    for (auto& e : ev) CK(cudaEventCreate(&e), "event create");
+    double tf = 0.0, te = 0.0;
+    for (int it = 0; it < nrep; ++it) {
+        for (int mode = 1; mode <= 3; ++mode) {
+            CK(cudaEventRecord(ev[0], c->stream), "event record");
+            cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
+            CK(cudaEventRecord(ev[1], c->stream), "event record");
+            // stage 1: U = Q + dt L; stages 2, 3: out = a0 Q0 + a1 (U + dt L) (written to scratch)
+            ElemParams P = mode == 1 ? elem_params(c, Q, Q, c->d_U, 1, 1e-9, 0.0, 1.0)
+                                     : elem_params(c, Q, Q, c->d_dQh, 2, 1e-9, mode == 2 ? 0.75 : 1.0 / 3.0,
+                                                   mode == 2 ? 0.25 : 2.0 / 3.0);
+            CK(cudaEventRecord(ev[2], c->stream), "event record");
+            e = launch_elem(elem_launch(c), P, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "element kernel launch");
+            CK(cudaEventRecord(ev[3], c->stream), "event record");
+            CK(cudaEventSynchronize(ev[3]), "event synchronize");
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[2], ev[3]);
+            tf += a;
+            te += b;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    *face_ms = tf / (3.0 * nrep);
+    *elem_ms = te / (3.0 * nrep);
+    return check_status(c);
+}
+
 int32_t flou_fp64_peak(double* gflops) {
     if (!gflops) return FLOU_ERR_ARG;
     flou_ctx* c = nullptr;

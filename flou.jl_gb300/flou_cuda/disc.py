@@ -207,12 +207,12 @@ class Context:
             if writable and not a.flags.writeable:
                 raise ValueError("state is read-only")
             return ctypes.c_void_p(a.ctypes.data), L.PTR_HOST
-        # torch tensor on the GPU
-        if not getattr(a, "is_cuda", False):
-            raise TypeError("state must be a numpy array or a CUDA tensor")
+        # torch tensor: CUDA (device pointer) or CPU, e.g. pinned (host pointer)
+        if not hasattr(a, "data_ptr"):
+            raise TypeError("state must be a numpy array or a torch tensor")
         if a.numel() != self.ndofs * self.nvars or not a.is_contiguous() or str(a.dtype) != "torch.float64":
-            raise ValueError("device state must be a contiguous float64 tensor (nvars, ndofs)")
-        return ctypes.c_void_p(a.data_ptr()), L.PTR_DEVICE
+            raise ValueError("state tensor must be a contiguous float64 tensor (nvars, ndofs)")
+        return ctypes.c_void_p(a.data_ptr()), (L.PTR_DEVICE if a.is_cuda else L.PTR_HOST)
 
     def set_stream(self, stream_ptr):
         L.check(self._lib.flou_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
@@ -233,6 +233,15 @@ class Context:
         out = ctypes.c_double()
         L.check(self._lib.flou_max_dt(self.h, pq, float(cfl), ctypes.byref(out), kq), self.h)
         return out.value
+
+    def time_kernels(self, Q, nrep=3):
+        """Mean launch durations (ms) of the face kernel and the element kernel (CUDA events)."""
+        pq, kq = self._ptr(Q)
+        if kq != L.PTR_DEVICE:
+            raise ValueError("time_kernels needs a device state")
+        f, e = ctypes.c_double(), ctypes.c_double()
+        L.check(self._lib.flou_time_kernels(self.h, pq, int(nrep), ctypes.byref(f), ctypes.byref(e)), self.h)
+        return f.value, e.value
 
     def take_status(self):
         f, e = ctypes.c_int32(), ctypes.c_int32()

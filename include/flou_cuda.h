@@ -154,6 +154,12 @@ int32_t flou_sizes(const flou_ctx* ctx, int64_t* ndofs, int32_t* nvars, int32_t*
  * lowest element index (1-based) that raised it, 0 if none.  Clears the word. */
 int32_t flou_take_status(flou_ctx* ctx, int32_t* flags, int32_t* elem);
 
+/* Times the two kernels of one RK stage on the context's stream with CUDA events: `nrep`
+ * launches of the face kernel and of the element kernel in each of the three stage modes
+ * (Q is a device state; the results go to internal scratch).  Returns the mean duration of
+ * one launch in milliseconds.  No counterpart in the reference (measurement hook). */
+int32_t flou_time_kernels(flou_ctx* ctx, const double* Q, int32_t nrep, double* face_ms, double* elem_ms);
+
 /* Measured FP64 fused-multiply-add throughput of the current device in GFLOP/s (2 flops per
  * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
 int32_t flou_fp64_peak(double* gflops);

@@ -164,7 +164,7 @@ def test_nonphysical_state_raises_domain_error():
     Q[17, 0] = -1.0   # negative density, planted on the host
     with pytest.raises(F.DomainError) as ei:
         disc.ctx.rhs(disc.new_state(), Q)
-    assert "element 1" in str(ei.value)
+    assert "element 2" in str(ei.value)   # node 17 of 16-node elements
     # the context stays usable
     Q[17, 0] = 1.0
     disc.ctx.rhs(disc.new_state(), Q)
