@@ -675,3 +675,81 @@ int32_t flou_fp64_peak(double* gflops) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Residual without any device allocation.
+//
+// flou_rhs allocates its face-flux buffer lazily with cudaMalloc on the first call.  Some
+// callers cannot allow that: a Julia caller whose device memory is owned by CUDA.jl's
+// memory pool, or a PyTorch caller whose caching allocator has already reserved the free
+// memory, may see that cudaMalloc fail (or may forbid allocations outside their pool once
+// the solve has started).  flou_rhs_noalloc computes the same residual with its face
+// fluxes in the fixed array below, which is part of the library image: every GPU that
+// loads libflou_cuda holds these 8 MiB until the process exits.
+//
+// Contract: device pointers only; nfaces * n^(d-1) * nvars must not exceed
+// FLOU_NOALLOC_MAX_FACE_VALUES.  All calls (from every context) share the array, so calls
+// that overlap on the GPU race on it; serialise them (one stream, or events).  The array
+// keeps the last call's contents; nothing in it has to start at zero, because the face
+// kernel overwrites every value it later reads.  The first call on a device looks up the
+// array's device address (cudaGetSymbolAddress) for that device; make that first call
+// before any stream capture.
+// ---------------------------------------------------------------------------------------
+#define FLOU_NOALLOC_MAX_FACE_VALUES (1 << 20)
+
+static __device__ __align__(256) double g_noalloc_face_flux[FLOU_NOALLOC_MAX_FACE_VALUES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Once per device, with that device current: the device address of the scratch array.
+// Returns nullptr (and sets *err) when the lookup fails.
+double* noalloc_scratch(cudaError_t* err) {
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= kMaxDevices) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        *err = cudaGetSymbolAddress(&p, g_noalloc_face_flux);
+        if (*err != cudaSuccess) return nullptr;
+        g_noalloc_ptr[dev] = (double*)p;
+    }
+    return g_noalloc_ptr[dev];
+}
+}  // namespace
+
+extern "C" int32_t flou_rhs_noalloc(flou_ctx* c, double* dQ, const double* Q, double t) {
+    (void)t;
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_ops || !c->have_mesh || !c->have_geom)
+        return fail(c, FLOU_ERR_STATE, "operators, mesh and geometry must be set before flou_rhs_noalloc");
+    for (int f = 0; f < c->nfaces; ++f) {
+        int b = c->h_face_bc[f];
+        if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
+            return fail(c, FLOU_ERR_STATE, "boundary index %d of face %d has no boundary condition", b + 1, f + 1);
+    }
+    if (!dQ || !Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
+    int64_t need = c->nfdofs * c->nv;
+    if (need > FLOU_NOALLOC_MAX_FACE_VALUES)
+        return fail(c, FLOU_ERR_ARG,
+                    "flou_rhs_noalloc: the mesh has %lld face values (nfaces x n^(d-1) x nvars); the fixed "
+                    "scratch holds at most %d",
+                    (long long)need, FLOU_NOALLOC_MAX_FACE_VALUES);
+    cudaError_t e = cudaSuccess;
+    double* scratch = noalloc_scratch(&e);
+    if (!scratch) return cuda_fail(c, e, "flou_rhs_noalloc scratch address");
+    FaceParams fp = face_params(c, Q);
+    fp.Fn = scratch;
+    e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
+    ElemParams ep = elem_params(c, Q, Q, dQ, 0, 0.0, 0.0, 0.0);
+    ep.Fn = scratch;
+    e = launch_elem(elem_launch(c), ep, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "element kernel launch");
+    return check_status(c);
+}

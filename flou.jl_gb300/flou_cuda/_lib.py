@@ -85,6 +85,7 @@ PROTOTYPES = {
     "flou_sizes": [_P, _I64, _I32, _I32, _I32],
     "flou_take_status": [_P, _I32, _I32],
     "flou_time_kernels": [_P, _P, ctypes.c_int32, _D, _D],
+    "flou_rhs_noalloc": [_P, _P, _P, ctypes.c_double],
     "flou_fp64_peak": [_D],
 }
 

@@ -147,6 +147,15 @@ int32_t flou_step(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps
 /* get_max_dt(q, disc, eq, cfl) (src/FlouSpatial/MultielementDiscontinuous.jl:162-178). */
 int32_t flou_max_dt(flou_ctx* ctx, const double* Q, double cfl, double* dt, int32_t ptr_kind);
 
+/* The residual of flou_rhs without any device allocation: device pointers only, face
+ * fluxes kept in a fixed 8 MiB array inside the library (at most 1,048,576 values of
+ * nfaces x n^(d-1) x nvars), shared by all calls, so overlapping calls race.  For callers
+ * whose device memory belongs to another allocator (CUDA.jl's pool, PyTorch's caching
+ * allocator), where flou_rhs's lazy cudaMalloc of its face buffer could fail or is not
+ * allowed.  The first call on a device looks up the array's address; make it before any
+ * stream capture.  No counterpart in the reference. */
+int32_t flou_rhs_noalloc(flou_ctx* ctx, double* dQ, const double* Q, double t);
+
 /* Number of nodes (DOFs in Flou's sense, DofHandler.jl:53) and of variables. */
 int32_t flou_sizes(const flou_ctx* ctx, int64_t* ndofs, int32_t* nvars, int32_t* nelem, int32_t* nfaces);
 
