@@ -224,6 +224,99 @@ __device__ __forceinline__ void euler_face_flux(const double* ql, const double* 
     for (int k = 0; k < NV; ++k) F[k] = Fk[k] + sk * (Us[k] - qk[k]);
 }
 
+// Signed axes of a Cartesian face frame (n, t, b) for a master at local position `pos`: the
+// same frames as frame_of (PhysicalRegions.jl:541-696), whose rotations are signed
+// permutations; rotating with them is exact.
+struct FrameAxes { int ax[3]; bool neg[3]; };
+
+template <int DIM>
+__device__ __forceinline__ FrameAxes frame_axes(int pos) {
+    FrameAxes A = {{0, 0, 0}, {false, false, false}};
+    if (DIM == 1) { A.neg[0] = (pos == 0); return A; }
+    if (DIM == 2) {
+        switch (pos) {
+            case 0: A.ax[0] = 0; A.neg[0] = true; A.ax[1] = 1; A.neg[1] = true; break;
+            case 1: A.ax[0] = 0; A.ax[1] = 1; break;
+            case 2: A.ax[0] = 1; A.neg[0] = true; A.ax[1] = 0; break;
+            default: A.ax[0] = 1; A.ax[1] = 0; A.neg[1] = true; break;
+        }
+        return A;
+    }
+    switch (pos) {
+        case 0: A.ax[0] = 0; A.neg[0] = true; A.ax[1] = 1; A.neg[1] = true; A.ax[2] = 2; break;
+        case 1: A.ax[0] = 0; A.ax[1] = 1; A.ax[2] = 2; break;
+        case 2: A.ax[0] = 1; A.neg[0] = true; A.ax[1] = 2; A.neg[1] = true; A.ax[2] = 0; break;
+        case 3: A.ax[0] = 1; A.ax[1] = 2; A.ax[2] = 0; break;
+        case 4: A.ax[0] = 2; A.neg[0] = true; A.ax[1] = 0; A.neg[1] = true; A.ax[2] = 1; break;
+        default: A.ax[0] = 2; A.ax[1] = 0; A.ax[2] = 1; break;
+    }
+    return A;
+}
+
+__device__ __forceinline__ double flip(double x, bool neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+}
+
+// StdAverage / LxF(StdAverage) / HLL / HLLC in the face frame with one reciprocal of the
+// density per side (u = m·(1/ρ), p = (γ-1)(ρe - ½|m|²/ρ)) and one shared reciprocal for the
+// HLLC star state; same formulas as euler_face_flux up to rounding.
+template <int DIM>
+__device__ __forceinline__ void euler_face_flux_fast(const double* ql, const double* qr, int kind, double intensity,
+                                                     double g, double* F) {
+    constexpr int NV = DIM + 2;
+    double irl = 1.0 / ql[0], irr = 1.0 / qr[0];
+    double ul = ql[1] * irl, ur = qr[1] * irr;
+    double sl2 = ql[1] * ql[1], sr2 = qr[1] * qr[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) { sl2 = fma(ql[1 + k], ql[1 + k], sl2); sr2 = fma(qr[1 + k], qr[1 + k], sr2); }
+    double pl = (g - 1.0) * fma(-0.5 * sl2, irl, ql[DIM + 1]);
+    double pr = (g - 1.0) * fma(-0.5 * sr2, irr, qr[DIM + 1]);
+    if (kind == FLOU_NF_STD_AVERAGE || kind == FLOU_NF_LXF) {   // Euler.jl:99-165
+        F[0] = (ql[1] + qr[1]) * 0.5;
+        F[1] = (fma(ql[1], ul, pl) + fma(qr[1], ur, pr)) * 0.5;
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) F[1 + k] = fma(ql[1 + k], ul, qr[1 + k] * ur) * 0.5;
+        F[DIM + 1] = fma(ql[DIM + 1] + pl, ul, (qr[DIM + 1] + pr) * ur) * 0.5;
+        if (kind == FLOU_NF_LXF) {
+            double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+            double lam = fmax(fabs(ul) + al, fabs(ur) + ar) * (0.5 * intensity);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) F[k] = fma(lam, ql[k] - qr[k], F[k]);
+        }
+        return;
+    }
+    double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+    double sl = fmin(ul - al, ur - ar), sr = fmax(ul + al, ur + ar);
+    double Fl[NV], Fr[NV];
+    euler_normal_flux<DIM>(ql, ul, pl, Fl);
+    euler_normal_flux<DIM>(qr, ur, pr, Fr);
+    if (sl >= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fl[k]; return; }
+    if (sr <= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fr[k]; return; }
+    if (kind == FLOU_NF_HLL) {
+        double r = 1.0 / (sr - sl), slr = sl * sr;
+        for (int k = 0; k < NV; ++k) F[k] = (fma(sr, Fl[k], -sl * Fr[k]) + slr * (qr[k] - ql[k])) * r;
+        return;
+    }
+    double ml = ql[0] * (sl - ul), mr = qr[0] * (sr - ur);
+    double ss = fma(ul, ml, (pr - pl) - ur * mr) / (ml - mr);
+    bool left = ss >= 0.0;
+    const double* qk = left ? ql : qr;
+    const double* Fk = left ? Fl : Fr;
+    double sk = left ? sl : sr, mk = left ? ml : mr, irk = left ? irl : irr, uk = left ? ul : ur,
+           pk = left ? pl : pr;
+    double R = 1.0 / ((sk - ss) * mk);
+    double coef = mk * mk * R;          // ρ_K (S_K - u_K)/(S_K - S*)
+    double pm = pk * (sk - ss) * R;     // p_K / (ρ_K (S_K - u_K))
+    double Us[NV];
+    Us[0] = coef;
+    Us[1] = coef * ss;
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) Us[1 + k] = coef * (qk[1 + k] * irk);
+    Us[DIM + 1] = coef * fma(ss - uk, ss + pm, qk[DIM + 1] * irk);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) F[k] = fma(sk, Us[k] - qk[k], Fk[k]);
+}
+
 // ---------------------------------------------------------------------------------------
 // Face kernel: traces (project2faces!, Interfaces.jl:51-109), boundary ghost states
 // (applyBCs!, :25-49) and numerical fluxes times the surface Jacobian
@@ -263,16 +356,11 @@ __global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
         if (kind == FLOU_BC_INFLOW) {
             for (int k = 0; k < NV; ++k) qr[k] = P.bc_state[b][k];
         } else if (kind == FLOU_BC_SLIP && EQ == FLOU_EQ_EULER) {
-            // EulerSlipBC: rotate to the face frame, flip the normal momentum, rotate back.
-            double mn = ql[1] * fr.n[0], mt = ql[1] * fr.t[0], mb = ql[1] * fr.b[0];
-            if (DIM > 1) { mn = mn + ql[2] * fr.n[1]; mt = mt + ql[2] * fr.t[1]; mb = mb + ql[2] * fr.b[1]; }
-            if (DIM > 2) { mn = mn + ql[3] * fr.n[2]; mt = mt + ql[3] * fr.t[2]; mb = mb + ql[3] * fr.b[2]; }
-            mn = -mn;
+            // EulerSlipBC (Euler.jl:88-94): rotate to the face frame, flip the normal momentum,
+            // rotate back -- for a Cartesian frame, the momentum along the normal axis changes sign.
             for (int k = 0; k < NV; ++k) qr[k] = ql[k];
-            qr[1] = mn * fr.n[0] + mt * fr.t[0] + (DIM > 2 ? mb * fr.b[0] : 0.0);
-            if (DIM > 1) qr[2] = mn * fr.n[1] + mt * fr.t[1] + (DIM > 2 ? mb * fr.b[1] : 0.0);
-            if (DIM > 2) qr[3] = mn * fr.n[2] + mt * fr.t[2] + mb * fr.b[2];
-            if (DIM == 1) qr[1] = mn * fr.n[0];
+            int an = frame_axes<DIM>(s0 & 7).ax[0];
+            qr[1 + an] = -ql[1 + an];
         } else {
             for (int k = 0; k < NV; ++k) qr[k] = ql[k];   // outflow
         }
@@ -280,36 +368,24 @@ __global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
     double F[NV];
     double J = P.faceJ[f];
     if (EQ == FLOU_EQ_EULER) {
-        // rotate2face (Euler.jl:16-64)
+        // rotate2face / rotate2phys (Euler.jl:16-64) as signed permutations
+        FrameAxes A = frame_axes<DIM>(s0 & 7);
         double a[NV], b[NV];
         a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-        if (DIM == 1) { a[1] = ql[1] * fr.n[0]; b[1] = qr[1] * fr.n[0]; }
-        if (DIM == 2) {
-            a[1] = ql[1] * fr.n[0] + ql[2] * fr.n[1]; a[2] = ql[1] * fr.t[0] + ql[2] * fr.t[1];
-            b[1] = qr[1] * fr.n[0] + qr[2] * fr.n[1]; b[2] = qr[1] * fr.t[0] + qr[2] * fr.t[1];
-        }
-        if (DIM == 3) {
-            a[1] = ql[1] * fr.n[0] + ql[2] * fr.n[1] + ql[3] * fr.n[2];
-            a[2] = ql[1] * fr.t[0] + ql[2] * fr.t[1] + ql[3] * fr.t[2];
-            a[3] = ql[1] * fr.b[0] + ql[2] * fr.b[1] + ql[3] * fr.b[2];
-            b[1] = qr[1] * fr.n[0] + qr[2] * fr.n[1] + qr[3] * fr.n[2];
-            b[2] = qr[1] * fr.t[0] + qr[2] * fr.t[1] + qr[3] * fr.t[2];
-            b[3] = qr[1] * fr.b[0] + qr[2] * fr.b[1] + qr[3] * fr.b[2];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+            a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
+            b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
         }
         double Fr[NV];
-        euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, P.intensity, P.gamma, Fr);
-        // rotate2phys
-        F[0] = Fr[0]; F[DIM + 1] = Fr[DIM + 1];
-        if (DIM == 1) F[1] = Fr[1] * fr.n[0];
-        if (DIM == 2) {
-            F[1] = Fr[1] * fr.n[0] + Fr[2] * fr.t[0];
-            F[2] = Fr[1] * fr.n[1] + Fr[2] * fr.t[1];
-        }
-        if (DIM == 3) {
-            F[1] = Fr[1] * fr.n[0] + Fr[2] * fr.t[0] + Fr[3] * fr.b[0];
-            F[2] = Fr[1] * fr.n[1] + Fr[2] * fr.t[1] + Fr[3] * fr.b[1];
-            F[3] = Fr[1] * fr.n[2] + Fr[2] * fr.t[2] + Fr[3] * fr.b[2];
-        }
+        if (P.numflux == FLOU_NF_CHANDRASHEKAR || (P.numflux == FLOU_NF_LXF && P.lxf_avg == FLOU_NF_CHANDRASHEKAR))
+            euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, P.intensity, P.gamma, Fr);
+        else
+            euler_face_flux_fast<DIM>(a, b, P.numflux, P.intensity, P.gamma, Fr);
+        F[0] = Fr[0];
+        F[DIM + 1] = Fr[DIM + 1];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) F[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]);
     } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
         // LinearAdvection.jl:27-39
         double an = P.adv[0] * fr.n[0];
@@ -420,19 +496,26 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
 #pragma unroll
         for (int k = 0; k < NV; ++k) q[k] = P.Q[k * P.ndofs + g];
         double F[NV];
+        double v[DIM], p = 0.0;
+        if (EQ == FLOU_EQ_EULER) {   // primitives once per node (volumeflux, Euler.jl:54-114)
+            double ir = 1.0 / q[0], ke = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                v[k] = q[1 + k] * ir;
+                ke = fma(q[1 + k], v[k], ke);
+            }
+            p = (P.gamma - 1.0) * fma(-0.5, ke, q[DIM + 1]);
+            if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
+        }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
             double Ja = P.elem_Ja[e * DIM + d];
             if (EQ == FLOU_EQ_EULER) {
-                double rho = q[0];
-                double p = euler_pressure<DIM>(q, P.gamma);
-                if (d == 0 && !(rho > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
-                double vd = q[1 + d] / rho;
                 F[0] = q[1 + d];
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) F[1 + k] = q[1 + d] * (q[1 + k] / rho);
+                for (int k = 0; k < DIM; ++k) F[1 + k] = q[1 + d] * v[k];
                 F[1 + d] = F[1 + d] + p;
-                F[DIM + 1] = (q[DIM + 1] + p) * vd;
+                F[DIM + 1] = (q[DIM + 1] + p) * v[d];
             } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
                 F[0] = P.adv[d] * q[0];
             } else {
@@ -469,65 +552,74 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
 //   dQ_i -= sum_j D♯_ij F♯(i, j), F♯(i, i) = F̃_i, F♯(i, j) = twopointflux(Q_i, Q_j).
 // The two-point fluxes of a line are symmetric; each pair is evaluated once by one thread
 // and kept in shared memory (the reference fills both triangle entries the same way).
-// Per-node primitive quantities (velocities, pressure, β = ρ/2p and the logarithms of ρ
-// and β) are computed once per node instead of once per pair.
+// The residual is bound by the FP64 pipe, so every quantity that depends on one node only
+// is computed once per node (pre-halved where the pair formulas average it) and the pair
+// formulas share one reciprocal.
 // ---------------------------------------------------------------------------------------
-struct PairPrims {   // primitive arrays in shared memory, each of length NN
-    double *rho, *v[3], *p, *beta, *lrho, *lbeta, *vv, *e;
+// Shared per-node arrays (length NN each) of the split form, by two-point flux:
+//   Chandrashekar:  rh = ρ/2, vh_k = v_k/2, bh = β/2 = ρ/(4p), vq = |v|²/4
+//   Kennedy-Gruber: rh = ρ/2, vh_k = v_k/2, ph = p/2, eh = e/2 (e = ρe/ρ)
+//   StdAverage:     v_k, p, then the conserved variables
+//   scalar equations: u
+template <int DIM, int EQ, int TP>
+struct SplitLayout {
+    static constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
+    static constexpr int NARR = (EQ != FLOU_EQ_EULER) ? 1 : (TP == FLOU_TP_STD_AVERAGE ? DIM + 1 + NV : DIM + 3);
 };
 
 // Chandrashekar two-point flux (Euler.jl:474-536) along direction d without the metric
-// factor.  The logarithmic means use the per-node logarithms:
-//   series branch (u = ((a-b)/(a+b))² < 0.01): mean = (a+b)/(2F), F = 1+u/3+u²/5+u³/7
-//   log branch:                               mean = (a-b)/(ln a - ln b)
-// which is the reference's log(ξ)/(2f) form rewritten with ln ξ = ln a - ln b.
+// factor, with the logarithmic means of Utilities.jl:34-44 written in sums and differences:
+//   u = ((a-b)/(a+b))²;  series branch (u < 0.01): mean = (a+b)/(2F), F = 1+u/3+u²/5+u³/7,
+//   log branch: mean = (a-b)/ln(a/b).
+// One reciprocal 1/(hs_ρ·hs_β) serves both means and the pressure average; 1/F comes from
+// two Newton steps started at 1 - u/3 (relative error (4u²/45)^4 < 1e-20 for u < 0.01).
 template <int DIM>
-__device__ __forceinline__ void chandrashekar_pair(const PairPrims& S, int i, int l, int d, double g,
-                                                   double* F) {
-    double r1 = S.rho[i], r2 = S.rho[l];
-    double b1 = S.beta[i], b2 = S.beta[l];
-    double vavg[DIM];
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) vavg[k] = (S.v[k][i] + S.v[k][l]) * 0.5;
-    // ρ log-mean and its inverse
-    double sr = r1 + r2, dr = r1 - r2;
-    double rho_ln, inv_rho_ln;
-    if (dr * dr < 0.01 * (sr * sr)) {
-        double rs = 1.0 / sr;
-        double f = dr * rs;
-        double u = f * f;
-        double Fs = ((1.0 + u * (1.0 / 3.0)) + (u * u) * 0.2) + (u * u * u) * (1.0 / 7.0);
-        double iF = 1.0 / Fs;
-        rho_ln = 0.5 * sr * iF;
-        inv_rho_ln = 2.0 * Fs * rs;
+__device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S, int NN, int i, int l, int d,
+                                                   double c_beta, double* F) {
+    const double* rh = S;
+    const double* vh = S + NN;
+    const double* bh = S + (1 + DIM) * NN;
+    const double* vq = S + (2 + DIM) * NN;
+    double rh1 = rh[i], rh2 = rh[l], bh1 = bh[i], bh2 = bh[l];
+    double hsr = rh1 + rh2, dhr = rh1 - rh2;   // (ρ1+ρ2)/2, (ρ1-ρ2)/2
+    double hsb = bh1 + bh2, dhb = bh1 - bh2;
+    double R = 1.0 / (hsr * hsb);
+    double rs = hsb * R, rb = hsr * R;         // 2/(ρ1+ρ2), 2/(β1+β2)
+    double fr = dhr * rs, fb = dhb * rb;
+    double ur = fr * fr, ub = fb * fb;
+    double rho_ln, inv_rho_ln, inv_beta_ln;
+    if (ur < 0.01) {
+        double Fs = fma(ur, fma(ur, fma(ur, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        double y = fma(-1.0 / 3.0, ur, 1.0);
+        y = y * fma(-Fs, y, 2.0);
+        y = y * fma(-Fs, y, 2.0);
+        rho_ln = hsr * y;
+        inv_rho_ln = Fs * rs;
     } else {
-        double L = S.lrho[i] - S.lrho[l];
-        rho_ln = dr / L;
-        inv_rho_ln = L / dr;
+        double L = log(rh1 / rh2);
+        rho_ln = (2.0 * dhr) / L;
+        inv_rho_ln = L / (2.0 * dhr);
     }
-    // β log-mean (only its inverse is needed) and the pressure average
-    double sb = b1 + b2, db = b1 - b2;
-    double rb = 1.0 / sb;
-    double inv_beta_ln;
-    {
-        double f = db * rb;
-        double u = f * f;
-        if (u < 0.01) {
-            double Fs = ((1.0 + u * (1.0 / 3.0)) + (u * u) * 0.2) + (u * u * u) * (1.0 / 7.0);
-            inv_beta_ln = 2.0 * Fs * rb;
-        } else {
-            inv_beta_ln = (S.lbeta[i] - S.lbeta[l]) / db;
-        }
+    if (ub < 0.01) {
+        double Fs = fma(ub, fma(ub, fma(ub, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        inv_beta_ln = Fs * rb;
+    } else {
+        inv_beta_ln = log(bh1 / bh2) / (2.0 * dhb);
     }
-    double p = 0.5 * sr * rb;
+    double p = 0.5 * hsr * rb;                 // (ρ1+ρ2)/(2(β1+β2))
+    double va[DIM];
     double vv = 0.0;
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) vv = vv + vavg[k] * vavg[k];
-    double h = (inv_beta_ln * (0.5 / (g - 1.0)) - (S.vv[i] + S.vv[l]) * 0.25) + p * inv_rho_ln + vv;
-    double m = rho_ln * vavg[d];
+    for (int k = 0; k < DIM; ++k) {
+        va[k] = vh[k * NN + i] + vh[k * NN + l];
+        vv = fma(va[k], va[k], vv);
+    }
+    // h = 1/(2β(γ-1)) - (|v1|²+|v2|²)/4 + p/ρ + |v̄|²
+    double h = fma(inv_beta_ln, c_beta, -(vq[i] + vq[l])) + fma(p, inv_rho_ln, vv);
+    double m = rho_ln * va[d];
     F[0] = m;
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) F[1 + k] = m * vavg[k];
+    for (int k = 0; k < DIM; ++k) F[1 + k] = m * va[k];
     F[1 + d] = F[1 + d] + p;
     F[DIM + 1] = m * h;
 }
@@ -535,17 +627,15 @@ __device__ __forceinline__ void chandrashekar_pair(const PairPrims& S, int i, in
 template <int DIM, int N, int EQ, int TP, bool LGL>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
     using S = Shape<DIM, N>;
-    constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
+    using Lay = SplitLayout<DIM, EQ, TP>;
+    constexpr int NV = Lay::NV;
     constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = S::EPB * NFD * NPAIR;   // pairs per direction in the block
     constexpr bool EULER = (EQ == FLOU_EQ_EULER);
-    // primitive arrays: rho, v[DIM], p, beta, lrho, lbeta, vv, e (+ conserved copies for
-    // the StdAverage two-point flux)
-    constexpr int NPRIM = EULER ? (DIM + 7 + (TP == FLOU_TP_STD_AVERAGE ? NV : 0)) : 1;
     extern __shared__ double smem[];
     double* sops = smem;
-    double* sprim = sops + S::NOPS;
-    double* spair = sprim + NPRIM * NN;   // [NV][NPT]
+    double* sprim = sops + S::NOPS;                 // [Lay::NARR][NN]
+    double* spair = sprim + Lay::NARR * NN;         // [NV][NPT]
     uint8_t* stab = (uint8_t*)(spair + NV * NPT);   // pair table: a, b
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
@@ -554,56 +644,50 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
         for (int a = 0; a < N; ++a)
             for (int b = a + 1; b < N; ++b) { stab[2 * c] = (uint8_t)a; stab[2 * c + 1] = (uint8_t)b; ++c; }
     }
-    PairPrims pp;
-    if (EULER) {
-        pp.rho = sprim;
-        for (int k = 0; k < 3; ++k) pp.v[k] = sprim + (1 + (k < DIM ? k : 0)) * NN;
-        pp.p = sprim + (1 + DIM) * NN;
-        pp.beta = sprim + (2 + DIM) * NN;
-        pp.lrho = sprim + (3 + DIM) * NN;
-        pp.lbeta = sprim + (4 + DIM) * NN;
-        pp.vv = sprim + (5 + DIM) * NN;
-        pp.e = sprim + (6 + DIM) * NN;
-    } else {
-        pp.rho = sprim;
-    }
-    double* sq = sprim + (EULER ? (DIM + 7) : 0) * NN;   // conserved copies (StdAverage)
     const int e0 = blockIdx.x * S::EPB;
     const int el = tid / NPE, i = tid - el * NPE;
     const int e = e0 + el;
     const bool active = (tid < NN) && (e < P.nelem);
     const double g = P.gamma;
     double q[NV];
+    double v[EULER ? DIM : 1];
+    double p = 0.0;
     if (active) {
         int64_t gi = (int64_t)e * NPE + i;
 #pragma unroll
         for (int k = 0; k < NV; ++k) q[k] = P.Q[k * P.ndofs + gi];
         if (EULER) {
-            double rho = q[0];
-            double p = euler_pressure<DIM>(q, g);
-            if (!(rho > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
-            pp.rho[tid] = rho;
-            double vv = 0.0;
+            double ir = 1.0 / q[0];
+            double ke = 0.0, vv = 0.0;
 #pragma unroll
             for (int k = 0; k < DIM; ++k) {
-                double vk = q[1 + k] / rho;
-                pp.v[k][tid] = vk;
-                vv = (k == 0) ? vk * vk : vv + vk * vk;
+                v[k] = q[1 + k] * ir;
+                ke = fma(q[1 + k], v[k], ke);
+                vv = fma(v[k], v[k], vv);
             }
-            pp.p[tid] = p;
-            pp.vv[tid] = vv;
+            p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
+            if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
             if (TP == FLOU_TP_CHANDRASHEKAR) {
-                double beta = rho / (2.0 * p);
-                pp.beta[tid] = beta;
-                pp.lrho[tid] = log(rho);
-                pp.lbeta[tid] = log(beta);
-            }
-            if (TP == FLOU_TP_KENNEDY_GRUBER) pp.e[tid] = q[DIM + 1] / rho;
-            if (TP == FLOU_TP_STD_AVERAGE)
+                sprim[tid] = 0.5 * q[0];
 #pragma unroll
-                for (int k = 0; k < NV; ++k) sq[k * NN + tid] = q[k];
+                for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
+                sprim[(1 + DIM) * NN + tid] = (0.25 * q[0]) / p;
+                sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
+            } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
+                sprim[tid] = 0.5 * q[0];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
+                sprim[(1 + DIM) * NN + tid] = 0.5 * p;
+                sprim[(2 + DIM) * NN + tid] = 0.5 * (q[DIM + 1] * ir);
+            } else {
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) sprim[k * NN + tid] = v[k];
+                sprim[DIM * NN + tid] = p;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sprim[(DIM + 1 + k) * NN + tid] = q[k];
+            }
         } else {
-            pp.rho[tid] = q[0];
+            sprim[tid] = q[0];
         }
     }
     __syncthreads();
@@ -611,6 +695,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
 #pragma unroll
     for (int k = 0; k < NV; ++k) dq[k] = 0.0;
     const double* Dsh = sops + N * N;
+    const double c_beta = 0.5 / (g - 1.0);
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
         // ---- pair phase: every symmetric two-point flux of the block, once ----
@@ -625,21 +710,23 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
             double F[NV];
             if (EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
-                    chandrashekar_pair<DIM>(pp, ia, ib, dir, g, F);
-                } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
-                    double rho = (pp.rho[ia] + pp.rho[ib]) * 0.5;
-                    double vd = (pp.v[dir][ia] + pp.v[dir][ib]) * 0.5;
-                    double p = (pp.p[ia] + pp.p[ib]) * 0.5;
-                    double en = (pp.e[ia] + pp.e[ib]) * 0.5;
+                    chandrashekar_pair<DIM>(sprim, NN, ia, ib, dir, c_beta, F);
+                } else if (TP == FLOU_TP_KENNEDY_GRUBER) {   // Kennedy & Gruber (2008)
+                    const double* vh = sprim + NN;
+                    double rho = sprim[ia] + sprim[ib];
+                    double pm = sprim[(1 + DIM) * NN + ia] + sprim[(1 + DIM) * NN + ib];
+                    double en = sprim[(2 + DIM) * NN + ia] + sprim[(2 + DIM) * NN + ib];
+                    double vd = vh[dir * NN + ia] + vh[dir * NN + ib];
                     double m = rho * vd;
                     F[0] = m;
 #pragma unroll
-                    for (int k = 0; k < DIM; ++k) F[1 + k] = m * ((pp.v[k][ia] + pp.v[k][ib]) * 0.5);
-                    F[1 + dir] = F[1 + dir] + p;
-                    F[DIM + 1] = m * en + p * vd;
+                    for (int k = 0; k < DIM; ++k) F[1 + k] = m * (vh[k * NN + ia] + vh[k * NN + ib]);
+                    F[1 + dir] = F[1 + dir] + pm;
+                    F[DIM + 1] = fma(m, en, pm * vd);
                 } else {   // StdAverage two-point flux, Euler.jl:385-472
-                    double v1 = pp.v[dir][ia], v2 = pp.v[dir][ib];
-                    double p1 = pp.p[ia], p2 = pp.p[ib];
+                    const double* sq = sprim + (DIM + 1) * NN;
+                    double v1 = sprim[dir * NN + ia], v2 = sprim[dir * NN + ib];
+                    double p1 = sprim[DIM * NN + ia], p2 = sprim[DIM * NN + ib];
                     F[0] = (sq[(1 + dir) * NN + ia] + sq[(1 + dir) * NN + ib]) * 0.5;
 #pragma unroll
                     for (int k = 0; k < DIM; ++k) {
@@ -649,9 +736,9 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
                     F[DIM + 1] = ((sq[(DIM + 1) * NN + ia] + p1) * v1 + (sq[(DIM + 1) * NN + ib] + p2) * v2) * 0.5;
                 }
             } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
-                F[0] = P.adv[dir] * (pp.rho[ia] + pp.rho[ib]) * 0.5;
+                F[0] = P.adv[dir] * (sprim[ia] + sprim[ib]) * 0.5;
             } else {
-                F[0] = (pp.rho[ia] * pp.rho[ia] + pp.rho[ib] * pp.rho[ib]) * 0.25;
+                F[0] = (sprim[ia] * sprim[ia] + sprim[ib] * sprim[ib]) * 0.25;
             }
 #pragma unroll
             for (int k = 0; k < NV; ++k) spair[k * NPT + kp] = F[k];
@@ -663,12 +750,11 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
             tp_coords<DIM>(N, i, dir, pos, line);
             double Fd[NV];   // F♯(i, i): the physical flux along dir
             if (EULER) {
-                double vd = pp.v[dir][tid], p = pp.p[tid];
                 Fd[0] = q[1 + dir];
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) Fd[1 + k] = q[1 + dir] * pp.v[k][tid];
+                for (int k = 0; k < DIM; ++k) Fd[1 + k] = q[1 + dir] * v[k];
                 Fd[1 + dir] = Fd[1 + dir] + p;
-                Fd[DIM + 1] = (q[DIM + 1] + p) * vd;
+                Fd[DIM + 1] = (q[DIM + 1] + p) * v[dir];
             } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
                 Fd[0] = P.adv[dir] * q[0];
             } else {
@@ -683,17 +769,17 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
                 double a = Dsh[pos + j * N];
                 if (j == pos) {
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] = acc[k] + a * Fd[k];
+                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, Fd[k], acc[k]);
                 } else {
                     int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
                     int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] = acc[k] + a * spair[k * NPT + pidx];
+                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPT + pidx], acc[k]);
                 }
             }
             double Ja = P.elem_Ja[e * DIM + dir];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) dq[k] = dq[k] - Ja * acc[k];
+            for (int k = 0; k < NV; ++k) dq[k] = fma(-Ja, acc[k], dq[k]);
         }
         __syncthreads();
     }
@@ -706,9 +792,9 @@ constexpr size_t elem_smem_bytes() {
     using S = Shape<DIM, N>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
-    constexpr int NPRIM = (EQ == FLOU_EQ_EULER) ? (DIM + 7 + (TP == FLOU_TP_STD_AVERAGE ? NV : 0)) : 1;
+    constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;
     constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
-    return sizeof(double) * (S::NOPS + NPRIM * S::NN + NV * NPT) + 2 * (S::NPAIR + 1);
+    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT) + 2 * (S::NPAIR + 1);
 }
 
 // Launch one instantiation; the dynamic shared-memory opt-in is set once per kernel.
