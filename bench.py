@@ -256,14 +256,15 @@ def main():
         peaks = json.load(open(pp))
     hbm_peak = peaks.get("hbm_gbs")
     prof = load_profile_summary().get(dom, {})
-    traffic = prof.get("dram_bytes_per_dof_stage")
-    fp64_ops = prof.get("fp64_flops_per_dof_stage")
+    traffic = prof.get("dram_bytes_per_dof_stage")   # ncu, stage-2 launch of the same kernel
+    fp64_ops = prof.get("fp64_flops_per_dof_stage")   # executed FP64 flops (2 per FMA), ncu
     roofline = {
         "kernel": "elem_split_kernel<3,%d,Euler,Chandrashekar> (%s)" % (int(dom[-1]) + 1, dom),
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": (achieved / hbm_peak) if hbm_peak else None,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None,
         "traffic": (traffic * dk["ndofs"]) if traffic else None,
+        "traffic_source": "profiles/tgv3d_split_elem_kernel.json: ncu dram__bytes_read+write of the stage-2 launch",
         "algorithmic_bytes_per_launch": algo_bytes,
         "launch_ms": dk["elem_ms"],
         "fp64": {
