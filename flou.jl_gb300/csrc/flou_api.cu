@@ -11,46 +11,9 @@
 #include <string>
 #include <vector>
 
-#include "flou_internal.cuh"
+#include "flou_ctx.cuh"
 
 using namespace flou;
-
-struct flou_ctx {
-    flou_config cfg;
-    int nv = 0, n = 0, npe = 0, nfd = 0;
-    bool lgl = false;
-    std::string err;
-    cudaStream_t own_stream = nullptr, stream = nullptr;
-    bool have_ops = false, have_mesh = false, have_geom = false;
-    int nelem = 0, nfaces = 0;
-    int64_t ndofs = 0, nfdofs = 0;
-    std::vector<double> omega;              // quadrature weights (1D)
-    std::vector<double> h_invJ, h_J;        // per element
-    int nbcs = 0;
-    int bc_kind[MAXBC] = {0};
-    double bc_state[MAXBC][5] = {{0}};
-    std::vector<int8_t> h_face_bc;
-    // device buffers
-    double* d_ops = nullptr;        // Ds, D♯, l_l, l_r, dg_l, dg_r
-    int32_t* d_elem_face = nullptr;
-    int32_t* d_face_elem = nullptr;
-    int8_t* d_face_bc = nullptr;
-    double* d_faceJ = nullptr;
-    double* d_invJ = nullptr;
-    double* d_Ja = nullptr;
-    double* d_dx = nullptr;         // per-element CFL length (vol / n^d)^(1/d)
-    double* d_Fn = nullptr;         // face-flux scratch
-    double* d_U = nullptr;          // RK stage scratch
-    double* d_Qh = nullptr;         // staging for host-pointer calls
-    double* d_dQh = nullptr;
-    int32_t* d_status = nullptr;    // [flags, lowest element]
-    unsigned long long* d_dtmin = nullptr;
-    // graph cache for flou_step
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    double* g_Q = nullptr;
-    double g_dt = 0.0;
-};
 
 namespace {
 
@@ -258,6 +221,22 @@ __global__ void fma_probe_kernel(double* sink, int iters, double x) {
 }
 
 }  // namespace
+
+namespace flou {
+int ctx_fail(flou_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
+int ctx_cuda_fail(flou_ctx* c, cudaError_t e, const char* what) { return cuda_fail(c, e, what); }
+int ctx_prepare(flou_ctx* c) {
+    int r = ready(c);
+    if (r) return r;
+    return ensure(c, &c->d_U, (size_t)c->ndofs * c->nv, "stage buffer");
+}
+FaceParams ctx_face_params(const flou_ctx* c, const double* Q) { return face_params(c, Q); }
+ElemParams ctx_elem_params(const flou_ctx* c, const double* Q, const double* Q0, double* out, int mode, double dt,
+                           double a0, double a1) {
+    return elem_params(c, Q, Q0, out, mode, dt, a0, a1);
+}
+ElemLaunch ctx_elem_launch(const flou_ctx* c) { return elem_launch(c); }
+}  // namespace flou
 
 extern "C" {
 

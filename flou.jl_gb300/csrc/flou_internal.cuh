@@ -323,9 +323,8 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
 // (interface_fluxes!, :111-136).  One thread per face node.
 // ---------------------------------------------------------------------------------------
 template <int DIM, int EQ, bool LGL>
-__global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
+__device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
-    int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
     int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
     int n = P.n;
@@ -405,15 +404,20 @@ __global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
     for (int k = 0; k < NV; ++k) P.Fn[k * P.nfdofs + o] = F[k] * J;
 }
 
+template <int DIM, int EQ, bool LGL>
+__global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
+    face_node<DIM, EQ, LGL>(P, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------------------
 // Element kernels: volume term + surface lift + inverse mass + fused RK stage update.
 // One block owns EPB consecutive elements, one thread per element node.
 // ---------------------------------------------------------------------------------------
-template <int DIM, int N>
+template <int DIM, int N, int TB = 256>
 struct Shape {
     static constexpr int NPE = ipow(N, DIM);
     static constexpr int NFD = ipow(N, DIM - 1);
-    static constexpr int EPB = (NPE >= 256) ? 1 : (256 / NPE);
+    static constexpr int EPB = (NPE >= TB) ? 1 : (TB / NPE);
     static constexpr int NN = EPB * NPE;
     static constexpr int BLOCK = ((NN + 31) / 32) * 32;
     static constexpr int NPAIR = N * (N - 1) / 2;
@@ -444,18 +448,18 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
             if (pos == 0) {
                 double c = dgl[0] * sl;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * P.Fn[k * P.nfdofs + ol];
+                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + ol);
             }
             if (pos == N - 1) {
                 double c = dgr[N - 1] * sr;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * P.Fn[k * P.nfdofs + orr];
+                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + orr);
             }
         } else {
             double cl = dgl[pos] * sl, cr = dgr[pos] * sr;
 #pragma unroll
             for (int k = 0; k < NV; ++k)
-                dq[k] = dq[k] - (cl * P.Fn[k * P.nfdofs + ol] + cr * P.Fn[k * P.nfdofs + orr]);
+                dq[k] = dq[k] - (cl * __ldcg(P.Fn + k * P.nfdofs + ol) + cr * __ldcg(P.Fn + k * P.nfdofs + orr));
         }
     }
     double invJ = P.elem_invJ[e];
@@ -476,17 +480,15 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
 
 // Strong (== weak on LGL) divergence: dQ_line -= Ds * F̃_line per direction
 // (OpDivergence.jl:109-160), F̃ = Ja_dd F_d (contravariant with a diagonal metric).
-template <int DIM, int N, int EQ, bool LGL>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemParams P) {
-    using S = Shape<DIM, N>;
+template <int DIM, int N, int EQ, bool LGL, int TB = 256>
+__device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double* smem) {
+    using S = Shape<DIM, N, TB>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     constexpr int NPE = S::NPE, NN = S::NN;
-    extern __shared__ double smem[];
     double* sops = smem;
     double* sF = sops + S::NOPS;   // [DIM][NV][NN]
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
-    const int e0 = blockIdx.x * S::EPB;
     const int el = tid / NPE, i = tid - el * NPE;
     const int e = e0 + el;
     const bool active = (tid < NN) && (e < P.nelem);
@@ -526,25 +528,32 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
         }
     }
     __syncthreads();
-    if (!active) return;
-    const double* Ds = sops;
-    double dq[NV];
+    if (active) {
+        const double* Ds = sops;
+        double dq[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) dq[k] = 0.0;
+        for (int k = 0; k < NV; ++k) dq[k] = 0.0;
 #pragma unroll
-    for (int dir = 0; dir < DIM; ++dir) {
-        int pos, line;
-        tp_coords<DIM>(N, i, dir, pos, line);
-        const double* Fd = sF + dir * NV * NN + el * NPE;
+        for (int dir = 0; dir < DIM; ++dir) {
+            int pos, line;
+            tp_coords<DIM>(N, i, dir, pos, line);
+            const double* Fd = sF + dir * NV * NN + el * NPE;
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-            int j = tp_node<DIM>(N, dir, line, c);
-            double a = Ds[pos + c * N];
+            for (int c = 0; c < N; ++c) {
+                int j = tp_node<DIM>(N, dir, line, c);
+                double a = Ds[pos + c * N];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) dq[k] = dq[k] - a * Fd[k * NN + j];
+                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - a * Fd[k * NN + j];
+            }
         }
+        surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
     }
-    surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
+}
+
+template <int DIM, int N, int EQ, bool LGL>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemParams P) {
+    extern __shared__ double smem[];
+    strong_tile<DIM, N, EQ, LGL>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -624,15 +633,14 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     F[DIM + 1] = m * h;
 }
 
-template <int DIM, int N, int EQ, int TP, bool LGL>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
-    using S = Shape<DIM, N>;
+template <int DIM, int N, int EQ, int TP, bool LGL, int TB = 256>
+__device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* smem) {
+    using S = Shape<DIM, N, TB>;
     using Lay = SplitLayout<DIM, EQ, TP>;
     constexpr int NV = Lay::NV;
     constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = S::EPB * NFD * NPAIR;   // pairs per direction in the block
     constexpr bool EULER = (EQ == FLOU_EQ_EULER);
-    extern __shared__ double smem[];
     double* sops = smem;
     double* sprim = sops + S::NOPS;                 // [Lay::NARR][NN]
     double* spair = sprim + Lay::NARR * NN;         // [NV][NPT]
@@ -644,7 +652,6 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
         for (int a = 0; a < N; ++a)
             for (int b = a + 1; b < N; ++b) { stab[2 * c] = (uint8_t)a; stab[2 * c + 1] = (uint8_t)b; ++c; }
     }
-    const int e0 = blockIdx.x * S::EPB;
     const int el = tid / NPE, i = tid - el * NPE;
     const int e = e0 + el;
     const bool active = (tid < NN) && (e < P.nelem);
@@ -783,13 +790,18 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
         }
         __syncthreads();
     }
-    if (!active) return;
-    surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
+    if (active) surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
 }
 
-template <int DIM, int N, int EQ, int VOL, int TP>
+template <int DIM, int N, int EQ, int TP, bool LGL>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
+    extern __shared__ double smem[];
+    split_tile<DIM, N, EQ, TP, LGL>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
+}
+
+template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256>
 constexpr size_t elem_smem_bytes() {
-    using S = Shape<DIM, N>;
+    using S = Shape<DIM, N, TB>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
     constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;

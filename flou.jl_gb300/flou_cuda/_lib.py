@@ -87,6 +87,14 @@ PROTOTYPES = {
     "flou_time_kernels": [_P, _P, ctypes.c_int32, _D, _D],
     "flou_rhs_noalloc": [_P, _P, _P, ctypes.c_double],
     "flou_fp64_peak": [_D],
+    "flou_batch_create": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "flou_batch_destroy": [_P],
+    "flou_batch_last_error": [_P],
+    "flou_batch_set_stream": [_P, _P],
+    "flou_batch_set_states": [_P, ctypes.POINTER(_P), _D],
+    "flou_batch_step": [_P, ctypes.c_int32],
+    "flou_batch_autotune": [_P, _I32],
+    "flou_batch_test_skip_faces": [_P, ctypes.c_int32],
 }
 
 _lib = None
@@ -103,7 +111,7 @@ def load():
     for name, args in PROTOTYPES.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name == "flou_last_error" else ctypes.c_int32
+        fn.restype = ctypes.c_char_p if name.endswith("last_error") else ctypes.c_int32
     _lib = lib
     return lib
 

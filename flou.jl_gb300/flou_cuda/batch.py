@@ -1,0 +1,65 @@
+"""Batched mode: many independent discretizations advanced by one persistent launch per
+SSP-RK3 stage (flou_batch_* in include/flou_cuda.h).  No counterpart in Flou, which solves one
+problem at a time; each instance is an ordinary MultielementDisc."""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Batch:
+    """Batch(discs, states, dts): `states` are CUDA tensors (nvars, ndofs), advanced in place."""
+
+    def __init__(self, discs, states, dts):
+        lib = L.load()
+        self._lib = lib
+        self.discs = list(discs)
+        self.states = list(states)
+        n = len(self.discs)
+        ctxs = (ctypes.c_void_p * n)(*[d.ctx.h.value for d in self.discs])
+        h = ctypes.c_void_p()
+        st = lib.flou_batch_create(n, ctxs, ctypes.byref(h))
+        self.h = h
+        self._check(st)
+        for d, q in zip(self.discs, self.states):
+            if not getattr(q, "is_cuda", False) or q.numel() != d.ndofs * d.nvariables:
+                raise ValueError("batch states must be CUDA tensors of each instance's size")
+        self.set_states(self.states, dts)
+
+    def _check(self, st):
+        if st == L.FLOU_OK:
+            return
+        msg = ""
+        if self.h is not None and self.h.value:
+            raw = self._lib.flou_batch_last_error(self.h)
+            msg = raw.decode() if raw else ""
+        cls = L.DomainError if st == L.FLOU_ERR_NONPHYSICAL else L.FlouError
+        raise cls(st, msg)
+
+    def set_states(self, states, dts):
+        self.states = list(states)
+        n = len(self.states)
+        ptrs = (ctypes.c_void_p * n)(*[q.data_ptr() for q in self.states])
+        self._dts = np.ascontiguousarray(dts, dtype=np.float64)
+        self._check(self._lib.flou_batch_set_states(self.h, ptrs, L.dptr(self._dts)))
+
+    def set_stream(self, stream_ptr):
+        self._check(self._lib.flou_batch_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def step(self, nsteps=1):
+        self._check(self._lib.flou_batch_step(self.h, int(nsteps)))
+
+    def autotune(self):
+        out = (ctypes.c_int32 * 3)()
+        self._check(self._lib.flou_batch_autotune(self.h, out))
+        return {"threads_per_block": out[0], "blocks_per_sm": out[1], "order": "by_order_desc" if out[2] else "by_instance"}
+
+    def test_skip_faces(self, inst):
+        self._check(self._lib.flou_batch_test_skip_faces(self.h, int(inst)))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            self._lib.flou_batch_destroy(h)
+            self.h = None

@@ -173,6 +173,30 @@ int32_t flou_time_kernels(flou_ctx* ctx, const double* Q, int32_t nrep, double* 
  * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
 int32_t flou_fp64_peak(double* gflops);
 
+/* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
+ * Many independent discretizations with uneven element counts and orders advance together:
+ * one persistent launch per SSP-RK3 stage serves every instance from one work queue of face
+ * items and element tiles, and the three stages of a step replay as one CUDA graph.  A batch is
+ * built from contexts whose set-up is complete; they must outlive the batch and share the
+ * dimension, equation and volume operator (2D Euler strong form, or 3D Euler split form with
+ * the Chandrashekar flux).  States are device pointers, one per instance. */
+typedef struct flou_batch flou_batch;
+int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out);
+int32_t flou_batch_destroy(flou_batch* b);
+const char* flou_batch_last_error(const flou_batch* b);
+int32_t flou_batch_set_stream(flou_batch* b, void* stream);
+/* Q[k]: device state of instance k (advanced in place); dt[k]: its fixed time step. */
+int32_t flou_batch_set_states(flou_batch* b, double* const* Q, const double* dt);
+/* nsteps SSP-RK3 steps of every instance.  FLOU_ERR_TIMEOUT if a bounded device-side wait ran
+ * out (the results of that call are then invalid; the batch stays usable). */
+int32_t flou_batch_step(flou_batch* b, int32_t nsteps);
+/* Autotuner: times the first stage for every (threads per block, resident blocks per SM,
+ * element-item order) candidate and keeps the fastest; out = {threads, blocks/SM, order}. */
+int32_t flou_batch_autotune(flou_batch* b, int32_t* out);
+/* Fault-injection hook for tests: instance `inst`'s face items never report completion, so its
+ * element tiles run out of their bounded wait; -1 restores normal operation. */
+int32_t flou_batch_test_skip_faces(flou_batch* b, int32_t inst);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,120 @@
+"""Batched mode: one persistent launch per SSP-RK3 stage over many uneven instances.
+
+The batched result must equal, bit for bit, each instance stepped on its own with the plain
+kernels (the same tile code runs in both), agree with the oracle, survive the autotuner's
+re-tiling, and report a bounded-wait timeout as FLOU_ERR_TIMEOUT without hanging.
+"""
+import numpy as np
+import pytest
+
+import flou_cuda as F
+from flou_cuda import _lib
+from cases import build, oracle_for, rel_linf, smooth_euler_state
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _instances_2d(seed=0, count=8):
+    rng = np.random.default_rng(seed)
+    eq = F.EulerEquation(2, 1.4)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(3, 9))          # p = 2..7
+        ne = tuple(int(x) for x in rng.integers(2, 6, size=2))
+        walls = bool(k % 2)
+        if walls:
+            bcs = {str(b): F.EulerSlipBC() for b in range(1, 5)}
+            disc = build(2, n, ne, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), periodic=(), bcs=bcs)
+        else:
+            disc = build(2, n, ne, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+        Q = smooth_euler_state(disc, seed=seed * 100 + k)
+        dt = 0.3 * disc.ctx.max_dt(Q, 1.0)
+        out.append((disc, Q, dt))
+    return out
+
+
+def _device(Q):
+    return torch.from_numpy(np.ascontiguousarray(Q.T)).cuda()
+
+
+def _serial(insts, nsteps):
+    res = []
+    for disc, Q, dt in insts:
+        q = _device(Q)
+        disc.ctx.step(q, dt, nsteps)
+        res.append(q)
+    return res
+
+
+def test_batch_2d_matches_serial_bitwise():
+    insts = _instances_2d(seed=1)
+    ref = _serial(insts, 3)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.step(3)
+    for q, r in zip(states, ref):
+        assert torch.equal(q, r)
+
+
+def test_batch_autotune_keeps_results():
+    insts = _instances_2d(seed=2, count=6)
+    ref = _serial(insts, 2)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    choice = b.autotune()
+    assert choice["threads_per_block"] in (128, 256) and choice["blocks_per_sm"] >= 1
+    b.step(2)
+    for q, r in zip(states, ref):
+        assert torch.equal(q, r)
+
+
+def test_batch_instance_against_oracle():
+    insts = _instances_2d(seed=3, count=4)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.step(4)
+    for (disc, Q, dt), q in zip(insts, states):
+        ref = oracle_for(disc).ssprk3(Q, dt, 4)
+        assert rel_linf(q.cpu().numpy().T, ref) <= 1e-10
+
+
+def test_batch_3d_split_matches_serial():
+    eq = F.EulerEquation(3, 1.4)
+    insts = []
+    for k, (n, ne) in enumerate(((4, (2, 3, 2)), (5, (2, 2, 2)), (6, (1, 2, 2)), (4, (3, 3, 3)))):
+        disc = build(3, n, ne, eq, F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()))
+        Q = smooth_euler_state(disc, seed=40 + k)
+        insts.append((disc, Q, 0.3 * disc.ctx.max_dt(Q, 1.0)))
+    ref = _serial(insts, 2)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.step(2)
+    for q, r in zip(states, ref):
+        assert torch.equal(q, r)
+
+
+def test_batch_wait_timeout_is_reported_and_recoverable():
+    insts = _instances_2d(seed=4, count=3)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.test_skip_faces(1)   # instance 1's face items never report: its tiles' waits run out
+    with pytest.raises(F.FlouError) as ei:
+        b.step(1)
+    assert ei.value.status == _lib.FLOU_ERR_TIMEOUT
+    b.test_skip_faces(-1)
+    fresh = [_device(Q) for _, Q, _ in insts]
+    b.set_states(fresh, [dt for _, _, dt in insts])
+    b.step(1)
+    ref = _serial(insts, 1)
+    for q, r in zip(fresh, ref):
+        assert torch.equal(q, r)
+
+
+def test_batch_rejects_mixed_operators():
+    eq = F.EulerEquation(2, 1.4)
+    a = build(2, 4, (2, 2), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    c = build(2, 4, (2, 2), eq, F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()))
+    qa, qc = _device(smooth_euler_state(a)), _device(smooth_euler_state(c))
+    with pytest.raises(F.FlouError):
+        F.Batch([a, c], [qa, qc], [1e-3, 1e-3])
