@@ -48,3 +48,18 @@ def taylor_green(eq, coords, mach=0.1, rho0=1.0):
     p = p0 + (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0) / 16.0
     rho = np.full_like(x, rho0)
     return eq.vars_prim2cons(np.stack([rho, u, v, w, p], axis=1))
+
+
+def vortex_bump(eq, coords, center, beta, amp, uinf=(1.0, 1.0), period=None, bump_center=(0.0, 0.0), sigma=1.0):
+    """Isentropic vortex of strength `beta` plus a Gaussian density perturbation of amplitude
+    `amp` (pressure unchanged), the initial state of the batched configuration.  Walled boxes
+    use uinf = (0, 0)."""
+    Q = isentropic_vortex(eq, coords, center, beta=beta, uinf=uinf, period=period)
+    P = eq.vars_cons2prim(Q)
+    dx = coords[:, 0] - bump_center[0]
+    dy = coords[:, 1] - bump_center[1]
+    if period is not None:
+        dx = dx - period[0] * np.round(dx / period[0])
+        dy = dy - period[1] * np.round(dy / period[1])
+    P[:, 0] = P[:, 0] + amp * np.exp(-(dx * dx + dy * dy) / (2 * sigma * sigma))
+    return eq.vars_prim2cons(P)

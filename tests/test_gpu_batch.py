@@ -16,8 +16,12 @@ torch = pytest.importorskip("torch")
 
 
 def _instances_2d(seed=0, count=8):
+    """Small instances of the batched configuration: periodic or slip-walled [-5,5]² boxes,
+    orders p = 2..7, isentropic vortex + Gaussian density bump."""
     rng = np.random.default_rng(seed)
     eq = F.EulerEquation(2, 1.4)
+    box = ((-5.0, -5.0), (5.0, 5.0))
+    op = lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
     out = []
     for k in range(count):
         n = int(rng.integers(3, 9))          # p = 2..7
@@ -25,10 +29,12 @@ def _instances_2d(seed=0, count=8):
         walls = bool(k % 2)
         if walls:
             bcs = {str(b): F.EulerSlipBC() for b in range(1, 5)}
-            disc = build(2, n, ne, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), periodic=(), bcs=bcs)
+            disc = build(2, n, ne, eq, op(), periodic=(), bcs=bcs, box=box)
         else:
-            disc = build(2, n, ne, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
-        Q = smooth_euler_state(disc, seed=seed * 100 + k)
+            disc = build(2, n, ne, eq, op(), box=box)
+        Q = np.asfortranarray(F.initial.vortex_bump(
+            eq, disc.coords, rng.uniform(-1, 1, 2), rng.uniform(1, 6), rng.uniform(0, 0.1),
+            uinf=(0.0, 0.0) if walls else (1.0, 1.0), period=None if walls else (10.0, 10.0)))
         dt = 0.3 * disc.ctx.max_dt(Q, 1.0)
         out.append((disc, Q, dt))
     return out
