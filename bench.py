@@ -150,6 +150,80 @@ def run_reference(args):
     return 0
 
 
+def make_batched(count=256, seed=2026, nmin=8, nmax=64):
+    """The batched configuration: `count` independent 2D Euler instances on [-5,5]², n×n
+    elements with n ~ U{nmin..nmax}, p ~ U{2..7}, periodic or slip walls (50/50), isentropic
+    vortex of strength U(1,6) plus a Gaussian density bump of amplitude U(0,0.1), Rusanov flux,
+    strong form, SSP-RK3 with a fixed per-instance dt = get_max_dt(U0, cfl=0.5)."""
+    import flou_cuda as F
+    rng = np.random.default_rng(seed)
+    eq = F.EulerEquation(2, 1.4)
+    out = []
+    for k in range(count):
+        ne = int(rng.integers(nmin, nmax + 1))
+        n = int(rng.integers(3, 9))
+        walls = bool(rng.integers(0, 2))
+        mesh = F.CartesianMesh((-5.0, -5.0), (5.0, 5.0), (ne, ne))
+        if walls:
+            bcs = {str(b): F.EulerSlipBC() for b in range(1, 5)}
+        else:
+            F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"))
+            bcs = {}
+        b = F.LagrangeBasis("GLL", n)
+        std = F.StdQuad(b, F.DGSEMrec(b), eq.nvariables)
+        disc = F.MultielementDisc(mesh, std, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), bcs)
+        Q0 = F.initial.vortex_bump(eq, disc.coords, rng.uniform(-2, 2, 2), rng.uniform(1, 6), rng.uniform(0, 0.1),
+                                   uinf=(0.0, 0.0) if walls else (1.0, 1.0), period=None if walls else (10.0, 10.0))
+        out.append((disc, np.asfortranarray(Q0)))
+    return out
+
+
+def bench_batched(steps, warmup, count=256):
+    """Batched (one persistent launch per stage for all instances) against the same instances
+    stepped one by one with the plain kernels (one flou_step call per instance)."""
+    import torch
+    import flou_cuda as F
+    insts = make_batched(count)
+    stream = torch.cuda.current_stream()
+    discs = [d for d, _ in insts]
+    Qs = [torch.from_numpy(np.ascontiguousarray(Q.T)).cuda() for _, Q in insts]
+    dts = [0.5 * d.ctx.max_dt(q, 1.0) for d, q in zip(discs, Qs)]
+    ndofs = sum(d.ndofs for d in discs)
+    batch = F.Batch(discs, Qs, dts)
+    batch.set_stream(stream.cuda_stream)
+    choice = batch.autotune()
+    for _ in range(warmup):
+        batch.step(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    batch.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    # one by one: each instance advanced `steps` steps with its own graph, then the next
+    for d in discs:
+        d.ctx.set_stream(stream.cuda_stream)
+    for d, q, dt in zip(discs, Qs, dts):
+        d.ctx.step(q, dt, warmup)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for d, q, dt in zip(discs, Qs, dts):
+        d.ctx.step(q, dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_s = e0.elapsed_time(e1)
+    for d in discs:
+        d.ctx.set_stream(0)
+    vb = ndofs * 3 * steps / (ms_b * 1e-3)
+    vs = ndofs * 3 * steps / (ms_s * 1e-3)
+    return {"value": vb, "unit": UNIT, "serial_value": vs, "speedup_vs_serial": vb / vs, "instances": count,
+            "ndofs": ndofs, "ms_per_step": ms_b / steps, "serial_ms_per_step": ms_s / steps, "autotune": choice,
+            "gpu_launches_per_step": 3, "serial_gpu_launches_per_step": 6 * count,
+            "workload": "256 x 2D Euler, n~U{8..64}^2 elements, p~U{2..7}, periodic/slip walls, vortex+bump, "
+                        "Rusanov, strong form, SSP-RK3"}
+
+
 def run_profile(which):
     """Two SSP-RK3 steps of one mesh on the device (the case the ncu captures use)."""
     import torch
@@ -170,6 +244,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--profile", choices=["A", "B"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3) or B (16^3 p=7) only")
     args = ap.parse_args()
@@ -299,6 +374,16 @@ def main():
     e2e = {"value": world * ndofs * 3 * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes}
 
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched(steps, warmup)
+        if dist is not None:
+            t = torch.tensor([batched["ms_per_step"], batched["serial_ms_per_step"]], device="cuda",
+                             dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            batched["value"] = world * batched["ndofs"] * 3 / (float(t[0]) * 1e-3)
+            batched["serial_value"] = world * batched["ndofs"] * 3 / (float(t[1]) * 1e-3)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -314,7 +399,7 @@ def main():
             "config": {"workload": "tgv3d_M0.1_split_chandrashekar_hllc_ssprk3: 32^3 p=3 + 16^3 p=7",
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
             "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
