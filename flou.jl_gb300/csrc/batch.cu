@@ -36,14 +36,22 @@ struct BatchArgs {
     int32_t skip_done_inst;      // fault-injection hook: this instance never reports its faces (-1: none)
 };
 
+// One call per order, not inlined: each order's tile gets its own register allocation instead
+// of the union of all orders (which would limit the persistent kernel to one block per SM).
 template <int DIM, int N, int EQ, int VOL, int TP, int TB>
-__device__ __forceinline__ void batch_tile_n(const ElemParams& P, int lgl, int e0, double* smem) {
+__device__ __noinline__ void batch_tile_n(const ElemParams& P, int lgl, int e0, double* smem) {
     if (VOL == FLOU_OP_STRONG) {
         if (lgl) strong_tile<DIM, N, EQ, true, TB>(P, e0, smem);
         else strong_tile<DIM, N, EQ, false, TB>(P, e0, smem);
     } else {
         split_tile<DIM, N, EQ, TP, true, TB>(P, e0, smem);
     }
+}
+
+template <int DIM, int EQ>
+__device__ __noinline__ void batch_face(const FaceParams& P, int64_t gid, int lgl) {
+    if (lgl) face_node<DIM, EQ, true>(P, gid);
+    else face_node<DIM, EQ, false>(P, gid);
 }
 
 template <int DIM, int EQ, int VOL, int TP, int TB>
@@ -60,7 +68,7 @@ __device__ __forceinline__ void batch_tile(const ElemParams& P, int n, int lgl, 
 }
 
 template <int DIM, int EQ, int VOL, int TP, int TB>
-__global__ void __launch_bounds__(TB) batch_stage_kernel(BatchArgs A) {
+__global__ void __launch_bounds__(TB, (TB >= 512 ? 1 : 1024 / TB)) batch_stage_kernel(BatchArgs A) {
     extern __shared__ double smem[];
     __shared__ int s_item;
     int32_t* done = A.counter + 2;
@@ -75,8 +83,7 @@ __global__ void __launch_bounds__(TB) batch_stage_kernel(BatchArgs A) {
         if ((w.x >> 30) == 0) {
             const FaceParams& fp = A.fp[inst];
             const int64_t gid = (int64_t)w.y + threadIdx.x;
-            if (A.inst_lgl[inst]) face_node<DIM, EQ, true>(fp, gid);
-            else face_node<DIM, EQ, false>(fp, gid);
+            batch_face<DIM, EQ>(fp, gid, A.inst_lgl[inst]);
             __threadfence();   // this thread's face fluxes are visible device-wide ...
             __syncthreads();   // ... for every thread of the block before the count goes up
             if (threadIdx.x == 0 && inst != A.skip_done_inst) atomicAdd(done + inst, 1);
