@@ -227,6 +227,17 @@ def bench_batched(steps, warmup, count=256):
 def run_profile(which):
     """Two SSP-RK3 steps of one mesh on the device (the case the ncu captures use)."""
     import torch
+    if which == "C":
+        import flou_cuda as F
+        insts = make_batched(256)
+        Qs = [torch.from_numpy(np.ascontiguousarray(Q.T)).cuda() for _, Q in insts]
+        dts = [0.3 * d.ctx.max_dt(q, 1.0) for (d, _), q in zip(insts, Qs)]
+        batch = F.Batch([d for d, _ in insts], Qs, dts)
+        batch.step(2)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "batched 256 x 2D Euler", "ndofs": sum(d.ndofs for d, _ in insts),
+                          "steps": 2}))
+        return 0
     nel, n = (32, 4) if which == "A" else (16, 8)
     disc, Q0 = make_tgv(nel, n)
     Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
@@ -245,8 +256,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--profile", choices=["A", "B"], default=None,
-                    help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3) or B (16^3 p=7) only")
+    ap.add_argument("--profile", choices=["A", "B", "C"], default=None,
+                    help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
+                         "configuration C (256 instances, one persistent launch per stage, default tiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
