@@ -1,0 +1,700 @@
+// adjoint.cu -- discrete adjoint (vector-Jacobian products) of the residual and of the
+// SSP-RK3 step for the Euler equations with the strong-form volume term and the LxF
+// (Rusanov, StdAverage) interface flux on LGL nodes, and the checkpointed reverse sweep of
+// a terminal functional.
+//
+// Residual (per element, node i):  dQ_i = (1/J) [ -Σ_d Ja_d Σ_j Ds(i,j) F_d(Q_j) - Σ_faces ∂g·(±Fn) ]
+// (Hyperbolic.jl:31-69 with OpDivergence.jl:42-160, Interfaces.jl:111-136).  Its transpose,
+// applied to a cotangent λ with w = λ/J:
+//   volume:   Q̄_j -= Ja_d (∂F_d/∂Q)(Q_j)ᵀ Σ_i Ds(i,j) w_i           (transposed line contraction)
+//   surface:  F̄(face node) = -∂g_1 w_1 + ∂g_2 w_2  (end nodes of side 1 / side 2)
+//             then the face flux VJP scatters to the two traces and to the dissipation scale.
+// SSP-RK3 step transpose (U1 = U0 + dt L0; U2 = 3/4 U0 + 1/4 (U1 + dt L1); U3 = 1/3 U0 + 2/3 (U2 + dt L2)):
+//   (a) Ū2 = 2/3 Ū3 + VJP(U2; 2/3 dt Ū3),  B = 1/3 Ū3
+//   (b) Ū1 = 1/4 Ū2 + VJP(U1; 1/4 dt Ū2),  B += 3/4 Ū2
+//   (c) Ū0 = Ū1 + B + VJP(U0; dt Ū1)
+// Non-smooth points follow Julia's Base (what ForwardDiff differentiates on the reference's
+// CPU path): max(a, b) takes b unless b < a; d|u|/du = -1 if u has its sign bit set, else +1.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "flou_ctx.cuh"
+
+namespace flou {
+
+struct AdjFaceParams {
+    const double* U;        // state the residual is linearised at
+    const double* Ain;      // adjoint input; λ = s_lam * Ain
+    double s_lam;
+    double* QbL;            // trace cotangent, side 1 [nv][nfdofs]
+    double* QbR;            // trace cotangent, side 2 [nv][nfdofs]
+    double* Ibar;           // cotangent of the face intensity [nfdofs]
+    const int32_t* face_elem;
+    const double* faceJ;
+    const int8_t* face_bc;
+    const double* invJ;
+    const double* ops;      // to read ∂g_l[0], ∂g_r[n-1]
+    const double* elem_c;
+    double intensity, gamma;
+    int64_t ndofs, nfdofs;
+    int32_t nfaces, n, npe, nfd;
+    int32_t bc_kind[MAXBC];
+};
+
+struct AdjElemParams {
+    const double* U;
+    const double* Ain;
+    double* Aout;           // alpha Ain + beta B + VJP
+    double* B;              // accumulator: B = gamma_B B + delta_B Ain (when writeB)
+    const double* QbL;
+    const double* QbR;
+    const double* Ibar;
+    double* cbar;           // per element, accumulated (nullable)
+    const int32_t* elem_face;
+    const int32_t* face_elem;
+    const double* invJ;
+    const double* Ja;
+    const double* ops;
+    int64_t ndofs, nfdofs;
+    int32_t nelem;
+    double s_lam, alpha, beta, gamma_B, delta_B;
+    int32_t readB, writeB;
+    double gamma;
+};
+
+// q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
+//   P̄ = ḡ_md + ḡ_E v_d,  s = Σ_k ḡ_mk v_k
+//   q̄_ρ  += -v_d (s + ḡ_E H) + (γ-1) |v|²/2 P̄
+//   q̄_mk += v_d ḡ_mk - (γ-1) v_k P̄ + [k = d] (ḡ_ρ + s + ḡ_E H)
+//   q̄_E  += ḡ_E + (γ-1) P̄
+template <int DIM>
+__device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv, double H, double g1,
+                                               const double* gb, double scale, double* qb) {
+    double Pb = gb[1 + d] + gb[DIM + 1] * v[d];
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) s = fma(gb[1 + k], v[k], s);
+    double t = s + gb[DIM + 1] * H;
+    qb[0] += scale * (fma(0.5 * g1 * vv, Pb, -v[d] * t));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        double r = fma(v[d], gb[1 + k], -g1 * v[k] * Pb);
+        if (k == d) r += gb[0] + t;
+        qb[1 + k] += scale * r;
+    }
+    qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1]);
+}
+
+struct Prim {
+    double rho, v[3], vv, p, H, a;
+};
+
+template <int DIM>
+__device__ __forceinline__ Prim prim_of(const double* q, double g) {
+    Prim P;
+    P.rho = q[0];
+    double ir = 1.0 / q[0], ke = 0.0, vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        P.v[k] = q[1 + k] * ir;
+        ke = fma(q[1 + k], P.v[k], ke);
+        vv = fma(P.v[k], P.v[k], vv);
+    }
+    P.vv = vv;
+    P.p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
+    P.H = (q[DIM + 1] + P.p) * ir;
+    P.a = sqrt(g * P.p * ir);
+    return P;
+}
+
+// q̄ += κ ∇λ, λ = |u_n| + a (face frame, normal momentum first).
+template <int DIM>
+__device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa, double* qb) {
+    double sg = signbit(P.v[0]) ? -1.0 : 1.0;
+    double ir = 1.0 / P.rho;
+    double ca = g * (g - 1.0) / (2.0 * P.a * P.rho);   // ∂a/∂p · ∂p/∂E
+    qb[0] += kappa * (-sg * P.v[0] * ir + ca * 0.5 * P.vv - P.a * 0.5 * ir);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) qb[1 + k] += kappa * ((k == 0 ? sg * ir : 0.0) - ca * P.v[k]);
+    qb[DIM + 1] += kappa * ca;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
+    constexpr int NV = DIM + 2;
+    int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)P.nfaces * P.nfd) return;
+    int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
+    int n = P.n;
+    int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
+    const double* dgl = P.ops + 2 * n * n + 2 * n;
+    const double* dgr = dgl + n;
+    auto endnode = [&](int32_t s, int64_t* g, double* dg) {
+        int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
+        *g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+        *dg = right ? dgr[n - 1] : dgl[0];
+    };
+    int64_t g1i, g2i = 0;
+    double dg1, dg2 = 0.0;
+    endnode(s0, &g1i, &dg1);
+    double qL[NV], qR[NV], Fb[NV];
+    double w1 = P.invJ[s0 >> 3] * P.s_lam;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        qL[k] = P.U[k * P.ndofs + g1i];
+        Fb[k] = -dg1 * (w1 * P.Ain[k * P.ndofs + g1i]);
+    }
+    if (s1 >= 0) {
+        endnode(s1, &g2i, &dg2);
+        double w2 = P.invJ[s1 >> 3] * P.s_lam;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qR[k] = P.U[k * P.ndofs + g2i];
+            Fb[k] = fma(dg2, w2 * P.Ain[k * P.ndofs + g2i], Fb[k]);
+        }
+    }
+    FrameAxes A = frame_axes<DIM>(s0 & 7);
+    double J = P.faceJ[f];
+    // face frame: a = R qL, b = R qR (or the boundary state), F̄ = J R F̄_phys
+    double a[NV], b[NV], fb[NV];
+    a[0] = qL[0];
+    a[DIM + 1] = qL[DIM + 1];
+    fb[0] = J * Fb[0];
+    fb[DIM + 1] = J * Fb[DIM + 1];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        a[1 + r] = flip(qL[1 + A.ax[r]], A.neg[r]);
+        fb[1 + r] = J * flip(Fb[1 + A.ax[r]], A.neg[r]);
+    }
+    int bck = 0;
+    if (s1 >= 0) {
+        b[0] = qR[0];
+        b[DIM + 1] = qR[DIM + 1];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) b[1 + r] = flip(qR[1 + A.ax[r]], A.neg[r]);
+    } else {
+        bck = P.bc_kind[P.face_bc[f]];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) b[k] = a[k];   // outflow; slip flips the normal momentum
+        if (bck == FLOU_BC_SLIP) b[1] = -a[1];
+    }
+    double inten = P.intensity;
+    if (P.elem_c) {
+        int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
+        inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
+    }
+    const double g = P.gamma, g1 = g - 1.0;
+    Prim pa = prim_of<DIM>(a, g);
+    const double* bb = b;
+    Prim pb = prim_of<DIM>(bb, g);
+    double ll = fabs(pa.v[0]) + pa.a, lr = fabs(pb.v[0]) + pb.a;
+    bool left = lr < ll;   // Base.max(ll, lr)
+    double lam = left ? ll : lr;
+    double dot = 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
+    double Ib = 0.5 * lam * dot;
+    double ab[NV], bbar[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        ab[k] = 0.5 * inten * lam * fb[k];
+        bbar[k] = -ab[k];
+    }
+    euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
+    euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
+    double kappa = 0.5 * inten * dot;
+    if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
+    else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    if (s1 < 0) {
+        if (bck == FLOU_BC_OUTFLOW) {
+            for (int k = 0; k < NV; ++k) ab[k] += bbar[k];
+        } else if (bck == FLOU_BC_SLIP) {
+            for (int k = 0; k < NV; ++k) ab[k] += (k == 1) ? -bbar[k] : bbar[k];
+        }
+    }
+    // back to the physical frame (Rᵀ)
+    double oL[NV], oR[NV];
+    oL[0] = ab[0];
+    oL[DIM + 1] = ab[DIM + 1];
+    oR[0] = bbar[0];
+    oR[DIM + 1] = bbar[DIM + 1];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        oL[1 + A.ax[r]] = flip(ab[1 + r], A.neg[r]);
+        oR[1 + A.ax[r]] = flip(bbar[1 + r], A.neg[r]);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        P.QbL[k * P.nfdofs + gid] = oL[k];
+        if (s1 >= 0) P.QbR[k * P.nfdofs + gid] = oR[k];
+    }
+    P.Ibar[gid] = Ib;
+}
+
+template <int DIM, int N>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
+    extern __shared__ double smem[];
+    double* sops = smem;
+    double* sw = sops + S::NOPS;   // [NV][NN]: w = λ / J
+    const int tid = threadIdx.x;
+    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    const int e0 = blockIdx.x * S::EPB;
+    const int el = tid / NPE, i = tid - el * NPE;
+    const int e = e0 + el;
+    const bool active = (tid < NN) && (e < P.nelem);
+    int64_t gi = (int64_t)e * NPE + i;
+    double ain[NV];
+    if (active) {
+        double w = P.invJ[e] * P.s_lam;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ain[k] = P.Ain[k * P.ndofs + gi];
+            sw[k * NN + tid] = w * ain[k];
+        }
+    }
+    __syncthreads();
+    if (!active) return;
+    double q[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
+    Prim pr = prim_of<DIM>(q, P.gamma);
+    const double g1 = P.gamma - 1.0;
+    double qb[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) qb[k] = 0.0;
+    const double* Ds = sops;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int pos, line;
+        tp_coords<DIM>(N, i, d, pos, line);
+        double G[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) G[k] = 0.0;
+#pragma unroll
+        for (int r = 0; r < N; ++r) {   // Σ_rows Ds(row, pos) w_row  (transpose)
+            int j = el * NPE + tp_node<DIM>(N, d, line, r);
+            double a = Ds[r + pos * N];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) G[k] = fma(a, sw[k * NN + j], G[k]);
+        }
+        euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
+        // trace cotangents of the faces this node lies on (LGL: the end nodes)
+        if (pos == 0 || pos == N - 1) {
+            int32_t pk = P.elem_face[e * 2 * DIM + 2 * d + (pos == 0 ? 0 : 1)];
+            const double* src = (pk & 1) ? P.QbR : P.QbL;
+            int64_t o = (int64_t)(pk >> 1) * NFD + line;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qb[k] += __ldcg(src + k * P.nfdofs + o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double o = fma(P.alpha, ain[k], qb[k]);
+        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
+        if (P.writeB) {
+            double b = P.delta_B * ain[k];
+            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
+            P.B[k * P.ndofs + gi] = b;
+        }
+        P.Aout[k * P.ndofs + gi] = o;
+    }
+    if (P.cbar && i == 0) {   // intensity (c1 + c2)/2: each side gets half, a boundary face all
+        double acc = 0.0;
+        for (int fk = 0; fk < 2 * DIM; ++fk) {
+            int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            int fc = pk >> 1;
+            double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+            for (int m = 0; m < NFD; ++m) acc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + m), acc);
+        }
+        P.cbar[e] += acc;
+    }
+}
+
+template <int DIM, int N>
+cudaError_t launch_adj_elem_n(const AdjElemParams& P, cudaStream_t s) {
+    using S = Shape<DIM, N>;
+    constexpr size_t smem = sizeof(double) * (S::NOPS + (DIM + 2) * S::NN);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(adj_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    int grid = (P.nelem + S::EPB - 1) / S::EPB;
+    adj_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
+    switch (n) {
+        case 2: return launch_adj_elem_n<DIM, 2>(P, s);
+        case 3: return launch_adj_elem_n<DIM, 3>(P, s);
+        case 4: return launch_adj_elem_n<DIM, 4>(P, s);
+        case 5: return launch_adj_elem_n<DIM, 5>(P, s);
+        case 6: return launch_adj_elem_n<DIM, 6>(P, s);
+        case 7: return launch_adj_elem_n<DIM, 7>(P, s);
+        case 8: return launch_adj_elem_n<DIM, 8>(P, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// Terminal functional J = 1/2 Σ w_i (ρ_i - ρt_i)²: seed Ū (density column) and per-block partials.
+__global__ void functional_kernel(const double* Q, const double* rho_t, const double* w, int64_t ndofs, int nv,
+                                  double* Ubar, double* partial) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double j = 0.0;
+    if (g < ndofs) {
+        double r = Q[g] - rho_t[g];
+        Ubar[g] = w[g] * r;
+        for (int k = 1; k < nv; ++k) Ubar[k * ndofs + g] = 0.0;
+        j = 0.5 * w[g] * (r * r);
+    }
+    for (int o = 16; o > 0; o >>= 1) j += __shfl_xor_sync(0xffffffffu, j, o);
+    __shared__ double sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = j;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x + 31) / 32; ++k) s += sm[k];
+        partial[blockIdx.x] = s;
+    }
+}
+
+}  // namespace flou
+
+using namespace flou;
+
+namespace {
+
+struct AdjBuffers {
+    double *QbL = nullptr, *QbR = nullptr, *Ibar = nullptr;
+};
+
+int adj_supported(flou_ctx* c) {
+    if (c->cfg.equation != FLOU_EQ_EULER || c->cfg.volume_op != FLOU_OP_STRONG || c->cfg.numflux != FLOU_NF_LXF ||
+        c->cfg.numflux_avg != FLOU_NF_STD_AVERAGE)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form and "
+                                                 "the LxF(StdAverage) flux");
+    if (!c->lgl) return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL)");
+    for (int b = 0; b < c->nbcs; ++b)
+        if (c->bc_kind[b] == FLOU_BC_INFLOW)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint supports periodic, slip and outflow boundaries");
+    return FLOU_OK;
+}
+
+int alloc_adj(flou_ctx* c, AdjBuffers& B) {
+    size_t nf = (size_t)c->nfdofs * c->nv;
+    cudaError_t e = cudaMalloc((void**)&B.QbL, nf * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&B.QbR, nf * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&B.Ibar, (size_t)c->nfdofs * sizeof(double));
+    if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint buffers");
+    return FLOU_OK;
+}
+
+void free_adj(AdjBuffers& B) {
+    if (B.QbL) cudaFree(B.QbL);
+    if (B.QbR) cudaFree(B.QbR);
+    if (B.Ibar) cudaFree(B.Ibar);
+    B = AdjBuffers();
+}
+
+// One transposed residual, fused with an adjoint stage combination:
+//   Aout = alpha Ain + beta B + (∂L/∂U)(U)ᵀ (s_lam Ain);  B = gamma_B B + delta_B Ain (writeB)
+//   cbar += (∂L/∂c)ᵀ (s_lam Ain)
+int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, const double* Ain, double* Aout,
+              double* Bacc, double* cbar, double s_lam, double alpha, double beta, int readB, int writeB,
+              double gamma_B, double delta_B) {
+    AdjFaceParams F;
+    memset(&F, 0, sizeof(F));
+    F.U = U;
+    F.Ain = Ain;
+    F.s_lam = s_lam;
+    F.QbL = Bf.QbL;
+    F.QbR = Bf.QbR;
+    F.Ibar = Bf.Ibar;
+    F.face_elem = c->d_face_elem;
+    F.faceJ = c->d_faceJ;
+    F.face_bc = c->d_face_bc;
+    F.invJ = c->d_invJ;
+    F.ops = c->d_ops;
+    F.elem_c = c->d_c;
+    F.intensity = c->cfg.numflux_intensity;
+    F.gamma = c->cfg.gamma;
+    F.ndofs = c->ndofs;
+    F.nfdofs = c->nfdofs;
+    F.nfaces = c->nfaces;
+    F.n = c->n;
+    F.npe = c->npe;
+    F.nfd = c->nfd;
+    for (int b = 0; b < MAXBC; ++b) F.bc_kind[b] = c->bc_kind[b];
+    int64_t nth = (int64_t)c->nfaces * c->nfd;
+    int grid = (int)((nth + 255) / 256);
+    int dim = c->cfg.dim;
+    if (dim == 1) adj_face_kernel<1><<<grid, 256, 0, s>>>(F);
+    else if (dim == 2) adj_face_kernel<2><<<grid, 256, 0, s>>>(F);
+    else adj_face_kernel<3><<<grid, 256, 0, s>>>(F);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
+    AdjElemParams P;
+    memset(&P, 0, sizeof(P));
+    P.U = U;
+    P.Ain = Ain;
+    P.Aout = Aout;
+    P.B = Bacc;
+    P.QbL = Bf.QbL;
+    P.QbR = Bf.QbR;
+    P.Ibar = Bf.Ibar;
+    P.cbar = c->d_c ? cbar : nullptr;
+    P.elem_face = c->d_elem_face;
+    P.face_elem = c->d_face_elem;
+    P.invJ = c->d_invJ;
+    P.Ja = c->d_Ja;
+    P.ops = c->d_ops;
+    P.ndofs = c->ndofs;
+    P.nfdofs = c->nfdofs;
+    P.nelem = c->nelem;
+    P.s_lam = s_lam;
+    P.alpha = alpha;
+    P.beta = beta;
+    P.gamma_B = gamma_B;
+    P.delta_B = delta_B;
+    P.readB = readB;
+    P.writeB = writeB;
+    P.gamma = c->cfg.gamma;
+    if (dim == 1) e = launch_adj_elem<1>(c->n, P, s);
+    else if (dim == 2) e = launch_adj_elem<2>(c->n, P, s);
+    else e = launch_adj_elem<3>(c->n, P, s);
+    if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint element kernel");
+    return FLOU_OK;
+}
+
+// Optimal binomial checkpointing split (Griewank & Walther's problem): minimal number of
+// forward steps to reverse n steps from a stored state with s free snapshot slots, by dynamic
+// programming over the position m of the next snapshot:
+//   cost(n, s) = min_m m + cost(n - m, s - 1) + cost(m, s),  cost(1, s) = 0,  cost(n, 0) = n(n-1)/2.
+struct Schedule {
+    int n, s;
+    std::vector<long long> cost;
+    std::vector<int> split;
+    long long& C(int nn, int ss) { return cost[(size_t)nn * (s + 1) + ss]; }
+    int& M(int nn, int ss) { return split[(size_t)nn * (s + 1) + ss]; }
+    // Binomial rule when the table is too large: with r the least repetition number such that
+    // C(ss + r, ss) >= nn, put the snapshot so that the remainder fits C(ss - 1 + r, ss - 1).
+    int split_of(int nn, int ss) {
+        if (dp) return M(nn, ss);
+        auto binom = [](int a, int b) {
+            double v = 1.0;
+            for (int i = 1; i <= b; ++i) v = v * (a - b + i) / i;
+            return v;
+        };
+        int r = 0;
+        while (binom(ss + r, ss) < nn) ++r;
+        int m = nn - (int)std::min<double>(binom(ss - 1 + r, ss - 1), nn - 1);
+        return std::max(1, std::min(nn - 1, m));
+    }
+    bool dp = true;
+    Schedule(int n_, int s_) : n(n_), s(std::min(s_, std::max(n_ - 1, 0))) {
+        if ((double)n * n * (s + 1) > 2e8) {   // too large for the table: binomial rule below
+            dp = false;
+            return;
+        }
+        cost.assign((size_t)(n + 1) * (s + 1), 0);
+        split.assign((size_t)(n + 1) * (s + 1), 0);
+        for (int nn = 0; nn <= n; ++nn) C(nn, 0) = (long long)nn * (nn - 1) / 2;
+        for (int ss = 1; ss <= s; ++ss)
+            for (int nn = 2; nn <= n; ++nn) {
+                long long best = -1;
+                int bm = 1;
+                for (int m = 1; m < nn; ++m) {
+                    long long v = m + C(nn - m, ss - 1) + C(m, ss);
+                    if (best < 0 || v < best) { best = v; bm = m; }
+                }
+                C(nn, ss) = best;
+                M(nn, ss) = bm;
+            }
+    }
+};
+
+struct Solver {
+    flou_ctx* c;
+    cudaStream_t st;
+    double dt;
+    int nsteps;
+    std::vector<double*> slot;          // snapshot states; slot[0] = U^0
+    std::vector<int> free_slots;
+    double *X = nullptr, *S1 = nullptr, *S2 = nullptr, *A = nullptr, *Bacc = nullptr, *T = nullptr;
+    double* cbar = nullptr;
+    const double* rho_t;
+    const double* w;
+    double* partial = nullptr;
+    int nblk = 0;
+    double J = 0.0;
+    bool seeded = false;
+    long long advances = 0;
+    AdjBuffers ab;
+    Schedule* sch = nullptr;
+    size_t bytes = 0;
+
+    int copy(double* dst, const double* src) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+        return e == cudaSuccess ? FLOU_OK : ctx_cuda_fail(c, e, "state copy");
+    }
+    int advance(double* Q, int k) {   // k SSP-RK3 steps in place (stage buffer: S1)
+        for (int i = 0; i < k; ++i) {
+            int r;
+            if ((r = ctx_stage(c, st, Q, Q, S1, 1, dt, 0.0, 1.0))) return r;
+            if ((r = ctx_stage(c, st, S1, Q, S1, 2, dt, 0.75, 0.25))) return r;
+            if ((r = ctx_stage(c, st, S1, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;
+            ++advances;
+        }
+        return FLOU_OK;
+    }
+    // Reverse one step from U^k held in X: the adjoint of U^(k+1) is in A on entry and that of
+    // U^k on exit.
+    int backward_step(int k) {
+        int r;
+        if ((r = ctx_stage(c, st, X, X, S1, 1, dt, 0.0, 1.0))) return r;             // U1
+        if ((r = ctx_stage(c, st, S1, X, S2, 2, dt, 0.75, 0.25))) return r;          // U2
+        if (!seeded) {   // the last step: form U^n, the functional and its gradient seed
+            if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
+            if ((r = ctx_stage(c, st, S2, X, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;   // U^n
+            functional_kernel<<<nblk, 256, 0, st>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return ctx_cuda_fail(c, e, "functional");
+            std::vector<double> h(nblk);
+            e = cudaMemcpyAsync(h.data(), partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return ctx_cuda_fail(c, e, "functional");
+            J = 0.0;
+            for (double v : h) J += v;
+            seeded = true;
+        }
+        if ((r = adj_stage(c, ab, st, S2, A, T, Bacc, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
+            return r;
+        if ((r = adj_stage(c, ab, st, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
+        if ((r = adj_stage(c, ab, st, X, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
+        return FLOU_OK;
+    }
+    // U^i0 is in slot[si]; ns free snapshot slots may be used; reverses steps i0 .. i0+n-1.
+    int rev(int i0, int n, int ns, int si) {
+        int r;
+        if (n <= 0) return FLOU_OK;
+        if (n == 1) {
+            if ((r = copy(X, slot[si]))) return r;
+            return backward_step(i0);
+        }
+        if (ns == 0 || free_slots.empty()) {
+            for (int k = n - 1; k >= 0; --k) {
+                if ((r = copy(X, slot[si]))) return r;
+                if ((r = advance(X, k))) return r;
+                if ((r = backward_step(i0 + k))) return r;
+            }
+            return FLOU_OK;
+        }
+        int m = sch->split_of(n, std::min(ns, sch->s));
+        if (m < 1 || m >= n) m = n / 2;
+        int sj = free_slots.back();
+        free_slots.pop_back();
+        if ((r = copy(slot[sj], slot[si]))) return r;
+        if ((r = advance(slot[sj], m))) return r;
+        if ((r = rev(i0 + m, n - m, ns - 1, sj))) return r;
+        free_slots.push_back(sj);
+        return rev(i0, m, ns, si);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int32_t flou_rhs_vjp(flou_ctx* c, double* Qbar, double* cbar, const double* Q, const double* lambda) {
+    if (!c) return FLOU_ERR_ARG;
+    int r = ctx_prepare(c);
+    if (r) return r;
+    if ((r = adj_supported(c))) return r;
+    if (!Qbar || !Q || !lambda) return ctx_fail(c, FLOU_ERR_ARG, "null pointer");
+    AdjBuffers B;
+    if ((r = alloc_adj(c, B))) return r;
+    cudaStream_t s = c->stream;
+    if (cbar && c->d_c) {
+        cudaError_t e = cudaMemsetAsync(cbar, 0, c->nelem * sizeof(double), s);
+        if (e != cudaSuccess) { free_adj(B); return ctx_cuda_fail(c, e, "cbar reset"); }
+    }
+    r = adj_stage(c, B, s, Q, lambda, Qbar, nullptr, cbar, 1.0, 0.0, 0.0, 0, 0, 0.0, 0.0);
+    cudaError_t e = cudaStreamSynchronize(s);
+    free_adj(B);
+    if (r) return r;
+    if (e != cudaSuccess) return ctx_cuda_fail(c, e, "vjp");
+    return ctx_check_status(c);
+}
+
+int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nsteps, int32_t nsnap,
+                           const double* rho_target, const double* weights, double* J, double* dJdQ0, double* dJdc,
+                           int64_t* forward_steps) {
+    if (!c) return FLOU_ERR_ARG;
+    int r = ctx_prepare(c);
+    if (r) return r;
+    if ((r = adj_supported(c))) return r;
+    if (!Q0 || !rho_target || !weights || !dJdQ0 || nsteps < 1 || nsnap < 0 || !std::isfinite(dt))
+        return ctx_fail(c, FLOU_ERR_ARG, "invalid arguments");
+    if (dJdc && !c->d_c)
+        return ctx_fail(c, FLOU_ERR_STATE, "dJ/dc needs the per-element dissipation scale (flou_set_dissipation)");
+    Solver S;
+    S.c = c;
+    S.st = c->stream;
+    S.dt = dt;
+    S.nsteps = nsteps;
+    S.rho_t = rho_target;
+    S.w = weights;
+    S.bytes = (size_t)c->ndofs * c->nv * sizeof(double);
+    S.nblk = (int)((c->ndofs + 255) / 256);
+    int nslots = std::min(nsnap, std::max(nsteps - 1, 0));
+    std::vector<double*> owned;
+    auto dalloc = [&](double** p, size_t bytes) {
+        cudaError_t e = cudaMalloc((void**)p, bytes);
+        if (e == cudaSuccess) owned.push_back(*p);
+        return e;
+    };
+    cudaError_t e = cudaSuccess;
+    S.slot.assign(nslots + 1, nullptr);
+    for (int i = 0; i <= nslots && e == cudaSuccess; ++i) e = dalloc(&S.slot[i], S.bytes);
+    double** bufs[] = {&S.X, &S.S1, &S.S2, &S.A, &S.Bacc, &S.T};
+    for (double** b : bufs)
+        if (e == cudaSuccess) e = dalloc(b, S.bytes);
+    if (e == cudaSuccess) e = dalloc(&S.partial, S.nblk * sizeof(double));
+    if (e == cudaSuccess && dJdc) S.cbar = dJdc;
+    int rr = FLOU_OK;
+    if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "adjoint storage");
+    if (!rr) rr = alloc_adj(c, S.ab);
+    if (!rr && S.cbar) {
+        e = cudaMemsetAsync(S.cbar, 0, c->nelem * sizeof(double), S.st);
+        if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "cbar reset");
+    }
+    Schedule sch(nsteps, nslots);
+    S.sch = &sch;
+    for (int i = 1; i <= nslots; ++i) S.free_slots.push_back(i);
+    if (!rr) rr = S.copy(S.slot[0], Q0);
+    if (!rr) rr = S.rev(0, nsteps, nslots, 0);
+    if (!rr) rr = S.copy(dJdQ0, S.A);
+    if (!rr) {
+        e = cudaStreamSynchronize(S.st);
+        if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "adjoint solve");
+    }
+    free_adj(S.ab);
+    for (double* p : owned) cudaFree(p);
+    if (rr) return rr;
+    if (J) *J = S.J;
+    if (forward_steps) *forward_steps = S.advances;
+    return ctx_check_status(c);
+}
+
+}  // extern "C"

@@ -84,6 +84,7 @@ FaceParams face_params(const flou_ctx* c, const double* Q) {
     P.faceJ = c->d_faceJ;
     P.face_bc = c->d_face_bc;
     P.l = c->d_ops + 2 * c->n * c->n;
+    P.elem_c = c->d_c;
     P.ndofs = c->ndofs;
     P.nfdofs = c->nfdofs;
     P.nfaces = c->nfaces;
@@ -236,6 +237,11 @@ ElemParams ctx_elem_params(const flou_ctx* c, const double* Q, const double* Q0,
     return elem_params(c, Q, Q0, out, mode, dt, a0, a1);
 }
 ElemLaunch ctx_elem_launch(const flou_ctx* c) { return elem_launch(c); }
+int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
+              double a0, double a1) {
+    return stage(c, s, Q, Q0, out, mode, dt, a0, a1);
+}
+int ctx_check_status(flou_ctx* c) { return check_status(c); }
 }  // namespace flou
 
 extern "C" {
@@ -282,7 +288,7 @@ int32_t flou_destroy(flou_ctx* c) {
     if (!c) return FLOU_ERR_ARG;
     drop_graph(c);
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
-                    c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin};
+                    c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -380,7 +386,7 @@ int32_t flou_set_mesh(flou_ctx* c, int32_t nelem, int32_t nfaces, const int32_t*
     if ((r = upload(c, &c->d_face_elem, fe.data(), fe.size(), "mesh upload"))) return r;
     if ((r = upload(c, &c->d_face_bc, fb.data(), fb.size(), "mesh upload"))) return r;
     // sizes changed: drop size-dependent buffers
-    double** sized[] = {&c->d_Fn, &c->d_U, &c->d_Qh, &c->d_dQh};
+    double** sized[] = {&c->d_Fn, &c->d_U, &c->d_Qh, &c->d_dQh, &c->d_c};
     for (double** b : sized)
         if (*b) { cudaFree(*b); *b = nullptr; }
     c->h_face_bc = fb;
@@ -475,6 +481,25 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_dx, dx.data(), dx.size(), "geometry upload"))) return r;
     c->have_geom = true;
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_dissipation(flou_ctx* c, const double* celem, int32_t ptr_kind) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh must come before flou_set_dissipation");
+    if (c->cfg.numflux != FLOU_NF_LXF)
+        return fail(c, FLOU_ERR_UNSUPPORTED, "a per-element dissipation scale applies to the LxF flux only");
+    if (!celem) {
+        if (c->d_c) cudaFree(c->d_c);
+        c->d_c = nullptr;
+        drop_graph(c);
+        return FLOU_OK;
+    }
+    if (!c->d_c) CK(cudaMalloc((void**)&c->d_c, c->nelem * sizeof(double)), "dissipation upload");
+    CK(cudaMemcpy(c->d_c, celem, c->nelem * sizeof(double),
+                  ptr_kind == FLOU_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
+       "dissipation upload");
     drop_graph(c);
     return FLOU_OK;
 }

@@ -39,6 +39,7 @@ struct flou_ctx {
     double* d_U = nullptr;          // RK stage scratch
     double* d_Qh = nullptr;         // staging for host-pointer calls
     double* d_dQh = nullptr;
+    double* d_c = nullptr;          // optional per-element LxF dissipation scale
     int32_t* d_status = nullptr;    // [flags, lowest element]
     unsigned long long* d_dtmin = nullptr;
     // graph cache for flou_step
@@ -57,4 +58,7 @@ FaceParams ctx_face_params(const flou_ctx* c, const double* Q);
 ElemParams ctx_elem_params(const flou_ctx* c, const double* Q, const double* Q0, double* out, int mode, double dt,
                            double a0, double a1);
 ElemLaunch ctx_elem_launch(const flou_ctx* c);
+int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
+              double a0, double a1);
+int ctx_check_status(flou_ctx* c);
 }  // namespace flou

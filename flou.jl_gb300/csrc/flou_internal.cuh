@@ -33,6 +33,7 @@ struct FaceParams {
     const double* faceJ;         // nfaces
     const int8_t* face_bc;       // nfaces: boundary index (0-based) or -1
     const double* l;             // l_l[n], l_r[n]
+    const double* elem_c;        // optional per-element LxF dissipation scale (face: (c1 + c2)/2)
     int64_t ndofs, nfdofs;
     int32_t nfaces, n, npe, nfd;
     int32_t numflux, lxf_avg;
@@ -366,6 +367,11 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
     }
     double F[NV];
     double J = P.faceJ[f];
+    double inten = P.intensity;
+    if (P.elem_c) {
+        int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
+        inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
+    }
     if (EQ == FLOU_EQ_EULER) {
         // rotate2face / rotate2phys (Euler.jl:16-64) as signed permutations
         FrameAxes A = frame_axes<DIM>(s0 & 7);
@@ -378,9 +384,9 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         }
         double Fr[NV];
         if (P.numflux == FLOU_NF_CHANDRASHEKAR || (P.numflux == FLOU_NF_LXF && P.lxf_avg == FLOU_NF_CHANDRASHEKAR))
-            euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, P.intensity, P.gamma, Fr);
+            euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
         else
-            euler_face_flux_fast<DIM>(a, b, P.numflux, P.intensity, P.gamma, Fr);
+            euler_face_flux_fast<DIM>(a, b, P.numflux, inten, P.gamma, Fr);
         F[0] = Fr[0];
         F[DIM + 1] = Fr[DIM + 1];
 #pragma unroll
@@ -391,13 +397,13 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         if (DIM > 1) an = an + P.adv[1] * fr.n[1];
         if (DIM > 2) an = an + P.adv[2] * fr.n[2];
         F[0] = an * (ql[0] + qr[0]) / 2.0;
-        if (P.numflux == FLOU_NF_LXF) F[0] = F[0] + fabs(an) * (ql[0] - qr[0]) / 2.0 * P.intensity;
+        if (P.numflux == FLOU_NF_LXF) F[0] = F[0] + fabs(an) * (ql[0] - qr[0]) / 2.0 * inten;
     } else {
         // Burgers.jl:27-38
         F[0] = (ql[0] * ql[0] + qr[0] * qr[0]) / 4.0 * fr.n[0];
         if (P.numflux == FLOU_NF_LXF) {
             double lam = fmax(fabs(ql[0]), fabs(qr[0]));
-            F[0] = F[0] + lam * (ql[0] - qr[0]) / 2.0 * P.intensity;
+            F[0] = F[0] + lam * (ql[0] - qr[0]) / 2.0 * inten;
         }
     }
     int64_t o = (int64_t)f * P.nfd + m;

@@ -87,6 +87,9 @@ PROTOTYPES = {
     "flou_time_kernels": [_P, _P, ctypes.c_int32, _D, _D],
     "flou_rhs_noalloc": [_P, _P, _P, ctypes.c_double],
     "flou_fp64_peak": [_D],
+    "flou_set_dissipation": [_P, _P, ctypes.c_int32],
+    "flou_rhs_vjp": [_P, _P, _P, _P, _P],
+    "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
     "flou_batch_create": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "flou_batch_destroy": [_P],
     "flou_batch_last_error": [_P],

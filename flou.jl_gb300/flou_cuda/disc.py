@@ -234,6 +234,34 @@ class Context:
         L.check(self._lib.flou_max_dt(self.h, pq, float(cfl), ctypes.byref(out), kq), self.h)
         return out.value
 
+    def set_dissipation(self, c):
+        """Per-element LxF dissipation scale (numpy or CUDA tensor, nelem entries); None removes it."""
+        if c is None:
+            L.check(self._lib.flou_set_dissipation(self.h, None, L.PTR_HOST), self.h)
+            return
+        if isinstance(c, np.ndarray):
+            c = np.ascontiguousarray(c, dtype=np.float64)
+            self._c_keep = c
+            L.check(self._lib.flou_set_dissipation(self.h, ctypes.c_void_p(c.ctypes.data), L.PTR_HOST), self.h)
+        else:
+            L.check(self._lib.flou_set_dissipation(self.h, ctypes.c_void_p(c.data_ptr()),
+                                                   L.PTR_DEVICE if c.is_cuda else L.PTR_HOST), self.h)
+
+    def rhs_vjp(self, Qbar, cbar, Q, lam):
+        """Qbar = (∂rhs/∂Q)ᵀ lam, cbar = (∂rhs/∂c)ᵀ lam (CUDA tensors; cbar may be None)."""
+        p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        L.check(self._lib.flou_rhs_vjp(self.h, p(Qbar), p(cbar), p(Q), p(lam)), self.h)
+
+    def adjoint_solve(self, Q0, dt, nsteps, nsnap, rho_target, weights, dJdQ0, dJdc=None):
+        """Returns (J, recomputed forward steps); fills dJdQ0 (and dJdc) -- CUDA tensors."""
+        p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        J = ctypes.c_double()
+        nf = ctypes.c_int64()
+        L.check(self._lib.flou_adjoint_solve(self.h, p(Q0), float(dt), int(nsteps), int(nsnap), p(rho_target),
+                                             p(weights), ctypes.byref(J), p(dJdQ0), p(dJdc), ctypes.byref(nf)),
+                self.h)
+        return J.value, nf.value
+
     def time_kernels(self, Q, nrep=3):
         """Mean launch durations (ms) of the face kernel and the element kernel (CUDA events)."""
         pq, kq = self._ptr(Q)

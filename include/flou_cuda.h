@@ -173,6 +173,31 @@ int32_t flou_time_kernels(flou_ctx* ctx, const double* Q, int32_t nrep, double* 
  * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
 int32_t flou_fp64_peak(double* gflops);
 
+/* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
+ * Covers the Euler equations with the strong-form volume term and the LxF(StdAverage)
+ * (Rusanov) interface flux on LGL nodes, with periodic, slip-wall and outflow boundaries.
+ * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):
+ * max(a, b) takes b unless b < a; d|u|/du = -1 for a set sign bit, else +1. */
+
+/* Per-element scale c_e of the LxF dissipation: a face uses intensity (c_1 + c_2)/2 of its
+ * two elements (c_1 on boundary faces); c = 1 everywhere reproduces LxF(StdAverage(), 1.0).
+ * NULL removes it.  c has nelem entries (host or device memory by ptr_kind). */
+int32_t flou_set_dissipation(flou_ctx* ctx, const double* c, int32_t ptr_kind);
+
+/* Vector-Jacobian product of the residual at Q (device pointers):
+ * Qbar = (∂rhs/∂Q)ᵀ lambda, cbar = (∂rhs/∂c)ᵀ lambda (cbar may be NULL; needs the scale c). */
+int32_t flou_rhs_vjp(flou_ctx* ctx, double* Qbar, double* cbar, const double* Q, const double* lambda);
+
+/* Gradient of J = 1/2 Σ_i w_i (ρ_i(T) - ρt_i)², T = nsteps·dt, with respect to the initial state
+ * Q0 and the dissipation scales c, by the discrete adjoint of the SSP-RK3 solve with binomial
+ * checkpointing: at most `nsnap` stored states besides Q0 (the schedule minimising recomputed
+ * forward steps for that budget).  Device pointers: Q0, rho_target, weights (ndofs), dJdQ0
+ * (state-sized), dJdc (nelem, may be NULL).  *forward_steps (may be NULL) returns the number of
+ * recomputed forward steps. */
+int32_t flou_adjoint_solve(flou_ctx* ctx, const double* Q0, double dt, int32_t nsteps, int32_t nsnap,
+                           const double* rho_target, const double* weights, double* J, double* dJdQ0, double* dJdc,
+                           int64_t* forward_steps);
+
 /* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
  * Many independent discretizations with uneven element counts and orders advance together:
  * one persistent launch per SSP-RK3 stage serves every instance from one work queue of face

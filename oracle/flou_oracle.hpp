@@ -647,13 +647,14 @@ template <class T> inline Vec<T> euler_hllc(const Vec<T>& Ql, const Vec<T>& Qr, 
 // normal (used by the scalar equations).  Interfaces.jl:111-136; Euler.jl:99-226;
 // LinearAdvection.jl:27-39; Burgers.jl:27-38.
 template <class T>
-inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n, const Config& c, int kind) {
+inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n, const Config& c, int kind,
+                           const T& intensity) {
     Vec<T> F{};
     if (c.eq == EQ_ADVECTION) {
         double an = 0;   // dot(eq.a, n)
         for (int d = 0; d < c.dim; ++d) an = an + c.a[d] * n[d];
         F[0] = an * (Ql[0] + Qr[0]) / 2.0;
-        if (kind == NF_LXF) F[0] = F[0] + std::fabs(an) * (Ql[0] - Qr[0]) / 2.0 * c.intensity;
+        if (kind == NF_LXF) F[0] = F[0] + std::fabs(an) * (Ql[0] - Qr[0]) / 2.0 * intensity;
         return F;
     }
     if (c.eq == EQ_BURGERS) {
@@ -661,7 +662,7 @@ inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n,
         F[0] = (sq(Ql[0]) + sq(Qr[0])) / 4.0 * n[0];
         if (kind == NF_LXF) {
             T lam = max(fabs(Ql[0]), fabs(Qr[0]));
-            F[0] = F[0] + lam * (Ql[0] - Qr[0]) / 2.0 * c.intensity;
+            F[0] = F[0] + lam * (Ql[0] - Qr[0]) / 2.0 * intensity;
         }
         return F;
     }
@@ -681,8 +682,13 @@ inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n,
     T al = soundvelocity(Pl[0], Pl[dim + 1], c.gamma);
     T ar = soundvelocity(Pr[0], Pr[dim + 1], c.gamma);
     T lam = max(fabs(Pl[1]) + al, fabs(Pr[1]) + ar);
-    for (int k = 0; k < nv; ++k) F[k] = Fa[k] + lam * (Ql[k] - Qr[k]) / 2.0 * c.intensity;
+    for (int k = 0; k < nv; ++k) F[k] = Fa[k] + lam * (Ql[k] - Qr[k]) / 2.0 * intensity;
     return F;
+}
+
+template <class T>
+inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n, const Config& c, int kind) {
+    return numericalflux(Ql, Qr, n, c, kind, T(c.intensity));
 }
 
 // twopointflux (contravariant, direction column of the metric averaged):
@@ -840,7 +846,10 @@ template <class T> inline Vec<T> apply_bc(const Bc& bc, const Vec<T>& Qin, const
 }
 
 // rhs!, src/FlouSpatial/Equations/Hyperbolic.jl:31-69 (steps C1-C8, in order).
-template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Workspace<T>& ws) {
+// `celem` (optional): per-element scale c_e of the LxF dissipation; a face uses
+// intensity = (c_1 + c_2)/2 of its two elements (c_1 on boundary faces).  c = 1 is LxF(., 1.0).
+template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Workspace<T>& ws,
+                            const T* celem = nullptr) {
     (void)time;
     const Config& c = g.cfg;
     const int dim = c.dim, n = g.n, nv = c.nv, npe = g.npe, nfd = g.nfd;
@@ -967,7 +976,12 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
             const Frame& fr = g.frames[ii];
             Vec<T> Qln = rotate2face(getv(ws.Qf[0].data(), nf, ii, nv), fr, c);
             Vec<T> Qrn = rotate2face(getv(ws.Qf[1].data(), nf, jj, nv), fr, c);
-            Vec<T> Fni = numericalflux(Qln, Qrn, fr.n, c, c.numflux);
+            T inten = T(c.intensity);
+            if (celem) {
+                int e1 = g.eleminds[2 * f] - 1, e2 = g.eleminds[2 * f + 1] - 1;
+                inten = (celem[e1] + celem[e2 >= 0 ? e2 : e1]) * 0.5;
+            }
+            Vec<T> Fni = numericalflux(Qln, Qrn, fr.n, c, c.numflux, inten);
             Vec<T> F = rotate2phys(Fni, fr, c);
             for (int k = 0; k < nv; ++k) {
                 F[k] = F[k] * g.faceJ[ii];
@@ -1007,17 +1021,17 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
 // Shu-Osher SSP-RK3 (Shu & Osher 1988), the method behind OrdinaryDiffEq's SSPRK33:
 //   U1 = U0 + dt L(U0); U2 = 3/4 U0 + 1/4 (U1 + dt L(U1)); U3 = 1/3 U0 + 2/3 (U2 + dt L(U2)).
 template <class T> void ssprk3_step(const Disc& g, T* Q, double dt, double t, Workspace<T>& ws,
-                                    std::vector<T>& U, std::vector<T>& L) {
+                                    std::vector<T>& U, std::vector<T>& L, const T* celem = nullptr) {
     long N = g.ndofs() * g.cfg.nv;
     U.resize(N);
     L.resize(N);
-    rhs(g, L.data(), Q, t, ws);
+    rhs(g, L.data(), Q, t, ws, celem);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < N; ++i) U[i] = Q[i] + dt * L[i];
-    rhs(g, L.data(), U.data(), t + dt, ws);
+    rhs(g, L.data(), U.data(), t + dt, ws, celem);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < N; ++i) U[i] = 0.75 * Q[i] + 0.25 * (U[i] + dt * L[i]);
-    rhs(g, L.data(), U.data(), t + 0.5 * dt, ws);
+    rhs(g, L.data(), U.data(), t + 0.5 * dt, ws, celem);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < N; ++i) Q[i] = (1.0 / 3.0) * Q[i] + (2.0 / 3.0) * (U[i] + dt * L[i]);
 }

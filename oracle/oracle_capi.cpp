@@ -46,6 +46,43 @@ static inline CD min(CD a, CD b) { g_count.cmp++; return a.v < b.v ? a : b; }
 static inline CD max(CD a, CD b) { g_count.cmp++; return a.v < b.v ? b : a; }
 }  // namespace std
 
+// ---------------------------------------------------------------------------------------
+// Forward-mode dual number (value, directional derivative): the derivative checks of the
+// adjoint run the oracle with it, the role ForwardDiff plays on the reference's CPU path.
+// Non-smooth points follow Base's conventions: max(a, b) = b unless b < a, abs' = sign with
+// abs'(+0) = 1.
+// ---------------------------------------------------------------------------------------
+struct Dual {
+    double v = 0, d = 0;
+    Dual() = default;
+    Dual(double x) : v(x), d(0) {}
+    Dual(double x, double dx) : v(x), d(dx) {}
+};
+static inline Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+static inline Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+static inline Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+static inline Dual operator/(Dual a, Dual b) { return Dual(a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)); }
+static inline Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+static inline Dual operator+(Dual a, double b) { return Dual(a.v + b, a.d); }
+static inline Dual operator-(Dual a, double b) { return Dual(a.v - b, a.d); }
+static inline Dual operator*(Dual a, double b) { return Dual(a.v * b, a.d * b); }
+static inline Dual operator/(Dual a, double b) { return Dual(a.v / b, a.d / b); }
+static inline Dual operator+(double a, Dual b) { return Dual(a + b.v, b.d); }
+static inline Dual operator-(double a, Dual b) { return Dual(a - b.v, -b.d); }
+static inline Dual operator*(double a, Dual b) { return Dual(a * b.v, a * b.d); }
+static inline Dual operator/(double a, Dual b) { return Dual(a / b.v, -a * b.d / (b.v * b.v)); }
+static inline bool operator<(Dual a, Dual b) { return a.v < b.v; }
+static inline bool operator<(Dual a, double b) { return a.v < b; }
+static inline bool operator>=(Dual a, double b) { return a.v >= b; }
+static inline bool operator<=(Dual a, double b) { return a.v <= b; }
+static inline Dual sqrt(Dual a) { double s = std::sqrt(a.v); return Dual(s, a.d / (2.0 * s)); }
+static inline Dual log(Dual a) { return Dual(std::log(a.v), a.d / a.v); }
+static inline Dual fabs(Dual a) { return std::signbit(a.v) ? -a : a; }
+namespace std {
+static inline Dual min(Dual a, Dual b) { return b.v < a.v ? b : a; }
+static inline Dual max(Dual a, Dual b) { return b.v < a.v ? a : b; }
+}  // namespace std
+
 extern "C" {
 
 void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
@@ -268,6 +305,46 @@ double oracle_max_dt(void* hp, const double* Q, double cfl, const double* omega_
     Handle* h = (Handle*)hp;
     std::vector<double> w(omega_tp, omega_tp + h->g.npe);
     return get_max_dt(h->g, Q, cfl, w);
+}
+
+// Directional derivative of one residual: rhs(Q + ε dQ, c + ε dc) -> (R, dR).  c may be null
+// (then the configured LxF intensity, no derivative).
+void oracle_rhs_jvp(void* hp, const double* Q, const double* dQ, const double* c, const double* dc, double* R,
+                    double* dR) {
+    Handle* h = (Handle*)hp;
+    long N = h->g.ndofs() * h->g.cfg.nv;
+    std::vector<Dual> q(N), r(N), ce;
+    for (long i = 0; i < N; ++i) q[i] = Dual(Q[i], dQ ? dQ[i] : 0.0);
+    if (c) {
+        ce.resize(h->g.nelem);
+        for (int e = 0; e < h->g.nelem; ++e) ce[e] = Dual(c[e], dc ? dc[e] : 0.0);
+    }
+    Workspace<Dual> ws;
+    rhs(h->g, r.data(), q.data(), 0.0, ws, c ? ce.data() : nullptr);
+    for (long i = 0; i < N; ++i) { R[i] = r[i].v; dR[i] = r[i].d; }
+}
+
+// Terminal functional J = 1/2 Σ_i w_i (ρ_i(T) - ρt_i)² after `nsteps` SSP-RK3 steps from Q0 with
+// dissipation scales c, and its directional derivative along (dQ0, dc).
+void oracle_solve_jvp(void* hp, const double* Q0, const double* dQ0, const double* c, const double* dc, double dt,
+                      int nsteps, const double* rho_t, const double* w, double* J, double* dJ) {
+    Handle* h = (Handle*)hp;
+    long nd = h->g.ndofs(), N = nd * h->g.cfg.nv;
+    std::vector<Dual> q(N), ce, U, L;
+    for (long i = 0; i < N; ++i) q[i] = Dual(Q0[i], dQ0 ? dQ0[i] : 0.0);
+    if (c) {
+        ce.resize(h->g.nelem);
+        for (int e = 0; e < h->g.nelem; ++e) ce[e] = Dual(c[e], dc ? dc[e] : 0.0);
+    }
+    Workspace<Dual> ws;
+    for (int s = 0; s < nsteps; ++s) ssprk3_step(h->g, q.data(), dt, s * dt, ws, U, L, c ? ce.data() : nullptr);
+    Dual acc(0.0);
+    for (long i = 0; i < nd; ++i) {
+        Dual r = q[i] - rho_t[i];
+        acc = acc + (0.5 * w[i]) * (r * r);
+    }
+    *J = acc.v;
+    *dJ = acc.d;
 }
 
 // Operation count of one residual evaluation (single thread).  out = {add, mul, div, sqrt,

@@ -39,6 +39,8 @@ def lib():
         _lib.oracle_max_dt.argtypes = [ctypes.c_void_p, D, ctypes.c_double, D]
         _lib.oracle_count_rhs.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
+        _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
+        _lib.oracle_solve_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D, D, D]
     return _lib
 
 
@@ -140,6 +142,28 @@ class Disc:
     def max_dt(self, Q, cfl, omega_tp):
         Q = np.asfortranarray(Q, dtype=np.float64)
         return self.L.oracle_max_dt(self.h, _d(Q), cfl, _d(np.ascontiguousarray(omega_tp)))
+
+    def rhs_jvp(self, Q, dQ, c=None, dc=None):
+        """(rhs, directional derivative) at (Q, c) along (dQ, dc) -- forward-mode duals."""
+        Q = np.asfortranarray(Q, dtype=np.float64)
+        dQ = np.asfortranarray(dQ, dtype=np.float64)
+        R, dR = np.zeros_like(Q, order="F"), np.zeros_like(Q, order="F")
+        cc = None if c is None else np.ascontiguousarray(c, dtype=np.float64)
+        dcc = None if dc is None else np.ascontiguousarray(dc, dtype=np.float64)
+        self.L.oracle_rhs_jvp(self.h, _d(Q), _d(dQ), _d(cc) if cc is not None else None,
+                              _d(dcc) if dcc is not None else None, _d(R), _d(dR))
+        return R, dR
+
+    def solve_jvp(self, Q0, dQ0, c, dc, dt, nsteps, rho_t, w):
+        """(J, dJ): J = 1/2 Σ w (ρ(T) - ρt)² after nsteps SSP-RK3 steps, and its derivative."""
+        Q0 = np.asfortranarray(Q0, dtype=np.float64)
+        dQ0 = np.asfortranarray(dQ0, dtype=np.float64)
+        J, dJ = ctypes.c_double(), ctypes.c_double()
+        args = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (c, dc, rho_t, w)]
+        p = lambda a: _d(a) if a is not None else None
+        self.L.oracle_solve_jvp(self.h, _d(Q0), _d(dQ0), p(args[0]), p(args[1]), dt, nsteps, p(args[2]),
+                                p(args[3]), ctypes.byref(J), ctypes.byref(dJ))
+        return J.value, dJ.value
 
     def count(self, Q, t=0.0):
         out = (ctypes.c_longlong * 6)()

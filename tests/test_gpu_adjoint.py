@@ -1,0 +1,155 @@
+"""Discrete adjoint: residual VJP and checkpointed gradient of a terminal functional.
+
+Checked against forward-mode dual numbers run through the oracle (the role ForwardDiff plays
+on the reference's CPU path): <VJP(λ), δ> must equal <λ, JVP(δ)>, and <∇J, δ> must equal the
+directional derivative of J; also against central finite differences (h = 1e-6).
+"""
+import numpy as np
+import pytest
+
+import flou_cuda as F
+from cases import build, oracle_for, smooth_euler_state
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a).T if np.asarray(a).ndim == 2 else a)).cuda()
+
+
+def _host(t):
+    x = t.cpu().numpy()
+    return np.asfortranarray(x.T) if x.ndim == 2 else x
+
+
+def _lxf():
+    return F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
+
+
+CASES = [
+    dict(dim=2, n=5, ne=(3, 3), periodic=True, bcs=None),
+    dict(dim=2, n=4, ne=(3, 4), periodic=(), bcs={"1": "slip", "2": "slip", "3": "out", "4": "slip"}),
+    dict(dim=1, n=6, ne=(5,), periodic=True, bcs=None),
+    dict(dim=3, n=4, ne=(2, 2, 3), periodic=True, bcs=None),
+    dict(dim=3, n=3, ne=(2, 2, 2), periodic=(2,), bcs={"1": "slip", "2": "out", "3": "slip", "4": "slip"}),
+]
+
+
+def _disc(case):
+    eq = F.EulerEquation(case["dim"], 1.4)
+    bcs = None
+    if case["bcs"]:
+        bcs = {k: (F.EulerSlipBC() if v == "slip" else F.EulerOutflowBC()) for k, v in case["bcs"].items()}
+    d = build(case["dim"], case["n"], case["ne"], eq, _lxf(), periodic=case["periodic"], bcs=bcs)
+    return d
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
+def test_rhs_vjp_dot_product(case):
+    disc = _disc(case)
+    rng = np.random.default_rng(7)
+    Q = smooth_euler_state(disc, seed=11)
+    if case["bcs"]:
+        P = disc.equation.vars_cons2prim(Q)
+        P[:, 1:1 + case["dim"]] *= 0.2   # gentle flow towards the walls
+        Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+    c = 1.0 + 0.3 * rng.random(disc.mesh.nelements)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    dc = rng.standard_normal(c.shape)
+    disc.ctx.set_dissipation(c)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + np.sum(cbar.cpu().numpy() * dc)
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    scale = np.sum(np.abs(lam * dR))
+    assert abs(lhs - rhs) <= 1e-12 * scale, (lhs, rhs, scale)
+    # the forward with c matches the oracle's residual too
+    dQg = disc.new_state()
+    disc.ctx.rhs(dQg, Q)
+    assert np.max(np.abs(dQg - R)) <= 1e-12 * np.max(np.abs(R))
+
+
+def _functional_inputs(disc, seed):
+    rng = np.random.default_rng(seed)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    rho_t = 1.0 + 0.05 * rng.standard_normal(disc.ndofs)
+    return rho_t, w
+
+
+def test_adjoint_solve_against_dual_numbers():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 4, (4, 3), eq, _lxf(), box=((-5.0, -5.0), (5.0, 5.0)))
+    Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.3, -0.4), 4.0, 0.05, period=(10.0, 10.0)))
+    rng = np.random.default_rng(3)
+    c = 1.0 + 0.2 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 5)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 12
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+def test_snapshot_budget_does_not_change_the_gradient():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 3, (3, 3), eq, _lxf())
+    Q0 = smooth_euler_state(disc, seed=4)
+    c = np.ones(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 6)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    res = []
+    for nsnap in (0, 2, 5, 15):
+        g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+        gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+        J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, 16, nsnap, _dev(rho_t), _dev(w), g, gc)
+        res.append((J, g, gc, nfwd))
+    for J, g, gc, _ in res[1:]:
+        assert J == res[0][0]
+        assert torch.equal(g, res[0][1]) and torch.equal(gc, res[0][2])
+    nf = [r[3] for r in res]
+    assert nf[0] == 16 * 15 // 2 and nf[-1] == 15 and nf[1] > nf[2] > nf[3]
+
+
+def test_adjoint_against_central_differences():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 5, (6, 6), eq, _lxf(), box=((-5.0, -5.0), (5.0, 5.0)))
+    Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.5, 0.1), 5.0, 0.08, period=(10.0, 10.0)))
+    rng = np.random.default_rng(9)
+    c = 1.0 + 0.1 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 8)
+    dt = 0.4 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 20
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 4, _dev(rho_t), _dev(w), g, gc)
+    wd, rtd = _dev(w), _dev(rho_t)
+
+    def Jof(Q, cc):
+        disc.ctx.set_dissipation(cc)
+        q = _dev(Q)
+        disc.ctx.step(q, dt, nsteps)
+        r = q[0] - rtd
+        return float(0.5 * torch.sum(wd * r * r))
+
+    h = 1e-6
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * 0.1
+        fd = (Jof(Q0 + h * dQ, c + h * dc) - Jof(Q0 - h * dQ, c - h * dc)) / (2 * h)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
