@@ -71,7 +71,7 @@ struct AdjElemParams {
 //   P̄ = ḡ_md + ḡ_E v_d,  s = Σ_k ḡ_mk v_k
 //   q̄_ρ  += -v_d (s + ḡ_E H) + (γ-1) |v|²/2 P̄
 //   q̄_mk += v_d ḡ_mk - (γ-1) v_k P̄ + [k = d] (ḡ_ρ + s + ḡ_E H)
-//   q̄_E  += ḡ_E + (γ-1) P̄
+//   q̄_E  += ḡ_E v_d + (γ-1) P̄
 template <int DIM>
 __device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv, double H, double g1,
                                                const double* gb, double scale, double* qb) {
@@ -87,7 +87,7 @@ __device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv
         if (k == d) r += gb[0] + t;
         qb[1 + k] += scale * r;
     }
-    qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1]);
+    qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1] * v[d]);
 }
 
 struct Prim {
