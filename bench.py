@@ -224,6 +224,83 @@ def bench_batched(steps, warmup, count=256):
                         "Rusanov, strong form, SSP-RK3"}
 
 
+def bench_adjoint(nsteps=400, nsnap=20, ndirs=32, seed=404):
+    """The adjoint configuration: 2D Euler, 64x64 elements, p=4, periodic [-5,5]², 400 SSP-RK3
+    steps at CFL 0.5, J = 1/2 Σ w (ρ(T) - ρt)² with quadrature weights w = Jω and ρt the density of
+    a perturbed vortex carried to T; gradients with respect to U0 and the per-element dissipation
+    scales c (at c = 1) with 20 snapshots, checked against central differences (h = 1e-6) along
+    `ndirs` random directions."""
+    import torch
+    import flou_cuda as F
+    rng = np.random.default_rng(seed)
+    eq = F.EulerEquation(2, 1.4)
+    mesh = F.CartesianMesh((-5.0, -5.0), (5.0, 5.0), (64, 64))
+    F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"))
+    b = F.LagrangeBasis("GLL", 5)
+    disc = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), 4), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    ctx = disc.ctx
+    center = rng.uniform(-1, 1, 2)
+    Q0 = np.asfortranarray(F.initial.isentropic_vortex(eq, disc.coords, center, beta=5.0, period=(10.0, 10.0)))
+    c = np.ones(mesh.nelements)
+    ctx.set_dissipation(c)
+    Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+    dt = 0.5 * ctx.max_dt(Qd, 1.0)
+    T = nsteps * dt
+    tgt = F.initial.isentropic_vortex(eq, disc.coords, center + T + rng.normal(0, 0.1, 2), beta=5.0 + rng.normal(0, 0.2),
+                                      period=(10.0, 10.0))
+    rho_t = torch.from_numpy(np.ascontiguousarray(tgt[:, 0])).cuda()
+    w = torch.from_numpy(np.tile(disc.std.omega, mesh.nelements) * disc.J).cuda()
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def forward(Q, cc=None):
+        if cc is not None:
+            ctx.set_dissipation(cc)
+        q = Q.clone()
+        ctx.step(q, dt, nsteps)
+        r = q[0] - rho_t
+        return float(0.5 * torch.sum(w * r * r))
+
+    forward(Qd)   # warm-up (graph capture)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    J0 = forward(Qd)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = ev[0].elapsed_time(ev[1])
+    g = torch.empty_like(Qd)
+    gc = torch.empty(mesh.nelements, dtype=torch.float64, device="cuda")
+    res = {}
+    for tag, ns in (("", nsnap), ("_store_all", nsteps - 1)):
+        ctx.adjoint_solve(Qd, dt, nsteps, ns, rho_t, w, g, gc)   # warm-up
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        J, nfwd = ctx.adjoint_solve(Qd, dt, nsteps, ns, rho_t, w, g, gc)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        res["adjoint_ms" + tag] = ev[0].elapsed_time(ev[1])
+        res["recomputed_forward_steps" + tag] = nfwd
+        res["snapshots" + tag] = ns
+    gh, gch = g.cpu().numpy(), gc.cpu().numpy()
+    h = 1e-6
+    errs = []
+    for k in range(ndirs):
+        dQ = torch.from_numpy(rng.standard_normal(Q0.shape[::-1])).cuda()
+        dc = rng.standard_normal(c.shape)
+        fd = (forward(Qd + h * dQ, c + h * dc) - forward(Qd - h * dQ, c - h * dc)) / (2 * h)
+        ours = float(np.sum(gh * dQ.cpu().numpy()) + np.sum(gch * dc))
+        errs.append(abs(ours - fd) / abs(fd))
+    ctx.set_dissipation(c)
+    ctx.set_stream(0)
+    res.update({"forward_ms": fwd_ms, "ratio": res["adjoint_ms"] / fwd_ms,
+                "ratio_store_all": res["adjoint_ms_store_all"] / fwd_ms, "J": J0, "steps": nsteps,
+                "ndofs": disc.ndofs, "fd_directions": ndirs, "fd_h": h, "fd_max_rel_err": max(errs),
+                "fd_median_rel_err": float(np.median(errs)),
+                "workload": "2D Euler 64x64 p=4 periodic vortex, 400 SSP-RK3 steps, dJ/dU0 and dJ/dc, 20 snapshots"})
+    return res
+
+
 def run_profile(which):
     """Two SSP-RK3 steps of one mesh on the device (the case the ncu captures use)."""
     import torch
@@ -256,6 +333,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile", choices=["A", "B", "C"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling)")
@@ -396,6 +474,10 @@ def main():
             batched["value"] = world * batched["ndofs"] * 3 / (float(t[0]) * 1e-3)
             batched["serial_value"] = world * batched["ndofs"] * 3 / (float(t[1]) * 1e-3)
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = bench_adjoint()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -411,7 +493,7 @@ def main():
             "config": {"workload": "tgv3d_M0.1_split_chandrashekar_hllc_ssprk3: 32^3 p=3 + 16^3 p=7",
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
             "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
