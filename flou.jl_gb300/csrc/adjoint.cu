@@ -94,7 +94,7 @@ struct Prim {
     double rho, v[3], vv, p, H, a;
 };
 
-template <int DIM>
+template <int DIM, bool SOUND = true>
 __device__ __forceinline__ Prim prim_of(const double* q, double g) {
     Prim P;
     P.rho = q[0];
@@ -108,7 +108,7 @@ __device__ __forceinline__ Prim prim_of(const double* q, double g) {
     P.vv = vv;
     P.p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
     P.H = (q[DIM + 1] + P.p) * ir;
-    P.a = sqrt(g * P.p * ir);
+    P.a = SOUND ? sqrt(g * P.p * ir) : 0.0;
     return P;
 }
 
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
     double q[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
-    Prim pr = prim_of<DIM>(q, P.gamma);
+    Prim pr = prim_of<DIM, false>(q, P.gamma);
     const double g1 = P.gamma - 1.0;
     double qb[NV];
 #pragma unroll
@@ -491,6 +491,7 @@ struct Schedule {
     // C(ss + r, ss) >= nn, put the snapshot so that the remainder fits C(ss - 1 + r, ss - 1).
     int split_of(int nn, int ss) {
         if (dp) return M(nn, ss);
+        if (ss >= nn - 1) return 1;
         auto binom = [](int a, int b) {
             double v = 1.0;
             for (int i = 1; i <= b; ++i) v = v * (a - b + i) / i;
@@ -503,6 +504,10 @@ struct Schedule {
     }
     bool dp = true;
     Schedule(int n_, int s_) : n(n_), s(std::min(s_, std::max(n_ - 1, 0))) {
+        if (s >= n - 1) {   // every state can be kept: advance one step per snapshot
+            dp = false;
+            return;
+        }
         if ((double)n * n * (s + 1) > 2e8) {   // too large for the table: binomial rule below
             dp = false;
             return;
