@@ -1,0 +1,218 @@
+"""
+    FlouCUDA
+
+Drop-in GPU discretization for Flou.jl: `GPUDisc(disc)` wraps a `MultielementDisc` built by
+Flou and hands its arrays to libflou_cuda (the C ABI of `include/flou_cuda.h`). Flou's own
+`rhs!(dQ, Q, EquationConfig(gpudisc, equation), t)` and `timeintegrate` then run on the GPU.
+
+Shipped as source: it is the binding a Flou maintainer adds; it mirrors the Python host
+package `flou_cuda` that the repository tests.
+"""
+module FlouCUDA
+
+using Flou
+using Flou.FlouCommon: AbstractSpatialDiscretization, EquationConfig, HyperbolicEquation
+import Flou.FlouCommon: rhs!, get_max_dt
+using ChainRulesCore
+using LinearAlgebra
+
+export GPUDisc, SSPRK3GPU, GPUBatch, solve_functional
+
+const libflou = joinpath(@__DIR__, "..", "..", "..", "lib", "libflou_cuda.so")
+
+# ---- C structs and status ------------------------------------------------------------------
+struct FlouConfig
+    dim::Int32
+    equation::Int32
+    gamma::Float64
+    advection::NTuple{3,Float64}
+    volume_op::Int32
+    twopoint_flux::Int32
+    numflux::Int32
+    numflux_avg::Int32
+    numflux_intensity::Float64
+    nnodes::Int32
+end
+
+const FLOU_ERR_NONPHYSICAL = 3
+const PTR_HOST = Int32(0)
+const PTR_DEVICE = Int32(1)
+
+function check(status, ctx)
+    status == 0 && return nothing
+    msg = ctx == C_NULL ? "" :
+          unsafe_string(ccall((:flou_last_error, libflou), Cstring, (Ptr{Cvoid},), ctx))
+    status == FLOU_ERR_NONPHYSICAL && throw(DomainError(msg, "non-physical state"))
+    error("libflou_cuda status $status: $msg")
+end
+
+# ---- configuration from Flou's objects -------------------------------------------------------
+eqcode(::LinearAdvection) = Int32(0)
+eqcode(::BurgersEquation) = Int32(1)
+eqcode(::EulerEquation) = Int32(2)
+
+tpcode(::StdAverage) = Int32(0)
+tpcode(::ChandrasekharAverage) = Int32(1)
+
+nfcode(::StdAverage) = Int32(0)
+nfcode(::LxF) = Int32(1)
+nfcode(::ChandrasekharAverage) = Int32(2)
+
+function flou_config(disc, equation)
+    op = disc.operators[1]
+    nf = op.numflux
+    adv = equation isa LinearAdvection ? (Tuple(equation.a)..., zeros(3 - length(equation.a))...) : (0.0, 0.0, 0.0)
+    vol = op isa SplitDivOperator ? Int32(1) : Int32(0)
+    tp = op isa SplitDivOperator ? tpcode(op.tpflux) : Int32(0)
+    avg = nf isa LxF ? (nf.avg isa ChandrasekharAverage ? Int32(2) : Int32(0)) : Int32(0)
+    inten = nf isa LxF ? Float64(nf.intensity) : 1.0
+    gamma = equation isa EulerEquation ? Float64(equation.γ) : 1.4
+    return FlouConfig(Int32(spatialdim(disc)), eqcode(equation), gamma, Float64.(adv), vol, tp,
+                      nfcode(nf), avg, inten, Int32(length(disc.std.basis.ξ)))
+end
+
+# ---- the drop-in discretization --------------------------------------------------------------
+mutable struct GPUDisc{ND,RT,D} <: AbstractSpatialDiscretization{ND,RT}
+    disc::D                 # Flou's MultielementDisc (host arrays come from it)
+    ctx::Ptr{Cvoid}
+end
+
+"""
+    GPUDisc(disc::MultielementDisc, equation)
+
+Uploads the operators (StdSegment.jl:77-89), the connectivity after `apply_periodicBCs!`
+(Mesh.jl:236-322), the boundary conditions and the geometry of `disc` to a libflou_cuda
+context. Only Cartesian geometry is accepted.
+"""
+function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
+    cfg = Ref(flou_config(disc, equation))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:flou_create, libflou), Int32, (Ref{FlouConfig}, Ref{Ptr{Cvoid}}), cfg, out)
+    st == 0 || error("flou_create rejected the configuration (status $st)")
+    ctx = out[]
+    s = disc.std.face isa Flou.StdPoint ? disc.std : disc.std   # segment matrices are shared
+    D, Ds, Dsh = Matrix{Float64}(s.D), Matrix{Float64}(s.Ds), Matrix{Float64}(s.D♯)
+    ω = Vector{Float64}(disc.std.basis.ω)
+    ll, lr = Vector{Float64}(s.l[1]), Vector{Float64}(s.l[2])
+    gl, gr = Vector{Float64}(s.∂g[1]), Vector{Float64}(s.∂g[2])
+    GC.@preserve D Ds Dsh ω ll lr gl gr check(ccall((:flou_set_operators, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}), ctx, D, Ds, Dsh, ω, ll, lr, gl, gr), ctx)
+    mesh = disc.mesh
+    ne, nf = nelements(mesh), nfaces(mesh)
+    faceinds = Int32.(mesh.elements.faceinds)
+    facepos = Int32.(mesh.elements.facepos)
+    eleminds = Int32.(mesh.faces.eleminds)
+    elempos = Int32.(mesh.faces.elempos)
+    orient = UInt8.(mesh.faces.orientation)
+    bdidx = zeros(Int32, nf)
+    for ib in eachboundary(mesh), f in eachbdface(mesh, ib)
+        bdidx[f] = ib
+    end
+    GC.@preserve faceinds facepos eleminds elempos orient bdidx check(ccall((:flou_set_mesh, libflou), Int32,
+        (Ptr{Cvoid}, Int32, Int32, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{UInt8}, Ptr{Int32}),
+        ctx, ne, nf, faceinds, facepos, eleminds, elempos, orient, bdidx), ctx)
+    kinds = Int32[bc isa EulerSlipBC ? 3 : bc isa EulerInflowBC ? 2 : 1 for bc in disc.bcs]
+    states = zeros(Float64, 5, length(kinds))
+    for (i, bc) in enumerate(disc.bcs)
+        bc isa EulerInflowBC && (states[1:length(bc.Qext), i] .= bc.Qext)
+    end
+    GC.@preserve kinds states check(ccall((:flou_set_bcs, libflou), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}), ctx, length(kinds), kinds, states), ctx)
+    g = disc.geometry
+    J = Vector{Float64}(g.elements.jac)
+    Ja = reduce(vcat, (vec(Matrix(M)) for M in g.elements.metric))
+    frames = reduce(vcat, ([f.n..., zeros(3 - ND)..., f.t..., zeros(3 - ND)..., f.b..., zeros(3 - ND)...]
+                           for f in g.faces.frames))
+    fJ = Vector{Float64}(g.faces.jac)
+    GC.@preserve J Ja frames fJ check(ccall((:flou_set_geometry, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx, J, Ja, frames, fJ), ctx)
+    gd = GPUDisc{ND,RT,typeof(disc)}(disc, ctx)
+    finalizer(x -> ccall((:flou_destroy, libflou), Int32, (Ptr{Cvoid},), x.ctx), gd)
+    return gd
+end
+
+# rhs!(dQ, Q, p, t): Flou's residual on the GPU (Hyperbolic.jl:31-69).
+function rhs!(dQ::Matrix{Float64}, Q::Matrix{Float64}, p::EquationConfig{<:GPUDisc}, t::Real)
+    ctx = p.disc.ctx
+    GC.@preserve dQ Q check(ccall((:flou_rhs, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64, Int32), ctx, dQ, Q, t, PTR_HOST), ctx)
+    return nothing
+end
+
+function get_max_dt(q::Matrix{Float64}, disc::GPUDisc, ::Any, cfl)
+    dt = Ref{Float64}(0.0)
+    GC.@preserve q check(ccall((:flou_max_dt, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Float64, Ref{Float64}, Int32), disc.ctx, q, cfl, dt, PTR_HOST), disc.ctx)
+    return dt[]
+end
+
+"SSP-RK3 run entirely on the GPU (one CUDA graph per step)."
+struct SSPRK3GPU end
+
+"""
+    timeintegrate(Q0, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt)
+
+Same contract as Flou's `timeintegrate` (FlouTime.jl:34-54): returns `(sol, exetime)`, logs
+"Simulation crashed!" on a DomainError.
+"""
+function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt, kwargs...)
+    Q = copy(Q0)
+    nsteps = round(Int, tfinal / dt)
+    exetime = @elapsed begin
+        try
+            GC.@preserve Q check(ccall((:flou_step, libflou), Int32,
+                (Ptr{Cvoid}, Ptr{Float64}, Float64, Float64, Int32, Int32), disc.ctx, Q, dt, 0.0, nsteps, PTR_HOST),
+                disc.ctx)
+        catch e
+            e isa DomainError ? (@error "Simulation crashed!") : rethrow()
+        end
+    end
+    return ((t=[0.0, tfinal], u=[Q0, Q]), exetime)
+end
+
+# ---- differentiable terminal functional --------------------------------------------------------
+"""
+    solve_functional(disc, Q0, c, dt, nsteps, ρtarget, w) -> J
+
+J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` SSP-RK3 steps with per-element dissipation scales `c`.
+Differentiable through the `rrule` below (discrete adjoint, binomial checkpointing).
+Arrays are device pointers wrapped by the caller's GPU array package (e.g. CuArray).
+"""
+function solve_functional end
+
+function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, dt, nsteps, ρt, w; nsnap=20)
+    J = Ref{Float64}(0.0)
+    g = similar(Q0)
+    gc = similar(c)
+    nf = Ref{Int64}(0)
+    ccall((:flou_set_dissipation, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32), disc.ctx, pointer(c), PTR_DEVICE)
+    check(ccall((:flou_adjoint_solve, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ref{Int64}),
+        disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), pointer(gc), nf), disc.ctx)
+    pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, J̄ .* gc, NoTangent(), NoTangent(), NoTangent(), NoTangent())
+    return J[], pullback
+end
+
+# ---- batched mode --------------------------------------------------------------------------------
+mutable struct GPUBatch
+    h::Ptr{Cvoid}
+    discs::Vector{GPUDisc}
+end
+
+function GPUBatch(discs::Vector{<:GPUDisc}, states, dts::Vector{Float64})
+    ctxs = [d.ctx for d in discs]
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:flou_batch_create, libflou), Int32, (Int32, Ptr{Ptr{Cvoid}}, Ref{Ptr{Cvoid}}), length(ctxs), ctxs, out)
+    st == 0 || error("flou_batch_create failed ($st)")
+    ptrs = [pointer(q) for q in states]
+    ccall((:flou_batch_set_states, libflou), Int32, (Ptr{Cvoid}, Ptr{Ptr{Float64}}, Ptr{Float64}), out[], ptrs, dts)
+    b = GPUBatch(out[], discs)
+    finalizer(x -> ccall((:flou_batch_destroy, libflou), Int32, (Ptr{Cvoid},), x.h), b)
+    return b
+end
+
+step!(b::GPUBatch, nsteps) = ccall((:flou_batch_step, libflou), Int32, (Ptr{Cvoid}, Int32), b.h, nsteps)
+
+end # module
