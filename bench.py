@@ -37,6 +37,20 @@ NV = 5
 BYTES_PER_DOF_STAGE = (8.0 / 3.0) * NV * 8   # compulsory state traffic, fused SSP-RK3
 
 
+def replica_throughput(local_ms, local_units, dist=None, device=None):
+    """Replicas of the workload, one per rank, no data exchange: the job's throughput is the
+    units all ranks processed divided by the slowest rank's time.  Returns (value, max_ms)."""
+    if dist is None:
+        return local_units / (local_ms * 1e-3), local_ms
+    import torch
+    t = torch.tensor([local_ms, local_units], dtype=torch.float64, device=device)
+    mx = t[:1].clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    tot = t[1:].clone()
+    dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+    return float(tot) / (float(mx) * 1e-3), float(mx)
+
+
 def make_tgv(nel, n, mach=0.1):
     import flou_cuda as F
     eq = F.EulerEquation(3, 1.4)
@@ -400,11 +414,7 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ndofs * 3 * steps / (ms * 1e-3)
+    value, ms = replica_throughput(ms, ndofs * 3 * steps, dist, "cuda")
 
     # ---- per-kernel timing for the roofline (CUDA events around single launches) ----
     kern = {}
@@ -457,23 +467,17 @@ def main():
             m["ctx"].step(h, m["dt"], 1)
     barrier()
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_value, _ = replica_throughput(e2e_s * 1e3, ndofs * 3 * steps, dist, "cuda")
     state_bytes = sum(m["ndofs"] * NV * 8 for m in meshes)
-    e2e = {"value": world * ndofs * 3 * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
-           "d2h_bytes_per_step": state_bytes}
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}
 
     batched = None
     if not args.no_batched:
         batched = bench_batched(steps, warmup)
-        if dist is not None:
-            t = torch.tensor([batched["ms_per_step"], batched["serial_ms_per_step"]], device="cuda",
-                             dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            batched["value"] = world * batched["ndofs"] * 3 / (float(t[0]) * 1e-3)
-            batched["serial_value"] = world * batched["ndofs"] * 3 / (float(t[1]) * 1e-3)
+        units = batched["ndofs"] * 3
+        batched["value"], _ = replica_throughput(batched["ms_per_step"], units, dist, "cuda")
+        batched["serial_value"], _ = replica_throughput(batched["serial_ms_per_step"], units, dist, "cuda")
+        batched["speedup_vs_serial"] = batched["value"] / batched["serial_value"]
 
     adjoint = None
     if not args.no_adjoint:

@@ -221,6 +221,130 @@ __global__ void fma_probe_kernel(double* sink, int iters, double x) {
     if (s == 1234.5678) sink[threadIdx.x] = s;   // never true; keeps the chains alive
 }
 
+// Validates Flou's 1-based connectivity and packs it for the kernels (no CUDA involved):
+//   ef[e*2d + k] = (face << 1) | side,  fe[2f + s] = (elem << 3) | local position (-1: none),
+//   fb[f] = boundary index (0-based) or -1.
+int validate_pack_mesh(int dim, int32_t nelem, int32_t nfaces, const int32_t* faceinds, const int32_t* facepos,
+                       const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
+                       const int32_t* bdface_index, std::vector<int32_t>& ef, std::vector<int32_t>& fe,
+                       std::vector<int8_t>& fb, std::string& msg) {
+    char buf[256];
+    auto bad = [&](int code, const char* fmt, int a, int b, int c2, int d) {
+        snprintf(buf, sizeof(buf), fmt, a, b, c2, d);
+        msg = buf;
+        return code;
+    };
+    if (dim < 1 || dim > 3) return bad(FLOU_ERR_ARG, "invalid dimension %d", dim, 0, 0, 0);
+    int nfpe = 2 * dim;
+    if (nelem <= 0 || nfaces <= 0 || nelem >= (1 << 27))
+        return bad(FLOU_ERR_ARG, "invalid sizes nelem=%d nfaces=%d", nelem, nfaces, 0, 0);
+    if (!faceinds || !facepos || !eleminds || !elempos || !orientation || !bdface_index)
+        return bad(FLOU_ERR_ARG, "null connectivity pointer", 0, 0, 0, 0);
+    ef.assign((size_t)nelem * nfpe, 0);
+    fe.assign((size_t)nfaces * 2, -1);
+    fb.assign(nfaces, -1);
+    for (int f = 0; f < nfaces; ++f) {
+        if (orientation[f] != 0)
+            return bad(FLOU_ERR_UNSUPPORTED, "face %d has orientation %d; only conforming Cartesian faces "
+                       "(orientation 0) are supported", f + 1, (int)orientation[f], 0, 0);
+        for (int s = 0; s < 2; ++s) {
+            int e = eleminds[2 * f + s], p = elempos[2 * f + s];
+            if (s == 1 && e == 0) continue;
+            if (e < 1 || e > nelem || p < 1 || p > nfpe)
+                return bad(FLOU_ERR_ARG, "face %d side %d: element %d / position %d out of range", f + 1, s + 1, e, p);
+            if (faceinds[(size_t)(e - 1) * nfpe + p - 1] != f + 1 || facepos[(size_t)(e - 1) * nfpe + p - 1] != s + 1)
+                return bad(FLOU_ERR_ARG, "face %d side %d is not face %d of element %d in faceinds/facepos", f + 1,
+                           s + 1, p, e);
+            fe[2 * f + s] = ((e - 1) << 3) | (p - 1);
+        }
+        int b = bdface_index[f];
+        if (eleminds[2 * f + 1] == 0) {
+            if (b < 1 || b > MAXBC) return bad(FLOU_ERR_ARG, "boundary face %d has boundary index %d", f + 1, b, 0, 0);
+            fb[f] = (int8_t)(b - 1);
+        } else if (b != 0) {
+            return bad(FLOU_ERR_ARG, "interior face %d has boundary index %d", f + 1, b, 0, 0);
+        }
+    }
+    for (int e = 0; e < nelem; ++e)
+        for (int k = 0; k < nfpe; ++k) {
+            int f = faceinds[(size_t)e * nfpe + k], s = facepos[(size_t)e * nfpe + k];
+            if (f < 1 || f > nfaces || s < 1 || s > 2)
+                return bad(FLOU_ERR_ARG, "element %d face %d: face %d / side %d out of range", e + 1, k + 1, f, s);
+            if (eleminds[2 * (f - 1) + s - 1] != e + 1 || elempos[2 * (f - 1) + s - 1] != k + 1)
+                return bad(FLOU_ERR_ARG, "element %d face %d does not point back through eleminds/elempos", e + 1,
+                           k + 1, 0, 0);
+            ef[(size_t)e * nfpe + k] = ((f - 1) << 1) | (s - 1);
+        }
+    return FLOU_OK;
+}
+
+// Validates Cartesian geometry (J and a diagonal metric constant per element, one frame and one
+// surface Jacobian per face, the frame being the Cartesian frame of the face's master side) and
+// compresses it: invJ[nelem], Jd[nelem*dim], fJ[nfaces], dx[nelem] (get_max_dt length scale).
+int validate_pack_geometry(int dim, int n, int32_t nelem, int32_t nfaces, const double* omega,
+                           const std::vector<int32_t>& fe, const double* J, const double* Ja, const double* frames,
+                           const double* face_J, std::vector<double>& invJ, std::vector<double>& Jd,
+                           std::vector<double>& fJ, std::vector<double>& dx, std::string& msg) {
+    char buf[256];
+    auto bad = [&](int code, const char* fmt, int a) {
+        snprintf(buf, sizeof(buf), fmt, a);
+        msg = buf;
+        return code;
+    };
+    if (!J || !Ja || !frames || !face_J || !omega) return bad(FLOU_ERR_ARG, "null geometry pointer%.0d", 0);
+    int npe = ipow(n, dim), nfd = ipow(n, dim - 1);
+    invJ.assign(nelem, 0.0);
+    Jd.assign((size_t)nelem * dim, 0.0);
+    fJ.assign(nfaces, 0.0);
+    dx.assign(nelem, 0.0);
+    for (int e = 0; e < nelem; ++e) {
+        const double* Je = J + (size_t)e * npe;
+        const double* Me = Ja + (size_t)e * npe * dim * dim;
+        for (int i = 0; i < npe; ++i) {
+            if (Je[i] != Je[0])
+                return bad(FLOU_ERR_UNSUPPORTED, "element %d: the Jacobian varies within the element "
+                           "(curvilinear geometry is not supported)", e + 1);
+            for (int q = 0; q < dim * dim; ++q) {
+                double v = Me[(size_t)i * dim * dim + q];
+                bool diag = (q % (dim + 1)) == 0;
+                if ((!diag && v != 0.0) || v != Me[q])
+                    return bad(FLOU_ERR_UNSUPPORTED, "element %d: the metric is not diagonal and constant "
+                               "(curvilinear geometry is not supported)", e + 1);
+            }
+        }
+        if (!(Je[0] > 0.0) || !std::isfinite(Je[0])) return bad(FLOU_ERR_ARG, "element %d: J <= 0", e + 1);
+        invJ[e] = 1.0 / Je[0];
+        for (int d = 0; d < dim; ++d) Jd[(size_t)e * dim + d] = Me[d * (dim + 1)];
+        // get_max_dt length scale: (Σ J ω / n^d)^(1/d), MultielementDiscontinuous.jl:169-171
+        double vol = 0.0;
+        for (int i = 0; i < npe; ++i) {
+            double w = 1.0;
+            int r = i;
+            for (int d = 0; d < dim; ++d) { w *= omega[r % n]; r /= n; }
+            vol += Je[i] * w;
+        }
+        double h = vol / npe;
+        dx[e] = dim == 1 ? h : (dim == 2 ? std::sqrt(h) : std::cbrt(h));
+    }
+    for (int f = 0; f < nfaces; ++f) {
+        FrameTab T = frame_of(dim, fe[2 * f] & 7);
+        for (int m = 0; m < nfd; ++m) {
+            size_t idx = (size_t)f * nfd + m;
+            if (face_J[idx] != face_J[(size_t)f * nfd])
+                return bad(FLOU_ERR_UNSUPPORTED, "face %d: the surface Jacobian varies along the face", f + 1);
+            const double* fr = frames + idx * 9;
+            for (int q = 0; q < 3; ++q) {
+                bool ok = (q >= dim || (fr[q] == T.n[q] && fr[3 + q] == T.t[q] && (dim < 3 || fr[6 + q] == T.b[q])));
+                if (!ok)
+                    return bad(FLOU_ERR_UNSUPPORTED, "face %d: the frame is not the Cartesian frame of its master "
+                               "side (curvilinear geometry is not supported)", f + 1);
+            }
+        }
+        fJ[f] = face_J[(size_t)f * nfd];
+    }
+    return FLOU_OK;
+}
+
 }  // namespace
 
 namespace flou {
@@ -342,46 +466,12 @@ int32_t flou_set_mesh(flou_ctx* c, int32_t nelem, int32_t nfaces, const int32_t*
                       const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
                       const int32_t* bdface_index) {
     if (!c) return FLOU_ERR_ARG;
-    int dim = c->cfg.dim, nfpe = 2 * dim;
-    if (nelem <= 0 || nfaces <= 0 || nelem >= (1 << 27))
-        return fail(c, FLOU_ERR_ARG, "invalid sizes nelem=%d nfaces=%d", nelem, nfaces);
-    if (!faceinds || !facepos || !eleminds || !elempos || !orientation || !bdface_index)
-        return fail(c, FLOU_ERR_ARG, "null connectivity pointer");
-    std::vector<int32_t> ef((size_t)nelem * nfpe), fe((size_t)nfaces * 2);
-    std::vector<int8_t> fb(nfaces, -1);
-    for (int f = 0; f < nfaces; ++f) {
-        if (orientation[f] != 0)
-            return fail(c, FLOU_ERR_UNSUPPORTED, "face %d has orientation %d; only conforming Cartesian faces "
-                        "(orientation 0) are supported", f + 1, (int)orientation[f]);
-        for (int s = 0; s < 2; ++s) {
-            int e = eleminds[2 * f + s], p = elempos[2 * f + s];
-            if (s == 1 && e == 0) { fe[2 * f + 1] = -1; continue; }
-            if (e < 1 || e > nelem || p < 1 || p > nfpe)
-                return fail(c, FLOU_ERR_ARG, "face %d side %d: element %d / position %d out of range", f + 1, s + 1, e, p);
-            if (faceinds[(size_t)(e - 1) * nfpe + p - 1] != f + 1 || facepos[(size_t)(e - 1) * nfpe + p - 1] != s + 1)
-                return fail(c, FLOU_ERR_ARG, "face %d side %d is not face %d of element %d in faceinds/facepos",
-                            f + 1, s + 1, p, e);
-            fe[2 * f + s] = ((e - 1) << 3) | (p - 1);
-        }
-        int b = bdface_index[f];
-        if (eleminds[2 * f + 1] == 0) {
-            if (b < 1 || b > MAXBC) return fail(c, FLOU_ERR_ARG, "boundary face %d has boundary index %d", f + 1, b);
-            fb[f] = (int8_t)(b - 1);
-        } else if (b != 0) {
-            return fail(c, FLOU_ERR_ARG, "interior face %d has boundary index %d", f + 1, b);
-        }
-    }
-    for (int e = 0; e < nelem; ++e)
-        for (int k = 0; k < nfpe; ++k) {
-            int f = faceinds[(size_t)e * nfpe + k], s = facepos[(size_t)e * nfpe + k];
-            if (f < 1 || f > nfaces || s < 1 || s > 2)
-                return fail(c, FLOU_ERR_ARG, "element %d face %d: face %d / side %d out of range", e + 1, k + 1, f, s);
-            if (eleminds[2 * (f - 1) + s - 1] != e + 1 || elempos[2 * (f - 1) + s - 1] != k + 1)
-                return fail(c, FLOU_ERR_ARG, "element %d face %d does not point back through eleminds/elempos",
-                            e + 1, k + 1);
-            ef[(size_t)e * nfpe + k] = ((f - 1) << 1) | (s - 1);
-        }
-    int r;
+    std::vector<int32_t> ef, fe;
+    std::vector<int8_t> fb;
+    std::string msg;
+    int r = validate_pack_mesh(c->cfg.dim, nelem, nfaces, faceinds, facepos, eleminds, elempos, orientation,
+                               bdface_index, ef, fe, fb, msg);
+    if (r) return fail(c, r, "%s", msg.c_str());
     if ((r = upload(c, &c->d_elem_face, ef.data(), ef.size(), "mesh upload"))) return r;
     if ((r = upload(c, &c->d_face_elem, fe.data(), fe.size(), "mesh upload"))) return r;
     if ((r = upload(c, &c->d_face_bc, fb.data(), fb.size(), "mesh upload"))) return r;
@@ -390,6 +480,7 @@ int32_t flou_set_mesh(flou_ctx* c, int32_t nelem, int32_t nfaces, const int32_t*
     for (double** b : sized)
         if (*b) { cudaFree(*b); *b = nullptr; }
     c->h_face_bc = fb;
+    c->h_face_elem = fe;
     c->nelem = nelem;
     c->nfaces = nfaces;
     c->ndofs = (int64_t)nelem * c->npe;
@@ -425,57 +516,11 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     if (!c) return FLOU_ERR_ARG;
     if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh must come before flou_set_geometry");
     if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators must come before flou_set_geometry");
-    if (!J || !Ja || !frames || !face_J) return fail(c, FLOU_ERR_ARG, "null geometry pointer");
-    int dim = c->cfg.dim, npe = c->npe, nfd = c->nfd;
-    std::vector<double> invJ(c->nelem), Jd((size_t)c->nelem * dim), fJ(c->nfaces), dx(c->nelem);
-    std::vector<int32_t> fe((size_t)c->nfaces * 2);
-    CK(cudaMemcpy(fe.data(), c->d_face_elem, fe.size() * sizeof(int32_t), cudaMemcpyDeviceToHost), "mesh readback");
-    for (int e = 0; e < c->nelem; ++e) {
-        const double* Je = J + (size_t)e * npe;
-        const double* Me = Ja + (size_t)e * npe * dim * dim;
-        for (int i = 0; i < npe; ++i) {
-            if (Je[i] != Je[0])
-                return fail(c, FLOU_ERR_UNSUPPORTED, "element %d: the Jacobian varies within the element "
-                            "(curvilinear geometry is not supported)", e + 1);
-            for (int q = 0; q < dim * dim; ++q) {
-                double v = Me[(size_t)i * dim * dim + q];
-                bool diag = (q % (dim + 1)) == 0;
-                if ((!diag && v != 0.0) || v != Me[q])
-                    return fail(c, FLOU_ERR_UNSUPPORTED, "element %d: the metric is not diagonal and constant "
-                                "(curvilinear geometry is not supported)", e + 1);
-            }
-        }
-        if (!(Je[0] > 0.0) || !std::isfinite(Je[0])) return fail(c, FLOU_ERR_ARG, "element %d: J <= 0", e + 1);
-        invJ[e] = 1.0 / Je[0];
-        for (int d = 0; d < dim; ++d) Jd[(size_t)e * dim + d] = Me[d * (dim + 1)];
-        // get_max_dt length scale: (Σ J ω / n^d)^(1/d), MultielementDiscontinuous.jl:169-171
-        double vol = 0.0;
-        for (int i = 0; i < npe; ++i) {
-            double w = 1.0;
-            int r = i;
-            for (int d = 0; d < dim; ++d) { w *= c->omega[r % c->n]; r /= c->n; }
-            vol += Je[i] * w;
-        }
-        double h = vol / npe;
-        dx[e] = dim == 1 ? h : (dim == 2 ? std::sqrt(h) : std::cbrt(h));
-    }
-    for (int f = 0; f < c->nfaces; ++f) {
-        FrameTab T = frame_of(dim, fe[2 * f] & 7);
-        for (int m = 0; m < nfd; ++m) {
-            size_t idx = (size_t)f * nfd + m;
-            if (face_J[idx] != face_J[(size_t)f * nfd])
-                return fail(c, FLOU_ERR_UNSUPPORTED, "face %d: the surface Jacobian varies along the face", f + 1);
-            const double* fr = frames + idx * 9;
-            for (int q = 0; q < 3; ++q) {
-                bool ok = (q >= dim || (fr[q] == T.n[q] && fr[3 + q] == T.t[q] && (dim < 3 || fr[6 + q] == T.b[q])));
-                if (!ok)
-                    return fail(c, FLOU_ERR_UNSUPPORTED, "face %d: the frame is not the Cartesian frame of its master "
-                                "side (curvilinear geometry is not supported)", f + 1);
-            }
-        }
-        fJ[f] = face_J[(size_t)f * nfd];
-    }
-    int r;
+    std::vector<double> invJ, Jd, fJ, dx;
+    std::string msg;
+    int r = validate_pack_geometry(c->cfg.dim, c->n, c->nelem, c->nfaces, c->omega.data(), c->h_face_elem, J, Ja,
+                                   frames, face_J, invJ, Jd, fJ, dx, msg);
+    if (r) return fail(c, r, "%s", msg.c_str());
     if ((r = upload(c, &c->d_invJ, invJ.data(), invJ.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_Ja, Jd.data(), Jd.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;
@@ -648,6 +693,43 @@ int32_t flou_time_kernels(flou_ctx* c, const double* Q, int32_t nrep, double* fa
     *face_ms = tf / (3.0 * nrep);
     *elem_ms = te / (3.0 * nrep);
     return check_status(c);
+}
+
+static int32_t copy_msg(const std::string& m, char* out, int32_t len) {
+    if (out && len > 0) {
+        size_t k = std::min((size_t)(len - 1), m.size());
+        memcpy(out, m.data(), k);
+        out[k] = 0;
+    }
+    return 0;
+}
+
+int32_t flou_check_mesh(int32_t dim, int32_t nelem, int32_t nfaces, const int32_t* faceinds, const int32_t* facepos,
+                        const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
+                        const int32_t* bdface_index, char* msg, int32_t msglen) {
+    std::vector<int32_t> ef, fe;
+    std::vector<int8_t> fb;
+    std::string m;
+    int r = validate_pack_mesh(dim, nelem, nfaces, faceinds, facepos, eleminds, elempos, orientation, bdface_index, ef,
+                               fe, fb, m);
+    copy_msg(m, msg, msglen);
+    return r;
+}
+
+int32_t flou_check_geometry(int32_t dim, int32_t nnodes, int32_t nelem, int32_t nfaces, const int32_t* elempos,
+                            const double* omega, const double* J, const double* Ja, const double* frames,
+                            const double* face_J, char* msg, int32_t msglen) {
+    if (!elempos || nfaces <= 0 || nelem <= 0 || nnodes < 2 || nnodes > MAXN || dim < 1 || dim > 3) {
+        copy_msg("invalid arguments", msg, msglen);
+        return FLOU_ERR_ARG;
+    }
+    std::vector<int32_t> fe((size_t)nfaces * 2, -1);
+    for (int f = 0; f < nfaces; ++f) fe[2 * f] = elempos[2 * f] - 1;   // only the master position is used
+    std::vector<double> invJ, Jd, fJ, dx;
+    std::string m;
+    int r = validate_pack_geometry(dim, nnodes, nelem, nfaces, omega, fe, J, Ja, frames, face_J, invJ, Jd, fJ, dx, m);
+    copy_msg(m, msg, msglen);
+    return r;
 }
 
 int32_t flou_fp64_peak(double* gflops) {

@@ -26,6 +26,7 @@ struct flou_ctx {
     int bc_kind[flou::MAXBC] = {0};
     double bc_state[flou::MAXBC][5] = {{0}};
     std::vector<int8_t> h_face_bc;
+    std::vector<int32_t> h_face_elem;   // packed face -> element table (host copy)
     // device buffers
     double* d_ops = nullptr;        // Ds, D♯, l_l, l_r, dg_l, dg_r
     int32_t* d_elem_face = nullptr;

@@ -88,6 +88,10 @@ PROTOTYPES = {
     "flou_rhs_noalloc": [_P, _P, _P, ctypes.c_double],
     "flou_fp64_peak": [_D],
     "flou_set_dissipation": [_P, _P, ctypes.c_int32],
+    "flou_check_mesh": [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32, _I32, _U8, _I32,
+                        ctypes.c_char_p, ctypes.c_int32],
+    "flou_check_geometry": [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _I32, _D, _D, _D, _D, _D,
+                            ctypes.c_char_p, ctypes.c_int32],
     "flou_rhs_vjp": [_P, _P, _P, _P, _P],
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
     "flou_batch_create": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P)],

@@ -169,6 +169,16 @@ int32_t flou_take_status(flou_ctx* ctx, int32_t* flags, int32_t* elem);
  * one launch in milliseconds.  No counterpart in the reference (measurement hook). */
 int32_t flou_time_kernels(flou_ctx* ctx, const double* Q, int32_t nrep, double* face_ms, double* elem_ms);
 
+/* Host-only validation (no GPU needed) of the set-up arrays exactly as flou_set_mesh /
+ * flou_set_geometry check them; msg receives the reason (may be NULL).  No counterpart in the
+ * reference (Flou's constructors build these arrays themselves). */
+int32_t flou_check_mesh(int32_t dim, int32_t nelem, int32_t nfaces, const int32_t* faceinds, const int32_t* facepos,
+                        const int32_t* eleminds, const int32_t* elempos, const uint8_t* orientation,
+                        const int32_t* bdface_index, char* msg, int32_t msglen);
+int32_t flou_check_geometry(int32_t dim, int32_t nnodes, int32_t nelem, int32_t nfaces, const int32_t* elempos,
+                            const double* omega, const double* J, const double* Ja, const double* frames,
+                            const double* face_J, char* msg, int32_t msglen);
+
 /* Measured FP64 fused-multiply-add throughput of the current device in GFLOP/s (2 flops per
  * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
 int32_t flou_fp64_peak(double* gflops);
