@@ -50,10 +50,14 @@ def smooth_euler_state(disc, seed=0, amp=0.1):
 
 
 def rel_linf(a, b):
-    """max_v max_i |a - b| / max_i |b| (per variable, relative to the reference's scale)."""
+    """Relative L-inf error per variable: max_v max_i |a - b| / s_v with s_v = max_i |b_v|, floored
+    at 1e-3 of the largest |b| over all variables.  The floor only matters for a component whose
+    reference is round-off (e.g. the density residual of a divergence-free field at constant
+    density), where a relative error of round-off against round-off carries no information."""
     a = np.asarray(a).reshape(b.shape, order="F") if np.asarray(a).shape != b.shape else np.asarray(a)
+    smax = np.max(np.abs(b)) if b.size else 0.0
     out = 0.0
     for v in range(b.shape[1]):
-        s = np.max(np.abs(b[:, v]))
+        s = max(np.max(np.abs(b[:, v])), 1e-3 * smax)
         out = max(out, np.max(np.abs(a[:, v] - b[:, v])) / (s if s > 0 else 1.0))
     return out

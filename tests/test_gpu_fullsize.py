@@ -56,10 +56,10 @@ def test_tgv_conservation_freestream_determinism(tgv):
     dQ = torch.empty_like(Qd)
     disc.ctx.rhs(dQ, Qd)
     w = torch.from_numpy(np.tile(disc.std.omega, disc.mesh.nelements) * disc.J).cuda()
+    scales = [float(torch.sum(w * torch.abs(dQ[v]))) for v in range(5)]
     for v in range(5):
         total = float(torch.sum(w * dQ[v]))
-        scale = float(torch.sum(w * torch.abs(dQ[v])))
-        assert abs(total) <= 1e-12 * scale
+        assert abs(total) <= 1e-12 * max(scales[v], 1e-3 * max(scales))
     again = torch.empty_like(Qd)
     disc.ctx.rhs(again, Qd)
     assert torch.equal(again, dQ)
