@@ -578,7 +578,7 @@ int32_t flou_rhs(flou_ctx* c, double* dQ, const double* Q, double t, int32_t ptr
     return check_status(c);
 }
 
-int32_t flou_step(flou_ctx* c, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind) {
+int32_t flou_step_async(flou_ctx* c, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind) {
     (void)t0;
     int r = ready(c);
     if (r) return r;
@@ -615,6 +615,18 @@ int32_t flou_step(flou_ctx* c, double* Q, double dt, double t0, int32_t nsteps, 
     for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
     if (ptr_kind == FLOU_PTR_HOST)
         CK(cudaMemcpyAsync(Q, c->d_Qh, bytes, cudaMemcpyDeviceToHost, c->stream), "state download");
+    return FLOU_OK;
+}
+
+int32_t flou_wait(flou_ctx* c) {
+    if (!c) return FLOU_ERR_ARG;
+    return check_status(c);
+}
+
+int32_t flou_step(flou_ctx* c, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind) {
+    int r = flou_step_async(c, Q, dt, t0, nsteps, ptr_kind);
+    if (r) return r;
+    if (nsteps == 0) return FLOU_OK;
     return check_status(c);
 }
 

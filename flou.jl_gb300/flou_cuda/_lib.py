@@ -81,6 +81,8 @@ PROTOTYPES = {
     "flou_set_geometry": [_P, _D, _D, _D, _D],
     "flou_rhs": [_P, _P, _P, ctypes.c_double, ctypes.c_int32],
     "flou_step": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32],
+    "flou_step_async": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32],
+    "flou_wait": [_P],
     "flou_max_dt": [_P, _P, ctypes.c_double, _D, ctypes.c_int32],
     "flou_sizes": [_P, _I64, _I32, _I32, _I32],
     "flou_take_status": [_P, _I32, _I32],

@@ -228,6 +228,14 @@ class Context:
         pq, kq = self._ptr(Q, True)
         L.check(self._lib.flou_step(self.h, pq, float(dt), float(t0), int(nsteps), kq), self.h)
 
+    def step_async(self, Q, dt, nsteps, t0=0.0):
+        """Queue `nsteps` steps (and, for host memory, the copies) without waiting; see wait()."""
+        pq, kq = self._ptr(Q, True)
+        L.check(self._lib.flou_step_async(self.h, pq, float(dt), float(t0), int(nsteps), kq), self.h)
+
+    def wait(self):
+        L.check(self._lib.flou_wait(self.h), self.h)
+
     def max_dt(self, Q, cfl):
         pq, kq = self._ptr(Q)
         out = ctypes.c_double()

@@ -144,6 +144,14 @@ int32_t flou_rhs(flou_ctx* ctx, double* dQ, const double* Q, double t, int32_t p
  * value (Flou raises a DomainError there, FlouTime.jl:37-51). */
 int32_t flou_step(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind);
 
+/* flou_step without the final synchronisation: the copies (host pointers; use pinned memory
+ * for them to overlap) and the steps are queued on the context's stream and the call returns.
+ * The state must stay untouched until flou_wait(ctx), which synchronises and reports the status
+ * (FLOU_ERR_NONPHYSICAL as flou_step would).  Contexts on different streams overlap one
+ * another's copies and kernels.  No counterpart in the reference. */
+int32_t flou_step_async(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind);
+int32_t flou_wait(flou_ctx* ctx);
+
 /* get_max_dt(q, disc, eq, cfl) (src/FlouSpatial/MultielementDiscontinuous.jl:162-178). */
 int32_t flou_max_dt(flou_ctx* ctx, const double* Q, double cfl, double* dt, int32_t ptr_kind);
 
