@@ -13,6 +13,12 @@
 //   (a) Ū2 = 2/3 Ū3 + VJP(U2; 2/3 dt Ū3),  B = 1/3 Ū3
 //   (b) Ū1 = 1/4 Ū2 + VJP(U1; 1/4 dt Ū2),  B += 3/4 Ū2
 //   (c) Ū0 = Ū1 + B + VJP(U0; dt Ū1)
+// Split form (OpDivergence.jl:200-282 with the Chandrashekar flux of Euler.jl:474-536): the
+// volume term -Ja_d Σ_j D♯(i,j) F♯(Q_i, Q_j) has, for a symmetric pair (a, b) of a line, the
+// flux cotangent F̄ = -Ja_d (D♯(a,b) w_a + D♯(b,a) w_b); its VJP goes to the primitive
+// variables (ρ, v, β = ρ/(2p)) of both nodes and from there to the conserved ones.  The
+// LxF(Chandrashekar) interface flux differentiates the same pair flux (3D keeps the
+// reference's mean of |v|² as written, Euler.jl:216).
 // Non-smooth points follow Julia's Base (what ForwardDiff differentiates on the reference's
 // CPU path): max(a, b) takes b unless b < a; d|u|/du = -1 if u has its sign bit set, else +1.
 #include <cuda_runtime.h>
@@ -20,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -124,7 +131,105 @@ __device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa
     qb[DIM + 1] += kappa * ca;
 }
 
+// Logarithmic mean (Utilities.jl:34-44) with its partial derivatives:
+//   u = ((a-b)/(a+b))²;  u < 0.01: L = (a+b)/(2F), F = 1+u/3+u²/5+u³/7,
+//     ∂L/∂a = 1/(2F) - 2F'(u) f b/(F² (a+b)),  ∂L/∂b = 1/(2F) + 2F'(u) f a/(F² (a+b));
+//   else L = (a-b)/ℓ, ℓ = ln(a/b):  ∂L/∂a = 1/ℓ - (a-b)/(ℓ² a),  ∂L/∂b = -1/ℓ + (a-b)/(ℓ² b).
+__device__ __forceinline__ void logmean_d(double a, double b, double& L, double& da, double& db) {
+    double s = a + b, dd = a - b, is = 1.0 / s, f = dd * is, u = f * f;
+    if (u < 0.01) {
+        double F = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        double iF = 1.0 / F;
+        L = 0.5 * s * iF;
+        double Fp = fma(u, fma(u, 3.0 / 7.0, 0.4), 1.0 / 3.0);
+        double t = 2.0 * Fp * f * iF * iF * is;
+        da = fma(-t, b, 0.5 * iF);
+        db = fma(t, a, 0.5 * iF);
+    } else {
+        double l = log(a / b), il = 1.0 / l;
+        L = dd * il;
+        double t = L * il;
+        da = il - t / a;
+        db = t / b - il;
+    }
+}
+
+// Cotangent of one node's primitive variables (ρ, v, β).
+struct PrimBar {
+    double r, v[3], b;
+};
+
+// VJP of the Chandrashekar pair flux along d, F = [m, m v̄ + p̂ e_d, m h] with
+//   m = ρ̂ v̄_d, ρ̂ = ln-mean(ρ), β̂ = ln-mean(β), p̂ = (ρ1+ρ2)/(2(β1+β2)), v̄ = (v1+v2)/2,
+//   h = 1/(2β̂(γ-1)) - S/4 + p̂/ρ̂ + |v̄|²,  S = |v1|² + |v2|²
+// (WL2: S = |v1|² + |v2|² - v2_z² + v1_z², the 3D interface average of Euler.jl:216).
+// SIDES = 1 returns the cotangent of side 1 only.
+template <int DIM, int SIDES, bool WL2>
+__device__ __forceinline__ void chandra_pair_vjp(int d, double r1, const double* v1, double b1, double r2,
+                                                 const double* v2, double b2, double g, const double* Fb,
+                                                 PrimBar& o1, PrimBar& o2) {
+    double rho, dra, drb, beta, dba, dbb;
+    logmean_d(r1, r2, rho, dra, drb);
+    logmean_d(b1, b2, beta, dba, dbb);
+    double isb = 1.0 / (b1 + b2);
+    double p = 0.5 * (r1 + r2) * isb;
+    double va[DIM], S = 0.0, vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        va[k] = 0.5 * (v1[k] + v2[k]);
+        vv = fma(va[k], va[k], vv);
+        S = fma(v1[k], v1[k], fma(v2[k], v2[k], S));
+    }
+    if (WL2 && DIM == 3) S = S + (v1[2] * v1[2] - v2[2] * v2[2]);
+    double irho = 1.0 / rho, ibeta = 1.0 / beta, cb = 0.5 / (g - 1.0);
+    double h = fma(cb, ibeta, -0.25 * S) + fma(p, irho, vv);
+    double m = rho * va[d];
+    double mb = fma(Fb[DIM + 1], h, Fb[0]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], va[k], mb);
+    double hb = m * Fb[DIM + 1];
+    double vab[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vab[k] = fma(m, Fb[1 + k], 2.0 * hb * va[k]);
+    vab[d] = fma(mb, rho, vab[d]);
+    double pb = fma(hb, irho, Fb[1 + d]);
+    double rhob = fma(mb, va[d], -hb * p * irho * irho);
+    double betab = -hb * cb * ibeta * ibeta;
+    double pr = 0.5 * pb * isb, pbb = -pb * p * isb;
+    o1.r = fma(rhob, dra, pr);
+    o1.b = fma(betab, dba, pbb);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o1.v[k] = 0.5 * fma(-hb, v1[k], vab[k]);
+    if (WL2 && DIM == 3) o1.v[2] -= 0.5 * hb * v1[2];
+    if (SIDES == 2) {
+        o2.r = fma(rhob, drb, pr);
+        o2.b = fma(betab, dbb, pbb);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) o2.v[k] = 0.5 * fma(-hb, v2[k], vab[k]);
+        if (WL2 && DIM == 3) o2.v[2] += 0.5 * hb * v2[2];
+    }
+}
+
+// q̄ += (∂(ρ, v, β)/∂q)ᵀ (ρ̄, v̄, β̄) with β = ρ/(2p):
+//   ρ̄' = ρ̄ + β̄/(2p),  p̄ = -β̄ β/p,
+//   q̄_ρ += ρ̄' - v·v̄/ρ + (γ-1)|v|²/2 p̄,  q̄_mk += v̄_k/ρ - (γ-1) v_k p̄,  q̄_E += (γ-1) p̄.
 template <int DIM>
+__device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, double vv, double p, double g1,
+                                                 const PrimBar& o, double* qb) {
+    double ip = 1.0 / p, ir = 1.0 / rho;
+    double rb = fma(0.5 * ip, o.b, o.r);
+    double pb = -o.b * (0.5 * rho * ip) * ip * g1;   // (γ-1) p̄
+    double vvb = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vvb = fma(v[k], o.v[k], vvb);
+        qb[1 + k] += fma(o.v[k], ir, -v[k] * pb);
+    }
+    qb[0] += fma(0.5 * vv, pb, fma(-vvb, ir, rb));
+    qb[DIM + 1] += pb;
+}
+
+template <int DIM, bool CHANDRA>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     constexpr int NV = DIM + 2;
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -205,8 +310,16 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         ab[k] = 0.5 * inten * lam * fb[k];
         bbar[k] = -ab[k];
     }
-    euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
-    euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
+    if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
+        PrimBar o1, o2;
+        chandra_pair_vjp<DIM, 2, true>(0, pa.rho, pa.v, 0.5 * pa.rho / pa.p, pb.rho, pb.v, 0.5 * pb.rho / pb.p, g,
+                                       fb, o1, o2);
+        prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
+        prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
+    } else {
+        euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
+        euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
+    }
     double kappa = 0.5 * inten * dot;
     if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
     else lambda_vjp<DIM>(pb, g, kappa, bbar);
@@ -321,13 +434,12 @@ template <int DIM, int N>
 cudaError_t launch_adj_elem_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
     constexpr size_t smem = sizeof(double) * (S::NOPS + (DIM + 2) * S::NN);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(adj_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
     adj_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
@@ -343,6 +455,200 @@ cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
         case 6: return launch_adj_elem_n<DIM, 6>(P, s);
         case 7: return launch_adj_elem_n<DIM, 7>(P, s);
         case 8: return launch_adj_elem_n<DIM, 8>(P, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// Split-form element adjoint.  Per direction, a pair phase evaluates every symmetric pair of
+// the block's lines once and keeps the primitive cotangents of both nodes in shared memory;
+// the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux)
+// and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved variables.
+template <int DIM, int N>
+struct AdjSplitShape {
+    using S = Shape<DIM, N>;
+    static constexpr int NV = DIM + 2;
+    static constexpr int NPB = DIM + 2;                         // ρ̄, v̄, β̄ per side
+    static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
+    static constexpr size_t SMEM =
+        sizeof(double) * (S::NOPS + (size_t)(DIM + 2) * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT) +
+        2 * (S::NPAIR + 1);
+};
+
+template <int DIM, int N>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_split_elem_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
+    constexpr int NPT = A::NPT, NPB = A::NPB;
+    extern __shared__ double smem[];
+    double* sops = smem;
+    double* sprim = sops + S::NOPS;        // [DIM+2][NN]: ρ, v, β
+    double* sw = sprim + (DIM + 2) * NN;   // [NV][NN]: w = λ / J
+    double* spb = sw + NV * NN;            // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
+    uint8_t* stab = (uint8_t*)(spb + 2 * NPB * NPT);
+    const int tid = threadIdx.x;
+    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    if (tid == 0) {
+        int c = 0;
+        for (int a = 0; a < N; ++a)
+            for (int b = a + 1; b < N; ++b) { stab[2 * c] = (uint8_t)a; stab[2 * c + 1] = (uint8_t)b; ++c; }
+    }
+    const int e0 = blockIdx.x * S::EPB;
+    const int el = tid / NPE, i = tid - el * NPE;
+    const int e = e0 + el;
+    const bool active = (tid < NN) && (e < P.nelem);
+    const int64_t gi = (int64_t)e * NPE + i;
+    const double g = P.gamma, g1 = g - 1.0;
+    double ain[NV];
+    Prim pr;
+    if (active) {
+        double w = P.invJ[e] * P.s_lam;
+        double q[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ain[k] = P.Ain[k * P.ndofs + gi];
+            sw[k * NN + tid] = w * ain[k];
+            q[k] = P.U[k * P.ndofs + gi];
+        }
+        pr = prim_of<DIM, false>(q, g);
+        sprim[tid] = pr.rho;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = pr.v[k];
+        sprim[(1 + DIM) * NN + tid] = 0.5 * pr.rho / pr.p;
+    }
+    __syncthreads();
+    const double* Dsh = sops + N * N;   // D♯(i, j) = Dsh[i + j N]
+    double qb[NV];
+    PrimBar acc;
+    acc.r = 0.0;
+    acc.b = 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) qb[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
+#pragma unroll 1
+    for (int dir = 0; dir < DIM; ++dir) {
+        for (int kp = tid; kp < NPT; kp += blockDim.x) {
+            int elp = kp / (NFD * NPAIR);
+            int r = kp - elp * (NFD * NPAIR);
+            int line = r / NPAIR, pp = r - line * NPAIR;
+            if (e0 + elp >= P.nelem) continue;
+            int a = stab[2 * pp], b = stab[2 * pp + 1];
+            int ia = elp * NPE + tp_node<DIM>(N, dir, line, a);
+            int ib = elp * NPE + tp_node<DIM>(N, dir, line, b);
+            double Ja = P.Ja[(e0 + elp) * DIM + dir];
+            double cab = -Ja * Dsh[a + b * N], cba = -Ja * Dsh[b + a * N];
+            double Fb[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) Fb[k] = fma(cab, sw[k * NN + ia], cba * sw[k * NN + ib]);
+            double v1[DIM], v2[DIM];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                v1[k] = sprim[(1 + k) * NN + ia];
+                v2[k] = sprim[(1 + k) * NN + ib];
+            }
+            PrimBar o1, o2;
+            chandra_pair_vjp<DIM, 2, false>(dir, sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[ib], v2,
+                                            sprim[(1 + DIM) * NN + ib], g, Fb, o1, o2);
+            spb[0 * NPT + kp] = o1.r;
+            spb[NPB * NPT + kp] = o2.r;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                spb[(1 + k) * NPT + kp] = o1.v[k];
+                spb[(NPB + 1 + k) * NPT + kp] = o2.v[k];
+            }
+            spb[(1 + DIM) * NPT + kp] = o1.b;
+            spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
+        }
+        __syncthreads();
+        if (active) {
+            int pos, line;
+            tp_coords<DIM>(N, i, dir, pos, line);
+            double Ja = P.Ja[e * DIM + dir];
+            double G[NV];   // diagonal: F♯(i, i) = F(Q_i)
+            double dii = Dsh[pos + pos * N];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) G[k] = dii * sw[k * NN + tid];
+            double H = 0.0;
+            {
+                double E = P.U[(DIM + 1) * P.ndofs + gi];
+                H = (E + pr.p) / pr.rho;
+            }
+            euler_flux_vjp<DIM>(dir, pr.v, pr.vv, H, g1, G, -Ja, qb);
+            int pbase = el * NFD * NPAIR + line * NPAIR;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                if (j == pos) continue;
+                int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+                int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+                const double* src = spb + (pos == lo ? 0 : NPB * NPT);
+                acc.r += src[pidx];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
+                acc.b += src[(1 + DIM) * NPT + pidx];
+            }
+            if (pos == 0 || pos == N - 1) {
+                int32_t pk = P.elem_face[e * 2 * DIM + 2 * dir + (pos == 0 ? 0 : 1)];
+                const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
+                int64_t o = (int64_t)(pk >> 1) * NFD + line;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    prim_to_cons_vjp<DIM>(pr.rho, pr.v, pr.vv, pr.p, g1, acc, qb);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double o = fma(P.alpha, ain[k], qb[k]);
+        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
+        if (P.writeB) {
+            double b = P.delta_B * ain[k];
+            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
+            P.B[k * P.ndofs + gi] = b;
+        }
+        P.Aout[k * P.ndofs + gi] = o;
+    }
+    if (P.cbar && i == 0) {
+        double cacc = 0.0;
+        for (int fk = 0; fk < 2 * DIM; ++fk) {
+            int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            int fc = pk >> 1;
+            double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+            for (int m = 0; m < NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + m), cacc);
+        }
+        P.cbar[e] += cacc;
+    }
+}
+
+template <int DIM, int N>
+cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
+    using S = Shape<DIM, N>;
+    constexpr size_t smem = AdjSplitShape<DIM, N>::SMEM;
+    static_assert(smem <= 227 * 1024, "split adjoint tile exceeds shared memory");
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem);
+    });
+    if (attr != cudaSuccess) return attr;
+    int grid = (P.nelem + S::EPB - 1) / S::EPB;
+    adj_split_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_adj_split(int n, const AdjElemParams& P, cudaStream_t s) {
+    switch (n) {
+        case 2: return launch_adj_split_n<DIM, 2>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -380,10 +686,15 @@ struct AdjBuffers {
 };
 
 int adj_supported(flou_ctx* c) {
-    if (c->cfg.equation != FLOU_EQ_EULER || c->cfg.volume_op != FLOU_OP_STRONG || c->cfg.numflux != FLOU_NF_LXF ||
-        c->cfg.numflux_avg != FLOU_NF_STD_AVERAGE)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form and "
-                                                 "the LxF(StdAverage) flux");
+    const flou_config& k = c->cfg;
+    bool vol = k.volume_op == FLOU_OP_STRONG ||
+               (k.volume_op == FLOU_OP_SPLIT && k.twopoint_flux == FLOU_TP_CHANDRASHEKAR);
+    bool nf = k.numflux == FLOU_NF_LXF &&
+              (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR);
+    if (k.equation != FLOU_EQ_EULER || !vol || !nf)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
+                                                 "the Chandrashekar split form, and the LxF(StdAverage) or "
+                                                 "LxF(ChandrasekharAverage) flux");
     if (!c->lgl) return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL)");
     for (int b = 0; b < c->nbcs; ++b)
         if (c->bc_kind[b] == FLOU_BC_INFLOW)
@@ -439,9 +750,10 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     int64_t nth = (int64_t)c->nfaces * c->nfd;
     int grid = (int)((nth + 255) / 256);
     int dim = c->cfg.dim;
-    if (dim == 1) adj_face_kernel<1><<<grid, 256, 0, s>>>(F);
-    else if (dim == 2) adj_face_kernel<2><<<grid, 256, 0, s>>>(F);
-    else adj_face_kernel<3><<<grid, 256, 0, s>>>(F);
+    bool ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR;
+    if (dim == 1) ch ? adj_face_kernel<1, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<1, false><<<grid, 256, 0, s>>>(F);
+    else if (dim == 2) ch ? adj_face_kernel<2, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<2, false><<<grid, 256, 0, s>>>(F);
+    else ch ? adj_face_kernel<3, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<3, false><<<grid, 256, 0, s>>>(F);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
@@ -470,9 +782,15 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.readB = readB;
     P.writeB = writeB;
     P.gamma = c->cfg.gamma;
-    if (dim == 1) e = launch_adj_elem<1>(c->n, P, s);
-    else if (dim == 2) e = launch_adj_elem<2>(c->n, P, s);
-    else e = launch_adj_elem<3>(c->n, P, s);
+    if (c->cfg.volume_op == FLOU_OP_SPLIT) {
+        if (dim == 1) e = launch_adj_split<1>(c->n, P, s);
+        else if (dim == 2) e = launch_adj_split<2>(c->n, P, s);
+        else e = launch_adj_split<3>(c->n, P, s);
+    } else {
+        if (dim == 1) e = launch_adj_elem<1>(c->n, P, s);
+        else if (dim == 2) e = launch_adj_elem<2>(c->n, P, s);
+        else e = launch_adj_elem<3>(c->n, P, s);
+    }
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint element kernel");
     return FLOU_OK;
 }

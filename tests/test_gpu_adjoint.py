@@ -27,6 +27,14 @@ def _lxf():
     return F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
 
 
+def _split(face_avg="chandra"):
+    avg = F.ChandrasekharAverage() if face_avg == "chandra" else F.StdAverage()
+    return F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(avg, 1.0))
+
+
+OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("std")}
+
+
 CASES = [
     dict(dim=2, n=5, ne=(3, 3), periodic=True, bcs=None),
     dict(dim=2, n=4, ne=(3, 4), periodic=(), bcs={"1": "slip", "2": "slip", "3": "out", "4": "slip"}),
@@ -36,18 +44,19 @@ CASES = [
 ]
 
 
-def _disc(case):
+def _disc(case, op="strong"):
     eq = F.EulerEquation(case["dim"], 1.4)
     bcs = None
     if case["bcs"]:
         bcs = {k: (F.EulerSlipBC() if v == "slip" else F.EulerOutflowBC()) for k, v in case["bcs"].items()}
-    d = build(case["dim"], case["n"], case["ne"], eq, _lxf(), periodic=case["periodic"], bcs=bcs)
+    d = build(case["dim"], case["n"], case["ne"], eq, OPERATORS[op](), periodic=case["periodic"], bcs=bcs)
     return d
 
 
+@pytest.mark.parametrize("op", ["strong", "split", "split_stdface"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
-def test_rhs_vjp_dot_product(case):
-    disc = _disc(case)
+def test_rhs_vjp_dot_product(case, op):
+    disc = _disc(case, op)
     rng = np.random.default_rng(7)
     Q = smooth_euler_state(disc, seed=11)
     if case["bcs"]:
@@ -134,6 +143,107 @@ def test_adjoint_against_central_differences():
     rho_t, w = _functional_inputs(disc, 8)
     dt = 0.4 * disc.ctx.max_dt(Q0, 1.0)
     nsteps = 20
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 4, _dev(rho_t), _dev(w), g, gc)
+    wd, rtd = _dev(w), _dev(rho_t)
+
+    def Jof(Q, cc):
+        disc.ctx.set_dissipation(cc)
+        q = _dev(Q)
+        disc.ctx.step(q, dt, nsteps)
+        r = q[0] - rtd
+        return float(0.5 * torch.sum(wd * r * r))
+
+    h = 1e-6
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * 0.1
+        fd = (Jof(Q0 + h * dQ, c + h * dc) - Jof(Q0 - h * dQ, c - h * dc)) / (2 * h)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
+
+
+@pytest.mark.parametrize("op", ["split", "split_stdface"])
+def test_split_rhs_vjp_columns(op):
+    """Every column of the transposed Jacobian at once on a small 3D case: (∂R/∂Q)ᵀ λ against
+    the dual-number JVPs of all unit directions of one element's nodes."""
+    case = dict(dim=3, n=3, ne=(2, 2, 2), periodic=True, bcs=None)
+    disc = _disc(case, op)
+    rng = np.random.default_rng(21)
+    Q = smooth_euler_state(disc, seed=2, amp=0.3)
+    c = 1.0 + 0.3 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 3
+    for v in range(Q.shape[1]):
+        for i in range(npe):
+            dQ = np.zeros_like(Q)
+            dQ[i, v] = 1.0
+            _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+            col = np.sum(lam * dR)
+            assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+def _tgv_state(disc, mach, seed):
+    """Taylor-Green vortex with a small random smooth perturbation of every primitive variable.
+    The plain vortex is symmetric: interface wave speeds tie exactly (|u_L| + a_L = |u_R| + a_R)
+    on its symmetry planes, where LxF's max is not differentiable and a one-ulp difference in a
+    stage state picks the other branch.  The perturbation moves the trajectory off the ties."""
+    eq = disc.equation
+    P = eq.vars_cons2prim(F.initial.taylor_green(eq, disc.coords, mach))
+    rng = np.random.default_rng(seed)
+    X = disc.coords
+    for v in range(P.shape[1]):
+        k = rng.integers(1, 3, size=3)
+        ph = rng.uniform(0, 2 * np.pi, size=3)
+        wave = np.prod([np.sin(k[i] * X[:, i] + ph[i]) for i in range(3)], axis=0)
+        scale = 0.05 * (np.max(np.abs(P[:, v])) if v in (0, 4) else 1.0)
+        P[:, v] = P[:, v] + scale * wave
+    return np.asfortranarray(eq.vars_prim2cons(P))
+
+
+@pytest.mark.parametrize("op", ["split", "strong"])
+def test_3d_adjoint_solve_against_dual_numbers(op):
+    eq = F.EulerEquation(3, 1.4)
+    L = 2 * np.pi
+    disc = build(3, 4, (2, 3, 2), eq, OPERATORS[op](), box=((0.0,) * 3, (L,) * 3))
+    Q0 = _tgv_state(disc, 0.3, 0)
+    rng = np.random.default_rng(13)
+    c = 1.0 + 0.2 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 5)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 10
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+def test_split_adjoint_against_central_differences():
+    eq = F.EulerEquation(3, 1.4)
+    L = 2 * np.pi
+    disc = build(3, 5, (3, 3, 3), eq, _split(), box=((0.0,) * 3, (L,) * 3))
+    Q0 = _tgv_state(disc, 0.2, 1)
+    rng = np.random.default_rng(17)
+    c = 1.0 + 0.1 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 8)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 12
     g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
     gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
     disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 4, _dev(rho_t), _dev(w), g, gc)
