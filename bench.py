@@ -320,6 +320,124 @@ def bench_adjoint(nsteps=400, nsnap=20, ndirs=32, seed=404):
     return res
 
 
+def make_adjoint_batch(count=64, seed=505, mmin=8, mmax=24):
+    """The batched-adjoint configuration: `count` periodic [0, 2π]³ hex meshes of m³ elements,
+    m ~ U{8..24}, p ~ U{3, 4, 5}, Taylor-Green vortex at Mach ~ U(0.05, 0.3) (plus a 1e-3 smooth
+    perturbation), split form with the
+    Chandrashekar two-point flux and the LxF(ChandrasekharAverage) interface flux (the interface
+    flux the adjoint differentiates), per-element dissipation scale c = 1."""
+    import flou_cuda as F
+    rng = np.random.default_rng(seed)
+    eq = F.EulerEquation(3, 1.4)
+    out = []
+    for _ in range(count):
+        m = int(rng.integers(mmin, mmax + 1))
+        p = int(rng.integers(3, 6))
+        mach = float(rng.uniform(0.05, 0.3))
+        mesh = F.CartesianMesh((0.0, 0.0, 0.0), (2 * math.pi,) * 3, (m,) * 3)
+        F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
+        b = F.LagrangeBasis("GLL", p + 1)
+        disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), eq.nvariables), eq,
+                                  F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(F.ChandrasekharAverage(), 1.0)),
+                                  {})
+        # the vortex plus a 1e-3 smooth perturbation of every primitive variable: the plain vortex
+        # is symmetric, its interface wave speeds tie exactly where LxF's max has a kink
+        P = eq.vars_cons2prim(F.initial.taylor_green(eq, disc.coords, mach=mach))
+        X = disc.coords
+        for v in range(5):
+            k = rng.integers(1, 3, size=3)
+            ph = rng.uniform(0, 2 * math.pi, size=3)
+            wave = np.prod([np.sin(k[i] * X[:, i] + ph[i]) for i in range(3)], axis=0)
+            P[:, v] += 1e-3 * (np.max(np.abs(P[:, v])) if v in (0, 4) else 1.0) * wave
+        Q0 = np.asfortranarray(eq.vars_prim2cons(P))
+        rho_t = Q0[:, 0] * (1.0 + 0.01 * np.sin(X[:, 0] + rng.uniform(0, 6)) * np.sin(X[:, 1]) * np.cos(X[:, 2]))
+        out.append(dict(disc=disc, Q0=Q0, rho_t=rho_t, m=m, p=p, mach=mach))
+    return out
+
+
+def bench_adjoint_batch(nsteps=200, budget=120e9, count=64, nstreams=8, fd_instances=2, seed=505):
+    """Forward and lockstep adjoint of the batched-adjoint configuration (200 SSP-RK3 steps at
+    CFL 0.15 per instance, J_k = 1/2 Σ w (ρ(T) - ρt)², gradients with respect to U0 and c under a
+    120 GB device-memory budget for snapshots and step scratch).  The forward is the same
+    instances advanced by their own step graphs, each context on its own stream, all in flight
+    together.  Central differences (h = 1e-6) check the gradients of the smallest instances."""
+    import torch
+    import flou_cuda as F
+    torch.cuda.empty_cache()
+    t_setup = time.perf_counter()
+    insts = make_adjoint_batch(count, seed)
+    setup_s = time.perf_counter() - t_setup
+    discs = [x["disc"] for x in insts]
+    for d in discs:
+        d.ctx.set_dissipation(np.ones(d.mesh.nelements))
+    Q0s = [torch.from_numpy(np.ascontiguousarray(x["Q0"].T)).cuda() for x in insts]
+    dts = [0.15 * d.ctx.max_dt(q, 1.0) for d, q in zip(discs, Q0s)]   # p = 5 at Mach 0.05 needs <= 0.15
+    rts = [torch.from_numpy(np.ascontiguousarray(x["rho_t"])).cuda() for x in insts]
+    ws = [torch.from_numpy(np.tile(d.std.omega, d.mesh.nelements) * d.J).cuda() for d in discs]
+    ndofs = sum(d.ndofs for d in discs)
+    state_bytes = sum(d.ndofs * 5 * 8 for d in discs)
+    work = [q.clone() for q in Q0s]
+
+    def forward_all():
+        for d, q, dt in zip(discs, work, dts):
+            d.ctx.step_async(q, dt, nsteps)
+        for d in discs:
+            d.ctx.wait()
+
+    for d, q, dt in zip(discs, work, dts):   # warm-up: graph capture of every instance
+        d.ctx.step(q, dt, 1)
+    for w_, q in zip(work, Q0s):
+        w_.copy_(q)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    forward_all()
+    torch.cuda.synchronize()
+    fwd_s = time.perf_counter() - t0
+    grads = [torch.empty_like(q) for q in Q0s]
+    cgrads = [torch.empty(d.mesh.nelements, dtype=torch.float64, device="cuda") for d in discs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, nfwd, nsnap = F.adjoint_solve_batch(discs, Q0s, dts, nsteps, int(budget), rts, ws, grads, cgrads,
+                                           nstreams=nstreams)
+    torch.cuda.synchronize()
+    adj_s = time.perf_counter() - t0
+    # J of the forward pass agrees with the adjoint's own forward
+    jf = [float(0.5 * torch.sum(w_ * (q[0] - r) ** 2)) for w_, q, r in zip(ws, work, rts)]
+    j_rel = max(abs(a - b) / abs(b) for a, b in zip(J, jf))
+    rng = np.random.default_rng(seed + 1)
+    errs = []
+    order = sorted(range(count), key=lambda k: discs[k].ndofs)[:fd_instances]
+    h = 1e-6
+    for k in order:
+        d, dt = discs[k], dts[k]
+
+        def Jof(Q, cc):
+            d.ctx.set_dissipation(cc)
+            q = Q.clone()
+            d.ctx.step(q, dt, nsteps)
+            return float(0.5 * torch.sum(ws[k] * (q[0] - rts[k]) ** 2))
+
+        c1 = np.ones(d.mesh.nelements)
+        for _ in range(2):
+            dQ = torch.from_numpy(rng.standard_normal(tuple(Q0s[k].shape))).cuda()
+            dc = 0.1 * rng.standard_normal(c1.shape)
+            fd = (Jof(Q0s[k] + h * dQ, c1 + h * dc) - Jof(Q0s[k] - h * dQ, c1 - h * dc)) / (2 * h)
+            ours = float(torch.sum(grads[k] * dQ)) + float(np.sum(cgrads[k].cpu().numpy() * dc))
+            errs.append(abs(ours - fd) / abs(fd))
+        d.ctx.set_dissipation(c1)
+    units = ndofs * 3 * nsteps
+    return {"forward_s": fwd_s, "adjoint_s": adj_s, "ratio": adj_s / fwd_s, "instances": count, "ndofs": ndofs,
+            "state_bytes": state_bytes, "budget_bytes": int(budget), "snapshots": nsnap,
+            "recomputed_forward_steps": nfwd, "steps": nsteps, "streams": nstreams,
+            "forward_value": units / fwd_s, "unit": UNIT, "J_rel_diff_vs_forward": j_rel,
+            "fd_instances": [int(discs[k].ndofs) for k in order], "fd_max_rel_err": max(errs) if errs else None,
+            "setup_s": setup_s,
+            "orders": [x["p"] for x in insts], "m": [x["m"] for x in insts],
+            "workload": "%d x 3D Euler TGV (+1e-3 perturbation) periodic m^3 hex, m~U{8..24}, p~U{3..5}, Mach~U(0.05,0.3), split "
+                        "Chandrashekar + LxF(Chandrashekar), %d SSP-RK3 steps forward + adjoint, %.0f GB budget"
+                        % (count, nsteps, budget / 1e9)}
+
+
 def run_profile(which):
     """Two SSP-RK3 steps of one mesh on the device (the case the ncu captures use)."""
     import torch
@@ -353,6 +471,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-batch", action="store_true",
+                    help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
+                         "several minutes)")
+    ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
     ap.add_argument("--profile", choices=["A", "B", "C"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling)")
@@ -364,6 +486,10 @@ def main():
 
     import torch
     import flou_cuda as F
+
+    if args.adjoint_batch_only:
+        print(json.dumps({"adjoint_batch": bench_adjoint_batch()}))
+        return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -490,6 +616,10 @@ def main():
     if not args.no_adjoint:
         adjoint = bench_adjoint()
 
+    adjoint_batch = None
+    if args.adjoint_batch:
+        adjoint_batch = bench_adjoint_batch()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -506,7 +636,7 @@ def main():
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
-            "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
+            "adjoint_batch": adjoint_batch, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
     if dist is not None:

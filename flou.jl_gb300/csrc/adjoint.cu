@@ -935,6 +935,132 @@ struct Solver {
     }
 };
 
+// Lockstep reverse sweep of many independent solves under one device-memory budget.  All
+// instances follow one checkpoint schedule (same number of steps, each its own dt), so a
+// snapshot holds every instance's state at one step and the budget sets the number of
+// snapshots for the whole batch.  Instance i runs on stream stream_of[i]: its operations stay
+// ordered, while instances on other streams overlap with it.  The step scratch (X, S1, S2, T, B
+// and the face cotangents) is per stream, sized for the largest instance on that stream; the
+// adjoint state of instance i lives in the caller's gradient buffer and its initial state is
+// read from the caller's Q0 (snapshot 0).
+struct BatchSolver {
+    struct Scratch {
+        double *X = nullptr, *S1 = nullptr, *S2 = nullptr, *T = nullptr, *B = nullptr;
+        AdjBuffers ab;
+    };
+    int n = 0, nsteps = 0;
+    std::vector<flou_ctx*> c;
+    std::vector<double> dt;
+    std::vector<cudaStream_t> st;
+    std::vector<int> stream_of;
+    std::vector<size_t> bytes, off;          // state bytes of instance i, its offset in a snapshot
+    size_t snap_bytes = 0;
+    std::vector<const double*> q0;
+    std::vector<double*> slot;               // slot[0] unused (the caller's Q0), 1..s snapshots
+    std::vector<int> free_slots;
+    std::vector<Scratch> scr;
+    std::vector<double*> A, cbar;
+    std::vector<const double*> rho_t, w;
+    std::vector<size_t> poff;
+    std::vector<int> nblk;
+    double* partial = nullptr;               // device, Σ nblk
+    double* h_partial = nullptr;             // pinned host copy
+    std::vector<char> seeded;
+    long long advances = 0;                  // forward steps per instance (the same for all)
+    Schedule* sch = nullptr;
+    int failed = -1;
+
+    cudaStream_t S(int i) const { return st[stream_of[i]]; }
+    Scratch& W(int i) { return scr[stream_of[i]]; }
+    const double* snap(int si, int i) const { return si == 0 ? q0[i] : slot[si] + off[i] / sizeof(double); }
+    double* snapw(int si, int i) { return slot[si] + off[i] / sizeof(double); }
+    int fail_at(int i, int r) {
+        if (failed < 0) failed = i;
+        return r;
+    }
+    int copy(double* dst, const double* src, int i) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes[i], cudaMemcpyDeviceToDevice, S(i));
+        return e == cudaSuccess ? FLOU_OK : fail_at(i, ctx_cuda_fail(c[i], e, "state copy"));
+    }
+    int advance(double* Q, int k, int i) {
+        flou_ctx* ci = c[i];
+        double* S1 = W(i).S1;
+        cudaStream_t s = S(i);
+        for (int j = 0; j < k; ++j) {
+            int r;
+            if ((r = ctx_stage(ci, s, Q, Q, S1, 1, dt[i], 0.0, 1.0))) return fail_at(i, r);
+            if ((r = ctx_stage(ci, s, S1, Q, S1, 2, dt[i], 0.75, 0.25))) return fail_at(i, r);
+            if ((r = ctx_stage(ci, s, S1, Q, Q, 2, dt[i], 1.0 / 3.0, 2.0 / 3.0))) return fail_at(i, r);
+        }
+        return FLOU_OK;
+    }
+    // U^k of instance i is in its stream's X; A[i] holds the adjoint of U^(k+1) on entry and
+    // that of U^k on exit.
+    int backward_step(int k, int i) {
+        flou_ctx* ci = c[i];
+        Scratch& w_ = W(i);
+        cudaStream_t s = S(i);
+        double h = dt[i];
+        int r;
+        if ((r = ctx_stage(ci, s, w_.X, w_.X, w_.S1, 1, h, 0.0, 1.0))) return fail_at(i, r);
+        if ((r = ctx_stage(ci, s, w_.S1, w_.X, w_.S2, 2, h, 0.75, 0.25))) return fail_at(i, r);
+        if (!seeded[i]) {
+            if (k != nsteps - 1) return fail_at(i, ctx_fail(ci, FLOU_ERR_STATE, "adjoint schedule out of order"));
+            if ((r = ctx_stage(ci, s, w_.S2, w_.X, w_.T, 2, h, 1.0 / 3.0, 2.0 / 3.0))) return fail_at(i, r);
+            functional_kernel<<<nblk[i], 256, 0, s>>>(w_.T, rho_t[i], w[i], ci->ndofs, ci->nv, A[i], partial + poff[i]);
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_partial + poff[i], partial + poff[i], nblk[i] * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return fail_at(i, ctx_cuda_fail(ci, e, "functional"));
+            seeded[i] = 1;
+        }
+        if ((r = adj_stage(ci, w_.ab, s, w_.S2, A[i], w_.T, w_.B, cbar[i], (2.0 / 3.0) * h, 2.0 / 3.0, 0.0, 0, 1,
+                           0.0, 1.0 / 3.0)))
+            return fail_at(i, r);
+        if ((r = adj_stage(ci, w_.ab, s, w_.S1, w_.T, A[i], w_.B, cbar[i], 0.25 * h, 0.25, 0.0, 0, 1, 1.0, 0.75)))
+            return fail_at(i, r);
+        if ((r = adj_stage(ci, w_.ab, s, w_.X, A[i], A[i], w_.B, cbar[i], h, 1.0, 1.0, 1, 0, 0.0, 0.0)))
+            return fail_at(i, r);
+        return FLOU_OK;
+    }
+    // Every instance's U^i0 is in snapshot si; ns free snapshots; reverses steps i0 .. i0+m-1.
+    int rev(int i0, int m, int ns, int si) {
+        int r;
+        if (m <= 0) return FLOU_OK;
+        if (m == 1) {
+            for (int i = 0; i < n; ++i) {
+                if ((r = copy(W(i).X, snap(si, i), i))) return r;
+                if ((r = backward_step(i0, i))) return r;
+            }
+            return FLOU_OK;
+        }
+        if (ns == 0 || free_slots.empty()) {
+            for (int k = m - 1; k >= 0; --k) {
+                for (int i = 0; i < n; ++i) {
+                    if ((r = copy(W(i).X, snap(si, i), i))) return r;
+                    if ((r = advance(W(i).X, k, i))) return r;
+                    if ((r = backward_step(i0 + k, i))) return r;
+                }
+                advances += k;
+            }
+            return FLOU_OK;
+        }
+        int mm = sch->split_of(m, std::min(ns, sch->s));
+        if (mm < 1 || mm >= m) mm = m / 2;
+        int sj = free_slots.back();
+        free_slots.pop_back();
+        for (int i = 0; i < n; ++i) {
+            if ((r = copy(snapw(sj, i), snap(si, i), i))) return r;
+            if ((r = advance(snapw(sj, i), mm, i))) return r;
+        }
+        advances += mm;
+        if ((r = rev(i0 + mm, m - mm, ns - 1, sj))) return r;
+        free_slots.push_back(sj);
+        return rev(i0, mm, ns, si);
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -1018,6 +1144,138 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     if (J) *J = S.J;
     if (forward_steps) *forward_steps = S.advances;
     return ctx_check_status(c);
+}
+
+int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const* Q0, const double* dt,
+                                 int32_t nsteps, int64_t budget_bytes, int32_t nstreams,
+                                 double* const* rho_target, double* const* weights, double* J,
+                                 double* const* dJdQ0, double* const* dJdc, int64_t* forward_steps,
+                                 int32_t* nsnap) {
+    if (n < 1 || !ctxs || !Q0 || !dt || !rho_target || !weights || !dJdQ0 || nsteps < 1) return FLOU_ERR_ARG;
+    for (int i = 0; i < n; ++i)
+        if (!ctxs[i]) return FLOU_ERR_ARG;
+    auto fail_all = [&](int code, const std::string& msg) {
+        for (int i = 0; i < n; ++i) ctxs[i]->err = msg;
+        return code;
+    };
+    int dev0 = -1;
+    if (cudaGetDevice(&dev0) != cudaSuccess) return fail_all(FLOU_ERR_CUDA, "no CUDA device");
+    for (int i = 0; i < n; ++i) {
+        flou_ctx* c = ctxs[i];
+        int r = ctx_prepare(c);
+        if (!r) r = adj_supported(c);
+        if (!r && (!Q0[i] || !rho_target[i] || !weights[i] || !dJdQ0[i] || !std::isfinite(dt[i])))
+            r = ctx_fail(c, FLOU_ERR_ARG, "invalid arguments");
+        if (!r && dJdc && dJdc[i] && !c->d_c)
+            r = ctx_fail(c, FLOU_ERR_STATE, "dJ/dc needs the per-element dissipation scale (flou_set_dissipation)");
+        if (r) return fail_all(r, "instance " + std::to_string(i) + ": " + c->err);
+    }
+    BatchSolver B;
+    B.n = n;
+    B.nsteps = nsteps;
+    B.c.assign(ctxs, ctxs + n);
+    B.dt.assign(dt, dt + n);
+    B.bytes.resize(n);
+    B.off.resize(n);
+    B.q0.assign(Q0, Q0 + n);
+    B.A.assign(dJdQ0, dJdQ0 + n);
+    B.cbar.assign(n, nullptr);
+    for (int i = 0; i < n; ++i) {
+        if (dJdc) B.cbar[i] = dJdc[i];
+        B.rho_t.push_back(rho_target[i]);
+        B.w.push_back(weights[i]);
+        B.bytes[i] = (size_t)ctxs[i]->ndofs * ctxs[i]->nv * sizeof(double);
+        B.off[i] = B.snap_bytes;
+        B.snap_bytes += (B.bytes[i] + 255) / 256 * 256;
+        B.nblk.push_back((int)((ctxs[i]->ndofs + 255) / 256));
+        B.poff.push_back(i ? B.poff[i - 1] + B.nblk[i - 1] : 0);
+    }
+    size_t npart = B.poff[n - 1] + B.nblk[n - 1];
+    // streams: largest instances first, each to the stream with the least work so far
+    int S = std::max(1, std::min(nstreams > 0 ? nstreams : 8, n));
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return B.bytes[a] > B.bytes[b]; });
+    std::vector<double> load(S, 0.0);
+    std::vector<size_t> maxb(S, 0), maxf(S, 0), maxfd(S, 0);
+    B.stream_of.assign(n, 0);
+    for (int i : order) {
+        int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        B.stream_of[i] = s;
+        load[s] += (double)B.bytes[i];
+        maxb[s] = std::max(maxb[s], B.bytes[i]);
+        maxf[s] = std::max(maxf[s], (size_t)ctxs[i]->nfdofs * ctxs[i]->nv);
+        maxfd[s] = std::max(maxfd[s], (size_t)ctxs[i]->nfdofs);
+    }
+    size_t fixed = npart * sizeof(double);
+    for (int s = 0; s < S; ++s) fixed += 5 * maxb[s] + (2 * maxf[s] + maxfd[s]) * sizeof(double);
+    if (budget_bytes < 0 || (size_t)budget_bytes < fixed)
+        return fail_all(FLOU_ERR_ARG, "device-memory budget below the " + std::to_string(fixed) +
+                                          " bytes of step scratch the batch needs");
+    int nslots = (int)std::min<size_t>((size_t)std::max(nsteps - 1, 0), ((size_t)budget_bytes - fixed) / B.snap_bytes);
+    std::vector<void*> owned;
+    cudaError_t e = cudaSuccess;
+    auto dalloc = [&](void** p, size_t b) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(p, b);
+        if (e == cudaSuccess) owned.push_back(*p);
+    };
+    B.st.assign(S, nullptr);
+    for (int s = 0; s < S && e == cudaSuccess; ++s) e = cudaStreamCreateWithFlags(&B.st[s], cudaStreamNonBlocking);
+    B.scr.resize(S);
+    for (int s = 0; s < S; ++s) {
+        BatchSolver::Scratch& w = B.scr[s];
+        double** bufs[] = {&w.X, &w.S1, &w.S2, &w.T, &w.B};
+        for (double** b : bufs) dalloc((void**)b, maxb[s]);
+        dalloc((void**)&w.ab.QbL, maxf[s] * sizeof(double));
+        dalloc((void**)&w.ab.QbR, maxf[s] * sizeof(double));
+        dalloc((void**)&w.ab.Ibar, std::max<size_t>(maxfd[s], 1) * sizeof(double));
+    }
+    dalloc((void**)&B.partial, npart * sizeof(double));
+    B.slot.assign(nslots + 1, nullptr);
+    for (int j = 1; j <= nslots; ++j) dalloc((void**)&B.slot[j], B.snap_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&B.h_partial, npart * sizeof(double));
+    int rr = FLOU_OK;
+    if (e != cudaSuccess) rr = fail_all(FLOU_ERR_OOM, std::string("batched adjoint storage: ") + cudaGetErrorString(e));
+    for (int i = 0; i < n && !rr; ++i)
+        if (B.cbar[i]) {
+            e = cudaMemsetAsync(B.cbar[i], 0, ctxs[i]->nelem * sizeof(double), B.S(i));
+            if (e != cudaSuccess) rr = fail_all(FLOU_ERR_CUDA, "cbar reset");
+        }
+    // the callers' inputs may still be in flight on the contexts' own streams
+    for (int i = 0; i < n && !rr; ++i)
+        if (cudaStreamSynchronize(ctxs[i]->stream) != cudaSuccess) rr = fail_all(FLOU_ERR_CUDA, "stream synchronize");
+    Schedule sch(nsteps, nslots);
+    B.sch = &sch;
+    B.seeded.assign(n, 0);
+    for (int j = 1; j <= nslots; ++j) B.free_slots.push_back(j);
+    if (!rr) {
+        rr = B.rev(0, nsteps, nslots, 0);
+        if (rr && B.failed >= 0) fail_all(rr, "instance " + std::to_string(B.failed) + ": " + ctxs[B.failed]->err);
+    }
+    for (int s = 0; s < S; ++s)
+        if (B.st[s]) {
+            cudaError_t es = cudaStreamSynchronize(B.st[s]);
+            if (es != cudaSuccess && !rr) rr = fail_all(FLOU_ERR_CUDA, std::string("batched adjoint: ") + cudaGetErrorString(es));
+        }
+    if (!rr) {
+        for (int i = 0; i < n; ++i) {
+            double j = 0.0;
+            for (int b = 0; b < B.nblk[i]; ++b) j += B.h_partial[B.poff[i] + b];
+            if (J) J[i] = j;
+        }
+        if (forward_steps) *forward_steps = B.advances;
+        if (nsnap) *nsnap = nslots;
+        for (int i = 0; i < n && !rr; ++i) {
+            int r = ctx_check_status(ctxs[i]);
+            if (r) rr = fail_all(r, "instance " + std::to_string(i) + ": " + ctxs[i]->err);
+        }
+    }
+    if (B.h_partial) cudaFreeHost(B.h_partial);
+    for (void* p : owned) cudaFree(p);
+    for (cudaStream_t s : B.st)
+        if (s) cudaStreamDestroy(s);
+    return rr;
 }
 
 }  // extern "C"

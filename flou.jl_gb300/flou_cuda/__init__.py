@@ -13,6 +13,6 @@ from .mesh import CartesianMesh, apply_periodicBCs
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
 from .timeint import SSPRK33, timeintegrate
 from . import initial
-from .batch import Batch
+from .batch import Batch, adjoint_solve_batch
 
 rhs = rhs_

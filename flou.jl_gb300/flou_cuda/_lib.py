@@ -96,6 +96,9 @@ PROTOTYPES = {
                             ctypes.c_char_p, ctypes.c_int32],
     "flou_rhs_vjp": [_P, _P, _P, _P, _P],
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
+    "flou_adjoint_solve_batch": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D, ctypes.c_int32,
+                                 ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D,
+                                 ctypes.POINTER(_P), ctypes.POINTER(_P), _I64, _I32],
     "flou_batch_create": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "flou_batch_destroy": [_P],
     "flou_batch_last_error": [_P],

@@ -63,3 +63,28 @@ class Batch:
         if h is not None and h.value:
             self._lib.flou_batch_destroy(h)
             self.h = None
+
+
+def adjoint_solve_batch(discs, Q0s, dts, nsteps, budget_bytes, rho_targets, weights, dJdQ0s, dJdcs=None,
+                        nstreams=8):
+    """Gradients of J_k = 1/2 Σ w (ρ(T) - ρt)² for every instance k in one lockstep reverse sweep
+    under one device-memory budget (flou_adjoint_solve_batch).  All arrays are CUDA tensors;
+    dJdQ0s (and dJdcs) are filled.  Returns (J list, recomputed forward steps per instance,
+    snapshots used)."""
+    import torch
+
+    lib = L.load()
+    n = len(discs)
+    vp = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() if t is not None else None for t in ts])
+    ctxs = (ctypes.c_void_p * n)(*[d.ctx.h.value for d in discs])
+    dt = np.ascontiguousarray(dts, dtype=np.float64)
+    J = np.zeros(n)
+    nf = ctypes.c_int64()
+    ns = ctypes.c_int32()
+    torch.cuda.synchronize()   # inputs written on torch's stream are complete
+    st = lib.flou_adjoint_solve_batch(n, ctxs, vp(Q0s), L.dptr(dt), int(nsteps), int(budget_bytes), int(nstreams),
+                                      vp(rho_targets), vp(weights), L.dptr(J), vp(dJdQ0s),
+                                      vp(dJdcs) if dJdcs is not None else None, ctypes.byref(nf),
+                                      ctypes.byref(ns))
+    L.check(st, discs[0].ctx.h)
+    return list(J), nf.value, ns.value

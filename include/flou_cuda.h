@@ -192,8 +192,10 @@ int32_t flou_check_geometry(int32_t dim, int32_t nnodes, int32_t nelem, int32_t 
 int32_t flou_fp64_peak(double* gflops);
 
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
- * Covers the Euler equations with the strong-form volume term and the LxF(StdAverage)
- * (Rusanov) interface flux on LGL nodes, with periodic, slip-wall and outflow boundaries.
+ * Covers the Euler equations with the strong-form volume term or the split form with the
+ * Chandrashekar two-point flux, and the LxF interface flux with the StdAverage (Rusanov) or
+ * ChandrasekharAverage central part, on LGL nodes, with periodic, slip-wall and outflow
+ * boundaries.
  * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):
  * max(a, b) takes b unless b < a; d|u|/du = -1 for a set sign bit, else +1. */
 
@@ -215,6 +217,23 @@ int32_t flou_rhs_vjp(flou_ctx* ctx, double* Qbar, double* cbar, const double* Q,
 int32_t flou_adjoint_solve(flou_ctx* ctx, const double* Q0, double dt, int32_t nsteps, int32_t nsnap,
                            const double* rho_target, const double* weights, double* J, double* dJdQ0, double* dJdc,
                            int64_t* forward_steps);
+
+/* Gradients of n independent solves (same functional form, same number of steps, each its own
+ * dt, context and targets) in one lockstep reverse sweep under one device-memory budget: one
+ * checkpoint schedule serves every instance, a snapshot holds all their states at one step,
+ * and the number of snapshots is what `budget_bytes` leaves after the step scratch (the
+ * schedule minimising recomputed forward steps for it).  The instances' kernels run on
+ * `nstreams` internal streams (<= 0: 8), the largest instances spread across them.
+ * Device pointers per instance: Q0[k] (read only; it is snapshot 0), rho_target[k] and
+ * weights[k] (ndofs), dJdQ0[k] (state-sized), dJdc[k] (nelem; dJdc or dJdc[k] may be NULL).
+ * Host outputs: J[k] (may be NULL), *forward_steps (recomputed forward steps per instance)
+ * and *nsnap (snapshots used); either may be NULL.  On failure every context's last error
+ * names the instance.  No counterpart in the reference. */
+int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const* Q0, const double* dt,
+                                 int32_t nsteps, int64_t budget_bytes, int32_t nstreams,
+                                 double* const* rho_target, double* const* weights, double* J,
+                                 double* const* dJdQ0, double* const* dJdc, int64_t* forward_steps,
+                                 int32_t* nsnap);
 
 /* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
  * Many independent discretizations with uneven element counts and orders advance together:
