@@ -452,6 +452,33 @@ def run_profile(which):
         print(json.dumps({"profile_case": "batched 256 x 2D Euler", "ndofs": sum(d.ndofs for d, _ in insts),
                           "steps": 2}))
         return 0
+    if which in ("D", "E"):
+        import flou_cuda as F
+        if which == "D":   # the adjoint configuration's discretization, 20 steps, 4 snapshots
+            eq = F.EulerEquation(2, 1.4)
+            mesh = F.CartesianMesh((-5.0, -5.0), (5.0, 5.0), (64, 64))
+            F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"))
+            b = F.LagrangeBasis("GLL", 5)
+            disc = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), 4), eq,
+                                      F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+            Q0 = F.initial.isentropic_vortex(eq, disc.coords, (0.2, -0.3), beta=5.0, period=(10.0, 10.0))
+            nsteps, nsnap, cfl = 20, 4, 0.4
+        else:              # one batched-adjoint instance: 16^3 elements, p = 4, 10 steps, 3 snapshots
+            x = make_adjoint_batch(1, seed=7, mmin=16, mmax=16)[0]
+            disc, Q0 = x["disc"], x["Q0"]
+            nsteps, nsnap, cfl = 10, 3, 0.15
+        disc.ctx.set_dissipation(np.ones(disc.mesh.nelements))
+        Qd = torch.from_numpy(np.ascontiguousarray(np.asarray(Q0).T)).cuda()
+        dt = cfl * disc.ctx.max_dt(Qd, 1.0)
+        rho_t = Qd[0].clone()
+        w = torch.from_numpy(np.tile(disc.std.omega, disc.mesh.nelements) * disc.J).cuda()
+        g = torch.empty_like(Qd)
+        gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+        J, nf = disc.ctx.adjoint_solve(Qd, dt, nsteps, nsnap, rho_t, w, g, gc)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "adjoint " + which, "ndofs": disc.ndofs, "steps": nsteps,
+                          "recomputed": nf, "J": J}))
+        return 0
     nel, n = (32, 4) if which == "A" else (16, 8)
     disc, Q0 = make_tgv(nel, n)
     Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
@@ -475,9 +502,10 @@ def main():
                     help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
                          "several minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
-    ap.add_argument("--profile", choices=["A", "B", "C"], default=None,
+    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
-                         "configuration C (256 instances, one persistent launch per stage, default tiling)")
+                         "configuration C (256 instances, one persistent launch per stage, default tiling); "
+                         "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

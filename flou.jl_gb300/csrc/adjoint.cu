@@ -131,82 +131,96 @@ __device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa
     qb[DIM + 1] += kappa * ca;
 }
 
-// Logarithmic mean (Utilities.jl:34-44) with its partial derivatives:
-//   u = ((a-b)/(a+b))²;  u < 0.01: L = (a+b)/(2F), F = 1+u/3+u²/5+u³/7,
-//     ∂L/∂a = 1/(2F) - 2F'(u) f b/(F² (a+b)),  ∂L/∂b = 1/(2F) + 2F'(u) f a/(F² (a+b));
-//   else L = (a-b)/ℓ, ℓ = ln(a/b):  ∂L/∂a = 1/ℓ - (a-b)/(ℓ² a),  ∂L/∂b = -1/ℓ + (a-b)/(ℓ² b).
-__device__ __forceinline__ void logmean_d(double a, double b, double& L, double& da, double& db) {
-    double s = a + b, dd = a - b, is = 1.0 / s, f = dd * is, u = f * f;
-    if (u < 0.01) {
-        double F = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
-        double iF = 1.0 / F;
-        L = 0.5 * s * iF;
-        double Fp = fma(u, fma(u, 3.0 / 7.0, 0.4), 1.0 / 3.0);
-        double t = 2.0 * Fp * f * iF * iF * is;
-        da = fma(-t, b, 0.5 * iF);
-        db = fma(t, a, 0.5 * iF);
-    } else {
-        double l = log(a / b), il = 1.0 / l;
-        L = dd * il;
-        double t = L * il;
-        da = il - t / a;
-        db = t / b - il;
-    }
-}
-
 // Cotangent of one node's primitive variables (ρ, v, β).
 struct PrimBar {
     double r, v[3], b;
 };
 
-// VJP of the Chandrashekar pair flux along d, F = [m, m v̄ + p̂ e_d, m h] with
-//   m = ρ̂ v̄_d, ρ̂ = ln-mean(ρ), β̂ = ln-mean(β), p̂ = (ρ1+ρ2)/(2(β1+β2)), v̄ = (v1+v2)/2,
+// Logarithmic mean (Utilities.jl:34-44) of a = 2 h1, b = 2 h2 given the half sum hs = (a+b)/2,
+// the half difference hd = (a-b)/2 and r = 1/hs, with its partial derivatives:
+//   f = (a-b)/(a+b), u = f²;  u < 0.01: L = (a+b)/(2F), F = 1+u/3+u²/5+u³/7, 1/L = F r,
+//     ∂L/∂a = 1/(2F) - 2F'(u) f b/(F²(a+b)),  ∂L/∂b = 1/(2F) + 2F'(u) f a/(F²(a+b));
+//   else L = (a-b)/ℓ, ℓ = ln(a/b):  ∂L/∂a = 1/ℓ - L/(ℓ a),  ∂L/∂b = L/(ℓ b) - 1/ℓ.
+// 1/F takes two Newton steps from 1 - u/3 (relative error (4u²/45)^4 < 1e-20 for u < 0.01).
+__device__ __forceinline__ void logmean_half(double h1, double h2, double hs, double hd, double r, double& L,
+                                             double& iL, double& da, double& db) {
+    double f = hd * r, u = f * f;
+    if (u < 0.01) {
+        double F = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        double y = fma(-1.0 / 3.0, u, 1.0);
+        y = y * fma(-F, y, 2.0);
+        y = y * fma(-F, y, 2.0);
+        L = hs * y;
+        iL = F * r;
+        double Fp2 = fma(u, fma(u, 6.0 / 7.0, 0.8), 2.0 / 3.0);   // 2 F'(u)
+        double t = Fp2 * f * (y * y) * r;
+        double hy = 0.5 * y;
+        da = fma(-t, h2, hy);
+        db = fma(t, h1, hy);
+    } else {
+        double l = log(h1 / h2), il = 1.0 / l;
+        L = (2.0 * hd) * il;
+        iL = l / (2.0 * hd);
+        double c = 0.5 * L * il;
+        da = il - c / h1;
+        db = c / h2 - il;
+    }
+}
+
+// VJP of the Chandrashekar pair flux along axis D (Euler.jl:474-536 as a function of the
+// primitive variables), F = [m, m v̄ + p̂ e_D, m h] with
+//   m = ρ̂ v̄_D, ρ̂ = ln-mean(ρ), β̂ = ln-mean(β), p̂ = (ρ1+ρ2)/(2(β1+β2)), v̄ = (v1+v2)/2,
 //   h = 1/(2β̂(γ-1)) - S/4 + p̂/ρ̂ + |v̄|²,  S = |v1|² + |v2|²
 // (WL2: S = |v1|² + |v2|² - v2_z² + v1_z², the 3D interface average of Euler.jl:216).
-// SIDES = 1 returns the cotangent of side 1 only.
-template <int DIM, int SIDES, bool WL2>
-__device__ __forceinline__ void chandra_pair_vjp(int d, double r1, const double* v1, double b1, double r2,
-                                                 const double* v2, double b2, double g, const double* Fb,
-                                                 PrimBar& o1, PrimBar& o2) {
-    double rho, dra, drb, beta, dba, dbb;
-    logmean_d(r1, r2, rho, dra, drb);
-    logmean_d(b1, b2, beta, dba, dbb);
-    double isb = 1.0 / (b1 + b2);
-    double p = 0.5 * (r1 + r2) * isb;
-    double va[DIM], S = 0.0, vv = 0.0;
+// Inputs are the halved node quantities rh = ρ/2, vh = v/2, bh = β/2, vq = |v|²/4; one
+// reciprocal 1/(ρ̄ β̄) serves both means and the pressure average.  Cotangents are with
+// respect to (ρ, v, β) of each side.
+template <int DIM, int D, bool WL2>
+__device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, double bh1, double vq1, double rh2,
+                                                 const double* vh2, double bh2, double vq2, double cb,
+                                                 const double* Fb, PrimBar& o1, PrimBar& o2) {
+    double hsr = rh1 + rh2, hdr = rh1 - rh2, hsb = bh1 + bh2, hdb = bh1 - bh2;
+    double R = 1.0 / (hsr * hsb);
+    double rs = hsb * R, rb = hsr * R;   // 1/hsr, 1/hsb
+    double rho, irho, dra, drb, beta, ibeta, dba, dbb;
+    logmean_half(rh1, rh2, hsr, hdr, rs, rho, irho, dra, drb);
+    logmean_half(bh1, bh2, hsb, hdb, rb, beta, ibeta, dba, dbb);
+    double p = 0.5 * hsr * rb;
+    double va[DIM], vv = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
-        va[k] = 0.5 * (v1[k] + v2[k]);
+        va[k] = vh1[k] + vh2[k];
         vv = fma(va[k], va[k], vv);
-        S = fma(v1[k], v1[k], fma(v2[k], v2[k], S));
     }
-    if (WL2 && DIM == 3) S = S + (v1[2] * v1[2] - v2[2] * v2[2]);
-    double irho = 1.0 / rho, ibeta = 1.0 / beta, cb = 0.5 / (g - 1.0);
-    double h = fma(cb, ibeta, -0.25 * S) + fma(p, irho, vv);
-    double m = rho * va[d];
+    double S4 = vq1 + vq2;
+    if (WL2 && DIM == 3) S4 = S4 + (vh1[2] * vh1[2] - vh2[2] * vh2[2]);
+    double h = fma(cb, ibeta, -S4) + fma(p, irho, vv);
+    double m = rho * va[D];
     double mb = fma(Fb[DIM + 1], h, Fb[0]);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], va[k], mb);
     double hb = m * Fb[DIM + 1];
-    double vab[DIM];
+    double mh = 0.5 * m;
+    double hvab[DIM];   // v̄̄/2: the cotangent of v̄, halved (v̄ = (v1 + v2)/2)
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) vab[k] = fma(m, Fb[1 + k], 2.0 * hb * va[k]);
-    vab[d] = fma(mb, rho, vab[d]);
-    double pb = fma(hb, irho, Fb[1 + d]);
-    double rhob = fma(mb, va[d], -hb * p * irho * irho);
-    double betab = -hb * cb * ibeta * ibeta;
-    double pr = 0.5 * pb * isb, pbb = -pb * p * isb;
+    for (int k = 0; k < DIM; ++k) hvab[k] = fma(mh, Fb[1 + k], hb * va[k]);
+    hvab[D] = fma(0.5 * mb, rho, hvab[D]);
+    double pb = fma(hb, irho, Fb[1 + D]);
+    double rhob = fma(mb, va[D], -hb * p * (irho * irho));
+    double betab = -hb * cb * (ibeta * ibeta);
+    double pr = 0.25 * pb * rb, pbb = -0.5 * pb * p * rb;
     o1.r = fma(rhob, dra, pr);
+    o2.r = fma(rhob, drb, pr);
     o1.b = fma(betab, dba, pbb);
+    o2.b = fma(betab, dbb, pbb);
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) o1.v[k] = 0.5 * fma(-hb, v1[k], vab[k]);
-    if (WL2 && DIM == 3) o1.v[2] -= 0.5 * hb * v1[2];
-    if (SIDES == 2) {
-        o2.r = fma(rhob, drb, pr);
-        o2.b = fma(betab, dbb, pbb);
-#pragma unroll
-        for (int k = 0; k < DIM; ++k) o2.v[k] = 0.5 * fma(-hb, v2[k], vab[k]);
-        if (WL2 && DIM == 3) o2.v[2] += 0.5 * hb * v2[2];
+    for (int k = 0; k < DIM; ++k) {
+        o1.v[k] = fma(-hb, vh1[k], hvab[k]);
+        o2.v[k] = fma(-hb, vh2[k], hvab[k]);
+    }
+    if (WL2 && DIM == 3) {
+        o1.v[2] = fma(-hb, vh1[2], o1.v[2]);
+        o2.v[2] = fma(hb, vh2[2], o2.v[2]);
     }
 }
 
@@ -312,8 +326,14 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     }
     if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
         PrimBar o1, o2;
-        chandra_pair_vjp<DIM, 2, true>(0, pa.rho, pa.v, 0.5 * pa.rho / pa.p, pb.rho, pb.v, 0.5 * pb.rho / pb.p, g,
-                                       fb, o1, o2);
+        double vh1[DIM], vh2[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            vh1[k] = 0.5 * pa.v[k];
+            vh2[k] = 0.5 * pb.v[k];
+        }
+        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho / pa.p, 0.25 * pa.vv, 0.5 * pb.rho, vh2,
+                                       0.25 * pb.rho / pb.p, 0.25 * pb.vv, 0.5 / g1, fb, o1, o2);
         prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
         prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
     } else {
@@ -461,33 +481,133 @@ cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
 
 // Split-form element adjoint.  Per direction, a pair phase evaluates every symmetric pair of
 // the block's lines once and keeps the primitive cotangents of both nodes in shared memory;
-// the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux)
-// and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved variables.
+// the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux;
+// zero on interior LGL nodes) and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved
+// variables.
 template <int DIM, int N>
 struct AdjSplitShape {
     using S = Shape<DIM, N>;
     static constexpr int NV = DIM + 2;
+    static constexpr int NARR = DIM + 3;                        // rh, vh, bh, vq
     static constexpr int NPB = DIM + 2;                         // ρ̄, v̄, β̄ per side
     static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
+    static constexpr int NSD = S::EPB * DIM * N * N;           // -Ja_d D♯ per element and direction
     static constexpr size_t SMEM =
-        sizeof(double) * (S::NOPS + (size_t)(DIM + 2) * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT) +
+        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
         2 * (S::NPAIR + 1);
+    // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
+    static constexpr int MINB = (S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
 };
 
-template <int DIM, int N>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_split_elem_kernel(AdjElemParams P) {
+template <int DIM, int N, int D>
+__device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, const double* sJD,
+                                                const double* sprim, const double* sw, double* spb,
+                                                const uint8_t* stab, double cb) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = A::NPT, NPB = A::NPB;
+    for (int kp = threadIdx.x; kp < NPT; kp += blockDim.x) {
+        int elp = kp / (NFD * NPAIR);
+        int r = kp - elp * (NFD * NPAIR);
+        int line = r / NPAIR, pp = r - line * NPAIR;
+        if (e0 + elp >= P.nelem) continue;
+        int a = stab[2 * pp], b = stab[2 * pp + 1];
+        int ia = elp * NPE + tp_node<DIM>(N, D, line, a);
+        int ib = elp * NPE + tp_node<DIM>(N, D, line, b);
+        const double* jd = sJD + (elp * DIM + D) * N * N;   // -Ja_D D♯(i, j) = jd[i + j N]
+        double cab = jd[a + b * N], cba = jd[b + a * N];
+        double Fb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fb[k] = fma(cab, sw[k * NN + ia], cba * sw[k * NN + ib]);
+        double v1[DIM], v2[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            v1[k] = sprim[(1 + k) * NN + ia];
+            v2[k] = sprim[(1 + k) * NN + ib];
+        }
+        PrimBar o1, o2;
+        chandra_pair_vjp<DIM, D, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
+                                        sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
+                                        Fb, o1, o2);
+        spb[kp] = o1.r;
+        spb[NPB * NPT + kp] = o2.r;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            spb[(1 + k) * NPT + kp] = o1.v[k];
+            spb[(NPB + 1 + k) * NPT + kp] = o2.v[k];
+        }
+        spb[(1 + DIM) * NPT + kp] = o1.b;
+        spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
+    }
+}
+
+template <int DIM, int N, int D>
+__device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
+                                                const double* Dsh, const double* sw, const double* spb,
+                                                const double* v, double rho, double p, double g1, double* qb,
+                                                PrimBar& acc) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N>;
+    constexpr int NV = DIM + 2, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
+    constexpr int NPT = A::NPT, NPB = A::NPB;
+    int pos, line;
+    tp_coords<DIM>(N, i, D, pos, line);
+    const int tid = threadIdx.x;
+    double dii = Dsh[pos + pos * N];
+    if (dii != 0.0) {   // diagonal: F♯(i, i) = F(Q_i)
+        double G[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) G[k] = dii * sw[k * NN + tid];
+        double vv = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
+        double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) / rho;
+        euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
+    }
+    int pbase = el * NFD * NPAIR + line * NPAIR;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if (j == pos) continue;
+        int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+        int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+        const double* src = spb + (pos == lo ? 0 : NPB * NPT);
+        acc.r += src[pidx];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
+        acc.b += src[(1 + DIM) * NPT + pidx];
+    }
+    if (pos == 0 || pos == N - 1) {
+        int32_t pk = P.elem_face[e * 2 * DIM + 2 * D + (pos == 0 ? 0 : 1)];
+        const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
+        int64_t o = (int64_t)(pk >> 1) * NFD + line;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
+    }
+}
+
+template <int DIM, int N>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::MINB)
+    adj_split_elem_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
+    constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
     extern __shared__ double smem[];
     double* sops = smem;
-    double* sprim = sops + S::NOPS;        // [DIM+2][NN]: ρ, v, β
-    double* sw = sprim + (DIM + 2) * NN;   // [NV][NN]: w = λ / J
-    double* spb = sw + NV * NN;            // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
-    uint8_t* stab = (uint8_t*)(spb + 2 * NPB * NPT);
+    double* sprim = sops + S::NOPS;   // [NARR][NN]: ρ/2, v/2, β/2, |v|²/4
+    double* sw = sprim + NARR * NN;   // [NV][NN]: w = λ / J
+    double* spb = sw + NV * NN;       // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
+    double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
+    uint8_t* stab = (uint8_t*)(sJD + A::NSD);
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    for (int t = tid; t < A::NSD; t += blockDim.x) {
+        int q = t / (N * N), ij = t - q * (N * N);
+        int elq = q / DIM, d = q - elq * DIM;
+        int eq_ = blockIdx.x * S::EPB + elq;
+        sJD[t] = eq_ < P.nelem ? -P.Ja[eq_ * DIM + d] * P.ops[N * N + ij] : 0.0;
+    }
     if (tid == 0) {
         int c = 0;
         for (int a = 0; a < N; ++a)
@@ -499,25 +619,36 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_split_elem_kernel(Ad
     const bool active = (tid < NN) && (e < P.nelem);
     const int64_t gi = (int64_t)e * NPE + i;
     const double g = P.gamma, g1 = g - 1.0;
-    double ain[NV];
-    Prim pr;
+    double rho = 1.0, p = 1.0, v[DIM];
     if (active) {
         double w = P.invJ[e] * P.s_lam;
         double q[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            ain[k] = P.Ain[k * P.ndofs + gi];
-            sw[k * NN + tid] = w * ain[k];
+            sw[k * NN + tid] = w * P.Ain[k * P.ndofs + gi];
             q[k] = P.U[k * P.ndofs + gi];
         }
-        pr = prim_of<DIM, false>(q, g);
-        sprim[tid] = pr.rho;
+        rho = q[0];
+        double ir = 1.0 / rho, ke = 0.0, vv = 0.0;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = pr.v[k];
-        sprim[(1 + DIM) * NN + tid] = 0.5 * pr.rho / pr.p;
+        for (int k = 0; k < DIM; ++k) {
+            v[k] = q[1 + k] * ir;
+            ke = fma(q[1 + k], v[k], ke);
+            vv = fma(v[k], v[k], vv);
+        }
+        p = g1 * fma(-0.5, ke, q[DIM + 1]);
+        sprim[tid] = 0.5 * rho;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
+        sprim[(1 + DIM) * NN + tid] = (0.25 * rho) / p;
+        sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
+    } else {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) v[k] = 0.0;
     }
     __syncthreads();
     const double* Dsh = sops + N * N;   // D♯(i, j) = Dsh[i + j N]
+    const double cb = 0.5 / g1;
     double qb[NV];
     PrimBar acc;
     acc.r = 0.0;
@@ -528,83 +659,29 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_split_elem_kernel(Ad
     for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
-        for (int kp = tid; kp < NPT; kp += blockDim.x) {
-            int elp = kp / (NFD * NPAIR);
-            int r = kp - elp * (NFD * NPAIR);
-            int line = r / NPAIR, pp = r - line * NPAIR;
-            if (e0 + elp >= P.nelem) continue;
-            int a = stab[2 * pp], b = stab[2 * pp + 1];
-            int ia = elp * NPE + tp_node<DIM>(N, dir, line, a);
-            int ib = elp * NPE + tp_node<DIM>(N, dir, line, b);
-            double Ja = P.Ja[(e0 + elp) * DIM + dir];
-            double cab = -Ja * Dsh[a + b * N], cba = -Ja * Dsh[b + a * N];
-            double Fb[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) Fb[k] = fma(cab, sw[k * NN + ia], cba * sw[k * NN + ib]);
-            double v1[DIM], v2[DIM];
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) {
-                v1[k] = sprim[(1 + k) * NN + ia];
-                v2[k] = sprim[(1 + k) * NN + ib];
-            }
-            PrimBar o1, o2;
-            chandra_pair_vjp<DIM, 2, false>(dir, sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[ib], v2,
-                                            sprim[(1 + DIM) * NN + ib], g, Fb, o1, o2);
-            spb[0 * NPT + kp] = o1.r;
-            spb[NPB * NPT + kp] = o2.r;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) {
-                spb[(1 + k) * NPT + kp] = o1.v[k];
-                spb[(NPB + 1 + k) * NPT + kp] = o2.v[k];
-            }
-            spb[(1 + DIM) * NPT + kp] = o1.b;
-            spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
-        }
+        if (dir == 0) adj_split_pairs<DIM, N, 0>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0)>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0)>(P, e0, sJD, sprim, sw, spb, stab, cb);
         __syncthreads();
         if (active) {
-            int pos, line;
-            tp_coords<DIM>(N, i, dir, pos, line);
-            double Ja = P.Ja[e * DIM + dir];
-            double G[NV];   // diagonal: F♯(i, i) = F(Q_i)
-            double dii = Dsh[pos + pos * N];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) G[k] = dii * sw[k * NN + tid];
-            double H = 0.0;
-            {
-                double E = P.U[(DIM + 1) * P.ndofs + gi];
-                H = (E + pr.p) / pr.rho;
-            }
-            euler_flux_vjp<DIM>(dir, pr.v, pr.vv, H, g1, G, -Ja, qb);
-            int pbase = el * NFD * NPAIR + line * NPAIR;
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                if (j == pos) continue;
-                int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
-                int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
-                const double* src = spb + (pos == lo ? 0 : NPB * NPT);
-                acc.r += src[pidx];
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
-                acc.b += src[(1 + DIM) * NPT + pidx];
-            }
-            if (pos == 0 || pos == N - 1) {
-                int32_t pk = P.elem_face[e * 2 * DIM + 2 * dir + (pos == 0 ? 0 : 1)];
-                const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
-                int64_t o = (int64_t)(pk >> 1) * NFD + line;
-#pragma unroll
-                for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
-            }
+            if (dir == 0) adj_split_nodes<DIM, N, 0>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            else if (dir == 1)
+                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0)>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            else adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0)>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
         }
         __syncthreads();
     }
     if (!active) return;
-    prim_to_cons_vjp<DIM>(pr.rho, pr.v, pr.vv, pr.p, g1, acc, qb);
+    double vv = 0.0;
 #pragma unroll
+    for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
+    prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
     for (int k = 0; k < NV; ++k) {
-        double o = fma(P.alpha, ain[k], qb[k]);
+        double ain = P.Ain[k * P.ndofs + gi];
+        double o = fma(P.alpha, ain, qb[k]);
         if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
         if (P.writeB) {
-            double b = P.delta_B * ain[k];
+            double b = P.delta_B * ain;
             if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
             P.B[k * P.ndofs + gi] = b;
         }
@@ -616,7 +693,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_split_elem_kernel(Ad
             int32_t pk = P.elem_face[e * 2 * DIM + fk];
             int fc = pk >> 1;
             double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
-            for (int m = 0; m < NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + m), cacc);
+            for (int m = 0; m < S::NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * S::NFD + m), cacc);
         }
         P.cbar[e] += cacc;
     }
@@ -847,80 +924,95 @@ struct Schedule {
     }
 };
 
+// Single-instance reverse sweep on two streams.  The forward stream `sf` places snapshots and
+// recomputes the state U^k each reverse step needs into one of two X buffers; the adjoint stream
+// `sa` runs the reverse steps.  Recomputation does not depend on the adjoint, so the forward
+// stream runs one reverse step ahead and both kinds of work overlap on the GPU.  Events hand each
+// X buffer from one stream to the other; snapshots are only touched by the forward stream, and
+// each stream has its own stage and face-flux scratch.
 struct Solver {
     flou_ctx* c;
-    cudaStream_t st;
+    cudaStream_t sa = nullptr, sf = nullptr;
     double dt;
     int nsteps;
     std::vector<double*> slot;          // snapshot states; slot[0] = U^0
     std::vector<int> free_slots;
-    double *X = nullptr, *S1 = nullptr, *S2 = nullptr, *A = nullptr, *Bacc = nullptr, *T = nullptr;
+    double* X[2] = {nullptr, nullptr};
+    cudaEvent_t ready[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr};
+    bool used[2] = {false, false};
+    int xi = 0;
+    double *F1 = nullptr, *Fnf = nullptr;                          // forward stream: stage, face flux
+    double *S1 = nullptr, *S2 = nullptr, *A = nullptr, *Bacc = nullptr, *T = nullptr;   // adjoint stream
     double* cbar = nullptr;
     const double* rho_t;
     const double* w;
     double* partial = nullptr;
+    double* h_partial = nullptr;
     int nblk = 0;
-    double J = 0.0;
     bool seeded = false;
     long long advances = 0;
     AdjBuffers ab;
     Schedule* sch = nullptr;
     size_t bytes = 0;
 
+    int cuda(cudaError_t e, const char* what) { return e == cudaSuccess ? FLOU_OK : ctx_cuda_fail(c, e, what); }
     int copy(double* dst, const double* src) {
-        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
-        return e == cudaSuccess ? FLOU_OK : ctx_cuda_fail(c, e, "state copy");
+        return cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, sf), "state copy");
     }
-    int advance(double* Q, int k) {   // k SSP-RK3 steps in place (stage buffer: S1)
+    int advance(double* Q, int k) {   // k SSP-RK3 steps in place on the forward stream
         for (int i = 0; i < k; ++i) {
             int r;
-            if ((r = ctx_stage(c, st, Q, Q, S1, 1, dt, 0.0, 1.0))) return r;
-            if ((r = ctx_stage(c, st, S1, Q, S1, 2, dt, 0.75, 0.25))) return r;
-            if ((r = ctx_stage(c, st, S1, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;
+            if ((r = ctx_stage(c, sf, Q, Q, F1, 1, dt, 0.0, 1.0, Fnf))) return r;
+            if ((r = ctx_stage(c, sf, F1, Q, F1, 2, dt, 0.75, 0.25, Fnf))) return r;
+            if ((r = ctx_stage(c, sf, F1, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf))) return r;
             ++advances;
         }
         return FLOU_OK;
     }
-    // Reverse one step from U^k held in X: the adjoint of U^(k+1) is in A on entry and that of
-    // U^k on exit.
-    int backward_step(int k) {
+    // U^(i0+k) from snapshot si into the next X buffer, then the reverse step i0+k on it.
+    int step_from(int si, int k, int kstep) {
         int r;
-        if ((r = ctx_stage(c, st, X, X, S1, 1, dt, 0.0, 1.0))) return r;             // U1
-        if ((r = ctx_stage(c, st, S1, X, S2, 2, dt, 0.75, 0.25))) return r;          // U2
+        int b = xi;
+        xi ^= 1;
+        if (used[b] && (r = cuda(cudaStreamWaitEvent(sf, done[b], 0), "event wait"))) return r;
+        if ((r = copy(X[b], slot[si]))) return r;
+        if ((r = advance(X[b], k))) return r;
+        if ((r = cuda(cudaEventRecord(ready[b], sf), "event record"))) return r;
+        if ((r = cuda(cudaStreamWaitEvent(sa, ready[b], 0), "event wait"))) return r;
+        if ((r = backward_step(kstep, X[b]))) return r;
+        used[b] = true;
+        return cuda(cudaEventRecord(done[b], sa), "event record");
+    }
+    // Reverse one step from U^k held in Xk: the adjoint of U^(k+1) is in A on entry and that of
+    // U^k on exit (adjoint stream).
+    int backward_step(int k, double* Xk) {
+        int r;
+        if ((r = ctx_stage(c, sa, Xk, Xk, S1, 1, dt, 0.0, 1.0))) return r;             // U1
+        if ((r = ctx_stage(c, sa, S1, Xk, S2, 2, dt, 0.75, 0.25))) return r;          // U2
         if (!seeded) {   // the last step: form U^n, the functional and its gradient seed
             if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
-            if ((r = ctx_stage(c, st, S2, X, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;   // U^n
-            functional_kernel<<<nblk, 256, 0, st>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return ctx_cuda_fail(c, e, "functional");
-            std::vector<double> h(nblk);
-            e = cudaMemcpyAsync(h.data(), partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) return ctx_cuda_fail(c, e, "functional");
-            J = 0.0;
-            for (double v : h) J += v;
+            if ((r = ctx_stage(c, sa, S2, Xk, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;   // U^n
+            functional_kernel<<<nblk, 256, 0, sa>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
+            if ((r = cuda(cudaGetLastError(), "functional"))) return r;
+            if ((r = cuda(cudaMemcpyAsync(h_partial, partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, sa),
+                          "functional")))
+                return r;
             seeded = true;
         }
-        if ((r = adj_stage(c, ab, st, S2, A, T, Bacc, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
+        if ((r = adj_stage(c, ab, sa, S2, A, T, Bacc, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
             return r;
-        if ((r = adj_stage(c, ab, st, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
-        if ((r = adj_stage(c, ab, st, X, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
+        if ((r = adj_stage(c, ab, sa, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
+        if ((r = adj_stage(c, ab, sa, Xk, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
         return FLOU_OK;
     }
     // U^i0 is in slot[si]; ns free snapshot slots may be used; reverses steps i0 .. i0+n-1.
     int rev(int i0, int n, int ns, int si) {
         int r;
         if (n <= 0) return FLOU_OK;
-        if (n == 1) {
-            if ((r = copy(X, slot[si]))) return r;
-            return backward_step(i0);
-        }
+        if (n == 1) return step_from(si, 0, i0);
         if (ns == 0 || free_slots.empty()) {
-            for (int k = n - 1; k >= 0; --k) {
-                if ((r = copy(X, slot[si]))) return r;
-                if ((r = advance(X, k))) return r;
-                if ((r = backward_step(i0 + k))) return r;
-            }
+            for (int k = n - 1; k >= 0; --k)
+                if ((r = step_from(si, k, i0 + k))) return r;
             return FLOU_OK;
         }
         int m = sch->split_of(n, std::min(ns, sch->s));
@@ -1099,49 +1191,74 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
         return ctx_fail(c, FLOU_ERR_STATE, "dJ/dc needs the per-element dissipation scale (flou_set_dissipation)");
     Solver S;
     S.c = c;
-    S.st = c->stream;
+    S.sa = c->stream;
     S.dt = dt;
     S.nsteps = nsteps;
     S.rho_t = rho_target;
     S.w = weights;
     S.bytes = (size_t)c->ndofs * c->nv * sizeof(double);
     S.nblk = (int)((c->ndofs + 255) / 256);
+    S.A = dJdQ0;   // the adjoint state lives in the output
     int nslots = std::min(nsnap, std::max(nsteps - 1, 0));
     std::vector<double*> owned;
-    auto dalloc = [&](double** p, size_t bytes) {
-        cudaError_t e = cudaMalloc((void**)p, bytes);
+    cudaError_t e = cudaStreamCreateWithFlags(&S.sf, cudaStreamNonBlocking);
+    auto dalloc = [&](double** p, size_t b) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc((void**)p, b);
         if (e == cudaSuccess) owned.push_back(*p);
-        return e;
     };
-    cudaError_t e = cudaSuccess;
     S.slot.assign(nslots + 1, nullptr);
-    for (int i = 0; i <= nslots && e == cudaSuccess; ++i) e = dalloc(&S.slot[i], S.bytes);
-    double** bufs[] = {&S.X, &S.S1, &S.S2, &S.A, &S.Bacc, &S.T};
-    for (double** b : bufs)
-        if (e == cudaSuccess) e = dalloc(b, S.bytes);
-    if (e == cudaSuccess) e = dalloc(&S.partial, S.nblk * sizeof(double));
+    for (int i = 0; i <= nslots; ++i) dalloc(&S.slot[i], S.bytes);
+    double** bufs[] = {&S.X[0], &S.X[1], &S.F1, &S.S1, &S.S2, &S.Bacc, &S.T};
+    for (double** b : bufs) dalloc(b, S.bytes);
+    dalloc(&S.Fnf, (size_t)c->nfdofs * c->nv * sizeof(double));
+    dalloc(&S.partial, S.nblk * sizeof(double));
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaEventCreateWithFlags(&S.ready[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.done[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&S.h_partial, S.nblk * sizeof(double));
     if (e == cudaSuccess && dJdc) S.cbar = dJdc;
     int rr = FLOU_OK;
     if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "adjoint storage");
     if (!rr) rr = alloc_adj(c, S.ab);
     if (!rr && S.cbar) {
-        e = cudaMemsetAsync(S.cbar, 0, c->nelem * sizeof(double), S.st);
+        e = cudaMemsetAsync(S.cbar, 0, c->nelem * sizeof(double), S.sa);
         if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "cbar reset");
     }
     Schedule sch(nsteps, nslots);
     S.sch = &sch;
     for (int i = 1; i <= nslots; ++i) S.free_slots.push_back(i);
-    if (!rr) rr = S.copy(S.slot[0], Q0);
-    if (!rr) rr = S.rev(0, nsteps, nslots, 0);
-    if (!rr) rr = S.copy(dJdQ0, S.A);
-    if (!rr) {
-        e = cudaStreamSynchronize(S.st);
-        if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "adjoint solve");
+    if (!rr) {   // the forward stream starts after what the caller queued on the context's stream
+        cudaEvent_t ev;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ev, S.sa);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(S.sf, ev, 0);
+        if (e == cudaSuccess) cudaEventDestroy(ev);
+        if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "stream order");
     }
+    if (!rr) {
+        e = cudaMemcpyAsync(S.slot[0], Q0, S.bytes, cudaMemcpyDeviceToDevice, S.sf);
+        if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "state copy");
+    }
+    if (!rr) rr = S.rev(0, nsteps, nslots, 0);
+    cudaError_t e1 = S.sf ? cudaStreamSynchronize(S.sf) : cudaSuccess;
+    cudaError_t e2 = cudaStreamSynchronize(S.sa);
+    if (!rr && (e1 != cudaSuccess || e2 != cudaSuccess))
+        rr = ctx_cuda_fail(c, e1 != cudaSuccess ? e1 : e2, "adjoint solve");
+    double Jv = 0.0;
+    if (!rr)
+        for (int b = 0; b < S.nblk; ++b) Jv += S.h_partial[b];
     free_adj(S.ab);
+    for (int i = 0; i < 2; ++i) {
+        if (S.ready[i]) cudaEventDestroy(S.ready[i]);
+        if (S.done[i]) cudaEventDestroy(S.done[i]);
+    }
+    if (S.h_partial) cudaFreeHost(S.h_partial);
     for (double* p : owned) cudaFree(p);
+    if (S.sf) cudaStreamDestroy(S.sf);
     if (rr) return rr;
-    if (J) *J = S.J;
+    if (J) *J = Jv;
     if (forward_steps) *forward_steps = S.advances;
     return ctx_check_status(c);
 }

@@ -141,11 +141,19 @@ ElemLaunch elem_launch(const flou_ctx* c) {
 }
 
 // One residual evaluation followed by the stage combination selected by `mode`.
+// Fn: face-flux scratch of this stage (NULL: the context's own).  Stages that may run
+// concurrently on different streams need different face-flux buffers.
 int stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
-          double a0, double a1) {
-    cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), s);
+          double a0, double a1, double* Fn = nullptr) {
+    FaceParams fp = face_params(c, Q);
+    ElemParams ep = elem_params(c, Q, Q0, out, mode, dt, a0, a1);
+    if (Fn) {
+        fp.Fn = Fn;
+        ep.Fn = Fn;
+    }
+    cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
-    e = launch_elem(elem_launch(c), elem_params(c, Q, Q0, out, mode, dt, a0, a1), s);
+    e = launch_elem(elem_launch(c), ep, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "element kernel launch");
     return FLOU_OK;
 }
@@ -362,8 +370,8 @@ ElemParams ctx_elem_params(const flou_ctx* c, const double* Q, const double* Q0,
 }
 ElemLaunch ctx_elem_launch(const flou_ctx* c) { return elem_launch(c); }
 int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
-              double a0, double a1) {
-    return stage(c, s, Q, Q0, out, mode, dt, a0, a1);
+              double a0, double a1, double* Fn) {
+    return stage(c, s, Q, Q0, out, mode, dt, a0, a1, Fn);
 }
 int ctx_check_status(flou_ctx* c) { return check_status(c); }
 }  // namespace flou

@@ -60,6 +60,6 @@ ElemParams ctx_elem_params(const flou_ctx* c, const double* Q, const double* Q0,
                            double a0, double a1);
 ElemLaunch ctx_elem_launch(const flou_ctx* c);
 int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
-              double a0, double a1);
+              double a0, double a1, double* Fn = nullptr);   // Fn: face-flux scratch (NULL: the context's)
 int ctx_check_status(flou_ctx* c);
 }  // namespace flou

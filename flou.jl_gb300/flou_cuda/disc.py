@@ -162,6 +162,14 @@ class MultielementDisc:
         return np.zeros((self.ndofs, self.nvariables), order="F")
 
 
+def _torch_stream_sync(t):
+    """Inputs written by torch on its current stream are complete before a call on the context's
+    own stream reads them (the context's stream does not order itself after torch's)."""
+    if getattr(t, "is_cuda", False):
+        import torch
+        torch.cuda.current_stream(t.device).synchronize()
+
+
 class Context:
     """Owns one flou_ctx (create + uploads); destroyed with the object."""
 
@@ -258,6 +266,7 @@ class Context:
     def rhs_vjp(self, Qbar, cbar, Q, lam):
         """Qbar = (∂rhs/∂Q)ᵀ lam, cbar = (∂rhs/∂c)ᵀ lam (CUDA tensors; cbar may be None)."""
         p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        _torch_stream_sync(Q)
         L.check(self._lib.flou_rhs_vjp(self.h, p(Qbar), p(cbar), p(Q), p(lam)), self.h)
 
     def adjoint_solve(self, Q0, dt, nsteps, nsnap, rho_target, weights, dJdQ0, dJdc=None):
@@ -265,6 +274,7 @@ class Context:
         p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
         J = ctypes.c_double()
         nf = ctypes.c_int64()
+        _torch_stream_sync(Q0)
         L.check(self._lib.flou_adjoint_solve(self.h, p(Q0), float(dt), int(nsteps), int(nsnap), p(rho_target),
                                              p(weights), ctypes.byref(J), p(dJdQ0), p(dJdc), ctypes.byref(nf)),
                 self.h)
