@@ -328,6 +328,7 @@ def make_adjoint_batch(count=64, seed=505, mmin=8, mmax=24):
     flux the adjoint differentiates), per-element dissipation scale c = 1."""
     import flou_cuda as F
     rng = np.random.default_rng(seed)
+    prng = np.random.default_rng(seed + 1)   # perturbations: the instance draws stay those of `seed`
     eq = F.EulerEquation(3, 1.4)
     out = []
     for _ in range(count):
@@ -345,8 +346,8 @@ def make_adjoint_batch(count=64, seed=505, mmin=8, mmax=24):
         P = eq.vars_cons2prim(F.initial.taylor_green(eq, disc.coords, mach=mach))
         X = disc.coords
         for v in range(5):
-            k = rng.integers(1, 3, size=3)
-            ph = rng.uniform(0, 2 * math.pi, size=3)
+            k = prng.integers(1, 3, size=3)
+            ph = prng.uniform(0, 2 * math.pi, size=3)
             wave = np.prod([np.sin(k[i] * X[:, i] + ph[i]) for i in range(3)], axis=0)
             P[:, v] += 1e-3 * (np.max(np.abs(P[:, v])) if v in (0, 4) else 1.0) * wave
         Q0 = np.asfortranarray(eq.vars_prim2cons(P))
