@@ -16,7 +16,7 @@ import Flou.FlouCommon: rhs!, get_max_dt
 using ChainRulesCore
 using LinearAlgebra
 
-export GPUDisc, SSPRK3GPU, GPUBatch, solve_functional
+export GPUDisc, SSPRK3GPU, GPUBatch, solve_functional, solve_functional_batch
 
 const libflou = joinpath(@__DIR__, "..", "..", "..", "lib", "libflou_cuda.so")
 
@@ -214,5 +214,30 @@ function GPUBatch(discs::Vector{<:GPUDisc}, states, dts::Vector{Float64})
 end
 
 step!(b::GPUBatch, nsteps) = ccall((:flou_batch_step, libflou), Int32, (Ptr{Cvoid}, Int32), b.h, nsteps)
+
+"""
+    solve_functional_batch(discs, Q0s, dts, nsteps, ρts, ws, budget_bytes; nstreams=8)
+        -> (J, dJdQ0s, dJdcs, recomputed_steps, snapshots)
+
+Gradients of J_k = 1/2 Σ w (ρ(T) - ρt)² for every instance in one lockstep reverse sweep under one
+device-memory budget (`flou_adjoint_solve_batch`).  Arrays are device arrays of the caller's GPU
+array package; each instance's dissipation scales are those set on its context.
+"""
+function solve_functional_batch(discs::Vector{<:GPUDisc}, Q0s, dts::Vector{Float64}, nsteps, ρts, ws,
+                                budget_bytes; nstreams=8)
+    n = length(discs)
+    J = zeros(n)
+    gs = [similar(q) for q in Q0s]
+    gcs = [similar(q, d.disc.mesh.nelements) for (q, d) in zip(Q0s, discs)]
+    fwd = Ref{Int64}(0)
+    ns = Ref{Int32}(0)
+    ptrs(v) = [pointer(x) for x in v]
+    check(ccall((:flou_adjoint_solve_batch, libflou), Int32,
+        (Int32, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Float64}}, Ptr{Float64}, Int32, Int64, Int32, Ptr{Ptr{Float64}},
+         Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Ref{Int64}, Ref{Int32}),
+        n, [d.ctx for d in discs], ptrs(Q0s), dts, nsteps, budget_bytes, nstreams, ptrs(ρts), ptrs(ws), J,
+        ptrs(gs), ptrs(gcs), fwd, ns), discs[1].ctx)
+    return J, gs, gcs, fwd[], ns[]
+end
 
 end # module
