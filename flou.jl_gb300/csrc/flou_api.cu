@@ -388,7 +388,8 @@ int32_t flou_create(const flou_config* cfg, flou_ctx** out) {
     if (cfg->equation < 0 || cfg->equation > 2) return FLOU_ERR_ARG;
     if (cfg->equation == FLOU_EQ_BURGERS && cfg->dim != 1) return FLOU_ERR_ARG;
     if (cfg->volume_op != FLOU_OP_STRONG && cfg->volume_op != FLOU_OP_SPLIT) return FLOU_ERR_ARG;
-    if (cfg->numflux < 0 || cfg->numflux > 4) return FLOU_ERR_ARG;
+    if (cfg->numflux < 0 || cfg->numflux > 6) return FLOU_ERR_ARG;
+    if (cfg->numflux_avg != FLOU_NF_STD_AVERAGE && cfg->numflux_avg != FLOU_NF_CHANDRASHEKAR) return FLOU_ERR_ARG;
     if (cfg->equation != FLOU_EQ_EULER && cfg->numflux != FLOU_NF_STD_AVERAGE && cfg->numflux != FLOU_NF_LXF)
         return FLOU_ERR_UNSUPPORTED;
     if (cfg->equation == FLOU_EQ_EULER && !(cfg->gamma > 1.0)) return FLOU_ERR_ARG;

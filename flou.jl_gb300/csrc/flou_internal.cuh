@@ -190,6 +190,85 @@ __device__ __forceinline__ void euler_face_flux(const double* ql, const double* 
     };
     if (kind == FLOU_NF_STD_AVERAGE) { stdavg(F); return; }
     if (kind == FLOU_NF_CHANDRASHEKAR) { chandra(F); return; }
+    if (kind == FLOU_NF_SCALAR_DISSIPATION || kind == FLOU_NF_MATRIX_DISSIPATION) {
+        double A[NV];
+        if (lxf_avg == FLOU_NF_CHANDRASHEKAR) chandra(A); else stdavg(A);
+        double vl[3] = {ul, DIM > 1 ? ql[2] / rl : 0.0, DIM > 2 ? ql[3] / rl : 0.0};
+        double vr[3] = {ur, DIM > 1 ? qr[2] / rr : 0.0, DIM > 2 ? qr[3] / rr : 0.0};
+        double vm[3] = {(vl[0] + vr[0]) / 2.0, (vl[1] + vr[1]) / 2.0, (vl[2] + vr[2]) / 2.0};
+        double bl = rl / (2.0 * pl), br = rr / (2.0 * pr);
+        double beta = logmean_ref(bl, br);
+        if (kind == FLOU_NF_SCALAR_DISSIPATION) {   // Euler.jl:233-301
+            double al = sqrt(g * pl / rl), ar = sqrt(g * pr / rr);
+            double lam = fmax(fabs(ul) + al, fabs(ur) + ar);
+            double D[NV];
+            D[0] = rr - rl;
+            // the 3D branch takes the left momenta from Qr (Euler.jl:257): no momentum jump there
+            for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? qr[1 + k] - qr[1 + k] : qr[1 + k] - ql[1 + k];
+            double c1 = 1.0 / beta / (g - 1.0);
+            for (int k = 0; k < DIM; ++k) c1 = c1 + vl[k] * vr[k];
+            double c2 = vm[0] * (vr[0] - vl[0]);
+            for (int k = 1; k < DIM; ++k) c2 = c2 + vm[k] * (vr[k] - vl[k]);
+            c2 = c2 + (1.0 / br - 1.0 / bl) / (2.0 * (g - 1.0));
+            D[DIM + 1] = c1 * (rr - rl) / 2.0 + ((rl + rr) / 2.0) * c2;
+            for (int k = 0; k < NV; ++k) F[k] = A[k] - lam / 2.0 * D[k] * intensity;
+            return;
+        }
+        // MatrixDissipation, Euler.jl:308-380: F = A + R Λ T Rᵀ (W_l - W_r)/2, evaluated as
+        // y = Rᵀ ΔW, z = Λ T y, R z (the same product in another association)
+        double vv = 0.0, sl2 = 0.0;
+        for (int k = 0; k < DIM; ++k) {
+            vv = vv + vm[k] * vm[k];
+            sl2 = sl2 + vl[k] * vl[k] + vr[k] * vr[k];
+        }
+        double v2 = 2.0 * vv - sl2 / 2.0;
+        double rho = logmean_ref(rl, rr);
+        double p = (rl + rr) / (2.0 * (bl + br));
+        double a = sqrt(g * p / rho);
+        double h = g / (2.0 * beta) / (g - 1.0) + v2 / 2.0;
+        double dW[NV];
+        {
+            double sLv = log(pl) - g * log(rl), sRv = log(pr) - g * log(rr);
+            double ml2 = 0.0, mr2 = 0.0;
+            for (int k = 0; k < DIM; ++k) {
+                ml2 = ml2 + ql[1 + k] * ql[1 + k];
+                mr2 = mr2 + qr[1 + k] * qr[1 + k];
+            }
+            dW[0] = ((g - sLv) / (g - 1.0) - ml2 / rl / (2.0 * pl)) - ((g - sRv) / (g - 1.0) - mr2 / rr / (2.0 * pr));
+            for (int k = 0; k < DIM; ++k) dW[1 + k] = ql[1 + k] / pl - qr[1 + k] / pr;
+            dW[DIM + 1] = -rl / pl + rr / pr;
+        }
+        const double u = vm[0];
+        // columns of R: acoustic (u - a), entropy (u), shear (one per tangential axis), acoustic (u + a)
+        double y[NV];
+        y[0] = dW[0] + (u - a) * dW[1];
+        y[DIM + 1] = dW[0] + (u + a) * dW[1];
+        double ye = dW[0] + u * dW[1];
+        for (int k = 1; k < DIM; ++k) {
+            y[0] = y[0] + vm[k] * dW[1 + k];
+            y[DIM + 1] = y[DIM + 1] + vm[k] * dW[1 + k];
+            ye = ye + vm[k] * dW[1 + k];
+            y[1 + k] = dW[1 + k] + vm[k] * dW[DIM + 1];
+        }
+        y[0] = y[0] + (h - u * a) * dW[DIM + 1];
+        y[DIM + 1] = y[DIM + 1] + (h + u * a) * dW[DIM + 1];
+        y[1] = ye + v2 / 2.0 * dW[DIM + 1];
+        double z[NV];
+        z[0] = fabs(u - a) * (rho / (2.0 * g)) * y[0];
+        z[1] = fabs(u) * ((g - 1.0) * rho / g) * y[1];
+        for (int k = 1; k < DIM; ++k) z[1 + k] = fabs(u) * p * y[1 + k];
+        z[DIM + 1] = fabs(u + a) * (rho / (2.0 * g)) * y[DIM + 1];
+        double o[NV];
+        o[0] = z[0] + z[1] + z[DIM + 1];
+        o[1] = (u - a) * z[0] + u * z[1] + (u + a) * z[DIM + 1];
+        o[DIM + 1] = (h - u * a) * z[0] + v2 / 2.0 * z[1] + (h + u * a) * z[DIM + 1];
+        for (int k = 1; k < DIM; ++k) {
+            o[1 + k] = vm[k] * (z[0] + z[1] + z[DIM + 1]) + z[1 + k];
+            o[DIM + 1] = o[DIM + 1] + vm[k] * z[1 + k];
+        }
+        for (int k = 0; k < NV; ++k) F[k] = A[k] + o[k] / 2.0 * intensity;
+        return;
+    }
     if (kind == FLOU_NF_LXF) {   // Euler.jl:138-165
         double A[NV];
         if (lxf_avg == FLOU_NF_CHANDRASHEKAR) chandra(A); else stdavg(A);
@@ -383,7 +462,8 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
             b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
         }
         double Fr[NV];
-        if (P.numflux == FLOU_NF_CHANDRASHEKAR || (P.numflux == FLOU_NF_LXF && P.lxf_avg == FLOU_NF_CHANDRASHEKAR))
+        if (P.numflux == FLOU_NF_CHANDRASHEKAR || P.numflux >= FLOU_NF_SCALAR_DISSIPATION ||
+            (P.numflux == FLOU_NF_LXF && P.lxf_avg == FLOU_NF_CHANDRASHEKAR))
             euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
         else
             euler_face_flux_fast<DIM>(a, b, P.numflux, inten, P.gamma, Fr);

@@ -8,7 +8,8 @@ from ._lib import DomainError, FlouError, load
 from .disc import Context, DofHandler, EquationConfig, MultielementDisc, get_max_dt, rhs_
 from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, EulerEquation, EulerInflowBC,
                         EulerOutflowBC, EulerSlipBC, HLL, HLLC, KennedyGruberAverage, LinearAdvection, LxF,
-                        OutflowBC, SplitDivOperator, StdAverage, StrongDivOperator)
+                        MatrixDissipation, OutflowBC, ScalarDissipation, SplitDivOperator, StdAverage,
+                        StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
 from .timeint import SSPRK33, timeintegrate

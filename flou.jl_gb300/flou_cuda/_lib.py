@@ -22,6 +22,7 @@ EQ_LINEAR_ADVECTION, EQ_BURGERS, EQ_EULER = 0, 1, 2
 OP_STRONG, OP_SPLIT = 0, 1
 TP_STD_AVERAGE, TP_CHANDRASHEKAR, TP_KENNEDY_GRUBER = 0, 1, 2
 NF_STD_AVERAGE, NF_LXF, NF_CHANDRASHEKAR, NF_HLL, NF_HLLC = 0, 1, 2, 3, 4
+NF_SCALAR_DISSIPATION, NF_MATRIX_DISSIPATION = 5, 6
 BC_OUTFLOW, BC_INFLOW, BC_SLIP = 1, 2, 3
 PTR_HOST, PTR_DEVICE = 0, 1
 

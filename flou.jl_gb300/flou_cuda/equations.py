@@ -120,6 +120,26 @@ class LxF:
         self.intensity = float(intensity)
 
 
+class ScalarDissipation:
+    """ScalarDissipation(avg, intensity): central flux `avg` minus λ/2 times the entropy-stable
+    scalar dissipation (Euler only; Euler.jl:228-301)."""
+    code = L.NF_SCALAR_DISSIPATION
+
+    def __init__(self, avg, intensity=1.0):
+        self.avg = avg
+        self.intensity = float(intensity)
+
+
+class MatrixDissipation:
+    """MatrixDissipation(avg, intensity): central flux `avg` plus R|Λ|TRᵀ(W_l - W_r)/2, the
+    entropy-stable matrix dissipation (Euler only; Euler.jl:303-380)."""
+    code = L.NF_MATRIX_DISSIPATION
+
+    def __init__(self, avg, intensity=1.0):
+        self.avg = avg
+        self.intensity = float(intensity)
+
+
 class HLL:
     code = L.NF_HLL
     avg = StdAverage()

@@ -57,6 +57,11 @@ tpcode(::ChandrasekharAverage) = Int32(1)
 nfcode(::StdAverage) = Int32(0)
 nfcode(::LxF) = Int32(1)
 nfcode(::ChandrasekharAverage) = Int32(2)
+nfcode(::ScalarDissipation) = Int32(5)
+nfcode(::MatrixDissipation) = Int32(6)
+
+# the central flux inside LxF / ScalarDissipation / MatrixDissipation, and their intensity
+has_avg(nf) = nf isa LxF || nf isa ScalarDissipation || nf isa MatrixDissipation
 
 function flou_config(disc, equation)
     op = disc.operators[1]
@@ -64,8 +69,8 @@ function flou_config(disc, equation)
     adv = equation isa LinearAdvection ? (Tuple(equation.a)..., zeros(3 - length(equation.a))...) : (0.0, 0.0, 0.0)
     vol = op isa SplitDivOperator ? Int32(1) : Int32(0)
     tp = op isa SplitDivOperator ? tpcode(op.tpflux) : Int32(0)
-    avg = nf isa LxF ? (nf.avg isa ChandrasekharAverage ? Int32(2) : Int32(0)) : Int32(0)
-    inten = nf isa LxF ? Float64(nf.intensity) : 1.0
+    avg = has_avg(nf) ? (nf.avg isa ChandrasekharAverage ? Int32(2) : Int32(0)) : Int32(0)
+    inten = has_avg(nf) ? Float64(nf.intensity) : 1.0
     gamma = equation isa EulerEquation ? Float64(equation.γ) : 1.4
     return FlouConfig(Int32(spatialdim(disc)), eqcode(equation), gamma, Float64.(adv), vol, tp,
                       nfcode(nf), avg, inten, Int32(length(disc.std.basis.ξ)))

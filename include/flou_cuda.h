@@ -63,6 +63,11 @@ extern "C" {
 #define FLOU_NF_CHANDRASHEKAR 2
 #define FLOU_NF_HLL 3
 #define FLOU_NF_HLLC 4
+/* Entropy-stable dissipation added to a central flux (numflux_avg: StdAverage or
+ * ChandrasekharAverage), Euler only: ScalarDissipation (Euler.jl:228-301) and
+ * MatrixDissipation (Euler.jl:303-380). */
+#define FLOU_NF_SCALAR_DISSIPATION 5
+#define FLOU_NF_MATRIX_DISSIPATION 6
 
 /* Boundary conditions applied on boundary faces (periodic faces are interior faces after
  * apply_periodicBCs!): EulerOutflowBC, EulerInflowBC(Qext), EulerSlipBC
@@ -89,7 +94,8 @@ typedef struct flou_config {
     int32_t volume_op;         /* FLOU_OP_*                                                 */
     int32_t twopoint_flux;     /* FLOU_TP_* (split form only)                               */
     int32_t numflux;           /* FLOU_NF_*                                                 */
-    int32_t numflux_avg;       /* averaging flux inside LxF: FLOU_NF_STD_AVERAGE or _CHANDRASHEKAR */
+    int32_t numflux_avg;       /* central flux inside LxF and the dissipation fluxes:
+                                  FLOU_NF_STD_AVERAGE or FLOU_NF_CHANDRASHEKAR                  */
     double numflux_intensity;  /* LxF intensity (1.0 = Rusanov)                             */
     int32_t nnodes;            /* nodes per direction n = p + 1, 2 <= n <= 8                */
 } flou_config;

@@ -443,7 +443,10 @@ inline StdOps std_operators(int n, bool lobatto) {
 enum EqKind { EQ_ADVECTION = 0, EQ_BURGERS = 1, EQ_EULER = 2 };
 enum VolOp { OP_STRONG = 0, OP_SPLIT = 1 };
 enum TwoPoint { TP_STDAVG = 0, TP_CHANDRASHEKAR = 1, TP_KENNEDY_GRUBER = 2 };
-enum NumFlux { NF_STDAVG = 0, NF_LXF = 1, NF_CHANDRASHEKAR = 2, NF_HLL = 3, NF_HLLC = 4 };
+enum NumFlux {
+    NF_STDAVG = 0, NF_LXF = 1, NF_CHANDRASHEKAR = 2, NF_HLL = 3, NF_HLLC = 4,
+    NF_SCALAR_DISSIPATION = 5, NF_MATRIX_DISSIPATION = 6
+};
 enum BcKind { BC_NONE = 0, BC_OUTFLOW = 1, BC_INFLOW = 2, BC_SLIP = 3 };
 
 struct Config {
@@ -643,6 +646,121 @@ template <class T> inline Vec<T> euler_hllc(const Vec<T>& Ql, const Vec<T>& Qr, 
     return F;
 }
 
+// Entropy variables, src/FlouCommon/Euler.jl:273-307 (s = log(p) - γ log(ρ), :202-206).
+template <class T> inline Vec<T> cons2entropy(const Vec<T>& Q, int dim, double g) {
+    using std::log;
+    T rho = Q[0];
+    T p = pressure(Q, dim, g);
+    T s = log(p) - g * log(rho);
+    T m2 = sq(Q[1]);
+    for (int k = 1; k < dim; ++k) m2 = m2 + sq(Q[1 + k]);
+    Vec<T> W{};
+    W[0] = (g - s) / (g - 1.0) - m2 / rho / (2.0 * p);
+    for (int k = 0; k < dim; ++k) W[1 + k] = Q[1 + k] / p;
+    W[dim + 1] = -rho / p;
+    return W;
+}
+
+template <class T> inline Vec<T> euler_average(const Vec<T>& Ql, const Vec<T>& Qr, int dim, double g, int avg) {
+    return avg == NF_CHANDRASHEKAR ? euler_chandrashekar(Ql, Qr, dim, g) : euler_stdavg(Ql, Qr, dim, g);
+}
+
+// ScalarDissipation, src/FlouSpatial/Equations/Euler.jl:228-301.  The 3D branch reads the left
+// momenta from Qr (Euler.jl:257), so its momentum jumps vanish; kept as written.
+template <class T>
+inline Vec<T> euler_scalar_dissipation(const Vec<T>& Ql, const Vec<T>& Qr, int dim, double g, int avg,
+                                       const T& intensity) {
+    using std::fabs; using std::max;
+    Vec<T> Pl = cons2prim(Ql, dim, g), Pr = cons2prim(Qr, dim, g);
+    T rl = Pl[0], rr = Pr[0], pl = Pl[dim + 1], pr = Pr[dim + 1];
+    T ml[3], mr[3], vm[3];
+    for (int k = 0; k < dim; ++k) {
+        mr[k] = Qr[1 + k];
+        ml[k] = (dim == 3) ? Qr[1 + k] : Ql[1 + k];
+        vm[k] = (Pl[1 + k] + Pr[1 + k]) / 2.0;
+    }
+    T rho = (rl + rr) / 2.0;
+    T bl = rl / (2.0 * pl), br = rr / (2.0 * pr);
+    T beta = logarithmic_mean(bl, br);
+    T al = soundvelocity(rl, pl, g), ar = soundvelocity(rr, pr, g);
+    Vec<T> Fn = euler_average(Ql, Qr, dim, g, avg);
+    T lam = max(fabs(Pl[1]) + al, fabs(Pr[1]) + ar);
+    Vec<T> D{};
+    D[0] = rr - rl;
+    for (int k = 0; k < dim; ++k) D[1 + k] = mr[k] - ml[k];
+    T c1 = 1.0 / beta / (g - 1.0);
+    for (int k = 0; k < dim; ++k) c1 = c1 + Pl[1 + k] * Pr[1 + k];
+    T c2 = vm[0] * (Pr[1] - Pl[1]);
+    for (int k = 1; k < dim; ++k) c2 = c2 + vm[k] * (Pr[1 + k] - Pl[1 + k]);
+    c2 = c2 + (1.0 / br - 1.0 / bl) / (2.0 * (g - 1.0));
+    D[dim + 1] = c1 * (rr - rl) / 2.0 + rho * c2;
+    Vec<T> F{};
+    for (int k = 0; k < dim + 2; ++k) F[k] = Fn[k] - lam / 2.0 * D[k] * intensity;
+    return F;
+}
+
+// MatrixDissipation, src/FlouSpatial/Equations/Euler.jl:303-380:
+// F = Fn + R Λ T Rᵀ (W_l - W_r)/2 · intensity, the matrix product formed first as written.
+template <class T>
+inline Vec<T> euler_matrix_dissipation(const Vec<T>& Ql, const Vec<T>& Qr, int dim, double g, int avg,
+                                       const T& intensity) {
+    using std::fabs;
+    Vec<T> Pl = cons2prim(Ql, dim, g), Pr = cons2prim(Qr, dim, g);
+    T rl = Pl[0], rr = Pr[0], pl = Pl[dim + 1], pr = Pr[dim + 1];
+    T vm[3], v2;
+    for (int k = 0; k < dim; ++k) vm[k] = (Pl[1 + k] + Pr[1 + k]) / 2.0;
+    if (dim == 1) v2 = 2.0 * sq(vm[0]) - (sq(Pl[1]) + sq(Pr[1])) / 2.0;
+    else if (dim == 2)
+        v2 = 2.0 * (sq(vm[0]) + sq(vm[1])) - (((sq(Pl[1]) + sq(Pl[2])) + sq(Pr[1])) + sq(Pr[2])) / 2.0;
+    else
+        v2 = 2.0 * ((sq(vm[0]) + sq(vm[1])) + sq(vm[2])) -
+             (((((sq(Pl[1]) + sq(Pl[2])) + sq(Pl[3])) + sq(Pr[1])) + sq(Pr[2])) + sq(Pr[3])) / 2.0;
+    T bl = rl / (2.0 * pl), br = rr / (2.0 * pr);
+    T rho = logarithmic_mean(rl, rr);
+    T p = (rl + rr) / (2.0 * (bl + br));
+    T beta = logarithmic_mean(bl, br);
+    T a = soundvelocity(rho, p, g);
+    T h = g / (2.0 * beta) / (g - 1.0) + v2 / 2.0;
+    Vec<T> Fn = euler_average(Ql, Qr, dim, g, avg);
+    Vec<T> Wl = cons2entropy(Ql, dim, g), Wr = cons2entropy(Qr, dim, g);
+    int nv = dim + 2;
+    T u = vm[0];
+    // R (column j = wave j), Λ and T as in the reference
+    T R[5][5], Lam[5], Td[5];
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) R[i][j] = T(0.0);
+    R[0][0] = T(1.0); R[1][0] = u - a;
+    R[0][1] = T(1.0); R[1][1] = u;
+    R[0][nv - 1] = T(1.0); R[1][nv - 1] = u + a;
+    for (int k = 1; k < dim; ++k) {
+        R[1 + k][0] = vm[k]; R[1 + k][1] = vm[k]; R[1 + k][nv - 1] = vm[k];
+        R[1 + k][1 + k] = T(1.0);
+        R[nv - 1][1 + k] = vm[k];
+    }
+    R[nv - 1][0] = h - u * a;
+    R[nv - 1][1] = v2 / 2.0;
+    R[nv - 1][nv - 1] = h + u * a;
+    Lam[0] = fabs(u - a); Lam[nv - 1] = fabs(u + a);
+    for (int k = 1; k < nv - 1; ++k) Lam[k] = fabs(u);
+    Td[0] = rho / (2.0 * g); Td[nv - 1] = rho / (2.0 * g);
+    Td[1] = (g - 1.0) * rho / g;
+    for (int k = 2; k < nv - 1; ++k) Td[k] = p;
+    T M[5][5];
+    for (int i = 0; i < nv; ++i)
+        for (int k = 0; k < nv; ++k) {
+            T acc = T(0.0);
+            for (int j = 0; j < nv; ++j) acc = acc + ((R[i][j] * Lam[j]) * Td[j]) * R[k][j];
+            M[i][k] = acc;
+        }
+    Vec<T> F{};
+    for (int i = 0; i < nv; ++i) {
+        T acc = T(0.0);
+        for (int k = 0; k < nv; ++k) acc = acc + M[i][k] * (Wl[k] - Wr[k]);
+        F[i] = Fn[i] + acc / 2.0 * intensity;
+    }
+    return F;
+}
+
 // numericalflux dispatch.  Ql/Qr are in the face frame (rotated), n is the physical
 // normal (used by the scalar equations).  Interfaces.jl:111-136; Euler.jl:99-226;
 // LinearAdvection.jl:27-39; Burgers.jl:27-38.
@@ -672,6 +790,8 @@ inline Vec<T> numericalflux(const Vec<T>& Ql, const Vec<T>& Qr, const double* n,
         case NF_CHANDRASHEKAR: return euler_chandrashekar(Ql, Qr, dim, c.gamma);
         case NF_HLL: return euler_hll(Ql, Qr, dim, c.gamma);
         case NF_HLLC: return euler_hllc(Ql, Qr, dim, c.gamma);
+        case NF_SCALAR_DISSIPATION: return euler_scalar_dissipation(Ql, Qr, dim, c.gamma, c.lxf_avg, intensity);
+        case NF_MATRIX_DISSIPATION: return euler_matrix_dissipation(Ql, Qr, dim, c.gamma, c.lxf_avg, intensity);
         default: break;
     }
     // LxF (Euler.jl:138-165)

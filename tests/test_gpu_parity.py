@@ -33,6 +33,10 @@ def _ops():
         "split_chandra_lxfc": lambda: F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)),
         "split_kg_lxf": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
         "split_std_lxf": lambda: F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)),
+        "split_chandra_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
+        "split_chandra_sd": lambda: F.SplitDivOperator(F.ScalarDissipation(F.ChandrasekharAverage(), 1.0)),
+        "strong_md_std": lambda: F.StrongDivOperator(F.MatrixDissipation(F.StdAverage(), 0.7)),
+        "strong_sd_std": lambda: F.StrongDivOperator(F.ScalarDissipation(F.StdAverage(), 1.0)),
     }
 
 
@@ -77,6 +81,37 @@ def _check(disc, Q, nsteps=5, res_tol=RES_TOL, step_tol=STEP_TOL, arrays=None):
 def test_euler_periodic(dim, n, ne, op):
     disc = build(dim, n, ne, _euler(dim), _ops()[op]())
     _check(disc, smooth_euler_state(disc, seed=dim * 10 + n))
+
+
+def _jumpy_state(disc, seed):
+    """A smooth state plus a different constant offset of the primitives in every element, so the
+    traces jump at every interface (the dissipation terms act)."""
+    eq = disc.equation
+    d = disc.mesh.dim
+    P = eq.vars_cons2prim(smooth_euler_state(disc, seed=seed))
+    rng = np.random.default_rng(seed)
+    P += np.repeat(0.05 * rng.standard_normal((disc.mesh.nelements, d + 2)), disc.std.n ** d, axis=0)
+    return np.asfortranarray(eq.vars_prim2cons(P))
+
+
+@pytest.mark.parametrize("dim,n,ne,op", [(1, 5, (6,), "split_chandra_md"), (1, 4, (5,), "split_chandra_sd"),
+                                         (2, 5, (3, 4), "split_chandra_md"), (2, 4, (3, 3), "split_chandra_sd"),
+                                         (2, 4, (3, 3), "strong_md_std"), (2, 3, (4, 3), "strong_sd_std"),
+                                         (3, 4, (2, 3, 2), "split_chandra_md"), (3, 3, (3, 2, 2), "split_chandra_sd"),
+                                         (3, 5, (2, 2, 2), "strong_md_std")])
+def test_euler_dissipation_fluxes(dim, n, ne, op):
+    """ScalarDissipation / MatrixDissipation (Euler.jl:228-380) on states whose traces jump."""
+    disc = build(dim, n, ne, _euler(dim), _ops()[op]())
+    _check(disc, _jumpy_state(disc, seed=dim * 7 + n))
+
+
+def test_euler_dissipation_fluxes_walls():
+    eq = _euler(2)
+    Pin = np.array([1.1, 0.0, 0.3, 1.05])
+    bcs = {"1": F.EulerSlipBC(), "2": F.EulerSlipBC(), "3": F.EulerInflowBC(eq.vars_prim2cons(Pin)),
+           "4": F.EulerOutflowBC()}
+    disc = build(2, 4, (3, 3), eq, _ops()["split_chandra_md"](), periodic=(), bcs=bcs)
+    _check(disc, _jumpy_state(disc, seed=3))
 
 
 @pytest.mark.parametrize("n", range(2, 9))

@@ -116,3 +116,67 @@ def test_oracle_max_dt_formula():
     c = np.sqrt(1.4 * P[:, 3] / P[:, 0])
     ref = np.min(0.5 * np.sqrt(2.5 ** 2 / 25) / (np.hypot(P[:, 1], P[:, 2]) + c))
     assert abs(dt - ref) < 1e-14 * ref
+
+
+def _entropy_rate(disc, Q, dQ):
+    """Σ_i J ω W(Q_i)·dQ_i: the semi-discrete rate of the total mathematical entropy."""
+    eq = disc.equation
+    d = disc.mesh.dim
+    g = eq.gamma
+    p = eq.pressure(Q)
+    s = np.log(p) - g * np.log(Q[:, 0])
+    m2 = np.sum(Q[:, 1:1 + d] ** 2, axis=1)
+    W = np.concatenate([((g - s) / (g - 1) - m2 / Q[:, 0] / (2 * p))[:, None], Q[:, 1:1 + d] / p[:, None],
+                        (-Q[:, 0] / p)[:, None]], axis=1)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    return w @ np.sum(W * dQ, axis=1), w @ np.sum(np.abs(W * dQ), axis=1)
+
+
+@pytest.mark.parametrize("flux,dim", [("matrix", 1), ("matrix", 2), ("matrix", 3), ("scalar", 1), ("scalar", 2)])
+def test_dissipative_fluxes_are_entropy_stable(flux, dim):
+    """Split form with the Chandrashekar volume flux and ScalarDissipation / MatrixDissipation of
+    the Chandrashekar average at the interfaces: the entropy can only decrease (Euler.jl:228-380),
+    and it does decrease when the traces jump.  (The 3D ScalarDissipation of the reference takes
+    the left momenta from the right state, Euler.jl:257, so its sign is not guaranteed there.)"""
+    eq = F.EulerEquation(dim, 1.4)
+    nf = (F.MatrixDissipation if flux == "matrix" else F.ScalarDissipation)(F.ChandrasekharAverage(), 1.0)
+    disc = build(dim, 4, (3,) * dim, eq, F.SplitDivOperator(F.ChandrasekharAverage(), nf))
+    o = oracle_for(disc)
+    Q = smooth_euler_state(disc, seed=5, amp=0.3)
+    dS0, scale0 = _entropy_rate(disc, Q, o.rhs(Q))   # LGL traces of a pointwise state do not jump
+    assert abs(dS0) < 1e-10 * scale0
+    # element-wise jumps: a different constant offset of the primitive variables per element
+    rng = np.random.default_rng(11)
+    P = eq.vars_cons2prim(Q)
+    npe = disc.std.n ** dim
+    P += np.repeat(0.05 * rng.standard_normal((disc.mesh.nelements, dim + 2)), npe, axis=0)
+    Qj = np.asfortranarray(eq.vars_prim2cons(P))
+    dS, scale = _entropy_rate(disc, Qj, o.rhs(Qj))
+    assert dS < -1e-6 * scale, (dS, scale)
+    # freestream preservation and conservation
+    P = np.zeros((disc.ndofs, dim + 2))
+    P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.3, 0.4, 2.0
+    assert np.max(np.abs(o.rhs(np.asfortranarray(eq.vars_prim2cons(P))))) < 1e-12
+    dQ = o.rhs(Q)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    for v in range(dim + 2):
+        assert abs(w @ dQ[:, v]) < 1e-12 * np.sum(w * np.abs(dQ[:, v]))
+
+
+def test_dissipative_fluxes_reduce_to_the_average_without_jumps():
+    """With continuous traces (a state that is one smooth polynomial across elements), the
+    dissipation terms vanish: ScalarDissipation and MatrixDissipation give the average flux."""
+    eq = F.EulerEquation(2, 1.4)
+    base = build(2, 4, (3, 3), eq, F.SplitDivOperator(F.ChandrasekharAverage(), F.ChandrasekharAverage()),
+                 periodic=(), bcs={"1": F.EulerOutflowBC(), "2": F.EulerOutflowBC(), "3": F.EulerOutflowBC(),
+                                   "4": F.EulerOutflowBC()})
+    X = base.coords
+    P = np.stack([1.2 + 0.1 * X[:, 0], 0.3 + 0.05 * X[:, 1], -0.2 + 0.02 * X[:, 0], 2.0 + 0.1 * X[:, 1]], axis=1)
+    Q = np.asfortranarray(eq.vars_prim2cons(P))
+    R0 = oracle_for(base).rhs(Q)
+    for nf in (F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), F.ScalarDissipation(F.ChandrasekharAverage(), 1.0)):
+        d = build(2, 4, (3, 3), eq, F.SplitDivOperator(F.ChandrasekharAverage(), nf), periodic=(),
+                  bcs={"1": F.EulerOutflowBC(), "2": F.EulerOutflowBC(), "3": F.EulerOutflowBC(),
+                       "4": F.EulerOutflowBC()})
+        R = oracle_for(d).rhs(Q)
+        assert np.max(np.abs(R - R0)) < 1e-12 * np.max(np.abs(R0))
