@@ -334,6 +334,11 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
             delete b;
             return r;
         }
+        if (c->limiter || c->mon_mask) {   // the persistent launch runs neither
+            c->err = "the batched launch runs no limiter and records no monitors";
+            delete b;
+            return FLOU_ERR_UNSUPPORTED;
+        }
         maxnpe = std::max(maxnpe, c->npe);
     }
     std::vector<const BatchKernel*> fit;

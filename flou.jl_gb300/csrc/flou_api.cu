@@ -158,12 +158,17 @@ int stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double
     return FLOU_OK;
 }
 
+// One SSP-RK3 step; with a limiter set, it acts after every stage (OrdinaryDiffEq's
+// stage_limiter!, FlouTime.jl:136-148), and the selected monitors are recorded after the step.
 int rk3_step(flou_ctx* c, cudaStream_t s, double* Q, double dt) {
     int r;
     if ((r = stage(c, s, Q, Q, c->d_U, 1, dt, 0.0, 1.0))) return r;
+    if ((r = ctx_limit(c, s, c->d_U))) return r;
     if ((r = stage(c, s, c->d_U, Q, c->d_U, 2, dt, 0.75, 0.25))) return r;
+    if ((r = ctx_limit(c, s, c->d_U))) return r;
     if ((r = stage(c, s, c->d_U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;
-    return FLOU_OK;
+    if ((r = ctx_limit(c, s, Q))) return r;
+    return ctx_record_monitors(c, s, Q);
 }
 
 int check_status(flou_ctx* c) {
@@ -374,6 +379,7 @@ int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, do
     return stage(c, s, Q, Q0, out, mode, dt, a0, a1, Fn);
 }
 int ctx_check_status(flou_ctx* c) { return check_status(c); }
+void drop_step_graph(flou_ctx* c) { drop_graph(c); }
 }  // namespace flou
 
 extern "C" {
@@ -424,6 +430,7 @@ int32_t flou_destroy(flou_ctx* c) {
                     c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c};
     for (void* b : bufs)
         if (b) cudaFree(b);
+    ctx_free_limiter(c);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return FLOU_OK;
@@ -530,6 +537,9 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     int r = validate_pack_geometry(c->cfg.dim, c->n, c->nelem, c->nfaces, c->omega.data(), c->h_face_elem, J, Ja,
                                    frames, face_J, invJ, Jd, fJ, dx, msg);
     if (r) return fail(c, r, "%s", msg.c_str());
+    std::vector<double> Jel(c->nelem);
+    for (int e = 0; e < c->nelem; ++e) Jel[e] = J[(size_t)e * c->npe];
+    if ((r = upload(c, &c->d_Jel, Jel.data(), Jel.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_invJ, invJ.data(), invJ.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_Ja, Jd.data(), Jd.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;

@@ -43,6 +43,16 @@ struct flou_ctx {
     double* d_c = nullptr;          // optional per-element LxF dissipation scale
     int32_t* d_status = nullptr;    // [flags, lowest element]
     unsigned long long* d_dtmin = nullptr;
+    // Zhang-Shu limiter and integral monitors (limiter.cu)
+    int limiter = 0;                // FLOU_LIMITER_*
+    double lim_min = 0.0;
+    double* d_Jel = nullptr;        // J per element
+    double* d_wtp = nullptr;        // tensor-product quadrature weights [npe]
+    int mon_mask = 0, mon_cap = 0;  // monitors recorded after every flou_step step
+    double* d_mon = nullptr;        // [mon_cap][2]: kinetic energy, entropy
+    int32_t* d_moncount = nullptr;  // [0]: steps recorded, [1]: single-evaluation slot counter
+    double* d_monpart = nullptr;    // block partial sums
+    double* d_monval = nullptr;     // single evaluation [2]
     // graph cache for flou_step
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -62,4 +72,9 @@ ElemLaunch ctx_elem_launch(const flou_ctx* c);
 int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double* out, int mode, double dt,
               double a0, double a1, double* Fn = nullptr);   // Fn: face-flux scratch (NULL: the context's)
 int ctx_check_status(flou_ctx* c);
+// limiter.cu: the stage limiter on Q (no-op when off) and the per-step monitor record
+int ctx_limit(flou_ctx* c, cudaStream_t s, double* Q);
+int ctx_record_monitors(flou_ctx* c, cudaStream_t s, const double* Q);
+void ctx_free_limiter(flou_ctx* c);
+void drop_step_graph(flou_ctx* c);   // settings that change the captured step
 }  // namespace flou

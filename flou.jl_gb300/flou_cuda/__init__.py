@@ -12,7 +12,7 @@ from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, Eule
                         StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
-from .timeint import SSPRK33, timeintegrate
+from .timeint import SSPRK33, get_limiter_callback, get_monitor_callback, timeintegrate
 from . import initial
 from .batch import Batch, adjoint_solve_batch
 

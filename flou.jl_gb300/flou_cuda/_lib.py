@@ -23,6 +23,8 @@ OP_STRONG, OP_SPLIT = 0, 1
 TP_STD_AVERAGE, TP_CHANDRASHEKAR, TP_KENNEDY_GRUBER = 0, 1, 2
 NF_STD_AVERAGE, NF_LXF, NF_CHANDRASHEKAR, NF_HLL, NF_HLLC = 0, 1, 2, 3, 4
 NF_SCALAR_DISSIPATION, NF_MATRIX_DISSIPATION = 5, 6
+LIMITER_NONE, LIMITER_ZHANG_SHU = 0, 1
+MONITOR_KINETIC_ENERGY, MONITOR_ENTROPY = 1, 2
 BC_OUTFLOW, BC_INFLOW, BC_SLIP = 1, 2, 3
 PTR_HOST, PTR_DEVICE = 0, 1
 
@@ -97,6 +99,11 @@ PROTOTYPES = {
                             ctypes.c_char_p, ctypes.c_int32],
     "flou_rhs_vjp": [_P, _P, _P, _P, _P],
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
+    "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
+    "flou_limit": [_P, _P, ctypes.c_int32],
+    "flou_monitor": [_P, _P, ctypes.c_int32, _D, ctypes.c_int32],
+    "flou_set_monitors": [_P, ctypes.c_int32, ctypes.c_int32],
+    "flou_take_monitors": [_P, _D, ctypes.c_int32, _I32],
     "flou_adjoint_solve_batch": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D, ctypes.c_int32,
                                  ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D,
                                  ctypes.POINTER(_P), ctypes.POINTER(_P), _I64, _I32],

@@ -244,6 +244,32 @@ class Context:
     def wait(self):
         L.check(self._lib.flou_wait(self.h), self.h)
 
+    def set_limiter(self, kind, minval=0.0):
+        """FLOU_LIMITER_ZHANG_SHU with its minimum value, or FLOU_LIMITER_NONE."""
+        L.check(self._lib.flou_set_limiter(self.h, int(kind), float(minval)), self.h)
+
+    def limit(self, Q):
+        """The set limiter applied once to Q in place."""
+        pq, kq = self._ptr(Q, True)
+        L.check(self._lib.flou_limit(self.h, pq, kq), self.h)
+
+    def monitor(self, Q, which):
+        pq, kq = self._ptr(Q)
+        v = ctypes.c_double()
+        L.check(self._lib.flou_monitor(self.h, pq, int(which), ctypes.byref(v), kq), self.h)
+        return v.value
+
+    def set_monitors(self, mask, capacity=1024):
+        L.check(self._lib.flou_set_monitors(self.h, int(mask), int(capacity)), self.h)
+
+    def take_monitors(self, max_steps=1 << 20):
+        """(nsteps, 2) array of (kinetic energy, entropy) recorded after each step since the last take."""
+        out = np.zeros((max_steps, 2))
+        n = ctypes.c_int32()
+        L.check(self._lib.flou_take_monitors(self.h, out.ctypes.data_as(L._D), int(max_steps), ctypes.byref(n)),
+                self.h)
+        return out[:n.value].copy()
+
     def max_dt(self, Q, cfl):
         pq, kq = self._ptr(Q)
         out = ctypes.c_double()

@@ -17,6 +17,7 @@ using ChainRulesCore
 using LinearAlgebra
 
 export GPUDisc, SSPRK3GPU, GPUBatch, solve_functional, solve_functional_batch
+export set_limiter!, monitor, record_monitors!, take_monitors!
 
 const libflou = joinpath(@__DIR__, "..", "..", "..", "lib", "libflou_cuda.so")
 
@@ -198,6 +199,53 @@ function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, 
         disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), pointer(gc), nf), disc.ctx)
     pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, J̄ .* gc, NoTangent(), NoTangent(), NoTangent(), NoTangent())
     return J[], pullback
+end
+
+# ---- stage limiter and monitors (Euler.jl:541-654, FlouTime.jl:107-148) ------------------------------
+"""
+    set_limiter!(disc::GPUDisc, :zhang_shu, minval)
+
+The Zhang-Shu limiter that `get_limiter_callback(disc, eq, :zhang_shu, minval)` passes to
+OrdinaryDiffEq as `stage_limiter!`; here it runs after every stage inside `flou_step`'s graph.
+`set_limiter!(disc, :none)` turns it off.
+"""
+function set_limiter!(disc::GPUDisc, name::Symbol, minval=0.0)
+    kind = name == :zhang_shu ? Int32(1) : name == :none ? Int32(0) : error("Unknown limiter '$(name)'.")
+    check(ccall((:flou_set_limiter, libflou), Int32, (Ptr{Cvoid}, Int32, Float64), disc.ctx, kind, minval), disc.ctx)
+end
+
+monitor_code(name::Symbol) = name in (:energy, :kinetic_energy) ? Int32(1) :
+                             name == :entropy ? Int32(2) : error("Unknown monitor '$(name)'.")
+
+"""
+    monitor(disc::GPUDisc, Q::Matrix{Float64}, name) -> value
+
+`get_monitor(disc, equation, name)` evaluated on the GPU: `:energy` / `:kinetic_energy` or `:entropy`.
+"""
+function monitor(disc::GPUDisc, Q::Matrix{Float64}, name::Symbol)
+    v = Ref{Float64}(0.0)
+    GC.@preserve Q check(ccall((:flou_monitor, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ref{Float64}, Int32),
+                               disc.ctx, Q, monitor_code(name), v, PTR_HOST), disc.ctx)
+    return v[]
+end
+
+"""
+    record_monitors!(disc, names, capacity); take_monitors!(disc) -> Matrix (nsteps × 2)
+
+Monitors recorded after every step of `flou_step` (get_monitor_callback with iter=true) without a
+host round trip; columns: kinetic energy, entropy.
+"""
+function record_monitors!(disc::GPUDisc, names, capacity)
+    mask = reduce(|, (monitor_code(n) for n in names); init=Int32(0))
+    check(ccall((:flou_set_monitors, libflou), Int32, (Ptr{Cvoid}, Int32, Int32), disc.ctx, mask, capacity), disc.ctx)
+end
+
+function take_monitors!(disc::GPUDisc, max_steps=1 << 16)
+    out = zeros(2, max_steps)
+    n = Ref{Int32}(0)
+    check(ccall((:flou_take_monitors, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ref{Int32}),
+                disc.ctx, out, max_steps, n), disc.ctx)
+    return permutedims(out[:, 1:n[]])
 end
 
 # ---- batched mode --------------------------------------------------------------------------------

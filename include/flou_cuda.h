@@ -241,6 +241,31 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
                                  double* const* dJdQ0, double* const* dJdc, int64_t* forward_steps,
                                  int32_t* nsnap);
 
+/* ---- stage limiter and integral monitors (Euler) ----------------------------------------------
+ * The Zhang-Shu positivity limiter of src/FlouSpatial/Equations/Euler.jl:611-654 (`get_limiter`
+ * :zhang_shu with its minimum value), applied after every SSP-RK3 stage of flou_step /
+ * flou_step_async, as Flou's `get_limiter_callback` passed as OrdinaryDiffEq's stage_limiter!
+ * (src/FlouTime/FlouTime.jl:136-148).  Per element: the density, then all variables, are scaled
+ * toward the element mean when the minimum density / pressure falls below min(minval, mean). */
+#define FLOU_LIMITER_NONE 0
+#define FLOU_LIMITER_ZHANG_SHU 1
+int32_t flou_set_limiter(flou_ctx* ctx, int32_t kind, double minval);
+/* The set limiter applied once to Q in place (host or device memory by ptr_kind). */
+int32_t flou_limit(flou_ctx* ctx, double* Q, int32_t ptr_kind);
+/* Integral monitors (Euler.jl:541-590, get_monitor :energy / :entropy): Σ_e Jω'·f(Q) with f the
+ * kinetic energy |ρv|²/(2ρ) or the mathematical entropy -ρ(log p - γ log ρ)/(γ-1). */
+#define FLOU_MONITOR_KINETIC_ENERGY 1
+#define FLOU_MONITOR_ENTROPY 2
+int32_t flou_monitor(flou_ctx* ctx, const double* Q, int32_t which, double* value, int32_t ptr_kind);
+/* Monitors recorded after every step of flou_step / flou_step_async (Flou's
+ * get_monitor_callback with iter=true) into a device buffer of `capacity` steps, without host
+ * synchronisation; mask = OR of FLOU_MONITOR_* bits (0 stops recording).  flou_take_monitors
+ * copies the values recorded since the last take, two per step (kinetic energy, entropy;
+ * unselected ones are 0), and restarts the record; FLOU_ERR_STATE if more steps ran than
+ * `capacity`. */
+int32_t flou_set_monitors(flou_ctx* ctx, int32_t mask, int32_t capacity);
+int32_t flou_take_monitors(flou_ctx* ctx, double* out, int32_t max_steps, int32_t* nsteps);
+
 /* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
  * Many independent discretizations with uneven element counts and orders advance together:
  * one persistent launch per SSP-RK3 stage serves every instance from one work queue of face

@@ -1156,6 +1156,99 @@ template <class T> void ssprk3_step(const Disc& g, T* Q, double dt, double t, Wo
     for (long i = 0; i < N; ++i) Q[i] = (1.0 / 3.0) * Q[i] + (2.0 / 3.0) * (U[i] + dt * L[i]);
 }
 
+// Zhang–Shu positivity limiter as written in src/FlouSpatial/Equations/Euler.jl:611-654, per
+// element: Q̄ = Σ Jω Q / vol (vol = Σ Jω, PhysicalRegions.jl:366-407); density scaled toward ρ̄
+// with θ = |(ρ̄ - m)/(ρ̄ - ρ_min)|, m = min(minval, ρ̄), when θ <= 1; then the pressure of the
+// density-limited nodes gives p̄ = Σ Jω p / vol and θ = |(p̄ - m)/(p̄ - p_min)|, m = min(minval,
+// p̄), and when θ <= 1 every variable is scaled toward the mean Q̄ taken before the density
+// step.  `omega` holds the tensor-product quadrature weights per element node.
+inline void zhang_shu(const Disc& g, double* Q, double minval, const std::vector<double>& omega) {
+    const Config& c = g.cfg;
+    long nd = g.ndofs();
+    int nv = c.nv, npe = g.npe;
+    std::vector<double> Jw(npe), p(npe);
+    for (int e = 0; e < g.nelem; ++e) {
+        long b = (long)e * npe;
+        double vol = 0.0;
+        for (int i = 0; i < npe; ++i) {
+            Jw[i] = g.J[b + i] * omega[i];
+            vol = vol + Jw[i];
+        }
+        Vec<double> Qm{};
+        for (int k = 0; k < nv; ++k) {
+            double acc = 0.0;
+            for (int i = 0; i < npe; ++i) acc = acc + Jw[i] * Q[k * nd + b + i];
+            Qm[k] = acc / vol;
+        }
+        double m = std::min(minval, Qm[0]);
+        double rmin = INFINITY;
+        for (int i = 0; i < npe; ++i) rmin = std::min(rmin, Q[b + i]);
+        double th = std::fabs((Qm[0] - m) / (Qm[0] - rmin));
+        if (th <= 1.0)
+            for (int i = 0; i < npe; ++i) Q[b + i] = th * (Q[b + i] - Qm[0]) + Qm[0];
+        double ps = 0.0, pmin = INFINITY;
+        for (int i = 0; i < npe; ++i) {
+            p[i] = pressure(getv(Q, nd, b + i, nv), c.dim, c.gamma);
+            ps = ps + Jw[i] * p[i];
+            pmin = std::min(pmin, p[i]);
+        }
+        double pbar = ps / vol;
+        m = std::min(minval, pbar);
+        th = std::fabs((pbar - m) / (pbar - pmin));
+        if (th <= 1.0)
+            for (int i = 0; i < npe; ++i)
+                for (int k = 0; k < nv; ++k) Q[k * nd + b + i] = th * (Q[k * nd + b + i] - Qm[k]) + Qm[k];
+    }
+}
+
+// Integral monitors, src/FlouSpatial/Equations/Euler.jl:560-590: Σ_e Jω'·f(Q) with f the kinetic
+// energy |ρv|²/(2ρ) (which = 1, Euler.jl:162-175 in FlouCommon) or the mathematical entropy
+// -ρ s/(γ-1), s = log p - γ log ρ (which = 2, FlouCommon/Euler.jl:202-217).
+inline double monitor(const Disc& g, const double* Q, int which, const std::vector<double>& omega) {
+    const Config& c = g.cfg;
+    long nd = g.ndofs();
+    double total = 0.0;
+    for (int e = 0; e < g.nelem; ++e) {
+        long b = (long)e * g.npe;
+        double se = 0.0;
+        for (int i = 0; i < g.npe; ++i) {
+            Vec<double> q = getv(Q, nd, b + i, c.nv);
+            double f;
+            if (which == 1) {
+                double m2 = sq(q[1]);
+                for (int k = 1; k < c.dim; ++k) m2 = m2 + sq(q[1 + k]);
+                f = m2 / (2.0 * q[0]);
+            } else {
+                double pr = pressure(q, c.dim, c.gamma);
+                double sv = std::log(pr) - c.gamma * std::log(q[0]);
+                f = -q[0] * sv / (c.gamma - 1.0);
+            }
+            se = se + (g.J[b + i] * omega[i]) * f;
+        }
+        total = total + se;
+    }
+    return total;
+}
+
+// SSP-RK3 with the limiter as OrdinaryDiffEq's stage_limiter! (FlouTime.jl:136-148): applied
+// to U1, U2 and the new state.
+inline void ssprk3_step_limited(const Disc& g, double* Q, double dt, double t, Workspace<double>& ws,
+                                std::vector<double>& U, std::vector<double>& L, double minval,
+                                const std::vector<double>& omega) {
+    long N = g.ndofs() * g.cfg.nv;
+    U.resize(N);
+    L.resize(N);
+    rhs(g, L.data(), Q, t, ws);
+    for (long i = 0; i < N; ++i) U[i] = Q[i] + dt * L[i];
+    zhang_shu(g, U.data(), minval, omega);
+    rhs(g, L.data(), U.data(), t + dt, ws);
+    for (long i = 0; i < N; ++i) U[i] = 0.75 * Q[i] + 0.25 * (U[i] + dt * L[i]);
+    zhang_shu(g, U.data(), minval, omega);
+    rhs(g, L.data(), U.data(), t + 0.5 * dt, ws);
+    for (long i = 0; i < N; ++i) Q[i] = (1.0 / 3.0) * Q[i] + (2.0 / 3.0) * (U[i] + dt * L[i]);
+    zhang_shu(g, Q, minval, omega);
+}
+
 // get_max_dt, MultielementDiscontinuous.jl:162-178 with the pointwise estimates of
 // src/FlouCommon/Euler.jl:116-135, LinearAdvection.jl:46-48, Burgers.jl:35-37 (no abs, as
 // in the reference).  `omega` holds the tensor-product quadrature weights per element node.

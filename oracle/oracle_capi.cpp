@@ -301,6 +301,32 @@ int oracle_ssprk3(void* hp, double* Q, double dt, int nsteps, double t0) {
     return 0;
 }
 
+void oracle_limit(void* hp, double* Q, double minval, const double* omega_tp) {
+    Handle* h = (Handle*)hp;
+    std::vector<double> w(omega_tp, omega_tp + h->g.npe);
+    zhang_shu(h->g, Q, minval, w);
+}
+
+double oracle_monitor(void* hp, const double* Q, int which, const double* omega_tp) {
+    Handle* h = (Handle*)hp;
+    std::vector<double> w(omega_tp, omega_tp + h->g.npe);
+    return monitor(h->g, Q, which, w);
+}
+
+int oracle_ssprk3_limited(void* hp, double* Q, double dt, int nsteps, double t0, double minval,
+                          const double* omega_tp) {
+    Handle* h = (Handle*)hp;
+    std::vector<double> w(omega_tp, omega_tp + h->g.npe);
+    try {
+        for (int s = 0; s < nsteps; ++s)
+            ssprk3_step_limited(h->g, Q, dt, t0 + s * dt, h->ws, h->U, h->L, minval, w);
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "oracle_ssprk3_limited: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
 double oracle_max_dt(void* hp, const double* Q, double cfl, const double* omega_tp) {
     Handle* h = (Handle*)hp;
     std::vector<double> w(omega_tp, omega_tp + h->g.npe);

@@ -37,6 +37,11 @@ def lib():
         _lib.oracle_ssprk3.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double]
         _lib.oracle_max_dt.restype = ctypes.c_double
         _lib.oracle_max_dt.argtypes = [ctypes.c_void_p, D, ctypes.c_double, D]
+        _lib.oracle_limit.argtypes = [ctypes.c_void_p, D, ctypes.c_double, D]
+        _lib.oracle_monitor.restype = ctypes.c_double
+        _lib.oracle_monitor.argtypes = [ctypes.c_void_p, D, ctypes.c_int, D]
+        _lib.oracle_ssprk3_limited.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, D]
         _lib.oracle_count_rhs.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
@@ -136,6 +141,24 @@ class Disc:
     def ssprk3(self, Q, dt, nsteps, t0=0.0):
         Q = np.array(Q, dtype=np.float64, order="F", copy=True)
         if self.L.oracle_ssprk3(self.h, _d(Q), dt, nsteps, t0) != 0:
+            raise RuntimeError("oracle ssprk3 failed")
+        return Q
+
+    def limit(self, Q, minval, omega_tp):
+        """Zhang–Shu limiter (Euler.jl:611-654) applied once; returns the limited copy."""
+        Q = np.array(Q, dtype=np.float64, order="F", copy=True)
+        self.L.oracle_limit(self.h, _d(Q), minval, _d(np.ascontiguousarray(omega_tp)))
+        return Q
+
+    def monitor(self, Q, which, omega_tp):
+        """1: kinetic energy, 2: mathematical entropy (Euler.jl:560-590)."""
+        Q = np.asfortranarray(Q, dtype=np.float64)
+        return self.L.oracle_monitor(self.h, _d(Q), int(which), _d(np.ascontiguousarray(omega_tp)))
+
+    def ssprk3_limited(self, Q, dt, nsteps, minval, omega_tp, t0=0.0):
+        Q = np.array(Q, dtype=np.float64, order="F", copy=True)
+        if self.L.oracle_ssprk3_limited(self.h, _d(Q), dt, nsteps, t0, minval,
+                                        _d(np.ascontiguousarray(omega_tp))) != 0:
             raise RuntimeError("oracle ssprk3 failed")
         return Q
 

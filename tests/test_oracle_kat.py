@@ -180,3 +180,59 @@ def test_dissipative_fluxes_reduce_to_the_average_without_jumps():
                        "4": F.EulerOutflowBC()})
         R = oracle_for(d).rhs(Q)
         assert np.max(np.abs(R - R0)) < 1e-12 * np.max(np.abs(R0))
+
+
+def _dipped_state(disc, seed, rho_dip=0.02, p_dip=0.03):
+    """Smooth state with a density dip in one element and a pressure dip in another."""
+    eq = disc.equation
+    P = eq.vars_cons2prim(smooth_euler_state(disc, seed=seed, amp=0.2))
+    npe = disc.std.n ** disc.mesh.dim
+    ne = disc.mesh.nelements
+    P[1 * npe + npe // 2, 0] = rho_dip
+    P[(ne - 1) * npe + 1, -1] = p_dip
+    return np.asfortranarray(eq.vars_prim2cons(P))
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_zhang_shu_limiter_properties(dim):
+    """Euler.jl:611-654: element means are kept, the density is raised to min(minval, ρ̄), and
+    elements already above the thresholds are untouched bit for bit."""
+    eq = F.EulerEquation(dim, 1.4)
+    disc = build(dim, 4, (3,) * dim, eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    o = oracle_for(disc)
+    Q = _dipped_state(disc, seed=4)
+    minval = 0.1
+    Ql = o.limit(Q, minval, disc.std.omega)
+    npe = disc.std.n ** dim
+    w = disc.std.omega
+    J = disc.J
+    changed = 0
+    for e in range(disc.mesh.nelements):
+        sl = slice(e * npe, (e + 1) * npe)
+        jw = J[sl] * w
+        m0 = jw @ Q[sl]
+        m1 = jw @ Ql[sl]
+        assert np.allclose(m1, m0, rtol=1e-13, atol=1e-15 * np.max(np.abs(m0)))
+        rbar = m0[0] / jw.sum()
+        assert Ql[sl, 0].min() >= min(minval, rbar) * (1 - 1e-13)
+        p = eq.pressure(Q[sl])
+        if Q[sl, 0].min() > minval and p.min() > minval:
+            assert np.array_equal(Ql[sl], Q[sl])
+        else:
+            changed += 1
+    assert changed == 2
+
+
+def test_monitors_and_limited_steps_are_consistent():
+    """The kinetic-energy monitor of the oracle equals the quadrature of |ρv|²/2ρ, and limited
+    steps keep the density above the minimum."""
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 4, (4, 4), eq, F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)))
+    o = oracle_for(disc)
+    Q = _dipped_state(disc, seed=8)
+    w = np.tile(disc.std.omega, disc.mesh.nelements) * disc.J
+    ke = w @ (np.sum(Q[:, 1:3] ** 2, axis=1) / (2 * Q[:, 0]))
+    assert abs(o.monitor(Q, 1, disc.std.omega) - ke) < 1e-12 * abs(ke)
+    dt = 0.2 * o.max_dt(Q, 1.0, disc.std.omega)
+    Qs = o.ssprk3_limited(Q, dt, 4, 0.05, disc.std.omega)
+    assert Qs[:, 0].min() > 0.0
