@@ -612,6 +612,27 @@ def main():
     if fp64_ops and fp64_peak:
         roofline["fp64"]["frac"] = roofline["fp64"]["achieved_gflops"] / fp64_peak
 
+    # ---- cost of the Zhang-Shu stage limiter (minval 1e-10, as examples/src/3D_Euler.jl:76) ----
+    limiter = None
+    try:
+        m0 = meshes[0]
+        q = m0["Qd"].clone()
+        res = {}
+        for tag, on in (("off", False), ("on", True)):
+            m0["ctx"].set_limiter(F._lib.LIMITER_ZHANG_SHU if on else F._lib.LIMITER_NONE, 1e-10)
+            m0["ctx"].step(q, m0["dt"], 2)   # capture
+            torch.cuda.synchronize()
+            e0.record(stream)
+            m0["ctx"].step(q, m0["dt"], steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            res[tag] = e0.elapsed_time(e1) / steps
+        m0["ctx"].set_limiter(F._lib.LIMITER_NONE)
+        limiter = {"mesh": m0["name"], "ms_per_step_off": res["off"], "ms_per_step_on": res["on"],
+                   "overhead": res["on"] / res["off"] - 1.0, "minval": 1e-10}
+    except Exception as exc:   # reported, not fatal to the bench line
+        limiter = {"error": str(exc)}
+
     # ---- e2e: through the public API with pinned host buffers ----
     hosts = []
     for m in meshes:
@@ -665,7 +686,7 @@ def main():
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
-            "adjoint_batch": adjoint_batch, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
+            "adjoint_batch": adjoint_batch, "limiter": limiter, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
     if dist is not None:
