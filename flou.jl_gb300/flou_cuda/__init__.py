@@ -11,6 +11,7 @@ from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, Eule
                         MatrixDissipation, OutflowBC, ScalarDissipation, SplitDivOperator, StdAverage,
                         StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs
+from .unstructured import UnstructuredMesh, perturbed_box, read_gmsh, write_gmsh22
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
 from .timeint import SSPRK33, get_limiter_callback, get_monitor_callback, timeintegrate
 from . import initial

@@ -14,6 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib as L
+from .unstructured import UnstructuredMesh, unstructured_geometry
 from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, HLL, HLLC, LinearAdvection, LxF,
                         SplitDivOperator, StdAverage, StrongDivOperator)
 
@@ -94,10 +95,14 @@ class MultielementDisc:
         self.mesh, self.std, self.equation, self.operator = mesh, std, equation, operator
         self.bcs = [None] * mesh.nboundaries
         for key, value in bcs.items():
-            self.bcs[mesh.bdmap[int(key)] - 1] = value
+            b = mesh.boundary_index(key) if hasattr(mesh, "boundary_index") else mesh.bdmap[int(key)]
+            self.bcs[b - 1] = value
         n, d = std.n, mesh.dim
         self.dofhandler = DofHandler(mesh.nelements, mesh.nfaces, n ** d, n ** (d - 1))
-        self.J, self.Ja, self.frames, self.faceJ, self.coords = cartesian_geometry(mesh, std)
+        if isinstance(mesh, UnstructuredMesh):
+            self.J, self.Ja, self.frames, self.faceJ, self.coords = unstructured_geometry(mesh, std)
+        else:
+            self.J, self.Ja, self.frames, self.faceJ, self.coords = cartesian_geometry(mesh, std)
         self.config = self._config()
         self._ctx = None
 

@@ -1,0 +1,151 @@
+"""Unstructured straight-sided meshes (GmshMesh.jl:16-394, Mesh.jl:380-487) and their geometry
+(PhysicalRegions.jl:438-472, 756-971), checked on the oracle: residuals are invariant under any
+rotation of the elements' local numbering (face orientations, master2slave, frames), freestream is
+preserved, and an unperturbed unrotated box reproduces CartesianMesh's geometry."""
+import os
+
+import numpy as np
+import pytest
+
+import flou_cuda as F
+from cases import oracle_for, smooth_euler_state
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _std(d, n, nv):
+    b = F.LagrangeBasis("GLL", n)
+    return {1: F.StdSegment, 2: F.StdQuad, 3: F.StdHex}[d](b, F.DGSEMrec(b), nv)
+
+
+def _disc(mesh, n, op, eq=None):
+    d = mesh.dim
+    eq = eq or F.EulerEquation(d, 1.4)
+    bcs = {name: F.EulerOutflowBC() for name in mesh.bdnames}
+    return F.MultielementDisc(mesh, _std(d, n, eq.nvariables), eq, op, bcs)
+
+
+def _state(disc, seed=0):
+    """A smooth state defined on physical coordinates (the same at the same point of any mesh)."""
+    d = disc.mesh.dim
+    X = disc.coords
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 6, size=(d + 2, 3))
+    P = np.zeros((disc.ndofs, d + 2))
+    for v in range(d + 2):
+        w = np.ones(disc.ndofs)
+        for q in range(d):
+            w = w * np.cos(2.0 * X[:, q] + ph[v, q])
+        P[:, v] = (1.0 if v in (0, d + 1) else 0.0) + (0.1 if v in (0, d + 1) else 0.3) * w
+    return np.asfortranarray(disc.equation.vars_prim2cons(P))
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_mesh_topology(dim):
+    nel = 3
+    m = F.perturbed_box(dim, nel, (0.0,) * dim, (1.0,) * dim, amp=0.1, seed=2)
+    assert m.nfaces == dim * nel ** (dim - 1) * (nel + 1)
+    assert len(m.intfaces) == dim * nel ** (dim - 1) * (nel - 1)
+    assert sorted(m.bdnames) == [str(k) for k in range(1, 2 * dim + 1)]
+    for b in m.bdfaces:
+        assert len(b) == nel ** (dim - 1)
+    # every element face points back to its element
+    for e in range(m.nelements):
+        for p in range(2 * dim):
+            f, s = m.faceinds[e, p] - 1, m.facepos[e, p] - 1
+            assert m.eleminds[f, s] == e + 1 and m.elempos[f, s] == p + 1
+    assert int(m.orientation.max()) <= (1 if dim == 2 else 7 if dim == 3 else 0)
+    plain = F.perturbed_box(dim, nel, (0.0,) * dim, (1.0,) * dim, amp=0.1, seed=2, rotate=False)
+    assert not plain.orientation.any()
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_unperturbed_box_reproduces_cartesian_geometry(dim):
+    n, nel = 4, 3
+    um = F.perturbed_box(dim, nel, (0.0,) * dim, (2.0,) * dim, amp=0.0, rotate=False)
+    cm = F.CartesianMesh((0.0,) * dim, (2.0,) * dim, (nel,) * dim)
+    op = F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
+    du, dc = _disc(um, n, op), _disc(cm, n, op)
+    npe = n ** dim
+    # same elements in the same order (x fastest) with the same local numbering
+    assert np.allclose(du.coords, dc.coords, atol=1e-14)
+    assert np.allclose(du.J, dc.J, rtol=1e-14)
+    assert np.allclose(du.Ja, dc.Ja, rtol=1e-14, atol=1e-15)
+    # faces: compare per (element, position)
+    for e in range(um.nelements):
+        for p in range(2 * dim):
+            fu, fc = um.faceinds[e, p] - 1, cm.faceinds[e, p] - 1
+            if um.facepos[e, p] == 1 and cm.facepos[e, p] == 1:
+                nfd = n ** (dim - 1)
+                assert np.allclose(du.frames[fu * nfd:(fu + 1) * nfd], dc.frames[fc * nfd:(fc + 1) * nfd], atol=1e-14)
+                assert np.allclose(du.faceJ[fu * nfd:(fu + 1) * nfd], dc.faceJ[fc * nfd:(fc + 1) * nfd], rtol=1e-14)
+
+
+def _match(coords_a, coords_b, npe):
+    """Index map b -> a of equal points within the same element (elements matched by centroid;
+    LGL nodes on element boundaries are shared by several elements)."""
+    ne = len(coords_a) // npe
+    ca = coords_a.reshape(ne, npe, 3)
+    cb = coords_b.reshape(ne, npe, 3)
+    ka = {tuple(np.round(c.mean(axis=0), 10)): e for e, c in enumerate(ca)}
+    out = np.zeros(len(coords_b), dtype=np.int64)
+    for eb in range(ne):
+        ea = ka[tuple(np.round(cb[eb].mean(axis=0), 10))]
+        kn = {tuple(np.round(c, 10)): i for i, c in enumerate(ca[ea])}
+        for i, c in enumerate(cb[eb]):
+            out[eb * npe + i] = ea * npe + kn[tuple(np.round(c, 10))]
+    return out
+
+
+@pytest.mark.parametrize("dim,op", [(2, "strong"), (2, "split"), (3, "strong"), (3, "split"), (3, "split_md")])
+def test_residual_is_invariant_under_element_rotations(dim, op):
+    """Rotating each element's local numbering permutes the nodes and re-orients the faces
+    (all orientation codes occur in 3D); the residual at each physical node must not change."""
+    ops = {"strong": lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+           "split": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(F.ChandrasekharAverage(), 1.0)),
+           "split_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0))}
+    n = 4
+    plain = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=5, rotate=False)
+    rot = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=5, rotate=True)
+    if dim == 3:
+        assert len(set(rot.orientation.tolist())) == 8
+    d0, d1 = _disc(plain, n, ops[op]()), _disc(rot, n, ops[op]())
+    Q0, Q1 = _state(d0, 3), _state(d1, 3)
+    R0 = oracle_for(d0).rhs(Q0)
+    R1 = oracle_for(d1).rhs(Q1)
+    perm = _match(d0.coords, d1.coords, n ** dim)
+    err = np.max(np.abs(R1 - R0[perm])) / np.max(np.abs(R0))
+    assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("dim,n", [(2, 3), (2, 5), (3, 3), (3, 4)])
+def test_freestream_on_perturbed_meshes(dim, n):
+    m = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.15, seed=7)
+    for op in (F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+               F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(F.ChandrasekharAverage(), 1.0))):
+        disc = _disc(m, n, op)
+        P = np.zeros((disc.ndofs, dim + 2))
+        P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.2, 0.3, 1.7
+        Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+        R = oracle_for(disc).rhs(Q)
+        assert np.max(np.abs(R)) < 1e-11, np.max(np.abs(R))
+
+
+def test_gmsh_round_trip(tmp_path):
+    m = F.perturbed_box(3, 2, (0.0,) * 3, (1.0,) * 3, amp=0.1, seed=3)
+    p = tmp_path / "box.msh"
+    F.write_gmsh22(str(p), m)
+    r = F.UnstructuredMesh.from_gmsh(str(p), 3)
+    assert np.array_equal(r.elements, m.elements) and np.allclose(r.nodes, m.nodes)
+    assert r.bdnames == m.bdnames
+    assert np.array_equal(r.faceinds, m.faceinds) and np.array_equal(r.orientation, m.orientation)
+
+
+def test_gmsh41_file():
+    """A two-quadrilateral mesh in format 4.1 (entities, node and element blocks, named groups)."""
+    m = F.UnstructuredMesh.from_gmsh(os.path.join(HERE, "golden", "two_quads_v41.msh"), 2)
+    assert m.nelements == 2 and m.nfaces == 7
+    assert sorted(m.bdnames) == ["outlet", "wall"]
+    assert len(m.bdfaces[m.boundary_index("wall") - 1]) == 5
+    assert len(m.bdfaces[m.boundary_index("outlet") - 1]) == 1
+    assert np.allclose(m.nodes[m.elements[1]], [[1, 0], [2, 0], [2, 1], [1, 1]])
