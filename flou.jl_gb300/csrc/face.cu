@@ -21,7 +21,25 @@ cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStre
     if (dim == 2) return launch_face_t<2, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
     return launch_face_t<3, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
 }
+// General geometry: the slave trace through master2slave, per-node frames and surface Jacobians.
+template <int DIM, int EQ>
+static cudaError_t launch_face_curv_t(const FaceParams& P, cudaStream_t s) {
+    int64_t nthreads = (int64_t)P.nfaces * P.nfd;
+    if (nthreads == 0) return cudaSuccess;
+    int grid = (int)((nthreads + 255) / 256);
+    face_kernel<DIM, EQ, true, true><<<grid, 256, 0, s>>>(P);
+    return cudaGetLastError();
+}
+cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t s) {
+    if (eq == FLOU_EQ_EULER) return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_EULER>(P, s)
+                                             : launch_face_curv_t<3, FLOU_EQ_EULER>(P, s);
+    if (eq == FLOU_EQ_LINEAR_ADVECTION)
+        return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_LINEAR_ADVECTION>(P, s)
+                        : launch_face_curv_t<3, FLOU_EQ_LINEAR_ADVECTION>(P, s);
+    return cudaErrorInvalidValue;
+}
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
+    if (L.curv) return L.dim == 2 ? launch_elem_curv2d(L, P, s) : launch_elem_curv3d(L, P, s);
     if (L.eq != FLOU_EQ_EULER) return launch_elem_scalar(L, P, s);
     if (L.dim == 1) return launch_elem_euler1d(L, P, s);
     if (L.dim == 2) return launch_elem_euler2d(L, P, s);

@@ -91,6 +91,9 @@ FaceParams face_params(const flou_ctx* c, const double* Q) {
     P.n = c->n;
     P.npe = c->npe;
     P.nfd = c->nfd;
+    P.frames = c->d_frames;
+    P.faceJn = c->d_faceJn;
+    P.orient = c->d_orient;
     P.numflux = c->cfg.numflux;
     P.lxf_avg = c->cfg.numflux_avg;
     P.intensity = c->cfg.numflux_intensity;
@@ -125,6 +128,9 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.gamma = c->cfg.gamma;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     P.status = c->d_status;
+    P.invJn = c->d_invJn;
+    P.Jan = c->d_Jan;
+    P.orient = c->d_orient;
     return P;
 }
 
@@ -137,6 +143,7 @@ ElemLaunch elem_launch(const flou_ctx* c) {
     L.tp = c->cfg.twopoint_flux;
     L.lgl = c->lgl;
     L.prepare = false;
+    L.curv = c->curv;
     return L;
 }
 
@@ -151,7 +158,8 @@ int stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double
         fp.Fn = Fn;
         ep.Fn = Fn;
     }
-    cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, s);
+    cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, fp, s)
+                            : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
     e = launch_elem(elem_launch(c), ep, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "element kernel launch");
@@ -256,10 +264,11 @@ int validate_pack_mesh(int dim, int32_t nelem, int32_t nfaces, const int32_t* fa
     ef.assign((size_t)nelem * nfpe, 0);
     fe.assign((size_t)nfaces * 2, -1);
     fb.assign(nfaces, -1);
+    const int maxo = dim == 1 ? 0 : (dim == 2 ? 1 : 7);   // master2slave: StdSegment / StdQuad
     for (int f = 0; f < nfaces; ++f) {
-        if (orientation[f] != 0)
-            return bad(FLOU_ERR_UNSUPPORTED, "face %d has orientation %d; only conforming Cartesian faces "
-                       "(orientation 0) are supported", f + 1, (int)orientation[f], 0, 0);
+        if (orientation[f] > maxo)
+            return bad(FLOU_ERR_ARG, "face %d has orientation %d; a %dD face takes 0..%d", f + 1,
+                       (int)orientation[f], dim, maxo);
         for (int s = 0; s < 2; ++s) {
             int e = eleminds[2 * f + s], p = elempos[2 * f + s];
             if (s == 1 && e == 0) continue;
@@ -291,13 +300,16 @@ int validate_pack_mesh(int dim, int32_t nelem, int32_t nfaces, const int32_t* fa
     return FLOU_OK;
 }
 
-// Validates Cartesian geometry (J and a diagonal metric constant per element, one frame and one
-// surface Jacobian per face, the frame being the Cartesian frame of the face's master side) and
-// compresses it: invJ[nelem], Jd[nelem*dim], fJ[nfaces], dx[nelem] (get_max_dt length scale).
+// Validates the geometry (J > 0 at every node, finite metric, unit face normals, positive
+// surface Jacobians) and computes dx[nelem], get_max_dt's length scale (Σ J ω / n^d)^(1/d)
+// (MultielementDiscontinuous.jl:169-171).  When the geometry is Cartesian (J and a diagonal
+// metric constant per element, one surface Jacobian per face, the Cartesian frame of the face's
+// master side) it is also compressed: invJ[nelem], Jd[nelem*dim], fJ[nfaces]; otherwise
+// *cartesian is false and the kernels read the per-node arrays.
 int validate_pack_geometry(int dim, int n, int32_t nelem, int32_t nfaces, const double* omega,
                            const std::vector<int32_t>& fe, const double* J, const double* Ja, const double* frames,
                            const double* face_J, std::vector<double>& invJ, std::vector<double>& Jd,
-                           std::vector<double>& fJ, std::vector<double>& dx, std::string& msg) {
+                           std::vector<double>& fJ, std::vector<double>& dx, bool* cartesian, std::string& msg) {
     char buf[256];
     auto bad = [&](int code, const char* fmt, int a) {
         snprintf(buf, sizeof(buf), fmt, a);
@@ -306,6 +318,7 @@ int validate_pack_geometry(int dim, int n, int32_t nelem, int32_t nfaces, const 
     };
     if (!J || !Ja || !frames || !face_J || !omega) return bad(FLOU_ERR_ARG, "null geometry pointer%.0d", 0);
     int npe = ipow(n, dim), nfd = ipow(n, dim - 1);
+    bool cart = true;
     invJ.assign(nelem, 0.0);
     Jd.assign((size_t)nelem * dim, 0.0);
     fJ.assign(nfaces, 0.0);
@@ -314,21 +327,17 @@ int validate_pack_geometry(int dim, int n, int32_t nelem, int32_t nfaces, const 
         const double* Je = J + (size_t)e * npe;
         const double* Me = Ja + (size_t)e * npe * dim * dim;
         for (int i = 0; i < npe; ++i) {
-            if (Je[i] != Je[0])
-                return bad(FLOU_ERR_UNSUPPORTED, "element %d: the Jacobian varies within the element "
-                           "(curvilinear geometry is not supported)", e + 1);
+            if (!(Je[i] > 0.0) || !std::isfinite(Je[i])) return bad(FLOU_ERR_ARG, "element %d: J <= 0", e + 1);
+            if (Je[i] != Je[0]) cart = false;
             for (int q = 0; q < dim * dim; ++q) {
                 double v = Me[(size_t)i * dim * dim + q];
+                if (!std::isfinite(v)) return bad(FLOU_ERR_ARG, "element %d: non-finite metric", e + 1);
                 bool diag = (q % (dim + 1)) == 0;
-                if ((!diag && v != 0.0) || v != Me[q])
-                    return bad(FLOU_ERR_UNSUPPORTED, "element %d: the metric is not diagonal and constant "
-                               "(curvilinear geometry is not supported)", e + 1);
+                if ((!diag && v != 0.0) || v != Me[q]) cart = false;
             }
         }
-        if (!(Je[0] > 0.0) || !std::isfinite(Je[0])) return bad(FLOU_ERR_ARG, "element %d: J <= 0", e + 1);
         invJ[e] = 1.0 / Je[0];
         for (int d = 0; d < dim; ++d) Jd[(size_t)e * dim + d] = Me[d * (dim + 1)];
-        // get_max_dt length scale: (Σ J ω / n^d)^(1/d), MultielementDiscontinuous.jl:169-171
         double vol = 0.0;
         for (int i = 0; i < npe; ++i) {
             double w = 1.0;
@@ -343,18 +352,23 @@ int validate_pack_geometry(int dim, int n, int32_t nelem, int32_t nfaces, const 
         FrameTab T = frame_of(dim, fe[2 * f] & 7);
         for (int m = 0; m < nfd; ++m) {
             size_t idx = (size_t)f * nfd + m;
-            if (face_J[idx] != face_J[(size_t)f * nfd])
-                return bad(FLOU_ERR_UNSUPPORTED, "face %d: the surface Jacobian varies along the face", f + 1);
+            if (!(face_J[idx] > 0.0) || !std::isfinite(face_J[idx]))
+                return bad(FLOU_ERR_ARG, "face %d: surface Jacobian <= 0", f + 1);
+            if (face_J[idx] != face_J[(size_t)f * nfd]) cart = false;
             const double* fr = frames + idx * 9;
+            double nn = 0.0;
+            for (int q = 0; q < 9; ++q)
+                if (!std::isfinite(fr[q])) return bad(FLOU_ERR_ARG, "face %d: non-finite frame", f + 1);
+            for (int q = 0; q < dim; ++q) nn += fr[q] * fr[q];
+            if (std::fabs(nn - 1.0) > 1e-10) return bad(FLOU_ERR_ARG, "face %d: the normal is not a unit vector", f + 1);
             for (int q = 0; q < 3; ++q) {
                 bool ok = (q >= dim || (fr[q] == T.n[q] && fr[3 + q] == T.t[q] && (dim < 3 || fr[6 + q] == T.b[q])));
-                if (!ok)
-                    return bad(FLOU_ERR_UNSUPPORTED, "face %d: the frame is not the Cartesian frame of its master "
-                               "side (curvilinear geometry is not supported)", f + 1);
+                if (!ok) cart = false;
             }
         }
         fJ[f] = face_J[(size_t)f * nfd];
     }
+    *cartesian = cart;
     return FLOU_OK;
 }
 
@@ -427,7 +441,8 @@ int32_t flou_destroy(flou_ctx* c) {
     if (!c) return FLOU_ERR_ARG;
     drop_graph(c);
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
-                    c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c};
+                    c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c, c->d_invJn, c->d_Jan,
+                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn};
     for (void* b : bufs)
         if (b) cudaFree(b);
     ctx_free_limiter(c);
@@ -491,6 +506,10 @@ int32_t flou_set_mesh(flou_ctx* c, int32_t nelem, int32_t nfaces, const int32_t*
     if ((r = upload(c, &c->d_elem_face, ef.data(), ef.size(), "mesh upload"))) return r;
     if ((r = upload(c, &c->d_face_elem, fe.data(), fe.size(), "mesh upload"))) return r;
     if ((r = upload(c, &c->d_face_bc, fb.data(), fb.size(), "mesh upload"))) return r;
+    if ((r = upload(c, &c->d_orient, orientation, (size_t)nfaces, "mesh upload"))) return r;
+    c->any_orient = false;
+    for (int f = 0; f < nfaces; ++f) c->any_orient |= orientation[f] != 0;
+    c->curv = false;
     // sizes changed: drop size-dependent buffers
     double** sized[] = {&c->d_Fn, &c->d_U, &c->d_Qh, &c->d_dQh, &c->d_c};
     for (double** b : sized)
@@ -534,12 +553,38 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators must come before flou_set_geometry");
     std::vector<double> invJ, Jd, fJ, dx;
     std::string msg;
+    bool cart = true;
     int r = validate_pack_geometry(c->cfg.dim, c->n, c->nelem, c->nfaces, c->omega.data(), c->h_face_elem, J, Ja,
-                                   frames, face_J, invJ, Jd, fJ, dx, msg);
+                                   frames, face_J, invJ, Jd, fJ, dx, &cart, msg);
     if (r) return fail(c, r, "%s", msg.c_str());
+    bool curv = !cart || c->any_orient;
+    if (curv && c->cfg.dim == 1)
+        return fail(c, FLOU_ERR_UNSUPPORTED, "1D geometry must have J constant per element and the Cartesian frames");
+    if (curv && !c->lgl)
+        return fail(c, FLOU_ERR_UNSUPPORTED, "general (curvilinear / unstructured) geometry needs a basis with "
+                                             "boundary nodes (LGL)");
+    if (curv && c->cfg.equation == FLOU_EQ_BURGERS)
+        return fail(c, FLOU_ERR_UNSUPPORTED, "Burgers' equation is 1D");
     std::vector<double> Jel(c->nelem);
     for (int e = 0; e < c->nelem; ++e) Jel[e] = J[(size_t)e * c->npe];
     if ((r = upload(c, &c->d_Jel, Jel.data(), Jel.size(), "geometry upload"))) return r;
+    if (curv) {   // per-node arrays, struct-of-arrays for coalesced reads
+        int d = c->cfg.dim;
+        size_t nd = (size_t)c->ndofs, nf = (size_t)c->nfdofs;
+        std::vector<double> invJn(nd), Jan(nd * d * d), fr(nf * 9);
+        for (size_t g = 0; g < nd; ++g) {
+            invJn[g] = 1.0 / J[g];
+            for (int q = 0; q < d * d; ++q) Jan[q * nd + g] = Ja[g * d * d + q];
+        }
+        for (size_t g = 0; g < nf; ++g)
+            for (int q = 0; q < 9; ++q) fr[q * nf + g] = frames[g * 9 + q];
+        if ((r = upload(c, &c->d_invJn, invJn.data(), nd, "geometry upload"))) return r;
+        if ((r = upload(c, &c->d_Jan, Jan.data(), Jan.size(), "geometry upload"))) return r;
+        if ((r = upload(c, &c->d_frames, fr.data(), fr.size(), "geometry upload"))) return r;
+        if ((r = upload(c, &c->d_faceJn, face_J, nf, "geometry upload"))) return r;
+        if ((r = upload(c, &c->d_Jn, J, nd, "geometry upload"))) return r;
+    }
+    c->curv = curv;
     if ((r = upload(c, &c->d_invJ, invJ.data(), invJ.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_Ja, Jd.data(), Jd.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;
@@ -701,7 +746,8 @@ int32_t flou_time_kernels(flou_ctx* c, const double* Q, int32_t nrep, double* fa
     for (int it = 0; it < nrep; ++it) {
         for (int mode = 1; mode <= 3; ++mode) {
             CK(cudaEventRecord(ev[0], c->stream), "event record");
-            cudaError_t e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), c->stream);
+            cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, face_params(c, Q), c->stream)
+                                    : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
             CK(cudaEventRecord(ev[1], c->stream), "event record");
             // stage 1: U = Q + dt L; stages 2, 3: out = a0 Q0 + a1 (U + dt L) (written to scratch)
@@ -758,7 +804,9 @@ int32_t flou_check_geometry(int32_t dim, int32_t nnodes, int32_t nelem, int32_t 
     for (int f = 0; f < nfaces; ++f) fe[2 * f] = elempos[2 * f] - 1;   // only the master position is used
     std::vector<double> invJ, Jd, fJ, dx;
     std::string m;
-    int r = validate_pack_geometry(dim, nnodes, nelem, nfaces, omega, fe, J, Ja, frames, face_J, invJ, Jd, fJ, dx, m);
+    bool cart = true;
+    int r = validate_pack_geometry(dim, nnodes, nelem, nfaces, omega, fe, J, Ja, frames, face_J, invJ, Jd, fJ, dx,
+                                   &cart, m);
     copy_msg(m, msg, msglen);
     return r;
 }
@@ -862,7 +910,8 @@ extern "C" int32_t flou_rhs_noalloc(flou_ctx* c, double* dQ, const double* Q, do
     if (!scratch) return cuda_fail(c, e, "flou_rhs_noalloc scratch address");
     FaceParams fp = face_params(c, Q);
     fp.Fn = scratch;
-    e = launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, c->stream);
+    e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, fp, c->stream)
+                : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
     ElemParams ep = elem_params(c, Q, Q, dQ, 0, 0.0, 0.0, 0.0);
     ep.Fn = scratch;

@@ -41,6 +41,15 @@ struct flou_ctx {
     double* d_Qh = nullptr;         // staging for host-pointer calls
     double* d_dQh = nullptr;
     double* d_c = nullptr;          // optional per-element LxF dissipation scale
+    // general (curvilinear / unstructured) geometry: the CURV kernels
+    bool curv = false;
+    bool any_orient = false;        // some face has a non-zero master2slave orientation
+    double* d_invJn = nullptr;      // [ndofs]
+    double* d_Jan = nullptr;        // [dim*dim][ndofs]
+    double* d_frames = nullptr;     // [9][nfdofs]
+    double* d_faceJn = nullptr;     // [nfdofs]
+    uint8_t* d_orient = nullptr;    // [nfaces]
+    double* d_Jn = nullptr;         // [ndofs] J (limiter, monitors)
     int32_t* d_status = nullptr;    // [flags, lowest element]
     unsigned long long* d_dtmin = nullptr;
     // Zhang-Shu limiter and integral monitors (limiter.cu)

@@ -41,6 +41,10 @@ struct FaceParams {
     double adv[3];
     int32_t bc_kind[MAXBC];
     double bc_state[MAXBC][5];
+    // general (curvilinear / unstructured) geometry, read by the CURV kernels only
+    const double* frames;        // [9][nfdofs]: n, t, b of every face node (master ordering)
+    const double* faceJn;        // [nfdofs] surface Jacobian of every face node
+    const uint8_t* orient;       // [nfaces] master2slave orientation
 };
 
 struct ElemParams {
@@ -59,7 +63,36 @@ struct ElemParams {
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
+    // general geometry (CURV kernels)
+    const double* invJn;         // [ndofs] 1/J of every node
+    const double* Jan;           // [DIM*DIM][ndofs]: metric Ja[k, d] at q = k + d*DIM (columns: dual basis)
+    const uint8_t* orient;       // [nfaces] master2slave orientation
 };
+
+// master2slave of a face dof (StdSegment.jl:161-167, StdQuad.jl:161-181), 0-based, x fastest:
+// the slave's face dof that holds the master's face dof m.
+template <int DIM>
+__host__ __device__ __forceinline__ int master2slave(int m, int o, int n) {
+    if (DIM <= 1 || o == 0) return m;
+    if (DIM == 2) return n - 1 - m;
+    int m1 = m % n, m2 = m / n;
+    switch (o) {
+        case 1: return m2 + n * (n - 1 - m1);
+        case 2: return (n - 1 - m1) + n * (n - 1 - m2);
+        case 3: return (n - 1 - m2) + n * m1;
+        case 4: return m2 + n * m1;
+        case 5: return (n - 1 - m1) + n * m2;
+        case 6: return (n - 1 - m2) + n * (n - 1 - m1);
+        default: return m1 + n * (n - 1 - m2);
+    }
+}
+
+// The orientation whose master2slave inverts o's (the two quarter turns of a quadrilateral
+// face are each other's inverse; every other map is an involution).
+template <int DIM>
+__host__ __device__ __forceinline__ int inverse_orientation(int o) {
+    return (DIM == 3 && (o == 1 || o == 3)) ? 4 - o : o;
+}
 
 // Local face positions follow the reference's face order: 2*dir (left) and 2*dir+1
 // (right); frames of a face are those of its master position (PhysicalRegions.jl:541-696).
@@ -402,33 +435,77 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
 // (applyBCs!, :25-49) and numerical fluxes times the surface Jacobian
 // (interface_fluxes!, :111-136).  One thread per face node.
 // ---------------------------------------------------------------------------------------
-template <int DIM, int EQ, bool LGL>
+// rotate2face / rotate2phys (Euler.jl:16-64) with a general frame (n, t, b): the momentum's
+// components along n, t, b, and back.
+template <int DIM>
+__device__ __forceinline__ void rotate_to_face(const double* q, const FrameTab& fr, double* a) {
+    a[0] = q[0];
+    a[DIM + 1] = q[DIM + 1];
+    if (DIM == 1) { a[1] = q[1] * fr.n[0]; return; }
+    if (DIM == 2) {
+        a[1] = q[1] * fr.n[0] + q[2] * fr.n[1];
+        a[2] = q[1] * fr.t[0] + q[2] * fr.t[1];
+        return;
+    }
+    a[1] = q[1] * fr.n[0] + q[2] * fr.n[1] + q[3] * fr.n[2];
+    a[2] = q[1] * fr.t[0] + q[2] * fr.t[1] + q[3] * fr.t[2];
+    a[3] = q[1] * fr.b[0] + q[2] * fr.b[1] + q[3] * fr.b[2];
+}
+
+template <int DIM>
+__device__ __forceinline__ void rotate_to_phys(const double* a, const FrameTab& fr, double* q) {
+    q[0] = a[0];
+    q[DIM + 1] = a[DIM + 1];
+    if (DIM == 1) { q[1] = a[1] * fr.n[0]; return; }
+    if (DIM == 2) {
+        q[1] = a[1] * fr.n[0] + a[2] * fr.t[0];
+        q[2] = a[1] * fr.n[1] + a[2] * fr.t[1];
+        return;
+    }
+    q[1] = a[1] * fr.n[0] + a[2] * fr.t[0] + a[3] * fr.b[0];
+    q[2] = a[1] * fr.n[1] + a[2] * fr.t[1] + a[3] * fr.b[1];
+    q[3] = a[1] * fr.n[2] + a[2] * fr.t[2] + a[3] * fr.b[2];
+}
+
+// CURV: general geometry -- the slave trace at master2slave(m), the frame and surface Jacobian
+// of this face node (Interfaces.jl:111-136 with PhysicalRegions.jl:797-971).
+template <int DIM, int EQ, bool LGL, bool CURV = false>
 __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
     int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
     int n = P.n;
     int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
-    auto trace = [&](int32_t s, double* q) {
+    auto trace = [&](int32_t s, int mm, double* q) {
         int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
         const double* Qe = P.Q + (int64_t)e * P.npe;
         if (LGL) {
-            int node = tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+            int node = tp_node<DIM>(n, dir, mm, right ? n - 1 : 0);
             for (int k = 0; k < NV; ++k) q[k] = Qe[k * P.ndofs + node];
         } else {
             const double* lv = P.l + (right ? n : 0);
             for (int k = 0; k < NV; ++k) {
                 double acc = 0.0;
-                for (int p = 0; p < n; ++p) acc = acc + lv[p] * Qe[k * P.ndofs + tp_node<DIM>(n, dir, m, p)];
+                for (int p = 0; p < n; ++p) acc = acc + lv[p] * Qe[k * P.ndofs + tp_node<DIM>(n, dir, mm, p)];
                 q[k] = acc;
             }
         }
     };
     double ql[NV], qr[NV];
-    trace(s0, ql);
-    FrameTab fr = frame_of(DIM, s0 & 7);
+    trace(s0, m, ql);
+    FrameTab fr;
+    if (CURV) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            fr.n[c] = P.frames[c * P.nfdofs + gid];
+            fr.t[c] = P.frames[(3 + c) * P.nfdofs + gid];
+            fr.b[c] = P.frames[(6 + c) * P.nfdofs + gid];
+        }
+    } else {
+        fr = frame_of(DIM, s0 & 7);
+    }
     if (s1 >= 0) {
-        trace(s1, qr);
+        trace(s1, CURV ? master2slave<DIM>(m, P.orient[f], n) : m, qr);
     } else {
         int b = P.face_bc[f];
         int kind = P.bc_kind[b];
@@ -437,29 +514,41 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         } else if (kind == FLOU_BC_SLIP && EQ == FLOU_EQ_EULER) {
             // EulerSlipBC (Euler.jl:88-94): rotate to the face frame, flip the normal momentum,
             // rotate back -- for a Cartesian frame, the momentum along the normal axis changes sign.
-            for (int k = 0; k < NV; ++k) qr[k] = ql[k];
-            int an = frame_axes<DIM>(s0 & 7).ax[0];
-            qr[1 + an] = -ql[1 + an];
+            if (CURV) {
+                double a[NV];
+                rotate_to_face<DIM>(ql, fr, a);
+                a[1] = -a[1];
+                rotate_to_phys<DIM>(a, fr, qr);
+            } else {
+                for (int k = 0; k < NV; ++k) qr[k] = ql[k];
+                int an = frame_axes<DIM>(s0 & 7).ax[0];
+                qr[1 + an] = -ql[1 + an];
+            }
         } else {
             for (int k = 0; k < NV; ++k) qr[k] = ql[k];   // outflow
         }
     }
     double F[NV];
-    double J = P.faceJ[f];
+    double J = CURV ? P.faceJn[gid] : P.faceJ[f];
     double inten = P.intensity;
     if (P.elem_c) {
         int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
         inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
     }
     if (EQ == FLOU_EQ_EULER) {
-        // rotate2face / rotate2phys (Euler.jl:16-64) as signed permutations
+        // rotate2face / rotate2phys (Euler.jl:16-64): signed permutations for a Cartesian frame
         FrameAxes A = frame_axes<DIM>(s0 & 7);
         double a[NV], b[NV];
-        a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+        if (CURV) {
+            rotate_to_face<DIM>(ql, fr, a);
+            rotate_to_face<DIM>(qr, fr, b);
+        } else {
+            a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
 #pragma unroll
-        for (int r = 0; r < DIM; ++r) {
-            a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
-            b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
+            for (int r = 0; r < DIM; ++r) {
+                a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
+                b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
+            }
         }
         double Fr[NV];
         if (P.numflux == FLOU_NF_CHANDRASHEKAR || P.numflux >= FLOU_NF_SCALAR_DISSIPATION ||
@@ -467,10 +556,14 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
             euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
         else
             euler_face_flux_fast<DIM>(a, b, P.numflux, inten, P.gamma, Fr);
-        F[0] = Fr[0];
-        F[DIM + 1] = Fr[DIM + 1];
+        if (CURV) {
+            rotate_to_phys<DIM>(Fr, fr, F);
+        } else {
+            F[0] = Fr[0];
+            F[DIM + 1] = Fr[DIM + 1];
 #pragma unroll
-        for (int r = 0; r < DIM; ++r) F[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]);
+            for (int r = 0; r < DIM; ++r) F[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]);
+        }
     } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
         // LinearAdvection.jl:27-39
         double an = P.adv[0] * fr.n[0];
@@ -490,9 +583,9 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
     for (int k = 0; k < NV; ++k) P.Fn[k * P.nfdofs + o] = F[k] * J;
 }
 
-template <int DIM, int EQ, bool LGL>
+template <int DIM, int EQ, bool LGL, bool CURV = false>
 __global__ void __launch_bounds__(256) face_kernel(FaceParams P) {
-    face_node<DIM, EQ, LGL>(P, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    face_node<DIM, EQ, LGL, CURV>(P, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -517,7 +610,9 @@ __device__ __forceinline__ void raise_nonphysical(int32_t* status, int elem) {
 
 // Surface lift (OpDivergence.jl:42-100) for node (pos along dir, line), then 1/J and the
 // stage update.  Shared by both volume operators.
-template <int DIM, int N, int NV, bool LGL>
+// CURV: a slave side reads the master's face dof that master2slave sends onto its own line
+// index (the inverse orientation), and 1/J is taken per node.
+template <int DIM, int N, int NV, bool LGL, bool CURV = false>
 __device__ __forceinline__ void surface_and_update(const ElemParams& P, const double* sops, int e, int i,
                                                    const double* q, double* dq) {
     const double* dgl = sops + 2 * N * N + 2 * N;
@@ -527,8 +622,13 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         int pos, line;
         tp_coords<DIM>(N, i, dir, pos, line);
         int32_t pl = P.elem_face[e * 2 * DIM + 2 * dir], pr = P.elem_face[e * 2 * DIM + 2 * dir + 1];
-        int64_t ol = (int64_t)(pl >> 1) * ipow(N, DIM - 1) + line;
-        int64_t orr = (int64_t)(pr >> 1) * ipow(N, DIM - 1) + line;
+        int linel = line, liner = line;
+        if (CURV) {
+            if (pl & 1) linel = master2slave<DIM>(line, inverse_orientation<DIM>(P.orient[pl >> 1]), N);
+            if (pr & 1) liner = master2slave<DIM>(line, inverse_orientation<DIM>(P.orient[pr >> 1]), N);
+        }
+        int64_t ol = (int64_t)(pl >> 1) * ipow(N, DIM - 1) + linel;
+        int64_t orr = (int64_t)(pr >> 1) * ipow(N, DIM - 1) + liner;
         double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
         if (LGL) {
             if (pos == 0) {
@@ -548,8 +648,8 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
                 dq[k] = dq[k] - (cl * __ldcg(P.Fn + k * P.nfdofs + ol) + cr * __ldcg(P.Fn + k * P.nfdofs + orr));
         }
     }
-    double invJ = P.elem_invJ[e];
     int64_t g = (int64_t)e * ipow(N, DIM) + i;
+    double invJ = CURV ? P.invJn[g] : P.elem_invJ[e];
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -566,7 +666,7 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
 
 // Strong (== weak on LGL) divergence: dQ_line -= Ds * F̃_line per direction
 // (OpDivergence.jl:109-160), F̃ = Ja_dd F_d (contravariant with a diagonal metric).
-template <int DIM, int N, int EQ, bool LGL, int TB = 256>
+template <int DIM, int N, int EQ, bool LGL, int TB = 256, bool CURV = false>
 __device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double* smem) {
     using S = Shape<DIM, N, TB>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
@@ -597,6 +697,31 @@ __device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double*
         }
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
+            if constexpr (CURV) {   // contravariant flux Σ_k F_k Ja[k, d] (PhysicalRegions.jl:1006-1033)
+                double a[DIM];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) a[k] = P.Jan[(k + d * DIM) * P.ndofs + g];
+                if constexpr (EQ == FLOU_EQ_EULER) {
+                    double mn = 0.0, vn = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) {
+                        mn = fma(q[1 + k], a[k], mn);
+                        vn = fma(v[k], a[k], vn);
+                    }
+                    F[0] = mn;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) F[1 + k] = fma(q[1 + k], vn, p * a[k]);
+                    F[DIM + 1] = (q[DIM + 1] + p) * vn;
+                } else {
+                    double an = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) an = fma(P.adv[k], a[k], an);
+                    F[0] = an * q[0];
+                }
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sF[(d * NV + k) * NN + tid] = F[k];
+                continue;
+            }
             double Ja = P.elem_Ja[e * DIM + d];
             if (EQ == FLOU_EQ_EULER) {
                 F[0] = q[1 + d];
@@ -632,14 +757,14 @@ __device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double*
                 for (int k = 0; k < NV; ++k) dq[k] = dq[k] - a * Fd[k * NN + j];
             }
         }
-        surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
+        surface_and_update<DIM, N, NV, LGL, CURV>(P, sops, e, i, q, dq);
     }
 }
 
-template <int DIM, int N, int EQ, bool LGL>
+template <int DIM, int N, int EQ, bool LGL, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemParams P) {
     extern __shared__ double smem[];
-    strong_tile<DIM, N, EQ, LGL>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
+    strong_tile<DIM, N, EQ, LGL, 256, CURV>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -668,9 +793,11 @@ struct SplitLayout {
 //   log branch: mean = (a-b)/ln(a/b).
 // One reciprocal 1/(hs_ρ·hs_β) serves both means and the pressure average; 1/F comes from
 // two Newton steps started at 1 - u/3 (relative error (4u²/45)^4 < 1e-20 for u < 0.01).
-template <int DIM>
+// GEN: the flux along a general vector nv (the averaged metric column of a curvilinear element,
+// Euler.jl:474-536 with n = (Ja1 + Ja2)/2) instead of the axis d.
+template <int DIM, bool GEN = false>
 __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S, int NN, int i, int l, int d,
-                                                   double c_beta, double* F) {
+                                                   double c_beta, double* F, const double* nv = nullptr) {
     const double* rh = S;
     const double* vh = S + NN;
     const double* bh = S + (1 + DIM) * NN;
@@ -711,6 +838,17 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     }
     // h = 1/(2β(γ-1)) - (|v1|²+|v2|²)/4 + p/ρ + |v̄|²
     double h = fma(inv_beta_ln, c_beta, -(vq[i] + vq[l])) + fma(p, inv_rho_ln, vv);
+    if (GEN) {
+        double vn = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) vn = fma(va[k], nv[k], vn);
+        double m = rho_ln * vn;
+        F[0] = m;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], p * nv[k]);
+        F[DIM + 1] = m * h;
+        return;
+    }
     double m = rho_ln * va[d];
     F[0] = m;
 #pragma unroll
@@ -719,7 +857,7 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     F[DIM + 1] = m * h;
 }
 
-template <int DIM, int N, int EQ, int TP, bool LGL, int TB = 256>
+template <int DIM, int N, int EQ, int TP, bool LGL, int TB = 256, bool CURV = false>
 __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* smem) {
     using S = Shape<DIM, N, TB>;
     using Lay = SplitLayout<DIM, EQ, TP>;
@@ -730,7 +868,8 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     double* sops = smem;
     double* sprim = sops + S::NOPS;                 // [Lay::NARR][NN]
     double* spair = sprim + Lay::NARR * NN;         // [NV][NPT]
-    uint8_t* stab = (uint8_t*)(spair + NV * NPT);   // pair table: a, b
+    double* sJa = spair + NV * NPT;                 // CURV: [DIM][NN] metric column of the direction
+    uint8_t* stab = (uint8_t*)(sJa + (CURV ? DIM * NN : 0));   // pair table: a, b
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
     if (tid == 0) {
@@ -791,6 +930,14 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     const double c_beta = 0.5 / (g - 1.0);
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
+        if (CURV) {   // this direction's metric column Ja[:, dir] of every node of the block
+            if (active) {
+                int64_t g = (int64_t)e * NPE + i;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) sJa[k * NN + tid] = P.Jan[(k + dir * DIM) * P.ndofs + g];
+            }
+            __syncthreads();
+        }
         // ---- pair phase: every symmetric two-point flux of the block, once ----
         for (int kp = tid; kp < NPT; kp += blockDim.x) {
             int elp = kp / (NFD * NPAIR);
@@ -801,7 +948,53 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             int ia = elp * NPE + tp_node<DIM>(N, dir, line, a);
             int ib = elp * NPE + tp_node<DIM>(N, dir, line, b);
             double F[NV];
-            if (EULER) {
+            double nv[DIM];   // CURV: the averaged metric column (Ja_a + Ja_b)/2
+            if (CURV) {
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) nv[k] = (sJa[k * NN + ia] + sJa[k * NN + ib]) / 2.0;
+            }
+            if constexpr (CURV && EULER) {
+                if (TP == FLOU_TP_CHANDRASHEKAR) {
+                    chandrashekar_pair<DIM, true>(sprim, NN, ia, ib, dir, c_beta, F, nv);
+                } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
+                    const double* vh = sprim + NN;
+                    double rho = sprim[ia] + sprim[ib];
+                    double pm = sprim[(1 + DIM) * NN + ia] + sprim[(1 + DIM) * NN + ib];
+                    double en = sprim[(2 + DIM) * NN + ia] + sprim[(2 + DIM) * NN + ib];
+                    double vm[DIM], vn = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) {
+                        vm[k] = vh[k * NN + ia] + vh[k * NN + ib];
+                        vn = fma(vm[k], nv[k], vn);
+                    }
+                    double m = rho * vn;
+                    F[0] = m;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, vm[k], pm * nv[k]);
+                    F[DIM + 1] = fma(m, en, pm * vn);
+                } else {   // StdAverage: the mean of the two contravariant fluxes
+                    const double* sq = sprim + (DIM + 1) * NN;
+                    double v1 = 0.0, v2 = 0.0, m1 = 0.0, m2 = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) {
+                        v1 = fma(sprim[k * NN + ia], nv[k], v1);
+                        v2 = fma(sprim[k * NN + ib], nv[k], v2);
+                        m1 = fma(sq[(1 + k) * NN + ia], nv[k], m1);
+                        m2 = fma(sq[(1 + k) * NN + ib], nv[k], m2);
+                    }
+                    double p1 = sprim[DIM * NN + ia], p2 = sprim[DIM * NN + ib];
+                    F[0] = (m1 + m2) * 0.5;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+                        F[1 + k] = (fma(sq[(1 + k) * NN + ia], v1, p1 * nv[k]) + fma(sq[(1 + k) * NN + ib], v2, p2 * nv[k])) * 0.5;
+                    F[DIM + 1] = ((sq[(DIM + 1) * NN + ia] + p1) * v1 + (sq[(DIM + 1) * NN + ib] + p2) * v2) * 0.5;
+                }
+            } else if constexpr (CURV) {   // linear advection (LinearAdvection.jl:44-47)
+                double an = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) an = fma(P.adv[k], nv[k], an);
+                F[0] = an * (sprim[ia] + sprim[ib]) * 0.5;
+            } else if (EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
                     chandrashekar_pair<DIM>(sprim, NN, ia, ib, dir, c_beta, F);
                 } else if (TP == FLOU_TP_KENNEDY_GRUBER) {   // Kennedy & Gruber (2008)
@@ -841,8 +1034,28 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
         if (active) {
             int pos, line;
             tp_coords<DIM>(N, i, dir, pos, line);
-            double Fd[NV];   // F♯(i, i): the physical flux along dir
-            if (EULER) {
+            double Fd[NV];   // F♯(i, i): the physical flux along dir (CURV: the contravariant flux)
+            if (CURV) {
+                double an = 0.0, mn = 0.0, vn = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) {
+                    double a = sJa[k * NN + tid];
+                    if constexpr (EULER) {
+                        mn = fma(q[1 + k], a, mn);
+                        vn = fma(v[k], a, vn);
+                    } else {
+                        an = fma(P.adv[k], a, an);
+                    }
+                }
+                if constexpr (EULER) {
+                    Fd[0] = mn;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) Fd[1 + k] = fma(q[1 + k], vn, p * sJa[k * NN + tid]);
+                    Fd[DIM + 1] = (q[DIM + 1] + p) * vn;
+                } else {
+                    Fd[0] = an * q[0];
+                }
+            } else if (EULER) {
                 Fd[0] = q[1 + dir];
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) Fd[1 + k] = q[1 + dir] * v[k];
@@ -870,41 +1083,41 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPT + pidx], acc[k]);
                 }
             }
-            double Ja = P.elem_Ja[e * DIM + dir];
+            double Ja = CURV ? 1.0 : P.elem_Ja[e * DIM + dir];   // CURV: the metric is in the fluxes
 #pragma unroll
             for (int k = 0; k < NV; ++k) dq[k] = fma(-Ja, acc[k], dq[k]);
         }
         __syncthreads();
     }
-    if (active) surface_and_update<DIM, N, NV, LGL>(P, sops, e, i, q, dq);
+    if (active) surface_and_update<DIM, N, NV, LGL, CURV>(P, sops, e, i, q, dq);
 }
 
-template <int DIM, int N, int EQ, int TP, bool LGL>
+template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
     extern __shared__ double smem[];
-    split_tile<DIM, N, EQ, TP, LGL>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
+    split_tile<DIM, N, EQ, TP, LGL, 256, CURV>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
-template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256>
+template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256, bool CURV = false>
 constexpr size_t elem_smem_bytes() {
     using S = Shape<DIM, N, TB>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
     constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;
     constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
-    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT) + 2 * (S::NPAIR + 1);
+    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT + (CURV ? DIM * S::NN : 0)) + 2 * (S::NPAIR + 1);
 }
 
 // Launch one instantiation; the dynamic shared-memory opt-in is set once per kernel.
 // With `prepare` set only the opt-in is made (it must precede stream capture).
-template <int DIM, int N, int EQ, int VOL, int TP, bool LGL>
+template <int DIM, int N, int EQ, int VOL, int TP, bool LGL, bool CURV = false>
 cudaError_t launch_elem_one(const ElemParams& P, cudaStream_t s, bool prepare) {
     using S = Shape<DIM, N>;
-    constexpr size_t smem = elem_smem_bytes<DIM, N, EQ, VOL, TP>();
+    constexpr size_t smem = elem_smem_bytes<DIM, N, EQ, VOL, TP, 256, CURV>();
     static bool attr_set = false;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    auto k = (VOL == FLOU_OP_STRONG) ? (void (*)(ElemParams))elem_strong_kernel<DIM, N, EQ, LGL>
-                                     : (void (*)(ElemParams))elem_split_kernel<DIM, N, EQ, TP, LGL>;
+    auto k = (VOL == FLOU_OP_STRONG) ? (void (*)(ElemParams))elem_strong_kernel<DIM, N, EQ, LGL, CURV>
+                                     : (void (*)(ElemParams))elem_split_kernel<DIM, N, EQ, TP, LGL, CURV>;
     if (!attr_set) {
         cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;
@@ -950,12 +1163,47 @@ cudaError_t launch_elem_dim(int n, int vol, int tp, bool lgl, const ElemParams& 
     }
 }
 
+// Curvilinear variants (LGL only): strong form and split form per two-point flux.
+template <int DIM, int N, int EQ>
+cudaError_t launch_elem_n_curv(int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    if (vol == FLOU_OP_STRONG) return launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, true, true>(P, s, prep);
+    if (EQ != FLOU_EQ_EULER)
+        return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true, true>(P, s, prep);
+    switch (tp) {
+        case FLOU_TP_STD_AVERAGE:
+            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true, true>(P, s, prep);
+        case FLOU_TP_CHANDRASHEKAR:
+            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, true, true>(P, s, prep);
+        case FLOU_TP_KENNEDY_GRUBER:
+            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_KENNEDY_GRUBER, true, true>(P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int DIM, int EQ>
+cudaError_t launch_elem_dim_curv(int n, int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (n) {
+        case 2: return launch_elem_n_curv<DIM, 2, EQ>(vol, tp, P, s, prep);
+        case 3: return launch_elem_n_curv<DIM, 3, EQ>(vol, tp, P, s, prep);
+        case 4: return launch_elem_n_curv<DIM, 4, EQ>(vol, tp, P, s, prep);
+        case 5: return launch_elem_n_curv<DIM, 5, EQ>(vol, tp, P, s, prep);
+        case 6: return launch_elem_n_curv<DIM, 6, EQ>(vol, tp, P, s, prep);
+        case 7: return launch_elem_n_curv<DIM, 7, EQ>(vol, tp, P, s, prep);
+        case 8: return launch_elem_n_curv<DIM, 8, EQ>(vol, tp, P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 // Host-side dispatch: one function per translation unit.
 struct ElemLaunch {
     int dim, eq, n, vol, tp;
     bool lgl;
     bool prepare;   // only set the kernel's shared-memory opt-in, launch nothing
+    bool curv;      // general geometry (the CURV kernels)
 };
+cudaError_t launch_elem_curv2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_curv3d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler1d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler3d_strong(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);

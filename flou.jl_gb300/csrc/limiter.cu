@@ -28,6 +28,7 @@ namespace flou {
 struct LimParams {
     double* Q;
     const double* J;   // per element
+    const double* Jn;  // per node (general geometry) or null
     const double* w;   // tensor quadrature weights [npe]
     int64_t ndofs;
     int nelem, npe;
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) S[k] = 0.0;
         for (int i = lane; i < P.npe; i += 32) {
-            double jw = Je * P.w[i];
+            double jw = (P.Jn ? P.Jn[b + i] : Je) * P.w[i];
             vol += jw;
 #pragma unroll
             for (int k = 0; k < NV; ++k) S[k] = fma(jw, P.Q[k * P.ndofs + b + i], S[k]);
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
             double r = P.Q[b + i];
             if (l1) r = th1 * (r - Qm[0]) + Qm[0];
             double p = node_pressure<DIM>(r, P.Q, P.ndofs, b + i, g1);
-            ps = fma(Je * P.w[i], p, ps);
+            ps = fma((P.Jn ? P.Jn[b + i] : Je) * P.w[i], p, ps);
             pmin = fmin(pmin, p);
         }
         double pbar = warp_sum(ps) / vol;
@@ -119,14 +120,14 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
 // Partial sums over blocks of nodes of Jω f(Q): [0] kinetic energy |ρv|²/(2ρ) (FlouCommon/Euler.jl:162-175),
 // [1] mathematical entropy -ρ s/(γ-1), s = log p - γ log ρ (FlouCommon/Euler.jl:202-217).
 template <int DIM>
-__global__ void __launch_bounds__(256) monitor_partial_kernel(const double* Q, const double* J, const double* w,
-                                                              int64_t ndofs, int npe, double gamma, int mask,
-                                                              double* partial) {
+__global__ void __launch_bounds__(256) monitor_partial_kernel(const double* Q, const double* J, const double* Jn,
+                                                              const double* w, int64_t ndofs, int npe, double gamma,
+                                                              int mask, double* partial) {
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double ke = 0.0, ent = 0.0;
     if (g < ndofs) {
         int64_t e = g / npe;
-        double jw = J[e] * w[g - e * npe];
+        double jw = (Jn ? Jn[g] : J[e]) * w[g - e * npe];
         double r = Q[g];
         double m2 = 0.0;
 #pragma unroll
@@ -252,9 +253,10 @@ int ensure_monitor_buffers(flou_ctx* c) {
 int launch_monitors(flou_ctx* c, cudaStream_t s, const double* Q, int mask, double* out, int32_t* count, int cap) {
     int nb = monitor_blocks(c);
     int d = c->cfg.dim;
-    if (d == 1) monitor_partial_kernel<1><<<nb, 256, 0, s>>>(Q, c->d_Jel, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
-    else if (d == 2) monitor_partial_kernel<2><<<nb, 256, 0, s>>>(Q, c->d_Jel, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
-    else monitor_partial_kernel<3><<<nb, 256, 0, s>>>(Q, c->d_Jel, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
+    const double* Jn = c->curv ? c->d_Jn : nullptr;
+    if (d == 1) monitor_partial_kernel<1><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
+    else if (d == 2) monitor_partial_kernel<2><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
+    else monitor_partial_kernel<3><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
     monitor_final_kernel<<<1, 256, 0, s>>>(c->d_monpart, nb, out, count, cap);
     return lcuda(c, cudaGetLastError(), "monitor kernels");
 }
@@ -278,6 +280,7 @@ int ctx_limit(flou_ctx* c, cudaStream_t s, double* Q) {
     LimParams P;
     P.Q = Q;
     P.J = c->d_Jel;
+    P.Jn = c->curv ? c->d_Jn : nullptr;
     P.w = c->d_wtp;
     P.ndofs = c->ndofs;
     P.nelem = c->nelem;

@@ -1,0 +1,142 @@
+"""General geometry on the GPU: unstructured straight-sided meshes whose elements are randomly
+rotated (every master2slave orientation occurs in 3D) and whose interior nodes are displaced,
+so J, the metric, the face frames and the surface Jacobians vary per node.  The residual and
+SSP-RK3 steps are checked against the oracle (which runs the reference's general loops)."""
+import numpy as np
+import pytest
+
+import flou_cuda as F
+from flou_cuda import _lib as L
+from cases import oracle_for, rel_linf
+from test_unstructured import _state, _std
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _ops():
+    return {
+        "strong_lxf": lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+        "strong_hllc": lambda: F.StrongDivOperator(F.HLLC()),
+        "split_chandra_lxfc": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(F.ChandrasekharAverage(), 1.0)),
+        "split_chandra_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
+        "split_kg_lxf": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
+        "split_std_lxf": lambda: F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)),
+    }
+
+
+def _bcs(dim, eq, walls):
+    if not walls:
+        return {str(k): F.EulerOutflowBC() for k in range(1, 2 * dim + 1)}
+    Pin = np.zeros(dim + 2)
+    Pin[0], Pin[1], Pin[-1] = 1.05, 0.2, 1.1
+    b = {"1": F.EulerInflowBC(eq.vars_prim2cons(Pin)), "2": F.EulerOutflowBC(), "3": F.EulerSlipBC(),
+         "4": F.EulerSlipBC()}
+    if dim == 3:
+        b.update({"5": F.EulerSlipBC(), "6": F.EulerOutflowBC()})
+    return b
+
+
+def _disc(dim, n, op, walls=False, nel=3, seed=5, amp=0.12):
+    eq = F.EulerEquation(dim, 1.4)
+    mesh = F.perturbed_box(dim, nel, (0.0,) * dim, (1.0,) * dim, amp=amp, seed=seed)
+    return F.MultielementDisc(mesh, _std(dim, n, dim + 2), eq, _ops()[op](), _bcs(dim, eq, walls))
+
+
+def _check(disc, Q, nsteps=4):
+    o = oracle_for(disc)
+    ref = o.rhs(Q)
+    dQ = disc.new_state()
+    disc.ctx.rhs(dQ, Q)
+    assert rel_linf(dQ, ref) <= 1e-12, rel_linf(dQ, ref)
+    dt = 0.2 * disc.ctx.max_dt(Q, 1.0)
+    assert abs(dt - 0.2 * o.max_dt(Q, 1.0, disc.std.omega)) <= 1e-14 * dt
+    Qg = Q.copy(order="F")
+    disc.ctx.step(Qg, dt, nsteps)
+    assert rel_linf(Qg, o.ssprk3(Q, dt, nsteps)) <= 1e-10
+
+
+@pytest.mark.parametrize("dim,n,op", [(2, 4, "strong_lxf"), (2, 5, "split_chandra_lxfc"), (2, 3, "strong_hllc"),
+                                      (2, 4, "split_kg_lxf"), (2, 4, "split_std_lxf"), (2, 4, "split_chandra_md"),
+                                      (3, 3, "strong_lxf"), (3, 4, "split_chandra_lxfc"), (3, 3, "strong_hllc"),
+                                      (3, 3, "split_kg_lxf"), (3, 4, "split_std_lxf"), (3, 3, "split_chandra_md"),
+                                      (3, 6, "split_chandra_lxfc"), (2, 8, "strong_lxf")])
+def test_unstructured_euler(dim, n, op):
+    disc = _disc(dim, n, op)
+    if dim == 3:
+        assert len(set(disc.mesh.orientation.tolist())) == 8
+    assert disc.ctx is not None
+    _check(disc, _state(disc, seed=dim + n))
+
+
+@pytest.mark.parametrize("dim,op", [(2, "strong_lxf"), (2, "split_chandra_lxfc"), (3, "split_chandra_lxfc"),
+                                    (3, "strong_hllc")])
+def test_unstructured_walls_inflow_outflow(dim, op):
+    disc = _disc(dim, 4, op, walls=True)
+    _check(disc, _state(disc, seed=11))
+
+
+@pytest.mark.parametrize("dim,op", [(2, "strong"), (2, "split"), (3, "strong"), (3, "split")])
+def test_unstructured_linear_advection(dim, op):
+    eq = F.LinearAdvection(*([1.0, -0.5, 0.3][:dim]))
+    mesh = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.1, seed=2)
+    nf = F.LxF(F.StdAverage(), 1.0)
+    oper = F.StrongDivOperator(nf) if op == "strong" else F.SplitDivOperator(nf)
+    bcs = {str(k): F.DirichletBC([1.0]) for k in range(1, 2 * dim + 1)}
+    disc = F.MultielementDisc(mesh, _std(dim, 4, 1), eq, oper, bcs)
+    X = disc.coords
+    Q = np.asfortranarray((1.0 + 0.3 * np.sin(3 * X[:, 0]) * np.cos(2 * X[:, 1]))[:, None])
+    o = oracle_for(disc)
+    dQ = disc.new_state()
+    disc.ctx.rhs(dQ, Q)
+    assert rel_linf(dQ, o.rhs(Q)) <= 1e-12
+    dt = 1e-3
+    Qg = Q.copy(order="F")
+    disc.ctx.step(Qg, dt, 4)
+    assert rel_linf(Qg, o.ssprk3(Q, dt, 4)) <= 1e-10
+
+
+def test_unstructured_freestream_on_gpu():
+    disc = _disc(3, 4, "split_chandra_lxfc", amp=0.2)
+    P = np.zeros((disc.ndofs, 5))
+    P[:, 0], P[:, 1:4], P[:, 4] = 1.2, (0.3, -0.2, 0.1), 1.7
+    Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+    dQ = disc.new_state()
+    disc.ctx.rhs(dQ, Q)
+    assert np.max(np.abs(dQ)) < 1e-11
+
+
+def test_unstructured_limiter_and_monitors():
+    disc = _disc(2, 4, "split_chandra_lxfc")
+    Q = _state(disc, seed=3)
+    P = disc.equation.vars_cons2prim(Q)
+    P[20, 0] = 0.02
+    Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+    o = oracle_for(disc)
+    disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.1)
+    Qg = Q.copy(order="F")
+    disc.ctx.limit(Qg)
+    assert rel_linf(Qg, o.limit(Q, 0.1, disc.std.omega)) <= 1e-13
+    disc.ctx.set_limiter(L.LIMITER_NONE)
+    for which in (L.MONITOR_KINETIC_ENERGY, L.MONITOR_ENTROPY):
+        ref = o.monitor(Q, which, disc.std.omega)
+        assert abs(disc.ctx.monitor(Q, which) - ref) <= 1e-13 * abs(ref)
+
+
+def test_general_geometry_is_rejected_where_not_covered():
+    disc = _disc(2, 4, "strong_lxf")
+    Q = torch.from_numpy(np.ascontiguousarray(_state(disc).T)).cuda()
+    with pytest.raises(F.FlouError) as ei:
+        F.Batch([disc], [Q], [1e-3])
+    g = torch.empty_like(Q)
+    with pytest.raises(F.FlouError) as ei:
+        disc.ctx.adjoint_solve(Q, 1e-3, 2, 1, Q[0].clone(), Q[0].clone(), g)
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+    eq = F.EulerEquation(2, 1.4)
+    mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=1)
+    b = F.LagrangeBasis("GL", 4)
+    gl = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), 4), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
+                            {str(k): F.EulerOutflowBC() for k in range(1, 5)})
+    with pytest.raises(F.FlouError) as ei:
+        gl.ctx
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED

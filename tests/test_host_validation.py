@@ -72,9 +72,12 @@ def test_corrupted_connectivity_is_rejected():
     st, msg = _check_mesh(2, b)
     assert st == L.FLOU_ERR_ARG and "out of range" in msg
     b = {k: v.copy() for k, v in a.items()}
-    b["orientation"][2] = 4                               # non-conforming face
+    b["orientation"][2] = 4                               # a 2D face takes orientation 0 or 1
     st, msg = _check_mesh(2, b)
-    assert st == L.FLOU_ERR_UNSUPPORTED and "orientation" in msg
+    assert st == L.FLOU_ERR_ARG and "orientation" in msg
+    b = {k: v.copy() for k, v in a.items()}
+    b["orientation"][2] = 1                               # reversed face: valid (general geometry)
+    assert _check_mesh(2, b)[0] == L.FLOU_OK
     b = {k: v.copy() for k, v in a.items()}
     f = int(np.nonzero(b["eleminds"][:, 1] == 0)[0][0])
     b["bdface_index"][f] = 0                              # boundary face without a boundary
@@ -87,21 +90,27 @@ def test_corrupted_connectivity_is_rejected():
     assert st == L.FLOU_ERR_ARG and "interior face" in msg
 
 
-def test_non_cartesian_geometry_is_rejected():
+def test_geometry_validation():
+    """General (curvilinear / unstructured) geometry is accepted; malformed geometry is not."""
     d = _disc(2)
     a = _mesh_args(d)
     Ja = a["Ja"].copy()
     Ja[5, 1] = 1e-3                                       # off-diagonal metric term
-    st, msg = _check_geom(2, 4, a, Ja=Ja)
-    assert st == L.FLOU_ERR_UNSUPPORTED and "metric" in msg
+    assert _check_geom(2, 4, a, Ja=Ja)[0] == L.FLOU_OK
     J = a["J"].copy()
     J[17] *= 1.01                                         # Jacobian varies inside element 2
-    st, msg = _check_geom(2, 4, a, J=J)
-    assert st == L.FLOU_ERR_UNSUPPORTED and "element 2" in msg
+    assert _check_geom(2, 4, a, J=J)[0] == L.FLOU_OK
     fr = a["frames"].copy()
-    fr[9, 0] = -fr[9, 0]                                  # face 3's normal flipped
+    fr[9, 0] = -fr[9, 0]                                  # another (unit) normal
+    assert _check_geom(2, 4, a, frames=fr)[0] == L.FLOU_OK
+    fr = a["frames"].copy()
+    fr[9, 0] = 2.0 * fr[9, 0]                             # not a unit normal
     st, msg = _check_geom(2, 4, a, frames=fr)
-    assert st == L.FLOU_ERR_UNSUPPORTED and "frame" in msg
+    assert st == L.FLOU_ERR_ARG and "unit" in msg
     J = -a["J"]
     st, msg = _check_geom(2, 4, a, J=J)
     assert st == L.FLOU_ERR_ARG and "J <= 0" in msg
+    fj = a["faceJ"].copy()
+    fj[3] = 0.0
+    st, msg = _check_geom(2, 4, a, faceJ=fj)
+    assert st == L.FLOU_ERR_ARG and "surface Jacobian" in msg
