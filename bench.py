@@ -320,6 +320,44 @@ def bench_adjoint(nsteps=400, nsnap=20, ndirs=32, seed=404):
     return res
 
 
+def bench_curvilinear(steps, warmup, stream, kern_cart):
+    """The general-geometry kernels on mesh A's size: a periodic-free [0, 2π]³ box of 32³
+    straight-sided hexahedra with interior nodes displaced by 10% of a cell and every element's
+    local numbering rotated at random (all master2slave orientations), p = 3, TGV Mach 0.1,
+    split form with the Chandrashekar flux and HLLC, outflow boundaries."""
+    import torch
+    import flou_cuda as F
+    t0 = time.perf_counter()
+    mesh = F.perturbed_box(3, 32, (0.0,) * 3, (2 * math.pi,) * 3, amp=0.1, seed=1)
+    eq = F.EulerEquation(3, 1.4)
+    b = F.LagrangeBasis("GLL", 4)
+    disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), 5), eq,
+                              F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()),
+                              {k: F.EulerOutflowBC() for k in mesh.bdnames})
+    Q0 = np.asfortranarray(F.initial.taylor_green(eq, disc.coords, mach=0.1))
+    setup_s = time.perf_counter() - t0
+    ctx = disc.ctx
+    ctx.set_stream(stream.cuda_stream)
+    q = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+    dt = 0.2 * ctx.max_dt(q, 1.0)
+    ctx.step(q, dt, warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx.step(q, dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    fms, ems = ctx.time_kernels(q, nrep=3)
+    ctx.set_stream(0)
+    units = disc.ndofs * 3
+    return {"value": units / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "face_ms": fms, "elem_ms": ems,
+            "ndofs": disc.ndofs, "cartesian_face_ms": kern_cart["face_ms"], "cartesian_elem_ms": kern_cart["elem_ms"],
+            "elem_cost_vs_cartesian": ems / kern_cart["elem_ms"], "face_cost_vs_cartesian": fms / kern_cart["face_ms"],
+            "orientations": sorted(set(int(o) for o in mesh.orientation)), "setup_s": setup_s,
+            "workload": "32^3 perturbed (10%) rotated hex, p=3, TGV M0.1, split Chandrashekar + HLLC, outflow"}
+
+
 def make_adjoint_batch(count=64, seed=505, mmin=8, mmax=24):
     """The batched-adjoint configuration: `count` periodic [0, 2π]³ hex meshes of m³ elements,
     m ~ U{8..24}, p ~ U{3, 4, 5}, Taylor-Green vortex at Mach ~ U(0.05, 0.3) (plus a 1e-3 smooth
@@ -499,6 +537,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-curvilinear", action="store_true")
     ap.add_argument("--adjoint-batch", action="store_true",
                     help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
                          "several minutes)")
@@ -612,6 +651,14 @@ def main():
     if fp64_ops and fp64_peak:
         roofline["fp64"]["frac"] = roofline["fp64"]["achieved_gflops"] / fp64_peak
 
+    # ---- general geometry: the curvilinear kernels on mesh A's size ----
+    curvilinear = None
+    if not args.no_curvilinear:
+        try:
+            curvilinear = bench_curvilinear(steps, warmup, stream, kern[meshes[0]["name"]])
+        except Exception as exc:   # reported, not fatal to the bench line
+            curvilinear = {"error": str(exc)}
+
     # ---- cost of the Zhang-Shu stage limiter (minval 1e-10, as examples/src/3D_Euler.jl:76) ----
     limiter = None
     try:
@@ -686,7 +733,7 @@ def main():
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
-            "adjoint_batch": adjoint_batch, "limiter": limiter, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
+            "adjoint_batch": adjoint_batch, "limiter": limiter, "curvilinear": curvilinear, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -385,7 +385,8 @@ def perturbed_box(dim, nel, start, finish, amp=0.1, seed=0, rotate=True):
 # Geometry of the linear mappings (Mesh.jl:380-487, PhysicalRegions.jl:438-472, 756-971)
 # ---------------------------------------------------------------------------------------
 def _main_basis(dim, P, r):
-    """d x / d ξ_k of the linear map at relative coordinates r = (ξ+1)/2; P: corner coordinates."""
+    """d x / d ξ_k of the linear map at relative coordinates r = (ξ+1)/2 (Mesh.jl:386-475).
+    P: corner coordinates, P[k] of shape (..., dim) (vectorised over elements)."""
     if dim == 1:
         return [(P[1] - P[0]) / 2]
     if dim == 2:
@@ -403,64 +404,70 @@ def _main_basis(dim, P, r):
 
 
 def _dual_basis(dim, main):
+    """Mesh.jl:391-394, 423-428, 477-483: J ∇ξ_k of the linear map."""
     if dim == 1:
-        return [np.ones(1)]
+        return [np.ones_like(main[0])]
     if dim == 2:
-        return [np.array([main[1][1], -main[1][0]]), np.array([-main[0][1], main[0][0]])]
+        return [np.stack([main[1][..., 1], -main[1][..., 0]], -1), np.stack([-main[0][..., 1], main[0][..., 0]], -1)]
     return [np.cross(main[1], main[2]), np.cross(main[2], main[0]), np.cross(main[0], main[1])]
 
 
 def _jacobian(dim, main):
+    """Mesh.jl:396-398, 430-432, 485-487."""
     if dim == 1:
-        return main[0][0]
+        return main[0][..., 0]
     if dim == 2:
-        return main[0][0] * main[1][1] - main[0][1] * main[1][0]
-    return np.dot(main[0], np.cross(main[1], main[2]))
+        return main[0][..., 0] * main[1][..., 1] - main[0][..., 1] * main[1][..., 0]
+    return np.einsum("...k,...k->...", main[0], np.cross(main[1], main[2]))
 
 
 def _phys(dim, P, r):
-    w = []
-    for c in CORNERS[dim]:
+    out = 0.0
+    for c, Pk in zip(CORNERS[dim], P):
         v = 1.0
         for q in range(dim):
             v = v * (r[q] if c[q] > 0 else (1 - r[q]))
-        w.append(v)
-    return sum(wk * Pk for wk, Pk in zip(w, P))
+        out = out + v * Pk
+    return out
 
 
 def unstructured_geometry(mesh, std):
     """Per-node J and metric (columns = dual basis), per-face-node frame (n, t, b) and surface
-    Jacobian (master side), and node coordinates of an UnstructuredMesh."""
+    Jacobian (master side), and node coordinates of an UnstructuredMesh
+    (PhysicalRegions.jl:438-472, 756-971); vectorised over elements and faces."""
     d, n = mesh.dim, std.n
     xi = std.xi1d
     npe, nfd = n ** d, n ** (d - 1)
     ne, nf = mesh.nelements, mesh.nfaces
-    J = np.zeros(ne * npe)
-    Ja = np.zeros((ne * npe, d * d))
-    coords = np.zeros((ne * npe, 3))
+    P = [mesh.nodes[mesh.elements[:, k]] for k in range(2 ** d)]   # each (ne, d)
+    J = np.zeros((ne, npe))
+    Ja = np.zeros((ne, npe, d * d))
+    coords = np.zeros((ne, npe, 3))
     loc = np.array(np.unravel_index(np.arange(npe), (n,) * d, order="F")).T   # x fastest
-    for e in range(ne):
-        P = [mesh.nodes[v] for v in mesh.elements[e]]
-        for i in range(npe):
-            r = [(xi[loc[i, q]] + 1) / 2 for q in range(d)]
-            main = _main_basis(d, P, r)
-            dual = _dual_basis(d, main)
-            jac = _jacobian(d, main)
-            if d < 3:
-                jac = abs(jac)
-            elif not jac > 0:
-                raise ValueError("Found a negative Jacobian in element %d." % (e + 1))
-            g = e * npe + i
-            J[g] = jac
-            Ja[g] = np.concatenate(dual)     # column-major: column k = dual[k]
-            coords[g, :d] = _phys(d, P, r)
-    frames = np.zeros((nf * nfd, 9))
-    faceJ = np.zeros(nf * nfd)
+    for i in range(npe):
+        r = [(xi[loc[i, q]] + 1) / 2 for q in range(d)]
+        main = _main_basis(d, P, r)
+        dual = _dual_basis(d, main)
+        jac = _jacobian(d, main)
+        if d < 3:
+            jac = np.abs(jac)
+        elif not np.all(jac > 0):
+            raise ValueError("Found a negative Jacobian in element %d." % (int(np.argmin(jac > 0)) + 1))
+        J[:, i] = jac
+        Ja[:, i, :] = np.concatenate(dual, axis=-1)    # column-major: column k = dual[k]
+        coords[:, i, :d] = _phys(d, P, r)
+    frames = np.zeros((nf, nfd, 9))
+    faceJ = np.zeros((nf, nfd))
     floc = np.array(np.unravel_index(np.arange(nfd), (n,) * (d - 1), order="F")).T if d > 1 else np.zeros((1, 0), int)
-    for f in range(nf):
-        e = mesh.eleminds[f, 0] - 1
-        pos = int(mesh.elempos[f, 0])
-        P = [mesh.nodes[v] for v in mesh.elements[e]]
+    me = mesh.eleminds[:, 0] - 1
+    mpos = mesh.elempos[:, 0]
+    tsign2 = {1: -1.0, 2: 1.0, 3: 1.0, 4: -1.0}
+    tax3 = {1: 1, 2: 1, 3: 2, 4: 2, 5: 0, 6: 0}
+    for pos in range(1, 2 * d + 1):
+        fs = np.nonzero(mpos == pos)[0]
+        if len(fs) == 0:
+            continue
+        Pf = [Pk[me[fs]] for Pk in P]
         ax = (pos - 1) // 2
         sgn = -1.0 if pos % 2 == 1 else 1.0
         tang = [q for q in range(d) if q != ax]
@@ -470,33 +477,29 @@ def unstructured_geometry(mesh, std):
             for k, q in enumerate(tang):
                 xi_e[q] = xi[floc[m, k]]
             r = [(v + 1) / 2 for v in xi_e]
-            main = _main_basis(d, P, r)
+            main = _main_basis(d, Pf, r)
             dual = _dual_basis(d, main)
-            nvec = np.zeros(3)
-            tvec = np.zeros(3)
-            bvec = np.zeros(3)
+            out = np.zeros((len(fs), 9))
             if d == 1:
-                s = np.sign(_jacobian(d, main))
+                s = np.sign(_jacobian(d, main))[:, None]
                 nv = sgn * dual[0] * s
             elif d == 2:
-                s = np.sign(_jacobian(d, main))
                 # PhysicalRegions.jl:797-871: n = ±dual[ax] s, t = ±normalize(main[other]) s
+                s = np.sign(_jacobian(d, main))[:, None]
                 nv = sgn * dual[ax] * s
-                other = 1 - ax
-                tsign = {1: -1.0, 2: 1.0, 3: 1.0, 4: -1.0}[pos]
-                tv = tsign * main[other] / np.linalg.norm(main[other]) * s
-                tvec[:2] = tv
+                mo = main[1 - ax]
+                out[:, 3:5] = tsign2[pos] * mo / np.linalg.norm(mo, axis=1)[:, None] * s
             else:
                 # PhysicalRegions.jl:873-971: n = ±dual[ax], t = ±normalize(main[next]), b = n × t
                 nv = sgn * dual[ax]
-                tax = {1: 1, 2: 1, 3: 2, 4: 2, 5: 0, 6: 0}[pos]
-                tv = sgn * main[tax] / np.linalg.norm(main[tax])
+                mt = main[tax3[pos]]
+                tv = sgn * mt / np.linalg.norm(mt, axis=1)[:, None]
                 bv = np.cross(nv, tv)
-                bvec[:] = bv / np.linalg.norm(bv)
-                tvec[:] = tv
-            jac = np.linalg.norm(nv)
-            nvec[:d] = nv / jac
-            idx = f * nfd + m
-            frames[idx] = np.concatenate([nvec, tvec, bvec])
-            faceJ[idx] = jac
-    return J, Ja, frames, faceJ, coords
+                out[:, 3:6] = tv
+                out[:, 6:9] = bv / np.linalg.norm(bv, axis=1)[:, None]
+            jac = np.linalg.norm(nv, axis=1)
+            out[:, :d] = nv / jac[:, None]
+            frames[fs, m] = out
+            faceJ[fs, m] = jac
+    return (J.ravel(), Ja.reshape(ne * npe, d * d), frames.reshape(nf * nfd, 9), faceJ.ravel(),
+            coords.reshape(ne * npe, 3))
