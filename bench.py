@@ -518,6 +518,16 @@ def run_profile(which):
         print(json.dumps({"profile_case": "adjoint " + which, "ndofs": disc.ndofs, "steps": nsteps,
                           "recomputed": nf, "J": J}))
         return 0
+    if which == "F":   # mesh A with the Zhang-Shu stage limiter (minval 1e-10), two steps
+        disc, Q0 = make_tgv(32, 4)
+        import flou_cuda as F
+        Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+        dt = 0.2 * disc.ctx.max_dt(Qd, 1.0)
+        disc.ctx.set_limiter(F._lib.LIMITER_ZHANG_SHU, 1e-10)
+        disc.ctx.step(Qd, dt, 2)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "tgv3d 32^3 p=3 + limiter", "ndofs": disc.ndofs, "steps": 2}))
+        return 0
     nel, n = (32, 4) if which == "A" else (16, 8)
     disc, Q0 = make_tgv(nel, n)
     Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
@@ -542,10 +552,11 @@ def main():
                     help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
                          "several minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
-    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E"], default=None,
+    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling); "
-                         "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps)")
+                         "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps); F: mesh A with the "
+                         "Zhang-Shu stage limiter")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

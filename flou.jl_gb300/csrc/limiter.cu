@@ -2,13 +2,13 @@
 // equations (src/FlouSpatial/Equations/Euler.jl:541-654), as the stage limiter and the monitor
 // callbacks of Flou's time integration (src/FlouTime/FlouTime.jl:107-148).
 //
-// Limiter: one warp per element.  Pass 1 forms the element mean Q̄ = Σ Jω Q / Σ Jω and the
-// minimum density; pass 2 the mean and minimum of the pressure of the density-limited nodes;
-// pass 3 writes the limited element (only elements that change).  The warp reductions are
+// Limiter: one warp per element.  A division-free test first skips elements whose density and
+// pressure are above the minimum everywhere (the reference changes nothing there); otherwise
+// pass 1 forms the element mean Q̄ = Σ Jω Q / Σ Jω and the minimum density, pass 2 the mean and
+// minimum of the pressure of the density-limited nodes, pass 3 writes the limited element.  The warp reductions are
 // butterfly shuffles: IEEE addition is commutative, so every lane ends with the same bits and
 // the result does not depend on scheduling.  Run after every stage inside the step graph, the
-// pass reads and writes the state once more (about 80 B per node against a stage that is bound by
-// the FP64 pipe, not by HBM).
+// pass reads the state once more; FP64 is the limit on GB300, hence the division-free test.
 //
 // Monitors: per-block partial sums of Jω f(Q) (f = kinetic energy or mathematical entropy) in a
 // fixed reduction order, then one block sums the partials in a fixed order and appends the
@@ -68,6 +68,26 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
     for (int e = warp; e < P.nelem; e += nwarps) {
         const double Je = P.J[e];
         const int64_t b = (int64_t)e * P.npe;
+        // Fast exit.  With m = min(minval, mean), θ > 1 (no change) exactly when the minimum is
+        // above minval: density when ρ_min > minval, pressure when p_min > minval, i.e. when
+        // 2ρ((γ-1)E - minval) > (γ-1)|ρv|² at every node (no division).  Elements that clear
+        // both tests by a relative margin of 1e-12 are left alone; the others take the full
+        // computation below, as the reference writes it.
+        bool clear = true;
+        for (int i = lane; i < P.npe; i += 32) {
+            double r = P.Q[b + i];
+            double ke = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                double mk = P.Q[(1 + k) * P.ndofs + b + i];
+                ke = fma(mk, mk, ke);
+            }
+            double E = P.Q[(DIM + 1) * P.ndofs + b + i];
+            double lhs = 2.0 * r * fma(g1, E, -P.minval), rhs = g1 * ke;
+            double tol = 1e-12 * (fabs(2.0 * r * g1 * E) + fabs(2.0 * r * P.minval) + rhs);
+            clear = clear && r > 0.0 && (r - P.minval > 1e-12 * fabs(P.minval) + 1e-300) && (lhs - rhs > tol);
+        }
+        if (__all_sync(0xffffffffu, clear)) continue;
         double S[NV], vol = 0.0, rmin = INFINITY;
 #pragma unroll
         for (int k = 0; k < NV; ++k) S[k] = 0.0;
