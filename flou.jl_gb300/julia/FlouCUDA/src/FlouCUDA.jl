@@ -88,7 +88,7 @@ end
 
 Uploads the operators (StdSegment.jl:77-89), the connectivity after `apply_periodicBCs!`
 (Mesh.jl:236-322), the boundary conditions and the geometry of `disc` to a libflou_cuda
-context. Only Cartesian geometry is accepted.
+context. Cartesian and UnstructuredMesh (straight-sided, per-node) geometry are accepted.
 """
 function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
     cfg = Ref(flou_config(disc, equation))

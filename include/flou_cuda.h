@@ -133,8 +133,11 @@ int32_t flou_set_bcs(flou_ctx* ctx, int32_t nbcs, const int32_t* kinds, const do
 /* Geometry (Geometry, src/FlouSpatial/PhysicalRegions.jl:982-991): per node J (ndofs),
  * metric Ja (ndofs x d x d, column-major per node); per face node the frame
  * (nfacedofs x 3 x 3: n, t, b with 3 components each) and the surface Jacobian
- * (nfacedofs).  Only Cartesian geometry is supported: J and a diagonal Ja constant per
- * element, one frame and one surface Jacobian per face. */
+ * (nfacedofs).  Cartesian geometry (J and a diagonal Ja constant per element, the Cartesian
+ * frames, every face orientation 0) takes a compressed fast path; any other geometry
+ * (curvilinear / unstructured, PhysicalRegions.jl:438-472 and :756-971) is used per node and
+ * needs an LGL basis in 2D or 3D.  Rejected: J <= 0, non-finite entries, non-unit normals,
+ * surface Jacobians <= 0. */
 int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, const double* frames,
                           const double* face_J);
 
