@@ -518,6 +518,16 @@ def run_profile(which):
         print(json.dumps({"profile_case": "adjoint " + which, "ndofs": disc.ndofs, "steps": nsteps,
                           "recomputed": nf, "J": J}))
         return 0
+    if which == "G":   # FP64 throughput probes: CUDA-core DFMA and tensor-core DMMA
+        import ctypes
+        import flou_cuda as F
+        lib = F.load()
+        g1, g2 = ctypes.c_double(), ctypes.c_double()
+        st1 = lib.flou_fp64_peak(ctypes.byref(g1))
+        st2 = lib.flou_fp64_dmma_peak(ctypes.byref(g2))
+        print(json.dumps({"profile_case": "fp64 probes", "dfma_gflops": g1.value if st1 == 0 else None,
+                          "dmma_gflops": g2.value if st2 == 0 else None}))
+        return 0
     if which == "F":   # mesh A with the Zhang-Shu stage limiter (minval 1e-10), two steps
         disc, Q0 = make_tgv(32, 4)
         import flou_cuda as F
@@ -552,11 +562,11 @@ def main():
                     help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
                          "several minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
-    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F"], default=None,
+    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling); "
                          "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps); F: mesh A with the "
-                         "Zhang-Shu stage limiter")
+                         "Zhang-Shu stage limiter; G: the FP64 DFMA and DMMA throughput probes")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -597,12 +607,14 @@ def main():
         m["ctx"].set_stream(stream.cuda_stream)
     ndofs = sum(m["ndofs"] for m in meshes)
 
-    fp64_peak = None
+    fp64_peak = dmma_peak = None
     try:
         import ctypes
         g = ctypes.c_double()
         if F.load().flou_fp64_peak(ctypes.byref(g)) == 0:
             fp64_peak = g.value
+        if F.load().flou_fp64_dmma_peak(ctypes.byref(g)) == 0:
+            dmma_peak = g.value
     except Exception:
         pass
 
@@ -654,6 +666,7 @@ def main():
         "launch_ms": dk["elem_ms"],
         "fp64": {
             "peak_gflops": fp64_peak, "peak_source": "DFMA throughput probe (flou_fp64_peak), this run",
+            "dmma_peak_gflops": dmma_peak,
             "executed_flops_per_dof_stage": fp64_ops,
             "achieved_gflops": (fp64_ops * dk["ndofs"] / (dk["elem_ms"] * 1e-3) / 1e9) if fp64_ops else None,
         },

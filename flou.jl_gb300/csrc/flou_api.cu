@@ -242,6 +242,27 @@ __global__ void fma_probe_kernel(double* sink, int iters, double x) {
     if (s == 1234.5678) sink[threadIdx.x] = s;   // never true; keeps the chains alive
 }
 
+// FP64 tensor-core probe: eight independent m8n8k4 DMMA chains per warp (mma.sync with f64
+// operands, the only FP64 matrix instruction of sm_103a; tcgen05 has no f64 kind).  Each
+// instruction does 8*8*4 multiply-adds for the warp.
+__global__ void dmma_probe_kernel(double* sink, int iters, double x) {
+    double a = 1e-3 * x, b = 1e-3 * x + 1e-6 * (threadIdx.x & 31);
+    double c[8][2];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = 1e-3 * k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(c[k][0]), "+d"(c[k][1])
+                         : "d"(a), "d"(b));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
+    if (s == 1234.5678) sink[threadIdx.x] = s;   // never true; keeps the chains alive
+}
+
 // Validates Flou's 1-based connectivity and packs it for the kernels (no CUDA involved):
 //   ef[e*2d + k] = (face << 1) | side,  fe[2f + s] = (elem << 3) | local position (-1: none),
 //   fb[f] = boundary index (0-based) or -1.
@@ -835,6 +856,34 @@ int32_t flou_fp64_peak(double* gflops) {
     cudaFree(sink);
     if (e != cudaSuccess) return FLOU_ERR_CUDA;
     double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+    *gflops = flops / (ms * 1e-3) / 1e9;
+    return FLOU_OK;
+}
+
+int32_t flou_fp64_dmma_peak(double* gflops) {
+    if (!gflops) return FLOU_ERR_ARG;
+    flou_ctx* c = nullptr;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    double* sink = nullptr;
+    CK(cudaMalloc((void**)&sink, 1024 * sizeof(double)), "probe buffer");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int iters = 1 << 12, threads = 256, blocks = sms * 8;
+    dmma_probe_kernel<<<blocks, threads>>>(sink, 16, 1.0);   // warm-up
+    cudaEventRecord(a);
+    dmma_probe_kernel<<<blocks, threads>>>(sink, iters, 1.0);
+    cudaEventRecord(b);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return FLOU_ERR_CUDA;
+    double flops = 2.0 * 8.0 * 8.0 * 4.0 * 8.0 * (double)iters * (threads / 32) * blocks;
     *gflops = flops / (ms * 1e-3) / 1e9;
     return FLOU_OK;
 }

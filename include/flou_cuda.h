@@ -199,6 +199,10 @@ int32_t flou_check_geometry(int32_t dim, int32_t nnodes, int32_t nelem, int32_t 
 /* Measured FP64 fused-multiply-add throughput of the current device in GFLOP/s (2 flops per
  * FMA), used as the FP64 roofline denominator.  No counterpart in the reference. */
 int32_t flou_fp64_peak(double* gflops);
+/* The same for the FP64 tensor cores: m8n8k4 DMMA (mma.sync with f64 operands) throughput in
+ * GFLOP/s, the measurement behind the choice of CUDA-core FP64 for the derivative-matrix
+ * contraction.  No counterpart in the reference. */
+int32_t flou_fp64_dmma_peak(double* gflops);
 
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
  * Covers the Euler equations with the strong-form volume term or the split form with the
