@@ -15,6 +15,7 @@ from .unstructured import UnstructuredMesh, perturbed_box, read_gmsh, write_gmsh
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
 from .timeint import SSPRK33, get_limiter_callback, get_monitor_callback, timeintegrate
 from . import initial
+from .io import load_restart, save_restart, variablenames, write_vtu
 from .batch import Batch, adjoint_solve_batch
 
 rhs = rhs_
