@@ -2,7 +2,6 @@
 #include "flou_internal.cuh"
 namespace flou {
 cudaError_t launch_elem_euler3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
-    if (L.vol != FLOU_OP_SPLIT) return cudaErrorInvalidValue;
-    return launch_elem_dim<3, FLOU_EQ_EULER>(L.n, L.vol, L.tp, L.lgl, P, s, L.prepare);
+    return launch_elem_dim<3, FLOU_EQ_EULER, FLOU_OP_SPLIT>(L.n, L.vol, L.tp, L.lgl, P, s, L.prepare);
 }
 }  // namespace flou

@@ -43,6 +43,7 @@ cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s
     if (L.eq != FLOU_EQ_EULER) return launch_elem_scalar(L, P, s);
     if (L.dim == 1) return launch_elem_euler1d(L, P, s);
     if (L.dim == 2) return launch_elem_euler2d(L, P, s);
-    return L.vol == FLOU_OP_STRONG ? launch_elem_euler3d_strong(L, P, s) : launch_elem_euler3d_split(L, P, s);
+    if (L.vol == FLOU_OP_STRONG) return launch_elem_euler3d_strong(L, P, s);
+    return L.vol == FLOU_OP_HYBRID ? launch_elem_euler3d_hybrid(L, P, s) : launch_elem_euler3d_split(L, P, s);
 }
 }  // namespace flou

@@ -66,6 +66,8 @@ int ready(flou_ctx* c) {
     if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators has not been called");
     if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh has not been called");
     if (!c->have_geom) return fail(c, FLOU_ERR_STATE, "flou_set_geometry has not been called");
+    if (c->cfg.volume_op == FLOU_OP_HYBRID && !c->have_hybrid)
+        return fail(c, FLOU_ERR_STATE, "flou_set_hybrid has not been called (hybrid operator)");
     for (int f = 0; f < c->nfaces; ++f) {
         int b = c->h_face_bc[f];
         if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
@@ -128,6 +130,11 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.gamma = c->cfg.gamma;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     P.status = c->d_status;
+    P.omega1 = c->d_omega1;
+    P.fvflux = c->fvflux;
+    P.fvavg = c->fvavg;
+    P.fvintensity = c->fvintensity;
+    P.blend = c->blend;
     P.invJn = c->d_invJn;
     P.Jan = c->d_Jan;
     P.orient = c->d_orient;
@@ -428,7 +435,9 @@ int32_t flou_create(const flou_config* cfg, flou_ctx** out) {
     if (cfg->nnodes < 2 || cfg->nnodes > MAXN) return FLOU_ERR_ARG;
     if (cfg->equation < 0 || cfg->equation > 2) return FLOU_ERR_ARG;
     if (cfg->equation == FLOU_EQ_BURGERS && cfg->dim != 1) return FLOU_ERR_ARG;
-    if (cfg->volume_op != FLOU_OP_STRONG && cfg->volume_op != FLOU_OP_SPLIT) return FLOU_ERR_ARG;
+    if (cfg->volume_op != FLOU_OP_STRONG && cfg->volume_op != FLOU_OP_SPLIT && cfg->volume_op != FLOU_OP_HYBRID)
+        return FLOU_ERR_ARG;
+    if (cfg->volume_op == FLOU_OP_HYBRID && cfg->equation != FLOU_EQ_EULER) return FLOU_ERR_UNSUPPORTED;
     if (cfg->numflux < 0 || cfg->numflux > 6) return FLOU_ERR_ARG;
     if (cfg->numflux_avg != FLOU_NF_STD_AVERAGE && cfg->numflux_avg != FLOU_NF_CHANDRASHEKAR) return FLOU_ERR_ARG;
     if (cfg->equation != FLOU_EQ_EULER && cfg->numflux != FLOU_NF_STD_AVERAGE && cfg->numflux != FLOU_NF_LXF)
@@ -463,7 +472,7 @@ int32_t flou_destroy(flou_ctx* c) {
     drop_graph(c);
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
                     c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c, c->d_invJn, c->d_Jan,
-                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn};
+                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1};
     for (void* b : bufs)
         if (b) cudaFree(b);
     ctx_free_limiter(c);
@@ -501,12 +510,13 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
         if (i != 0 && (l_l[i] != 0.0 || dg_l[i] != 0.0)) lgl = false;
         if (i != n - 1 && (l_r[i] != 0.0 || dg_r[i] != 0.0)) lgl = false;
     }
-    if (c->cfg.volume_op == FLOU_OP_SPLIT && !lgl)
+    if (c->cfg.volume_op != FLOU_OP_STRONG && !lgl)
         return fail(c, FLOU_ERR_UNSUPPORTED,
-                    "the split-form operator needs a basis with boundary nodes (the subcell path of "
-                    "OpDivergence.jl:301-437 is not implemented)");
+                    "the split-form and hybrid operators need a basis with boundary nodes (the entropy-"
+                    "projected Gauss-node path of OpDivergence.jl:301-437 is not implemented)");
     int r = upload(c, &c->d_ops, ops.data(), ops.size(), "operator upload");
     if (r) return r;
+    if ((r = upload(c, &c->d_omega1, omega, (size_t)n, "operator upload"))) return r;
     c->lgl = lgl;
     c->omega.assign(omega, omega + n);
     c->have_ops = true;
@@ -586,6 +596,9 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
                                              "boundary nodes (LGL)");
     if (curv && c->cfg.equation == FLOU_EQ_BURGERS)
         return fail(c, FLOU_ERR_UNSUPPORTED, "Burgers' equation is 1D");
+    if (curv && c->cfg.volume_op == FLOU_OP_HYBRID)
+        return fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator covers Cartesian geometry (its subcell frames "
+                                             "are those of the axes)");
     std::vector<double> Jel(c->nelem);
     for (int e = 0; e < c->nelem; ++e) Jel[e] = J[(size_t)e * c->npe];
     if ((r = upload(c, &c->d_Jel, Jel.data(), Jel.size(), "geometry upload"))) return r;
@@ -611,6 +624,22 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     if ((r = upload(c, &c->d_faceJ, fJ.data(), fJ.size(), "geometry upload"))) return r;
     if ((r = upload(c, &c->d_dx, dx.data(), dx.size(), "geometry upload"))) return r;
     c->have_geom = true;
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_hybrid(flou_ctx* c, int32_t fvflux, int32_t fvflux_avg, double fvflux_intensity, double blend) {
+    if (!c) return FLOU_ERR_ARG;
+    if (c->cfg.volume_op != FLOU_OP_HYBRID) return fail(c, FLOU_ERR_STATE, "the context's operator is not hybrid");
+    if (fvflux < 0 || fvflux > 6 || (fvflux_avg != FLOU_NF_STD_AVERAGE && fvflux_avg != FLOU_NF_CHANDRASHEKAR))
+        return fail(c, FLOU_ERR_ARG, "invalid subcell flux %d / %d", fvflux, fvflux_avg);
+    if (!std::isfinite(fvflux_intensity) || !std::isfinite(blend) || blend < 0.0)
+        return fail(c, FLOU_ERR_ARG, "invalid intensity or blending constant");
+    c->fvflux = fvflux;
+    c->fvavg = fvflux_avg;
+    c->fvintensity = fvflux_intensity;
+    c->blend = blend;
+    c->have_hybrid = true;
     drop_graph(c);
     return FLOU_OK;
 }

@@ -41,6 +41,11 @@ struct flou_ctx {
     double* d_Qh = nullptr;         // staging for host-pointer calls
     double* d_dQh = nullptr;
     double* d_c = nullptr;          // optional per-element LxF dissipation scale
+    // HybridDivOperator: 1D weights, subcell FV flux, blending constant
+    double* d_omega1 = nullptr;
+    bool have_hybrid = false;
+    int fvflux = 0, fvavg = 0;
+    double fvintensity = 1.0, blend = 0.0;
     // general (curvilinear / unstructured) geometry: the CURV kernels
     bool curv = false;
     bool any_orient = false;        // some face has a non-zero master2slave orientation

@@ -63,6 +63,10 @@ struct ElemParams {
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
+    // HybridDivOperator (OpDivergence.jl:442-604): subcell FV flux and blending
+    const double* omega1;        // [n] 1D quadrature weights
+    int32_t fvflux, fvavg;
+    double fvintensity, blend;
     // general geometry (CURV kernels)
     const double* invJn;         // [ndofs] 1/J of every node
     const double* Jan;           // [DIM*DIM][ndofs]: metric Ja[k, d] at q = k + d*DIM (columns: dual basis)
@@ -857,7 +861,12 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     F[DIM + 1] = m * h;
 }
 
-template <int DIM, int N, int EQ, int TP, bool LGL, int TB = 256, bool CURV = false>
+// HYB: the hybrid (telescopic) form of HybridDivOperator on LGL nodes (OpDivergence.jl:553-604):
+// the split-form node sums give the high-order subcell fluxes by F̄_{p+1} = F̄_p + ω_p Σ_j D♯_pj F♯_pj
+// (F̄ = 0 at both element ends; algebraically the reference's Σ_{l<p<=k} 2 ω_l D_lk F♯(l,k)), each
+// blended with the subcell FV flux by δ = max((√(b²+c) - b)/√(b²+c), 1/2), b = ΔW·(F̄ - F̄_FV),
+// and dQ_p += (F̄_p - F̄_{p+1})/ω_p.  Cartesian geometry (subcell frames along the axes).
+template <int DIM, int N, int EQ, int TP, bool LGL, int TB = 256, bool CURV = false, bool HYB = false>
 __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* smem) {
     using S = Shape<DIM, N, TB>;
     using Lay = SplitLayout<DIM, EQ, TP>;
@@ -869,7 +878,10 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     double* sprim = sops + S::NOPS;                 // [Lay::NARR][NN]
     double* spair = sprim + Lay::NARR * NN;         // [NV][NPT]
     double* sJa = spair + NV * NPT;                 // CURV: [DIM][NN] metric column of the direction
-    uint8_t* stab = (uint8_t*)(sJa + (CURV ? DIM * NN : 0));   // pair table: a, b
+    double* sW = sJa + (CURV ? DIM * NN : 0);       // HYB: [NV][NN] entropy variables
+    double* sH = sW + (HYB ? NV * NN : 0);          // HYB: [NV][NN] ω_p Ja Σ_j D♯ F♯ of each node
+    double* sFb = sH + (HYB ? NV * NN : 0);         // HYB: [NV][NN] blended flux at the node's left interface
+    uint8_t* stab = (uint8_t*)(sFb + (HYB ? NV * NN : 0));   // pair table: a, b
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
     if (tid == 0) {
@@ -899,6 +911,14 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             }
             p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
             if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
+            if constexpr (HYB) {   // vars_cons2entropy, FlouCommon/Euler.jl:273-307
+                double ip = 1.0 / p;
+                double sv = log(p) - g * log(q[0]);
+                sW[tid] = (g - sv) / (g - 1.0) - ke * ip * 0.5;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) sW[(1 + k) * NN + tid] = q[1 + k] * ip;
+                sW[(DIM + 1) * NN + tid] = -q[0] * ip;
+            }
             if (TP == FLOU_TP_CHANDRASHEKAR) {
                 sprim[tid] = 0.5 * q[0];
 #pragma unroll
@@ -1084,18 +1104,84 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 }
             }
             double Ja = CURV ? 1.0 : P.elem_Ja[e * DIM + dir];   // CURV: the metric is in the fluxes
+            if constexpr (HYB) {
+                double w = P.omega1[pos] * Ja;
 #pragma unroll
-            for (int k = 0; k < NV; ++k) dq[k] = fma(-Ja, acc[k], dq[k]);
+                for (int k = 0; k < NV; ++k) sH[k * NN + tid] = w * acc[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) dq[k] = fma(-Ja, acc[k], dq[k]);
+            }
+        }
+        if constexpr (HYB && EULER) {
+            __syncthreads();
+            if (active) {
+                int pos, line;
+                tp_coords<DIM>(N, i, dir, pos, line);
+                if (pos > 0) {   // the subcell interface between positions pos-1 and pos
+                    const int il = el * NPE + tp_node<DIM>(N, dir, line, pos - 1);
+                    double Fh[NV];
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) Fh[k] = 0.0;
+                    for (int r = 0; r < pos; ++r) {
+                        int j = el * NPE + tp_node<DIM>(N, dir, line, r);
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) Fh[k] += sH[k * NN + j];
+                    }
+                    // FV flux in the frame of the positive axis, times the subcell surface
+                    // Jacobian (PhysicalRegions.jl:68-148: Ja_dd of the Cartesian element)
+                    FrameAxes A = frame_axes<DIM>(2 * dir + 1);
+                    double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV];
+                    const int64_t gl = (int64_t)e * NPE + (il - el * NPE);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) {
+                        ql[k] = P.Q[k * P.ndofs + gl];
+                        qr[k] = q[k];
+                    }
+                    a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+#pragma unroll
+                    for (int r = 0; r < DIM; ++r) {
+                        a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
+                        b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
+                    }
+                    euler_face_flux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                    const double Js = P.elem_Ja[e * DIM + dir];
+                    Fv[0] = Fr[0] * Js;
+                    Fv[DIM + 1] = Fr[DIM + 1] * Js;
+#pragma unroll
+                    for (int r = 0; r < DIM; ++r) Fv[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]) * Js;
+                    double bb = 0.0;
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + tid] - sW[k * NN + il], Fh[k] - Fv[k], bb);
+                    double dl = sqrt(fma(bb, bb, P.blend));
+                    dl = fmax((dl - bb) / dl, 0.5);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = fma(dl, Fh[k] - Fv[k], Fv[k]);
+                }
+            }
+            __syncthreads();
+            if (active) {
+                int pos, line;
+                tp_coords<DIM>(N, i, dir, pos, line);
+                double iw = 1.0 / P.omega1[pos];
+                int jr = (pos < N - 1) ? el * NPE + tp_node<DIM>(N, dir, line, pos + 1) : -1;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    double fl = pos > 0 ? sFb[k * NN + tid] : 0.0;
+                    double fr = jr >= 0 ? sFb[k * NN + jr] : 0.0;
+                    dq[k] += (fl - fr) * iw;
+                }
+            }
         }
         __syncthreads();
     }
     if (active) surface_and_update<DIM, N, NV, LGL, CURV>(P, sops, e, i, q, dq);
 }
 
-template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false>
+template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false, bool HYB = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
     extern __shared__ double smem[];
-    split_tile<DIM, N, EQ, TP, LGL, 256, CURV>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
+    split_tile<DIM, N, EQ, TP, LGL, 256, CURV, HYB>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
 template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256, bool CURV = false>
@@ -1105,7 +1191,8 @@ constexpr size_t elem_smem_bytes() {
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
     constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;
     constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
-    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT + (CURV ? DIM * S::NN : 0)) + 2 * (S::NPAIR + 1);
+    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT + (CURV ? DIM * S::NN : 0) +
+                             (VOL == FLOU_OP_HYBRID ? 3 * NV * S::NN : 0)) + 2 * (S::NPAIR + 1);
 }
 
 // Launch one instantiation; the dynamic shared-memory opt-in is set once per kernel.
@@ -1117,7 +1204,8 @@ cudaError_t launch_elem_one(const ElemParams& P, cudaStream_t s, bool prepare) {
     static bool attr_set = false;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
     auto k = (VOL == FLOU_OP_STRONG) ? (void (*)(ElemParams))elem_strong_kernel<DIM, N, EQ, LGL, CURV>
-                                     : (void (*)(ElemParams))elem_split_kernel<DIM, N, EQ, TP, LGL, CURV>;
+                                     : (void (*)(ElemParams))elem_split_kernel<DIM, N, EQ, TP, LGL, CURV,
+                                                                               VOL == FLOU_OP_HYBRID>;
     if (!attr_set) {
         cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;
@@ -1130,35 +1218,57 @@ cudaError_t launch_elem_one(const ElemParams& P, cudaStream_t s, bool prepare) {
 
 // All volume variants of one (dim, N, equation): strong (LGL or general basis) and split
 // (LGL only, one kernel per two-point flux).
-template <int DIM, int N, int EQ>
+// VSEL >= 0 instantiates only that volume operator (one translation unit per operator).
+template <int DIM, int N, int EQ, int VSEL = -1>
 cudaError_t launch_elem_n(int vol, int tp, bool lgl, const ElemParams& P, cudaStream_t s, bool prep) {
-    if (vol == FLOU_OP_STRONG)
-        return lgl ? launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, true>(P, s, prep)
-                   : launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, false>(P, s, prep);
-    if (!lgl) return cudaErrorInvalidValue;
-    if (EQ != FLOU_EQ_EULER)
-        return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true>(P, s, prep);
-    switch (tp) {
-        case FLOU_TP_STD_AVERAGE:
-            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true>(P, s, prep);
-        case FLOU_TP_CHANDRASHEKAR:
-            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, true>(P, s, prep);
-        case FLOU_TP_KENNEDY_GRUBER:
-            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_KENNEDY_GRUBER, true>(P, s, prep);
-        default: return cudaErrorInvalidValue;
+    if (VSEL >= 0 && vol != VSEL) return cudaErrorInvalidValue;
+    if (vol == FLOU_OP_STRONG) {
+        if constexpr (VSEL < 0 || VSEL == FLOU_OP_STRONG)
+            return lgl ? launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, true>(P, s, prep)
+                       : launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, false>(P, s, prep);
+        return cudaErrorInvalidValue;
     }
+    if (!lgl) return cudaErrorInvalidValue;
+    if (vol == FLOU_OP_HYBRID) {
+        if constexpr (EQ == FLOU_EQ_EULER && (VSEL < 0 || VSEL == FLOU_OP_HYBRID)) {
+            switch (tp) {
+                case FLOU_TP_STD_AVERAGE:
+                    return launch_elem_one<DIM, N, EQ, FLOU_OP_HYBRID, FLOU_TP_STD_AVERAGE, true>(P, s, prep);
+                case FLOU_TP_CHANDRASHEKAR:
+                    return launch_elem_one<DIM, N, EQ, FLOU_OP_HYBRID, FLOU_TP_CHANDRASHEKAR, true>(P, s, prep);
+                case FLOU_TP_KENNEDY_GRUBER:
+                    return launch_elem_one<DIM, N, EQ, FLOU_OP_HYBRID, FLOU_TP_KENNEDY_GRUBER, true>(P, s, prep);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        return cudaErrorInvalidValue;
+    }
+    if constexpr (VSEL < 0 || VSEL == FLOU_OP_SPLIT) {
+        if (EQ != FLOU_EQ_EULER)
+            return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true>(P, s, prep);
+        switch (tp) {
+            case FLOU_TP_STD_AVERAGE:
+                return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true>(P, s, prep);
+            case FLOU_TP_CHANDRASHEKAR:
+                return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, true>(P, s, prep);
+            case FLOU_TP_KENNEDY_GRUBER:
+                return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_KENNEDY_GRUBER, true>(P, s, prep);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    return cudaErrorInvalidValue;
 }
 
-template <int DIM, int EQ>
+template <int DIM, int EQ, int VSEL = -1>
 cudaError_t launch_elem_dim(int n, int vol, int tp, bool lgl, const ElemParams& P, cudaStream_t s, bool prep) {
     switch (n) {
-        case 2: return launch_elem_n<DIM, 2, EQ>(vol, tp, lgl, P, s, prep);
-        case 3: return launch_elem_n<DIM, 3, EQ>(vol, tp, lgl, P, s, prep);
-        case 4: return launch_elem_n<DIM, 4, EQ>(vol, tp, lgl, P, s, prep);
-        case 5: return launch_elem_n<DIM, 5, EQ>(vol, tp, lgl, P, s, prep);
-        case 6: return launch_elem_n<DIM, 6, EQ>(vol, tp, lgl, P, s, prep);
-        case 7: return launch_elem_n<DIM, 7, EQ>(vol, tp, lgl, P, s, prep);
-        case 8: return launch_elem_n<DIM, 8, EQ>(vol, tp, lgl, P, s, prep);
+        case 2: return launch_elem_n<DIM, 2, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 3: return launch_elem_n<DIM, 3, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 4: return launch_elem_n<DIM, 4, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 5: return launch_elem_n<DIM, 5, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 6: return launch_elem_n<DIM, 6, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 7: return launch_elem_n<DIM, 7, EQ, VSEL>(vol, tp, lgl, P, s, prep);
+        case 8: return launch_elem_n<DIM, 8, EQ, VSEL>(vol, tp, lgl, P, s, prep);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -1208,6 +1318,7 @@ cudaError_t launch_elem_euler1d(const ElemLaunch& L, const ElemParams& P, cudaSt
 cudaError_t launch_elem_euler2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler3d_strong(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_euler3d_hybrid(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_scalar(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s);
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);

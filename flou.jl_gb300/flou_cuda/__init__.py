@@ -7,7 +7,7 @@ EquationConfig, rhs!, timeintegrate, get_max_dt); all arithmetic runs in libflou
 from ._lib import DomainError, FlouError, load
 from .disc import Context, DofHandler, EquationConfig, MultielementDisc, get_max_dt, rhs_
 from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, EulerEquation, EulerInflowBC,
-                        EulerOutflowBC, EulerSlipBC, HLL, HLLC, KennedyGruberAverage, LinearAdvection, LxF,
+                        EulerOutflowBC, EulerSlipBC, HLL, HLLC, HybridDivOperator, KennedyGruberAverage, LinearAdvection, LxF,
                         MatrixDissipation, OutflowBC, ScalarDissipation, SplitDivOperator, StdAverage,
                         StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs

@@ -19,7 +19,7 @@ FLOU_ERR_UNSUPPORTED = 6
 FLOU_ERR_STATE = 7
 
 EQ_LINEAR_ADVECTION, EQ_BURGERS, EQ_EULER = 0, 1, 2
-OP_STRONG, OP_SPLIT = 0, 1
+OP_STRONG, OP_SPLIT, OP_HYBRID = 0, 1, 2
 TP_STD_AVERAGE, TP_CHANDRASHEKAR, TP_KENNEDY_GRUBER = 0, 1, 2
 NF_STD_AVERAGE, NF_LXF, NF_CHANDRASHEKAR, NF_HLL, NF_HLLC = 0, 1, 2, 3, 4
 NF_SCALAR_DISSIPATION, NF_MATRIX_DISSIPATION = 5, 6
@@ -100,6 +100,7 @@ PROTOTYPES = {
                             ctypes.c_char_p, ctypes.c_int32],
     "flou_rhs_vjp": [_P, _P, _P, _P, _P],
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
+    "flou_set_hybrid": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double],
     "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
     "flou_limit": [_P, _P, ctypes.c_int32],
     "flou_monitor": [_P, _P, ctypes.c_int32, _D, ctypes.c_int32],

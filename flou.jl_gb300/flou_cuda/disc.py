@@ -117,7 +117,7 @@ class MultielementDisc:
         for k in range(3):
             cfg.advection[k] = float(adv[k]) if k < len(adv) else 0.0
         cfg.volume_op = op.code
-        cfg.twopoint_flux = op.tpflux.tpcode if op.code == L.OP_SPLIT else L.TP_STD_AVERAGE
+        cfg.twopoint_flux = op.tpflux.tpcode if op.code in (L.OP_SPLIT, L.OP_HYBRID) else L.TP_STD_AVERAGE
         nf = op.numflux
         if nf.code is None:
             raise ValueError("%s is not a numerical flux" % type(nf).__name__)
@@ -147,7 +147,18 @@ class MultielementDisc:
             bdface_index=np.ascontiguousarray(m.bdface_index, dtype=np.int32),
             bc_kinds=kinds, bc_states=np.ascontiguousarray(states),
             J=self.J, Ja=np.ascontiguousarray(self.Ja), frames=np.ascontiguousarray(self.frames), faceJ=self.faceJ,
+            hybrid=self._hybrid_params(),
         )
+
+    def _hybrid_params(self):
+        """(fvflux, its central flux, intensity, blend) of a HybridDivOperator, else None."""
+        op = self.operator
+        if getattr(op, "code", None) != L.OP_HYBRID:
+            return None
+        fv = op.fvflux
+        avg = getattr(fv, "avg", StdAverage())
+        return (fv.code, L.NF_CHANDRASHEKAR if isinstance(avg, ChandrasekharAverage) else L.NF_STD_AVERAGE,
+                float(getattr(fv, "intensity", 1.0)), op.blend)
 
     @property
     def ctx(self):
@@ -196,6 +207,9 @@ class Context:
                                   i32(a["bdface_index"])), h)
         L.check(lib.flou_set_bcs(h, len(a["bc_kinds"]), i32(a["bc_kinds"]), d(a["bc_states"])), h)
         L.check(lib.flou_set_geometry(h, d(a["J"]), d(a["Ja"]), d(a["frames"]), d(a["faceJ"])), h)
+        if a.get("hybrid") is not None:
+            fv, fvavg, fvint, blend = a["hybrid"]
+            L.check(lib.flou_set_hybrid(h, int(fv), int(fvavg), float(fvint), float(blend)), h)
         nd = ctypes.c_int64()
         nv = ctypes.c_int32()
         L.check(lib.flou_sizes(h, ctypes.byref(nd), ctypes.byref(nv), None, None), h)

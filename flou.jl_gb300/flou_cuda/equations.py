@@ -158,6 +158,26 @@ class StrongDivOperator:
         self.tpflux = StdAverage()
 
 
+class HybridDivOperator:
+    """HybridDivOperator([tpflux=numflux.avg, [fvflux=numflux]], numflux, blend)
+    (OpDivergence.jl:442-466): the split form in telescopic (subcell) form, blended with the
+    subcell finite-volume flux `fvflux` by the entropy indicator with constant `blend`."""
+
+    def __init__(self, *args):
+        if len(args) == 2:
+            self.numflux, self.blend = args
+            self.tpflux, self.fvflux = self.numflux.avg, self.numflux
+        elif len(args) == 3:
+            self.tpflux, self.numflux, self.blend = args
+            self.fvflux = self.numflux
+        elif len(args) == 4:
+            self.tpflux, self.fvflux, self.numflux, self.blend = args
+        else:
+            raise ValueError("HybridDivOperator([tpflux, [fvflux]], numflux, blend)")
+        self.blend = float(self.blend)
+        self.code = L.OP_HYBRID
+
+
 class SplitDivOperator:
     """SplitDivOperator([tpflux=numflux.avg], numflux)."""
 

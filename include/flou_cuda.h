@@ -48,6 +48,10 @@ extern "C" {
  * SplitDivOperator (OpDivergence.jl:184-282, LGL nodes only). */
 #define FLOU_OP_STRONG 0
 #define FLOU_OP_SPLIT 1
+/* HybridDivOperator (OpDivergence.jl:442-604): the split form in telescopic (subcell) form,
+ * blended with a subcell finite-volume flux; LGL nodes, Cartesian geometry, Euler.  The FV flux
+ * and the blending constant are set with flou_set_hybrid. */
+#define FLOU_OP_HYBRID 2
 
 /* Two-point volume fluxes of the split form: StdAverage (Euler.jl:385-472),
  * ChandrasekharAverage (Euler.jl:474-536), Kennedy-Gruber (no Flou counterpart). */
@@ -140,6 +144,11 @@ int32_t flou_set_bcs(flou_ctx* ctx, int32_t nbcs, const int32_t* kinds, const do
  * surface Jacobians <= 0. */
 int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, const double* frames,
                           const double* face_J);
+
+/* The hybrid operator's subcell finite-volume flux (HybridDivOperator's fvflux: FLOU_NF_* with
+ * its central flux and intensity) and blending constant c (δ = max((√(b²+c) - b)/√(b²+c), 1/2),
+ * OpDivergence.jl:777-801).  Required before the first residual of a FLOU_OP_HYBRID context. */
+int32_t flou_set_hybrid(flou_ctx* ctx, int32_t fvflux, int32_t fvflux_avg, double fvflux_intensity, double blend);
 
 /* ---- residual and stepping ------------------------------------------------------------- */
 /* FlouCommon.rhs!(dQ, Q, p::EquationConfig{<:MultielementDisc,<:HyperbolicEquation}, t)

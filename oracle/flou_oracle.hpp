@@ -441,7 +441,7 @@ inline StdOps std_operators(int n, bool lobatto) {
 // Equations and fluxes
 // ============================================================================
 enum EqKind { EQ_ADVECTION = 0, EQ_BURGERS = 1, EQ_EULER = 2 };
-enum VolOp { OP_STRONG = 0, OP_SPLIT = 1 };
+enum VolOp { OP_STRONG = 0, OP_SPLIT = 1, OP_HYBRID = 2 };
 enum TwoPoint { TP_STDAVG = 0, TP_CHANDRASHEKAR = 1, TP_KENNEDY_GRUBER = 2 };
 enum NumFlux {
     NF_STDAVG = 0, NF_LXF = 1, NF_CHANDRASHEKAR = 2, NF_HLL = 3, NF_HLLC = 4,
@@ -455,6 +455,9 @@ struct Config {
     double a[3] = {0, 0, 0};
     int volop = OP_STRONG, tpflux = TP_STDAVG, numflux = NF_LXF, lxf_avg = NF_STDAVG;
     double intensity = 1.0;
+    // HybridDivOperator (OpDivergence.jl:442-466): subcell FV flux and blending constant
+    int fvflux = NF_LXF, fvavg = NF_STDAVG;
+    double fvintensity = 1.0, blend = 0.0;
 };
 
 template <class T> using Vec = std::array<T, 5>;
@@ -893,6 +896,7 @@ struct Disc {
     int n = 0, npe = 0, nfd = 0, nelem = 0, nfaces = 0;
     // operators (n x n column-major)
     std::vector<double> Ds, Dsharp, ll, lr, dgl, dgr;
+    std::vector<double> D, omega1d;       // derivative matrix, 1D weights (HybridDivOperator)
     // connectivity (1-based, like the reference)
     std::vector<int> faceinds, facepos;   // nelem * 2dim
     std::vector<int> eleminds, elempos;   // nfaces * 2
@@ -1026,7 +1030,64 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                 Ft[i * dim + d] = r;
             }
         }
-        if (c.volop == OP_STRONG) {
+        if (c.volop == OP_HYBRID) {
+            // _vol_hybrid_tensorproduct!, OpDivergence.jl:553-604, with the Cartesian subgrid of
+            // PhysicalRegions.jl:68-148 (frames along the positive axes, Js the face Jacobian)
+            using std::sqrt; using std::max;
+            std::vector<Vec<T>> W(npe);
+            for (int i = 0; i < npe; ++i) W[i] = cons2entropy(getv(Q, nd, base + i, nv), dim, c.gamma);
+            Config fv = c;
+            fv.lxf_avg = c.fvavg;
+            std::vector<Vec<T>> Fb(n + 1);
+            for (int dir = 0; dir < dim; ++dir) {
+                Frame fr{};
+                if (dim == 1) { fr.n[0] = 1; }
+                else if (dim == 2) {
+                    if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; } else { fr.n[1] = 1; fr.t[0] = -1; }
+                } else {
+                    if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; fr.b[2] = 1; }
+                    else if (dir == 1) { fr.n[1] = 1; fr.t[2] = 1; fr.b[0] = 1; }
+                    else { fr.n[2] = 1; fr.t[0] = 1; fr.b[1] = 1; }
+                }
+                double Js = g.Ja[base * dim * dim + dir + dir * dim];
+                for (int line = 0; line < nfd; ++line) {
+                    for (int ii = 0; ii <= n; ++ii) Fb[ii] = Vec<T>{};
+                    for (int ii = 1; ii < n; ++ii) {
+                        for (int ik = ii; ik < n; ++ik) {
+                            int k = tp_node(dim, n, dir, line, ik);
+                            for (int il = 0; il < ii; ++il) {
+                                int l = tp_node(dim, n, dir, line, il);
+                                Vec<T> Ft = twopointflux(getv(Q, nd, base + l, nv), getv(Q, nd, base + k, nv),
+                                                         &g.Ja[(base + l) * dim * dim + dir * dim],
+                                                         &g.Ja[(base + k) * dim * dim + dir * dim], c);
+                                double coef = (2.0 * g.omega1d[il]) * g.D[il + ik * n];
+                                for (int q = 0; q < nv; ++q) Fb[ii][q] = Fb[ii][q] + coef * Ft[q];
+                            }
+                        }
+                        int i = tp_node(dim, n, dir, line, ii), il = tp_node(dim, n, dir, line, ii - 1);
+                        Vec<T> Qln = rotate2face(getv(Q, nd, base + il, nv), fr, c);
+                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + i, nv), fr, c);
+                        Vec<T> Fn = numericalflux(Qln, Qrn, fr.n, fv, c.fvflux, T(c.fvintensity));
+                        Vec<T> Fv = rotate2phys(Fn, fr, c);
+                        for (int q = 0; q < nv; ++q) Fv[q] = Fv[q] * Js;
+                        T bb = T(0.0);
+                        for (int q = 0; q < nv; ++q) bb = bb + (W[i][q] - W[il][q]) * (Fb[ii][q] - Fv[q]);
+                        // _hybrid_compute_delta, OpDivergence.jl:777-801 (Fisher's, limited at 0.5)
+                        T dl = sqrt(bb * bb + c.blend);
+                        dl = (dl - bb) / dl;
+                        dl = max(dl, T(0.5));
+                        for (int q = 0; q < nv; ++q) Fb[ii][q] = (1.0 - dl) * Fv[q] + dl * Fb[ii][q];
+                    }
+                    for (int ii = 0; ii < n; ++ii) {
+                        int i = tp_node(dim, n, dir, line, ii);
+                        for (int q = 0; q < nv; ++q) {
+                            T& y = dQ[q * nd + base + i];
+                            y = y + (Fb[ii][q] - Fb[ii + 1][q]) / g.omega1d[ii];
+                        }
+                    }
+                }
+            }
+        } else if (c.volop == OP_STRONG) {
             for (int dir = 0; dir < dim; ++dir)
                 for (int line = 0; line < nfd; ++line)
                     for (int col = 0; col < n; ++col) {   // mul!(y, Ds, x, -1, 1): y[i] += Ds[i,k]*(-x[k])

@@ -301,6 +301,21 @@ int oracle_ssprk3(void* hp, double* Q, double dt, int nsteps, double t0) {
     return 0;
 }
 
+// HybridDivOperator parameters: the subcell FV flux (kind, its central flux, intensity), the
+// blending constant, the 1D weights and the derivative matrix (n x n, column-major).
+void oracle_set_hybrid(void* hp, int fvflux, int fvavg, double fvintensity, double blend, const double* omega1d,
+                       const double* D) {
+    Handle* h = (Handle*)hp;
+    Config& c = h->g.cfg;
+    c.fvflux = fvflux;
+    c.fvavg = fvavg;
+    c.fvintensity = fvintensity;
+    c.blend = blend;
+    int n = h->g.n;
+    h->g.omega1d.assign(omega1d, omega1d + n);
+    h->g.D.assign(D, D + (size_t)n * n);
+}
+
 void oracle_limit(void* hp, double* Q, double minval, const double* omega_tp) {
     Handle* h = (Handle*)hp;
     std::vector<double> w(omega_tp, omega_tp + h->g.npe);

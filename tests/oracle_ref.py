@@ -38,6 +38,8 @@ def lib():
         _lib.oracle_max_dt.restype = ctypes.c_double
         _lib.oracle_max_dt.argtypes = [ctypes.c_void_p, D, ctypes.c_double, D]
         _lib.oracle_limit.argtypes = [ctypes.c_void_p, D, ctypes.c_double, D]
+        _lib.oracle_set_hybrid.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, D, D]
         _lib.oracle_monitor.restype = ctypes.c_double
         _lib.oracle_monitor.argtypes = [ctypes.c_void_p, D, ctypes.c_int, D]
         _lib.oracle_ssprk3_limited.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -125,6 +127,12 @@ class Disc:
             _i(a["eleminds"]), _i(a["elempos"]), a["orientation"].ctypes.data_as(U8), _i(a["bdface_index"]),
             len(a["bc_kinds"]), _i(a["bc_kinds"]), _d(a["bc_states"]), _d(a["J"]), _d(a["Ja"]), _d(a["frames"]),
             _d(a["faceJ"]))
+        if a.get("hybrid") is not None:
+            fv, fvavg, fvint, blend = a["hybrid"]
+            om = np.ascontiguousarray(a["omega"], dtype=np.float64)
+            Dm = np.asfortranarray(a["D"], dtype=np.float64)
+            self._keep = (adv, a, om, Dm)
+            L.oracle_set_hybrid(self.h, int(fv), int(fvavg), float(fvint), float(blend), _d(om), _d(Dm))
 
     def __del__(self):
         if getattr(self, "h", None):

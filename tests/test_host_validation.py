@@ -10,8 +10,7 @@ from flou_cuda import _lib as L
 
 
 def _mesh_args(disc):
-    a = disc.abi_arrays()
-    return a
+    return {k: v for k, v in disc.abi_arrays().items() if v is not None}
 
 
 def _check_mesh(dim, a):

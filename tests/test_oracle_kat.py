@@ -236,3 +236,27 @@ def test_monitors_and_limited_steps_are_consistent():
     dt = 0.2 * o.max_dt(Q, 1.0, disc.std.omega)
     Qs = o.ssprk3_limited(Q, dt, 4, 0.05, disc.std.omega)
     assert Qs[:, 0].min() > 0.0
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_hybrid_operator_properties(dim):
+    """HybridDivOperator (OpDivergence.jl:442-604): with δ -> 1 (huge blending constant) the
+    telescopic subcell form is the split form (Fisher & Carpenter's equivalence); with blending it
+    stays conservative and freestream-preserving."""
+    eq = F.EulerEquation(dim, 1.4)
+    nf = F.LxF(F.ChandrasekharAverage(), 1.0)
+    hy = build(dim, 4, (3,) * dim, eq, F.HybridDivOperator(F.ChandrasekharAverage(), nf, 1e30))
+    sp = build(dim, 4, (3,) * dim, eq, F.SplitDivOperator(F.ChandrasekharAverage(), nf))
+    Q = smooth_euler_state(hy, seed=3, amp=0.2)
+    Rh, Rs = oracle_for(hy).rhs(Q), oracle_for(sp).rhs(Q)
+    assert np.max(np.abs(Rh - Rs)) < 1e-13 * np.max(np.abs(Rs))
+    bl = build(dim, 4, (3,) * dim, eq, F.HybridDivOperator(F.ChandrasekharAverage(), nf, 1e-3))
+    o = oracle_for(bl)
+    R = o.rhs(Q)
+    assert np.max(np.abs(R - Rs)) > 1e-3 * np.max(np.abs(Rs))   # the blending acts
+    w = np.tile(bl.std.omega, bl.mesh.nelements) * bl.J
+    for v in range(dim + 2):
+        assert abs(w @ R[:, v]) < 1e-12 * np.sum(w * np.abs(R[:, v]))
+    P = np.zeros((bl.ndofs, dim + 2))
+    P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.3, 0.4, 2.0
+    assert np.max(np.abs(o.rhs(np.asfortranarray(eq.vars_prim2cons(P))))) < 1e-12
