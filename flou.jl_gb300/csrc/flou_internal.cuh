@@ -63,7 +63,7 @@ struct ElemParams {
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
-    // HybridDivOperator (OpDivergence.jl:442-604): subcell FV flux and blending
+    // HybridDivOperator (OpDivergence.jl:439-612, 781-801): subcell FV flux and blending
     const double* omega1;        // [n] 1D quadrature weights
     int32_t fvflux, fvavg;
     double fvintensity, blend;

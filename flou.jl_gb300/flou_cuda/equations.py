@@ -160,7 +160,7 @@ class StrongDivOperator:
 
 class HybridDivOperator:
     """HybridDivOperator([tpflux=numflux.avg, [fvflux=numflux]], numflux, blend)
-    (OpDivergence.jl:442-466): the split form in telescopic (subcell) form, blended with the
+    (OpDivergence.jl:439-472): the split form in telescopic (subcell) form, blended with the
     subcell finite-volume flux `fvflux` by the entropy indicator with constant `blend`."""
 
     def __init__(self, *args):

@@ -68,8 +68,8 @@ function flou_config(disc, equation)
     op = disc.operators[1]
     nf = op.numflux
     adv = equation isa LinearAdvection ? (Tuple(equation.a)..., zeros(3 - length(equation.a))...) : (0.0, 0.0, 0.0)
-    vol = op isa SplitDivOperator ? Int32(1) : Int32(0)
-    tp = op isa SplitDivOperator ? tpcode(op.tpflux) : Int32(0)
+    vol = op isa HybridDivOperator ? Int32(2) : op isa SplitDivOperator ? Int32(1) : Int32(0)
+    tp = (op isa SplitDivOperator || op isa HybridDivOperator) ? tpcode(op.tpflux) : Int32(0)
     avg = has_avg(nf) ? (nf.avg isa ChandrasekharAverage ? Int32(2) : Int32(0)) : Int32(0)
     inten = has_avg(nf) ? Float64(nf.intensity) : 1.0
     gamma = equation isa EulerEquation ? Float64(equation.γ) : 1.4
@@ -104,6 +104,14 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
     GC.@preserve D Ds Dsh ω ll lr gl gr check(ccall((:flou_set_operators, libflou), Int32,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
          Ptr{Float64}, Ptr{Float64}), ctx, D, Ds, Dsh, ω, ll, lr, gl, gr), ctx)
+    op = disc.operators[1]
+    if op isa HybridDivOperator   # subcell FV flux and blending constant (OpDivergence.jl:452-470)
+        fv = op.fvflux
+        fvavg = has_avg(fv) ? (fv.avg isa ChandrasekharAverage ? Int32(2) : Int32(0)) : Int32(0)
+        fvint = has_avg(fv) ? Float64(fv.intensity) : 1.0
+        check(ccall((:flou_set_hybrid, libflou), Int32, (Ptr{Cvoid}, Int32, Int32, Float64, Float64),
+                    ctx, nfcode(fv), fvavg, fvint, Float64(op.blend)), ctx)
+    end
     mesh = disc.mesh
     ne, nf = nelements(mesh), nfaces(mesh)
     faceinds = Int32.(mesh.elements.faceinds)

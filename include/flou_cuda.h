@@ -48,7 +48,7 @@ extern "C" {
  * SplitDivOperator (OpDivergence.jl:184-282, LGL nodes only). */
 #define FLOU_OP_STRONG 0
 #define FLOU_OP_SPLIT 1
-/* HybridDivOperator (OpDivergence.jl:442-604): the split form in telescopic (subcell) form,
+/* HybridDivOperator (OpDivergence.jl:439-612, 781-801): the split form in telescopic (subcell) form,
  * blended with a subcell finite-volume flux; LGL nodes, Cartesian geometry, Euler.  The FV flux
  * and the blending constant are set with flou_set_hybrid. */
 #define FLOU_OP_HYBRID 2

@@ -455,7 +455,7 @@ struct Config {
     double a[3] = {0, 0, 0};
     int volop = OP_STRONG, tpflux = TP_STDAVG, numflux = NF_LXF, lxf_avg = NF_STDAVG;
     double intensity = 1.0;
-    // HybridDivOperator (OpDivergence.jl:442-466): subcell FV flux and blending constant
+    // HybridDivOperator (OpDivergence.jl:439-472): subcell FV flux and blending constant
     int fvflux = NF_LXF, fvavg = NF_STDAVG;
     double fvintensity = 1.0, blend = 0.0;
 };
