@@ -775,6 +775,8 @@ int adj_supported(flou_ctx* c) {
     if (!c->lgl) return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL)");
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
+    if (c->lsrk_s)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint steps with SSP-RK3 (flou_set_integrator 0)");
     if (c->curv)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers Cartesian geometry");
     for (int b = 0; b < c->nbcs; ++b)

@@ -334,8 +334,8 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
             delete b;
             return r;
         }
-        if (c->limiter || c->mon_mask || c->curv) {   // the persistent launch runs none of these
-            c->err = "the batched launch covers Cartesian geometry without limiter or monitors";
+        if (c->limiter || c->mon_mask || c->curv || c->lsrk_s) {   // the persistent launch runs none of these
+            c->err = "the batched launch covers Cartesian geometry, SSP-RK3, without limiter or monitors";
             delete b;
             return FLOU_ERR_UNSUPPORTED;
         }

@@ -127,6 +127,7 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.dt = dt;
     P.a0 = a0;
     P.a1 = a1;
+    P.aux = mode == 3 ? const_cast<double*>(Q0) : nullptr;   // the 2N register travels in Q0's slot
     P.gamma = c->cfg.gamma;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     P.status = c->d_status;
@@ -184,6 +185,22 @@ int rk3_step(flou_ctx* c, cudaStream_t s, double* Q, double dt) {
     if ((r = stage(c, s, c->d_U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;
     if ((r = ctx_limit(c, s, Q))) return r;
     return ctx_record_monitors(c, s, Q);
+}
+
+// One step of a 2N-storage Runge-Kutta method (Williamson 1980; OrdinaryDiffEq's LowStorageRK2N
+// with williamson_condition = false, the ORK256 of test/tests.jl:19): every stage is one residual
+// whose element epilogue updates k = A_i k + dt L(u) in d_U and u = u + B_i k in place.
+int lsrk_step(flou_ctx* c, cudaStream_t s, double* Q, double dt) {
+    int r;
+    for (int st = 0; st < c->lsrk_s; ++st) {
+        if ((r = stage(c, s, Q, c->d_U, Q, 3, dt, st == 0 ? 0.0 : c->lsrk_A[st], c->lsrk_B[st]))) return r;
+        if ((r = ctx_limit(c, s, Q))) return r;
+    }
+    return ctx_record_monitors(c, s, Q);
+}
+
+int step_once(flou_ctx* c, cudaStream_t s, double* Q, double dt) {
+    return c->lsrk_s ? lsrk_step(c, s, Q, dt) : rk3_step(c, s, Q, dt);
 }
 
 int check_status(flou_ctx* c) {
@@ -644,6 +661,28 @@ int32_t flou_set_hybrid(flou_ctx* c, int32_t fvflux, int32_t fvflux_avg, double 
     return FLOU_OK;
 }
 
+int32_t flou_set_integrator(flou_ctx* c, int32_t nstages, const double* A, const double* B) {
+    if (!c) return FLOU_ERR_ARG;
+    if (nstages == 0) {
+        c->lsrk_s = 0;
+        drop_graph(c);
+        return FLOU_OK;
+    }
+    if (nstages < 1 || nstages > FLOU_MAX_LSRK_STAGES || !A || !B)
+        return fail(c, FLOU_ERR_ARG, "a 2N-storage method takes 1..%d stages and its A and B coefficients",
+                    FLOU_MAX_LSRK_STAGES);
+    for (int i = 0; i < nstages; ++i)
+        if (!std::isfinite(B[i]) || (i > 0 && !std::isfinite(A[i])))
+            return fail(c, FLOU_ERR_ARG, "non-finite coefficient in stage %d", i + 1);
+    c->lsrk_s = nstages;
+    for (int i = 0; i < nstages; ++i) {
+        c->lsrk_A[i] = i ? A[i] : 0.0;
+        c->lsrk_B[i] = B[i];
+    }
+    drop_graph(c);
+    return FLOU_OK;
+}
+
 int32_t flou_set_dissipation(flou_ctx* c, const double* celem, int32_t ptr_kind) {
     if (!c) return FLOU_ERR_ARG;
     if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh must come before flou_set_dissipation");
@@ -716,7 +755,7 @@ int32_t flou_step_async(flou_ctx* c, double* Q, double dt, double t0, int32_t ns
         cudaError_t pe = launch_elem(L, elem_params(c, Qd, Qd, c->d_U, 1, dt, 0.0, 1.0), c->own_stream);
         if (pe != cudaSuccess) return cuda_fail(c, pe, "element kernel set-up");
         CK(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-        int rr = rk3_step(c, c->own_stream, Qd, dt);
+        int rr = step_once(c, c->own_stream, Qd, dt);
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(c->own_stream, &g);
         if (rr) { if (g) cudaGraphDestroy(g); return rr; }

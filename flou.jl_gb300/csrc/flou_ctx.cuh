@@ -67,6 +67,9 @@ struct flou_ctx {
     int32_t* d_moncount = nullptr;  // [0]: steps recorded, [1]: single-evaluation slot counter
     double* d_monpart = nullptr;    // block partial sums
     double* d_monval = nullptr;     // single evaluation [2]
+    // step method of flou_step: 0 stages = Shu-Osher SSP-RK3, else a 2N-storage method
+    int lsrk_s = 0;
+    double lsrk_A[FLOU_MAX_LSRK_STAGES], lsrk_B[FLOU_MAX_LSRK_STAGES];
     // graph cache for flou_step
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;

@@ -58,8 +58,10 @@ struct ElemParams {
     const double* ops;           // Ds[n*n], Dsharp[n*n], l_l[n], l_r[n], dg_l[n], dg_r[n]
     int64_t ndofs, nfdofs;
     int32_t nelem;
-    int32_t mode;                // 0: out = dQ; 1: out = U + dt dQ; 2: out = a0 U^n + a1 (U + dt dQ)
+    int32_t mode;                // 0: out = dQ; 1: out = U + dt dQ; 2: out = a0 U^n + a1 (U + dt dQ);
+                                 // 3: 2N-storage stage, k = a0 k + dt dQ (in aux), out = U + a1 k
     double dt, a0, a1;
+    double* aux;                 // mode 3: the 2N-storage register k, read and rewritten per node
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
@@ -661,7 +663,13 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         double o;
         if (P.mode == 0) o = r;
         else if (P.mode == 1) o = q[k] + P.dt * r;
-        else o = P.a0 * P.Q0[k * P.ndofs + g] + P.a1 * (q[k] + P.dt * r);
+        else if (P.mode == 2) o = P.a0 * P.Q0[k * P.ndofs + g] + P.a1 * (q[k] + P.dt * r);
+        else {
+            double kk = P.dt * r;
+            if (P.a0 != 0.0) kk = P.a0 * P.aux[k * P.ndofs + g] + kk;   // first stage: k is not read
+            P.aux[k * P.ndofs + g] = kk;
+            o = q[k] + P.a1 * kk;
+        }
         bad |= !isfinite(o);
         P.out[k * P.ndofs + g] = o;
     }

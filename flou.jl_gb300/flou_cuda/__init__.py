@@ -1,4 +1,4 @@
-"""flou_cuda: Flou.jl's DGSEM residual and SSP-RK3 stepping on GB300 (sm_103a, FP64).
+"""flou_cuda: Flou.jl's DGSEM residual and explicit Runge-Kutta stepping on GB300 (sm_103a, FP64).
 
 The Python side mirrors Flou's set-up API (CartesianMesh, apply_periodicBCs!, LagrangeBasis,
 DGSEMrec, StdSegment/StdQuad/StdHex, equations, fluxes, operators, MultielementDisc,
@@ -7,13 +7,14 @@ EquationConfig, rhs!, timeintegrate, get_max_dt); all arithmetic runs in libflou
 from ._lib import DomainError, FlouError, load
 from .disc import Context, DofHandler, EquationConfig, MultielementDisc, get_max_dt, rhs_
 from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, EulerEquation, EulerInflowBC,
-                        EulerOutflowBC, EulerSlipBC, HLL, HLLC, HybridDivOperator, KennedyGruberAverage, LinearAdvection, LxF,
+                        EulerOutflowBC, EulerSlipBC, GenericBC, HLL, HLLC, HybridDivOperator, KennedyGruberAverage, LinearAdvection, LxF,
                         MatrixDissipation, OutflowBC, ScalarDissipation, SplitDivOperator, StdAverage,
                         StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs
 from .unstructured import UnstructuredMesh, perturbed_box, read_gmsh, write_gmsh22
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
-from .timeint import SSPRK33, get_limiter_callback, get_monitor_callback, timeintegrate
+from .timeint import (ORK256, SSPRK33, CarpenterKennedy2N54, LowStorageRK2N, get_limiter_callback,
+                      get_monitor_callback, timeintegrate)
 from . import initial
 from .io import load_restart, save_restart, variablenames, write_vtu
 from .batch import Batch, adjoint_solve_batch

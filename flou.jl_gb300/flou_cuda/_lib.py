@@ -102,6 +102,7 @@ PROTOTYPES = {
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
     "flou_set_hybrid": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double],
     "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
+    "flou_set_integrator": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "flou_limit": [_P, _P, ctypes.c_int32],
     "flou_monitor": [_P, _P, ctypes.c_int32, _D, ctypes.c_int32],
     "flou_set_monitors": [_P, ctypes.c_int32, ctypes.c_int32],

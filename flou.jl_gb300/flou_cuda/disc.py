@@ -15,8 +15,8 @@ import numpy as np
 
 from . import _lib as L
 from .unstructured import UnstructuredMesh, unstructured_geometry
-from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, HLL, HLLC, LinearAdvection, LxF,
-                        SplitDivOperator, StdAverage, StrongDivOperator)
+from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, EulerInflowBC, GenericBC, HLL, HLLC,
+                        LinearAdvection, LxF, SplitDivOperator, StdAverage, StrongDivOperator)
 
 
 class DofHandler:
@@ -83,7 +83,7 @@ def cartesian_geometry(mesh, std):
 class MultielementDisc:
     """MultielementDisc(mesh, std, equation, operator, bcs) on the GPU.
 
-    `bcs` maps boundary names ("1".."2d") to EulerInflowBC / EulerOutflowBC / EulerSlipBC.
+    `bcs` maps boundary names ("1".."2d") to EulerInflowBC / EulerOutflowBC / EulerSlipBC / GenericBC.
     """
 
     def __init__(self, mesh, std, equation, operator, bcs=None):
@@ -103,8 +103,38 @@ class MultielementDisc:
             self.J, self.Ja, self.frames, self.faceJ, self.coords = unstructured_geometry(mesh, std)
         else:
             self.J, self.Ja, self.frames, self.faceJ, self.coords = cartesian_geometry(mesh, std)
+        self._resolve_generic_bcs()
         self.config = self._config()
         self._ctx = None
+
+    def _boundary_face_coords(self, ib):
+        """Physical coordinates of the face nodes of boundary `ib` (1-based), as the trace
+        Σ_i l_i x_i of the master element's node coordinates across the face (Interfaces.jl:51-109;
+        exact for the linear element mappings)."""
+        m, s = self.mesh, self.std
+        n, d = s.n, m.dim
+        out = []
+        for f in np.nonzero(np.asarray(m.bdface_index) == ib)[0]:
+            e, pos = int(m.eleminds[f, 0]) - 1, int(m.elempos[f, 0]) - 1
+            X = self.coords[e * n ** d:(e + 1) * n ** d, :d].reshape((n,) * d + (d,), order="F")
+            lv = s.l[pos % 2]
+            out.append(np.tensordot(X, lv, axes=([pos // 2], [0])).reshape(-1, d))
+        return np.concatenate(out) if out else np.zeros((0, d))
+
+    def _resolve_generic_bcs(self):
+        for ib, bc in enumerate(self.bcs):
+            if not isinstance(bc, GenericBC):
+                continue
+            try:
+                vals = [np.asarray(bc.Qext(None, x, None, 0.0, self.equation), dtype=np.float64)
+                        for x in self._boundary_face_coords(ib + 1)]
+            except Exception as exc:   # Qext reads the interior state or the frame
+                raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "GenericBC on boundary %d: Qext must give the external "
+                                  "state from the position alone (%s)" % (ib + 1, exc)) from exc
+            if not vals or any(not np.array_equal(v, vals[0]) for v in vals):
+                raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "GenericBC on boundary %d: the external state varies "
+                                  "along the boundary; one state per boundary is supported" % (ib + 1))
+            self.bcs[ib] = EulerInflowBC(vals[0])
 
     # -- C ABI configuration ------------------------------------------------------------
     def _config(self):
@@ -262,6 +292,18 @@ class Context:
 
     def wait(self):
         L.check(self._lib.flou_wait(self.h), self.h)
+
+    def set_integrator(self, A=None, B=None):
+        """The step method of step(): a 2N-storage method (A[0] unused), or SSP-RK3 when None."""
+        if B is None:
+            L.check(self._lib.flou_set_integrator(self.h, 0, None, None), self.h)
+            return
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        if A.shape != B.shape:
+            raise ValueError("A and B must have one coefficient per stage")
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.check(self._lib.flou_set_integrator(self.h, len(B), A.ctypes.data_as(dp), B.ctypes.data_as(dp)), self.h)
 
     def set_limiter(self, kind, minval=0.0):
         """FLOU_LIMITER_ZHANG_SHU with its minimum value, or FLOU_LIMITER_NONE."""

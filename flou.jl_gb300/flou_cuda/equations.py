@@ -90,6 +90,18 @@ class EulerSlipBC:
         self.state = None
 
 
+class GenericBC:
+    """GenericBC(Qext) with Qext(Qin, x, frame, time, equation) (FlouSpatial.jl:80-91).  The device
+    holds one external state per boundary, so MultielementDisc evaluates Qext at every face node
+    of the boundary (Qin = frame = None, time = 0) and accepts it when the state is the same at
+    all of them; it then acts as EulerInflowBC(state)."""
+
+    def __init__(self, Qext):
+        self.Qext = Qext
+        self.kind = L.BC_INFLOW
+        self.state = None
+
+
 DirichletBC = EulerInflowBC   # constant state for the scalar equations
 OutflowBC = EulerOutflowBC
 

@@ -1,8 +1,9 @@
-"""timeintegrate with the Shu-Osher SSP-RK3 integrator, on the GPU.
+"""timeintegrate on the GPU, with the fixed-step explicit Runge-Kutta methods the reference uses.
 
 Reference: src/FlouTime/FlouTime.jl:34-54 (timeintegrate -> ODEProblem(rhs!, ...) + solve).
-Flou hands the stepping to OrdinaryDiffEq; here the solver is SSPRK33 (Shu & Osher 1988),
-fixed step, run by flou_step with each stage fused into the residual kernel.
+Flou hands the stepping to OrdinaryDiffEq (6.49.1); here the solver is SSPRK33 (Shu & Osher
+1988) or a 2N-storage method (Williamson 1980: ORK256, CarpenterKennedy2N54, or any
+LowStorageRK2N tableau), run by flou_step with each stage fused into the residual kernel.
 """
 import math
 
@@ -17,6 +18,59 @@ class SSPRK33:
 
     def __init__(self, stage_limiter=None):
         self.stage_limiter = stage_limiter
+
+
+class LowStorageRK2N:
+    """A 2N-storage Runge-Kutta method (Williamson 1980) in OrdinaryDiffEq's LowStorageRK2N form
+    with williamson_condition = false:
+        k = dt L(u); u += B_1 k;   k = A_i k + dt L(u); u += B_i k   (i = 2..s).
+    `A[0]` is not used.  The stage limiter, when given, acts after every stage."""
+
+    def __init__(self, A, B, stage_limiter=None, williamson_condition=False):
+        if len(A) != len(B) or not 1 <= len(B) <= 16:
+            raise ValueError("a 2N-storage method takes 1..16 stages with one A and one B each")
+        self.A = [0.0] + [float(a) for a in A[1:]]
+        self.B = [float(b) for b in B]
+        self.stage_limiter = stage_limiter
+        self.williamson_condition = williamson_condition   # an implementation choice; no effect here
+
+    @property
+    def c(self):
+        """Stage abscissae c_i = Σ_j a_ij of the equivalent Butcher tableau (unused by the
+        stepping: no boundary condition on this path depends on time)."""
+        s = len(self.B)
+        alpha = [[0.0] * s for _ in range(s)]
+        beta = [0.0] * s
+        out = []
+        for i in range(s):
+            out.append(sum(beta))
+            for j in range(s):
+                alpha[i][j] = (self.A[i] * alpha[i - 1][j] if i else 0.0) + (1.0 if i == j else 0.0)
+                beta[j] += self.B[i] * alpha[i][j]
+        return out
+
+
+class ORK256(LowStorageRK2N):
+    """Five-stage, second-order 2N-storage method of Allampalli, Hixon, Nallasamy and Sawyer
+    (J. Comput. Phys. 228, 2009), the solver of the reference's tests (test/tests.jl:19,56,93,139)
+    and examples (examples/src/3D_Euler.jl:77)."""
+
+    def __init__(self, stage_limiter=None, williamson_condition=False):
+        super().__init__([0.0, -1.0, -1.55798, -1.0, -0.45031], [0.2, 0.83204, 0.6, 0.35394, 0.2],
+                         stage_limiter, williamson_condition)
+
+
+class CarpenterKennedy2N54(LowStorageRK2N):
+    """Five-stage, fourth-order 2N-storage method of Carpenter and Kennedy (NASA TM-109112,
+    1994), solution 3."""
+
+    def __init__(self, stage_limiter=None, williamson_condition=False):
+        super().__init__(
+            [0.0, -567301805773 / 1357537059087, -2404267990393 / 2016746695238,
+             -3550918686646 / 2091501179385, -1275806237668 / 842570457699],
+            [1432997174477 / 9575080441755, 5161836677717 / 13612068292357, 1720146321549 / 2090206949498,
+             3134564353537 / 4481467310338, 2277821191437 / 14882151754819],
+            stage_limiter, williamson_condition)
 
 
 class LimiterCallback:
@@ -78,8 +132,9 @@ def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t
     """
     import time as _time
 
-    if not isinstance(solver, SSPRK33):
-        raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "only SSPRK33 is implemented")
+    if not isinstance(solver, (SSPRK33, LowStorageRK2N)):
+        raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "the solvers are SSPRK33 and the 2N-storage methods "
+                                                  "(ORK256, CarpenterKennedy2N54, LowStorageRK2N)")
     ctx = disc.ctx
     if dt is None:
         if cfl is None:
@@ -97,6 +152,9 @@ def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t
     for m in mons:
         mask |= m.which
     ctx.set_monitors(mask, max(nsteps, 1))
+    lowstorage = isinstance(solver, LowStorageRK2N)
+    if lowstorage:
+        ctx.set_integrator(solver.A, solver.B)
     start = _time.perf_counter()
     try:
         ctx.step(Q, dt, nsteps, t0)
@@ -104,6 +162,8 @@ def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t
         vals = ctx.take_monitors(max(nsteps, 1)) if mask else None
         ctx.set_monitors(0, 1)
         ctx.set_limiter(L.LIMITER_NONE)
+        if lowstorage:
+            ctx.set_integrator(None)
     exetime = _time.perf_counter() - start
     for m in mons:
         col = 0 if m.which == L.MONITOR_KINETIC_ENERGY else 1

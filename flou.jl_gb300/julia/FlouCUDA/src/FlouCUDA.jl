@@ -15,8 +15,9 @@ using Flou.FlouCommon: AbstractSpatialDiscretization, EquationConfig, Hyperbolic
 import Flou.FlouCommon: rhs!, get_max_dt
 using ChainRulesCore
 using LinearAlgebra
+using OrdinaryDiffEq
 
-export GPUDisc, SSPRK3GPU, GPUBatch, solve_functional, solve_functional_batch
+export GPUDisc, SSPRK3GPU, LowStorageGPU, GPUBatch, solve_functional, solve_functional_batch
 export set_limiter!, monitor, record_monitors!, take_monitors!
 
 const libflou = joinpath(@__DIR__, "..", "..", "..", "lib", "libflou_cuda.so")
@@ -126,10 +127,14 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
     GC.@preserve faceinds facepos eleminds elempos orient bdidx check(ccall((:flou_set_mesh, libflou), Int32,
         (Ptr{Cvoid}, Int32, Int32, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{UInt8}, Ptr{Int32}),
         ctx, ne, nf, faceinds, facepos, eleminds, elempos, orient, bdidx), ctx)
-    kinds = Int32[bc isa EulerSlipBC ? 3 : bc isa EulerInflowBC ? 2 : 1 for bc in disc.bcs]
+    kinds = Int32[bc isa EulerSlipBC ? 3 : (bc isa EulerInflowBC || bc isa GenericBC) ? 2 : 1 for bc in disc.bcs]
     states = zeros(Float64, 5, length(kinds))
     for (i, bc) in enumerate(disc.bcs)
         bc isa EulerInflowBC && (states[1:length(bc.Qext), i] .= bc.Qext)
+        if bc isa GenericBC   # one external state per boundary (FlouSpatial.jl:80-91)
+            q = genericbc_state(bc, disc, i, equation)
+            states[1:length(q), i] .= q
+        end
     end
     GC.@preserve kinds states check(ccall((:flou_set_bcs, libflou), Int32,
         (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}), ctx, length(kinds), kinds, states), ctx)
@@ -161,8 +166,49 @@ function get_max_dt(q::Matrix{Float64}, disc::GPUDisc, ::Any, cfl)
     return dt[]
 end
 
+"The external state of a GenericBC, evaluated at every face node of boundary `ib`; it must be one state."
+function genericbc_state(bc, disc, ib, equation)
+    vals = [bc.Qext(nothing, x, nothing, 0.0, equation)
+            for f in eachbdface(disc.mesh, ib) for x in disc.geometry.faces.coords[f]]
+    all(v -> v == vals[1], vals) ||
+        error("GenericBC on boundary $ib: the external state varies along the boundary; one state per boundary is supported")
+    return Vector{Float64}(vals[1])
+end
+
 "SSP-RK3 run entirely on the GPU (one CUDA graph per step)."
 struct SSPRK3GPU end
+
+"""
+    LowStorageGPU(solver)
+
+A 2N-storage method of OrdinaryDiffEq (ORK256, CarpenterKennedy2N54, ...: the LowStorageRK2N
+family) run on the GPU by `flou_step` after `flou_set_integrator`; its coefficients come from
+OrdinaryDiffEq's own tableau (`<Name>ConstantCache(Float64, Float64)`: A2end, B1, B2end).  The
+stage limiter of the solver is not carried over: set it with `set_limiter!`.
+"""
+struct LowStorageGPU
+    A::Vector{Float64}
+    B::Vector{Float64}
+end
+
+function LowStorageGPU(solver)
+    cache = getproperty(OrdinaryDiffEq, Symbol(nameof(typeof(solver)), "ConstantCache"))
+    tab = cache(Float64, Float64)
+    return LowStorageGPU(vcat(0.0, collect(tab.A2end)), vcat(tab.B1, collect(tab.B2end)))
+end
+
+function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, solver::LowStorageGPU, tfinal; dt,
+                            kwargs...)
+    A, B = solver.A, solver.B
+    GC.@preserve A B check(ccall((:flou_set_integrator, libflou), Int32,
+        (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}), disc.ctx, length(B), A, B), disc.ctx)
+    try
+        return Flou.timeintegrate(Q0, disc, equation, SSPRK3GPU(), tfinal; dt=dt, kwargs...)
+    finally
+        ccall((:flou_set_integrator, libflou), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}),
+              disc.ctx, 0, C_NULL, C_NULL)
+    end
+end
 
 """
     timeintegrate(Q0, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt)

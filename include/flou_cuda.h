@@ -162,6 +162,19 @@ int32_t flou_rhs(flou_ctx* ctx, double* dQ, const double* Q, double t, int32_t p
  * value (Flou raises a DomainError there, FlouTime.jl:37-51). */
 int32_t flou_step(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps, int32_t ptr_kind);
 
+/* The step method of flou_step / flou_step_async.  nstages = 0 restores the Shu-Osher SSP-RK3
+ * (the default).  nstages in 1..FLOU_MAX_LSRK_STAGES selects the 2N-storage Runge-Kutta method
+ * (Williamson 1980) with coefficients A[0..s-1] (A[0] is not read) and B[0..s-1]:
+ *   k = dt L(u); u += B[0] k;   for i = 1..s-1: k = A[i] k + dt L(u); u += B[i] k,
+ * the LowStorageRK2N form of OrdinaryDiffEq 6.49.1 with williamson_condition = false, which
+ * the reference steps its tests and examples with (ORK256, test/tests.jl:19,56,93,139;
+ * CarpenterKennedy2N54).  No boundary condition on this path depends on time, so the stage
+ * abscissae are not needed.  Each stage is one residual whose element epilogue updates k and
+ * u in place; the limiter, when set, acts after every stage.  The adjoint and the batched
+ * launch step with SSP-RK3 only. */
+#define FLOU_MAX_LSRK_STAGES 16
+int32_t flou_set_integrator(flou_ctx* ctx, int32_t nstages, const double* A, const double* B);
+
 /* flou_step without the final synchronisation: the copies (host pointers; use pinned memory
  * for them to overlap) and the steps are queued on the context's stream and the call returns.
  * The state must stay untouched until flou_wait(ctx), which synchronises and reports the status

@@ -847,7 +847,7 @@ inline Vec<T> twopointflux(const Vec<T>& Q1, const Vec<T>& Q2, const double* Ja1
     }
     if (c.tpflux == TP_KENNEDY_GRUBER) {
         T rho = (P1[0] + P2[0]) / 2.0;
-        T vel[3];
+        T vel[3]{};
         for (int k = 0; k < dim; ++k) vel[k] = (P1[1 + k] + P2[1 + k]) / 2.0;
         T p = (P1[dim + 1] + P2[dim + 1]) / 2.0;
         T e = (Q1[dim + 1] / P1[0] + Q2[dim + 1] / P2[0]) / 2.0;
@@ -1308,6 +1308,32 @@ inline void ssprk3_step_limited(const Disc& g, double* Q, double dt, double t, W
     rhs(g, L.data(), U.data(), t + 0.5 * dt, ws);
     for (long i = 0; i < N; ++i) Q[i] = (1.0 / 3.0) * Q[i] + (2.0 / 3.0) * (U[i] + dt * L[i]);
     zhang_shu(g, Q, minval, omega);
+}
+
+// Williamson (1980) 2N-storage Runge-Kutta, the form of OrdinaryDiffEq 6.49.1's LowStorageRK2N
+// methods (ORK256, CarpenterKennedy2N54) with williamson_condition = false, which the reference's
+// tests and examples step with (test/tests.jl:19,56,93,139; examples/src/3D_Euler.jl:77):
+//   k = dt L(u); u = u + B_1 k;   for i = 2..s: k = A_i k + dt L(u, t + c_i dt); u = u + B_i k.
+// The stage limiter, when `omega` is given, acts on u after every stage.
+inline void lsrk2n_step(const Disc& g, double* Q, double dt, double t, Workspace<double>& ws,
+                        std::vector<double>& K, std::vector<double>& L, int s, const double* A, const double* B,
+                        const double* c, double minval = 0.0, const std::vector<double>* omega = nullptr) {
+    long N = g.ndofs() * g.cfg.nv;
+    K.resize(N);
+    L.resize(N);
+    for (int st = 0; st < s; ++st) {
+        rhs(g, L.data(), Q, t + c[st] * dt, ws);
+        if (st == 0) {
+#pragma omp parallel for schedule(static)
+            for (long i = 0; i < N; ++i) K[i] = dt * L[i];
+        } else {
+#pragma omp parallel for schedule(static)
+            for (long i = 0; i < N; ++i) K[i] = A[st] * K[i] + dt * L[i];
+        }
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < N; ++i) Q[i] = Q[i] + B[st] * K[i];
+        if (omega) zhang_shu(g, Q, minval, *omega);
+    }
 }
 
 // get_max_dt, MultielementDiscontinuous.jl:162-178 with the pointwise estimates of

@@ -301,6 +301,24 @@ int oracle_ssprk3(void* hp, double* Q, double dt, int nsteps, double t0) {
     return 0;
 }
 
+// `nsteps` steps of a 2N-storage Runge-Kutta method with `nstages` stages (A[0] unused); with
+// omega_tp set, the Zhang-Shu limiter with `minval` after every stage.
+int oracle_lsrk2n(void* hp, double* Q, double dt, int nsteps, double t0, int nstages, const double* A,
+                  const double* B, const double* c, double minval, const double* omega_tp) {
+    Handle* h = (Handle*)hp;
+    std::vector<double> w;
+    if (omega_tp) w.assign(omega_tp, omega_tp + h->g.npe);
+    try {
+        for (int s = 0; s < nsteps; ++s)
+            lsrk2n_step(h->g, Q, dt, t0 + s * dt, h->ws, h->U, h->L, nstages, A, B, c, minval,
+                        omega_tp ? &w : nullptr);
+    } catch (std::exception& e) {
+        std::fprintf(stderr, "oracle_lsrk2n: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
 // HybridDivOperator parameters: the subcell FV flux (kind, its central flux, intensity), the
 // blending constant, the 1D weights and the derivative matrix (n x n, column-major).
 void oracle_set_hybrid(void* hp, int fvflux, int fvavg, double fvintensity, double blend, const double* omega1d,

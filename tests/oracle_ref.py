@@ -44,7 +44,9 @@ def lib():
         _lib.oracle_monitor.argtypes = [ctypes.c_void_p, D, ctypes.c_int, D]
         _lib.oracle_ssprk3_limited.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                                ctypes.c_double, D]
-        _lib.oracle_count_rhs.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
+        _lib.oracle_lsrk2n.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int, D, D, D, ctypes.c_double, D]
+        _lib.oracle_count_rhs.argtypes =[ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
         _lib.oracle_solve_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D, D, D]
@@ -168,6 +170,17 @@ class Disc:
         if self.L.oracle_ssprk3_limited(self.h, _d(Q), dt, nsteps, t0, minval,
                                         _d(np.ascontiguousarray(omega_tp))) != 0:
             raise RuntimeError("oracle ssprk3 failed")
+        return Q
+
+    def lsrk2n(self, Q, dt, nsteps, A, B, c, t0=0.0, minval=None, omega_tp=None):
+        """`nsteps` steps of the 2N-storage method (A, B, c); the limiter after every stage when
+        `minval` is given."""
+        Q = np.array(Q, dtype=np.float64, order="F", copy=True)
+        A, B, c = (np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, c))
+        w = None if minval is None else np.ascontiguousarray(omega_tp, dtype=np.float64)
+        if self.L.oracle_lsrk2n(self.h, _d(Q), dt, nsteps, t0, len(B), _d(A), _d(B), _d(c),
+                                0.0 if minval is None else float(minval), _d(w) if w is not None else None) != 0:
+            raise RuntimeError("oracle lsrk2n failed")
         return Q
 
     def max_dt(self, Q, cfl, omega_tp):

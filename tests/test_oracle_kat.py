@@ -1,14 +1,19 @@
 """The oracle against the reference's own known-answer tests and the invariants of the
-scheme.  Pins: the Advection1D / Advection2D period property (test/tests.jl:16-88,
-test/runtests.jl:23-32: u(T) ≈ u(0), rtol 1e-3) re-run with SSP-RK3 at the reference's dt;
-freestream preservation; discrete conservation; entropy conservation of the split form
-with entropy-conserving fluxes; the convergence order of examples/src/Convergence.jl."""
+scheme.  Pins: the golden values of the Sod tube and the 2D normal shock (test/runtests.jl:34-45,
+rtol 1e-7: split form and hybrid operator with MatrixDissipation, GenericBC, ORK256); the
+Advection1D / Advection2D period property (test/tests.jl:16-88, test/runtests.jl:23-32:
+u(T) ≈ u(0), rtol 1e-3) with ORK256 at the reference's dt; freestream preservation; discrete
+conservation; entropy conservation of the split form with entropy-conserving fluxes; the
+convergence order of examples/src/Convergence.jl."""
 import numpy as np
 import pytest
 
 import flou_cuda as F
 import oracle_ref
+import reference_problems as RP
 from cases import build, oracle_for, smooth_euler_state
+
+ORK = F.ORK256()
 
 
 def _norm_close(a, b, rtol):   # Julia's isapprox for arrays: norm(a-b) <= rtol*max(norm(a), norm(b))
@@ -31,9 +36,10 @@ def test_advection1d_period():
                  box=((0.0,), (1.0,)))
     Q0 = np.asfortranarray(F.initial.gaussian_bump(disc.coords, (0.5,), (0.1,), 1.0)[:, None])
     o = _oracle_disc(disc, lobatto=False)
-    Q = o.ssprk3(Q0, 1e-3, 500)
+    Q = o.lsrk2n(Q0, 1e-3, 500, ORK.A, ORK.B, ORK.c)
     assert _norm_close(Q, Q0, 1e-3)
-    assert not np.allclose(o.ssprk3(Q0, 1e-3, 250), Q0, rtol=1e-3)   # it did move
+    assert not np.allclose(o.lsrk2n(Q0, 1e-3, 250, ORK.A, ORK.B, ORK.c), Q0, rtol=1e-3)   # it did move
+    assert _norm_close(o.ssprk3(Q0, 1e-3, 500), Q0, 1e-3)   # and so does SSP-RK3 at that dt
 
 
 def test_advection2d_period():
@@ -43,8 +49,51 @@ def test_advection2d_period():
                  box=((0.0, 0.0), (1.5, 2.0)))
     Q0 = np.asfortranarray(F.initial.gaussian_bump(disc.coords[:, :2], (0.75, 1.0), (0.2, 0.2), 1.0)[:, None])
     o = _oracle_disc(disc, lobatto=False)
-    Q = o.ssprk3(Q0, 1e-3, 500)
+    Q = o.lsrk2n(Q0, 1e-3, 500, ORK.A, ORK.B, ORK.c)
     assert _norm_close(Q, Q0, 1e-3)
+
+
+def test_sod_tube_golden():
+    """SodTube1D (test/tests.jl:90-134) hits the reference's golden min / max (rtol 1e-7)."""
+    disc, Q0, dt, tf = RP.sod_tube()
+    o = _oracle_disc(disc, lobatto=True)
+    Q = o.lsrk2n(Q0, dt, int(round(tf / dt)), ORK.A, ORK.B, ORK.c)
+    assert RP.isclose(Q.min(), RP.SOD_MIN, 1e-7), Q.min()
+    assert RP.isclose(Q.max(), RP.SOD_MAX, 1e-7), Q.max()
+
+
+def test_shockwave2d_golden():
+    """Shockwave2D (test/tests.jl:136-181), the hybrid operator, hits the reference's golden
+    maximum (rtol 1e-7) and its minimum test (rtol 1: a round-off y-momentum of either sign
+    passes when it is negative, as the reference's is)."""
+    disc, Q0, dt, tf = RP.shockwave_2d()
+    o = _oracle_disc(disc, lobatto=True)
+    Q = o.lsrk2n(Q0, dt, int(round(tf / dt)), ORK.A, ORK.B, ORK.c)
+    assert RP.isclose(Q.max(), RP.SHOCK_MAX, 1e-7), Q.max()
+    assert RP.isclose(Q.min(), RP.SHOCK_MIN, 1.0), Q.min()
+
+
+def test_low_storage_tableaux_orders():
+    """ORK256 is second order and CarpenterKennedy2N54 fourth order: the order conditions of
+    the Butcher tableau equivalent to each 2N-storage form (ORK256's five-digit coefficients
+    meet b·c = 1/2 to 6e-7)."""
+    def butcher(m):
+        s = len(m.B)
+        alpha, beta = np.zeros((s, s)), np.zeros((s + 1, s))
+        for i in range(s):
+            alpha[i] = (m.A[i] * alpha[i - 1] if i else 0.0) + np.eye(s)[i]
+            beta[i + 1] = beta[i] + m.B[i] * alpha[i]
+        return beta[:s], beta[s]
+    a, b = butcher(F.ORK256())
+    c = a.sum(1)
+    assert abs(b.sum() - 1) < 1e-15 and abs(b @ c - 0.5) < 1e-6
+    assert np.allclose(c, F.ORK256().c, atol=1e-15)
+    a, b = butcher(F.CarpenterKennedy2N54())
+    c = a.sum(1)
+    conds = [(b.sum(), 1), (b @ c, 1 / 2), (b @ c ** 2, 1 / 3), (b @ a @ c, 1 / 6), (b @ c ** 3, 1 / 4),
+             (b @ (c * (a @ c)), 1 / 8), (b @ a @ c ** 2, 1 / 12), (b @ a @ a @ c, 1 / 24)]
+    for got, want in conds:
+        assert abs(got - want) < 1e-14
 
 
 @pytest.mark.parametrize("dim,n,vol", [(1, 5, "strong"), (2, 4, "strong"), (2, 5, "split"), (3, 3, "split"),
