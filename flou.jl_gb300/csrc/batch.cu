@@ -334,8 +334,10 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
             delete b;
             return r;
         }
-        if (c->limiter || c->mon_mask || c->curv || c->lsrk_s) {   // the persistent launch runs none of these
-            c->err = "the batched launch covers Cartesian geometry, SSP-RK3, without limiter or monitors";
+        if (c->limiter || c->mon_mask || c->curv || c->lsrk_s ||
+            (c->cfg.volume_op != FLOU_OP_STRONG && !c->bnodes)) {   // the persistent launch runs none of these
+            c->err = "the batched launch covers Cartesian geometry, SSP-RK3, without limiter or monitors, and "
+                     "the split form on Gauss-Lobatto nodes";
             delete b;
             return FLOU_ERR_UNSUPPORTED;
         }

@@ -41,6 +41,11 @@ cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t 
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
     if (L.curv) return L.dim == 2 ? launch_elem_curv2d(L, P, s) : launch_elem_curv3d(L, P, s);
     if (L.eq != FLOU_EQ_EULER) return launch_elem_scalar(L, P, s);
+    if (!L.lgl && L.vol != FLOU_OP_STRONG) {   // entropy-projected Gauss-node operators
+        if (L.dim == 1) return launch_elem_gauss1d(L, P, s);
+        if (L.dim == 2) return launch_elem_gauss2d(L, P, s);
+        return L.vol == FLOU_OP_HYBRID ? launch_elem_gauss3d_hybrid(L, P, s) : launch_elem_gauss3d_split(L, P, s);
+    }
     if (L.dim == 1) return launch_elem_euler1d(L, P, s);
     if (L.dim == 2) return launch_elem_euler2d(L, P, s);
     if (L.vol == FLOU_OP_STRONG) return launch_elem_euler3d_strong(L, P, s);

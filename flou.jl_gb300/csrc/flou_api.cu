@@ -149,7 +149,9 @@ ElemLaunch elem_launch(const flou_ctx* c) {
     L.n = c->n;
     L.vol = c->cfg.volume_op;
     L.tp = c->cfg.twopoint_flux;
-    L.lgl = c->lgl;
+    // the strong form takes the specialised path only on exact end-node operators; the split and
+    // hybrid kernels follow the basis type (their Gauss-Lobatto lift reads the end entries only)
+    L.lgl = c->cfg.volume_op == FLOU_OP_STRONG ? c->lgl : c->bnodes;
     L.prepare = false;
     L.curv = c->curv;
     return L;
@@ -527,14 +529,27 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
         if (i != 0 && (l_l[i] != 0.0 || dg_l[i] != 0.0)) lgl = false;
         if (i != n - 1 && (l_r[i] != 0.0 || dg_r[i] != 0.0)) lgl = false;
     }
-    if (c->cfg.volume_op != FLOU_OP_STRONG && !lgl)
+    // Whether the basis has boundary nodes (the reference's hasboundaries, a property of the node
+    // type) decides the split and hybrid operators' coupling to the faces.  Operators fitted the
+    // way the reference builds them carry round-off in the entries that vanish on Gauss-Lobatto
+    // nodes, so this test has a tolerance; Gauss nodes are far from it.
+    bool bnodes = fabs(l_l[0] - 1.0) < 1e-10 && fabs(l_r[n - 1] - 1.0) < 1e-10;
+    for (int i = 0; i < n; ++i) {
+        if (i != 0 && (fabs(l_l[i]) > 1e-10 || fabs(dg_l[i]) > 1e-10 * fabs(dg_l[0]))) bnodes = false;
+        if (i != n - 1 && (fabs(l_r[i]) > 1e-10 || fabs(dg_r[i]) > 1e-10 * fabs(dg_r[n - 1]))) bnodes = false;
+    }
+    // Without boundary nodes the split and hybrid operators couple the volume to the faces
+    // through entropy-projected states (OpDivergence.jl:301-437, 614-780): Euler only, since
+    // the scalar equations have no entropy variables in the reference.
+    if (c->cfg.volume_op != FLOU_OP_STRONG && !bnodes && c->cfg.equation != FLOU_EQ_EULER)
         return fail(c, FLOU_ERR_UNSUPPORTED,
-                    "the split-form and hybrid operators need a basis with boundary nodes (the entropy-"
-                    "projected Gauss-node path of OpDivergence.jl:301-437 is not implemented)");
+                    "the split-form and hybrid operators of the scalar equations need a basis with boundary "
+                    "nodes (the Gauss-node path projects the entropy variables of the Euler equations)");
     int r = upload(c, &c->d_ops, ops.data(), ops.size(), "operator upload");
     if (r) return r;
     if ((r = upload(c, &c->d_omega1, omega, (size_t)n, "operator upload"))) return r;
     c->lgl = lgl;
+    c->bnodes = bnodes;
     c->omega.assign(omega, omega + n);
     c->have_ops = true;
     drop_graph(c);
@@ -608,7 +623,7 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     bool curv = !cart || c->any_orient;
     if (curv && c->cfg.dim == 1)
         return fail(c, FLOU_ERR_UNSUPPORTED, "1D geometry must have J constant per element and the Cartesian frames");
-    if (curv && !c->lgl)
+    if (curv && !c->bnodes)
         return fail(c, FLOU_ERR_UNSUPPORTED, "general (curvilinear / unstructured) geometry needs a basis with "
                                              "boundary nodes (LGL)");
     if (curv && c->cfg.equation == FLOU_EQ_BURGERS)

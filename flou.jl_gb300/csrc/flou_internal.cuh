@@ -618,13 +618,15 @@ __device__ __forceinline__ void raise_nonphysical(int32_t* status, int elem) {
 // stage update.  Shared by both volume operators.
 // CURV: a slave side reads the master's face dof that master2slave sends onto its own line
 // index (the inverse orientation), and 1/J is taken per node.
-template <int DIM, int N, int NV, bool LGL, bool CURV = false>
+// LIFT = false: the face fluxes already entered through the volume term (the hybrid operator on
+// Gauss nodes, OpDivergence.jl:633-730), so only 1/J and the stage update remain.
+template <int DIM, int N, int NV, bool LGL, bool CURV = false, bool LIFT = true>
 __device__ __forceinline__ void surface_and_update(const ElemParams& P, const double* sops, int e, int i,
                                                    const double* q, double* dq) {
     const double* dgl = sops + 2 * N * N + 2 * N;
     const double* dgr = dgl + N;
 #pragma unroll
-    for (int dir = 0; dir < DIM; ++dir) {
+    for (int dir = 0; dir < (LIFT ? DIM : 0); ++dir) {
         int pos, line;
         tp_coords<DIM>(N, i, dir, pos, line);
         int32_t pl = P.elem_face[e * 2 * DIM + 2 * dir], pr = P.elem_face[e * 2 * DIM + 2 * dir + 1];
@@ -869,6 +871,38 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     F[DIM + 1] = m * h;
 }
 
+// The per-node quantities of SplitLayout for one state (q conserved, v velocity, p pressure,
+// vv = |v|², ir = 1/ρ), written at column `col` of arrays with stride `st`.
+template <int DIM, int TP>
+__device__ __forceinline__ void store_split_node(double* S, int st, int col, const double* q, const double* v,
+                                                 double p, double vv, double ir) {
+    if (TP == FLOU_TP_CHANDRASHEKAR) {
+        S[col] = 0.5 * q[0];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
+        S[(1 + DIM) * st + col] = (0.25 * q[0]) / p;
+        S[(2 + DIM) * st + col] = 0.25 * vv;
+    } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
+        S[col] = 0.5 * q[0];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
+        S[(1 + DIM) * st + col] = 0.5 * p;
+        S[(2 + DIM) * st + col] = 0.5 * (q[DIM + 1] * ir);
+    } else {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) S[k * st + col] = v[k];
+        S[DIM * st + col] = p;
+#pragma unroll
+        for (int k = 0; k < DIM + 2; ++k) S[(DIM + 1 + k) * st + col] = q[k];
+    }
+}
+
+// GAUSS (Euler on a basis without boundary nodes, Cartesian): the entropy-projected coupling of
+// OpDivergence.jl:301-437.  Per line, W is interpolated to both ends, Q̃ = entropy2cons(W̃), and
+// each node adds ∂g_l (F♯(Q_i, Q̃_l) - l·F♯(·, Q̃_l)) - ∂g_r (F♯(Q_i, Q̃_r) - r·F♯(·, Q̃_r)) to
+// the split volume term; the projected states sit behind the nodes in the per-node arrays and
+// their 2N two-point fluxes per line behind the volume pairs.  With HYB (OpDivergence.jl:633-
+// 780) the same terms enter the subcell fluxes, which start at the element's own face fluxes.
 // HYB: the hybrid (telescopic) form of HybridDivOperator on LGL nodes (OpDivergence.jl:553-604):
 // the split-form node sums give the high-order subcell fluxes by F̄_{p+1} = F̄_p + ω_p Σ_j D♯_pj F♯_pj
 // (F̄ = 0 at both element ends; algebraically the reference's Σ_{l<p<=k} 2 ω_l D_lk F♯(l,k)), each
@@ -882,12 +916,16 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = S::EPB * NFD * NPAIR;   // pairs per direction in the block
     constexpr bool EULER = (EQ == FLOU_EQ_EULER);
+    constexpr bool GAUSS = !LGL && EULER && !CURV;
+    constexpr int NPROJ = GAUSS ? 2 * S::EPB * NFD : 0;       // projected states, 2 per line
+    constexpr int SST = NN + NPROJ;                            // stride of the per-node arrays
+    constexpr int NPTX = NPT + (GAUSS ? NPROJ * N : 0);        // + node x projected-state fluxes
     double* sops = smem;
-    double* sprim = sops + S::NOPS;                 // [Lay::NARR][NN]
-    double* spair = sprim + Lay::NARR * NN;         // [NV][NPT]
-    double* sJa = spair + NV * NPT;                 // CURV: [DIM][NN] metric column of the direction
-    double* sW = sJa + (CURV ? DIM * NN : 0);       // HYB: [NV][NN] entropy variables
-    double* sH = sW + (HYB ? NV * NN : 0);          // HYB: [NV][NN] ω_p Ja Σ_j D♯ F♯ of each node
+    double* sprim = sops + S::NOPS;                 // [Lay::NARR][SST]
+    double* spair = sprim + Lay::NARR * SST;        // [NV][NPTX]
+    double* sJa = spair + NV * NPTX;                // CURV: [DIM][NN] metric column of the direction
+    double* sW = sJa + (CURV ? DIM * NN : 0);       // HYB, GAUSS: [NV][NN] entropy variables
+    double* sH = sW + ((HYB || GAUSS) ? NV * NN : 0);   // HYB: [NV][NN] the node's subcell increment
     double* sFb = sH + (HYB ? NV * NN : 0);         // HYB: [NV][NN] blended flux at the node's left interface
     uint8_t* stab = (uint8_t*)(sFb + (HYB ? NV * NN : 0));   // pair table: a, b
     const int tid = threadIdx.x;
@@ -919,7 +957,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             }
             p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
             if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
-            if constexpr (HYB) {   // vars_cons2entropy, FlouCommon/Euler.jl:273-307
+            if constexpr (HYB || GAUSS) {   // vars_cons2entropy, FlouCommon/Euler.jl:273-307
                 double ip = 1.0 / p;
                 double sv = log(p) - g * log(q[0]);
                 sW[tid] = (g - sv) / (g - 1.0) - ke * ip * 0.5;
@@ -927,25 +965,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 for (int k = 0; k < DIM; ++k) sW[(1 + k) * NN + tid] = q[1 + k] * ip;
                 sW[(DIM + 1) * NN + tid] = -q[0] * ip;
             }
-            if (TP == FLOU_TP_CHANDRASHEKAR) {
-                sprim[tid] = 0.5 * q[0];
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
-                sprim[(1 + DIM) * NN + tid] = (0.25 * q[0]) / p;
-                sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
-            } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
-                sprim[tid] = 0.5 * q[0];
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
-                sprim[(1 + DIM) * NN + tid] = 0.5 * p;
-                sprim[(2 + DIM) * NN + tid] = 0.5 * (q[DIM + 1] * ir);
-            } else {
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) sprim[k * NN + tid] = v[k];
-                sprim[DIM * NN + tid] = p;
-#pragma unroll
-                for (int k = 0; k < NV; ++k) sprim[(DIM + 1 + k) * NN + tid] = q[k];
-            }
+            if constexpr (EULER) store_split_node<DIM, TP>(sprim, SST, tid, q, v, p, vv, ir);
         } else {
             sprim[tid] = q[0];
         }
@@ -958,6 +978,41 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     const double c_beta = 0.5 / (g - 1.0);
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
+        double fls[NV], frs[NV];   // GAUSS && HYB: this element's side values of its line's face fluxes
+        if constexpr (GAUSS) {   // entropy-projected states at both ends of every line (OpDivergence.jl:405-409)
+            for (int t = tid; t < NPROJ; t += blockDim.x) {
+                int elp = t / (2 * NFD);
+                if (e0 + elp >= P.nelem) continue;
+                int rr = t - elp * 2 * NFD, line = rr >> 1, side = rr & 1;
+                const double* lv = sops + 2 * N * N + side * N;
+                double w[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) w[k] = 0.0;
+                for (int pos = 0; pos < N; ++pos) {
+                    int j = elp * NPE + tp_node<DIM>(N, dir, line, pos);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) w[k] = fma(lv[pos], sW[k * NN + j], w[k]);
+                }
+                // vars_entropy2prim, FlouCommon/Euler.jl:309-334, then vars_prim2cons
+                double wl = w[DIM + 1], iwl = 1.0 / wl;
+                double vp[DIM], qp[NV], vv = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) {
+                    vp[k] = -w[1 + k] * iwl;
+                    vv = fma(vp[k], vp[k], vv);
+                }
+                double sv = g - (g - 1.0) * (w[0] - wl * vv * 0.5);
+                double pp = pow(pow(-wl, g) * exp(sv), 1.0 / (1.0 - g));
+                double rho = -pp * wl;
+                qp[0] = rho;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) qp[1 + k] = rho * vp[k];
+                qp[DIM + 1] = pp / (g - 1.0) + 0.5 * rho * vv;
+                if (!(rho > 0.0 && pp > 0.0)) raise_nonphysical(P.status, e0 + elp);
+                store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, vv, 1.0 / rho);
+            }
+            __syncthreads();
+        }
         if (CURV) {   // this direction's metric column Ja[:, dir] of every node of the block
             if (active) {
                 int64_t g = (int64_t)e * NPE + i;
@@ -966,15 +1021,26 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             }
             __syncthreads();
         }
-        // ---- pair phase: every symmetric two-point flux of the block, once ----
-        for (int kp = tid; kp < NPT; kp += blockDim.x) {
-            int elp = kp / (NFD * NPAIR);
-            int r = kp - elp * (NFD * NPAIR);
-            int line = r / NPAIR, pr = r - line * NPAIR;
-            if (e0 + elp >= P.nelem) continue;
-            int a = stab[2 * pr], b = stab[2 * pr + 1];
-            int ia = elp * NPE + tp_node<DIM>(N, dir, line, a);
-            int ib = elp * NPE + tp_node<DIM>(N, dir, line, b);
+        // ---- pair phase: every symmetric two-point flux of the block, once (GAUSS: then every
+        // node with both projected states of its line) ----
+        for (int kp = tid; kp < NPTX; kp += blockDim.x) {
+            int elp, ia, ib;
+            if (kp < NPT) {
+                elp = kp / (NFD * NPAIR);
+                int r = kp - elp * (NFD * NPAIR);
+                int line = r / NPAIR, pr = r - line * NPAIR;
+                if (e0 + elp >= P.nelem) continue;
+                int a = stab[2 * pr], b = stab[2 * pr + 1];
+                ia = elp * NPE + tp_node<DIM>(N, dir, line, a);
+                ib = elp * NPE + tp_node<DIM>(N, dir, line, b);
+            } else {   // x = 2 (N (elp NFD + line) + pos) + side
+                int x = kp - NPT, side = x & 1, rest = x >> 1;
+                int pos = rest % N, ln = rest / N;
+                elp = ln / NFD;
+                if (e0 + elp >= P.nelem) continue;
+                ia = elp * NPE + tp_node<DIM>(N, dir, ln - elp * NFD, pos);
+                ib = NN + 2 * ln + side;
+            }
             double F[NV];
             double nv[DIM];   // CURV: the averaged metric column (Ja_a + Ja_b)/2
             if (CURV) {
@@ -983,16 +1049,16 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             }
             if constexpr (CURV && EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
-                    chandrashekar_pair<DIM, true>(sprim, NN, ia, ib, dir, c_beta, F, nv);
+                    chandrashekar_pair<DIM, true>(sprim, SST, ia, ib, dir, c_beta, F, nv);
                 } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
-                    const double* vh = sprim + NN;
+                    const double* vh = sprim + SST;
                     double rho = sprim[ia] + sprim[ib];
-                    double pm = sprim[(1 + DIM) * NN + ia] + sprim[(1 + DIM) * NN + ib];
-                    double en = sprim[(2 + DIM) * NN + ia] + sprim[(2 + DIM) * NN + ib];
+                    double pm = sprim[(1 + DIM) * SST + ia] + sprim[(1 + DIM) * SST + ib];
+                    double en = sprim[(2 + DIM) * SST + ia] + sprim[(2 + DIM) * SST + ib];
                     double vm[DIM], vn = 0.0;
 #pragma unroll
                     for (int k = 0; k < DIM; ++k) {
-                        vm[k] = vh[k * NN + ia] + vh[k * NN + ib];
+                        vm[k] = vh[k * SST + ia] + vh[k * SST + ib];
                         vn = fma(vm[k], nv[k], vn);
                     }
                     double m = rho * vn;
@@ -1001,21 +1067,21 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, vm[k], pm * nv[k]);
                     F[DIM + 1] = fma(m, en, pm * vn);
                 } else {   // StdAverage: the mean of the two contravariant fluxes
-                    const double* sq = sprim + (DIM + 1) * NN;
+                    const double* sq = sprim + (DIM + 1) * SST;
                     double v1 = 0.0, v2 = 0.0, m1 = 0.0, m2 = 0.0;
 #pragma unroll
                     for (int k = 0; k < DIM; ++k) {
-                        v1 = fma(sprim[k * NN + ia], nv[k], v1);
-                        v2 = fma(sprim[k * NN + ib], nv[k], v2);
-                        m1 = fma(sq[(1 + k) * NN + ia], nv[k], m1);
-                        m2 = fma(sq[(1 + k) * NN + ib], nv[k], m2);
+                        v1 = fma(sprim[k * SST + ia], nv[k], v1);
+                        v2 = fma(sprim[k * SST + ib], nv[k], v2);
+                        m1 = fma(sq[(1 + k) * SST + ia], nv[k], m1);
+                        m2 = fma(sq[(1 + k) * SST + ib], nv[k], m2);
                     }
-                    double p1 = sprim[DIM * NN + ia], p2 = sprim[DIM * NN + ib];
+                    double p1 = sprim[DIM * SST + ia], p2 = sprim[DIM * SST + ib];
                     F[0] = (m1 + m2) * 0.5;
 #pragma unroll
                     for (int k = 0; k < DIM; ++k)
-                        F[1 + k] = (fma(sq[(1 + k) * NN + ia], v1, p1 * nv[k]) + fma(sq[(1 + k) * NN + ib], v2, p2 * nv[k])) * 0.5;
-                    F[DIM + 1] = ((sq[(DIM + 1) * NN + ia] + p1) * v1 + (sq[(DIM + 1) * NN + ib] + p2) * v2) * 0.5;
+                        F[1 + k] = (fma(sq[(1 + k) * SST + ia], v1, p1 * nv[k]) + fma(sq[(1 + k) * SST + ib], v2, p2 * nv[k])) * 0.5;
+                    F[DIM + 1] = ((sq[(DIM + 1) * SST + ia] + p1) * v1 + (sq[(DIM + 1) * SST + ib] + p2) * v2) * 0.5;
                 }
             } else if constexpr (CURV) {   // linear advection (LinearAdvection.jl:44-47)
                 double an = 0.0;
@@ -1024,30 +1090,30 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 F[0] = an * (sprim[ia] + sprim[ib]) * 0.5;
             } else if (EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
-                    chandrashekar_pair<DIM>(sprim, NN, ia, ib, dir, c_beta, F);
+                    chandrashekar_pair<DIM>(sprim, SST, ia, ib, dir, c_beta, F);
                 } else if (TP == FLOU_TP_KENNEDY_GRUBER) {   // Kennedy & Gruber (2008)
-                    const double* vh = sprim + NN;
+                    const double* vh = sprim + SST;
                     double rho = sprim[ia] + sprim[ib];
-                    double pm = sprim[(1 + DIM) * NN + ia] + sprim[(1 + DIM) * NN + ib];
-                    double en = sprim[(2 + DIM) * NN + ia] + sprim[(2 + DIM) * NN + ib];
-                    double vd = vh[dir * NN + ia] + vh[dir * NN + ib];
+                    double pm = sprim[(1 + DIM) * SST + ia] + sprim[(1 + DIM) * SST + ib];
+                    double en = sprim[(2 + DIM) * SST + ia] + sprim[(2 + DIM) * SST + ib];
+                    double vd = vh[dir * SST + ia] + vh[dir * SST + ib];
                     double m = rho * vd;
                     F[0] = m;
 #pragma unroll
-                    for (int k = 0; k < DIM; ++k) F[1 + k] = m * (vh[k * NN + ia] + vh[k * NN + ib]);
+                    for (int k = 0; k < DIM; ++k) F[1 + k] = m * (vh[k * SST + ia] + vh[k * SST + ib]);
                     F[1 + dir] = F[1 + dir] + pm;
                     F[DIM + 1] = fma(m, en, pm * vd);
                 } else {   // StdAverage two-point flux, Euler.jl:385-472
-                    const double* sq = sprim + (DIM + 1) * NN;
-                    double v1 = sprim[dir * NN + ia], v2 = sprim[dir * NN + ib];
-                    double p1 = sprim[DIM * NN + ia], p2 = sprim[DIM * NN + ib];
-                    F[0] = (sq[(1 + dir) * NN + ia] + sq[(1 + dir) * NN + ib]) * 0.5;
+                    const double* sq = sprim + (DIM + 1) * SST;
+                    double v1 = sprim[dir * SST + ia], v2 = sprim[dir * SST + ib];
+                    double p1 = sprim[DIM * SST + ia], p2 = sprim[DIM * SST + ib];
+                    F[0] = (sq[(1 + dir) * SST + ia] + sq[(1 + dir) * SST + ib]) * 0.5;
 #pragma unroll
                     for (int k = 0; k < DIM; ++k) {
-                        double m1 = sq[(1 + k) * NN + ia] * v1, m2 = sq[(1 + k) * NN + ib] * v2;
+                        double m1 = sq[(1 + k) * SST + ia] * v1, m2 = sq[(1 + k) * SST + ib] * v2;
                         F[1 + k] = (k == dir) ? (((m1 + p1) + m2) + p2) * 0.5 : (m1 + m2) * 0.5;
                     }
-                    F[DIM + 1] = ((sq[(DIM + 1) * NN + ia] + p1) * v1 + (sq[(DIM + 1) * NN + ib] + p2) * v2) * 0.5;
+                    F[DIM + 1] = ((sq[(DIM + 1) * SST + ia] + p1) * v1 + (sq[(DIM + 1) * SST + ib] + p2) * v2) * 0.5;
                 }
             } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
                 F[0] = P.adv[dir] * (sprim[ia] + sprim[ib]) * 0.5;
@@ -1055,7 +1121,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 F[0] = (sprim[ia] * sprim[ia] + sprim[ib] * sprim[ib]) * 0.25;
             }
 #pragma unroll
-            for (int k = 0; k < NV; ++k) spair[k * NPT + kp] = F[k];
+            for (int k = 0; k < NV; ++k) spair[k * NPTX + kp] = F[k];
         }
         __syncthreads();
         // ---- node phase: dQ_i -= Ja_dd sum_j D♯_ij F♯(i, j) ----
@@ -1108,15 +1174,58 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
                     int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPT + pidx], acc[k]);
+                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPTX + pidx], acc[k]);
                 }
             }
             double Ja = CURV ? 1.0 : P.elem_Ja[e * DIM + dir];   // CURV: the metric is in the fluxes
+            double Fl[NV], Fr[NV];   // GAUSS: F♯(Q_i, Q̃) - l·F♯(·, Q̃) at both ends (OpDivergence.jl:410-425)
+            if constexpr (GAUSS) {
+                const double* lvl = sops + 2 * N * N;
+                const double* lvr = lvl + N;
+                const int xb = NPT + 2 * N * (el * NFD + line);
+                double lF[NV], rF[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) lF[k] = rF[k] = 0.0;
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) {
+                        lF[k] = fma(lvl[j], spair[k * NPTX + xb + 2 * j], lF[k]);
+                        rF[k] = fma(lvr[j], spair[k * NPTX + xb + 2 * j + 1], rF[k]);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    Fl[k] = spair[k * NPTX + xb + 2 * pos] - lF[k];
+                    Fr[k] = spair[k * NPTX + xb + 2 * pos + 1] - rF[k];
+                }
+            }
             if constexpr (HYB) {
                 double w = P.omega1[pos] * Ja;
+                if constexpr (GAUSS) {   // F̄_{p+1} - F̄_p, OpDivergence.jl:747-751
+                    const double* lvl = sops + 2 * N * N;
+                    const double* lvr = lvl + N;
+                    int32_t pl = P.elem_face[e * 2 * DIM + 2 * dir], pr = P.elem_face[e * 2 * DIM + 2 * dir + 1];
+                    double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
+                    int64_t ol = (int64_t)(pl >> 1) * NFD + line, orr = (int64_t)(pr >> 1) * NFD + line;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) sH[k * NN + tid] = w * acc[k];
+                    for (int k = 0; k < NV; ++k) {
+                        fls[k] = sl * __ldcg(P.Fn + k * P.nfdofs + ol);
+                        frs[k] = sr * __ldcg(P.Fn + k * P.nfdofs + orr);
+                        sH[k * NN + tid] = w * acc[k] - lvl[pos] * fma(Ja, Fl[k], -fls[k]) +
+                                           lvr[pos] * fma(Ja, Fr[k], frs[k]);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) sH[k * NN + tid] = w * acc[k];
+                }
             } else {
+                if constexpr (GAUSS) {
+                    const double* dgl = sops + 2 * N * N + 2 * N;
+                    const double* dgr = dgl + N;
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] = acc[k] - (dgl[pos] * Fl[k] - dgr[pos] * Fr[k]);
+                }
 #pragma unroll
                 for (int k = 0; k < NV; ++k) dq[k] = fma(-Ja, acc[k], dq[k]);
             }
@@ -1131,10 +1240,12 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     double Fh[NV];
 #pragma unroll
                     for (int k = 0; k < NV; ++k) Fh[k] = 0.0;
-                    for (int r = 0; r < pos; ++r) {
-                        int j = el * NPE + tp_node<DIM>(N, dir, line, r);
+                    if constexpr (!GAUSS) {
+                        for (int r = 0; r < pos; ++r) {
+                            int j = el * NPE + tp_node<DIM>(N, dir, line, r);
 #pragma unroll
-                        for (int k = 0; k < NV; ++k) Fh[k] += sH[k * NN + j];
+                            for (int k = 0; k < NV; ++k) Fh[k] += sH[k * NN + j];
+                        }
                     }
                     // FV flux in the frame of the positive axis, times the subcell surface
                     // Jacobian (PhysicalRegions.jl:68-148: Ja_dd of the Cartesian element)
@@ -1158,32 +1269,71 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     Fv[DIM + 1] = Fr[DIM + 1] * Js;
 #pragma unroll
                     for (int r = 0; r < DIM; ++r) Fv[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]) * Js;
-                    double bb = 0.0;
+                    if constexpr (GAUSS) {   // blended in the scan below
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + tid] - sW[k * NN + il], Fh[k] - Fv[k], bb);
-                    double dl = sqrt(fma(bb, bb, P.blend));
-                    dl = fmax((dl - bb) / dl, 0.5);
+                        for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = Fv[k];
+                    } else {
+                        double bb = 0.0;
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = fma(dl, Fh[k] - Fv[k], Fv[k]);
+                        for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + tid] - sW[k * NN + il], Fh[k] - Fv[k], bb);
+                        double dl = sqrt(fma(bb, bb, P.blend));
+                        dl = fmax((dl - bb) / dl, 0.5);
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = fma(dl, Fh[k] - Fv[k], Fv[k]);
+                    }
                 }
             }
             __syncthreads();
+            if constexpr (GAUSS) {
+                // On Gauss nodes each subcell flux starts from the blended one before it
+                // (OpDivergence.jl:741-769): F̄_1 = -Fn_left, F̄_{p+1} = blend(F̄_p + increment_p).
+                // One thread per line runs the scan over the FV fluxes left in sFb.
+                if (active) {
+                    int pos, line;
+                    tp_coords<DIM>(N, i, dir, pos, line);
+                    if (pos == 0) {
+                        double Fb[NV];
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) Fb[k] = -fls[k];
+                        int jp = tid;
+                        for (int pp = 1; pp < N; ++pp) {
+                            const int jn = el * NPE + tp_node<DIM>(N, dir, line, pp);
+                            double bb = 0.0;
+#pragma unroll
+                            for (int k = 0; k < NV; ++k) {
+                                Fb[k] += sH[k * NN + jp];
+                                bb = fma(sW[k * NN + jn] - sW[k * NN + jp], Fb[k] - sFb[k * NN + jn], bb);
+                            }
+                            double dl = sqrt(fma(bb, bb, P.blend));
+                            dl = fmax((dl - bb) / dl, 0.5);
+#pragma unroll
+                            for (int k = 0; k < NV; ++k) {
+                                double fv = sFb[k * NN + jn];
+                                Fb[k] = fma(dl, Fb[k] - fv, fv);
+                                sFb[k * NN + jn] = Fb[k];
+                            }
+                            jp = jn;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
             if (active) {
                 int pos, line;
                 tp_coords<DIM>(N, i, dir, pos, line);
                 double iw = 1.0 / P.omega1[pos];
                 int jr = (pos < N - 1) ? el * NPE + tp_node<DIM>(N, dir, line, pos + 1) : -1;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    double fl = pos > 0 ? sFb[k * NN + tid] : 0.0;
-                    double fr = jr >= 0 ? sFb[k * NN + jr] : 0.0;
+                for (int k = 0; k < NV; ++k) {   // GAUSS: the element's face fluxes close both ends
+                    double fl = pos > 0 ? sFb[k * NN + tid] : (GAUSS ? -fls[k] : 0.0);
+                    double fr = jr >= 0 ? sFb[k * NN + jr] : (GAUSS ? frs[k] : 0.0);
                     dq[k] += (fl - fr) * iw;
                 }
             }
         }
         __syncthreads();
     }
-    if (active) surface_and_update<DIM, N, NV, LGL, CURV>(P, sops, e, i, q, dq);
+    if (active) surface_and_update<DIM, N, NV, LGL, CURV, !(GAUSS && HYB)>(P, sops, e, i, q, dq);
 }
 
 template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false, bool HYB = false>
@@ -1192,15 +1342,18 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemPa
     split_tile<DIM, N, EQ, TP, LGL, 256, CURV, HYB>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
-template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256, bool CURV = false>
+template <int DIM, int N, int EQ, int VOL, int TP, int TB = 256, bool CURV = false, bool LGL = true>
 constexpr size_t elem_smem_bytes() {
     using S = Shape<DIM, N, TB>;
     constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
     constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;
     constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
-    return sizeof(double) * (S::NOPS + NARR * S::NN + NV * NPT + (CURV ? DIM * S::NN : 0) +
-                             (VOL == FLOU_OP_HYBRID ? 3 * NV * S::NN : 0)) + 2 * (S::NPAIR + 1);
+    constexpr bool GAUSS = !LGL && EQ == FLOU_EQ_EULER && !CURV;
+    constexpr int NPROJ = GAUSS ? 2 * S::EPB * S::NFD : 0;
+    constexpr bool HYB = VOL == FLOU_OP_HYBRID;
+    return sizeof(double) * (S::NOPS + NARR * (S::NN + NPROJ) + NV * (NPT + NPROJ * N) + (CURV ? DIM * S::NN : 0) +
+                             (HYB ? 3 * NV * S::NN : (GAUSS ? NV * S::NN : 0))) + 2 * (S::NPAIR + 1);
 }
 
 // Launch one instantiation; the dynamic shared-memory opt-in is set once per kernel.
@@ -1208,7 +1361,8 @@ constexpr size_t elem_smem_bytes() {
 template <int DIM, int N, int EQ, int VOL, int TP, bool LGL, bool CURV = false>
 cudaError_t launch_elem_one(const ElemParams& P, cudaStream_t s, bool prepare) {
     using S = Shape<DIM, N>;
-    constexpr size_t smem = elem_smem_bytes<DIM, N, EQ, VOL, TP, 256, CURV>();
+    constexpr size_t smem = elem_smem_bytes<DIM, N, EQ, VOL, TP, 256, CURV, LGL>();
+    static_assert(smem <= 227 * 1024, "element tile exceeds the shared memory of one block");
     static bool attr_set = false;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
     auto k = (VOL == FLOU_OP_STRONG) ? (void (*)(ElemParams))elem_strong_kernel<DIM, N, EQ, LGL, CURV>
@@ -1281,6 +1435,34 @@ cudaError_t launch_elem_dim(int n, int vol, int tp, bool lgl, const ElemParams& 
     }
 }
 
+// Gauss-node split and hybrid variants (Euler, Cartesian), one per two-point flux.
+template <int DIM, int N, int VOL>
+cudaError_t launch_elem_gauss_n(int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (tp) {
+        case FLOU_TP_STD_AVERAGE:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, VOL, FLOU_TP_STD_AVERAGE, false>(P, s, prep);
+        case FLOU_TP_CHANDRASHEKAR:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, VOL, FLOU_TP_CHANDRASHEKAR, false>(P, s, prep);
+        case FLOU_TP_KENNEDY_GRUBER:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, VOL, FLOU_TP_KENNEDY_GRUBER, false>(P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int DIM, int VOL>
+cudaError_t launch_elem_gauss_dim(int n, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (n) {
+        case 2: return launch_elem_gauss_n<DIM, 2, VOL>(tp, P, s, prep);
+        case 3: return launch_elem_gauss_n<DIM, 3, VOL>(tp, P, s, prep);
+        case 4: return launch_elem_gauss_n<DIM, 4, VOL>(tp, P, s, prep);
+        case 5: return launch_elem_gauss_n<DIM, 5, VOL>(tp, P, s, prep);
+        case 6: return launch_elem_gauss_n<DIM, 6, VOL>(tp, P, s, prep);
+        case 7: return launch_elem_gauss_n<DIM, 7, VOL>(tp, P, s, prep);
+        case 8: return launch_elem_gauss_n<DIM, 8, VOL>(tp, P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 // Curvilinear variants (LGL only): strong form and split form per two-point flux.
 template <int DIM, int N, int EQ>
 cudaError_t launch_elem_n_curv(int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
@@ -1328,6 +1510,10 @@ cudaError_t launch_elem_euler3d_strong(const ElemLaunch& L, const ElemParams& P,
 cudaError_t launch_elem_euler3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler3d_hybrid(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_scalar(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_gauss1d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_gauss2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_gauss3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_gauss3d_hybrid(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s);
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 

@@ -664,6 +664,25 @@ template <class T> inline Vec<T> cons2entropy(const Vec<T>& Q, int dim, double g
     return W;
 }
 
+// vars_entropy2cons = vars_prim2cons ∘ vars_entropy2prim, src/FlouCommon/Euler.jl:309-339.
+template <class T> inline Vec<T> entropy2cons(const Vec<T>& W, int dim, double g) {
+    using std::exp; using std::pow;
+    T wl = W[dim + 1];
+    T u[3], u2 = T(0.0);
+    for (int k = 0; k < dim; ++k) {
+        u[k] = -W[1 + k] / wl;
+        u2 = u2 + sq(u[k]);
+    }
+    T s = g - (g - 1.0) * (W[0] - wl * u2 / 2.0);
+    T p = pow(pow(-wl, g) * exp(s), 1.0 / (1.0 - g));
+    T rho = -p * wl;
+    Vec<T> Q{};
+    Q[0] = rho;
+    for (int k = 0; k < dim; ++k) Q[1 + k] = rho * u[k];
+    Q[dim + 1] = p / (g - 1.0) + rho * u2 / 2.0;
+    return Q;
+}
+
 template <class T> inline Vec<T> euler_average(const Vec<T>& Ql, const Vec<T>& Qr, int dim, double g, int avg) {
     return avg == NF_CHANDRASHEKAR ? euler_chandrashekar(Ql, Qr, dim, g) : euler_stdavg(Ql, Qr, dim, g);
 }
@@ -897,6 +916,7 @@ struct Disc {
     // operators (n x n column-major)
     std::vector<double> Ds, Dsharp, ll, lr, dgl, dgr;
     std::vector<double> D, omega1d;       // derivative matrix, 1D weights (HybridDivOperator)
+    bool lobatto = true;                  // hasboundaries(basis): l_l, l_r pick the end nodes
     // connectivity (1-based, like the reference)
     std::vector<int> faceinds, facepos;   // nelem * 2dim
     std::vector<int> eleminds, elempos;   // nfaces * 2
@@ -972,6 +992,72 @@ template <class T> inline Vec<T> apply_bc(const Bc& bc, const Vec<T>& Qin, const
 // rhs!, src/FlouSpatial/Equations/Hyperbolic.jl:31-69 (steps C1-C8, in order).
 // `celem` (optional): per-element scale c_e of the LxF dissipation; a face uses
 // intensity = (c_1 + c_2)/2 of its two elements (c_1 on boundary faces).  c = 1 is LxF(., 1.0).
+// Frame of the subgrid interfaces of a Cartesian element along `dir` (PhysicalRegions.jl:68-148):
+// the positive axis, completed like the face frames of the reference.
+inline Frame subgrid_frame(int dim, int dir) {
+    Frame fr{};
+    if (dim == 1) { fr.n[0] = 1; }
+    else if (dim == 2) {
+        if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; } else { fr.n[1] = 1; fr.t[0] = -1; }
+    } else {
+        if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; fr.b[2] = 1; }
+        else if (dir == 1) { fr.n[1] = 1; fr.t[2] = 1; fr.b[0] = 1; }
+        else { fr.n[2] = 1; fr.t[0] = 1; fr.b[1] = 1; }
+    }
+    return fr;
+}
+
+// _hybrid_compute_delta, OpDivergence.jl:781-801 (Fisher's indicator, limited at 0.5)
+template <class T> inline T hybrid_delta(const T& b, double c) {
+    using std::sqrt; using std::max;
+    T dl = sqrt(b * b + c);
+    dl = (dl - b) / dl;
+    return max(dl, T(0.5));
+}
+
+// _flux_splitdiv_nb_tensorproduct!, OpDivergence.jl:382-427, on one line of direction `dir`:
+// Fl[ii], Fr[ii] for the line's nodes from the entropy-projected boundary states, with the
+// line's interface fluxes Fnl, Fnr (this element's sides).  Cartesian subgrid: nl = nr = the
+// positive axis times Js.
+template <class T>
+void splitdiv_nb_line(const Disc& g, const T* Q, long base, int dir, int line, const std::vector<Vec<T>>& W,
+                      const Vec<T>& Fnl, const Vec<T>& Fnr, std::vector<Vec<T>>& Fl, std::vector<Vec<T>>& Fr) {
+    const Config& c = g.cfg;
+    const int dim = c.dim, n = g.n, nv = c.nv;
+    const long nd = g.ndofs();
+    Frame fr = subgrid_frame(dim, dir);
+    double Js = g.Ja[base * dim * dim + dir + dir * dim];
+    double nl[3], nr[3];
+    for (int k = 0; k < 3; ++k) { nl[k] = fr.n[k] * Js; nr[k] = fr.n[k] * Js; }
+    Vec<T> Wl{}, Wr{};
+    for (int ii = 0; ii < n; ++ii) {
+        int i = tp_node(dim, n, dir, line, ii);
+        for (int q = 0; q < nv; ++q) {
+            Wl[q] = Wl[q] + g.ll[ii] * W[i][q];
+            Wr[q] = Wr[q] + g.lr[ii] * W[i][q];
+        }
+    }
+    Vec<T> Ql = entropy2cons(Wl, dim, c.gamma), Qr = entropy2cons(Wr, dim, c.gamma);
+    for (int ii = 0; ii < n; ++ii) {
+        int i = tp_node(dim, n, dir, line, ii);
+        Vec<T> Qi = getv(Q, nd, base + i, nv);
+        const double* Jai = &g.Ja[(base + i) * dim * dim + dir * dim];
+        Fl[ii] = twopointflux(Qi, Ql, Jai, nl, c);
+        Fr[ii] = twopointflux(Qi, Qr, Jai, nr, c);
+    }
+    Vec<T> lF{}, rF{};
+    for (int ii = 0; ii < n; ++ii)
+        for (int q = 0; q < nv; ++q) {
+            lF[q] = lF[q] + g.ll[ii] * Fl[ii][q];
+            rF[q] = rF[q] + g.lr[ii] * Fr[ii][q];
+        }
+    for (int ii = 0; ii < n; ++ii)
+        for (int q = 0; q < nv; ++q) {
+            Fl[ii][q] = Fl[ii][q] - (lF[q] + Fnl[q]);
+            Fr[ii][q] = Fr[ii][q] - (rF[q] - Fnr[q]);
+        }
+}
+
 template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Workspace<T>& ws,
                             const T* celem = nullptr) {
     (void)time;
@@ -1030,7 +1116,9 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                 Ft[i * dim + d] = r;
             }
         }
-        if (c.volop == OP_HYBRID) {
+        if (c.volop == OP_HYBRID && !g.lobatto) {
+            // Gauss nodes: "everything as a surface contribution" (OpDivergence.jl:485-490)
+        } else if (c.volop == OP_HYBRID) {
             // _vol_hybrid_tensorproduct!, OpDivergence.jl:553-604, with the Cartesian subgrid of
             // PhysicalRegions.jl:68-148 (frames along the positive axes, Js the face Jacobian)
             using std::sqrt; using std::max;
@@ -1040,15 +1128,7 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
             fv.lxf_avg = c.fvavg;
             std::vector<Vec<T>> Fb(n + 1);
             for (int dir = 0; dir < dim; ++dir) {
-                Frame fr{};
-                if (dim == 1) { fr.n[0] = 1; }
-                else if (dim == 2) {
-                    if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; } else { fr.n[1] = 1; fr.t[0] = -1; }
-                } else {
-                    if (dir == 0) { fr.n[0] = 1; fr.t[1] = 1; fr.b[2] = 1; }
-                    else if (dir == 1) { fr.n[1] = 1; fr.t[2] = 1; fr.b[0] = 1; }
-                    else { fr.n[2] = 1; fr.t[0] = 1; fr.b[1] = 1; }
-                }
+                Frame fr = subgrid_frame(dim, dir);
                 double Js = g.Ja[base * dim * dim + dir + dir * dim];
                 for (int line = 0; line < nfd; ++line) {
                     for (int ii = 0; ii <= n; ++ii) Fb[ii] = Vec<T>{};
@@ -1072,10 +1152,7 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                         for (int q = 0; q < nv; ++q) Fv[q] = Fv[q] * Js;
                         T bb = T(0.0);
                         for (int q = 0; q < nv; ++q) bb = bb + (W[i][q] - W[il][q]) * (Fb[ii][q] - Fv[q]);
-                        // _hybrid_compute_delta, OpDivergence.jl:777-801 (Fisher's, limited at 0.5)
-                        T dl = sqrt(bb * bb + c.blend);
-                        dl = (dl - bb) / dl;
-                        dl = max(dl, T(0.5));
+                        T dl = hybrid_delta(bb, c.blend);
                         for (int q = 0; q < nv; ++q) Fb[ii][q] = (1.0 - dl) * Fv[q] + dl * Fb[ii][q];
                     }
                     for (int ii = 0; ii < n; ++ii) {
@@ -1172,10 +1249,89 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
         }
     }
 
-    // 6. surface_contribution! -> _reconstruction_tensorproduct!, OpDivergence.jl:42-100
+    // 6. surface_contribution! -> _reconstruction_tensorproduct!, OpDivergence.jl:42-100, or on
+    // Gauss nodes the entropy-projected split form (:284-437) / hybrid form (:614-780)
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < g.nelem; ++e) {
         long base = (long)e * npe;
+        if (!g.lobatto && (c.volop == OP_SPLIT || c.volop == OP_HYBRID)) {
+            std::vector<Vec<T>> W(npe), Fl(n), Fr(n), Fs(n * npe), Fb(n + 1);
+            for (int i = 0; i < npe; ++i) W[i] = cons2entropy(getv(Q, nd, base + i, nv), dim, c.gamma);
+            Config fv = c;
+            fv.lxf_avg = c.fvavg;
+            for (int dir = 0; dir < dim; ++dir) {
+                int fl = g.faceinds[e * 2 * dim + 2 * dir] - 1, sl = g.facepos[e * 2 * dim + 2 * dir] - 1;
+                int fr = g.faceinds[e * 2 * dim + 2 * dir + 1] - 1, sr = g.facepos[e * 2 * dim + 2 * dir + 1] - 1;
+                if (c.volop == OP_HYBRID) {   // _flux_splitdiv_tensorproduct!: F♯ of every line
+                    for (int line = 0; line < nfd; ++line)
+                        for (int ii = 0; ii < n; ++ii) {
+                            int i = tp_node(dim, n, dir, line, ii);
+                            Vec<T> Qi = getv(Q, nd, base + i, nv);
+                            const double* Jai = &g.Ja[(base + i) * dim * dim + dir * dim];
+                            std::array<Vec<T>, 3> F;
+                            for (int d = 0; d < dim; ++d) F[d] = volumeflux(Qi, d, c);
+                            Vec<T> Ft{};
+                            for (int k = 0; k < nv; ++k) {
+                                T acc = F[0][k] * Jai[0];
+                                for (int q = 1; q < dim; ++q) acc = acc + F[q][k] * Jai[q];
+                                Ft[k] = acc;
+                            }
+                            Fs[ii + n * i] = Ft;
+                            for (int il = ii + 1; il < n; ++il) {
+                                int l = tp_node(dim, n, dir, line, il);
+                                const double* Jal = &g.Ja[(base + l) * dim * dim + dir * dim];
+                                Vec<T> F2 = twopointflux(Qi, getv(Q, nd, base + l, nv), Jai, Jal, c);
+                                Fs[il + n * i] = F2;
+                                Fs[ii + n * l] = F2;
+                            }
+                        }
+                }
+                Frame sfr = subgrid_frame(dim, dir);
+                double Js = g.Ja[base * dim * dim + dir + dir * dim];
+                for (int line = 0; line < nfd; ++line) {
+                    Vec<T> Fnl = getv(ws.Fn[sl].data(), nf, (long)fl * nfd + line, nv);
+                    Vec<T> Fnr = getv(ws.Fn[sr].data(), nf, (long)fr * nfd + line, nv);
+                    splitdiv_nb_line(g, Q, base, dir, line, W, Fnl, Fnr, Fl, Fr);
+                    if (c.volop == OP_SPLIT) {   // _surf_splitdiv_nb_tensorproduct!, :429-437
+                        for (int ii = 0; ii < n; ++ii) {
+                            int i = tp_node(dim, n, dir, line, ii);
+                            for (int k = 0; k < nv; ++k) {
+                                T& y = dQ[k * nd + base + i];
+                                y = y + (g.dgl[ii] * Fl[ii][k] - g.dgr[ii] * Fr[ii][k]);
+                            }
+                        }
+                        continue;
+                    }
+                    // _surf_hybrid_nb_tensorproduct!, :732-779
+                    for (int k = 0; k < nv; ++k) { Fb[0][k] = -Fnl[k]; Fb[n][k] = Fnr[k]; }
+                    for (int ii = 0; ii < n - 1; ++ii) {
+                        int i = tp_node(dim, n, dir, line, ii), ir = tp_node(dim, n, dir, line, ii + 1);
+                        Vec<T> sum{};
+                        for (int j = 0; j < n; ++j)
+                            for (int k = 0; k < nv; ++k) sum[k] = sum[k] + g.Dsharp[ii + j * n] * Fs[j + n * i][k];
+                        for (int k = 0; k < nv; ++k)
+                            Fb[ii + 1][k] = Fb[ii][k] + sum[k] * g.omega1d[ii] - g.ll[ii] * Fl[ii][k] +
+                                            g.lr[ii] * Fr[ii][k];
+                        Vec<T> Qln = rotate2face(getv(Q, nd, base + i, nv), sfr, c);
+                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + ir, nv), sfr, c);
+                        Vec<T> Fv = rotate2phys(numericalflux(Qln, Qrn, sfr.n, fv, c.fvflux, T(c.fvintensity)), sfr, c);
+                        for (int k = 0; k < nv; ++k) Fv[k] = Fv[k] * Js;
+                        T bb = T(0.0);
+                        for (int k = 0; k < nv; ++k) bb = bb + (W[ir][k] - W[i][k]) * (Fb[ii + 1][k] - Fv[k]);
+                        T dl = hybrid_delta(bb, c.blend);
+                        for (int k = 0; k < nv; ++k) Fb[ii + 1][k] = (1.0 - dl) * Fv[k] + dl * Fb[ii + 1][k];
+                    }
+                    for (int ii = 0; ii < n; ++ii) {
+                        int i = tp_node(dim, n, dir, line, ii);
+                        for (int k = 0; k < nv; ++k) {
+                            T& y = dQ[k * nd + base + i];
+                            y = y + (Fb[ii][k] - Fb[ii + 1][k]) / g.omega1d[ii];
+                        }
+                    }
+                }
+            }
+            continue;
+        }
         for (int dir = 0; dir < dim; ++dir) {
             int fl = g.faceinds[e * 2 * dim + 2 * dir] - 1, sl = g.facepos[e * 2 * dim + 2 * dir] - 1;
             int fr = g.faceinds[e * 2 * dim + 2 * dir + 1] - 1, sr = g.facepos[e * 2 * dim + 2 * dir + 1] - 1;

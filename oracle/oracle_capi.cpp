@@ -41,6 +41,8 @@ static inline bool operator<=(CD a, double b) { g_count.cmp++; return a.v <= b; 
 static inline CD sqrt(CD a) { g_count.sqrt++; return CD(std::sqrt(a.v)); }
 static inline CD log(CD a) { g_count.log++; return CD(std::log(a.v)); }
 static inline CD fabs(CD a) { return CD(std::fabs(a.v)); }
+static inline CD exp(CD a) { g_count.log++; return CD(std::exp(a.v)); }
+static inline CD pow(CD a, double b) { g_count.log++; return CD(std::pow(a.v, b)); }
 namespace std {
 static inline CD min(CD a, CD b) { g_count.cmp++; return a.v < b.v ? a : b; }
 static inline CD max(CD a, CD b) { g_count.cmp++; return a.v < b.v ? b : a; }
@@ -78,6 +80,8 @@ static inline bool operator<=(Dual a, double b) { return a.v <= b; }
 static inline Dual sqrt(Dual a) { double s = std::sqrt(a.v); return Dual(s, a.d / (2.0 * s)); }
 static inline Dual log(Dual a) { return Dual(std::log(a.v), a.d / a.v); }
 static inline Dual fabs(Dual a) { return std::signbit(a.v) ? -a : a; }
+static inline Dual exp(Dual a) { double e = std::exp(a.v); return Dual(e, e * a.d); }
+static inline Dual pow(Dual a, double b) { double p = std::pow(a.v, b); return Dual(p, b * std::pow(a.v, b - 1.0) * a.d); }
 namespace std {
 static inline Dual min(Dual a, Dual b) { return b.v < a.v ? b : a; }
 static inline Dual max(Dual a, Dual b) { return b.v < a.v ? a : b; }
@@ -252,6 +256,13 @@ void* oracle_disc_new(int dim, int eq, double gamma, const double* adv, int volo
     g.lr.assign(lr, lr + n);
     g.dgl.assign(dgl, dgl + n);
     g.dgr.assign(dgr, dgr + n);
+    // hasboundaries(basis): the end-node interpolation to round-off (operators fitted like the
+    // reference's carry ~1e-16 in the entries that vanish on Gauss-Lobatto nodes)
+    g.lobatto = std::fabs(ll[0] - 1.0) < 1e-10 && std::fabs(lr[n - 1] - 1.0) < 1e-10;
+    for (int i = 0; i < n; ++i) {
+        if (i != 0 && std::fabs(ll[i]) > 1e-10) g.lobatto = false;
+        if (i != n - 1 && std::fabs(lr[i]) > 1e-10) g.lobatto = false;
+    }
     g.faceinds.assign(faceinds, faceinds + nelem * 2 * dim);
     g.facepos.assign(facepos, facepos + nelem * 2 * dim);
     g.eleminds.assign(eleminds, eleminds + nfaces * 2);

@@ -126,6 +126,33 @@ def test_euler_hybrid_operator(dim, n, ne, op):
     _check(disc, _jumpy_state(disc, seed=dim * 5 + n), cfl=0.2)
 
 
+GAUSS_CASES = [
+    (1, 4, (5,), "split_chandra_lxfc"), (1, 5, (4,), "hybrid_md"), (1, 2, (6,), "split_std_lxf"),
+    (2, 4, (3, 3), "split_chandra_chandra"), (2, 5, (3, 2), "split_kg_lxf"), (2, 3, (3, 3), "split_std_lxf"),
+    (2, 4, (3, 3), "hybrid_chandra_hllc_fv"), (2, 6, (2, 2), "hybrid_kg_lxf"), (2, 8, (2, 2), "hybrid_highorder"),
+    (3, 3, (2, 2, 2), "split_chandra_hllc"), (3, 4, (2, 2, 2), "hybrid_chandra_lxfc"),
+    (3, 8, (2, 1, 1), "split_chandra_lxfc"), (3, 8, (1, 1, 2), "hybrid_md"), (3, 5, (2, 2, 1), "split_std_lxf"),
+]
+
+
+@pytest.mark.parametrize("dim,n,ne,op", GAUSS_CASES)
+def test_euler_gauss_nodes(dim, n, ne, op):
+    """Split and hybrid operators on Gauss nodes: the entropy-projected coupling of
+    OpDivergence.jl:301-437 / 614-780, on states whose traces jump."""
+    disc = build(dim, n, ne, _euler(dim), _ops()[op](), basis="GL")
+    _check(disc, _jumpy_state(disc, seed=dim * 11 + n), cfl=0.2)
+
+
+def test_euler_gauss_nodes_walls():
+    eq = _euler(2)
+    Pin = np.array([1.1, 0.0, 0.3, 1.05])
+    bcs = {"1": F.EulerSlipBC(), "2": F.EulerSlipBC(), "3": F.EulerInflowBC(eq.vars_prim2cons(Pin)),
+           "4": F.EulerOutflowBC()}
+    for op in ("split_chandra_md", "hybrid_chandra_lxfc"):
+        disc = build(2, 4, (3, 3), eq, _ops()[op](), periodic=(), bcs=bcs, basis="GL")
+        _check(disc, _jumpy_state(disc, seed=4), cfl=0.2)
+
+
 def test_euler_dissipation_fluxes_walls():
     eq = _euler(2)
     Pin = np.array([1.1, 0.0, 0.3, 1.05])

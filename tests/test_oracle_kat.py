@@ -309,3 +309,51 @@ def test_hybrid_operator_properties(dim):
     P = np.zeros((bl.ndofs, dim + 2))
     P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.3, 0.4, 2.0
     assert np.max(np.abs(o.rhs(np.asfortranarray(eq.vars_prim2cons(P))))) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_gauss_node_split_and_hybrid_properties(dim):
+    """The Gauss-node branches (OpDivergence.jl:301-437, 614-780): entropy-projected boundary
+    states couple the split volume term to the faces.  Conservative and freestream-preserving;
+    the hybrid form with δ -> 1 equals the Gauss split form (the subcell fluxes telescope to the
+    face fluxes by the SBP property of the Gauss operators); with blending it stays conservative."""
+    eq = F.EulerEquation(dim, 1.4)
+    nf = F.LxF(F.ChandrasekharAverage(), 1.0)
+    sp = build(dim, 4, (3,) * dim, eq, F.SplitDivOperator(F.ChandrasekharAverage(), nf), basis="GL")
+    hy = build(dim, 4, (3,) * dim, eq, F.HybridDivOperator(F.ChandrasekharAverage(), nf, 1e30), basis="GL")
+    bl = build(dim, 4, (3,) * dim, eq, F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(), nf, 1e-2),
+               basis="GL")
+    Q = smooth_euler_state(sp, seed=5, amp=0.2)
+    w = np.tile(sp.std.omega, sp.mesh.nelements) * sp.J
+    P = np.zeros((sp.ndofs, dim + 2))
+    P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.3, 0.4, 2.0
+    Qc = np.asfortranarray(eq.vars_prim2cons(P))
+    Rs = oracle_for(sp).rhs(Q)
+    Rh = oracle_for(hy).rhs(Q)
+    assert np.max(np.abs(Rh - Rs)) < 1e-12 * np.max(np.abs(Rs))
+    for d in (sp, bl):
+        o = oracle_for(d)
+        R = o.rhs(Q)
+        for v in range(dim + 2):
+            assert abs(w @ R[:, v]) < 1e-12 * np.sum(w * np.abs(R[:, v]))
+        assert np.max(np.abs(o.rhs(Qc))) < 1e-12
+    assert np.max(np.abs(oracle_for(bl).rhs(Q) - Rs)) > 1e-3 * np.max(np.abs(Rs))   # the blending acts
+
+
+def test_gauss_node_split_convergence():
+    """examples/src/Convergence.jl runs SplitDivOperator(LxF(ChandrasekharAverage(), 1)) on Gauss
+    nodes too: the density wave ρ = 2 + sin(π(x - t)), u = p = 1 on [-1, 1] converges at the
+    design order p + 1 = 4 (CarpenterKennedy2N54, dt small enough not to pollute it)."""
+    eq = F.EulerEquation(1, 1.4)
+    ck = F.CarpenterKennedy2N54()
+    errs = []
+    for ne in (8, 16):
+        d = build(1, 4, (ne,), eq, F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)), basis="GL")
+        x = d.coords[:, 0]
+        exact = lambda t: eq.vars_prim2cons(np.column_stack([2 + np.sin(np.pi * (x - t)), np.ones_like(x),
+                                                            np.ones_like(x)]))
+        tf, nsteps = 0.2, 40 * ne // 8
+        Q = oracle_for(d).lsrk2n(np.asfortranarray(exact(0.0)), tf / nsteps, nsteps, ck.A, ck.B, ck.c)
+        errs.append(np.sqrt(np.mean((Q - exact(tf)) ** 2)))
+    order = np.log2(errs[0] / errs[1])
+    assert order > 3.5, (errs, order)
