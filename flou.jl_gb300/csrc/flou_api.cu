@@ -59,6 +59,11 @@ void drop_graph(flou_ctx* c) {
     c->gexec = nullptr;
     c->graph = nullptr;
     c->g_Q = nullptr;
+    if (c->cfl_exec) cudaGraphExecDestroy(c->cfl_exec);
+    if (c->cfl_graph) cudaGraphDestroy(c->cfl_graph);
+    c->cfl_exec = nullptr;
+    c->cfl_graph = nullptr;
+    c->cfl_Q = nullptr;
 }
 
 int ready(flou_ctx* c) {
@@ -128,6 +133,7 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.a0 = a0;
     P.a1 = a1;
     P.aux = mode == 3 ? const_cast<double*>(Q0) : nullptr;   // the 2N register travels in Q0's slot
+    P.dtp = c->d_gate;
     P.gamma = c->cfg.gamma;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     P.status = c->d_status;
@@ -254,6 +260,32 @@ __global__ void max_dt_kernel(const double* Q, const double* dx, int64_t ndofs, 
             atomicMin(out, (unsigned long long)__double_as_longlong(w));
         }
     }
+}
+
+// Step control of CFL-limited stepping (get_cfl_callback, FlouTime.jl:92-105, with OrdinaryDiffEq
+// landing the last step on tfinal): dt = min(CFL bound, dtmax), cut to tfinal - t; dt = 0 once t
+// has reached tfinal, after which every kernel of the step returns at once.  A bound that is not
+// positive (a broken state) ends the run and raises S[5].
+__global__ void cfl_control_kernel(double* S, unsigned long long* bound) {
+    double b = __longlong_as_double((long long)*bound);
+    double t = S[0], tf = S[2];
+    double dt = fmin(b, S[3]);
+    if (!(t < tf)) {
+        dt = 0.0;
+    } else if (!(dt > 0.0)) {
+        dt = 0.0;
+        S[5] = 1.0;
+        t = tf;
+    } else if (t + dt >= tf) {
+        dt = tf - t;
+        t = tf;
+    } else {
+        t = t + dt;
+    }
+    S[0] = t;
+    S[1] = dt;
+    if (dt > 0.0) S[4] = S[4] + 1.0;
+    *bound = (unsigned long long)__double_as_longlong(INFINITY);
 }
 
 // Throughput probe: independent FMA chains per thread, eight per thread for ILP.
@@ -491,7 +523,7 @@ int32_t flou_destroy(flou_ctx* c) {
     drop_graph(c);
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
                     c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c, c->d_invJn, c->d_Jan,
-                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1};
+                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1, c->d_cfl, c->d_cflmin};
     for (void* b : bufs)
         if (b) cudaFree(b);
     ctx_free_limiter(c);
@@ -783,6 +815,88 @@ int32_t flou_step_async(flou_ctx* c, double* Q, double dt, double t0, int32_t ns
     for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
     if (ptr_kind == FLOU_PTR_HOST)
         CK(cudaMemcpyAsync(Q, c->d_Qh, bytes, cudaMemcpyDeviceToHost, c->stream), "state download");
+    return FLOU_OK;
+}
+
+int32_t flou_step_cfl(flou_ctx* c, double* Q, double t0, double tfinal, double cfl, double dtmax, int64_t max_steps,
+                      int32_t ptr_kind, int64_t* nsteps, double* t_out) {
+    int r = ready(c);
+    if (r) return r;
+    if (!Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
+    if (!std::isfinite(t0) || !std::isfinite(tfinal) || !(cfl > 0.0) || !std::isfinite(cfl) || std::isnan(dtmax) ||
+        !(dtmax > 0.0) || max_steps < 0)
+        return fail(c, FLOU_ERR_ARG, "invalid t0/tfinal/cfl/dtmax/max_steps");
+    if (nsteps) *nsteps = 0;
+    if (t_out) *t_out = t0;
+    if ((r = ensure(c, &c->d_U, (size_t)c->ndofs * c->nv, "stage buffer"))) return r;
+    if (!c->d_cfl) CK(cudaMalloc((void**)&c->d_cfl, 8 * sizeof(double)), "CFL state");
+    if (!c->d_cflmin) CK(cudaMalloc((void**)&c->d_cflmin, sizeof(unsigned long long)), "CFL state");
+    size_t bytes = (size_t)c->ndofs * c->nv * sizeof(double);
+    double* Qd = Q;
+    if (ptr_kind == FLOU_PTR_HOST) {
+        if ((r = ensure(c, &c->d_Qh, (size_t)c->ndofs * c->nv, "staging buffer"))) return r;
+        CK(cudaMemcpyAsync(c->d_Qh, Q, bytes, cudaMemcpyHostToDevice, c->stream), "state upload");
+        Qd = c->d_Qh;
+    } else if (ptr_kind != FLOU_PTR_DEVICE) {
+        return fail(c, FLOU_ERR_ARG, "unknown pointer kind %d", ptr_kind);
+    }
+    double S[8] = {t0, 0.0, tfinal, dtmax, 0.0, 0.0, 0.0, 0.0};
+    unsigned long long inf;
+    double dinf = INFINITY;
+    memcpy(&inf, &dinf, sizeof(inf));
+    CK(cudaMemcpyAsync(c->d_cfl, S, sizeof(S), cudaMemcpyHostToDevice, c->stream), "CFL state");
+    CK(cudaMemcpyAsync(c->d_cflmin, &inf, sizeof(inf), cudaMemcpyHostToDevice, c->stream), "CFL state");
+    if (!c->cfl_exec || c->cfl_Q != Qd || c->cfl_value != cfl) {
+        drop_graph(c);
+        ElemLaunch L = elem_launch(c);
+        L.prepare = true;
+        cudaError_t pe = launch_elem(L, elem_params(c, Qd, Qd, c->d_U, 1, 0.0, 0.0, 1.0), c->own_stream);
+        if (pe != cudaSuccess) return cuda_fail(c, pe, "element kernel set-up");
+        CK(cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        int grid = (int)((c->ndofs + 255) / 256);
+        const double* a = c->cfg.advection;
+        max_dt_kernel<<<grid, 256, 0, c->own_stream>>>(Qd, c->d_dx, c->ndofs, c->npe, c->cfg.dim, c->cfg.equation,
+                                                       c->cfg.gamma, a[0], a[1], a[2], cfl, c->d_cflmin);
+        cfl_control_kernel<<<1, 1, 0, c->own_stream>>>(c->d_cfl, c->d_cflmin);
+        c->d_gate = c->d_cfl + 1;
+        int rr = step_once(c, c->own_stream, Qd, 0.0);
+        c->d_gate = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(c->own_stream, &g);
+        if (rr) { if (g) cudaGraphDestroy(g); return rr; }
+        if (ce != cudaSuccess) return cuda_fail(c, ce, "graph capture");
+        c->cfl_graph = g;
+        CK(cudaGraphInstantiate(&c->cfl_exec, g, 0), "graph instantiate");
+        c->cfl_Q = Qd;
+        c->cfl_value = cfl;
+    }
+    // Launch steps in batches sized from the last dt, reading the device state between batches;
+    // never more than max_steps in all.
+    int64_t done_steps = 0;
+    double last_dt = 0.0;
+    while (done_steps < max_steps) {
+        int64_t k = 1;
+        if (last_dt > 0.0) {
+            double left = (tfinal - S[0]) / last_dt;
+            k = left > 255.0 ? 256 : (int64_t)left + 1;
+        }
+        if (k > max_steps - done_steps) k = max_steps - done_steps;
+        for (int64_t i = 0; i < k; ++i) CK(cudaGraphLaunch(c->cfl_exec, c->stream), "graph launch");
+        CK(cudaMemcpyAsync(S, c->d_cfl, sizeof(S), cudaMemcpyDeviceToHost, c->stream), "CFL state");
+        CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+        done_steps = (int64_t)S[4];
+        last_dt = S[1];
+        if (!(S[0] < tfinal) || S[5] != 0.0) break;
+    }
+    if (nsteps) *nsteps = done_steps;
+    if (t_out) *t_out = S[0];
+    if ((r = check_status(c))) return r;
+    if (S[5] != 0.0)
+        return fail(c, FLOU_ERR_NONPHYSICAL, "no positive CFL time step at t = %.17g", S[0]);
+    if (ptr_kind == FLOU_PTR_HOST) {
+        CK(cudaMemcpyAsync(Q, c->d_Qh, bytes, cudaMemcpyDeviceToHost, c->stream), "state download");
+        CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    }
     return FLOU_OK;
 }
 

@@ -71,6 +71,15 @@ struct flou_ctx {
     // step method of flou_step: 0 stages = Shu-Osher SSP-RK3, else a 2N-storage method
     int lsrk_s = 0;
     double lsrk_A[FLOU_MAX_LSRK_STAGES], lsrk_B[FLOU_MAX_LSRK_STAGES];
+    // CFL-limited stepping (flou_step_cfl): the step state lives on the device
+    double* d_cfl = nullptr;        // [0] t, [1] dt of the step (0 once t reached tfinal), [2] tfinal,
+                                    // [3] dtmax, [4] steps taken, [5] 1 when no positive dt was found
+    unsigned long long* d_cflmin = nullptr;   // ordered-bit minimum of the CFL bound
+    const double* d_gate = nullptr;           // &d_cfl[1] while the CFL step is captured
+    cudaGraph_t cfl_graph = nullptr;
+    cudaGraphExec_t cfl_exec = nullptr;
+    double* cfl_Q = nullptr;
+    double cfl_value = 0.0;
     // graph cache for flou_step
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;

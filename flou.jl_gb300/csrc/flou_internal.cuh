@@ -62,6 +62,7 @@ struct ElemParams {
                                  // 3: 2N-storage stage, k = a0 k + dt dQ (in aux), out = U + a1 k
     double dt, a0, a1;
     double* aux;                 // mode 3: the 2N-storage register k, read and rewritten per node
+    const double* dtp;           // CFL stepping: dt lives in device memory (0: the run is over, skip)
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
@@ -658,16 +659,17 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
     }
     int64_t g = (int64_t)e * ipow(N, DIM) + i;
     double invJ = CURV ? P.invJn[g] : P.elem_invJ[e];
+    const double dt = P.dtp ? *P.dtp : P.dt;
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         double r = dq[k] * invJ;
         double o;
         if (P.mode == 0) o = r;
-        else if (P.mode == 1) o = q[k] + P.dt * r;
-        else if (P.mode == 2) o = P.a0 * P.Q0[k * P.ndofs + g] + P.a1 * (q[k] + P.dt * r);
+        else if (P.mode == 1) o = q[k] + dt * r;
+        else if (P.mode == 2) o = P.a0 * P.Q0[k * P.ndofs + g] + P.a1 * (q[k] + dt * r);
         else {
-            double kk = P.dt * r;
+            double kk = dt * r;
             if (P.a0 != 0.0) kk = P.a0 * P.aux[k * P.ndofs + g] + kk;   // first stage: k is not read
             P.aux[k * P.ndofs + g] = kk;
             o = q[k] + P.a1 * kk;
@@ -778,6 +780,7 @@ __device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double*
 template <int DIM, int N, int EQ, bool LGL, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemParams P) {
     extern __shared__ double smem[];
+    if (P.dtp && *P.dtp == 0.0) return;   // CFL stepping past tfinal: the state stays as it is
     strong_tile<DIM, N, EQ, LGL, 256, CURV>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 
@@ -1339,6 +1342,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
 template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false, bool HYB = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
     extern __shared__ double smem[];
+    if (P.dtp && *P.dtp == 0.0) return;   // CFL stepping past tfinal: the state stays as it is
     split_tile<DIM, N, EQ, TP, LGL, 256, CURV, HYB>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);
 }
 

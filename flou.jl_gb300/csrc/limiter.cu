@@ -33,6 +33,7 @@ struct LimParams {
     int64_t ndofs;
     int nelem, npe;
     double minval, gamma;
+    const double* gate;   // CFL stepping: *gate == 0 once the run is over (skip)
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -65,6 +66,7 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
     const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
     const double g1 = P.gamma - 1.0;
+    if (P.gate && *P.gate == 0.0) return;
     for (int e = warp; e < P.nelem; e += nwarps) {
         const double Je = P.J[e];
         const int64_t b = (int64_t)e * P.npe;
@@ -183,8 +185,12 @@ __global__ void __launch_bounds__(256) monitor_partial_kernel(const double* Q, c
 }
 
 // One block: fixed-order sums of the partials, appended at slot *count (if below cap).
+// `times` (cap entries behind the values) receives *tdev, the device time after the step (CFL
+// stepping), or NaN when the time is known on the host.
 __global__ void __launch_bounds__(256) monitor_final_kernel(const double* partial, int nblk, double* out,
-                                                            int32_t* count, int cap) {
+                                                            int32_t* count, int cap, const double* gate,
+                                                            double* times, const double* tdev) {
+    if (gate && *gate == 0.0) return;   // CFL stepping past tfinal: no step, no record
     double a = 0.0, c = 0.0;
     for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
         a += partial[i];
@@ -209,6 +215,7 @@ __global__ void __launch_bounds__(256) monitor_final_kernel(const double* partia
         if (slot < cap) {
             out[2 * slot] = x;
             out[2 * slot + 1] = y;
+            if (times) times[slot] = tdev ? *tdev : __longlong_as_double(0x7ff8000000000000LL);
         }
         *count = slot + 1;
     }
@@ -277,7 +284,10 @@ int launch_monitors(flou_ctx* c, cudaStream_t s, const double* Q, int mask, doub
     if (d == 1) monitor_partial_kernel<1><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
     else if (d == 2) monitor_partial_kernel<2><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
     else monitor_partial_kernel<3><<<nb, 256, 0, s>>>(Q, c->d_Jel, Jn, c->d_wtp, c->ndofs, c->npe, c->cfg.gamma, mask, c->d_monpart);
-    monitor_final_kernel<<<1, 256, 0, s>>>(c->d_monpart, nb, out, count, cap);
+    bool rec = count == c->d_moncount;   // the per-step record (not a single evaluation)
+    monitor_final_kernel<<<1, 256, 0, s>>>(c->d_monpart, nb, out, count, cap, rec ? c->d_gate : nullptr,
+                                           rec ? out + 2 * (size_t)cap : nullptr,
+                                           rec && c->d_gate ? c->d_gate - 1 : nullptr);
     return lcuda(c, cudaGetLastError(), "monitor kernels");
 }
 
@@ -307,6 +317,7 @@ int ctx_limit(flou_ctx* c, cudaStream_t s, double* Q) {
     P.npe = c->npe;
     P.minval = c->lim_min;
     P.gamma = c->cfg.gamma;
+    P.gate = c->d_gate;
     int grid = (c->nelem + 7) / 8;   // 8 warps per block, one element per warp
     int d = c->cfg.dim;
     if (d == 1) zhang_shu_kernel<1><<<grid, 256, 0, s>>>(P);
@@ -414,7 +425,7 @@ int32_t flou_set_monitors(flou_ctx* c, int32_t mask, int32_t capacity) {
             if (c->d_mon) cudaFree(c->d_mon);
             c->d_mon = nullptr;
             c->mon_cap = 0;
-            if ((r = lcuda(c, cudaMalloc((void**)&c->d_mon, 2 * (size_t)capacity * sizeof(double)), "monitor buffer")))
+            if ((r = lcuda(c, cudaMalloc((void**)&c->d_mon, 3 * (size_t)capacity * sizeof(double)), "monitor buffer")))
                 return r;
             c->mon_cap = capacity;
         }
@@ -426,6 +437,10 @@ int32_t flou_set_monitors(flou_ctx* c, int32_t mask, int32_t capacity) {
 }
 
 int32_t flou_take_monitors(flou_ctx* c, double* out, int32_t max_steps, int32_t* nsteps) {
+    return flou_take_monitors_timed(c, out, nullptr, max_steps, nsteps);
+}
+
+int32_t flou_take_monitors_timed(flou_ctx* c, double* out, double* times, int32_t max_steps, int32_t* nsteps) {
     if (!c) return FLOU_ERR_ARG;
     if (!nsteps) return lfail(c, FLOU_ERR_ARG, "null pointer");
     *nsteps = 0;
@@ -438,6 +453,9 @@ int32_t flou_take_monitors(flou_ctx* c, double* out, int32_t max_steps, int32_t*
     if (n > max_steps) return lfail(c, FLOU_ERR_ARG, "%d steps recorded, the output holds %d", n, max_steps);
     if (n && out && (r = lcuda(c, cudaMemcpy(out, c->d_mon, 2 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost),
                                 "monitor read")))
+        return r;
+    if (n && times && (r = lcuda(c, cudaMemcpy(times, c->d_mon + 2 * (size_t)c->mon_cap, (size_t)n * sizeof(double),
+                                              cudaMemcpyDeviceToHost), "monitor read")))
         return r;
     if ((r = lcuda(c, cudaMemset(c->d_moncount, 0, sizeof(int32_t)), "monitor reset"))) return r;
     *nsteps = n;

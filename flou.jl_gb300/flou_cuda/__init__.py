@@ -13,8 +13,8 @@ from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, Eule
 from .mesh import CartesianMesh, apply_periodicBCs
 from .unstructured import UnstructuredMesh, perturbed_box, read_gmsh, write_gmsh22
 from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
-from .timeint import (ORK256, SSPRK33, CarpenterKennedy2N54, LowStorageRK2N, get_limiter_callback,
-                      get_monitor_callback, timeintegrate)
+from .timeint import (ORK256, SSPRK33, CarpenterKennedy2N54, LowStorageRK2N, get_cfl_callback, get_limiter_callback,
+                      get_monitor_callback, get_save_callback, make_callback_list, timeintegrate)
 from . import initial
 from .io import load_restart, save_restart, variablenames, write_vtu
 from .batch import Batch, adjoint_solve_batch

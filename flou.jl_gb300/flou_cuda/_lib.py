@@ -103,10 +103,13 @@ PROTOTYPES = {
     "flou_set_hybrid": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double],
     "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
     "flou_set_integrator": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+    "flou_step_cfl": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                      ctypes.c_int32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)],
     "flou_limit": [_P, _P, ctypes.c_int32],
     "flou_monitor": [_P, _P, ctypes.c_int32, _D, ctypes.c_int32],
     "flou_set_monitors": [_P, ctypes.c_int32, ctypes.c_int32],
     "flou_take_monitors": [_P, _D, ctypes.c_int32, _I32],
+    "flou_take_monitors_timed": [_P, _D, _D, ctypes.c_int32, _I32],
     "flou_adjoint_solve_batch": [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D, ctypes.c_int32,
                                  ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(_P), _D,
                                  ctypes.POINTER(_P), ctypes.POINTER(_P), _I64, _I32],

@@ -269,6 +269,7 @@ class Context:
             raise TypeError("state must be a numpy array or a torch tensor")
         if a.numel() != self.ndofs * self.nvars or not a.is_contiguous() or str(a.dtype) != "torch.float64":
             raise ValueError("state tensor must be a contiguous float64 tensor (nvars, ndofs)")
+        _torch_stream_sync(a)
         return ctypes.c_void_p(a.data_ptr()), (L.PTR_DEVICE if a.is_cuda else L.PTR_HOST)
 
     def set_stream(self, stream_ptr):
@@ -284,6 +285,14 @@ class Context:
     def step(self, Q, dt, nsteps, t0=0.0):
         pq, kq = self._ptr(Q, True)
         L.check(self._lib.flou_step(self.h, pq, float(dt), float(t0), int(nsteps), kq), self.h)
+
+    def step_cfl(self, Q, t0, tfinal, cfl, dtmax=float("inf"), max_steps=100000):
+        """CFL-limited steps from t0 towards tfinal (at most max_steps); returns (steps, t reached)."""
+        pq, kq = self._ptr(Q, True)
+        n, t = ctypes.c_int64(), ctypes.c_double()
+        L.check(self._lib.flou_step_cfl(self.h, pq, float(t0), float(tfinal), float(cfl), float(dtmax),
+                                        int(max_steps), kq, ctypes.byref(n), ctypes.byref(t)), self.h)
+        return n.value, t.value
 
     def step_async(self, Q, dt, nsteps, t0=0.0):
         """Queue `nsteps` steps (and, for host memory, the copies) without waiting; see wait()."""
@@ -323,13 +332,17 @@ class Context:
     def set_monitors(self, mask, capacity=1024):
         L.check(self._lib.flou_set_monitors(self.h, int(mask), int(capacity)), self.h)
 
-    def take_monitors(self, max_steps=1 << 20):
-        """(nsteps, 2) array of (kinetic energy, entropy) recorded after each step since the last take."""
+    def take_monitors(self, max_steps=1 << 20, with_times=False):
+        """(nsteps, 2) array of (kinetic energy, entropy) recorded after each step since the last take;
+        with_times: also the time after each step (CFL stepping; NaN after fixed steps)."""
         out = np.zeros((max_steps, 2))
+        times = np.zeros(max_steps)
         n = ctypes.c_int32()
-        L.check(self._lib.flou_take_monitors(self.h, out.ctypes.data_as(L._D), int(max_steps), ctypes.byref(n)),
-                self.h)
-        return out[:n.value].copy()
+        L.check(self._lib.flou_take_monitors_timed(self.h, out.ctypes.data_as(L._D),
+                                                   times.ctypes.data_as(L._D) if with_times else None,
+                                                   int(max_steps), ctypes.byref(n)), self.h)
+        vals = out[:n.value].copy()
+        return (vals, times[:n.value].copy()) if with_times else vals
 
     def max_dt(self, Q, cfl):
         pq, kq = self._ptr(Q)

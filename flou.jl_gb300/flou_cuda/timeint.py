@@ -117,49 +117,160 @@ def get_monitor_callback(timetype, valuetype, disc, equation, name, p=None, iter
     return MonitorCallback(which, out), out
 
 
+class CFLCallback:
+    def __init__(self, cfl, dtmax):
+        self.cfl = cfl
+        self.dtmax = dtmax
+
+
+def get_cfl_callback(cfl, dtmax=math.inf, iter=True):
+    """get_cfl_callback(cfl, Δtmax=Inf; iter=true) (FlouTime.jl:92-105): before every step
+    dt = min(get_max_dt(Q, cfl), Δtmax), the last step cut to land on tfinal.  The step control
+    runs on the device (flou_step_cfl): no host round trip per step."""
+    if iter is not True:
+        raise ValueError("only iter=true (every step) is implemented")
+    if not cfl > 0 or not dtmax > 0:
+        raise ValueError("cfl and Δtmax must be positive")
+    return CFLCallback(float(cfl), float(dtmax))
+
+
+class SaveCallback:
+    def __init__(self, basename, iter):
+        self.basename = basename
+        self.iter = iter if iter is True else set(int(i) for i in iter)
+        self.files = []
+
+    def selected(self, it):
+        return self.iter is True or it in self.iter
+
+    def next_after(self, it):
+        if self.iter is True:
+            return it + 1
+        later = [i for i in self.iter if i > it]
+        return min(later) if later else math.inf
+
+    def save(self, disc, Q, it, t):
+        from .io import write_vtu
+        path = "%s_%010d.vtu" % (self.basename, it)
+        write_vtu(path, disc, Q, time=t)
+        self.files.append(path)
+
+
+def get_save_callback(basename, iter=True):
+    """get_save_callback(basename; iter=true) (FlouTime.jl:67-90): the solution at the start and
+    after every selected step, with its time, as `basename_%010d.vtu` (VTK Lagrange cells on
+    equispaced nodes; the reference writes the same content as VTKHDF `.hdf`, and this image has
+    no HDF5 library)."""
+    return SaveCallback(basename, iter)
+
+
+class CallbackList(list):
+    pass
+
+
+def make_callback_list(*callbacks):
+    """make_callback_list(callbacks...) (FlouTime.jl:150-156): None when empty."""
+    return CallbackList(callbacks) if callbacks else None
+
+
+def _flatten(callback):
+    if callback is None:
+        return []
+    if isinstance(callback, (list, tuple)):
+        out = []
+        for c in callback:
+            out += _flatten(c)
+        return out
+    return [callback]
+
+
 class Solution:
     def __init__(self, t, u):
         self.t = t
         self.u = u
 
 
-def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t0=0.0, cfl=None, callback=None):
+def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t0=0.0, cfl=None, callback=None,
+                  maxiters=10 ** 6, **_ignored):
     """timeintegrate(Q0, disc, equation, solver, tfinal; dt, alias_u0, callback) -> (sol, exetime).
 
     Q0 is a column-major (ndofs, nvars) numpy matrix or a CUDA tensor (nvars, ndofs).
     With `cfl` set and no `dt`, the step is fixed once from get_max_dt(Q0, cfl).
-    `callback`: monitor callbacks (one or a list) from get_monitor_callback.
+    `callback`: one callback, a list or make_callback_list(...) of get_monitor_callback,
+    get_cfl_callback (then dt is ignored: the step follows the CFL bound on the device) and
+    get_save_callback callbacks.  Other keyword arguments of the reference's call (saveat,
+    adaptive=false, save_everystep, ...) do not change the result and are accepted.
     """
     import time as _time
 
     if not isinstance(solver, (SSPRK33, LowStorageRK2N)):
         raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "the solvers are SSPRK33 and the 2N-storage methods "
                                                   "(ORK256, CarpenterKennedy2N54, LowStorageRK2N)")
+    cbs = _flatten(callback)
+    for c in cbs:
+        if not isinstance(c, (MonitorCallback, CFLCallback, SaveCallback)):
+            raise TypeError("unknown callback %r" % (c,))
+    cflcb = [c for c in cbs if isinstance(c, CFLCallback)]
+    mons = [c for c in cbs if isinstance(c, MonitorCallback)]
+    saves = [c for c in cbs if isinstance(c, SaveCallback)]
+    if len(cflcb) > 1:
+        raise ValueError("one CFL callback at most")
     ctx = disc.ctx
-    if dt is None:
-        if cfl is None:
-            raise ValueError("give dt or cfl")
-        dt = ctx.max_dt(Q0, cfl)
-    nsteps = int(math.floor((tfinal - t0) / dt + 0.5))
-    if abs(t0 + nsteps * dt - tfinal) > 1e-12 * max(1.0, abs(tfinal)):
-        raise ValueError("tfinal - t0 must be a whole number of steps of size dt")
+    if cflcb:
+        nsteps, capacity = None, int(min(maxiters, 10 ** 6))
+    else:
+        if dt is None:
+            if cfl is None:
+                raise ValueError("give dt or cfl")
+            dt = ctx.max_dt(Q0, cfl)
+        nsteps = int(math.floor((tfinal - t0) / dt + 0.5))
+        if abs(t0 + nsteps * dt - tfinal) > 1e-12 * max(1.0, abs(tfinal)):
+            raise ValueError("tfinal - t0 must be a whole number of steps of size dt")
+        capacity = max(nsteps, 1)
     Q = Q0 if alias_u0 else Q0.copy(order="F") if hasattr(Q0, "flags") else Q0.clone()
     u0 = None if alias_u0 else Q0
     lim = solver.stage_limiter
     ctx.set_limiter(lim.kind, lim.minval) if lim is not None else ctx.set_limiter(L.LIMITER_NONE)
-    mons = [] if callback is None else (list(callback) if isinstance(callback, (list, tuple)) else [callback])
     mask = 0
     for m in mons:
         mask |= m.which
-    ctx.set_monitors(mask, max(nsteps, 1))
+    ctx.set_monitors(mask, capacity)
     lowstorage = isinstance(solver, LowStorageRK2N)
     if lowstorage:
         ctx.set_integrator(solver.A, solver.B)
+
+    def next_stop(it):
+        return min([s.next_after(it) for s in saves] + [math.inf])
+
     start = _time.perf_counter()
+    it, t = 0, t0
     try:
-        ctx.step(Q, dt, nsteps, t0)
+        for s in saves:
+            s.save(disc, Q, it, t)
+        if cflcb:
+            c = cflcb[0]
+            while t < tfinal and it < maxiters:
+                k = min(next_stop(it), maxiters) - it
+                n, t = ctx.step_cfl(Q, t, tfinal, c.cfl, c.dtmax, max_steps=int(min(k, 2 ** 62)))
+                it += n
+                if n == 0:
+                    break
+                for s in saves:
+                    if s.selected(it):
+                        s.save(disc, Q, it, t)
+            if t < tfinal:
+                raise L.FlouError(L.FLOU_ERR_STATE, "maxiters = %d steps reached at t = %.17g" % (maxiters, t))
+        else:
+            while it < nsteps:
+                k = int(min(next_stop(it), nsteps)) - it
+                ctx.step(Q, dt, k, t0 + it * dt)
+                it += k
+                t = t0 + it * dt
+                for s in saves:
+                    if s.selected(it):
+                        s.save(disc, Q, it, t)
     finally:
-        vals = ctx.take_monitors(max(nsteps, 1)) if mask else None
+        vals, times = ctx.take_monitors(capacity, with_times=True) if mask else (None, None)
         ctx.set_monitors(0, 1)
         ctx.set_limiter(L.LIMITER_NONE)
         if lowstorage:
@@ -168,7 +279,7 @@ def timeintegrate(Q0, disc, equation, solver, tfinal, dt=None, alias_u0=False, t
     for m in mons:
         col = 0 if m.which == L.MONITOR_KINETIC_ENERGY else 1
         for k in range(vals.shape[0]):
-            m.out.time.append(t0 + (k + 1) * dt)
+            m.out.time.append(float(times[k]) if cflcb else t0 + (k + 1) * dt)
             m.out.iter.append(k + 1)
             m.out.value.append(float(vals[k, col]))
-    return Solution([t0, tfinal], [u0, Q]), exetime
+    return Solution([t0, t], [u0, Q]), exetime

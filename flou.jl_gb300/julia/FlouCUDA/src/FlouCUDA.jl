@@ -211,24 +211,35 @@ function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, solver
 end
 
 """
-    timeintegrate(Q0, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt)
+    timeintegrate(Q0, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt, cfl=nothing, dtmax=Inf)
 
 Same contract as Flou's `timeintegrate` (FlouTime.jl:34-54): returns `(sol, exetime)`, logs
-"Simulation crashed!" on a DomainError.
+"Simulation crashed!" on a DomainError.  With `cfl` the step follows
+`get_cfl_callback(cfl, dtmax)` (FlouTime.jl:92-105), computed on the device by `flou_step_cfl`.
 """
-function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt, kwargs...)
+function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, ::SSPRK3GPU, tfinal; dt=nothing,
+                            cfl=nothing, dtmax=Inf, maxiters=10^6, kwargs...)
     Q = copy(Q0)
-    nsteps = round(Int, tfinal / dt)
+    t = Ref{Float64}(0.0)
     exetime = @elapsed begin
         try
-            GC.@preserve Q check(ccall((:flou_step, libflou), Int32,
-                (Ptr{Cvoid}, Ptr{Float64}, Float64, Float64, Int32, Int32), disc.ctx, Q, dt, 0.0, nsteps, PTR_HOST),
-                disc.ctx)
+            if cfl === nothing
+                nsteps = round(Int, tfinal / dt)
+                GC.@preserve Q check(ccall((:flou_step, libflou), Int32,
+                    (Ptr{Cvoid}, Ptr{Float64}, Float64, Float64, Int32, Int32), disc.ctx, Q, dt, 0.0, nsteps,
+                    PTR_HOST), disc.ctx)
+                t[] = tfinal
+            else
+                n = Ref{Int64}(0)
+                GC.@preserve Q check(ccall((:flou_step_cfl, libflou), Int32,
+                    (Ptr{Cvoid}, Ptr{Float64}, Float64, Float64, Float64, Float64, Int64, Int32, Ref{Int64},
+                     Ref{Float64}), disc.ctx, Q, 0.0, tfinal, cfl, dtmax, maxiters, PTR_HOST, n, t), disc.ctx)
+            end
         catch e
             e isa DomainError ? (@error "Simulation crashed!") : rethrow()
         end
     end
-    return ((t=[0.0, tfinal], u=[Q0, Q]), exetime)
+    return ((t=[0.0, t[]], u=[Q0, Q]), exetime)
 end
 
 # ---- differentiable terminal functional --------------------------------------------------------

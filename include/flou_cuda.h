@@ -173,6 +173,17 @@ int32_t flou_step(flou_ctx* ctx, double* Q, double dt, double t0, int32_t nsteps
  * u in place; the limiter, when set, acts after every stage.  The adjoint and the batched
  * launch step with SSP-RK3 only. */
 #define FLOU_MAX_LSRK_STAGES 16
+
+/* CFL-limited stepping: get_cfl_callback(cfl, dtmax) (src/FlouTime/FlouTime.jl:92-105) with the
+ * step method of flou_set_integrator.  Before every step dt = min(get_max_dt(Q, cfl), dtmax), and
+ * the last step is cut to land on tfinal (OrdinaryDiffEq stops on tfinal).  The time, dt and the
+ * step count live on the device: each step is one CUDA graph (CFL bound, step control, stages),
+ * the host only reads the state back between batches of steps.  Stops after max_steps steps at
+ * most; *nsteps receives the steps taken, *t_out the time reached (tfinal unless max_steps cut
+ * the run short).  dtmax may be +inf.  The limiter and the monitors act as in flou_step.
+ * FLOU_ERR_NONPHYSICAL when a state breaks or no positive time step exists. */
+int32_t flou_step_cfl(flou_ctx* ctx, double* Q, double t0, double tfinal, double cfl, double dtmax,
+                      int64_t max_steps, int32_t ptr_kind, int64_t* nsteps, double* t_out);
 int32_t flou_set_integrator(flou_ctx* ctx, int32_t nstages, const double* A, const double* B);
 
 /* flou_step without the final synchronisation: the copies (host pointers; use pinned memory
@@ -294,6 +305,9 @@ int32_t flou_monitor(flou_ctx* ctx, const double* Q, int32_t which, double* valu
  * `capacity`. */
 int32_t flou_set_monitors(flou_ctx* ctx, int32_t mask, int32_t capacity);
 int32_t flou_take_monitors(flou_ctx* ctx, double* out, int32_t max_steps, int32_t* nsteps);
+/* flou_take_monitors plus the time after each recorded step (flou_step_cfl; NaN for steps of
+ * flou_step, whose times t0 + k dt the caller knows). */
+int32_t flou_take_monitors_timed(flou_ctx* ctx, double* out, double* times, int32_t max_steps, int32_t* nsteps);
 
 /* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
  * Many independent discretizations with uneven element counts and orders advance together:
