@@ -264,11 +264,13 @@ def read_gmsh(filename, dim):
     used = sorted({node_id[t] for e in cells for t in e[2]})
     remap = {old: new for new, old in enumerate(used)}
     elements = np.array([[remap[node_id[t]] for t in e[2]] for e in cells], dtype=np.int64)
-    boundaries = {}
+    # boundaries in the order of their physical tags, as gmsh.model.get_physical_groups lists
+    # them to the reference's reader (GmshMesh.jl:112-126)
+    groups = {}
     for etype, phys, tags in elems:
         if etype in _GMSH_TYPE and _GMSH_TYPE[etype][0] == dim - 1 and phys:
-            name = phys_names.get((dim - 1, phys), str(phys))
-            boundaries.setdefault(name, []).append(tuple(remap[node_id[t]] for t in tags))
+            groups.setdefault(phys, []).append(tuple(remap[node_id[t]] for t in tags))
+    boundaries = {phys_names.get((dim - 1, tag), str(tag)): groups[tag] for tag in sorted(groups)}
     return coords[used], elements, boundaries
 
 

@@ -149,3 +149,36 @@ def test_gmsh41_file():
     assert len(m.bdfaces[m.boundary_index("wall") - 1]) == 5
     assert len(m.bdfaces[m.boundary_index("outlet") - 1]) == 1
     assert np.allclose(m.nodes[m.elements[1]], [[1, 0], [2, 0], [2, 1], [1, 1]])
+
+
+REF_MESHES = "/root/reference/test/meshes"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="the reference's mesh files are not present")
+@pytest.mark.parametrize("name,dim,nelem,names", [
+    ("2D_cylinder", 2, 73, ["Bottom", "Right", "Top", "Left", "Hole"]),
+    ("3D_bullet", 3, 295, ["Body", "Interior", "Inlet", "Wall", "Outlet", "Left", "Right"]),
+])
+def test_reference_meshes(name, dim, nelem, names):
+    """The reference's own Gmsh 4.1 meshes (test/meshes/*.msh; 3D_bullet is the coarse version of
+    the mesh of examples/src/3D_Euler.jl): read in the order of their physical groups, the
+    connectivity is consistent, the geometry is valid (positive Jacobians, unit normals) and the
+    split form with MatrixDissipation, as the 3D example runs it, preserves a uniform flow."""
+    m = F.UnstructuredMesh.from_gmsh(os.path.join(REF_MESHES, name + ".msh"), dim)
+    assert m.nelements == nelem and m.bdnames == names
+    for f in range(m.nfaces):   # every face is held by the element positions that name it
+        for side in range(2):
+            e, pos = int(m.eleminds[f, side]), int(m.elempos[f, side])
+            if e:
+                assert m.faceinds[e - 1, pos - 1] == f + 1
+    assert sum(len(b) for b in m.bdfaces) == int(np.sum(m.eleminds[:, 1] == 0))
+    op = F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0))
+    disc = _disc(m, 3, op)
+    assert np.all(disc.J > 0) and np.all(disc.faceJ > 0)
+    fr = np.asarray(disc.frames).reshape(-1, 9)
+    assert np.allclose(np.linalg.norm(fr[:, 0:3], axis=1), 1.0)
+    P = np.zeros((disc.ndofs, dim + 2))
+    P[:, 0], P[:, 1], P[:, -1] = 1.0, 2.0, 1.0   # the example's inflow state (1, 2, 0, 0, 1)
+    Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+    R = oracle_for(disc).rhs(Q)
+    assert np.max(np.abs(R)) < 1e-10, np.max(np.abs(R))
