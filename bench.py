@@ -548,6 +548,31 @@ def run_profile(which):
     return 0
 
 
+def bench_operators(nel=16, n=8):
+    """Kernel cost of the operator variants on mesh B's size (16³ hexahedra, p = 7, TGV Mach 0.1):
+    the split form and the hybrid (telescopic subcell) operator with MatrixDissipation, as the
+    reference's Shockwave2D test uses them, on Gauss-Lobatto and on Gauss nodes.  CUDA-event
+    times of single face and element launches (stage 2), and DOF·stage-updates/s of one stage."""
+    import torch
+    import flou_cuda as F
+    eq = F.EulerEquation(3, 1.4)
+    md = F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)
+    out = {}
+    for basis in ("GLL", "GL"):
+        for name, op in (("split", F.SplitDivOperator(md)), ("hybrid", F.HybridDivOperator(md, 1.0))):
+            mesh = F.CartesianMesh((0.0,) * 3, (2 * math.pi,) * 3, (nel,) * 3)
+            F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
+            b = F.LagrangeBasis(basis, n)
+            disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), 5), eq, op, {})
+            q = torch.from_numpy(np.ascontiguousarray(F.initial.taylor_green(eq, disc.coords, mach=0.1).T)).cuda()
+            fms, ems = disc.ctx.time_kernels(q, nrep=3)
+            out["%s_%s" % (name, basis)] = {"face_ms": fms, "elem_ms": ems,
+                                            "value": disc.ndofs / ((fms + ems) * 1e-3), "unit": UNIT}
+            del disc, q
+    out["workload"] = "16^3 p=7 TGV M0.1, MatrixDissipation(Chandrashekar) interface (and subcell FV) flux"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -683,6 +708,13 @@ def main():
         except Exception as exc:   # reported, not fatal to the bench line
             curvilinear = {"error": str(exc)}
 
+    operators = None
+    if not args.no_curvilinear:
+        try:
+            operators = bench_operators()
+        except Exception as exc:   # reported, not fatal to the bench line
+            operators = {"error": str(exc)}
+
     # ---- cost of the Zhang-Shu stage limiter (minval 1e-10, as examples/src/3D_Euler.jl:76) ----
     limiter = None
     try:
@@ -757,7 +789,8 @@ def main():
                        "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
-            "adjoint_batch": adjoint_batch, "limiter": limiter, "curvilinear": curvilinear, "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
+            "adjoint_batch": adjoint_batch, "limiter": limiter, "curvilinear": curvilinear, "operators": operators,
+            "gpu_launches": steps * 6 * len(meshes), "clocks": clk,
         }
         print(json.dumps(line))
     if dist is not None:

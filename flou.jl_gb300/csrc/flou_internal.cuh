@@ -178,170 +178,183 @@ __device__ __forceinline__ void euler_normal_flux(const double* q, double un, do
     F[DIM + 1] = (q[DIM + 1] + p) * un;
 }
 
-// logarithmic_mean (src/FlouCommon/Utilities.jl:34-44) with the series of Ismail & Roe
-// when u = ((a-b)/(a+b))² < 0.01, otherwise log(a/b)/(2f) -- evaluated here as in the
-// reference (the face path is not the bottleneck).
-__device__ __forceinline__ double logmean_ref(double al, double ar) {
-    double xi = al / ar;
-    double f = (xi - 1.0) / (xi + 1.0);
-    double u = f * f;
-    double F;
-    if (u < 0.01) F = ((1.0 + u / 3.0) + (u * u) / 5.0) + (u * u * u) / 7.0;
-    else F = log(xi) / (2.0 * f);
-    return (al + ar) / (2.0 * F);
+// Logarithmic mean (src/FlouCommon/Utilities.jl:34-44) of a, b > 0 in sums and differences, given
+// s = a + b and rs = 1/s (often from one reciprocal shared with a second mean):
+//   f = (a - b)/s, u = f²;  u < 0.01: mean = s/(2F) with the reference's F = 1+u/3+u²/5+u³/7
+//   (1/F by two Newton steps from 1 - u/3, relative error (4u²/45)^4 < 1e-20), else the log branch
+//   mean = (a - b)/ln(a/b).  L = ln(a/b) comes along: from the log branch, or on the series
+//   branch from 2f·atanh(f)/f summed to u⁸/17 (remainder below 1e-19 relative).
+struct LogMean { double mean, inv, L; };
+
+__device__ __forceinline__ LogMean logmean_sd(double a, double b, double s, double rs) {
+    const double d = a - b, f = d * rs, u = f * f;
+    LogMean m;
+    if (u < 0.01) {
+        double Fs = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        double y = fma(-1.0 / 3.0, u, 1.0);
+        y = y * fma(-Fs, y, 2.0);
+        y = y * fma(-Fs, y, 2.0);
+        m.mean = 0.5 * s * y;
+        m.inv = 2.0 * Fs * rs;
+        double Fe = fma(u, 1.0 / 17.0, 1.0 / 15.0);
+        Fe = fma(u, Fe, 1.0 / 13.0);
+        Fe = fma(u, Fe, 1.0 / 11.0);
+        Fe = fma(u, Fe, 1.0 / 9.0);
+        Fe = fma(u, Fe, 1.0 / 7.0);
+        Fe = fma(u, Fe, 0.2);
+        Fe = fma(u, Fe, 1.0 / 3.0);
+        Fe = fma(u, Fe, 1.0);
+        m.L = 2.0 * f * Fe;
+    } else {
+        double L = log(a / b);
+        m.mean = d / L;
+        m.inv = L / d;
+        m.L = L;
+    }
+    return m;
 }
 
+// The entropy-conserving and entropy-stable interface fluxes of src/FlouSpatial/Equations/Euler.jl
+// in the face frame (momentum index 1 normal): ChandrasekharAverage (:167-226, 3D with the
+// reference's wl² counted twice), LxF with either central flux (:138-165), ScalarDissipation
+// (:228-301, 3D with the reference's zero momentum jump) and MatrixDissipation (:303-380).  One
+// reciprocal per density and pressure, one shared by both logarithmic means; the entropy-variable
+// jump takes its logarithms from the means, ln(p_l/p_r) = ln(ρ_l/ρ_r) - ln(β_l/β_r), so
+// (s_r - s_l)/(γ-1) = L_ρ + L_β/(γ-1).  Same formulas as the reference up to rounding.
 template <int DIM>
-__device__ __forceinline__ void euler_face_flux(const double* ql, const double* qr, int kind, int lxf_avg,
-                                                double intensity, double g, double* F) {
+__device__ __forceinline__ void euler_face_flux_es(const double* ql, const double* qr, int kind, int avg,
+                                                   double intensity, double g, double* F) {
     constexpr int NV = DIM + 2;
-    double rl = ql[0], rr = qr[0];
-    double ul = ql[1] / rl, ur = qr[1] / rr;
-    double pl = euler_pressure<DIM>(ql, g), pr = euler_pressure<DIM>(qr, g);
-    auto stdavg = [&](double* A) {   // Euler.jl:99-136
-        A[0] = (ql[1] + qr[1]) / 2.0;
-        A[1] = (((ql[1] * ul + pl) + qr[1] * ur) + pr) / 2.0;
-        for (int k = 1; k < DIM; ++k) A[1 + k] = (ql[1 + k] * ul + qr[1 + k] * ur) / 2.0;
-        A[DIM + 1] = ((ql[DIM + 1] + pl) * ul + (qr[DIM + 1] + pr) * ur) / 2.0;
-    };
-    auto chandra = [&](double* A) {   // Euler.jl:167-226 (3D keeps the reference's wl² term)
-        double vl[3] = {ul, DIM > 1 ? ql[2] / rl : 0.0, DIM > 2 ? ql[3] / rl : 0.0};
-        double vr[3] = {ur, DIM > 1 ? qr[2] / rr : 0.0, DIM > 2 ? qr[3] / rr : 0.0};
-        double u = (vl[0] + vr[0]) / 2.0, v = (vl[1] + vr[1]) / 2.0, w = (vl[2] + vr[2]) / 2.0;
-        double bl = rl / (2.0 * pl), br = rr / (2.0 * pr);
-        double rho = logmean_ref(rl, rr);
-        double p = (rl + rr) / (2.0 * (bl + br));
-        double beta = logmean_ref(bl, br);
-        double s = vl[0] * vl[0];
-        if (DIM > 1) s = s + vl[1] * vl[1];
-        if (DIM > 2) s = s + vl[2] * vl[2];
-        s = s + vr[0] * vr[0];
+    const double rl = ql[0], rr = qr[0];
+    const double irl = 1.0 / rl, irr = 1.0 / rr;
+    double vl[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0};
+    double vl2 = 0.0, vr2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vl[k] = ql[1 + k] * irl;
+        vr[k] = qr[1 + k] * irr;
+        vl2 = fma(vl[k], vl[k], vl2);
+        vr2 = fma(vr[k], vr[k], vr2);
+    }
+    const double g1 = g - 1.0;
+    const double pl = g1 * fma(-0.5 * rl, vl2, ql[DIM + 1]), pr = g1 * fma(-0.5 * rr, vr2, qr[DIM + 1]);
+    double vm[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vm[k] = 0.5 * (vl[k] + vr[k]);
+    double A[NV];
+    const bool chandra = kind == FLOU_NF_CHANDRASHEKAR || avg == FLOU_NF_CHANDRASHEKAR;
+    const bool needs_means = chandra || kind == FLOU_NF_SCALAR_DISSIPATION || kind == FLOU_NF_MATRIX_DISSIPATION;
+    LogMean mr{0.0, 0.0, 0.0}, mb{0.0, 0.0, 0.0};
+    double bl = 0.0, br = 0.0, phat = 0.0;
+    if (needs_means) {
+        const double ipl = 1.0 / pl, ipr = 1.0 / pr;
+        bl = 0.5 * rl * ipl;
+        br = 0.5 * rr * ipr;
+        const double sr = rl + rr, sb = bl + br;
+        const double R = 1.0 / (sr * sb);
+        const double rsr = sb * R, rsb = sr * R;
+        mr = logmean_sd(rl, rr, sr, rsr);
+        mb = logmean_sd(bl, br, sb, rsb);
+        phat = 0.5 * sr * rsb;   // (ρl + ρr)/(2(βl + βr))
+    }
+    if (chandra) {
+        double s = vl2 + vr[0] * vr[0];
         if (DIM > 1) s = s + vr[1] * vr[1];
         if (DIM > 2) s = s + vl[2] * vl[2];
-        double h = (1.0 / ((2.0 * beta) * (g - 1.0)) - s / 4.0) + p / rho;
-        h = h + u * u;
-        if (DIM > 1) h = h + v * v;
-        if (DIM > 2) h = h + w * w;
-        A[0] = rho * u;
-        A[1] = rho * (u * u) + p;
-        if (DIM > 1) A[2] = rho * u * v;
-        if (DIM > 2) A[3] = rho * u * w;
-        A[DIM + 1] = rho * u * h;
-    };
-    if (kind == FLOU_NF_STD_AVERAGE) { stdavg(F); return; }
-    if (kind == FLOU_NF_CHANDRASHEKAR) { chandra(F); return; }
-    if (kind == FLOU_NF_SCALAR_DISSIPATION || kind == FLOU_NF_MATRIX_DISSIPATION) {
-        double A[NV];
-        if (lxf_avg == FLOU_NF_CHANDRASHEKAR) chandra(A); else stdavg(A);
-        double vl[3] = {ul, DIM > 1 ? ql[2] / rl : 0.0, DIM > 2 ? ql[3] / rl : 0.0};
-        double vr[3] = {ur, DIM > 1 ? qr[2] / rr : 0.0, DIM > 2 ? qr[3] / rr : 0.0};
-        double vm[3] = {(vl[0] + vr[0]) / 2.0, (vl[1] + vr[1]) / 2.0, (vl[2] + vr[2]) / 2.0};
-        double bl = rl / (2.0 * pl), br = rr / (2.0 * pr);
-        double beta = logmean_ref(bl, br);
-        if (kind == FLOU_NF_SCALAR_DISSIPATION) {   // Euler.jl:233-301
-            double al = sqrt(g * pl / rl), ar = sqrt(g * pr / rr);
-            double lam = fmax(fabs(ul) + al, fabs(ur) + ar);
-            double D[NV];
-            D[0] = rr - rl;
-            // the 3D branch takes the left momenta from Qr (Euler.jl:257): no momentum jump there
-            for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? qr[1 + k] - qr[1 + k] : qr[1 + k] - ql[1 + k];
-            double c1 = 1.0 / beta / (g - 1.0);
-            for (int k = 0; k < DIM; ++k) c1 = c1 + vl[k] * vr[k];
-            double c2 = vm[0] * (vr[0] - vl[0]);
-            for (int k = 1; k < DIM; ++k) c2 = c2 + vm[k] * (vr[k] - vl[k]);
-            c2 = c2 + (1.0 / br - 1.0 / bl) / (2.0 * (g - 1.0));
-            D[DIM + 1] = c1 * (rr - rl) / 2.0 + ((rl + rr) / 2.0) * c2;
-            for (int k = 0; k < NV; ++k) F[k] = A[k] - lam / 2.0 * D[k] * intensity;
+        double vv = vm[0] * vm[0];
+        if (DIM > 1) vv = fma(vm[1], vm[1], vv);
+        if (DIM > 2) vv = fma(vm[2], vm[2], vv);
+        double h = fma(mb.inv, 0.5 / g1, fma(-0.25, s, fma(phat, mr.inv, vv)));
+        double m = mr.mean * vm[0];
+        A[0] = m;
+        A[1] = fma(m, vm[0], phat);
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) A[1 + k] = m * vm[k];
+        A[DIM + 1] = m * h;
+    } else {   // StdAverage, Euler.jl:99-136
+        A[0] = (ql[1] + qr[1]) * 0.5;
+        A[1] = (fma(ql[1], vl[0], pl) + fma(qr[1], vr[0], pr)) * 0.5;
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) A[1 + k] = fma(ql[1 + k], vl[0], qr[1 + k] * vr[0]) * 0.5;
+        A[DIM + 1] = fma(ql[DIM + 1] + pl, vl[0], (qr[DIM + 1] + pr) * vr[0]) * 0.5;
+    }
+    if (kind == FLOU_NF_CHANDRASHEKAR || kind == FLOU_NF_STD_AVERAGE) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = A[k];
+        return;
+    }
+    if (kind == FLOU_NF_LXF || kind == FLOU_NF_SCALAR_DISSIPATION) {
+        const double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+        const double lam = fmax(fabs(vl[0]) + al, fabs(vr[0]) + ar) * (0.5 * intensity);
+        if (kind == FLOU_NF_LXF) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) F[k] = fma(lam, ql[k] - qr[k], A[k]);
             return;
         }
-        // MatrixDissipation, Euler.jl:308-380: F = A + R Λ T Rᵀ (W_l - W_r)/2, evaluated as
-        // y = Rᵀ ΔW, z = Λ T y, R z (the same product in another association)
-        double vv = 0.0, sl2 = 0.0;
+        double D[NV];
+        D[0] = rr - rl;
+        // the 3D branch takes the left momenta from Qr (Euler.jl:257): no momentum jump there
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? 0.0 : qr[1 + k] - ql[1 + k];
+        double c1 = mb.inv / g1, c2 = 0.0;
+#pragma unroll
         for (int k = 0; k < DIM; ++k) {
-            vv = vv + vm[k] * vm[k];
-            sl2 = sl2 + vl[k] * vl[k] + vr[k] * vr[k];
+            c1 = fma(vl[k], vr[k], c1);
+            c2 = fma(vm[k], vr[k] - vl[k], c2);
         }
-        double v2 = 2.0 * vv - sl2 / 2.0;
-        double rho = logmean_ref(rl, rr);
-        double p = (rl + rr) / (2.0 * (bl + br));
-        double a = sqrt(g * p / rho);
-        double h = g / (2.0 * beta) / (g - 1.0) + v2 / 2.0;
-        double dW[NV];
-        {
-            double sLv = log(pl) - g * log(rl), sRv = log(pr) - g * log(rr);
-            double ml2 = 0.0, mr2 = 0.0;
-            for (int k = 0; k < DIM; ++k) {
-                ml2 = ml2 + ql[1 + k] * ql[1 + k];
-                mr2 = mr2 + qr[1 + k] * qr[1 + k];
-            }
-            dW[0] = ((g - sLv) / (g - 1.0) - ml2 / rl / (2.0 * pl)) - ((g - sRv) / (g - 1.0) - mr2 / rr / (2.0 * pr));
-            for (int k = 0; k < DIM; ++k) dW[1 + k] = ql[1 + k] / pl - qr[1 + k] / pr;
-            dW[DIM + 1] = -rl / pl + rr / pr;
-        }
-        const double u = vm[0];
-        // columns of R: acoustic (u - a), entropy (u), shear (one per tangential axis), acoustic (u + a)
-        double y[NV];
-        y[0] = dW[0] + (u - a) * dW[1];
-        y[DIM + 1] = dW[0] + (u + a) * dW[1];
-        double ye = dW[0] + u * dW[1];
-        for (int k = 1; k < DIM; ++k) {
-            y[0] = y[0] + vm[k] * dW[1 + k];
-            y[DIM + 1] = y[DIM + 1] + vm[k] * dW[1 + k];
-            ye = ye + vm[k] * dW[1 + k];
-            y[1 + k] = dW[1 + k] + vm[k] * dW[DIM + 1];
-        }
-        y[0] = y[0] + (h - u * a) * dW[DIM + 1];
-        y[DIM + 1] = y[DIM + 1] + (h + u * a) * dW[DIM + 1];
-        y[1] = ye + v2 / 2.0 * dW[DIM + 1];
-        double z[NV];
-        z[0] = fabs(u - a) * (rho / (2.0 * g)) * y[0];
-        z[1] = fabs(u) * ((g - 1.0) * rho / g) * y[1];
-        for (int k = 1; k < DIM; ++k) z[1 + k] = fabs(u) * p * y[1 + k];
-        z[DIM + 1] = fabs(u + a) * (rho / (2.0 * g)) * y[DIM + 1];
-        double o[NV];
-        o[0] = z[0] + z[1] + z[DIM + 1];
-        o[1] = (u - a) * z[0] + u * z[1] + (u + a) * z[DIM + 1];
-        o[DIM + 1] = (h - u * a) * z[0] + v2 / 2.0 * z[1] + (h + u * a) * z[DIM + 1];
-        for (int k = 1; k < DIM; ++k) {
-            o[1 + k] = vm[k] * (z[0] + z[1] + z[DIM + 1]) + z[1 + k];
-            o[DIM + 1] = o[DIM + 1] + vm[k] * z[1 + k];
-        }
-        for (int k = 0; k < NV; ++k) F[k] = A[k] + o[k] / 2.0 * intensity;
+        c2 = c2 + (pr * irr - pl * irl) / g1;   // (1/βr - 1/βl)/(2(γ-1))
+        D[DIM + 1] = fma(0.5 * c1, rr - rl, 0.5 * (rl + rr) * c2);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = fma(-lam, D[k], A[k]);
         return;
     }
-    if (kind == FLOU_NF_LXF) {   // Euler.jl:138-165
-        double A[NV];
-        if (lxf_avg == FLOU_NF_CHANDRASHEKAR) chandra(A); else stdavg(A);
-        double al = sqrt(g * pl / rl), ar = sqrt(g * pr / rr);
-        double lam = fmax(fabs(ul) + al, fabs(ur) + ar);
-        for (int k = 0; k < NV; ++k) F[k] = A[k] + lam * (ql[k] - qr[k]) / 2.0 * intensity;
-        return;
+    // MatrixDissipation: F = A + R Λ T Rᵀ (W_l - W_r)/2, evaluated as y = Rᵀ ΔW, z = Λ T y, R z
+    double vv = vm[0] * vm[0];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vv = fma(vm[k], vm[k], vv);
+    const double v2 = fma(2.0, vv, -0.5 * (vl2 + vr2));
+    const double a = sqrt(g * phat * mr.inv);
+    const double h = fma(0.5 * g / g1, mb.inv, 0.5 * v2);
+    double dW[NV];
+    dW[0] = (mr.L + mb.L / g1) - (vl2 * bl - vr2 * br);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) dW[1 + k] = 2.0 * (bl * vl[k] - br * vr[k]);
+    dW[DIM + 1] = -2.0 * (bl - br);
+    const double u = vm[0];
+    double y[NV];
+    double ye = fma(u, dW[1], dW[0]);
+    y[0] = fma(-a, dW[1], ye);
+    y[DIM + 1] = fma(a, dW[1], ye);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        y[0] = fma(vm[k], dW[1 + k], y[0]);
+        y[DIM + 1] = fma(vm[k], dW[1 + k], y[DIM + 1]);
+        ye = fma(vm[k], dW[1 + k], ye);
+        y[1 + k] = fma(vm[k], dW[DIM + 1], dW[1 + k]);
     }
-    // HLL / HLLC (Toro 2009, eqs. 10.21 and 10.37-10.39; Davis wave-speed estimates).
-    double al = sqrt(g * pl / rl), ar = sqrt(g * pr / rr);
-    double sl = fmin(ul - al, ur - ar), sr = fmax(ul + al, ur + ar);
-    double Fl[NV], Fr[NV];
-    euler_normal_flux<DIM>(ql, ul, pl, Fl);
-    euler_normal_flux<DIM>(qr, ur, pr, Fr);
-    if (sl >= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fl[k]; return; }
-    if (sr <= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fr[k]; return; }
-    if (kind == FLOU_NF_HLL) {
-        for (int k = 0; k < NV; ++k) F[k] = ((sr * Fl[k] - sl * Fr[k]) + (sl * sr) * (qr[k] - ql[k])) / (sr - sl);
-        return;
+    y[0] = fma(fma(-u, a, h), dW[DIM + 1], y[0]);
+    y[DIM + 1] = fma(fma(u, a, h), dW[DIM + 1], y[DIM + 1]);
+    y[1] = fma(0.5 * v2, dW[DIM + 1], ye);
+    const double rho = mr.mean, ta = rho / (2.0 * g);
+    double z[NV];
+    z[0] = fabs(u - a) * ta * y[0];
+    z[1] = fabs(u) * (g1 * rho / g) * y[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) z[1 + k] = fabs(u) * phat * y[1 + k];
+    z[DIM + 1] = fabs(u + a) * ta * y[DIM + 1];
+    const double zs = z[0] + z[1] + z[DIM + 1];
+    double o[NV];
+    o[0] = zs;
+    o[1] = fma(u - a, z[0], fma(u, z[1], (u + a) * z[DIM + 1]));
+    o[DIM + 1] = fma(fma(-u, a, h), z[0], fma(0.5 * v2, z[1], fma(u, a, h) * z[DIM + 1]));
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        o[1 + k] = fma(vm[k], zs, z[1 + k]);
+        o[DIM + 1] = fma(vm[k], z[1 + k], o[DIM + 1]);
     }
-    double ml = rl * (sl - ul), mr = rr * (sr - ur);
-    double ss = ((pr - pl) + ul * ml - ur * mr) / (ml - mr);
-    bool left = ss >= 0.0;
-    const double* qk = left ? ql : qr;
-    const double* Fk = left ? Fl : Fr;
-    double sk = left ? sl : sr, mk = left ? ml : mr, rk = left ? rl : rr, uk = left ? ul : ur, pk = left ? pl : pr;
-    double coef = mk / (sk - ss);
-    double Us[NV];
-    Us[0] = coef;
-    Us[1] = coef * ss;
-    for (int k = 1; k < DIM; ++k) Us[1 + k] = coef * (qk[1 + k] / rk);
-    Us[DIM + 1] = coef * (qk[DIM + 1] / rk + (ss - uk) * (ss + pk / mk));
-    for (int k = 0; k < NV; ++k) F[k] = Fk[k] + sk * (Us[k] - qk[k]);
+    const double c = 0.5 * intensity;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) F[k] = fma(c, o[k], A[k]);
 }
 
 // Signed axes of a Cartesian face frame (n, t, b) for a master at local position `pos`: the
@@ -435,6 +448,18 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
     Us[DIM + 1] = coef * fma(ss - uk, ss + pm, qk[DIM + 1] * irk);
 #pragma unroll
     for (int k = 0; k < NV; ++k) F[k] = fma(sk, Us[k] - qk[k], Fk[k]);
+}
+
+// numericalflux(Ql, Qr, n, eq, kind) in the face frame: the entropy-based fluxes through
+// euler_face_flux_es, the others through euler_face_flux_fast.
+template <int DIM>
+__device__ __forceinline__ void euler_numflux(const double* ql, const double* qr, int kind, int avg,
+                                              double intensity, double g, double* F) {
+    if (kind == FLOU_NF_CHANDRASHEKAR || kind >= FLOU_NF_SCALAR_DISSIPATION ||
+        (kind == FLOU_NF_LXF && avg == FLOU_NF_CHANDRASHEKAR))
+        euler_face_flux_es<DIM>(ql, qr, kind, avg, intensity, g, F);
+    else
+        euler_face_flux_fast<DIM>(ql, qr, kind, intensity, g, F);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -558,11 +583,7 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
             }
         }
         double Fr[NV];
-        if (P.numflux == FLOU_NF_CHANDRASHEKAR || P.numflux >= FLOU_NF_SCALAR_DISSIPATION ||
-            (P.numflux == FLOU_NF_LXF && P.lxf_avg == FLOU_NF_CHANDRASHEKAR))
-            euler_face_flux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
-        else
-            euler_face_flux_fast<DIM>(a, b, P.numflux, inten, P.gamma, Fr);
+        euler_numflux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
         if (CURV) {
             rotate_to_phys<DIM>(Fr, fr, F);
         } else {
@@ -1266,7 +1287,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                         a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
                         b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
                     }
-                    euler_face_flux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                    euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
                     const double Js = P.elem_Ja[e * DIM + dir];
                     Fv[0] = Fr[0] * Js;
                     Fv[DIM + 1] = Fr[DIM + 1] * Js;
@@ -1339,8 +1360,18 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     if (active) surface_and_update<DIM, N, NV, LGL, CURV, !(GAUSS && HYB)>(P, sops, e, i, q, dq);
 }
 
+// Register cap of the split-form kernels (0: none): resident blocks per SM = 64K / (BLOCK * cap).
+#ifndef FLOU_SPLIT_REGCAP
+#define FLOU_SPLIT_REGCAP 0
+#endif
+template <int BLOCK>
+constexpr int split_min_blocks() {
+    return FLOU_SPLIT_REGCAP > 0 && 65536 / (BLOCK * FLOU_SPLIT_REGCAP) > 1 ? 65536 / (BLOCK * FLOU_SPLIT_REGCAP) : 1;
+}
+
 template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false, bool HYB = false>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_split_kernel(ElemParams P) {
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, split_min_blocks<Shape<DIM, N>::BLOCK>())
+    elem_split_kernel(ElemParams P) {
     extern __shared__ double smem[];
     if (P.dtp && *P.dtp == 0.0) return;   // CFL stepping past tfinal: the state stays as it is
     split_tile<DIM, N, EQ, TP, LGL, 256, CURV, HYB>(P, blockIdx.x * Shape<DIM, N>::EPB, smem);

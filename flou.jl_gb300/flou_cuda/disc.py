@@ -269,11 +269,15 @@ class Context:
             raise TypeError("state must be a numpy array or a torch tensor")
         if a.numel() != self.ndofs * self.nvars or not a.is_contiguous() or str(a.dtype) != "torch.float64":
             raise ValueError("state tensor must be a contiguous float64 tensor (nvars, ndofs)")
-        _torch_stream_sync(a)
+        if a.is_cuda:   # torch's pending writes to `a` complete first, unless both share a stream
+            import torch
+            if torch.cuda.current_stream(a.device).cuda_stream != getattr(self, "_stream", 0):
+                _torch_stream_sync(a)
         return ctypes.c_void_p(a.data_ptr()), (L.PTR_DEVICE if a.is_cuda else L.PTR_HOST)
 
     def set_stream(self, stream_ptr):
         L.check(self._lib.flou_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h)
+        self._stream = int(stream_ptr or 0)
 
     def rhs(self, dQ, Q, t=0.0):
         pd, kd = self._ptr(dQ, True)
