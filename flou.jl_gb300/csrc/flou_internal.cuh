@@ -944,6 +944,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     constexpr int NPROJ = GAUSS ? 2 * S::EPB * NFD : 0;       // projected states, 2 per line
     constexpr int SST = NN + NPROJ;                            // stride of the per-node arrays
     constexpr int NPTX = NPT + (GAUSS ? NPROJ * N : 0);        // + node x projected-state fluxes
+    static_assert(!GAUSS || Lay::NARR >= NV, "the line reductions reuse the projected columns");
     double* sops = smem;
     double* sprim = sops + S::NOPS;                 // [Lay::NARR][SST]
     double* spair = sprim + Lay::NARR * SST;        // [NV][NPTX]
@@ -1026,7 +1027,8 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     vv = fma(vp[k], vp[k], vv);
                 }
                 double sv = g - (g - 1.0) * (w[0] - wl * vv * 0.5);
-                double pp = pow(pow(-wl, g) * exp(sv), 1.0 / (1.0 - g));
+                // ((-W_last)^γ e^s)^(1/(1-γ)) as one exponential
+                double pp = exp(fma(g, log(-wl), sv) / (1.0 - g));
                 double rho = -pp * wl;
                 qp[0] = rho;
 #pragma unroll
@@ -1148,6 +1150,26 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             for (int k = 0; k < NV; ++k) spair[k * NPTX + kp] = F[k];
         }
         __syncthreads();
+        if constexpr (GAUSS) {   // l·F♯(·, Q̃_l) and r·F♯(·, Q̃_r) once per line, into the projected columns
+            for (int t = tid; t < NPROJ; t += blockDim.x) {
+                int elp = t / (2 * NFD);
+                if (e0 + elp >= P.nelem) continue;
+                int rr = t - elp * 2 * NFD, side = rr & 1;
+                const double* lv = sops + 2 * N * N + side * N;
+                const int xb = NPT + 2 * N * (elp * NFD + (rr >> 1)) + side;
+                double acc[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) acc[k] = fma(lv[j], spair[k * NPTX + xb + 2 * j], acc[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < NV; ++k) sprim[k * SST + NN + t] = acc[k];
+            }
+            __syncthreads();
+        }
         // ---- node phase: dQ_i -= Ja_dd sum_j D♯_ij F♯(i, j) ----
         if (active) {
             int pos, line;
@@ -1204,24 +1226,12 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             double Ja = CURV ? 1.0 : P.elem_Ja[e * DIM + dir];   // CURV: the metric is in the fluxes
             double Fl[NV], Fr[NV];   // GAUSS: F♯(Q_i, Q̃) - l·F♯(·, Q̃) at both ends (OpDivergence.jl:410-425)
             if constexpr (GAUSS) {
-                const double* lvl = sops + 2 * N * N;
-                const double* lvr = lvl + N;
                 const int xb = NPT + 2 * N * (el * NFD + line);
-                double lF[NV], rF[NV];
-#pragma unroll
-                for (int k = 0; k < NV; ++k) lF[k] = rF[k] = 0.0;
-#pragma unroll
-                for (int j = 0; j < N; ++j) {
-#pragma unroll
-                    for (int k = 0; k < NV; ++k) {
-                        lF[k] = fma(lvl[j], spair[k * NPTX + xb + 2 * j], lF[k]);
-                        rF[k] = fma(lvr[j], spair[k * NPTX + xb + 2 * j + 1], rF[k]);
-                    }
-                }
+                const int cl = NN + 2 * (el * NFD + line);   // the line's reductions, left and right
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
-                    Fl[k] = spair[k * NPTX + xb + 2 * pos] - lF[k];
-                    Fr[k] = spair[k * NPTX + xb + 2 * pos + 1] - rF[k];
+                    Fl[k] = spair[k * NPTX + xb + 2 * pos] - sprim[k * SST + cl];
+                    Fr[k] = spair[k * NPTX + xb + 2 * pos + 1] - sprim[k * SST + cl + 1];
                 }
             }
             if constexpr (HYB) {
