@@ -815,14 +815,16 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
 // formulas share one reciprocal.
 // ---------------------------------------------------------------------------------------
 // Shared per-node arrays (length NN each) of the split form, by two-point flux:
-//   Chandrashekar:  rh = ρ/2, vh_k = v_k/2, bh = β/2 = ρ/(4p), vq = |v|²/4
+//   Chandrashekar:  rh = ρ/2, vh_k = v_k/2, bh = β/2 = ρ/(4p)
 //   Kennedy-Gruber: rh = ρ/2, vh_k = v_k/2, ph = p/2, eh = e/2 (e = ρe/ρ)
 //   StdAverage:     v_k, p, then the conserved variables
 //   scalar equations: u
 template <int DIM, int EQ, int TP>
 struct SplitLayout {
     static constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
-    static constexpr int NARR = (EQ != FLOU_EQ_EULER) ? 1 : (TP == FLOU_TP_STD_AVERAGE ? DIM + 1 + NV : DIM + 3);
+    static constexpr int NARR = (EQ != FLOU_EQ_EULER) ? 1
+                                : (TP == FLOU_TP_STD_AVERAGE ? DIM + 1 + NV
+                                                             : (TP == FLOU_TP_CHANDRASHEKAR ? DIM + 2 : DIM + 3));
 };
 
 // Chandrashekar two-point flux (Euler.jl:474-536) along direction d without the metric
@@ -839,7 +841,6 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     const double* rh = S;
     const double* vh = S + NN;
     const double* bh = S + (1 + DIM) * NN;
-    const double* vq = S + (2 + DIM) * NN;
     double rh1 = rh[i], rh2 = rh[l], bh1 = bh[i], bh2 = bh[l];
     double hsr = rh1 + rh2, dhr = rh1 - rh2;   // (ρ1+ρ2)/2, (ρ1-ρ2)/2
     double hsb = bh1 + bh2, dhb = bh1 - bh2;
@@ -868,14 +869,14 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     }
     double p = 0.5 * hsr * rb;                 // (ρ1+ρ2)/(2(β1+β2))
     double va[DIM];
-    double vv = 0.0;
+    double dot = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
         va[k] = vh[k * NN + i] + vh[k * NN + l];
-        vv = fma(va[k], va[k], vv);
+        dot = fma(vh[k * NN + i], vh[k * NN + l], dot);
     }
-    // h = 1/(2β(γ-1)) - (|v1|²+|v2|²)/4 + p/ρ + |v̄|²
-    double h = fma(inv_beta_ln, c_beta, -(vq[i] + vq[l])) + fma(p, inv_rho_ln, vv);
+    // h = 1/(2β(γ-1)) - (|v1|²+|v2|²)/4 + p/ρ + |v̄|², with |v̄|² - (|v1|²+|v2|²)/4 = v1·v2/2 = 2 vh1·vh2
+    double h = fma(inv_beta_ln, c_beta, fma(p, inv_rho_ln, 2.0 * dot));
     if (GEN) {
         double vn = 0.0;
 #pragma unroll
@@ -896,16 +897,15 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
 }
 
 // The per-node quantities of SplitLayout for one state (q conserved, v velocity, p pressure,
-// vv = |v|², ir = 1/ρ), written at column `col` of arrays with stride `st`.
+// ir = 1/ρ), written at column `col` of arrays with stride `st`.
 template <int DIM, int TP>
 __device__ __forceinline__ void store_split_node(double* S, int st, int col, const double* q, const double* v,
-                                                 double p, double vv, double ir) {
+                                                 double p, double ir) {
     if (TP == FLOU_TP_CHANDRASHEKAR) {
         S[col] = 0.5 * q[0];
 #pragma unroll
         for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
         S[(1 + DIM) * st + col] = (0.25 * q[0]) / p;
-        S[(2 + DIM) * st + col] = 0.25 * vv;
     } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
         S[col] = 0.5 * q[0];
 #pragma unroll
@@ -973,12 +973,11 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
         for (int k = 0; k < NV; ++k) q[k] = P.Q[k * P.ndofs + gi];
         if (EULER) {
             double ir = 1.0 / q[0];
-            double ke = 0.0, vv = 0.0;
+            double ke = 0.0;
 #pragma unroll
             for (int k = 0; k < DIM; ++k) {
                 v[k] = q[1 + k] * ir;
                 ke = fma(q[1 + k], v[k], ke);
-                vv = fma(v[k], v[k], vv);
             }
             p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
             if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
@@ -990,7 +989,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 for (int k = 0; k < DIM; ++k) sW[(1 + k) * NN + tid] = q[1 + k] * ip;
                 sW[(DIM + 1) * NN + tid] = -q[0] * ip;
             }
-            if constexpr (EULER) store_split_node<DIM, TP>(sprim, SST, tid, q, v, p, vv, ir);
+            if constexpr (EULER) store_split_node<DIM, TP>(sprim, SST, tid, q, v, p, ir);
         } else {
             sprim[tid] = q[0];
         }
@@ -1035,7 +1034,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 for (int k = 0; k < DIM; ++k) qp[1 + k] = rho * vp[k];
                 qp[DIM + 1] = pp / (g - 1.0) + 0.5 * rho * vv;
                 if (!(rho > 0.0 && pp > 0.0)) raise_nonphysical(P.status, e0 + elp);
-                store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, vv, 1.0 / rho);
+                store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, 1.0 / rho);
             }
             __syncthreads();
         }
@@ -1174,7 +1173,11 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
         if (active) {
             int pos, line;
             tp_coords<DIM>(N, i, dir, pos, line);
-            double Fd[NV];   // F♯(i, i): the physical flux along dir (CURV: the contravariant flux)
+            // F♯(i, i): the physical flux along dir (CURV: the contravariant flux).  Its weight D♯_ii
+            // vanishes for an exact SBP operator, but the computed diagonal carries the round-off
+            // that keeps the rows of D♯ summing to zero: dropping it loses discrete conservation
+            // against a large constant pressure (the TGV's p0 = 1/(γM²)).
+            double Fd[NV];
             if (CURV) {
                 double an = 0.0, mn = 0.0, vn = 0.0;
 #pragma unroll
