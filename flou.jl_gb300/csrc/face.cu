@@ -39,6 +39,8 @@ cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t 
     return cudaErrorInvalidValue;
 }
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
+    if (L.curv && L.vol == FLOU_OP_HYBRID)
+        return L.dim == 2 ? launch_elem_curv_hybrid2d(L, P, s) : launch_elem_curv_hybrid3d(L, P, s);
     if (L.curv) return L.dim == 2 ? launch_elem_curv2d(L, P, s) : launch_elem_curv3d(L, P, s);
     if (L.eq != FLOU_EQ_EULER) return launch_elem_scalar(L, P, s);
     if (!L.lgl && L.vol != FLOU_OP_STRONG) {   // entropy-projected Gauss-node operators

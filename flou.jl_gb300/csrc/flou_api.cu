@@ -73,6 +73,8 @@ int ready(flou_ctx* c) {
     if (!c->have_geom) return fail(c, FLOU_ERR_STATE, "flou_set_geometry has not been called");
     if (c->cfg.volume_op == FLOU_OP_HYBRID && !c->have_hybrid)
         return fail(c, FLOU_ERR_STATE, "flou_set_hybrid has not been called (hybrid operator)");
+    if (c->cfg.volume_op == FLOU_OP_HYBRID && c->curv && !c->d_subJ)
+        return fail(c, FLOU_ERR_STATE, "flou_set_subgrid has not been called (hybrid operator, general geometry)");
     for (int f = 0; f < c->nfaces; ++f) {
         int b = c->h_face_bc[f];
         if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
@@ -134,6 +136,8 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.a1 = a1;
     P.aux = mode == 3 ? const_cast<double*>(Q0) : nullptr;   // the 2N register travels in Q0's slot
     P.dtp = c->d_gate;
+    P.subfr = c->d_subfr;
+    P.subJ = c->d_subJ;
     P.gamma = c->cfg.gamma;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     P.status = c->d_status;
@@ -523,7 +527,8 @@ int32_t flou_destroy(flou_ctx* c) {
     drop_graph(c);
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
                     c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c, c->d_invJn, c->d_Jan,
-                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1, c->d_cfl, c->d_cflmin};
+                    c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1, c->d_cfl, c->d_cflmin,
+                    c->d_subfr, c->d_subJ};
     for (void* b : bufs)
         if (b) cudaFree(b);
     ctx_free_limiter(c);
@@ -660,9 +665,6 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
                                              "boundary nodes (LGL)");
     if (curv && c->cfg.equation == FLOU_EQ_BURGERS)
         return fail(c, FLOU_ERR_UNSUPPORTED, "Burgers' equation is 1D");
-    if (curv && c->cfg.volume_op == FLOU_OP_HYBRID)
-        return fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator covers Cartesian geometry (its subcell frames "
-                                             "are those of the axes)");
     std::vector<double> Jel(c->nelem);
     for (int e = 0; e < c->nelem; ++e) Jel[e] = J[(size_t)e * c->npe];
     if ((r = upload(c, &c->d_Jel, Jel.data(), Jel.size(), "geometry upload"))) return r;
@@ -726,6 +728,30 @@ int32_t flou_set_integrator(flou_ctx* c, int32_t nstages, const double* A, const
         c->lsrk_A[i] = i ? A[i] : 0.0;
         c->lsrk_B[i] = B[i];
     }
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_subgrid(flou_ctx* c, const double* frames, const double* jac) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_ops || !c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_subgrid needs the operators and the mesh");
+    if (!frames || !jac) return fail(c, FLOU_ERR_ARG, "null subgrid array");
+    const int d = c->cfg.dim, n = c->n;
+    const size_t ns = (size_t)c->nelem * d * c->nfd * (n + 1);
+    for (size_t i = 0; i < ns; ++i) {
+        const double* f = frames + 9 * i;
+        double nn = 0.0;
+        for (int q = 0; q < d; ++q) nn += f[q] * f[q];
+        if (!(jac[i] > 0.0) || !std::isfinite(jac[i]) || !(fabs(nn - 1.0) < 1e-10))
+            return fail(c, FLOU_ERR_ARG, "subgrid point %zu: the surface Jacobian must be positive and the normal a "
+                                         "unit vector", i);
+    }
+    std::vector<double> soa(9 * ns);
+    for (size_t i = 0; i < ns; ++i)
+        for (int q = 0; q < 9; ++q) soa[q * ns + i] = frames[9 * i + q];
+    int r;
+    if ((r = upload(c, &c->d_subfr, soa.data(), soa.size(), "subgrid upload"))) return r;
+    if ((r = upload(c, &c->d_subJ, jac, ns, "subgrid upload"))) return r;
     drop_graph(c);
     return FLOU_OK;
 }

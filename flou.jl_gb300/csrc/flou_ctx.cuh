@@ -71,6 +71,9 @@ struct flou_ctx {
     // step method of flou_step: 0 stages = Shu-Osher SSP-RK3, else a 2N-storage method
     int lsrk_s = 0;
     double lsrk_A[FLOU_MAX_LSRK_STAGES], lsrk_B[FLOU_MAX_LSRK_STAGES];
+    // subcell-interface geometry of general elements (flou_set_subgrid): [9][ns] frames, [ns] J
+    double* d_subfr = nullptr;
+    double* d_subJ = nullptr;
     // CFL-limited stepping (flou_step_cfl): the step state lives on the device
     double* d_cfl = nullptr;        // [0] t, [1] dt of the step (0 once t reached tfinal), [2] tfinal,
                                     // [3] dtmax, [4] steps taken, [5] 1 when no positive dt was found

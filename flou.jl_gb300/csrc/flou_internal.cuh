@@ -63,6 +63,8 @@ struct ElemParams {
     double dt, a0, a1;
     double* aux;                 // mode 3: the 2N-storage register k, read and rewritten per node
     const double* dtp;           // CFL stepping: dt lives in device memory (0: the run is over, skip)
+    const double* subfr;         // CURV hybrid: [9][ns] n, t, b of each subcell interface
+    const double* subJ;          //   and its surface Jacobian; point ((e·DIM + dir)·n^(d-1) + line)·(n+1) + s
     double gamma;
     double adv[3];
     int32_t* status;             // [0] flags, [1] lowest offending element (1-based)
@@ -1284,9 +1286,9 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                             for (int k = 0; k < NV; ++k) Fh[k] += sH[k * NN + j];
                         }
                     }
-                    // FV flux in the frame of the positive axis, times the subcell surface
-                    // Jacobian (PhysicalRegions.jl:68-148: Ja_dd of the Cartesian element)
-                    FrameAxes A = frame_axes<DIM>(2 * dir + 1);
+                    // FV flux in the subcell interface's frame times its surface Jacobian
+                    // (PhysicalRegions.jl:68-300): the positive axis and Ja_dd on a Cartesian
+                    // element, the uploaded subgrid geometry on a general one
                     double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV];
                     const int64_t gl = (int64_t)e * NPE + (il - el * NPE);
 #pragma unroll
@@ -1294,18 +1296,38 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                         ql[k] = P.Q[k * P.ndofs + gl];
                         qr[k] = q[k];
                     }
-                    a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+                    if constexpr (CURV) {
+                        const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+                        const int64_t si = (((int64_t)e * DIM + dir) * NFD + line) * (N + 1) + pos;
+                        FrameTab fr;
 #pragma unroll
-                    for (int r = 0; r < DIM; ++r) {
-                        a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
-                        b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
+                        for (int r = 0; r < 3; ++r) {
+                            fr.n[r] = P.subfr[r * ns + si];
+                            fr.t[r] = P.subfr[(3 + r) * ns + si];
+                            fr.b[r] = P.subfr[(6 + r) * ns + si];
+                        }
+                        rotate_to_face<DIM>(ql, fr, a);
+                        rotate_to_face<DIM>(qr, fr, b);
+                        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                        rotate_to_phys<DIM>(Fr, fr, Fv);
+                        const double Js = P.subJ[si];
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) Fv[k] = Fv[k] * Js;
+                    } else {
+                        FrameAxes A = frame_axes<DIM>(2 * dir + 1);
+                        a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+#pragma unroll
+                        for (int r = 0; r < DIM; ++r) {
+                            a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
+                            b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
+                        }
+                        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                        const double Js = P.elem_Ja[e * DIM + dir];
+                        Fv[0] = Fr[0] * Js;
+                        Fv[DIM + 1] = Fr[DIM + 1] * Js;
+#pragma unroll
+                        for (int r = 0; r < DIM; ++r) Fv[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]) * Js;
                     }
-                    euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
-                    const double Js = P.elem_Ja[e * DIM + dir];
-                    Fv[0] = Fr[0] * Js;
-                    Fv[DIM + 1] = Fr[DIM + 1] * Js;
-#pragma unroll
-                    for (int r = 0; r < DIM; ++r) Fv[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]) * Js;
                     if constexpr (GAUSS) {   // blended in the scan below
 #pragma unroll
                         for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = Fv[k];
@@ -1512,9 +1534,38 @@ cudaError_t launch_elem_gauss_dim(int n, int tp, const ElemParams& P, cudaStream
 }
 
 // Curvilinear variants (LGL only): strong form and split form per two-point flux.
+// The hybrid operator on general elements (Euler), one per two-point flux.
+template <int DIM, int N>
+cudaError_t launch_elem_n_curv_hybrid(int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (tp) {
+        case FLOU_TP_STD_AVERAGE:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, FLOU_OP_HYBRID, FLOU_TP_STD_AVERAGE, true, true>(P, s, prep);
+        case FLOU_TP_CHANDRASHEKAR:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, FLOU_OP_HYBRID, FLOU_TP_CHANDRASHEKAR, true, true>(P, s, prep);
+        case FLOU_TP_KENNEDY_GRUBER:
+            return launch_elem_one<DIM, N, FLOU_EQ_EULER, FLOU_OP_HYBRID, FLOU_TP_KENNEDY_GRUBER, true, true>(P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int DIM>
+cudaError_t launch_elem_dim_curv_hybrid(int n, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (n) {
+        case 2: return launch_elem_n_curv_hybrid<DIM, 2>(tp, P, s, prep);
+        case 3: return launch_elem_n_curv_hybrid<DIM, 3>(tp, P, s, prep);
+        case 4: return launch_elem_n_curv_hybrid<DIM, 4>(tp, P, s, prep);
+        case 5: return launch_elem_n_curv_hybrid<DIM, 5>(tp, P, s, prep);
+        case 6: return launch_elem_n_curv_hybrid<DIM, 6>(tp, P, s, prep);
+        case 7: return launch_elem_n_curv_hybrid<DIM, 7>(tp, P, s, prep);
+        case 8: return launch_elem_n_curv_hybrid<DIM, 8>(tp, P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 template <int DIM, int N, int EQ>
 cudaError_t launch_elem_n_curv(int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
     if (vol == FLOU_OP_STRONG) return launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, true, true>(P, s, prep);
+    if (vol != FLOU_OP_SPLIT) return cudaErrorInvalidValue;
     if (EQ != FLOU_EQ_EULER)
         return launch_elem_one<DIM, N, EQ, FLOU_OP_SPLIT, FLOU_TP_STD_AVERAGE, true, true>(P, s, prep);
     switch (tp) {
@@ -1559,6 +1610,8 @@ cudaError_t launch_elem_euler3d_split(const ElemLaunch& L, const ElemParams& P, 
 cudaError_t launch_elem_euler3d_hybrid(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_scalar(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss1d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_curv_hybrid2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_curv_hybrid3d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss3d_hybrid(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);

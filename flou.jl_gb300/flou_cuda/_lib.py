@@ -102,6 +102,7 @@ PROTOTYPES = {
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
     "flou_set_hybrid": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double],
     "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
+    "flou_set_subgrid": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "flou_set_integrator": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "flou_step_cfl": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                       ctypes.c_int32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)],

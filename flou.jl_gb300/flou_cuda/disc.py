@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib as L
-from .unstructured import UnstructuredMesh, unstructured_geometry
+from .unstructured import UnstructuredMesh, unstructured_geometry, unstructured_subgrid
 from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, EulerInflowBC, GenericBC, HLL, HLLC,
                         LinearAdvection, LxF, SplitDivOperator, StdAverage, StrongDivOperator)
 
@@ -178,7 +178,18 @@ class MultielementDisc:
             bc_kinds=kinds, bc_states=np.ascontiguousarray(states),
             J=self.J, Ja=np.ascontiguousarray(self.Ja), frames=np.ascontiguousarray(self.frames), faceJ=self.faceJ,
             hybrid=self._hybrid_params(),
+            subgrid=self._subgrid(),
         )
+
+    def _subgrid(self):
+        """Subcell-interface frames and Jacobians (flou_set_subgrid layout) of a hybrid operator on
+        an UnstructuredMesh, else None (Cartesian elements use the axes)."""
+        if getattr(self.operator, "code", None) != L.OP_HYBRID or not isinstance(self.mesh, UnstructuredMesh):
+            return None
+        if getattr(self, "_subgrid_cache", None) is None:
+            fr, jac = unstructured_subgrid(self.mesh, self.std)
+            self._subgrid_cache = (np.ascontiguousarray(fr.reshape(-1, 9)), np.ascontiguousarray(jac.ravel()))
+        return self._subgrid_cache
 
     def _hybrid_params(self):
         """(fvflux, its central flux, intensity, blend) of a HybridDivOperator, else None."""
@@ -240,6 +251,9 @@ class Context:
         if a.get("hybrid") is not None:
             fv, fvavg, fvint, blend = a["hybrid"]
             L.check(lib.flou_set_hybrid(h, int(fv), int(fvavg), float(fvint), float(blend)), h)
+        if a.get("subgrid") is not None:
+            fr, jac = a["subgrid"]
+            L.check(lib.flou_set_subgrid(h, d(fr), d(jac)), h)
         nd = ctypes.c_int64()
         nv = ctypes.c_int32()
         L.check(lib.flou_sizes(h, ctypes.byref(nd), ctypes.byref(nv), None, None), h)

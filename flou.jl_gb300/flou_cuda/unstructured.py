@@ -505,3 +505,69 @@ def unstructured_geometry(mesh, std):
             faceJ[fs, m] = jac
     return (J.ravel(), Ja.reshape(ne * npe, d * d), frames.reshape(nf * nfd, 9), faceJ.ravel(),
             coords.reshape(ne * npe, 3))
+
+
+def subgrid_points(omega):
+    """The n + 1 subcell interfaces of one direction (StdSegment.jl:60-73): the running sums of the
+    weights from both ends, averaged, with the ends at exactly -1 and 1."""
+    n = len(omega)
+    a = np.empty(n + 1)
+    b = np.empty(n + 1)
+    a[0], b[n] = -1.0, 1.0
+    for i in range(n):
+        a[i + 1] = a[i] + omega[i]
+    for i in range(n - 1, -1, -1):
+        b[i] = b[i + 1] - omega[i]
+    c = (a + b) / 2
+    c[0], c[n] = -1.0, 1.0
+    return c
+
+
+def unstructured_subgrid(mesh, std):
+    """Frames (n, t, b) and surface Jacobians of the subcell interfaces of every element of an
+    UnstructuredMesh (PhysicalRegions.jl:180-300), the geometry the hybrid operator's subcell
+    finite-volume fluxes use: for direction d, line m (the face-dof order of a face normal to d)
+    and interface s = 0..n, the point with ξ_d = ξc[s] and the line's node coordinates on the other
+    axes.  Returns frames (nelem, d, n^(d-1), n + 1, 9) and jac (nelem, d, n^(d-1), n + 1)."""
+    d, n = mesh.dim, std.n
+    xi, xc = std.xi1d, subgrid_points(std.omega1d)
+    ne, nfd = mesh.nelements, n ** (d - 1)
+    P = [mesh.nodes[mesh.elements[:, k]] for k in range(2 ** d)]
+    frames = np.zeros((ne, d, nfd, n + 1, 9))
+    jac = np.zeros((ne, d, nfd, n + 1))
+    for ax in range(d):
+        others = [q for q in range(d) if q != ax]
+        for m in range(nfd):
+            rest = np.unravel_index(m, (n,) * (d - 1), order="F") if d > 1 else ()
+            for s in range(n + 1):
+                pt = [0.0] * d
+                pt[ax] = xc[s]
+                for k, q in enumerate(others):
+                    pt[q] = xi[rest[k]]
+                main = _main_basis(d, P, [(v + 1) / 2 for v in pt])
+                dual = _dual_basis(d, main)
+                out = np.zeros((ne, 9))
+                if d == 1:
+                    sg = np.sign(_jacobian(d, main))[:, None]
+                    nv = sg * dual[0][:, None] if dual[0].ndim == 1 else sg * dual[0]
+                    jv = np.ones(ne)
+                    out[:, :1] = nv
+                elif d == 2:
+                    sg = np.sign(_jacobian(d, main))[:, None]
+                    nv = sg * dual[ax]
+                    mo = main[1 - ax]
+                    out[:, 3:5] = (1.0 if ax == 0 else -1.0) * sg * mo / np.linalg.norm(mo, axis=1)[:, None]
+                    jv = np.linalg.norm(nv, axis=1)
+                    out[:, :2] = nv / jv[:, None]
+                else:
+                    nv = dual[ax]
+                    mt = main[(ax + 1) % 3]
+                    tv = mt / np.linalg.norm(mt, axis=1)[:, None]
+                    bv = np.cross(nv, tv)
+                    jv = np.linalg.norm(nv, axis=1)
+                    out[:, :3] = nv / jv[:, None]
+                    out[:, 3:6] = tv
+                    out[:, 6:9] = bv / np.linalg.norm(bv, axis=1)[:, None]
+                frames[:, ax, m, s] = out
+                jac[:, ax, m, s] = jv
+    return frames, jac

@@ -149,6 +149,13 @@ int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, cons
  * its central flux and intensity) and blending constant c (δ = max((√(b²+c) - b)/√(b²+c), 1/2),
  * OpDivergence.jl:777-801).  Required before the first residual of a FLOU_OP_HYBRID context. */
 int32_t flou_set_hybrid(flou_ctx* ctx, int32_t fvflux, int32_t fvflux_avg, double fvflux_intensity, double blend);
+/* Subcell-interface geometry of general (curvilinear / unstructured) elements, which the hybrid
+ * operator's subcell finite-volume fluxes need (geometry.subgrids, PhysicalRegions.jl:180-300):
+ * for element e, direction d, line m (the face-dof order of a face normal to d) and interface
+ * s = 0..n of that line, point ((e·dim + d)·n^(dim-1) + m)·(n+1) + s holds the unit normal, tangent
+ * and binormal (9 doubles in `frames`, zero-padded to 3 components) and the surface Jacobian
+ * (`jac`).  Required before stepping a hybrid context whose geometry is not Cartesian. */
+int32_t flou_set_subgrid(flou_ctx* ctx, const double* frames, const double* jac);
 
 /* ---- residual and stepping ------------------------------------------------------------- */
 /* FlouCommon.rhs!(dQ, Q, p::EquationConfig{<:MultielementDisc,<:HyperbolicEquation}, t)

@@ -917,6 +917,10 @@ struct Disc {
     std::vector<double> Ds, Dsharp, ll, lr, dgl, dgr;
     std::vector<double> D, omega1d;       // derivative matrix, 1D weights (HybridDivOperator)
     bool lobatto = true;                  // hasboundaries(basis): l_l, l_r pick the end nodes
+    // subcell-interface geometry of general elements (geometry.subgrids, PhysicalRegions.jl:180-300):
+    // point ((e·dim + d)·nfd + line)·(n+1) + s; empty on Cartesian meshes (the axes)
+    std::vector<Frame> subframes;
+    std::vector<double> subjac;
     // connectivity (1-based, like the reference)
     std::vector<int> faceinds, facepos;   // nelem * 2dim
     std::vector<int> eleminds, elempos;   // nfaces * 2
@@ -1131,6 +1135,7 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                 Frame fr = subgrid_frame(dim, dir);
                 double Js = g.Ja[base * dim * dim + dir + dir * dim];
                 for (int line = 0; line < nfd; ++line) {
+                    long sbase = (((long)e * dim + dir) * nfd + line) * (n + 1);
                     for (int ii = 0; ii <= n; ++ii) Fb[ii] = Vec<T>{};
                     for (int ii = 1; ii < n; ++ii) {
                         for (int ik = ii; ik < n; ++ik) {
@@ -1145,11 +1150,14 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                             }
                         }
                         int i = tp_node(dim, n, dir, line, ii), il = tp_node(dim, n, dir, line, ii - 1);
-                        Vec<T> Qln = rotate2face(getv(Q, nd, base + il, nv), fr, c);
-                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + i, nv), fr, c);
-                        Vec<T> Fn = numericalflux(Qln, Qrn, fr.n, fv, c.fvflux, T(c.fvintensity));
-                        Vec<T> Fv = rotate2phys(Fn, fr, c);
-                        for (int q = 0; q < nv; ++q) Fv[q] = Fv[q] * Js;
+                        const bool gen = !g.subjac.empty();   // frames[dir][is], Js[dir][is] of the element
+                        const Frame& sf = gen ? g.subframes[sbase + ii] : fr;
+                        double sJ = gen ? g.subjac[sbase + ii] : Js;
+                        Vec<T> Qln = rotate2face(getv(Q, nd, base + il, nv), sf, c);
+                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + i, nv), sf, c);
+                        Vec<T> Fn = numericalflux(Qln, Qrn, sf.n, fv, c.fvflux, T(c.fvintensity));
+                        Vec<T> Fv = rotate2phys(Fn, sf, c);
+                        for (int q = 0; q < nv; ++q) Fv[q] = Fv[q] * sJ;
                         T bb = T(0.0);
                         for (int q = 0; q < nv; ++q) bb = bb + (W[i][q] - W[il][q]) * (Fb[ii][q] - Fv[q]);
                         T dl = hybrid_delta(bb, c.blend);

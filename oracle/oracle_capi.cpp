@@ -345,6 +345,22 @@ void oracle_set_hybrid(void* hp, int fvflux, int fvavg, double fvintensity, doub
     h->g.D.assign(D, D + (size_t)n * n);
 }
 
+// Subcell-interface frames (9 doubles per point) and surface Jacobians of general elements, in
+// the layout of flou_set_subgrid.
+void oracle_set_subgrid(void* hp, const double* frames, const double* jac) {
+    Handle* h = (Handle*)hp;
+    Disc& g = h->g;
+    size_t ns = (size_t)g.nelem * g.cfg.dim * g.nfd * (g.n + 1);
+    g.subframes.resize(ns);
+    g.subjac.assign(jac, jac + ns);
+    for (size_t i = 0; i < ns; ++i)
+        for (int q = 0; q < 3; ++q) {
+            g.subframes[i].n[q] = frames[9 * i + q];
+            g.subframes[i].t[q] = frames[9 * i + 3 + q];
+            g.subframes[i].b[q] = frames[9 * i + 6 + q];
+        }
+}
+
 void oracle_limit(void* hp, double* Q, double minval, const double* omega_tp) {
     Handle* h = (Handle*)hp;
     std::vector<double> w(omega_tp, omega_tp + h->g.npe);

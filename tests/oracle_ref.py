@@ -44,9 +44,10 @@ def lib():
         _lib.oracle_monitor.argtypes = [ctypes.c_void_p, D, ctypes.c_int, D]
         _lib.oracle_ssprk3_limited.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                                ctypes.c_double, D]
+        _lib.oracle_set_subgrid.argtypes = [ctypes.c_void_p, D, D]
         _lib.oracle_lsrk2n.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, D, D, D, ctypes.c_double, D]
-        _lib.oracle_count_rhs.argtypes =[ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
+        _lib.oracle_count_rhs.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
         _lib.oracle_solve_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D, D, D]
@@ -135,6 +136,9 @@ class Disc:
             Dm = np.asfortranarray(a["D"], dtype=np.float64)
             self._keep = (adv, a, om, Dm)
             L.oracle_set_hybrid(self.h, int(fv), int(fvavg), float(fvint), float(blend), _d(om), _d(Dm))
+        if a.get("subgrid") is not None:
+            fr, jac = a["subgrid"]
+            L.oracle_set_subgrid(self.h, _d(np.ascontiguousarray(fr)), _d(np.ascontiguousarray(jac)))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -22,6 +22,11 @@ def _ops():
         "split_chandra_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
         "split_kg_lxf": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
         "split_std_lxf": lambda: F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)),
+        # blend 0.5: dδ/db ~ 1/√c, so a small blending constant amplifies round-off in the indicator
+        "hybrid_hllc": lambda: F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(),
+                                                   F.LxF(F.ChandrasekharAverage(), 1.0), 0.5),
+        "hybrid_md": lambda: F.HybridDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), 1.0),
+        "hybrid_kg": lambda: F.HybridDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0), 1e-3),
     }
 
 
@@ -69,8 +74,36 @@ def test_unstructured_euler(dim, n, op):
     _check(disc, _state(disc, seed=dim + n))
 
 
+@pytest.mark.parametrize("dim,n,op", [(2, 4, "hybrid_hllc"), (2, 5, "hybrid_md"), (2, 6, "hybrid_kg"),
+                                      (3, 3, "hybrid_hllc"), (3, 4, "hybrid_md"), (3, 5, "hybrid_kg"),
+                                      (3, 7, "hybrid_hllc")])
+def test_unstructured_hybrid(dim, n, op):
+    """HybridDivOperator on perturbed, rotated elements: the subcell FV fluxes in the uploaded
+    subcell-interface frames (flou_set_subgrid), against the oracle."""
+    disc = _disc(dim, n, op, nel=2 if n > 6 else 3)
+    _check(disc, _state(disc, seed=dim * 3 + n))
+
+
+def test_unstructured_hybrid_p7_against_the_oracles_conditioning():
+    """p = 7 on curved 3D elements: the oracle's own residual moves by ~5e-13 when its input is
+    perturbed by one ulp (the split form's too), so the device is held to four times that spread."""
+    disc = _disc(3, 8, "hybrid_hllc", nel=2)
+    Q = _state(disc, seed=17)
+    o = oracle_for(disc)
+    ref = o.rhs(Q)
+    rng = np.random.default_rng(0)
+    spread = rel_linf(o.rhs(Q * (1 + 2.2e-16 * rng.choice([-1.0, 1.0], size=Q.shape))), ref)
+    dQ = disc.new_state()
+    disc.ctx.rhs(dQ, Q)
+    assert rel_linf(dQ, ref) <= max(1e-12, 4 * spread)
+    dt = 0.2 * disc.ctx.max_dt(Q, 1.0)
+    Qg = Q.copy(order="F")
+    disc.ctx.step(Qg, dt, 3)
+    assert rel_linf(Qg, o.ssprk3(Q, dt, 3)) <= 1e-10
+
+
 @pytest.mark.parametrize("dim,op", [(2, "strong_lxf"), (2, "split_chandra_lxfc"), (3, "split_chandra_lxfc"),
-                                    (3, "strong_hllc")])
+                                    (3, "strong_hllc"), (2, "hybrid_md"), (3, "hybrid_hllc")])
 def test_unstructured_walls_inflow_outflow(dim, op):
     disc = _disc(dim, 4, op, walls=True)
     _check(disc, _state(disc, seed=11))
