@@ -146,6 +146,26 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
     fJ = Vector{Float64}(g.faces.jac)
     GC.@preserve J Ja frames fJ check(ccall((:flou_set_geometry, libflou), Int32,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx, J, Ja, frames, fJ), ctx)
+    if op isa HybridDivOperator && !(mesh isa CartesianMesh)
+        # subcell-interface geometry (geometry.subgrids, PhysicalRegions.jl:180-300) in the layout of
+        # flou_set_subgrid: element, direction, line (tpdofs_subgrid order), interface
+        n = length(disc.std.basis.ξ)
+        nfd = n^(ND - 1)
+        sfr = zeros(Float64, 9, n + 1, nfd, ND, ne)
+        sjac = zeros(Float64, n + 1, nfd, ND, ne)
+        for ie in 1:ne, d in 1:ND
+            sg = g.subgrids[ie]
+            for (m, sinds) in enumerate(Flou.tpdofs_subgrid(disc.std, Val(d))), (s, is) in enumerate(sinds)
+                f = sg.frames[d][is]
+                sfr[1:ND, s, m, d, ie] .= f.n
+                sfr[4:3+ND, s, m, d, ie] .= f.t
+                ND == 3 && (sfr[7:9, s, m, d, ie] .= f.b)
+                sjac[s, m, d, ie] = sg.jac[d][is]
+            end
+        end
+        GC.@preserve sfr sjac check(ccall((:flou_set_subgrid, libflou), Int32,
+            (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), ctx, sfr, sjac), ctx)
+    end
     gd = GPUDisc{ND,RT,typeof(disc)}(disc, ctx)
     finalizer(x -> ccall((:flou_destroy, libflou), Int32, (Ptr{Cvoid},), x.ctx), gd)
     return gd
