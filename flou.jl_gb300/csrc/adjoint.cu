@@ -772,7 +772,8 @@ int adj_supported(flou_ctx* c) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
                                                  "the Chandrashekar split form, and the LxF(StdAverage) or "
                                                  "LxF(ChandrasekharAverage) flux");
-    if (!c->bnodes) return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL)");
+    if (!c->lift_ends)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
     if (c->lsrk_s)

@@ -136,6 +136,7 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.a1 = a1;
     P.aux = mode == 3 ? const_cast<double*>(Q0) : nullptr;   // the 2N register travels in Q0's slot
     P.dtp = c->d_gate;
+    P.lift_ends = c->lift_ends ? 1 : 0;
     P.subfr = c->d_subfr;
     P.subJ = c->d_subJ;
     P.gamma = c->cfg.gamma;
@@ -571,13 +572,25 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
     // way the reference builds them carry round-off in the entries that vanish on Gauss-Lobatto
     // nodes, so this test has a tolerance; Gauss nodes are far from it.
     bool bnodes = fabs(l_l[0] - 1.0) < 1e-10 && fabs(l_r[n - 1] - 1.0) < 1e-10;
+    bool lift_ends = true;   // ∂g vanishes off the end nodes (DGSEM on Gauss-Lobatto nodes; not VCJH)
     for (int i = 0; i < n; ++i) {
-        if (i != 0 && (fabs(l_l[i]) > 1e-10 || fabs(dg_l[i]) > 1e-10 * fabs(dg_l[0]))) bnodes = false;
-        if (i != n - 1 && (fabs(l_r[i]) > 1e-10 || fabs(dg_r[i]) > 1e-10 * fabs(dg_r[n - 1]))) bnodes = false;
+        if (i != 0 && fabs(l_l[i]) > 1e-10) bnodes = false;
+        if (i != n - 1 && fabs(l_r[i]) > 1e-10) bnodes = false;
+        if (i != 0 && fabs(dg_l[i]) > 1e-10 * fabs(dg_l[0])) lift_ends = false;
+        if (i != n - 1 && fabs(dg_r[i]) > 1e-10 * fabs(dg_r[n - 1])) lift_ends = false;
     }
     // Without boundary nodes the split and hybrid operators couple the volume to the faces
     // through entropy-projected states (OpDivergence.jl:301-437, 614-780): Euler only, since
     // the scalar equations have no entropy variables in the reference.
+    // The hybrid operator on a basis with boundary nodes sums 2 ω_l D_lk F♯ (OpDivergence.jl:557-
+    // 604), whatever the reconstruction: its telescoped form uses 2D - B with the corner B of
+    // DGSEM (-1/ω_1, 1/ω_n), which equals the given D♯ only when ∂g acts on the end nodes alone.
+    if (c->cfg.volume_op == FLOU_OP_HYBRID && bnodes) {
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) ops[n * n + i + j * n] = 2.0 * D[i + j * n];
+        ops[n * n] += 1.0 / omega[0];
+        ops[n * n + (n - 1) + (n - 1) * n] -= 1.0 / omega[n - 1];
+    }
     if (c->cfg.volume_op != FLOU_OP_STRONG && !bnodes && c->cfg.equation != FLOU_EQ_EULER)
         return fail(c, FLOU_ERR_UNSUPPORTED,
                     "the split-form and hybrid operators of the scalar equations need a basis with boundary "
@@ -587,6 +600,7 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
     if ((r = upload(c, &c->d_omega1, omega, (size_t)n, "operator upload"))) return r;
     c->lgl = lgl;
     c->bnodes = bnodes;
+    c->lift_ends = bnodes && lift_ends;
     c->omega.assign(omega, omega + n);
     c->have_ops = true;
     drop_graph(c);

@@ -16,6 +16,7 @@ struct flou_ctx {
     int nv = 0, n = 0, npe = 0, nfd = 0;
     bool lgl = false;               // l_l = e_1, l_r = e_n exactly: the kernels skip the zero terms
     bool bnodes = false;            // the basis has boundary nodes (hasboundaries), to round-off
+    bool lift_ends = false;         // and ∂g vanishes off the end nodes (DGSEM; not a VCJH correction)
     std::string err;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     bool have_ops = false, have_mesh = false, have_geom = false;

@@ -63,6 +63,7 @@ struct ElemParams {
     double dt, a0, a1;
     double* aux;                 // mode 3: the 2N-storage register k, read and rewritten per node
     const double* dtp;           // CFL stepping: dt lives in device memory (0: the run is over, skip)
+    int32_t lift_ends;           // the lift ∂g acts on the end nodes only (else: every node of the line)
     const double* subfr;         // CURV hybrid: [9][ns] n, t, b of each subcell interface
     const double* subJ;          //   and its surface Jacobian; point ((e·DIM + dir)·n^(d-1) + line)·(n+1) + s
     double gamma;
@@ -662,7 +663,7 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         int64_t ol = (int64_t)(pl >> 1) * ipow(N, DIM - 1) + linel;
         int64_t orr = (int64_t)(pr >> 1) * ipow(N, DIM - 1) + liner;
         double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
-        if (LGL) {
+        if (LGL && P.lift_ends) {
             if (pos == 0) {
                 double c = dgl[0] * sl;
 #pragma unroll

@@ -12,7 +12,7 @@ from .equations import (BurgersEquation, ChandrasekharAverage, DirichletBC, Eule
                         StrongDivOperator)
 from .mesh import CartesianMesh, apply_periodicBCs
 from .unstructured import UnstructuredMesh, perturbed_box, read_gmsh, write_gmsh22
-from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment
+from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment, VCJHrec
 from .timeint import (ORK256, SSPRK33, CarpenterKennedy2N54, LowStorageRK2N, get_cfl_callback, get_limiter_callback,
                       get_monitor_callback, get_save_callback, make_callback_list, timeintegrate)
 from . import initial

@@ -132,12 +132,36 @@ class DGSEMrec:
         self.basis = basis
 
 
+class VCJHrec:
+    """VCJHrec(p, η) (Reconstruction.jl:69-110): the energy-stable flux-reconstruction correction
+    functions of Vincent, Castonguay and Jameson, g_l = (-1)^(p-1) (L_{p-1} - (η L_{p-2} + L_p)/(1+η))/2
+    and g_r = (L_{p-1} + (η L_{p-2} + L_p)/(1+η))/2 with Legendre polynomials L_k; η = 0 (:DGSEM_GL)
+    is DGSEM on Gauss nodes, η = (p-1)/p (:SD), η = p/(p-1) (:Huynh)."""
+
+    def __init__(self, p, eta):
+        self.p = int(p)
+        if isinstance(eta, str):
+            key = eta.lstrip(":")
+            eta = {"DGSEM_GL": 0.0, "SD": (self.p - 1) / self.p, "Huynh": self.p / (self.p - 1)}[key]
+        self.eta = float(eta)
+
+    def derivatives(self, x):
+        from numpy.polynomial import legendre as Lg
+        p, eta = self.p, self.eta
+        unit = lambda k: np.eye(k + 1)[k] if k >= 0 else np.zeros(1)
+        Lkm, Lk, Lkp = unit(p - 2), unit(p - 1), unit(p)
+        mix = Lg.legadd(Lg.legmul(eta, Lkm), Lkp) / (1.0 + eta)
+        gl = (-1.0) ** (p - 1) * Lg.legsub(Lk, mix) / 2.0
+        gr = Lg.legadd(Lk, mix) / 2.0
+        return Lg.legval(x, Lg.legder(gl)), Lg.legval(x, Lg.legder(gr))
+
+
 class _StdRegion:
     dim = 0
 
     def __init__(self, basis, rec, nvars=1):
-        if not isinstance(rec, DGSEMrec):
-            raise ValueError("only DGSEM reconstructions are supported")
+        if not isinstance(rec, (DGSEMrec, VCJHrec)):
+            raise ValueError("the reconstructions are DGSEMrec and VCJHrec")
         self.basis = basis
         self.reconstruction = rec
         x, w = basis.xi, basis.omega
@@ -148,7 +172,11 @@ class _StdRegion:
         ll = interp_matrix([-1.0], x)[0]
         lr = interp_matrix([1.0], x)[0]
         D = derivative_matrix(x)
-        dgl, dgr = ll / w, lr / w   # StdSegment.jl:84-85: ∂g = (l_l/ω, l_r/ω)
+        if isinstance(rec, VCJHrec):   # StdSegment.jl:82-83: ∂g = (-g_l', g_r')
+            gl, gr = rec.derivatives(np.asarray(x))
+            dgl, dgr = -gl, gr
+        else:
+            dgl, dgr = ll / w, lr / w   # StdSegment.jl:84-85: ∂g = (l_l/ω, l_r/ω)
         B = np.outer(dgr, lr) - np.outer(dgl, ll)
         self.D = D
         self.Ds = D - B

@@ -271,3 +271,21 @@ def test_device_pointers_and_determinism():
     disc.ctx.step(b, 1e-3, 2)
     disc.ctx.step(b, 1e-3, 2)
     assert torch.equal(a, b)   # graph replays are deterministic
+
+
+@pytest.mark.parametrize("basis,eta,op", [("GLL", "SD", "strong_lxf"), ("GLL", "SD", "split_chandra_lxfc"),
+                                          ("GLL", 0.3, "hybrid_chandra_lxfc"), ("GL", "SD", "split_kg_lxf"),
+                                          ("GL", 0.0, "strong_hllc")])
+def test_vcjh_reconstructions(basis, eta, op):
+    """VCJHrec lifts (Reconstruction.jl:69-110) reach every node of a line (on Gauss-Lobatto nodes
+    Huynh's η is DGSEM again, so SD and η = 0.3 are used there); the split and hybrid kernels keep
+    their volume terms and take the general lift, the hybrid's telescoped sums use 2D - B with
+    DGSEM's corner B as the reference's 2 ω_l D_lk sums do."""
+    eq = _euler(2)
+    mesh = F.CartesianMesh((-1.0, -1.0), (1.0, 1.0), (3, 3))
+    F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"))
+    b = F.LagrangeBasis(basis, 5)
+    std = F.StdQuad(b, F.VCJHrec(5, eta), 4)
+    disc = F.MultielementDisc(mesh, std, eq, _ops()[op](), {})
+    assert np.abs(disc.std.dg[0][1:]).max() > 1e-3   # the lift is not confined to the end nodes
+    _check(disc, smooth_euler_state(disc, seed=13), cfl=0.2)
