@@ -23,22 +23,24 @@ cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStre
 }
 // General geometry: the slave trace through master2slave, per-node frames and surface Jacobians.
 template <int DIM, int EQ>
-static cudaError_t launch_face_curv_t(const FaceParams& P, cudaStream_t s) {
+static cudaError_t launch_face_curv_t(bool lgl, const FaceParams& P, cudaStream_t s) {
     int64_t nthreads = (int64_t)P.nfaces * P.nfd;
     if (nthreads == 0) return cudaSuccess;
     int grid = (int)((nthreads + 255) / 256);
-    face_kernel<DIM, EQ, true, true><<<grid, 256, 0, s>>>(P);
+    if (lgl) face_kernel<DIM, EQ, true, true><<<grid, 256, 0, s>>>(P);
+    else face_kernel<DIM, EQ, false, true><<<grid, 256, 0, s>>>(P);
     return cudaGetLastError();
 }
-cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t s) {
-    if (eq == FLOU_EQ_EULER) return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_EULER>(P, s)
-                                             : launch_face_curv_t<3, FLOU_EQ_EULER>(P, s);
+cudaError_t launch_face_curv(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s) {
+    if (eq == FLOU_EQ_EULER) return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_EULER>(lgl, P, s)
+                                             : launch_face_curv_t<3, FLOU_EQ_EULER>(lgl, P, s);
     if (eq == FLOU_EQ_LINEAR_ADVECTION)
-        return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_LINEAR_ADVECTION>(P, s)
-                        : launch_face_curv_t<3, FLOU_EQ_LINEAR_ADVECTION>(P, s);
+        return dim == 2 ? launch_face_curv_t<2, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s)
+                        : launch_face_curv_t<3, FLOU_EQ_LINEAR_ADVECTION>(lgl, P, s);
     return cudaErrorInvalidValue;
 }
 cudaError_t launch_elem(const ElemLaunch& L, const ElemParams& P, cudaStream_t s) {
+    if (L.curv && !L.lgl) return L.dim == 2 ? launch_elem_curv_gauss2d(L, P, s) : launch_elem_curv_gauss3d(L, P, s);
     if (L.curv && L.vol == FLOU_OP_HYBRID)
         return L.dim == 2 ? launch_elem_curv_hybrid2d(L, P, s) : launch_elem_curv_hybrid3d(L, P, s);
     if (L.curv) return L.dim == 2 ? launch_elem_curv2d(L, P, s) : launch_elem_curv3d(L, P, s);

@@ -73,8 +73,10 @@ int ready(flou_ctx* c) {
     if (!c->have_geom) return fail(c, FLOU_ERR_STATE, "flou_set_geometry has not been called");
     if (c->cfg.volume_op == FLOU_OP_HYBRID && !c->have_hybrid)
         return fail(c, FLOU_ERR_STATE, "flou_set_hybrid has not been called (hybrid operator)");
-    if (c->cfg.volume_op == FLOU_OP_HYBRID && c->curv && !c->d_subJ)
-        return fail(c, FLOU_ERR_STATE, "flou_set_subgrid has not been called (hybrid operator, general geometry)");
+    if (c->curv && !c->d_subJ &&
+        (c->cfg.volume_op == FLOU_OP_HYBRID || (c->cfg.volume_op == FLOU_OP_SPLIT && !c->bnodes)))
+        return fail(c, FLOU_ERR_STATE, "flou_set_subgrid has not been called (general geometry: the hybrid "
+                                       "operator, or the split form on a basis without boundary nodes)");
     for (int f = 0; f < c->nfaces; ++f) {
         int b = c->h_face_bc[f];
         if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
@@ -179,7 +181,7 @@ int stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, double
         fp.Fn = Fn;
         ep.Fn = Fn;
     }
-    cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, fp, s)
+    cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, c->lgl, fp, s)
                             : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
     e = launch_elem(elem_launch(c), ep, s);
@@ -674,9 +676,6 @@ int32_t flou_set_geometry(flou_ctx* c, const double* J, const double* Ja, const 
     bool curv = !cart || c->any_orient;
     if (curv && c->cfg.dim == 1)
         return fail(c, FLOU_ERR_UNSUPPORTED, "1D geometry must have J constant per element and the Cartesian frames");
-    if (curv && !c->bnodes)
-        return fail(c, FLOU_ERR_UNSUPPORTED, "general (curvilinear / unstructured) geometry needs a basis with "
-                                             "boundary nodes (LGL)");
     if (curv && c->cfg.equation == FLOU_EQ_BURGERS)
         return fail(c, FLOU_ERR_UNSUPPORTED, "Burgers' equation is 1D");
     std::vector<double> Jel(c->nelem);
@@ -1004,7 +1003,7 @@ int32_t flou_time_kernels(flou_ctx* c, const double* Q, int32_t nrep, double* fa
     for (int it = 0; it < nrep; ++it) {
         for (int mode = 1; mode <= 3; ++mode) {
             CK(cudaEventRecord(ev[0], c->stream), "event record");
-            cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, face_params(c, Q), c->stream)
+            cudaError_t e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), c->stream)
                                     : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, face_params(c, Q), c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
             CK(cudaEventRecord(ev[1], c->stream), "event record");
@@ -1196,7 +1195,7 @@ extern "C" int32_t flou_rhs_noalloc(flou_ctx* c, double* dQ, const double* Q, do
     if (!scratch) return cuda_fail(c, e, "flou_rhs_noalloc scratch address");
     FaceParams fp = face_params(c, Q);
     fp.Fn = scratch;
-    e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, fp, c->stream)
+    e = c->curv ? launch_face_curv(c->cfg.dim, c->cfg.equation, c->lgl, fp, c->stream)
                 : launch_face(c->cfg.dim, c->cfg.equation, c->lgl, fp, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "face kernel launch");
     ElemParams ep = elem_params(c, Q, Q, dQ, 0, 0.0, 0.0, 0.0);

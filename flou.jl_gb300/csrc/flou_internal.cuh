@@ -943,7 +943,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = S::EPB * NFD * NPAIR;   // pairs per direction in the block
     constexpr bool EULER = (EQ == FLOU_EQ_EULER);
-    constexpr bool GAUSS = !LGL && EULER && !CURV;
+    constexpr bool GAUSS = !LGL && EULER;
     constexpr int NPROJ = GAUSS ? 2 * S::EPB * NFD : 0;       // projected states, 2 per line
     constexpr int SST = NN + NPROJ;                            // stride of the per-node arrays
     constexpr int NPTX = NPT + (GAUSS ? NPROJ * N : 0);        // + node x projected-state fluxes
@@ -951,11 +951,15 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     double* sops = smem;
     double* sprim = sops + S::NOPS;                 // [Lay::NARR][SST]
     double* spair = sprim + Lay::NARR * SST;        // [NV][NPTX]
-    double* sJa = spair + NV * NPTX;                // CURV: [DIM][NN] metric column of the direction
-    double* sW = sJa + (CURV ? DIM * NN : 0);       // HYB, GAUSS: [NV][NN] entropy variables
+    double* sJa = spair + NV * NPTX;                // CURV: [DIM][SST] metric column of the direction
+                                                    // (GAUSS: then n·Js of each line end's subcell interface)
+    double* sW = sJa + (CURV ? DIM * SST : 0);      // HYB, GAUSS: [NV][NN] entropy variables
     double* sH = sW + ((HYB || GAUSS) ? NV * NN : 0);   // HYB: [NV][NN] the node's subcell increment
-    double* sFb = sH + (HYB ? NV * NN : 0);         // HYB: [NV][NN] blended flux at the node's left interface
-    uint8_t* stab = (uint8_t*)(sFb + (HYB ? NV * NN : 0));   // pair table: a, b
+    // HYB: [NV][NN] blended flux at the node's left interface; written once the node phase has read
+    // the pair fluxes, so it reuses their space when that is large enough
+    constexpr bool FB_IN_PAIRS = NPTX >= NN;
+    double* sFb = FB_IN_PAIRS ? spair : sH + (HYB ? NV * NN : 0);
+    uint8_t* stab = (uint8_t*)(sH + (HYB ? (FB_IN_PAIRS ? 1 : 2) * NV * NN : 0));   // pair table: a, b
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
     if (tid == 0) {
@@ -1038,6 +1042,13 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 qp[DIM + 1] = pp / (g - 1.0) + 0.5 * rho * vv;
                 if (!(rho > 0.0 && pp > 0.0)) raise_nonphysical(P.status, e0 + elp);
                 store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, 1.0 / rho);
+                if constexpr (CURV) {   // the line end's subcell interface: n·Js (OpDivergence.jl:403-404)
+                    const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+                    const int64_t si = (((int64_t)(e0 + elp) * DIM + dir) * NFD + line) * (N + 1) + (side ? N : 0);
+                    const double js = P.subJ[si];
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) sJa[k * SST + NN + t] = P.subfr[k * ns + si] * js;
+                }
             }
             __syncthreads();
         }
@@ -1045,7 +1056,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             if (active) {
                 int64_t g = (int64_t)e * NPE + i;
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) sJa[k * NN + tid] = P.Jan[(k + dir * DIM) * P.ndofs + g];
+                for (int k = 0; k < DIM; ++k) sJa[k * SST + tid] = P.Jan[(k + dir * DIM) * P.ndofs + g];
             }
             __syncthreads();
         }
@@ -1073,7 +1084,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             double nv[DIM];   // CURV: the averaged metric column (Ja_a + Ja_b)/2
             if (CURV) {
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) nv[k] = (sJa[k * NN + ia] + sJa[k * NN + ib]) / 2.0;
+                for (int k = 0; k < DIM; ++k) nv[k] = (sJa[k * SST + ia] + sJa[k * SST + ib]) / 2.0;
             }
             if constexpr (CURV && EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
@@ -1185,7 +1196,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 double an = 0.0, mn = 0.0, vn = 0.0;
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) {
-                    double a = sJa[k * NN + tid];
+                    double a = sJa[k * SST + tid];
                     if constexpr (EULER) {
                         mn = fma(q[1 + k], a, mn);
                         vn = fma(v[k], a, vn);
@@ -1196,7 +1207,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 if constexpr (EULER) {
                     Fd[0] = mn;
 #pragma unroll
-                    for (int k = 0; k < DIM; ++k) Fd[1 + k] = fma(q[1 + k], vn, p * sJa[k * NN + tid]);
+                    for (int k = 0; k < DIM; ++k) Fd[1 + k] = fma(q[1 + k], vn, p * sJa[k * SST + tid]);
                     Fd[DIM + 1] = (q[DIM + 1] + p) * vn;
                 } else {
                     Fd[0] = an * q[0];
@@ -1247,7 +1258,12 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     const double* lvr = lvl + N;
                     int32_t pl = P.elem_face[e * 2 * DIM + 2 * dir], pr = P.elem_face[e * 2 * DIM + 2 * dir + 1];
                     double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
-                    int64_t ol = (int64_t)(pl >> 1) * NFD + line, orr = (int64_t)(pr >> 1) * NFD + line;
+                    int linel = line, liner = line;   // CURV: a slave side reads through the orientation
+                    if (CURV) {
+                        if (pl & 1) linel = master2slave<DIM>(line, inverse_orientation<DIM>(P.orient[pl >> 1]), N);
+                        if (pr & 1) liner = master2slave<DIM>(line, inverse_orientation<DIM>(P.orient[pr >> 1]), N);
+                    }
+                    int64_t ol = (int64_t)(pl >> 1) * NFD + linel, orr = (int64_t)(pr >> 1) * NFD + liner;
 #pragma unroll
                     for (int k = 0; k < NV; ++k) {
                         fls[k] = sl * __ldcg(P.Fn + k * P.nfdofs + ol);
@@ -1420,11 +1436,13 @@ constexpr size_t elem_smem_bytes() {
     if (VOL == FLOU_OP_STRONG) return sizeof(double) * (S::NOPS + DIM * NV * S::NN);
     constexpr int NARR = SplitLayout<DIM, EQ, TP>::NARR;
     constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
-    constexpr bool GAUSS = !LGL && EQ == FLOU_EQ_EULER && !CURV;
+    constexpr bool GAUSS = !LGL && EQ == FLOU_EQ_EULER;
     constexpr int NPROJ = GAUSS ? 2 * S::EPB * S::NFD : 0;
     constexpr bool HYB = VOL == FLOU_OP_HYBRID;
-    return sizeof(double) * (S::NOPS + NARR * (S::NN + NPROJ) + NV * (NPT + NPROJ * N) + (CURV ? DIM * S::NN : 0) +
-                             (HYB ? 3 * NV * S::NN : (GAUSS ? NV * S::NN : 0))) + 2 * (S::NPAIR + 1);
+    constexpr int NPTX = NPT + NPROJ * N;
+    return sizeof(double) * (S::NOPS + NARR * (S::NN + NPROJ) + NV * NPTX + (CURV ? DIM * (S::NN + NPROJ) : 0) +
+                             (HYB ? (NPTX >= S::NN ? 2 : 3) * NV * S::NN : (GAUSS ? NV * S::NN : 0))) +
+           2 * (S::NPAIR + 1);
 }
 
 // Launch one instantiation; the dynamic shared-memory opt-in is set once per kernel.
@@ -1563,6 +1581,43 @@ cudaError_t launch_elem_dim_curv_hybrid(int n, int tp, const ElemParams& P, cuda
     }
 }
 
+// General elements on a basis without boundary nodes: the strong form (any equation on this
+// path) and the entropy-projected split and hybrid forms (Euler), one per two-point flux.
+template <int DIM, int N, int EQ>
+cudaError_t launch_elem_n_curv_gauss(int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    if (vol == FLOU_OP_STRONG) return launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, false, true>(P, s, prep);
+    if constexpr (EQ == FLOU_EQ_EULER) {
+#define FLOU_CG(VOL)                                                                                            \
+        switch (tp) {                                                                                           \
+            case FLOU_TP_STD_AVERAGE:                                                                           \
+                return launch_elem_one<DIM, N, EQ, VOL, FLOU_TP_STD_AVERAGE, false, true>(P, s, prep);          \
+            case FLOU_TP_CHANDRASHEKAR:                                                                         \
+                return launch_elem_one<DIM, N, EQ, VOL, FLOU_TP_CHANDRASHEKAR, false, true>(P, s, prep);        \
+            case FLOU_TP_KENNEDY_GRUBER:                                                                        \
+                return launch_elem_one<DIM, N, EQ, VOL, FLOU_TP_KENNEDY_GRUBER, false, true>(P, s, prep);       \
+            default: return cudaErrorInvalidValue;                                                              \
+        }
+        if (vol == FLOU_OP_SPLIT) { FLOU_CG(FLOU_OP_SPLIT) }
+        if (vol == FLOU_OP_HYBRID) { FLOU_CG(FLOU_OP_HYBRID) }
+#undef FLOU_CG
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int DIM, int EQ>
+cudaError_t launch_elem_dim_curv_gauss(int n, int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
+    switch (n) {
+        case 2: return launch_elem_n_curv_gauss<DIM, 2, EQ>(vol, tp, P, s, prep);
+        case 3: return launch_elem_n_curv_gauss<DIM, 3, EQ>(vol, tp, P, s, prep);
+        case 4: return launch_elem_n_curv_gauss<DIM, 4, EQ>(vol, tp, P, s, prep);
+        case 5: return launch_elem_n_curv_gauss<DIM, 5, EQ>(vol, tp, P, s, prep);
+        case 6: return launch_elem_n_curv_gauss<DIM, 6, EQ>(vol, tp, P, s, prep);
+        case 7: return launch_elem_n_curv_gauss<DIM, 7, EQ>(vol, tp, P, s, prep);
+        case 8: return launch_elem_n_curv_gauss<DIM, 8, EQ>(vol, tp, P, s, prep);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 template <int DIM, int N, int EQ>
 cudaError_t launch_elem_n_curv(int vol, int tp, const ElemParams& P, cudaStream_t s, bool prep) {
     if (vol == FLOU_OP_STRONG) return launch_elem_one<DIM, N, EQ, FLOU_OP_STRONG, 0, true, true>(P, s, prep);
@@ -1603,7 +1658,7 @@ struct ElemLaunch {
 };
 cudaError_t launch_elem_curv2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_curv3d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
-cudaError_t launch_face_curv(int dim, int eq, const FaceParams& P, cudaStream_t s);
+cudaError_t launch_face_curv(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler1d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_euler3d_strong(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
@@ -1612,6 +1667,8 @@ cudaError_t launch_elem_euler3d_hybrid(const ElemLaunch& L, const ElemParams& P,
 cudaError_t launch_elem_scalar(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss1d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_curv_hybrid2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_curv_gauss2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
+cudaError_t launch_elem_curv_gauss3d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_curv_hybrid3d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss2d(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);
 cudaError_t launch_elem_gauss3d_split(const ElemLaunch& L, const ElemParams& P, cudaStream_t s);

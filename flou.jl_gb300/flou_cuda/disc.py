@@ -182,9 +182,12 @@ class MultielementDisc:
         )
 
     def _subgrid(self):
-        """Subcell-interface frames and Jacobians (flou_set_subgrid layout) of a hybrid operator on
-        an UnstructuredMesh, else None (Cartesian elements use the axes)."""
-        if getattr(self.operator, "code", None) != L.OP_HYBRID or not isinstance(self.mesh, UnstructuredMesh):
+        """Subcell-interface frames and Jacobians (flou_set_subgrid layout) on an UnstructuredMesh for
+        the hybrid operator, and for the split form on a basis without boundary nodes (its projected
+        states' normals); else None (Cartesian elements use the axes)."""
+        code = getattr(self.operator, "code", None)
+        gauss_split = code == L.OP_SPLIT and not self.std.basis.hasboundaries
+        if not isinstance(self.mesh, UnstructuredMesh) or not (code == L.OP_HYBRID or gauss_split):
             return None
         if getattr(self, "_subgrid_cache", None) is None:
             fr, jac = unstructured_subgrid(self.mesh, self.std)

@@ -1029,10 +1029,19 @@ void splitdiv_nb_line(const Disc& g, const T* Q, long base, int dir, int line, c
     const Config& c = g.cfg;
     const int dim = c.dim, n = g.n, nv = c.nv;
     const long nd = g.ndofs();
+    // nl = frames[dir][i1].n Js[dir][i1], nr likewise at the last subcell interface (OpDivergence.jl:
+    // 403-404): the positive axis and Ja_dd on a Cartesian element, the subgrid data on a general one
     Frame fr = subgrid_frame(dim, dir);
     double Js = g.Ja[base * dim * dim + dir + dir * dim];
     double nl[3], nr[3];
     for (int k = 0; k < 3; ++k) { nl[k] = fr.n[k] * Js; nr[k] = fr.n[k] * Js; }
+    if (!g.subjac.empty()) {
+        long sb = (((base / g.npe) * dim + dir) * g.nfd + line) * (n + 1);
+        for (int k = 0; k < 3; ++k) {
+            nl[k] = g.subframes[sb].n[k] * g.subjac[sb];
+            nr[k] = g.subframes[sb + n].n[k] * g.subjac[sb + n];
+        }
+    }
     Vec<T> Wl{}, Wr{};
     for (int ii = 0; ii < n; ++ii) {
         int i = tp_node(dim, n, dir, line, ii);
@@ -1320,10 +1329,14 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
                         for (int k = 0; k < nv; ++k)
                             Fb[ii + 1][k] = Fb[ii][k] + sum[k] * g.omega1d[ii] - g.ll[ii] * Fl[ii][k] +
                                             g.lr[ii] * Fr[ii][k];
-                        Vec<T> Qln = rotate2face(getv(Q, nd, base + i, nv), sfr, c);
-                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + ir, nv), sfr, c);
-                        Vec<T> Fv = rotate2phys(numericalflux(Qln, Qrn, sfr.n, fv, c.fvflux, T(c.fvintensity)), sfr, c);
-                        for (int k = 0; k < nv; ++k) Fv[k] = Fv[k] * Js;
+                        const bool gen = !g.subjac.empty();   // frames[dir][sinds[ii+1]] of the element
+                        long sidx = (((long)e * dim + dir) * nfd + line) * (n + 1) + ii + 1;
+                        const Frame& f2 = gen ? g.subframes[sidx] : sfr;
+                        double J2 = gen ? g.subjac[sidx] : Js;
+                        Vec<T> Qln = rotate2face(getv(Q, nd, base + i, nv), f2, c);
+                        Vec<T> Qrn = rotate2face(getv(Q, nd, base + ir, nv), f2, c);
+                        Vec<T> Fv = rotate2phys(numericalflux(Qln, Qrn, f2.n, fv, c.fvflux, T(c.fvintensity)), f2, c);
+                        for (int k = 0; k < nv; ++k) Fv[k] = Fv[k] * J2;
                         T bb = T(0.0);
                         for (int k = 0; k < nv; ++k) bb = bb + (W[ir][k] - W[i][k]) * (Fb[ii + 1][k] - Fv[k]);
                         T dl = hybrid_delta(bb, c.blend);

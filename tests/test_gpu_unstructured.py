@@ -42,10 +42,10 @@ def _bcs(dim, eq, walls):
     return b
 
 
-def _disc(dim, n, op, walls=False, nel=3, seed=5, amp=0.12):
+def _disc(dim, n, op, walls=False, nel=3, seed=5, amp=0.12, basis="GLL"):
     eq = F.EulerEquation(dim, 1.4)
     mesh = F.perturbed_box(dim, nel, (0.0,) * dim, (1.0,) * dim, amp=amp, seed=seed)
-    return F.MultielementDisc(mesh, _std(dim, n, dim + 2), eq, _ops()[op](), _bcs(dim, eq, walls))
+    return F.MultielementDisc(mesh, _std(dim, n, dim + 2, basis), eq, _ops()[op](), _bcs(dim, eq, walls))
 
 
 def _check(disc, Q, nsteps=4):
@@ -82,6 +82,22 @@ def test_unstructured_hybrid(dim, n, op):
     subcell-interface frames (flou_set_subgrid), against the oracle."""
     disc = _disc(dim, n, op, nel=2 if n > 6 else 3)
     _check(disc, _state(disc, seed=dim * 3 + n))
+
+
+@pytest.mark.parametrize("dim,n,op", [(2, 4, "strong_lxf"), (2, 5, "split_chandra_lxfc"), (2, 4, "split_kg_lxf"),
+                                      (2, 4, "hybrid_md"), (3, 3, "strong_hllc"), (3, 4, "split_chandra_lxfc"),
+                                      (3, 3, "split_std_lxf"), (3, 4, "hybrid_hllc"), (3, 6, "split_chandra_md")])
+def test_unstructured_gauss_nodes(dim, n, op):
+    """Gauss nodes on perturbed, rotated elements: interpolated traces through master2slave, the
+    general lift, and for the split and hybrid forms the projected states with the subcell normals
+    of the line ends (flou_set_subgrid)."""
+    disc = _disc(dim, n, op, basis="GL")
+    _check(disc, _state(disc, seed=dim * 5 + n))
+
+
+def test_unstructured_gauss_nodes_walls():
+    disc = _disc(2, 4, "split_chandra_lxfc", walls=True, basis="GL")
+    _check(disc, _state(disc, seed=12))
 
 
 def test_unstructured_hybrid_p7_against_the_oracles_conditioning():
@@ -165,11 +181,12 @@ def test_general_geometry_is_rejected_where_not_covered():
     with pytest.raises(F.FlouError) as ei:
         disc.ctx.adjoint_solve(Q, 1e-3, 2, 1, Q[0].clone(), Q[0].clone(), g)
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
-    eq = F.EulerEquation(2, 1.4)
+    # the split form of a scalar equation has no Gauss-node form (no entropy variables)
     mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=1)
     b = F.LagrangeBasis("GL", 4)
-    gl = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), 4), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
-                            {str(k): F.EulerOutflowBC() for k in range(1, 5)})
+    adv = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), 1), F.LinearAdvection(1.0, 0.5),
+                             F.SplitDivOperator(F.StdAverage(), F.StdAverage()),
+                             {str(k): F.DirichletBC([1.0]) for k in range(1, 5)})
     with pytest.raises(F.FlouError) as ei:
-        gl.ctx
+        adv.ctx
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED

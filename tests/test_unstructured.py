@@ -13,16 +13,16 @@ from cases import oracle_for, smooth_euler_state
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def _std(d, n, nv):
-    b = F.LagrangeBasis("GLL", n)
+def _std(d, n, nv, basis="GLL"):
+    b = F.LagrangeBasis(basis, n)
     return {1: F.StdSegment, 2: F.StdQuad, 3: F.StdHex}[d](b, F.DGSEMrec(b), nv)
 
 
-def _disc(mesh, n, op, eq=None):
+def _disc(mesh, n, op, eq=None, basis="GLL"):
     d = mesh.dim
     eq = eq or F.EulerEquation(d, 1.4)
     bcs = {name: F.EulerOutflowBC() for name in mesh.bdnames}
-    return F.MultielementDisc(mesh, _std(d, n, eq.nvariables), eq, op, bcs)
+    return F.MultielementDisc(mesh, _std(d, n, eq.nvariables, basis), eq, op, bcs)
 
 
 def _state(disc, seed=0):
@@ -102,25 +102,39 @@ OPS = {"strong": lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)),
        "split_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
        "hybrid": lambda: F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(),
                                              F.LxF(F.ChandrasekharAverage(), 1.0), 1e-2),
-       "hybrid_md": lambda: F.HybridDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), 1.0)}
+       "hybrid_md": lambda: F.HybridDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), 1.0),
+       # δ -> 1: no blending (OpDivergence.jl:781-801 with a huge constant)
+       "hybrid_unblended": lambda: F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(),
+                                                       F.LxF(F.ChandrasekharAverage(), 1.0), 1e30),
+       # HLLC interfaces: rotation-invariant in 3D also when the traces jump (Gauss nodes)
+       "split_hllc": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()),
+       "hybrid_unblended_hllc": lambda: F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(), F.HLLC(), 1e30)}
 
 
-@pytest.mark.parametrize("dim,op", [(2, "strong"), (2, "split"), (3, "strong"), (3, "split"), (3, "split_md"),
-                                    (2, "hybrid"), (2, "hybrid_md"), (3, "hybrid")])
-def test_residual_is_invariant_under_element_rotations(dim, op):
+@pytest.mark.parametrize("dim,op,basis", [(2, "strong", "GLL"), (2, "split", "GLL"), (3, "strong", "GLL"),
+                                          (3, "split", "GLL"), (3, "split_md", "GLL"), (2, "hybrid", "GLL"),
+                                          (2, "hybrid_md", "GLL"), (3, "hybrid", "GLL"), (2, "strong", "GL"),
+                                          (2, "split", "GL"), (2, "hybrid_unblended", "GL"), (3, "strong", "GL"),
+                                          (3, "split_hllc", "GL"), (3, "hybrid_unblended_hllc", "GL")])
+def test_residual_is_invariant_under_element_rotations(dim, op, basis):
     """Rotating each element's local numbering permutes the nodes and re-orients the faces
     (all orientation codes occur in 3D); the residual at each physical node must not change.
     For the hybrid operator this also turns the subcell lines (and their subgrid frames).  Not
     for the 3D hybrid with MatrixDissipation(ChandrasekharAverage): the reference's 3D Chandrashekar
     interface flux counts wl² twice (Euler.jl:216), so it changes when the subcell frames' two
-    tangents trade places and the states jump between nodes (1.5e-7 here)."""
+    tangents trade places and the states jump between nodes (1.5e-7 here).  Nor for the blended
+    hybrid on Gauss nodes: the reference sweeps each line from its first node, every subcell flux
+    starting from the blended one before it (OpDivergence.jl:741-769), so reversing a line's
+    direction changes the result (1e-3 here); unblended (δ = 1) it is invariant.  On Gauss nodes the
+    traces jump, so the 3D cases take HLLC interfaces (the Chandrashekar interface flux's wl² term
+    would show, as above)."""
     ops = OPS
     n = 4
     plain = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=5, rotate=False)
     rot = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=5, rotate=True)
     if dim == 3:
         assert len(set(rot.orientation.tolist())) == 8
-    d0, d1 = _disc(plain, n, ops[op]()), _disc(rot, n, ops[op]())
+    d0, d1 = _disc(plain, n, ops[op](), basis=basis), _disc(rot, n, ops[op](), basis=basis)
     Q0, Q1 = _state(d0, 3), _state(d1, 3)
     R0 = oracle_for(d0).rhs(Q0)
     R1 = oracle_for(d1).rhs(Q1)
@@ -216,3 +230,25 @@ def test_hybrid_subgrid_geometry(dim):
     P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.2, 0.3, 1.7
     R = oracle_for(dp).rhs(np.asfortranarray(dp.equation.vars_prim2cons(P)))
     assert np.max(np.abs(R)) < 1e-11, np.max(np.abs(R))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gauss_nodes_on_general_elements(dim):
+    """Gauss nodes on unstructured elements: an unperturbed box reproduces the Cartesian strong,
+    split and hybrid residuals (interpolated traces, subcell normals at the line ends), and a
+    uniform flow stays uniform on perturbed elements."""
+    n, nel = 4, 3
+    um = F.perturbed_box(dim, nel, (0.0,) * dim, (2.0,) * dim, amp=0.0, rotate=False)
+    cm = F.CartesianMesh((0.0,) * dim, (2.0,) * dim, (nel,) * dim)
+    for op in ("strong", "split", "hybrid"):
+        du, dc = _disc(um, n, OPS[op](), basis="GL"), _disc(cm, n, OPS[op](), basis="GL")
+        Qu, Qc = _state(du, 4), _state(dc, 4)
+        Ru, Rc = oracle_for(du).rhs(Qu), oracle_for(dc).rhs(Qc)
+        assert np.max(np.abs(Ru - Rc)) < 1e-12 * np.max(np.abs(Rc)), op
+    pm = F.perturbed_box(dim, nel, (0.0,) * dim, (1.0,) * dim, amp=0.15, seed=7)
+    for op in ("strong", "split", "hybrid_md"):
+        dp = _disc(pm, n, OPS[op](), basis="GL")
+        P = np.zeros((dp.ndofs, dim + 2))
+        P[:, 0], P[:, 1:1 + dim], P[:, -1] = 1.2, 0.3, 1.7
+        R = oracle_for(dp).rhs(np.asfortranarray(dp.equation.vars_prim2cons(P)))
+        assert np.max(np.abs(R)) < 1e-11, (op, np.max(np.abs(R)))
