@@ -146,7 +146,8 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
     fJ = Vector{Float64}(g.faces.jac)
     GC.@preserve J Ja frames fJ check(ccall((:flou_set_geometry, libflou), Int32,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx, J, Ja, frames, fJ), ctx)
-    if op isa HybridDivOperator && !(mesh isa CartesianMesh)
+    needs_subgrid = op isa HybridDivOperator || (op isa SplitDivOperator && !Flou.hasboundaries(disc.std.basis))
+    if needs_subgrid && !(mesh isa CartesianMesh)
         # subcell-interface geometry (geometry.subgrids, PhysicalRegions.jl:180-300) in the layout of
         # flou_set_subgrid: element, direction, line (tpdofs_subgrid order), interface
         n = length(disc.std.basis.ξ)
