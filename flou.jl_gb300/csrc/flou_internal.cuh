@@ -1412,17 +1412,21 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     if (active) surface_and_update<DIM, N, NV, LGL, CURV, !(GAUSS && HYB)>(P, sops, e, i, q, dq);
 }
 
-// Register cap of the split-form kernels (0: none): resident blocks per SM = 64K / (BLOCK * cap).
+// Register cap of the plain 3D split-form kernels: resident blocks per SM = 64K / (BLOCK * cap).
+// 64 registers (a few spilled words) measured 1.5% faster at p = 7 and 0.6% at p = 3 than the
+// compiler's 101; the hybrid, Gauss-node and curvilinear variants keep their registers.
 #ifndef FLOU_SPLIT_REGCAP
-#define FLOU_SPLIT_REGCAP 0
+#define FLOU_SPLIT_REGCAP 64
 #endif
-template <int BLOCK>
+template <int BLOCK, bool CAPPED>
 constexpr int split_min_blocks() {
-    return FLOU_SPLIT_REGCAP > 0 && 65536 / (BLOCK * FLOU_SPLIT_REGCAP) > 1 ? 65536 / (BLOCK * FLOU_SPLIT_REGCAP) : 1;
+    return CAPPED && FLOU_SPLIT_REGCAP > 0 && 65536 / (BLOCK * FLOU_SPLIT_REGCAP) > 1
+               ? 65536 / (BLOCK * FLOU_SPLIT_REGCAP) : 1;
 }
 
 template <int DIM, int N, int EQ, int TP, bool LGL, bool CURV = false, bool HYB = false>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, split_min_blocks<Shape<DIM, N>::BLOCK>())
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK,
+                                  split_min_blocks<Shape<DIM, N>::BLOCK, DIM == 3 && LGL && !CURV && !HYB>())
     elem_split_kernel(ElemParams P) {
     extern __shared__ double smem[];
     if (P.dtp && *P.dtp == 0.0) return;   // CFL stepping past tfinal: the state stays as it is
