@@ -781,7 +781,7 @@ int adj_supported(flou_ctx* c) {
     if (c->curv)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers Cartesian geometry");
     for (int b = 0; b < c->nbcs; ++b)
-        if (c->bc_kind[b] == FLOU_BC_INFLOW)
+        if (c->bc_kind[b] == FLOU_BC_INFLOW || c->bc_kind[b] == FLOU_BC_STATE_FIELD)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint supports periodic, slip and outflow boundaries");
     return FLOU_OK;
 }

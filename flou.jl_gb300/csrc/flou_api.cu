@@ -81,6 +81,8 @@ int ready(flou_ctx* c) {
         int b = c->h_face_bc[f];
         if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
             return fail(c, FLOU_ERR_STATE, "boundary index %d of face %d has no boundary condition", b + 1, f + 1);
+        if (b >= 0 && c->bc_kind[b] == FLOU_BC_STATE_FIELD && !c->d_bcfield)
+            return fail(c, FLOU_ERR_STATE, "flou_set_bc_field has not been called (boundary %d)", b + 1);
     }
     int e = ensure(c, &c->d_Fn, (size_t)c->nfdofs * c->nv, "face-flux buffer");
     return e;
@@ -94,6 +96,7 @@ FaceParams face_params(const flou_ctx* c, const double* Q) {
     P.face_elem = c->d_face_elem;
     P.faceJ = c->d_faceJ;
     P.face_bc = c->d_face_bc;
+    P.bc_field = c->d_bcfield;
     P.l = c->d_ops + 2 * c->n * c->n;
     P.elem_c = c->d_c;
     P.ndofs = c->ndofs;
@@ -531,7 +534,7 @@ int32_t flou_destroy(flou_ctx* c) {
     void* bufs[] = {c->d_ops, c->d_elem_face, c->d_face_elem, c->d_face_bc, c->d_faceJ, c->d_invJ, c->d_Ja, c->d_dx,
                     c->d_Fn, c->d_U, c->d_Qh, c->d_dQh, c->d_status, c->d_dtmin, c->d_c, c->d_invJn, c->d_Jan,
                     c->d_frames, c->d_faceJn, c->d_orient, c->d_Jn, c->d_omega1, c->d_cfl, c->d_cflmin,
-                    c->d_subfr, c->d_subJ};
+                    c->d_subfr, c->d_subJ, c->d_bcfield};
     for (void* b : bufs)
         if (b) cudaFree(b);
     ctx_free_limiter(c);
@@ -648,7 +651,7 @@ int32_t flou_set_bcs(flou_ctx* c, int32_t nbcs, const int32_t* kinds, const doub
     if (nbcs > 0 && !kinds) return fail(c, FLOU_ERR_ARG, "null kinds");
     for (int b = 0; b < nbcs; ++b) {
         int k = kinds[b];
-        if (k != FLOU_BC_OUTFLOW && k != FLOU_BC_INFLOW && k != FLOU_BC_SLIP)
+        if (k != FLOU_BC_OUTFLOW && k != FLOU_BC_INFLOW && k != FLOU_BC_SLIP && k != FLOU_BC_STATE_FIELD)
             return fail(c, FLOU_ERR_ARG, "unknown boundary condition kind %d", k);
         if (k == FLOU_BC_SLIP && c->cfg.equation != FLOU_EQ_EULER)
             return fail(c, FLOU_ERR_ARG, "slip walls apply to the Euler equations only");
@@ -659,6 +662,24 @@ int32_t flou_set_bcs(flou_ctx* c, int32_t nbcs, const int32_t* kinds, const doub
         c->bc_kind[b] = b < nbcs ? kinds[b] : 0;
         for (int k = 0; k < 5; ++k) c->bc_state[b][k] = (b < nbcs && states) ? states[b * 5 + k] : 0.0;
     }
+    drop_graph(c);
+    return FLOU_OK;
+}
+
+int32_t flou_set_bc_field(flou_ctx* c, const double* states) {
+    if (!c) return FLOU_ERR_ARG;
+    if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh must come before flou_set_bc_field");
+    if (!states) return fail(c, FLOU_ERR_ARG, "null boundary states");
+    const size_t nf = (size_t)c->nfdofs;
+    std::vector<double> soa((size_t)c->nv * nf);
+    for (size_t i = 0; i < nf; ++i)
+        for (int k = 0; k < c->nv; ++k) {
+            double v = states[5 * i + k];
+            if (!std::isfinite(v)) return fail(c, FLOU_ERR_ARG, "non-finite boundary state at face node %zu", i);
+            soa[k * nf + i] = v;
+        }
+    int r = upload(c, &c->d_bcfield, soa.data(), soa.size(), "boundary-state upload");
+    if (r) return r;
     drop_graph(c);
     return FLOU_OK;
 }
@@ -1182,6 +1203,8 @@ extern "C" int32_t flou_rhs_noalloc(flou_ctx* c, double* dQ, const double* Q, do
         int b = c->h_face_bc[f];
         if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
             return fail(c, FLOU_ERR_STATE, "boundary index %d of face %d has no boundary condition", b + 1, f + 1);
+        if (b >= 0 && c->bc_kind[b] == FLOU_BC_STATE_FIELD && !c->d_bcfield)
+            return fail(c, FLOU_ERR_STATE, "flou_set_bc_field has not been called (boundary %d)", b + 1);
     }
     if (!dQ || !Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
     int64_t need = c->nfdofs * c->nv;

@@ -72,6 +72,7 @@ struct flou_ctx {
     // step method of flou_step: 0 stages = Shu-Osher SSP-RK3, else a 2N-storage method
     int lsrk_s = 0;
     double lsrk_A[FLOU_MAX_LSRK_STAGES], lsrk_B[FLOU_MAX_LSRK_STAGES];
+    double* d_bcfield = nullptr;    // [nv][nfdofs] FLOU_BC_STATE_FIELD states
     // subcell-interface geometry of general elements (flou_set_subgrid): [9][ns] frames, [ns] J
     double* d_subfr = nullptr;
     double* d_subJ = nullptr;

@@ -41,6 +41,7 @@ struct FaceParams {
     double adv[3];
     int32_t bc_kind[MAXBC];
     double bc_state[MAXBC][5];
+    const double* bc_field;      // [NV][nfdofs]: FLOU_BC_STATE_FIELD states per face node
     // general (curvilinear / unstructured) geometry, read by the CURV kernels only
     const double* frames;        // [9][nfdofs]: n, t, b of every face node (master ordering)
     const double* faceJn;        // [nfdofs] surface Jacobian of every face node
@@ -546,6 +547,8 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         int kind = P.bc_kind[b];
         if (kind == FLOU_BC_INFLOW) {
             for (int k = 0; k < NV; ++k) qr[k] = P.bc_state[b][k];
+        } else if (kind == FLOU_BC_STATE_FIELD) {
+            for (int k = 0; k < NV; ++k) qr[k] = P.bc_field[k * P.nfdofs + gid];
         } else if (kind == FLOU_BC_SLIP && EQ == FLOU_EQ_EULER) {
             // EulerSlipBC (Euler.jl:88-94): rotate to the face frame, flip the normal momentum,
             // rotate back -- for a Cartesian frame, the momentum along the normal axis changes sign.

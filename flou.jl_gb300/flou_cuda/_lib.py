@@ -25,7 +25,7 @@ NF_STD_AVERAGE, NF_LXF, NF_CHANDRASHEKAR, NF_HLL, NF_HLLC = 0, 1, 2, 3, 4
 NF_SCALAR_DISSIPATION, NF_MATRIX_DISSIPATION = 5, 6
 LIMITER_NONE, LIMITER_ZHANG_SHU = 0, 1
 MONITOR_KINETIC_ENERGY, MONITOR_ENTROPY = 1, 2
-BC_OUTFLOW, BC_INFLOW, BC_SLIP = 1, 2, 3
+BC_OUTFLOW, BC_INFLOW, BC_SLIP, BC_STATE_FIELD = 1, 2, 3, 4
 PTR_HOST, PTR_DEVICE = 0, 1
 
 STATUS_NAMES = {
@@ -102,6 +102,7 @@ PROTOTYPES = {
     "flou_adjoint_solve": [_P, _P, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _P, _P, _D, _P, _P, _I64],
     "flou_set_hybrid": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double],
     "flou_set_limiter": [_P, ctypes.c_int32, ctypes.c_double],
+    "flou_set_bc_field": [_P, ctypes.POINTER(ctypes.c_double)],
     "flou_set_subgrid": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "flou_set_integrator": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "flou_step_cfl": [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64,

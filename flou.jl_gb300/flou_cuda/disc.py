@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib as L
 from .unstructured import UnstructuredMesh, unstructured_geometry, unstructured_subgrid
 from .equations import (BurgersEquation, ChandrasekharAverage, EulerEquation, EulerInflowBC, GenericBC, HLL, HLLC,
-                        LinearAdvection, LxF, SplitDivOperator, StdAverage, StrongDivOperator)
+                        LinearAdvection, LxF, SplitDivOperator, StateFieldBC, StdAverage, StrongDivOperator)
 
 
 class DofHandler:
@@ -108,33 +108,50 @@ class MultielementDisc:
         self._ctx = None
 
     def _boundary_face_coords(self, ib):
-        """Physical coordinates of the face nodes of boundary `ib` (1-based), as the trace
-        Σ_i l_i x_i of the master element's node coordinates across the face (Interfaces.jl:51-109;
-        exact for the linear element mappings)."""
+        """(faces, coordinates) of the face nodes of boundary `ib` (1-based): the boundary's face
+        indices (0-based) and, per face in face-dof order, the trace Σ_i l_i x_i of the master
+        element's node coordinates across the face (Interfaces.jl:51-109; exact for the linear
+        element mappings)."""
         m, s = self.mesh, self.std
         n, d = s.n, m.dim
+        faces = np.nonzero(np.asarray(m.bdface_index) == ib)[0]
         out = []
-        for f in np.nonzero(np.asarray(m.bdface_index) == ib)[0]:
+        for f in faces:
             e, pos = int(m.eleminds[f, 0]) - 1, int(m.elempos[f, 0]) - 1
             X = self.coords[e * n ** d:(e + 1) * n ** d, :d].reshape((n,) * d + (d,), order="F")
             lv = s.l[pos % 2]
-            out.append(np.tensordot(X, lv, axes=([pos // 2], [0])).reshape(-1, d))
-        return np.concatenate(out) if out else np.zeros((0, d))
+            # the remaining axes in order, the first fastest: the face-dof (line) order
+            out.append(np.tensordot(X, lv, axes=([pos // 2], [0])).reshape(-1, d, order="F"))
+        return faces, (np.stack(out) if out else np.zeros((0, n ** (d - 1), d)))
 
     def _resolve_generic_bcs(self):
         for ib, bc in enumerate(self.bcs):
             if not isinstance(bc, GenericBC):
                 continue
+            faces, X = self._boundary_face_coords(ib + 1)
             try:
-                vals = [np.asarray(bc.Qext(None, x, None, 0.0, self.equation), dtype=np.float64)
-                        for x in self._boundary_face_coords(ib + 1)]
+                vals = np.array([[np.asarray(bc.Qext(None, x, None, 0.0, self.equation), dtype=np.float64)
+                                  for x in Xf] for Xf in X])
             except Exception as exc:   # Qext reads the interior state or the frame
                 raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "GenericBC on boundary %d: Qext must give the external "
                                   "state from the position alone (%s)" % (ib + 1, exc)) from exc
-            if not vals or any(not np.array_equal(v, vals[0]) for v in vals):
-                raise L.FlouError(L.FLOU_ERR_UNSUPPORTED, "GenericBC on boundary %d: the external state varies "
-                                  "along the boundary; one state per boundary is supported" % (ib + 1))
-            self.bcs[ib] = EulerInflowBC(vals[0])
+            flat = vals.reshape(-1, vals.shape[-1]) if vals.size else vals
+            if vals.size and np.all(flat == flat[0]):
+                self.bcs[ib] = EulerInflowBC(flat[0])
+            else:
+                self.bcs[ib] = StateFieldBC({int(f): v for f, v in zip(faces, vals)})
+
+    def _bc_field(self):
+        """flou_set_bc_field's array (nfaces·n^(d-1) x 5) when a boundary holds a varying state."""
+        fields = [b for b in self.bcs if isinstance(b, StateFieldBC)]
+        if not fields:
+            return None
+        nfd = self.std.n ** (self.mesh.dim - 1)
+        out = np.zeros((self.mesh.nfaces * nfd, 5))
+        for b in fields:
+            for f, v in b.states.items():
+                out[f * nfd:(f + 1) * nfd, :v.shape[1]] = v
+        return out
 
     # -- C ABI configuration ------------------------------------------------------------
     def _config(self):
@@ -179,6 +196,7 @@ class MultielementDisc:
             J=self.J, Ja=np.ascontiguousarray(self.Ja), frames=np.ascontiguousarray(self.frames), faceJ=self.faceJ,
             hybrid=self._hybrid_params(),
             subgrid=self._subgrid(),
+            bc_field=self._bc_field(),
         )
 
     def _subgrid(self):
@@ -257,6 +275,8 @@ class Context:
         if a.get("subgrid") is not None:
             fr, jac = a["subgrid"]
             L.check(lib.flou_set_subgrid(h, d(fr), d(jac)), h)
+        if a.get("bc_field") is not None:
+            L.check(lib.flou_set_bc_field(h, d(np.ascontiguousarray(a["bc_field"]))), h)
         nd = ctypes.c_int64()
         nv = ctypes.c_int32()
         L.check(lib.flou_sizes(h, ctypes.byref(nd), ctypes.byref(nv), None, None), h)

@@ -91,15 +91,26 @@ class EulerSlipBC:
 
 
 class GenericBC:
-    """GenericBC(Qext) with Qext(Qin, x, frame, time, equation) (FlouSpatial.jl:80-91).  The device
-    holds one external state per boundary, so MultielementDisc evaluates Qext at every face node
-    of the boundary (Qin = frame = None, time = 0) and accepts it when the state is the same at
-    all of them; it then acts as EulerInflowBC(state)."""
+    """GenericBC(Qext) with Qext(Qin, x, frame, time, equation) (FlouSpatial.jl:80-91).
+    MultielementDisc evaluates Qext at every face node of the boundary (Qin = frame = None,
+    time = 0): one state everywhere acts as EulerInflowBC(state); a state varying along the
+    boundary is uploaded per face node (FLOU_BC_STATE_FIELD).  A Qext that reads the interior
+    state or the frame is rejected; one that depends on time is evaluated at t = 0."""
 
     def __init__(self, Qext):
         self.Qext = Qext
         self.kind = L.BC_INFLOW
         self.state = None
+
+
+class StateFieldBC:
+    """A GenericBC resolved per face node: `states` maps each of the boundary's face nodes
+    (face index, face dof) to its external state."""
+
+    def __init__(self, states):
+        self.kind = L.BC_STATE_FIELD
+        self.state = None
+        self.states = states
 
 
 DirichletBC = EulerInflowBC   # constant state for the scalar equations

@@ -129,15 +129,29 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
         ctx, ne, nf, faceinds, facepos, eleminds, elempos, orient, bdidx), ctx)
     kinds = Int32[bc isa EulerSlipBC ? 3 : (bc isa EulerInflowBC || bc isa GenericBC) ? 2 : 1 for bc in disc.bcs]
     states = zeros(Float64, 5, length(kinds))
+    nfd = length(disc.std.basis.ξ)^(ND - 1)
+    field = nothing   # flou_set_bc_field's states, 5 per face node, face by face
     for (i, bc) in enumerate(disc.bcs)
         bc isa EulerInflowBC && (states[1:length(bc.Qext), i] .= bc.Qext)
-        if bc isa GenericBC   # one external state per boundary (FlouSpatial.jl:80-91)
+        if bc isa GenericBC   # FlouSpatial.jl:80-91
             q = genericbc_state(bc, disc, i, equation)
-            states[1:length(q), i] .= q
+            if q isa Vector   # one external state on the whole boundary: an inflow state
+                states[1:length(q), i] .= q
+            else              # a state per face node: FLOU_BC_STATE_FIELD
+                kinds[i] = 4
+                field === nothing && (field = zeros(Float64, 5, nfd * nf))
+                for (f, M) in q
+                    field[1:size(M, 1), (f - 1) * nfd + 1:f * nfd] .= M
+                end
+            end
         end
     end
     GC.@preserve kinds states check(ccall((:flou_set_bcs, libflou), Int32,
         (Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{Float64}), ctx, length(kinds), kinds, states), ctx)
+    if field !== nothing
+        GC.@preserve field check(ccall((:flou_set_bc_field, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}),
+                                       ctx, field), ctx)
+    end
     g = disc.geometry
     J = Vector{Float64}(g.elements.jac)
     Ja = reduce(vcat, (vec(Matrix(M)) for M in g.elements.metric))
@@ -151,7 +165,6 @@ function GPUDisc(disc::MultielementDisc{ND,RT}, equation) where {ND,RT}
         # subcell-interface geometry (geometry.subgrids, PhysicalRegions.jl:180-300) in the layout of
         # flou_set_subgrid: element, direction, line (tpdofs_subgrid order), interface
         n = length(disc.std.basis.ξ)
-        nfd = n^(ND - 1)
         sfr = zeros(Float64, 9, n + 1, nfd, ND, ne)
         sjac = zeros(Float64, n + 1, nfd, ND, ne)
         for ie in 1:ne, d in 1:ND
@@ -187,13 +200,19 @@ function get_max_dt(q::Matrix{Float64}, disc::GPUDisc, ::Any, cfl)
     return dt[]
 end
 
-"The external state of a GenericBC, evaluated at every face node of boundary `ib`; it must be one state."
+"""
+The external state of a GenericBC evaluated at every face node of boundary `ib`
+(`Qext(nothing, x, nothing, 0, equation)`: a state given by the position alone).  Returns one
+vector when every node gets the same state, else `face => (nvars x face nodes)` pairs in the
+face-dof order of `geometry.faces.coords`.
+"""
 function genericbc_state(bc, disc, ib, equation)
-    vals = [bc.Qext(nothing, x, nothing, 0.0, equation)
-            for f in eachbdface(disc.mesh, ib) for x in disc.geometry.faces.coords[f]]
-    all(v -> v == vals[1], vals) ||
-        error("GenericBC on boundary $ib: the external state varies along the boundary; one state per boundary is supported")
-    return Vector{Float64}(vals[1])
+    per_face = [f => reduce(hcat, [Vector{Float64}(bc.Qext(nothing, x, nothing, 0.0, equation))
+                                   for x in disc.geometry.faces.coords[f]])
+                for f in eachbdface(disc.mesh, ib)]
+    q1 = per_face[1].second[:, 1]
+    all(p -> all(==(q1), eachcol(p.second)), per_face) && return q1
+    return per_face
 end
 
 "SSP-RK3 run entirely on the GPU (one CUDA graph per step)."

@@ -1,6 +1,6 @@
 /*
  * flou_cuda.h -- C ABI of libflou_cuda, the GB300 (sm_103a) FP64 implementation of Flou.jl's
- * DGSEM semidiscrete residual and explicit SSP-RK3 stepping.
+ * DGSEM semidiscrete residual and its explicit Runge-Kutta stepping.
  *
  * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns an int32
  * status (FLOU_OK = 0).  flou_last_error(ctx) gives a message for the last failure on ctx.
@@ -34,7 +34,7 @@ extern "C" {
 #define FLOU_ERR_NONPHYSICAL 3  /* rho <= 0, p <= 0 or a non-finite value was produced       */
 #define FLOU_ERR_TIMEOUT 4      /* a bounded device-side wait ran out                        */
 #define FLOU_ERR_OOM 5          /* device allocation failed                                   */
-#define FLOU_ERR_UNSUPPORTED 6  /* valid in Flou but outside this library (e.g. curvilinear) */
+#define FLOU_ERR_UNSUPPORTED 6  /* valid in Flou but outside this library                      */
 #define FLOU_ERR_STATE 7        /* call order violated (e.g. rhs before set_mesh)            */
 
 /* ---- enumerations --------------------------------------------------------------------- */
@@ -45,12 +45,13 @@ extern "C" {
 #define FLOU_EQ_EULER 2
 
 /* Volume operators: StrongDivOperator (OpDivergence.jl:105-160; weak == strong on LGL),
- * SplitDivOperator (OpDivergence.jl:184-282, LGL nodes only). */
+ * SplitDivOperator (OpDivergence.jl:184-437; on a basis without boundary nodes the entropy-
+ * projected form of :301-437, Euler only). */
 #define FLOU_OP_STRONG 0
 #define FLOU_OP_SPLIT 1
-/* HybridDivOperator (OpDivergence.jl:439-612, 781-801): the split form in telescopic (subcell) form,
- * blended with a subcell finite-volume flux; LGL nodes, Cartesian geometry, Euler.  The FV flux
- * and the blending constant are set with flou_set_hybrid. */
+/* HybridDivOperator (OpDivergence.jl:439-801): the split form in telescopic (subcell) form,
+ * blended with a subcell finite-volume flux; Euler.  The FV flux and the blending constant are
+ * set with flou_set_hybrid; general (non-Cartesian) geometry also needs flou_set_subgrid. */
 #define FLOU_OP_HYBRID 2
 
 /* Two-point volume fluxes of the split form: StdAverage (Euler.jl:385-472),
@@ -80,6 +81,9 @@ extern "C" {
 #define FLOU_BC_OUTFLOW 1
 #define FLOU_BC_INFLOW 2
 #define FLOU_BC_SLIP 3
+/* A Dirichlet state given per boundary face node (a GenericBC whose Qext(x) varies along the
+ * boundary, FlouSpatial.jl:80-91), set with flou_set_bc_field. */
+#define FLOU_BC_STATE_FIELD 4
 
 /* Pointer kinds for state arrays. */
 #define FLOU_PTR_HOST 0
@@ -133,15 +137,18 @@ int32_t flou_set_mesh(flou_ctx* ctx, int32_t nelem, int32_t nfaces, const int32_
  * MultielementDiscontinuous.jl:40-51): kinds[nbcs] (FLOU_BC_*), states[nbcs x 5]
  * (the Qext of inflow conditions, row per boundary). */
 int32_t flou_set_bcs(flou_ctx* ctx, int32_t nbcs, const int32_t* kinds, const double* states);
+/* External states of the FLOU_BC_STATE_FIELD boundaries: states[nfaces x n^(dim-1) x 5], the face
+ * nodes in the face-dof order of each face (master side), 5 values per node (zero-padded); the
+ * entries of other faces are not read. */
+int32_t flou_set_bc_field(flou_ctx* ctx, const double* states);
 
 /* Geometry (Geometry, src/FlouSpatial/PhysicalRegions.jl:982-991): per node J (ndofs),
  * metric Ja (ndofs x d x d, column-major per node); per face node the frame
  * (nfacedofs x 3 x 3: n, t, b with 3 components each) and the surface Jacobian
  * (nfacedofs).  Cartesian geometry (J and a diagonal Ja constant per element, the Cartesian
  * frames, every face orientation 0) takes a compressed fast path; any other geometry
- * (curvilinear / unstructured, PhysicalRegions.jl:438-472 and :756-971) is used per node and
- * needs an LGL basis in 2D or 3D.  Rejected: J <= 0, non-finite entries, non-unit normals,
- * surface Jacobians <= 0. */
+ * (curvilinear / unstructured, PhysicalRegions.jl:438-472 and :756-971) is used per node, in 2D
+ * or 3D.  Rejected: J <= 0, non-finite entries, non-unit normals, surface Jacobians <= 0. */
 int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, const double* frames,
                           const double* face_J);
 
@@ -150,11 +157,12 @@ int32_t flou_set_geometry(flou_ctx* ctx, const double* J, const double* Ja, cons
  * OpDivergence.jl:777-801).  Required before the first residual of a FLOU_OP_HYBRID context. */
 int32_t flou_set_hybrid(flou_ctx* ctx, int32_t fvflux, int32_t fvflux_avg, double fvflux_intensity, double blend);
 /* Subcell-interface geometry of general (curvilinear / unstructured) elements, which the hybrid
- * operator's subcell finite-volume fluxes need (geometry.subgrids, PhysicalRegions.jl:180-300):
+ * operator's subcell finite-volume fluxes and, on a basis without boundary nodes, the split
+ * form's projected states need (geometry.subgrids, PhysicalRegions.jl:180-300):
  * for element e, direction d, line m (the face-dof order of a face normal to d) and interface
  * s = 0..n of that line, point ((e·dim + d)·n^(dim-1) + m)·(n+1) + s holds the unit normal, tangent
  * and binormal (9 doubles in `frames`, zero-padded to 3 components) and the surface Jacobian
- * (`jac`).  Required before stepping a hybrid context whose geometry is not Cartesian. */
+ * (`jac`).  Required before stepping such a context whose geometry is not Cartesian. */
 int32_t flou_set_subgrid(flou_ctx* ctx, const double* frames, const double* jac);
 
 /* ---- residual and stepping ------------------------------------------------------------- */
@@ -162,8 +170,9 @@ int32_t flou_set_subgrid(flou_ctx* ctx, const double* frames, const double* jac)
  * (src/FlouSpatial/Equations/Hyperbolic.jl:31-69): dQ is overwritten.  Synchronous. */
 int32_t flou_rhs(flou_ctx* ctx, double* dQ, const double* Q, double t, int32_t ptr_kind);
 
-/* `nsteps` Shu-Osher SSP-RK3 steps of size dt, in place on Q (the SSPRK33 solver that
- * timeintegrate hands to OrdinaryDiffEq, src/FlouTime/FlouTime.jl:34-54).  Each stage's
+/* `nsteps` Shu-Osher SSP-RK3 steps of size dt (or steps of the method of flou_set_integrator), in
+ * place on Q (the SSPRK33 solver that timeintegrate hands to OrdinaryDiffEq,
+ * src/FlouTime/FlouTime.jl:34-54).  Each stage's
  * combination is fused into the residual kernel; the step is replayed as a CUDA graph.
  * Returns FLOU_ERR_NONPHYSICAL when any stage produced rho <= 0, p <= 0 or a non-finite
  * value (Flou raises a DomainError there, FlouTime.jl:37-51). */
@@ -290,8 +299,8 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
 
 /* ---- stage limiter and integral monitors (Euler) ----------------------------------------------
  * The Zhang-Shu positivity limiter of src/FlouSpatial/Equations/Euler.jl:611-654 (`get_limiter`
- * :zhang_shu with its minimum value), applied after every SSP-RK3 stage of flou_step /
- * flou_step_async, as Flou's `get_limiter_callback` passed as OrdinaryDiffEq's stage_limiter!
+ * :zhang_shu with its minimum value), applied after every stage of flou_step /
+ * flou_step_async / flou_step_cfl, as Flou's `get_limiter_callback` passed as OrdinaryDiffEq's stage_limiter!
  * (src/FlouTime/FlouTime.jl:136-148).  Per element: the density, then all variables, are scaled
  * toward the element mean when the minimum density / pressure falls below min(minval, mean). */
 #define FLOU_LIMITER_NONE 0

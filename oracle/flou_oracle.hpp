@@ -447,7 +447,7 @@ enum NumFlux {
     NF_STDAVG = 0, NF_LXF = 1, NF_CHANDRASHEKAR = 2, NF_HLL = 3, NF_HLLC = 4,
     NF_SCALAR_DISSIPATION = 5, NF_MATRIX_DISSIPATION = 6
 };
-enum BcKind { BC_NONE = 0, BC_OUTFLOW = 1, BC_INFLOW = 2, BC_SLIP = 3 };
+enum BcKind { BC_NONE = 0, BC_OUTFLOW = 1, BC_INFLOW = 2, BC_SLIP = 3, BC_STATE_FIELD = 4 };
 
 struct Config {
     int dim = 2, nv = 4, eq = EQ_EULER;
@@ -921,6 +921,8 @@ struct Disc {
     // point ((e·dim + d)·nfd + line)·(n+1) + s; empty on Cartesian meshes (the axes)
     std::vector<Frame> subframes;
     std::vector<double> subjac;
+    // GenericBC external states per boundary face node, 5 per node (BC_STATE_FIELD boundaries)
+    std::vector<double> bcfield;
     // connectivity (1-based, like the reference)
     std::vector<int> faceinds, facepos;   // nelem * 2dim
     std::vector<int> eleminds, elempos;   // nfaces * 2
@@ -1238,6 +1240,12 @@ template <class T> void rhs(const Disc& g, T* dQ, const T* Q, double time, Works
         for (int m = 0; m < nfd; ++m) {
             long idx = (long)f * nfd + m;
             Vec<T> Qin = getv(ws.Qf[0].data(), nf, idx, nv);
+            if (bc.kind == BC_STATE_FIELD) {   // GenericBC: Qext(x) at this face node
+                Vec<T> Qe{};
+                for (int k = 0; k < nv; ++k) Qe[k] = T(g.bcfield.at(5 * idx + k));
+                setv(ws.Qf[1].data(), nf, idx, Qe, nv);
+                continue;
+            }
             setv(ws.Qf[1].data(), nf, idx, apply_bc(bc, Qin, g.frames[idx], c), nv);
         }
     }

@@ -361,6 +361,12 @@ void oracle_set_subgrid(void* hp, const double* frames, const double* jac) {
         }
 }
 
+// External states of the BC_STATE_FIELD boundaries, 5 per face node (flou_set_bc_field's layout).
+void oracle_set_bc_field(void* hp, const double* states) {
+    Handle* h = (Handle*)hp;
+    h->g.bcfield.assign(states, states + 5 * (size_t)h->g.nfdofs());
+}
+
 void oracle_limit(void* hp, double* Q, double minval, const double* omega_tp) {
     Handle* h = (Handle*)hp;
     std::vector<double> w(omega_tp, omega_tp + h->g.npe);

@@ -45,6 +45,7 @@ def lib():
         _lib.oracle_ssprk3_limited.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                                ctypes.c_double, D]
         _lib.oracle_set_subgrid.argtypes = [ctypes.c_void_p, D, D]
+        _lib.oracle_set_bc_field.argtypes = [ctypes.c_void_p, D]
         _lib.oracle_lsrk2n.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, D, D, D, ctypes.c_double, D]
         _lib.oracle_count_rhs.argtypes = [ctypes.c_void_p, D, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
@@ -139,6 +140,8 @@ class Disc:
         if a.get("subgrid") is not None:
             fr, jac = a["subgrid"]
             L.oracle_set_subgrid(self.h, _d(np.ascontiguousarray(fr)), _d(np.ascontiguousarray(jac)))
+        if a.get("bc_field") is not None:
+            L.oracle_set_bc_field(self.h, _d(np.ascontiguousarray(a["bc_field"])))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -190,6 +190,27 @@ def test_euler_walls_inflow_outflow(dim, op):
     _check(disc, smooth_euler_state(disc, seed=7))
 
 
+@pytest.mark.parametrize("dim,op", [(2, "split_chandra_lxfc"), (3, "split_chandra_hllc"), (2, "strong_hllc"),
+                                    (2, "hybrid_chandra_lxfc")])
+def test_euler_generic_bc_varying_state(dim, op):
+    """GenericBC(Qext) with a state that varies along the boundary (FlouSpatial.jl:80-91): the
+    device reads one state per boundary face node from flou_set_bc_field."""
+    eq = _euler(dim)
+
+    def prim(x):
+        P = np.zeros(dim + 2)
+        P[0] = 1.0 + 0.3 * np.sin(2 * np.pi * x[1]) * (np.cos(2 * np.pi * x[2]) if dim == 3 else 1.0)
+        P[1], P[2], P[-1] = 0.4, 0.1 * np.cos(2 * np.pi * x[1]), 1.0 + 0.1 * x[1]
+        return eq.vars_prim2cons(P)
+
+    qext = lambda _q, x, _f, _t, _e: prim(x)
+    disc = build(dim, 4, (3,) * dim, eq, _ops()[op](), periodic=tuple(range(2, dim)),
+                 bcs={"1": F.GenericBC(qext), "2": F.GenericBC(qext), "3": F.EulerSlipBC(),
+                      "4": F.EulerSlipBC()}, box=((0.0,) * dim, (1.0,) * dim))
+    assert isinstance(disc.bcs[0], F.equations.StateFieldBC)
+    _check(disc, smooth_euler_state(disc, seed=13))
+
+
 def test_oracle_built_operators_general_path():
     """Flou-style fitted operators (tiny non-zero off-end entries) take the general
     interpolation path on the GPU."""

@@ -357,3 +357,34 @@ def test_gauss_node_split_convergence():
         errs.append(np.sqrt(np.mean((Q - exact(tf)) ** 2)))
     order = np.log2(errs[0] / errs[1])
     assert order > 3.5, (errs, order)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_generic_bc_with_a_varying_state(dim):
+    """GenericBC(Qext) whose state varies along the boundary (FlouSpatial.jl:80-91), uploaded per
+    face node: a shear flow ρ(y, z), u = const, v = w = 0, p = const is a steady solution, so with
+    its own profile imposed at the inflow and outflow the residual is round-off; a profile
+    mapped to the wrong face nodes would not be."""
+    eq = F.EulerEquation(dim, 1.4)
+
+    def prim(x):
+        rho = 1.0 + 0.3 * np.sin(2 * np.pi * x[1]) * (np.cos(2 * np.pi * x[2]) if dim == 3 else 1.0)
+        P = np.zeros(dim + 2)
+        P[0], P[1], P[-1] = rho, 0.4, 1.0
+        return eq.vars_prim2cons(P)
+
+    qext = lambda _q, x, _f, _t, _e: prim(x)
+    bcs = {"1": F.GenericBC(qext), "2": F.GenericBC(qext)}
+    disc = build(dim, 4, (3,) * dim, eq, F.SplitDivOperator(F.LxF(F.ChandrasekharAverage(), 1.0)),
+                 periodic=tuple(range(1, dim)), bcs=bcs, box=((0.0,) * dim, (1.0,) * dim))
+    assert isinstance(disc.bcs[0], F.equations.StateFieldBC)
+    Q = np.asfortranarray(np.array([prim(x) for x in disc.coords[:, :dim]]))
+    R = oracle_for(disc).rhs(Q)
+    assert np.max(np.abs(R)) < 1e-11, np.max(np.abs(R))
+    a = disc.abi_arrays()
+    nfd = disc.std.n ** (dim - 1)
+    wrong = a["bc_field"].copy()
+    for f in disc.bcs[0].states:   # the same states on the wrong nodes of each face
+        wrong[f * nfd:(f + 1) * nfd] = wrong[f * nfd:(f + 1) * nfd][::-1]
+    a["bc_field"] = wrong
+    assert np.max(np.abs(oracle_for(disc, a).rhs(Q))) > 1e-3
