@@ -821,7 +821,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
 // formulas share one reciprocal.
 // ---------------------------------------------------------------------------------------
 // Shared per-node arrays (length NN each) of the split form, by two-point flux:
-//   Chandrashekar:  rh = ρ/2, vh_k = v_k/2, bh = β/2 = ρ/(4p)
+//   Chandrashekar:  ρ, vh_k = v_k/2, β = ρ/(2p)
 //   Kennedy-Gruber: rh = ρ/2, vh_k = v_k/2, ph = p/2, eh = e/2 (e = ρe/ρ)
 //   StdAverage:     v_k, p, then the conserved variables
 //   scalar equations: u
@@ -833,47 +833,70 @@ struct SplitLayout {
                                                              : (TP == FLOU_TP_CHANDRASHEKAR ? DIM + 2 : DIM + 3));
 };
 
+// The pair kernels of the Chandrashekar flux return 2F♯ (one scale for all variables, exact):
+// the node phase halves the metric factor and doubles the diagonal weight to match.
+template <int EQ, int TP>
+struct PairScale {
+    static constexpr double value = (EQ == FLOU_EQ_EULER && TP == FLOU_TP_CHANDRASHEKAR) ? 2.0 : 1.0;
+};
+
+// x < 0.01 for x >= 0 (or NaN, which fails like the floating-point test) as an integer
+// comparison of the bit patterns, keeping the FP64 pipe for arithmetic.
+__device__ __forceinline__ bool below_001(double x) {
+    return __double_as_longlong(x) < 0x3F847AE147AE147BLL;   // the bits of 0.01
+}
+
+// 1/x for a normal x: the hardware's approximate reciprocal (rcp.approx.ftz.f64, on the MUFU
+// unit) refined by one third-order step y(1 + e + e²), e = 1 - x y (the series of y/(1 - e)):
+// three FMAs on the FP64 pipe instead of a correctly rounded division.  The seed's relative
+// error measured on GB300 over 2^30 samples is below 2^-22, so the step leaves about 2^-66 plus
+// the rounding of the last two FMAs (within 1 ulp).
+__device__ __forceinline__ double rcp_refined(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
+}
+
 // Chandrashekar two-point flux (Euler.jl:474-536) along direction d without the metric
-// factor, with the logarithmic means of Utilities.jl:34-44 written in sums and differences:
+// factor, times 2, with the logarithmic means of Utilities.jl:34-44 written in sums and
+// differences:
 //   u = ((a-b)/(a+b))²;  series branch (u < 0.01): mean = (a+b)/(2F), F = 1+u/3+u²/5+u³/7,
 //   log branch: mean = (a-b)/ln(a/b).
-// One reciprocal 1/(hs_ρ·hs_β) serves both means and the pressure average; 1/F comes from
-// two Newton steps started at 1 - u/3 (relative error (4u²/45)^4 < 1e-20 for u < 0.01).
+// With sρ = ρ1+ρ2, sβ = β1+β2, one reciprocal R = 1/(sρ sβ) gives 1/sρ and 1/sβ; the averaged
+// pressure is p̂ = sρ/(2 sβ), and with A = ρ̄/ρ_ln, B = β̄/β_ln (F itself on a series branch) the
+// enthalpy is h = 1/(2(γ-1)β_ln) + p̂/ρ_ln + v1·v2/2 = (A + B/(γ-1))/sβ + v1·v2/2.
+// Both reciprocals (R and 1/F) come from rcp_refined.  c_g = 1/(γ-1).
 // GEN: the flux along a general vector nv (the averaged metric column of a curvilinear element,
 // Euler.jl:474-536 with n = (Ja1 + Ja2)/2) instead of the axis d.
 template <int DIM, bool GEN = false>
 __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S, int NN, int i, int l, int d,
-                                                   double c_beta, double* F, const double* nv = nullptr) {
-    const double* rh = S;
+                                                   double c_g, double* F, const double* nv = nullptr) {
+    const double* rho = S;
     const double* vh = S + NN;
-    const double* bh = S + (1 + DIM) * NN;
-    double rh1 = rh[i], rh2 = rh[l], bh1 = bh[i], bh2 = bh[l];
-    double hsr = rh1 + rh2, dhr = rh1 - rh2;   // (ρ1+ρ2)/2, (ρ1-ρ2)/2
-    double hsb = bh1 + bh2, dhb = bh1 - bh2;
-    double R = 1.0 / (hsr * hsb);
-    double rs = hsb * R, rb = hsr * R;         // 2/(ρ1+ρ2), 2/(β1+β2)
-    double fr = dhr * rs, fb = dhb * rb;
+    const double* beta = S + (1 + DIM) * NN;
+    double r1 = rho[i], r2 = rho[l], b1 = beta[i], b2 = beta[l];
+    double sr = r1 + r2, dr = r1 - r2;
+    double sb = b1 + b2, db = b1 - b2;
+    double R = rcp_refined(sr * sb);
+    double rs = sb * R, rb = sr * R;           // 1/(ρ1+ρ2), 1/(β1+β2)
+    double fr = dr * rs, fb = db * rb;
     double ur = fr * fr, ub = fb * fb;
-    double rho_ln, inv_rho_ln, inv_beta_ln;
-    if (ur < 0.01) {
-        double Fs = fma(ur, fma(ur, fma(ur, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
-        double y = fma(-1.0 / 3.0, ur, 1.0);
-        y = y * fma(-Fs, y, 2.0);
-        y = y * fma(-Fs, y, 2.0);
-        rho_ln = hsr * y;
-        inv_rho_ln = Fs * rs;
+    double rl2, A, B;                          // 2ρ_ln, ρ̄/ρ_ln, β̄/β_ln
+    if (below_001(ur)) {
+        A = fma(ur, fma(ur, fma(ur, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        rl2 = sr * rcp_refined(A);
     } else {
-        double L = log(rh1 / rh2);
-        rho_ln = (2.0 * dhr) / L;
-        inv_rho_ln = L / (2.0 * dhr);
+        double L = log(r1 / r2);
+        rl2 = (2.0 * dr) / L;
+        A = sr / rl2;
     }
-    if (ub < 0.01) {
-        double Fs = fma(ub, fma(ub, fma(ub, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
-        inv_beta_ln = Fs * rb;
+    if (below_001(ub)) {
+        B = fma(ub, fma(ub, fma(ub, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
     } else {
-        inv_beta_ln = log(bh1 / bh2) / (2.0 * dhb);
+        B = (0.5 * log(b1 / b2)) / fb;
     }
-    double p = 0.5 * hsr * rb;                 // (ρ1+ρ2)/(2(β1+β2))
+    double p2 = sr * rb;                       // 2p̂
     double va[DIM];
     double dot = 0.0;
 #pragma unroll
@@ -881,24 +904,22 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
         va[k] = vh[k * NN + i] + vh[k * NN + l];
         dot = fma(vh[k * NN + i], vh[k * NN + l], dot);
     }
-    // h = 1/(2β(γ-1)) - (|v1|²+|v2|²)/4 + p/ρ + |v̄|², with |v̄|² - (|v1|²+|v2|²)/4 = v1·v2/2 = 2 vh1·vh2
-    double h = fma(inv_beta_ln, c_beta, fma(p, inv_rho_ln, 2.0 * dot));
+    double h = fma(rb, fma(c_g, B, A), 2.0 * dot);
     if (GEN) {
         double vn = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vn = fma(va[k], nv[k], vn);
-        double m = rho_ln * vn;
+        double m = rl2 * vn;
         F[0] = m;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], p * nv[k]);
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], p2 * nv[k]);
         F[DIM + 1] = m * h;
         return;
     }
-    double m = rho_ln * va[d];
+    double m = rl2 * va[d];
     F[0] = m;
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) F[1 + k] = m * va[k];
-    F[1 + d] = F[1 + d] + p;
+    for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], k == d ? p2 : 0.0);
     F[DIM + 1] = m * h;
 }
 
@@ -908,10 +929,10 @@ template <int DIM, int TP>
 __device__ __forceinline__ void store_split_node(double* S, int st, int col, const double* q, const double* v,
                                                  double p, double ir) {
     if (TP == FLOU_TP_CHANDRASHEKAR) {
-        S[col] = 0.5 * q[0];
+        S[col] = q[0];
 #pragma unroll
         for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
-        S[(1 + DIM) * st + col] = (0.25 * q[0]) / p;
+        S[(1 + DIM) * st + col] = (0.5 * q[0]) / p;
     } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
         S[col] = 0.5 * q[0];
 #pragma unroll
@@ -1009,7 +1030,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
 #pragma unroll
     for (int k = 0; k < NV; ++k) dq[k] = 0.0;
     const double* Dsh = sops + N * N;
-    const double c_beta = 0.5 / (g - 1.0);
+    const double c_g = 1.0 / (g - 1.0);
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
         double fls[NV], frs[NV];   // GAUSS && HYB: this element's side values of its line's face fluxes
@@ -1091,7 +1112,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             }
             if constexpr (CURV && EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
-                    chandrashekar_pair<DIM, true>(sprim, SST, ia, ib, dir, c_beta, F, nv);
+                    chandrashekar_pair<DIM, true>(sprim, SST, ia, ib, dir, c_g, F, nv);
                 } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
                     const double* vh = sprim + SST;
                     double rho = sprim[ia] + sprim[ib];
@@ -1132,7 +1153,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 F[0] = an * (sprim[ia] + sprim[ib]) * 0.5;
             } else if (EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
-                    chandrashekar_pair<DIM>(sprim, SST, ia, ib, dir, c_beta, F);
+                    chandrashekar_pair<DIM>(sprim, SST, ia, ib, dir, c_g, F);
                 } else if (TP == FLOU_TP_KENNEDY_GRUBER) {   // Kennedy & Gruber (2008)
                     const double* vh = sprim + SST;
                     double rho = sprim[ia] + sprim[ib];
@@ -1234,6 +1255,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             for (int j = 0; j < N; ++j) {
                 double a = Dsh[pos + j * N];
                 if (j == pos) {
+                    a = PairScale<EQ, TP>::value * a;   // the scale the pair fluxes carry
 #pragma unroll
                     for (int k = 0; k < NV; ++k) acc[k] = fma(a, Fd[k], acc[k]);
                 } else {
@@ -1243,7 +1265,8 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPTX + pidx], acc[k]);
                 }
             }
-            double Ja = CURV ? 1.0 : P.elem_Ja[e * DIM + dir];   // CURV: the metric is in the fluxes
+            // CURV: the metric is in the fluxes; the pair scale comes off with it
+            double Ja = (CURV ? 1.0 : P.elem_Ja[e * DIM + dir]) * (1.0 / PairScale<EQ, TP>::value);
             double Fl[NV], Fr[NV];   // GAUSS: F♯(Q_i, Q̃) - l·F♯(·, Q̃) at both ends (OpDivergence.jl:410-425)
             if constexpr (GAUSS) {
                 const int xb = NPT + 2 * N * (el * NFD + line);
