@@ -182,10 +182,40 @@ __device__ __forceinline__ void euler_normal_flux(const double* q, double un, do
     F[DIM + 1] = (q[DIM + 1] + p) * un;
 }
 
+// x < 0.01 for x >= 0 (or NaN, which fails like the floating-point test) as an integer
+// comparison of the bit patterns, keeping the FP64 pipe for arithmetic.
+__device__ __forceinline__ bool below_001(double x) {
+    return __double_as_longlong(x) < 0x3F847AE147AE147BLL;   // the bits of 0.01
+}
+
+// 1/x for a normal x: the hardware's approximate reciprocal (rcp.approx.ftz.f64, on the MUFU
+// unit) refined by one third-order step y(1 + e + e²), e = 1 - x y (the series of y/(1 - e)):
+// three FMAs on the FP64 pipe instead of a correctly rounded division.  Measured on GB300 over
+// 2^30 samples: the seed's relative error is below 2^-19.9, the refined value within 1 ulp of the
+// correctly rounded 1/x (the step's remainder e³ is below 1e-18).
+__device__ __forceinline__ double rcp_refined(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
+}
+
+// sqrt(x) for a normal x > 0: the hardware's approximate 1/√x (rsqrt.approx.ftz.f64, MUFU) gives
+// s0 = x y; with e = 1 - s0 y = 1 - x y², √x = s0 (1 - e)^(-1/2), and the binomial series
+// 1 + e/2 + 3e²/8 truncated after e² (remainder 5e³/16) gives one third-order step: four
+// FP64 operations and a multiply instead of a correctly rounded square root.
+__device__ __forceinline__ double sqrt_refined(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double s0 = x * y;
+    double e = fma(-s0, y, 1.0);
+    return fma(s0, e * fma(e, 0.375, 0.5), s0);
+}
+
 // Logarithmic mean (src/FlouCommon/Utilities.jl:34-44) of a, b > 0 in sums and differences, given
 // s = a + b and rs = 1/s (often from one reciprocal shared with a second mean):
 //   f = (a - b)/s, u = f²;  u < 0.01: mean = s/(2F) with the reference's F = 1+u/3+u²/5+u³/7
-//   (1/F by two Newton steps from 1 - u/3, relative error (4u²/45)^4 < 1e-20), else the log branch
+//   (1/F from rcp_refined), else the log branch
 //   mean = (a - b)/ln(a/b).  L = ln(a/b) comes along: from the log branch, or on the series
 //   branch from 2f·atanh(f)/f summed to u⁸/17 (remainder below 1e-19 relative).
 struct LogMean { double mean, inv, L; };
@@ -193,12 +223,9 @@ struct LogMean { double mean, inv, L; };
 __device__ __forceinline__ LogMean logmean_sd(double a, double b, double s, double rs) {
     const double d = a - b, f = d * rs, u = f * f;
     LogMean m;
-    if (u < 0.01) {
+    if (below_001(u)) {
         double Fs = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
-        double y = fma(-1.0 / 3.0, u, 1.0);
-        y = y * fma(-Fs, y, 2.0);
-        y = y * fma(-Fs, y, 2.0);
-        m.mean = 0.5 * s * y;
+        m.mean = 0.5 * s * rcp_refined(Fs);
         m.inv = 2.0 * Fs * rs;
         double Fe = fma(u, 1.0 / 17.0, 1.0 / 15.0);
         Fe = fma(u, Fe, 1.0 / 13.0);
@@ -230,7 +257,7 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
                                                    double intensity, double g, double* F) {
     constexpr int NV = DIM + 2;
     const double rl = ql[0], rr = qr[0];
-    const double irl = 1.0 / rl, irr = 1.0 / rr;
+    const double irl = rcp_refined(rl), irr = rcp_refined(rr);
     double vl[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0};
     double vl2 = 0.0, vr2 = 0.0;
 #pragma unroll
@@ -251,11 +278,11 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
     LogMean mr{0.0, 0.0, 0.0}, mb{0.0, 0.0, 0.0};
     double bl = 0.0, br = 0.0, phat = 0.0;
     if (needs_means) {
-        const double ipl = 1.0 / pl, ipr = 1.0 / pr;
+        const double ipl = rcp_refined(pl), ipr = rcp_refined(pr);
         bl = 0.5 * rl * ipl;
         br = 0.5 * rr * ipr;
         const double sr = rl + rr, sb = bl + br;
-        const double R = 1.0 / (sr * sb);
+        const double R = rcp_refined(sr * sb);
         const double rsr = sb * R, rsb = sr * R;
         mr = logmean_sd(rl, rr, sr, rsr);
         mb = logmean_sd(bl, br, sb, rsb);
@@ -288,7 +315,7 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
         return;
     }
     if (kind == FLOU_NF_LXF || kind == FLOU_NF_SCALAR_DISSIPATION) {
-        const double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+        const double al = sqrt_refined(g * pl * irl), ar = sqrt_refined(g * pr * irr);
         const double lam = fmax(fabs(vl[0]) + al, fabs(vr[0]) + ar) * (0.5 * intensity);
         if (kind == FLOU_NF_LXF) {
 #pragma unroll
@@ -317,7 +344,7 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
 #pragma unroll
     for (int k = 1; k < DIM; ++k) vv = fma(vm[k], vm[k], vv);
     const double v2 = fma(2.0, vv, -0.5 * (vl2 + vr2));
-    const double a = sqrt(g * phat * mr.inv);
+    const double a = sqrt_refined(g * phat * mr.inv);
     const double h = fma(0.5 * g / g1, mb.inv, 0.5 * v2);
     double dW[NV];
     dW[0] = (mr.L + mb.L / g1) - (vl2 * bl - vr2 * br);
@@ -396,12 +423,13 @@ __device__ __forceinline__ double flip(double x, bool neg) {
 
 // StdAverage / LxF(StdAverage) / HLL / HLLC in the face frame with one reciprocal of the
 // density per side (u = m·(1/ρ), p = (γ-1)(ρe - ½|m|²/ρ)) and one shared reciprocal for the
-// HLLC star state; same formulas as euler_face_flux up to rounding.
+// HLLC star state, reciprocals and sound speeds from rcp_refined / sqrt_refined; the
+// reference's formulas (Euler.jl:99-165 and the HLL/HLLC of Toro 2009) up to rounding.
 template <int DIM>
 __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const double* qr, int kind, double intensity,
                                                      double g, double* F) {
     constexpr int NV = DIM + 2;
-    double irl = 1.0 / ql[0], irr = 1.0 / qr[0];
+    double irl = rcp_refined(ql[0]), irr = rcp_refined(qr[0]);
     double ul = ql[1] * irl, ur = qr[1] * irr;
     double sl2 = ql[1] * ql[1], sr2 = qr[1] * qr[1];
 #pragma unroll
@@ -415,14 +443,14 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
         for (int k = 1; k < DIM; ++k) F[1 + k] = fma(ql[1 + k], ul, qr[1 + k] * ur) * 0.5;
         F[DIM + 1] = fma(ql[DIM + 1] + pl, ul, (qr[DIM + 1] + pr) * ur) * 0.5;
         if (kind == FLOU_NF_LXF) {
-            double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+            double al = sqrt_refined(g * pl * irl), ar = sqrt_refined(g * pr * irr);
             double lam = fmax(fabs(ul) + al, fabs(ur) + ar) * (0.5 * intensity);
 #pragma unroll
             for (int k = 0; k < NV; ++k) F[k] = fma(lam, ql[k] - qr[k], F[k]);
         }
         return;
     }
-    double al = sqrt(g * pl * irl), ar = sqrt(g * pr * irr);
+    double al = sqrt_refined(g * pl * irl), ar = sqrt_refined(g * pr * irr);
     double sl = fmin(ul - al, ur - ar), sr = fmax(ul + al, ur + ar);
     double Fl[NV], Fr[NV];
     euler_normal_flux<DIM>(ql, ul, pl, Fl);
@@ -430,18 +458,18 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
     if (sl >= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fl[k]; return; }
     if (sr <= 0.0) { for (int k = 0; k < NV; ++k) F[k] = Fr[k]; return; }
     if (kind == FLOU_NF_HLL) {
-        double r = 1.0 / (sr - sl), slr = sl * sr;
+        double r = rcp_refined(sr - sl), slr = sl * sr;
         for (int k = 0; k < NV; ++k) F[k] = (fma(sr, Fl[k], -sl * Fr[k]) + slr * (qr[k] - ql[k])) * r;
         return;
     }
     double ml = ql[0] * (sl - ul), mr = qr[0] * (sr - ur);
-    double ss = fma(ul, ml, (pr - pl) - ur * mr) / (ml - mr);
+    double ss = fma(ul, ml, (pr - pl) - ur * mr) * rcp_refined(ml - mr);
     bool left = ss >= 0.0;
     const double* qk = left ? ql : qr;
     const double* Fk = left ? Fl : Fr;
     double sk = left ? sl : sr, mk = left ? ml : mr, irk = left ? irl : irr, uk = left ? ul : ur,
            pk = left ? pl : pr;
-    double R = 1.0 / ((sk - ss) * mk);
+    double R = rcp_refined((sk - ss) * mk);
     double coef = mk * mk * R;          // ρ_K (S_K - u_K)/(S_K - S*)
     double pm = pk * (sk - ss) * R;     // p_K / (ρ_K (S_K - u_K))
     double Us[NV];
@@ -729,7 +757,7 @@ __device__ __forceinline__ void strong_tile(const ElemParams& P, int e0, double*
         double F[NV];
         double v[DIM], p = 0.0;
         if (EQ == FLOU_EQ_EULER) {   // primitives once per node (volumeflux, Euler.jl:54-114)
-            double ir = 1.0 / q[0], ke = 0.0;
+            double ir = rcp_refined(q[0]), ke = 0.0;
 #pragma unroll
             for (int k = 0; k < DIM; ++k) {
                 v[k] = q[1 + k] * ir;
@@ -840,23 +868,7 @@ struct PairScale {
     static constexpr double value = (EQ == FLOU_EQ_EULER && TP == FLOU_TP_CHANDRASHEKAR) ? 2.0 : 1.0;
 };
 
-// x < 0.01 for x >= 0 (or NaN, which fails like the floating-point test) as an integer
-// comparison of the bit patterns, keeping the FP64 pipe for arithmetic.
-__device__ __forceinline__ bool below_001(double x) {
-    return __double_as_longlong(x) < 0x3F847AE147AE147BLL;   // the bits of 0.01
-}
 
-// 1/x for a normal x: the hardware's approximate reciprocal (rcp.approx.ftz.f64, on the MUFU
-// unit) refined by one third-order step y(1 + e + e²), e = 1 - x y (the series of y/(1 - e)):
-// three FMAs on the FP64 pipe instead of a correctly rounded division.  The seed's relative
-// error measured on GB300 over 2^30 samples is below 2^-22, so the step leaves about 2^-66 plus
-// the rounding of the last two FMAs (within 1 ulp).
-__device__ __forceinline__ double rcp_refined(double x) {
-    double y;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double e = fma(-x, y, 1.0);
-    return fma(y, fma(e, e, e), y);
-}
 
 // Chandrashekar two-point flux (Euler.jl:474-536) along direction d without the metric
 // factor, times 2, with the logarithmic means of Utilities.jl:34-44 written in sums and
@@ -932,7 +944,7 @@ __device__ __forceinline__ void store_split_node(double* S, int st, int col, con
         S[col] = q[0];
 #pragma unroll
         for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
-        S[(1 + DIM) * st + col] = (0.5 * q[0]) / p;
+        S[(1 + DIM) * st + col] = (0.5 * q[0]) * rcp_refined(p);
     } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
         S[col] = 0.5 * q[0];
 #pragma unroll
@@ -1003,7 +1015,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
 #pragma unroll
         for (int k = 0; k < NV; ++k) q[k] = P.Q[k * P.ndofs + gi];
         if (EULER) {
-            double ir = 1.0 / q[0];
+            double ir = rcp_refined(q[0]);
             double ke = 0.0;
 #pragma unroll
             for (int k = 0; k < DIM; ++k) {
