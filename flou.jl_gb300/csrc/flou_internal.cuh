@@ -715,16 +715,16 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
     int64_t g = (int64_t)e * ipow(N, DIM) + i;
     double invJ = CURV ? P.invJn[g] : P.elem_invJ[e];
     const double dt = P.dtp ? *P.dtp : P.dt;
+    const double c = dt * invJ;   // dt/J once per node: q + dt (dq/J) = q + c dq
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        double r = dq[k] * invJ;
         double o;
-        if (P.mode == 0) o = r;
-        else if (P.mode == 1) o = q[k] + dt * r;
-        else if (P.mode == 2) o = P.a0 * P.Q0[k * P.ndofs + g] + P.a1 * (q[k] + dt * r);
+        if (P.mode == 0) o = dq[k] * invJ;
+        else if (P.mode == 1) o = fma(c, dq[k], q[k]);
+        else if (P.mode == 2) o = fma(P.a0, P.Q0[k * P.ndofs + g], P.a1 * fma(c, dq[k], q[k]));
         else {
-            double kk = dt * r;
+            double kk = c * dq[k];
             if (P.a0 != 0.0) kk = P.a0 * P.aux[k * P.ndofs + g] + kk;   // first stage: k is not read
             P.aux[k * P.ndofs + g] = kk;
             o = q[k] + P.a1 * kk;
@@ -849,7 +849,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) elem_strong_kernel(ElemP
 // formulas share one reciprocal.
 // ---------------------------------------------------------------------------------------
 // Shared per-node arrays (length NN each) of the split form, by two-point flux:
-//   Chandrashekar:  ρ, vh_k = v_k/2, β = ρ/(2p)
+//   Chandrashekar:  ρ, vh_k = v_k/2, β = ρ/(2p), v_k
 //   Kennedy-Gruber: rh = ρ/2, vh_k = v_k/2, ph = p/2, eh = e/2 (e = ρe/ρ)
 //   StdAverage:     v_k, p, then the conserved variables
 //   scalar equations: u
@@ -858,7 +858,7 @@ struct SplitLayout {
     static constexpr int NV = (EQ == FLOU_EQ_EULER) ? DIM + 2 : 1;
     static constexpr int NARR = (EQ != FLOU_EQ_EULER) ? 1
                                 : (TP == FLOU_TP_STD_AVERAGE ? DIM + 1 + NV
-                                                             : (TP == FLOU_TP_CHANDRASHEKAR ? DIM + 2 : DIM + 3));
+                                                             : (TP == FLOU_TP_CHANDRASHEKAR ? 2 * DIM + 2 : DIM + 3));
 };
 
 // The pair kernels of the Chandrashekar flux return 2F♯ (one scale for all variables, exact):
@@ -877,7 +877,8 @@ struct PairScale {
 //   log branch: mean = (a-b)/ln(a/b).
 // With sρ = ρ1+ρ2, sβ = β1+β2, one reciprocal R = 1/(sρ sβ) gives 1/sρ and 1/sβ; the averaged
 // pressure is p̂ = sρ/(2 sβ), and with A = ρ̄/ρ_ln, B = β̄/β_ln (F itself on a series branch) the
-// enthalpy is h = 1/(2(γ-1)β_ln) + p̂/ρ_ln + v1·v2/2 = (A + B/(γ-1))/sβ + v1·v2/2.
+// enthalpy is h = 1/(2(γ-1)β_ln) + p̂/ρ_ln + v1·v2/2 = (A + B/(γ-1))/sβ + v1·v2/2, the last term
+// from the full velocity of one node and the halved one of the other.
 // Both reciprocals (R and 1/F) come from rcp_refined.  c_g = 1/(γ-1).
 // GEN: the flux along a general vector nv (the averaged metric column of a curvilinear element,
 // Euler.jl:474-536 with n = (Ja1 + Ja2)/2) instead of the axis d.
@@ -887,6 +888,7 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
     const double* rho = S;
     const double* vh = S + NN;
     const double* beta = S + (1 + DIM) * NN;
+    const double* vf = S + (2 + DIM) * NN;
     double r1 = rho[i], r2 = rho[l], b1 = beta[i], b2 = beta[l];
     double sr = r1 + r2, dr = r1 - r2;
     double sb = b1 + b2, db = b1 - b2;
@@ -914,9 +916,9 @@ __device__ __forceinline__ void chandrashekar_pair(const double* __restrict__ S,
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
         va[k] = vh[k * NN + i] + vh[k * NN + l];
-        dot = fma(vh[k * NN + i], vh[k * NN + l], dot);
+        dot = fma(vf[k * NN + i], vh[k * NN + l], dot);   // v1·v2/2
     }
-    double h = fma(rb, fma(c_g, B, A), 2.0 * dot);
+    double h = fma(rb, fma(c_g, B, A), dot);
     if (GEN) {
         double vn = 0.0;
 #pragma unroll
@@ -945,6 +947,8 @@ __device__ __forceinline__ void store_split_node(double* S, int st, int col, con
 #pragma unroll
         for (int k = 0; k < DIM; ++k) S[(1 + k) * st + col] = 0.5 * v[k];
         S[(1 + DIM) * st + col] = (0.5 * q[0]) * rcp_refined(p);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) S[(2 + DIM + k) * st + col] = v[k];
     } else if (TP == FLOU_TP_KENNEDY_GRUBER) {
         S[col] = 0.5 * q[0];
 #pragma unroll
@@ -997,7 +1001,12 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     double* sFb = FB_IN_PAIRS ? spair : sH + (HYB ? NV * NN : 0);
     uint8_t* stab = (uint8_t*)(sH + (HYB ? (FB_IN_PAIRS ? 1 : 2) * NV * NN : 0));   // pair table: a, b
     const int tid = threadIdx.x;
-    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    for (int t = tid; t < S::NOPS; t += blockDim.x) {
+        double v = P.ops[t];
+        // the diagonal of D♯ carries the pair scale (F♯(i, i) = F̃_i is not computed as a pair)
+        if (t >= N * N && t < 2 * N * N && (t - N * N) % (N + 1) == 0) v = PairScale<EQ, TP>::value * v;
+        sops[t] = v;
+    }
     if (tid == 0) {
         int c = 0;
         for (int a = 0; a < N; ++a)
@@ -1009,7 +1018,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     const double g = P.gamma;
     double q[NV];
     double v[EULER ? DIM : 1];
-    double p = 0.0;
+    double p = 0.0, qe = 0.0;   // pressure, ρe + p
     if (active) {
         int64_t gi = (int64_t)e * NPE + i;
 #pragma unroll
@@ -1023,6 +1032,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 ke = fma(q[1 + k], v[k], ke);
             }
             p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
+            qe = q[DIM + 1] + p;
             if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
             if constexpr (HYB || GAUSS) {   // vars_cons2entropy, FlouCommon/Euler.jl:273-307
                 double ip = 1.0 / p;
@@ -1227,8 +1237,10 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             // vanishes for an exact SBP operator, but the computed diagonal carries the round-off
             // that keeps the rows of D♯ summing to zero: dropping it loses discrete conservation
             // against a large constant pressure (the TGV's p0 = 1/(γM²)).
-            double Fd[NV];
-            if (CURV) {
+            // The diagonal of D♯ in shared memory already carries the pair scale.
+            const double ad = Dsh[pos + pos * N];
+            double acc[NV];
+            if constexpr (CURV) {
                 double an = 0.0, mn = 0.0, vn = 0.0;
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) {
@@ -1241,41 +1253,38 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     }
                 }
                 if constexpr (EULER) {
-                    Fd[0] = mn;
+                    acc[0] = ad * mn;
 #pragma unroll
-                    for (int k = 0; k < DIM; ++k) Fd[1 + k] = fma(q[1 + k], vn, p * sJa[k * SST + tid]);
-                    Fd[DIM + 1] = (q[DIM + 1] + p) * vn;
+                    for (int k = 0; k < DIM; ++k) acc[1 + k] = ad * fma(q[1 + k], vn, p * sJa[k * SST + tid]);
+                    acc[DIM + 1] = ad * ((q[DIM + 1] + p) * vn);
                 } else {
-                    Fd[0] = an * q[0];
+                    acc[0] = ad * (an * q[0]);
                 }
-            } else if (EULER) {
-                Fd[0] = q[1 + dir];
+            } else if constexpr (EULER) {
+                // D♯_ii (m_d, m_d v + p e_d, (ρe + p) v_d) with the common factors taken once; the
+                // pressure enters through the addend of an FMA (a select, not a predicated update)
+                const double aq = ad * q[1 + dir], adp = ad * p;
+                acc[0] = aq;
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) Fd[1 + k] = q[1 + dir] * v[k];
-                Fd[1 + dir] = Fd[1 + dir] + p;
-                Fd[DIM + 1] = (q[DIM + 1] + p) * v[dir];
-            } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
-                Fd[0] = P.adv[dir] * q[0];
+                for (int k = 0; k < DIM; ++k) acc[1 + k] = fma(aq, v[k], k == dir ? adp : 0.0);
+                acc[DIM + 1] = (ad * qe) * v[dir];
+            } else if constexpr (EQ == FLOU_EQ_LINEAR_ADVECTION) {
+                acc[0] = ad * (P.adv[dir] * q[0]);
             } else {
-                Fd[0] = q[0] * q[0] / 2.0;
+                acc[0] = ad * (q[0] * q[0] / 2.0);
             }
-            double acc[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+            // the N-1 other nodes of the line, from pos+1 on cyclically: every iteration is a pair
+            // (a loop over all j that skipped j = pos would still spend the FP64 issue slots of
+            // the skipped iteration, as predicated-off instructions)
             int pbase = el * NFD * NPAIR + line * NPAIR;
 #pragma unroll
-            for (int j = 0; j < N; ++j) {
-                double a = Dsh[pos + j * N];
-                if (j == pos) {
-                    a = PairScale<EQ, TP>::value * a;   // the scale the pair fluxes carry
+            for (int r = 1; r < N; ++r) {
+                const int j = pos + r < N ? pos + r : pos + r - N;
+                const double a = Dsh[pos + j * N];
+                int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+                int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, Fd[k], acc[k]);
-                } else {
-                    int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
-                    int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
-#pragma unroll
-                    for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPTX + pidx], acc[k]);
-                }
+                for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPTX + pidx], acc[k]);
             }
             // CURV: the metric is in the fluxes; the pair scale comes off with it
             double Ja = (CURV ? 1.0 : P.elem_Ja[e * DIM + dir]) * (1.0 / PairScale<EQ, TP>::value);
