@@ -695,15 +695,30 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         int64_t orr = (int64_t)(pr >> 1) * ipow(N, DIM - 1) + liner;
         double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
         if (LGL && P.lift_ends) {
-            if (pos == 0) {
-                double c = dgl[0] * sl;
+            // Only the two end nodes of a line take a face flux.  Where pos is the same for a whole
+            // warp (a direction whose node stride is a multiple of the warp) the branches skip the
+            // warp; elsewhere every thread would spend both branches' FP64 slots as predicated-off
+            // instructions, so each thread selects its coefficient (zero inside the line) instead.
+            constexpr int STRIDE = ipow(N, DIM - 1);   // the largest node stride, of the last direction
+            const bool uniform = dir == DIM - 1 && STRIDE % 32 == 0 && ipow(N, DIM) % 32 == 0;
+            if (uniform) {
+                if (pos == 0) {
+                    double c = dgl[0] * sl;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + ol);
-            }
-            if (pos == N - 1) {
-                double c = dgr[N - 1] * sr;
+                    for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + ol);
+                }
+                if (pos == N - 1) {
+                    double c = dgr[N - 1] * sr;
 #pragma unroll
-                for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + orr);
+                    for (int k = 0; k < NV; ++k) dq[k] = dq[k] - c * __ldcg(P.Fn + k * P.nfdofs + orr);
+                }
+            } else {
+                const bool atl = pos == 0;
+                const double c0 = atl ? dgl[0] : dgr[N - 1], sg = atl ? sl : sr;
+                const double c = (atl || pos == N - 1) ? c0 * sg : 0.0;
+                const int64_t o = atl ? ol : orr;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) dq[k] = fma(-c, __ldcg(P.Fn + k * P.nfdofs + o), dq[k]);
             }
         } else {
             double cl = dgl[pos] * sl, cr = dgr[pos] * sr;
