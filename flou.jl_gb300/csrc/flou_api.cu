@@ -142,6 +142,7 @@ ElemParams elem_params(const flou_ctx* c, const double* Q, const double* Q0, dou
     P.aux = mode == 3 ? const_cast<double*>(Q0) : nullptr;   // the 2N register travels in Q0's slot
     P.dtp = c->d_gate;
     P.lift_ends = c->lift_ends ? 1 : 0;
+    P.diag_roundoff = c->diag_roundoff ? 1 : 0;
     P.subfr = c->d_subfr;
     P.subJ = c->d_subJ;
     P.gamma = c->cfg.gamma;
@@ -596,6 +597,14 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
         ops[n * n] += 1.0 / omega[0];
         ops[n * n + (n - 1) + (n - 1) * n] -= 1.0 / omega[n - 1];
     }
+    // Whether every diagonal entry of the (possibly replaced) D♯ is round-off against its row:
+    // true for an SBP operator (2 ω_i D_ii = B_ii), false for a VCJH correction.
+    bool diag_roundoff = true;
+    for (int i = 0; i < n; ++i) {
+        double rowmax = 0.0;
+        for (int j = 0; j < n; ++j) rowmax = fmax(rowmax, fabs(ops[n * n + i + j * n]));
+        if (fabs(ops[n * n + i + i * n]) > 1e-14 * rowmax) diag_roundoff = false;
+    }
     if (c->cfg.volume_op != FLOU_OP_STRONG && !bnodes && c->cfg.equation != FLOU_EQ_EULER)
         return fail(c, FLOU_ERR_UNSUPPORTED,
                     "the split-form and hybrid operators of the scalar equations need a basis with boundary "
@@ -606,6 +615,7 @@ int32_t flou_set_operators(flou_ctx* c, const double* D, const double* Ds, const
     c->lgl = lgl;
     c->bnodes = bnodes;
     c->lift_ends = bnodes && lift_ends;
+    c->diag_roundoff = diag_roundoff;
     c->omega.assign(omega, omega + n);
     c->have_ops = true;
     drop_graph(c);

@@ -17,6 +17,7 @@ struct flou_ctx {
     bool lgl = false;               // l_l = e_1, l_r = e_n exactly: the kernels skip the zero terms
     bool bnodes = false;            // the basis has boundary nodes (hasboundaries), to round-off
     bool lift_ends = false;         // and ∂g vanishes off the end nodes (DGSEM; not a VCJH correction)
+    bool diag_roundoff = false;     // every diagonal entry of D♯ is round-off (an SBP operator's D♯ = 2D - B)
     std::string err;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     bool have_ops = false, have_mesh = false, have_geom = false;

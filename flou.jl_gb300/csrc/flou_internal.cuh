@@ -65,6 +65,7 @@ struct ElemParams {
     double* aux;                 // mode 3: the 2N-storage register k, read and rewritten per node
     const double* dtp;           // CFL stepping: dt lives in device memory (0: the run is over, skip)
     int32_t lift_ends;           // the lift ∂g acts on the end nodes only (else: every node of the line)
+    int32_t diag_roundoff;       // the diagonal of D♯ is round-off (DGSEM on Gauss-Lobatto nodes)
     const double* subfr;         // CURV hybrid: [9][ns] n, t, b of each subcell interface
     const double* subJ;          //   and its surface Jacobian; point ((e·DIM + dir)·n^(d-1) + line)·(n+1) + s
     double gamma;
@@ -1276,12 +1277,24 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     acc[0] = ad * (an * q[0]);
                 }
             } else if constexpr (EULER) {
-                // D♯_ii (m_d, m_d v + p e_d, (ρe + p) v_d) with the common factors taken once; the
-                // pressure enters through the addend of an FMA (a select, not a predicated update)
-                const double aq = ad * q[1 + dir], adp = ad * p;
-                acc[0] = aq;
+                // D♯_ii F̃_i = D♯_ii (m_d, m_d v + p e_d, (ρe + p) v_d) with the common factors
+                // taken once (the pressure as a selected FMA addend, not a predicated update).
+                // When D♯_ii is round-off (an SBP operator: DGSEM on Gauss-Lobatto nodes) the term
+                // only completes the computed row sums of D♯ against the large fluxes, the pressure
+                // and the enthalpy flux; the density and convective parts, D♯_ii m_d and
+                // D♯_ii m_d v, are smaller than the pressure part by ρ|v|²/p, and with a round-off
+                // weight they fall below the rounding of the terms kept, so they are left out.
+                const double adp = ad * p;
+                if (P.diag_roundoff) {
+                    acc[0] = 0.0;
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) acc[1 + k] = fma(aq, v[k], k == dir ? adp : 0.0);
+                    for (int k = 0; k < DIM; ++k) acc[1 + k] = k == dir ? adp : 0.0;
+                } else {
+                    const double aq = ad * q[1 + dir];
+                    acc[0] = aq;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) acc[1 + k] = fma(aq, v[k], k == dir ? adp : 0.0);
+                }
                 acc[DIM + 1] = (ad * qe) * v[dir];
             } else if constexpr (EQ == FLOU_EQ_LINEAR_ADVECTION) {
                 acc[0] = ad * (P.adv[dir] * q[0]);
