@@ -877,11 +877,14 @@ struct SplitLayout {
                                                              : (TP == FLOU_TP_CHANDRASHEKAR ? 2 * DIM + 2 : DIM + 3));
 };
 
-// The pair kernels of the Chandrashekar flux return 2F♯ (one scale for all variables, exact):
-// the node phase halves the metric factor and doubles the diagonal weight to match.
-template <int EQ, int TP>
+// The pair kernels return a power-of-two multiple of F♯ (one scale for all variables, exact):
+// 2 for the Chandrashekar flux, and on a general element a further 2 because the averaged
+// metric column enters as Ja_a + Ja_b, the pair fluxes being linear in it.  The node phase
+// divides the metric factor by the scale and multiplies the diagonal weight by it.
+template <int EQ, int TP, bool CURV = false>
 struct PairScale {
-    static constexpr double value = (EQ == FLOU_EQ_EULER && TP == FLOU_TP_CHANDRASHEKAR) ? 2.0 : 1.0;
+    static constexpr double value = ((EQ == FLOU_EQ_EULER && TP == FLOU_TP_CHANDRASHEKAR) ? 2.0 : 1.0) *
+                                    (CURV ? 2.0 : 1.0);
 };
 
 
@@ -1020,7 +1023,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
     for (int t = tid; t < S::NOPS; t += blockDim.x) {
         double v = P.ops[t];
         // the diagonal of D♯ carries the pair scale (F♯(i, i) = F̃_i is not computed as a pair)
-        if (t >= N * N && t < 2 * N * N && (t - N * N) % (N + 1) == 0) v = PairScale<EQ, TP>::value * v;
+        if (t >= N * N && t < 2 * N * N && (t - N * N) % (N + 1) == 0) v = PairScale<EQ, TP, CURV>::value * v;
         sops[t] = v;
     }
     if (tid == 0) {
@@ -1143,10 +1146,10 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 ib = NN + 2 * ln + side;
             }
             double F[NV];
-            double nv[DIM];   // CURV: the averaged metric column (Ja_a + Ja_b)/2
+            double nv[DIM];   // CURV: twice the averaged metric column, Ja_a + Ja_b (the pair scale)
             if (CURV) {
 #pragma unroll
-                for (int k = 0; k < DIM; ++k) nv[k] = (sJa[k * SST + ia] + sJa[k * SST + ib]) / 2.0;
+                for (int k = 0; k < DIM; ++k) nv[k] = sJa[k * SST + ia] + sJa[k * SST + ib];
             }
             if constexpr (CURV && EULER) {
                 if (TP == FLOU_TP_CHANDRASHEKAR) {
@@ -1315,7 +1318,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 for (int k = 0; k < NV; ++k) acc[k] = fma(a, spair[k * NPTX + pidx], acc[k]);
             }
             // CURV: the metric is in the fluxes; the pair scale comes off with it
-            double Ja = (CURV ? 1.0 : P.elem_Ja[e * DIM + dir]) * (1.0 / PairScale<EQ, TP>::value);
+            double Ja = (CURV ? 1.0 : P.elem_Ja[e * DIM + dir]) * (1.0 / PairScale<EQ, TP, CURV>::value);
             double Fl[NV], Fr[NV];   // GAUSS: F♯(Q_i, Q̃) - l·F♯(·, Q̃) at both ends (OpDivergence.jl:410-425)
             if constexpr (GAUSS) {
                 const int xb = NPT + 2 * N * (el * NFD + line);
