@@ -269,6 +269,7 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
         vr2 = fma(vr[k], vr[k], vr2);
     }
     const double g1 = g - 1.0;
+    const double ig1 = rcp_refined(g1);   // 1/(γ-1): multiplications instead of divisions below
     const double pl = g1 * fma(-0.5 * rl, vl2, ql[DIM + 1]), pr = g1 * fma(-0.5 * rr, vr2, qr[DIM + 1]);
     double vm[3];
 #pragma unroll
@@ -296,7 +297,7 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
         double vv = vm[0] * vm[0];
         if (DIM > 1) vv = fma(vm[1], vm[1], vv);
         if (DIM > 2) vv = fma(vm[2], vm[2], vv);
-        double h = fma(mb.inv, 0.5 / g1, fma(-0.25, s, fma(phat, mr.inv, vv)));
+        double h = fma(mb.inv, 0.5 * ig1, fma(-0.25, s, fma(phat, mr.inv, vv)));
         double m = mr.mean * vm[0];
         A[0] = m;
         A[1] = fma(m, vm[0], phat);
@@ -328,13 +329,13 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
         // the 3D branch takes the left momenta from Qr (Euler.jl:257): no momentum jump there
 #pragma unroll
         for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? 0.0 : qr[1 + k] - ql[1 + k];
-        double c1 = mb.inv / g1, c2 = 0.0;
+        double c1 = mb.inv * ig1, c2 = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) {
             c1 = fma(vl[k], vr[k], c1);
             c2 = fma(vm[k], vr[k] - vl[k], c2);
         }
-        c2 = c2 + (pr * irr - pl * irl) / g1;   // (1/βr - 1/βl)/(2(γ-1))
+        c2 = c2 + (pr * irr - pl * irl) * ig1;   // (1/βr - 1/βl)/(2(γ-1))
         D[DIM + 1] = fma(0.5 * c1, rr - rl, 0.5 * (rl + rr) * c2);
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = fma(-lam, D[k], A[k]);
@@ -346,9 +347,10 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
     for (int k = 1; k < DIM; ++k) vv = fma(vm[k], vm[k], vv);
     const double v2 = fma(2.0, vv, -0.5 * (vl2 + vr2));
     const double a = sqrt_refined(g * phat * mr.inv);
-    const double h = fma(0.5 * g / g1, mb.inv, 0.5 * v2);
+    const double ig = rcp_refined(g);
+    const double h = fma(0.5 * g * ig1, mb.inv, 0.5 * v2);
     double dW[NV];
-    dW[0] = (mr.L + mb.L / g1) - (vl2 * bl - vr2 * br);
+    dW[0] = fma(mb.L, ig1, mr.L) - (vl2 * bl - vr2 * br);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) dW[1 + k] = 2.0 * (bl * vl[k] - br * vr[k]);
     dW[DIM + 1] = -2.0 * (bl - br);
@@ -367,10 +369,10 @@ __device__ __forceinline__ void euler_face_flux_es(const double* ql, const doubl
     y[0] = fma(fma(-u, a, h), dW[DIM + 1], y[0]);
     y[DIM + 1] = fma(fma(u, a, h), dW[DIM + 1], y[DIM + 1]);
     y[1] = fma(0.5 * v2, dW[DIM + 1], ye);
-    const double rho = mr.mean, ta = rho / (2.0 * g);
+    const double rho = mr.mean, ta = rho * (0.5 * ig);
     double z[NV];
     z[0] = fabs(u - a) * ta * y[0];
-    z[1] = fabs(u) * (g1 * rho / g) * y[1];
+    z[1] = fabs(u) * (g1 * rho * ig) * y[1];
 #pragma unroll
     for (int k = 1; k < DIM; ++k) z[1 + k] = fabs(u) * phat * y[1 + k];
     z[DIM + 1] = fabs(u + a) * ta * y[DIM + 1];
@@ -1366,6 +1368,28 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
         }
         if constexpr (HYB && EULER) {
             __syncthreads();
+            if constexpr (!GAUSS) {
+                // F̄_p = Σ_{r<p} increment_r: exclusive prefix sums along each line, in place, one
+                // thread per line (the same order of additions as a sum from r = 0; a sum per node
+                // would repeat the additions and diverge within warps on its trip count)
+                for (int t = tid; t < S::EPB * NFD; t += blockDim.x) {
+                    const int elp = t / NFD, ln = t - elp * NFD;
+                    if (e0 + elp >= P.nelem) continue;
+                    double run[NV];
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) run[k] = 0.0;
+                    for (int pp = 0; pp < N; ++pp) {
+                        const int j = elp * NPE + tp_node<DIM>(N, dir, ln, pp);
+#pragma unroll
+                        for (int k = 0; k < NV; ++k) {
+                            const double x = sH[k * NN + j];
+                            sH[k * NN + j] = run[k];
+                            run[k] += x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
             if (active) {
                 int pos, line;
                 tp_coords<DIM>(N, i, dir, pos, line);
@@ -1373,14 +1397,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     const int il = el * NPE + tp_node<DIM>(N, dir, line, pos - 1);
                     double Fh[NV];
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) Fh[k] = 0.0;
-                    if constexpr (!GAUSS) {
-                        for (int r = 0; r < pos; ++r) {
-                            int j = el * NPE + tp_node<DIM>(N, dir, line, r);
-#pragma unroll
-                            for (int k = 0; k < NV; ++k) Fh[k] += sH[k * NN + j];
-                        }
-                    }
+                    for (int k = 0; k < NV; ++k) Fh[k] = GAUSS ? 0.0 : sH[k * NN + tid];
                     // FV flux in the subcell interface's frame times its surface Jacobian
                     // (PhysicalRegions.jl:68-300): the positive axis and Ja_dd on a Cartesian
                     // element, the uploaded subgrid geometry on a general one
@@ -1430,8 +1447,8 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                         double bb = 0.0;
 #pragma unroll
                         for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + tid] - sW[k * NN + il], Fh[k] - Fv[k], bb);
-                        double dl = sqrt(fma(bb, bb, P.blend));
-                        dl = fmax((dl - bb) / dl, 0.5);
+                        double dl = sqrt_refined(fma(bb, bb, P.blend));
+                        dl = fmax((dl - bb) * rcp_refined(dl), 0.5);
 #pragma unroll
                         for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = fma(dl, Fh[k] - Fv[k], Fv[k]);
                     }
@@ -1458,8 +1475,8 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                                 Fb[k] += sH[k * NN + jp];
                                 bb = fma(sW[k * NN + jn] - sW[k * NN + jp], Fb[k] - sFb[k * NN + jn], bb);
                             }
-                            double dl = sqrt(fma(bb, bb, P.blend));
-                            dl = fmax((dl - bb) / dl, 0.5);
+                            double dl = sqrt_refined(fma(bb, bb, P.blend));
+                            dl = fmax((dl - bb) * rcp_refined(dl), 0.5);
 #pragma unroll
                             for (int k = 0; k < NV; ++k) {
                                 double fv = sFb[k * NN + jn];
@@ -1475,7 +1492,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             if (active) {
                 int pos, line;
                 tp_coords<DIM>(N, i, dir, pos, line);
-                double iw = 1.0 / P.omega1[pos];
+                double iw = rcp_refined(P.omega1[pos]);
                 int jr = (pos < N - 1) ? el * NPE + tp_node<DIM>(N, dir, line, pos + 1) : -1;
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {   // GAUSS: the element's face fluxes close both ends
