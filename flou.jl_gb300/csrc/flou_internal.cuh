@@ -1056,9 +1056,9 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
             qe = q[DIM + 1] + p;
             if (!(q[0] > 0.0 && p > 0.0)) raise_nonphysical(P.status, e);
             if constexpr (HYB || GAUSS) {   // vars_cons2entropy, FlouCommon/Euler.jl:273-307
-                double ip = 1.0 / p;
+                double ip = rcp_refined(p);
                 double sv = log(p) - g * log(q[0]);
-                sW[tid] = (g - sv) / (g - 1.0) - ke * ip * 0.5;
+                sW[tid] = (g - sv) * rcp_refined(g - 1.0) - ke * ip * 0.5;
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) sW[(1 + k) * NN + tid] = q[1 + k] * ip;
                 sW[(DIM + 1) * NN + tid] = -q[0] * ip;
@@ -1092,7 +1092,7 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     for (int k = 0; k < NV; ++k) w[k] = fma(lv[pos], sW[k * NN + j], w[k]);
                 }
                 // vars_entropy2prim, FlouCommon/Euler.jl:309-334, then vars_prim2cons
-                double wl = w[DIM + 1], iwl = 1.0 / wl;
+                double wl = w[DIM + 1], iwl = rcp_refined(wl);
                 double vp[DIM], qp[NV], vv = 0.0;
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) {
@@ -1101,14 +1101,15 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 }
                 double sv = g - (g - 1.0) * (w[0] - wl * vv * 0.5);
                 // ((-W_last)^γ e^s)^(1/(1-γ)) as one exponential
-                double pp = exp(fma(g, log(-wl), sv) / (1.0 - g));
+                const double ig1 = rcp_refined(g - 1.0);
+                double pp = exp(-fma(g, log(-wl), sv) * ig1);
                 double rho = -pp * wl;
                 qp[0] = rho;
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) qp[1 + k] = rho * vp[k];
-                qp[DIM + 1] = pp / (g - 1.0) + 0.5 * rho * vv;
+                qp[DIM + 1] = fma(pp, ig1, 0.5 * rho * vv);
                 if (!(rho > 0.0 && pp > 0.0)) raise_nonphysical(P.status, e0 + elp);
-                store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, 1.0 / rho);
+                store_split_node<DIM, TP>(sprim, SST, NN + t, qp, vp, pp, rcp_refined(rho));
                 if constexpr (CURV) {   // the line end's subcell interface: n·Js (OpDivergence.jl:403-404)
                     const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
                     const int64_t si = (((int64_t)(e0 + elp) * DIM + dir) * NFD + line) * (N + 1) + (side ? N : 0);
