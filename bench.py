@@ -544,19 +544,22 @@ def run_profile(which):
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "tgv3d 32^3 p=3 + limiter", "ndofs": disc.ndofs, "steps": 2}))
         return 0
-    if which == "H":   # mesh B with the hybrid operator and MatrixDissipation (Shockwave2D's operator)
-        import flou_cuda as F
+    if which in ("H", "I"):   # mesh B, MatrixDissipation (Shockwave2D's flux): H the hybrid operator on
+        import flou_cuda as F    # Gauss-Lobatto nodes, I the split form on Gauss nodes
         eq = F.EulerEquation(3, 1.4)
         mesh = F.CartesianMesh((0.0,) * 3, (2 * math.pi,) * 3, (16,) * 3)
         F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
-        b = F.LagrangeBasis("GLL", 8)
+        b = F.LagrangeBasis("GLL" if which == "H" else "GL", 8)
         md = F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)
-        disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), 5), eq, F.HybridDivOperator(md, 1.0), {})
+        op = F.HybridDivOperator(md, 1.0) if which == "H" else F.SplitDivOperator(md)
+        disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), 5), eq, op, {})
         Qd = torch.from_numpy(np.ascontiguousarray(F.initial.taylor_green(eq, disc.coords, mach=0.1).T)).cuda()
         dt = 0.2 * disc.ctx.max_dt(Qd, 1.0)
         disc.ctx.step(Qd, dt, 2)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": "tgv3d 16^3 p=7 hybrid MatrixDissipation", "ndofs": disc.ndofs, "steps": 2}))
+        print(json.dumps({"profile_case": "tgv3d 16^3 p=7 %s MatrixDissipation" % ("hybrid GLL" if which == "H" else
+                                                                                  "split GL"),
+                          "ndofs": disc.ndofs, "steps": 2}))
         return 0
     nel, n = (32, 4) if which == "A" else (16, 8)
     disc, Q0 = make_tgv(nel, n)
@@ -607,7 +610,7 @@ def main():
                     help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
                          "several minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
-    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G", "H"], default=None,
+    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G", "H", "I"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling); "
                          "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps); F: mesh A with the "
