@@ -311,6 +311,40 @@ __global__ void fma_probe_kernel(double* sink, int iters, double x) {
     if (s == 1234.5678) sink[threadIdx.x] = s;   // never true; keeps the chains alive
 }
 
+// Accuracy of rcp_refined and sqrt_refined against the correctly rounded 1/x and sqrt(x): the
+// largest error in units of 2^-53 relative over n doubles with random mantissas and exponents in
+// [2^-40, 2^40] (splitmix64 of the sample index), one (rcp, sqrt) pair per block in out.
+// Launched with 256 threads per block.
+__global__ void refined_math_kernel(long long n, double* out) {
+    double mr = 0.0, ms = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        unsigned long long z = (unsigned long long)t + 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const unsigned long long ex = 1023ull - 40ull + (z >> 52) % 81ull;
+        const double x = __longlong_as_double((long long)((ex << 52) | (z & 0xFFFFFFFFFFFFFull)));
+        const double r = 1.0 / x, q = sqrt(x);
+        mr = fmax(mr, fabs(rcp_refined(x) - r) / (r * 0x1p-53));
+        ms = fmax(ms, fabs(sqrt_refined(x) - q) / (q * 0x1p-53));
+    }
+    __shared__ double red[2][256];
+    red[0][threadIdx.x] = mr;
+    red[1][threadIdx.x] = ms;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            red[0][threadIdx.x] = fmax(red[0][threadIdx.x], red[0][threadIdx.x + h]);
+            red[1][threadIdx.x] = fmax(red[1][threadIdx.x], red[1][threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 * blockIdx.x] = red[0][0];
+        out[2 * blockIdx.x + 1] = red[1][0];
+    }
+}
+
 // FP64 tensor-core probe: eight independent m8n8k4 DMMA chains per warp (mma.sync with f64
 // operands, the only FP64 matrix instruction of sm_103a; tcgen05 has no f64 kind).  Each
 // instruction does 8*8*4 multiply-adds for the warp.
@@ -1124,6 +1158,31 @@ int32_t flou_fp64_peak(double* gflops) {
     if (e != cudaSuccess) return FLOU_ERR_CUDA;
     double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
     *gflops = flops / (ms * 1e-3) / 1e9;
+    return FLOU_OK;
+}
+
+int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_err) {
+    if (!rcp_err || !sqrt_err || nsamples < 1) return FLOU_ERR_ARG;
+    flou_ctx* c = nullptr;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FLOU_ERR_CUDA;
+    const int blocks = sms * 4;
+    double* d = nullptr;
+    CK(cudaMalloc((void**)&d, 2 * (size_t)blocks * sizeof(double)), "check buffer");
+    refined_math_kernel<<<blocks, 256>>>((long long)nsamples, d);
+    std::vector<double> h(2 * (size_t)blocks);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(h.data(), d, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return FLOU_ERR_CUDA;
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < blocks; ++k) {
+        a = std::max(a, h[2 * k]);
+        b = std::max(b, h[2 * k + 1]);
+    }
+    *rcp_err = a;
+    *sqrt_err = b;
     return FLOU_OK;
 }
 

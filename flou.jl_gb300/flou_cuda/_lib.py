@@ -93,6 +93,7 @@ PROTOTYPES = {
     "flou_rhs_noalloc": [_P, _P, _P, ctypes.c_double],
     "flou_fp64_peak": [_D],
     "flou_fp64_dmma_peak": [_D],
+    "flou_check_refined_math": [ctypes.c_int64, _D, _D],
     "flou_set_dissipation": [_P, _P, ctypes.c_int32],
     "flou_check_mesh": [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32, _I32, _U8, _I32,
                         ctypes.c_char_p, ctypes.c_int32],

@@ -252,6 +252,11 @@ int32_t flou_fp64_peak(double* gflops);
  * GFLOP/s, the measurement behind the choice of CUDA-core FP64 for the derivative-matrix
  * contraction.  No counterpart in the reference. */
 int32_t flou_fp64_dmma_peak(double* gflops);
+/* Accuracy check of the FP64 reciprocal and square root the kernels build from the MUFU
+ * approximations refined by one third-order step: the largest error against the correctly rounded
+ * 1/x and sqrt(x) over nsamples doubles with exponents in [2^-40, 2^40], in units of 2^-53
+ * relative (2 = 1 ulp).  No counterpart in the reference. */
+int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_err);
 
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
  * Covers the Euler equations with the strong-form volume term or the split form with the

@@ -310,3 +310,14 @@ def test_vcjh_reconstructions(basis, eta, op):
     disc = F.MultielementDisc(mesh, std, eq, _ops()[op](), {})
     assert np.abs(disc.std.dg[0][1:]).max() > 1e-3   # the lift is not confined to the end nodes
     _check(disc, smooth_euler_state(disc, seed=13), cfl=0.2)
+
+
+def test_refined_reciprocal_and_square_root_within_one_ulp():
+    """The kernels' reciprocal and square root (the MUFU approximations rcp.approx.ftz.f64 /
+    rsqrt.approx.ftz.f64 refined by one third-order step) against CUDA's correctly rounded 1/x
+    and sqrt(x) on 2^26 doubles with exponents in [2^-40, 2^40]: within 1 ulp (2 units of 2^-53)."""
+    import ctypes
+    lib = F.load()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    assert lib.flou_check_refined_math(1 << 26, ctypes.byref(a), ctypes.byref(b)) == 0
+    assert 0.0 < a.value <= 2.0 and 0.0 < b.value <= 2.0, (a.value, b.value)
