@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -66,7 +67,9 @@ void drop_graph(flou_ctx* c) {
     c->cfl_Q = nullptr;
 }
 
-int ready(flou_ctx* c) {
+// Every set-up check a residual needs, with no allocation: flou_rhs (through ready) and
+// flou_rhs_noalloc accept exactly the same contexts.
+int validate(flou_ctx* c) {
     if (!c) return FLOU_ERR_ARG;
     if (!c->have_ops) return fail(c, FLOU_ERR_STATE, "flou_set_operators has not been called");
     if (!c->have_mesh) return fail(c, FLOU_ERR_STATE, "flou_set_mesh has not been called");
@@ -84,8 +87,13 @@ int ready(flou_ctx* c) {
         if (b >= 0 && c->bc_kind[b] == FLOU_BC_STATE_FIELD && !c->d_bcfield)
             return fail(c, FLOU_ERR_STATE, "flou_set_bc_field has not been called (boundary %d)", b + 1);
     }
-    int e = ensure(c, &c->d_Fn, (size_t)c->nfdofs * c->nv, "face-flux buffer");
-    return e;
+    return FLOU_OK;
+}
+
+int ready(flou_ctx* c) {
+    int r = validate(c);
+    if (r) return r;
+    return ensure(c, &c->d_Fn, (size_t)c->nfdofs * c->nv, "face-flux buffer");
 }
 
 FaceParams face_params(const flou_ctx* c, const double* Q) {
@@ -1233,7 +1241,10 @@ int32_t flou_fp64_dmma_peak(double* gflops) {
 // keeps the last call's contents; nothing in it has to start at zero, because the face
 // kernel overwrites every value it later reads.  The first call on a device looks up the
 // array's device address (cudaGetSymbolAddress) for that device; make that first call
-// before any stream capture.
+// before any stream capture.  The address is cached per device for the life of the
+// process; cudaDeviceReset destroys every context's memory and the library's module on
+// that device, so after a reset neither old contexts nor this cache may be used (a process
+// that resets a device must not call flou_rhs_noalloc on it again).
 // ---------------------------------------------------------------------------------------
 #define FLOU_NOALLOC_MAX_FACE_VALUES (1 << 20)
 
@@ -1241,7 +1252,9 @@ static __device__ __align__(256) double g_noalloc_face_flux[FLOU_NOALLOC_MAX_FAC
 
 namespace {
 constexpr int kMaxDevices = 64;
-double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+// Written once per device; concurrent first calls from several host threads store the same
+// address, so a relaxed atomic is enough.
+std::atomic<double*> g_noalloc_ptr[kMaxDevices] = {};
 
 // Once per device, with that device current: the device address of the scratch array.
 // Returns nullptr (and sets *err) when the lookup fails.
@@ -1253,28 +1266,22 @@ double* noalloc_scratch(cudaError_t* err) {
         *err = cudaErrorInvalidDevice;
         return nullptr;
     }
-    if (!g_noalloc_ptr[dev]) {
+    double* cached = g_noalloc_ptr[dev].load(std::memory_order_relaxed);
+    if (!cached) {
         void* p = nullptr;
         *err = cudaGetSymbolAddress(&p, g_noalloc_face_flux);
         if (*err != cudaSuccess) return nullptr;
-        g_noalloc_ptr[dev] = (double*)p;
+        cached = (double*)p;
+        g_noalloc_ptr[dev].store(cached, std::memory_order_relaxed);
     }
-    return g_noalloc_ptr[dev];
+    return cached;
 }
 }  // namespace
 
 extern "C" int32_t flou_rhs_noalloc(flou_ctx* c, double* dQ, const double* Q, double t) {
     (void)t;
-    if (!c) return FLOU_ERR_ARG;
-    if (!c->have_ops || !c->have_mesh || !c->have_geom)
-        return fail(c, FLOU_ERR_STATE, "operators, mesh and geometry must be set before flou_rhs_noalloc");
-    for (int f = 0; f < c->nfaces; ++f) {
-        int b = c->h_face_bc[f];
-        if (b >= 0 && (b >= c->nbcs || c->bc_kind[b] == 0))
-            return fail(c, FLOU_ERR_STATE, "boundary index %d of face %d has no boundary condition", b + 1, f + 1);
-        if (b >= 0 && c->bc_kind[b] == FLOU_BC_STATE_FIELD && !c->d_bcfield)
-            return fail(c, FLOU_ERR_STATE, "flou_set_bc_field has not been called (boundary %d)", b + 1);
-    }
+    int r = validate(c);
+    if (r) return r;
     if (!dQ || !Q) return fail(c, FLOU_ERR_ARG, "null state pointer");
     int64_t need = c->nfdofs * c->nv;
     if (need > FLOU_NOALLOC_MAX_FACE_VALUES)

@@ -218,8 +218,11 @@ int32_t flou_max_dt(flou_ctx* ctx, const double* Q, double cfl, double* dt, int3
  * nfaces x n^(d-1) x nvars), shared by all calls, so overlapping calls race.  For callers
  * whose device memory belongs to another allocator (CUDA.jl's pool, PyTorch's caching
  * allocator), where flou_rhs's lazy cudaMalloc of its face buffer could fail or is not
- * allowed.  The first call on a device looks up the array's address; make it before any
- * stream capture.  No counterpart in the reference. */
+ * allowed.  It accepts exactly the contexts flou_rhs accepts (FLOU_ERR_STATE, before any
+ * launch, when a set-up call the operator needs is missing).  The first call on a device
+ * looks up the array's address and caches it for the process; make it before any stream
+ * capture, and make no call on a device after cudaDeviceReset.  No counterpart in the
+ * reference. */
 int32_t flou_rhs_noalloc(flou_ctx* ctx, double* dQ, const double* Q, double t);
 
 /* Number of nodes (DOFs in Flou's sense, DofHandler.jl:53) and of variables. */
