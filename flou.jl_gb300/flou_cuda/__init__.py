@@ -16,7 +16,7 @@ from .std import DGSEMrec, LagrangeBasis, StdHex, StdQuad, StdSegment, VCJHrec
 from .timeint import (ORK256, SSPRK33, CarpenterKennedy2N54, LowStorageRK2N, get_cfl_callback, get_limiter_callback,
                       get_monitor_callback, get_save_callback, make_callback_list, timeintegrate)
 from . import initial
-from .io import load_restart, save_restart, variablenames, write_vtu
+from .io import load_restart, save_restart, variablenames, write_vtkhdf, write_vtu
 from .batch import Batch, adjoint_solve_batch
 
 rhs = rhs_

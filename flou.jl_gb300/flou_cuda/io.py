@@ -3,10 +3,13 @@
 Reference: src/FlouSpatial/IO.jl:16-126 and src/FlouBiz/FlouBiz.jl:30-113 write VTKHDF files
 (HDF5) with Lagrange cells on equispaced nodes (StdSegment.jl:56-58, vtk_connectivities of
 StdQuad.jl:185-195 / StdHex.jl:174-196, vtk_type 68 / 70 / 72), the solution variables under
-`variablenames`, the cell region and the time as field data.  This image has no HDF5 library, so
-the same content is written as a VTK XML UnstructuredGrid (.vtu, raw appended binary), which
-ParaView / VTK read the same way.  A state on the device is resampled to the equispaced nodes on
-the device before it is copied out.
+`variablenames`, the cell region and the time as field data.  `write_vtkhdf` writes the same
+file: the /VTKHDF group with its Version and Type attributes, NumberOfPoints, Points,
+NumberOfConnectivityIds, Connectivity, NumberOfCells, Types, Offsets, CellData/Region,
+FieldData/Time and one PointData dataset per variable, through the HDF5 encoder of
+`flou_cuda.hdf5` (no HDF5 library is needed).  `write_vtu` writes the same content as a VTK XML
+UnstructuredGrid (.vtu).  A state on the device is resampled to the equispaced nodes on the
+device before it is copied out.
 
 Restart files hold the state bit for bit: a 64-byte header (magic, version, dim, nodes per
 direction, elements, variables, DOFs, time, iteration, CRC-32 of the data) and the column-major
@@ -103,6 +106,13 @@ def vtk_connectivity(dim, n):
     return corners + edges + faces + interior
 
 
+def cell_connectivity(dim, n, ne):
+    """The connectivity both writers store: element e's local points in VTK order, offset by
+    e n^dim (IO.jl:45-46)."""
+    local = np.array(vtk_connectivity(dim, n), dtype=np.int64)
+    return (np.arange(ne, dtype=np.int64)[:, None] * n ** dim + local[None, :]).ravel()
+
+
 def _equispaced_operator(disc):
     """Tensor-product interpolation from the solution nodes to n equispaced nodes per
     direction (StdSegment.jl:56-58: range(-1, 1, n))."""
@@ -137,8 +147,7 @@ def write_vtu(path, disc, Q, time=None, names=None):
     pts = _project(disc, disc.coords, I)                # (ndofs, 3)
     vals = _project(disc, Q, I)                          # (ndofs, nvars)
     names = names or variablenames(disc.equation)
-    local = np.array(vtk_connectivity(d, n), dtype=np.int64)
-    conn = (np.arange(ne, dtype=np.int64)[:, None] * npe + local[None, :]).ravel()
+    conn = cell_connectivity(d, n, ne)
     offsets = np.arange(1, ne + 1, dtype=np.int64) * npe
     types = np.full(ne, VTK_TYPE[d], dtype=np.uint8)
     regions = np.ones(ne, dtype=np.int64)
@@ -190,3 +199,50 @@ def read_vtu(path):
         arr = np.frombuffer(rest[off + 8:off + 8 + nb], dtype=dt[typ])
         out[name] = arr.reshape(-1, int(ncomp)) if ncomp else arr
     return out
+
+
+def _snapshot_arrays(disc, Q):
+    """Points (npoints, 3), values (npoints, nvars), connectivity, offsets (ncells + 1), types,
+    regions of a snapshot, element by element as IO.jl:33-66 builds them."""
+    d, n = disc.mesh.dim, disc.std.n
+    ne, npe = disc.mesh.nelements, n ** d
+    I = _equispaced_operator(disc)
+    pts = _project(disc, disc.coords, I)
+    if pts.shape[1] < 3:   # IO.jl pads the coordinates with zeros to three components
+        pts = np.hstack([pts, np.zeros((pts.shape[0], 3 - pts.shape[1]))])
+    vals = _project(disc, Q, I)
+    conn = cell_connectivity(d, n, ne)
+    offsets = np.arange(0, ne + 1, dtype=np.int64) * npe
+    types = np.full(ne, VTK_TYPE[d], dtype=np.uint8)
+    regions = np.asarray(getattr(disc.mesh, "regions", np.ones(ne)), dtype=np.int64)
+    return np.ascontiguousarray(pts, dtype=np.float64), vals, conn, offsets, types, regions
+
+
+def write_vtkhdf(path, disc, Q, time=None, names=None):
+    """A snapshot of Q (numpy (ndofs, nvars) or a CUDA tensor (nvars, ndofs)) as the VTKHDF file
+    Flou writes (open_for_write + add_fielddata!(file, [t], "Time") + add_solution!, IO.jl:16-126,
+    FlouBiz.jl:38-113, FlouTime.jl:67-80)."""
+    from . import hdf5
+    pts, vals, conn, offsets, types, regions = _snapshot_arrays(disc, Q)
+    names = names or variablenames(disc.equation)
+    root = {
+        "@attrs": {"Version": np.array([1, 0], dtype=np.int64), "Type": b"UnstructuredGrid"},
+        "NumberOfPoints": np.array([pts.shape[0]], dtype=np.int64),
+        "Points": pts,
+        "NumberOfConnectivityIds": np.array([conn.size], dtype=np.int64),
+        "Connectivity": conn,
+        "NumberOfCells": np.array([types.size], dtype=np.int64),
+        "Types": types,
+        "Offsets": offsets,
+        "CellData": {"Region": regions},
+    }
+    if time is not None:
+        root["FieldData"] = {"Time": np.array([float(time)])}
+    root["PointData"] = {nm: np.ascontiguousarray(vals[:, k]) for k, nm in enumerate(names)}
+    hdf5.write(path, {"VTKHDF": root})
+
+
+def read_vtkhdf(path):
+    """The /VTKHDF group of a file written by write_vtkhdf, as a dict of numpy arrays."""
+    from . import hdf5
+    return hdf5.read(path)["VTKHDF"]

@@ -150,17 +150,16 @@ class SaveCallback:
         return min(later) if later else math.inf
 
     def save(self, disc, Q, it, t):
-        from .io import write_vtu
-        path = "%s_%010d.vtu" % (self.basename, it)
-        write_vtu(path, disc, Q, time=t)
+        from .io import write_vtkhdf
+        path = "%s_%010d.hdf" % (self.basename, it)
+        write_vtkhdf(path, disc, Q, time=t)
         self.files.append(path)
 
 
 def get_save_callback(basename, iter=True):
     """get_save_callback(basename; iter=true) (FlouTime.jl:67-90): the solution at the start and
-    after every selected step, with its time, as `basename_%010d.vtu` (VTK Lagrange cells on
-    equispaced nodes; the reference writes the same content as VTKHDF `.hdf`, and this image has
-    no HDF5 library)."""
+    after every selected step, with its time, as the VTKHDF file `basename_%010d.hdf` that
+    FlouTime.jl:70-75 writes (Lagrange cells on equispaced nodes, FieldData/Time)."""
     return SaveCallback(basename, iter)
 
 

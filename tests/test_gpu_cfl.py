@@ -113,20 +113,20 @@ def test_save_callback_writes_selected_steps(tmp_path):
     base = os.path.join(tmp_path, "sol")
     cb = F.get_save_callback(base, iter=[2, 5])
     sol, _ = F.timeintegrate(Q0, disc, disc.equation, F.SSPRK33(), 6 * dt, dt=dt, callback=cb)
-    assert [os.path.basename(f) for f in cb.files] == ["sol_%010d.vtu" % i for i in (0, 2, 5)]
-    d = F.io.read_vtu(cb.files[1])
-    assert abs(d["Time"][0] - 2 * dt) < 1e-15
+    assert [os.path.basename(f) for f in cb.files] == ["sol_%010d.hdf" % i for i in (0, 2, 5)]
+    d = F.io.read_vtkhdf(cb.files[1])
+    assert abs(d["FieldData"]["Time"][0] - 2 * dt) < 1e-15
     ref2 = oracle_for(disc).ssprk3(Q0, dt, 2)
     # the snapshot holds the state resampled to equispaced nodes; the density at the element
     # corners (shared by both node sets on Gauss-Lobatto nodes) equals the state's
-    assert abs(d["rho"][0] - ref2[0, 0]) < 1e-12
+    assert abs(d["PointData"]["rho"][0] - ref2[0, 0]) < 1e-12
     assert rel_linf(sol.u[-1], oracle_for(disc).ssprk3(Q0, dt, 6)) <= STEP_TOL
     base2 = os.path.join(tmp_path, "cfl")
     cb2 = F.get_save_callback(base2)
     tf = 3.5 * disc.ctx.max_dt(Q0, 0.4)
     F.timeintegrate(Q0, disc, disc.equation, F.SSPRK33(), tf, callback=[F.get_cfl_callback(0.4), cb2])
     assert len(cb2.files) == 5   # the start and 4 steps
-    assert abs(F.io.read_vtu(cb2.files[-1])["Time"][0] - tf) == 0.0
+    assert abs(F.io.read_vtkhdf(cb2.files[-1])["FieldData"]["Time"][0] - tf) == 0.0
 
 
 @pytest.mark.parametrize("basis", ["GLL", "GL"])

@@ -49,5 +49,5 @@ def test_example_2d_linear_advection(tmp_path):
     m = F.ORK256()
     ref = oracle_for(dg).lsrk2n(Q, dt, int(round(tf / dt)), m.A, m.B, m.c)
     assert rel_linf(sol.u[-1], ref) <= 1e-10
-    assert [os.path.basename(f) for f in sb.files] == ["solution_%010d.vtu" % i for i in (0, 50, 100)]
-    assert abs(F.io.read_vtu(sb.files[-1])["Time"][0] - tf) < 1e-15
+    assert [os.path.basename(f) for f in sb.files] == ["solution_%010d.hdf" % i for i in (0, 50, 100)]
+    assert abs(F.io.read_vtkhdf(sb.files[-1])["FieldData"]["Time"][0] - tf) < 1e-15

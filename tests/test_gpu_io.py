@@ -23,6 +23,10 @@ def test_device_snapshot_and_restart(tmp_path):
     vd, vh = fio.read_vtu(str(tmp_path / "d.vtu")), fio.read_vtu(str(tmp_path / "h.vtu"))
     for name in fio.variablenames(eq):
         assert np.allclose(vd[name], vh[name], rtol=1e-13, atol=1e-14)
+    fio.write_vtkhdf(str(tmp_path / "d.hdf"), disc, Qd, time=3e-3)
+    hd = fio.read_vtkhdf(str(tmp_path / "d.hdf"))
+    for name in fio.variablenames(eq):
+        assert np.allclose(hd["PointData"][name], vh[name], rtol=1e-13, atol=1e-14)
     fio.save_restart(str(tmp_path / "r.bin"), disc, Qd, time=3e-3, iteration=3)
     R, t, it = fio.load_restart(str(tmp_path / "r.bin"), disc)
     assert np.array_equal(R, Qh) and it == 3
