@@ -35,6 +35,7 @@
 namespace flou {
 
 struct AdjFaceParams {
+    int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
     const double* U;        // state the residual is linearised at
     const double* Ain;      // adjoint input; λ = s_lam * Ain
     double s_lam;
@@ -54,6 +55,7 @@ struct AdjFaceParams {
 };
 
 struct AdjElemParams {
+    int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
     const double* U;
     const double* Ain;
     double* Aout;           // alpha Ain + beta B + VJP
@@ -97,15 +99,18 @@ __device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv
     qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1] * v[d]);
 }
 
+// Primitive quantities of one node with the reciprocals the VJPs reuse (1/ρ, 1/a), from the
+// refined hardware reciprocals (within 1 ulp of the correctly rounded values).
 struct Prim {
-    double rho, v[3], vv, p, H, a;
+    double rho, v[3], vv, p, H, a, ir, ia;
 };
 
 template <int DIM, bool SOUND = true>
 __device__ __forceinline__ Prim prim_of(const double* q, double g) {
     Prim P;
     P.rho = q[0];
-    double ir = 1.0 / q[0], ke = 0.0, vv = 0.0;
+    double ir = rcp_refined(q[0]), ke = 0.0, vv = 0.0;
+    P.ir = ir;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
         P.v[k] = q[1 + k] * ir;
@@ -115,7 +120,13 @@ __device__ __forceinline__ Prim prim_of(const double* q, double g) {
     P.vv = vv;
     P.p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
     P.H = (q[DIM + 1] + P.p) * ir;
-    P.a = SOUND ? sqrt(g * P.p * ir) : 0.0;
+    if (SOUND) {
+        const double a2 = g * P.p * ir;
+        P.ia = rsqrt_refined(a2);
+        P.a = a2 * P.ia;
+    } else {
+        P.a = P.ia = 0.0;
+    }
     return P;
 }
 
@@ -123,8 +134,8 @@ __device__ __forceinline__ Prim prim_of(const double* q, double g) {
 template <int DIM>
 __device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa, double* qb) {
     double sg = signbit(P.v[0]) ? -1.0 : 1.0;
-    double ir = 1.0 / P.rho;
-    double ca = g * (g - 1.0) / (2.0 * P.a * P.rho);   // ∂a/∂p · ∂p/∂E
+    double ir = P.ir;
+    double ca = (0.5 * g * (g - 1.0)) * (P.ia * ir);   // ∂a/∂p · ∂p/∂E
     qb[0] += kappa * (-sg * P.v[0] * ir + ca * 0.5 * P.vv - P.a * 0.5 * ir);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) qb[1 + k] += kappa * ((k == 0 ? sg * ir : 0.0) - ca * P.v[k]);
@@ -180,7 +191,7 @@ __device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, 
                                                  const double* vh2, double bh2, double vq2, double cb,
                                                  const double* Fb, PrimBar& o1, PrimBar& o2) {
     double hsr = rh1 + rh2, hdr = rh1 - rh2, hsb = bh1 + bh2, hdb = bh1 - bh2;
-    double R = 1.0 / (hsr * hsb);
+    double R = rcp_refined(hsr * hsb);
     double rs = hsb * R, rb = hsr * R;   // 1/hsr, 1/hsb
     double rho, irho, dra, drb, beta, ibeta, dba, dbb;
     logmean_half(rh1, rh2, hsr, hdr, rs, rho, irho, dra, drb);
@@ -230,7 +241,7 @@ __device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, 
 template <int DIM>
 __device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, double vv, double p, double g1,
                                                  const PrimBar& o, double* qb) {
-    double ip = 1.0 / p, ir = 1.0 / rho;
+    double ip = rcp_refined(p), ir = rcp_refined(rho);
     double rb = fma(0.5 * ip, o.b, o.r);
     double pb = -o.b * (0.5 * rho * ip) * ip * g1;   // (γ-1) p̄
     double vvb = 0.0;
@@ -243,8 +254,190 @@ __device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, do
     qb[DIM + 1] += pb;
 }
 
-template <int DIM, bool CHANDRA>
+// Cotangents of one side's primitive quantities in the face frame (normal velocity u, tangential
+// velocities, pressure, sound speed), mapped to its conserved variables and added to qb:
+//   p̄' = p̄ + ā γ/(2aρ)   (a = sqrt(γp/ρ)),
+//   q̄_ρ += -ā a/(2ρ) - (ū u + Σ v̄_t v_t)/ρ + (γ-1)|v|²/2 p̄',
+//   q̄_m1 += ū/ρ - (γ-1) u p̄',  q̄_mt += v̄_t/ρ - (γ-1) v_t p̄',  q̄_E += (γ-1) p̄'.
+struct SideBar {
+    double u, vt[2], p, a;
+};
+
+template <int DIM>
+__device__ __forceinline__ void side_prim_vjp(const Prim& P, double g, const SideBar& b, double* qb) {
+    const double g1 = g - 1.0, ir = P.ir;
+    const double pb = fma(b.a * g, 0.5 * ir * P.ia, b.p);
+    double vdot = b.u * P.v[0];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vdot = fma(b.vt[k - 1], P.v[k], vdot);
+    qb[0] += fma(0.5 * g1 * P.vv, pb, -(fma(b.a, 0.5 * P.a, vdot)) * ir);
+    qb[1] += fma(b.u, ir, -g1 * P.v[0] * pb);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) qb[1 + k] += fma(b.vt[k - 1], ir, -g1 * P.v[k] * pb);
+    qb[DIM + 1] += g1 * pb;
+}
+
+// VJP of the physical normal flux F = [m1, m1 u + p, m_t u, (E + p) u] (face frame) with the
+// cotangent gb scaled by sc: the conserved variables it reads directly go to qb, u and p to b.
+template <int DIM>
+__device__ __forceinline__ void normal_flux_vjp(const double* q, const Prim& P, const double* gb, double sc,
+                                                double* qb, SideBar& b) {
+    const double u = P.v[0];
+    double ub = gb[1] * q[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        ub = fma(gb[1 + k], q[1 + k], ub);
+        qb[1 + k] += sc * gb[1 + k] * u;
+    }
+    ub = fma(gb[DIM + 1], q[DIM + 1] + P.p, ub);
+    qb[1] += sc * fma(gb[1], u, gb[0]);
+    qb[DIM + 1] += sc * gb[DIM + 1] * u;
+    b.u += sc * ub;
+    b.p += sc * fma(gb[DIM + 1], u, gb[1]);
+}
+
+// VJP of the HLL (hllc = false) and HLLC interface fluxes in the face frame (no counterpart in
+// Flou; Toro 2009, eqs. 10.21 and 10.37-10.39 with the Davis wave speeds S_L = min(u_L - a_L,
+// u_R - a_R), S_R = max(u_L + a_L, u_R + a_R)).  a, b: the two states; fb: the flux cotangent;
+// qa, qb: the states' cotangents (accumulated).  Branches and ties as the oracle's dual numbers
+// take them: min(x, y) is y only when y < x, max(x, y) is x only when y < x, the supersonic
+// cases when S_L >= 0 or S_R <= 0, the left star state when S* >= 0.
+template <int DIM>
+__device__ __forceinline__ void hll_family_vjp(bool hllc, const double* a, const double* b, const Prim& pa,
+                                               const Prim& pb, double g, const double* fb, double* qa,
+                                               double* qb) {
+    constexpr int NV = DIM + 2;
+    SideBar L = {}, R = {};
+    const double ul = pa.v[0], ur = pb.v[0];
+    const double sl1 = ul - pa.a, sl2 = ur - pb.a, sr1 = ul + pa.a, sr2 = ur + pb.a;
+    const bool slR = sl2 < sl1, srL = sr2 < sr1;
+    const double sl = slR ? sl2 : sl1, sr = srL ? sr1 : sr2;
+    double slb = 0.0, srb = 0.0;
+    if (sl >= 0.0) {
+        normal_flux_vjp<DIM>(a, pa, fb, 1.0, qa, L);
+    } else if (sr <= 0.0) {
+        normal_flux_vjp<DIM>(b, pb, fb, 1.0, qb, R);
+    } else if (!hllc) {
+        double Fl[NV], Fr[NV];
+        euler_normal_flux<DIM>(a, ul, pa.p, Fl);
+        euler_normal_flux<DIM>(b, ur, pb.p, Fr);
+        const double r = rcp_refined(sr - sl), slr = sl * sr * r;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double dq = b[k] - a[k];
+            const double F = (sr * Fl[k] - sl * Fr[k] + sl * sr * dq) * r;
+            srb = fma(fb[k], (Fl[k] + sl * dq - F) * r, srb);
+            slb = fma(fb[k], (F - Fr[k] + sr * dq) * r, slb);
+            qb[k] += fb[k] * slr;
+            qa[k] -= fb[k] * slr;
+        }
+        normal_flux_vjp<DIM>(a, pa, fb, sr * r, qa, L);
+        normal_flux_vjp<DIM>(b, pb, fb, -sl * r, qb, R);
+    } else {
+        const double rl = pa.rho, rr = pb.rho;
+        const double ml = rl * (sl - ul), mr = rr * (sr - ur);
+        const double Dm = ml - mr;
+        const double iDm = rcp_refined(Dm);
+        const double ss = ((pb.p - pa.p) + ul * ml - ur * mr) * iDm;
+        const bool left = ss >= 0.0;
+        // the star side K, selected per component (no local memory); its cotangents are formed in
+        // qkb / K and added to the side they belong to below
+        double qk[NV], qkb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qk[k] = left ? a[k] : b[k];
+            qkb[k] = 0.0;
+        }
+        Prim pk;
+        pk.rho = left ? pa.rho : pb.rho;
+        pk.p = left ? pa.p : pb.p;
+        pk.ir = left ? pa.ir : pb.ir;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) pk.v[k] = left ? pa.v[k] : pb.v[k];
+        SideBar K = {};
+        const double sk = left ? sl : sr, mk = left ? ml : mr, uk = pk.v[0];
+        const double isk = rcp_refined(sk - ss), coef = mk * isk, irk = pk.ir, imk = rcp_refined(mk);
+        const double X = fma(ss - uk, ss + pk.p * imk, qk[DIM + 1] * irk);
+        double Us[NV];
+        Us[0] = coef;
+        Us[1] = coef * ss;
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) Us[1 + k] = coef * pk.v[k];
+        Us[DIM + 1] = coef * X;
+        double skb = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            skb = fma(fb[k], Us[k] - qk[k], skb);
+            qkb[k] -= sk * fb[k];
+        }
+        normal_flux_vjp<DIM>(qk, pk, fb, 1.0, qkb, K);
+        // Us̄ = sk fb
+        double coefb = sk * fma(fb[1], ss, fma(fb[DIM + 1], X, fb[0]));
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) {
+            coefb = fma(sk * fb[1 + k], pk.v[k], coefb);
+            K.vt[k - 1] += sk * fb[1 + k] * coef;
+        }
+        const double Xb = sk * fb[DIM + 1] * coef;
+        double ssb = sk * fb[1] * coef + Xb * ((ss + pk.p * imk) + (ss - uk));
+        qkb[DIM + 1] += Xb * irk;
+        qkb[0] -= Xb * qk[DIM + 1] * irk * irk;
+        K.u -= Xb * (ss + pk.p * imk);
+        K.p += Xb * (ss - uk) * imk;
+        double mkb = -Xb * (ss - uk) * pk.p * imk * imk;
+        // coef = mk / (sk - ss)
+        mkb = fma(coefb, isk, mkb);
+        skb -= coefb * coef * isk;
+        ssb = fma(coefb * coef, isk, ssb);
+        // ss = N / Dm, N = (pr - pl) + ul ml - ur mr, Dm = ml - mr
+        const double Nb = ssb * iDm, Dmb = -ssb * ss * iDm;
+        // the star side's own cotangents go to the side it is
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qa[k] += left ? qkb[k] : 0.0;
+            qb[k] += left ? 0.0 : qkb[k];
+        }
+        L.u += left ? K.u : 0.0;
+        R.u += left ? 0.0 : K.u;
+        L.p += left ? K.p : 0.0;
+        R.p += left ? 0.0 : K.p;
+#pragma unroll
+        for (int k = 0; k < DIM - 1; ++k) {
+            L.vt[k] += left ? K.vt[k] : 0.0;
+            R.vt[k] += left ? 0.0 : K.vt[k];
+        }
+        R.p += Nb;
+        L.p -= Nb;
+        L.u += Nb * ml;
+        R.u -= Nb * mr;
+        double mlb = fma(Nb, ul, Dmb), mrb = -fma(Nb, ur, Dmb);
+        if (left) mlb += mkb;
+        else mrb += mkb;
+        if (left) slb += skb;
+        else srb += skb;
+        // ml = ρl (sl - ul), mr = ρr (sr - ur)
+        qa[0] += mlb * (sl - ul);
+        slb = fma(mlb, rl, slb);
+        L.u -= mlb * rl;
+        qb[0] += mrb * (sr - ur);
+        srb = fma(mrb, rr, srb);
+        R.u -= mrb * rr;
+    }
+    // S_L = min(u_L - a_L, u_R - a_R), S_R = max(u_L + a_L, u_R + a_R)
+    const double slbL = slR ? 0.0 : slb, slbR = slR ? slb : 0.0;
+    const double srbL = srL ? srb : 0.0, srbR = srL ? 0.0 : srb;
+    L.u += slbL + srbL;
+    L.a += srbL - slbL;
+    R.u += slbR + srbR;
+    R.a += srbR - slbR;
+    side_prim_vjp<DIM>(pa, g, L, qa);
+    side_prim_vjp<DIM>(pb, g, R, qb);
+}
+
+// KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC.
+template <int DIM, int KIND>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
+    constexpr bool CHANDRA = KIND == 1;
     constexpr int NV = DIM + 2;
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
@@ -260,6 +453,10 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     };
     int64_t g1i, g2i = 0;
     double dg1, dg2 = 0.0;
+    if (kChecked && !(index_ok(s0 >> 3, P.ndofs / P.npe, P.status, 0) &&
+                      (s1 < 0 || index_ok(s1 >> 3, P.ndofs / P.npe, P.status, s0 >> 3)) &&
+                      (s1 >= 0 || index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3))))
+        return;
     endnode(s0, &g1i, &dg1);
     double qL[NV], qR[NV], Fb[NV];
     double w1 = P.invJ[s0 >> 3] * P.s_lam;
@@ -285,17 +482,18 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     a[DIM + 1] = qL[DIM + 1];
     fb[0] = J * Fb[0];
     fb[DIM + 1] = J * Fb[DIM + 1];
+    cart_to_face<DIM>(qL, A, a);
+    {
+        double t[NV];
+        cart_to_face<DIM>(Fb, A, t);
 #pragma unroll
-    for (int r = 0; r < DIM; ++r) {
-        a[1 + r] = flip(qL[1 + A.ax[r]], A.neg[r]);
-        fb[1 + r] = J * flip(Fb[1 + A.ax[r]], A.neg[r]);
+        for (int r = 0; r < DIM; ++r) fb[1 + r] = J * t[1 + r];
     }
     int bck = 0;
     if (s1 >= 0) {
         b[0] = qR[0];
         b[DIM + 1] = qR[DIM + 1];
-#pragma unroll
-        for (int r = 0; r < DIM; ++r) b[1 + r] = flip(qR[1 + A.ax[r]], A.neg[r]);
+        cart_to_face<DIM>(qR, A, b);
     } else {
         bck = P.bc_kind[P.face_bc[f]];
 #pragma unroll
@@ -311,14 +509,20 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     Prim pa = prim_of<DIM>(a, g);
     const double* bb = b;
     Prim pb = prim_of<DIM>(bb, g);
+    double ab[NV], bbar[NV];
+    double Ib = 0.0;
+    if (KIND >= 2) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
+#pragma unroll
+        for (int k = 0; k < NV; ++k) ab[k] = bbar[k] = 0.0;
+        hll_family_vjp<DIM>(KIND == 3, a, bb, pa, pb, g, fb, ab, bbar);
+    } else {
     double ll = fabs(pa.v[0]) + pa.a, lr = fabs(pb.v[0]) + pb.a;
     bool left = lr < ll;   // Base.max(ll, lr)
     double lam = left ? ll : lr;
     double dot = 0.0;
 #pragma unroll
     for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
-    double Ib = 0.5 * lam * dot;
-    double ab[NV], bbar[NV];
+    Ib = 0.5 * lam * dot;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         ab[k] = 0.5 * inten * lam * fb[k];
@@ -332,8 +536,9 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
             vh1[k] = 0.5 * pa.v[k];
             vh2[k] = 0.5 * pb.v[k];
         }
-        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho / pa.p, 0.25 * pa.vv, 0.5 * pb.rho, vh2,
-                                       0.25 * pb.rho / pb.p, 0.25 * pb.vv, 0.5 / g1, fb, o1, o2);
+        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho * rcp_refined(pa.p), 0.25 * pa.vv,
+                                       0.5 * pb.rho, vh2, 0.25 * pb.rho * rcp_refined(pb.p), 0.25 * pb.vv,
+                                       0.5 / g1, fb, o1, o2);
         prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
         prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
     } else {
@@ -343,10 +548,13 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     double kappa = 0.5 * inten * dot;
     if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
     else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    }
     if (s1 < 0) {
         if (bck == FLOU_BC_OUTFLOW) {
+#pragma unroll
             for (int k = 0; k < NV; ++k) ab[k] += bbar[k];
         } else if (bck == FLOU_BC_SLIP) {
+#pragma unroll
             for (int k = 0; k < NV; ++k) ab[k] += (k == 1) ? -bbar[k] : bbar[k];
         }
     }
@@ -356,11 +564,8 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     oL[DIM + 1] = ab[DIM + 1];
     oR[0] = bbar[0];
     oR[DIM + 1] = bbar[DIM + 1];
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) {
-        oL[1 + A.ax[r]] = flip(ab[1 + r], A.neg[r]);
-        oR[1 + A.ax[r]] = flip(bbar[1 + r], A.neg[r]);
-    }
+    cart_to_phys<DIM>(ab, A, oL);
+    cart_to_phys<DIM>(bbar, A, oR);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         P.QbL[k * P.nfdofs + gid] = oL[k];
@@ -423,6 +628,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
             int32_t pk = P.elem_face[e * 2 * DIM + 2 * d + (pos == 0 ? 0 : 1)];
             const double* src = (pk & 1) ? P.QbR : P.QbL;
             int64_t o = (int64_t)(pk >> 1) * NFD + line;
+            if (!index_ok(o, P.nfdofs, P.status, e)) continue;
 #pragma unroll
             for (int k = 0; k < NV; ++k) qb[k] += __ldcg(src + k * P.nfdofs + o);
         }
@@ -443,6 +649,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
         for (int fk = 0; fk < 2 * DIM; ++fk) {
             int32_t pk = P.elem_face[e * 2 * DIM + fk];
             int fc = pk >> 1;
+            if (!index_ok((int64_t)fc * NFD + NFD - 1, P.nfdofs, P.status, e)) continue;
             double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
             for (int m = 0; m < NFD; ++m) acc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + m), acc);
         }
@@ -562,13 +769,15 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         double vv = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
-        double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) / rho;
+        double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) * rcp_refined(rho);
         euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
     }
     int pbase = el * NFD * NPAIR + line * NPAIR;
+    // the N-1 partners of pos, cyclically from pos + 1: every iteration is a pair (a skipped
+    // j == pos would still take its FP64 issue slots as predicated-off instructions)
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-        if (j == pos) continue;
+    for (int t = 1; t < N; ++t) {
+        const int j = pos + t < N ? pos + t : pos + t - N;
         int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
         int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
         const double* src = spb + (pos == lo ? 0 : NPB * NPT);
@@ -581,8 +790,10 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         int32_t pk = P.elem_face[e * 2 * DIM + 2 * D + (pos == 0 ? 0 : 1)];
         const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
         int64_t o = (int64_t)(pk >> 1) * NFD + line;
+        if (index_ok(o, P.nfdofs, P.status, e)) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
+            for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
+        }
     }
 }
 
@@ -629,7 +840,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
             q[k] = P.U[k * P.ndofs + gi];
         }
         rho = q[0];
-        double ir = 1.0 / rho, ke = 0.0, vv = 0.0;
+        double ir = rcp_refined(rho), ke = 0.0, vv = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) {
             v[k] = q[1 + k] * ir;
@@ -640,7 +851,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
         sprim[tid] = 0.5 * rho;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
-        sprim[(1 + DIM) * NN + tid] = (0.25 * rho) / p;
+        sprim[(1 + DIM) * NN + tid] = (0.25 * rho) * rcp_refined(p);
         sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
     } else {
 #pragma unroll
@@ -692,6 +903,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
         for (int fk = 0; fk < 2 * DIM; ++fk) {
             int32_t pk = P.elem_face[e * 2 * DIM + fk];
             int fc = pk >> 1;
+            if (!index_ok((int64_t)fc * S::NFD + S::NFD - 1, P.nfdofs, P.status, e)) continue;
             double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
             for (int m = 0; m < S::NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * S::NFD + m), cacc);
         }
@@ -766,12 +978,13 @@ int adj_supported(flou_ctx* c) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                (k.volume_op == FLOU_OP_SPLIT && k.twopoint_flux == FLOU_TP_CHANDRASHEKAR);
-    bool nf = k.numflux == FLOU_NF_LXF &&
-              (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR);
+    bool nf = (k.numflux == FLOU_NF_LXF &&
+               (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR)) ||
+              k.numflux == FLOU_NF_HLL || k.numflux == FLOU_NF_HLLC;
     if (k.equation != FLOU_EQ_EULER || !vol || !nf)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
-                                                 "the Chandrashekar split form, and the LxF(StdAverage) or "
-                                                 "LxF(ChandrasekharAverage) flux");
+                                                 "the Chandrashekar split form, and the LxF(StdAverage), "
+                                                 "LxF(ChandrasekharAverage), HLL or HLLC interface flux");
     if (!c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
     if (c->limiter)
@@ -810,6 +1023,7 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
               double gamma_B, double delta_B) {
     AdjFaceParams F;
     memset(&F, 0, sizeof(F));
+    F.status = c->d_status;
     F.U = U;
     F.Ain = Ain;
     F.s_lam = s_lam;
@@ -832,16 +1046,30 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     F.nfd = c->nfd;
     for (int b = 0; b < MAXBC; ++b) F.bc_kind[b] = c->bc_kind[b];
     int64_t nth = (int64_t)c->nfaces * c->nfd;
-    int grid = (int)((nth + 255) / 256);
+    const int tb = face_block_size(nth);
+    int grid = (int)((nth + tb - 1) / tb);
     int dim = c->cfg.dim;
-    bool ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR;
-    if (dim == 1) ch ? adj_face_kernel<1, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<1, false><<<grid, 256, 0, s>>>(F);
-    else if (dim == 2) ch ? adj_face_kernel<2, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<2, false><<<grid, 256, 0, s>>>(F);
-    else ch ? adj_face_kernel<3, true><<<grid, 256, 0, s>>>(F) : adj_face_kernel<3, false><<<grid, 256, 0, s>>>(F);
+    const int nf = c->cfg.numflux;
+    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
+    switch (dim * 4 + kind) {
+        case 4: adj_face_kernel<1, 0><<<grid, tb, 0, s>>>(F); break;
+        case 5: adj_face_kernel<1, 1><<<grid, tb, 0, s>>>(F); break;
+        case 6: adj_face_kernel<1, 2><<<grid, tb, 0, s>>>(F); break;
+        case 7: adj_face_kernel<1, 3><<<grid, tb, 0, s>>>(F); break;
+        case 8: adj_face_kernel<2, 0><<<grid, tb, 0, s>>>(F); break;
+        case 9: adj_face_kernel<2, 1><<<grid, tb, 0, s>>>(F); break;
+        case 10: adj_face_kernel<2, 2><<<grid, tb, 0, s>>>(F); break;
+        case 11: adj_face_kernel<2, 3><<<grid, tb, 0, s>>>(F); break;
+        case 12: adj_face_kernel<3, 0><<<grid, tb, 0, s>>>(F); break;
+        case 13: adj_face_kernel<3, 1><<<grid, tb, 0, s>>>(F); break;
+        case 14: adj_face_kernel<3, 2><<<grid, tb, 0, s>>>(F); break;
+        default: adj_face_kernel<3, 3><<<grid, tb, 0, s>>>(F); break;
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
     memset(&P, 0, sizeof(P));
+    P.status = c->d_status;
     P.U = U;
     P.Ain = Ain;
     P.Aout = Aout;

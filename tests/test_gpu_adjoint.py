@@ -32,7 +32,23 @@ def _split(face_avg="chandra"):
     return F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(avg, 1.0))
 
 
-OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("std")}
+# HLL and HLLC carry no dissipation scale: their contexts take no flou_set_dissipation and no dJ/dc
+HLL_FAMILY = ("split_hllc", "strong_hll", "strong_hllc")
+
+
+def _with_c(disc, op, c):
+    """Sets the dissipation scale where the flux has one; returns the scale the oracle is given."""
+    if op in HLL_FAMILY:
+        return np.ones_like(c)
+    disc.ctx.set_dissipation(c)
+    return c
+
+
+OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("std"),
+             # the headline configuration's pair: Chandrashekar split form with the HLLC interface flux
+             "split_hllc": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()),
+             "strong_hll": lambda: F.StrongDivOperator(F.HLL()),
+             "strong_hllc": lambda: F.StrongDivOperator(F.HLLC())}
 
 
 CASES = [
@@ -53,7 +69,7 @@ def _disc(case, op="strong"):
     return d
 
 
-@pytest.mark.parametrize("op", ["strong", "split", "split_stdface"])
+@pytest.mark.parametrize("op", ["strong", "split", "split_stdface", "split_hllc", "strong_hll", "strong_hllc"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
 def test_rhs_vjp_dot_product(case, op):
     disc = _disc(case, op)
@@ -67,11 +83,14 @@ def test_rhs_vjp_dot_product(case, op):
     lam = rng.standard_normal(Q.shape)
     dQ = rng.standard_normal(Q.shape)
     dc = rng.standard_normal(c.shape)
-    disc.ctx.set_dissipation(c)
+    c = _with_c(disc, op, c)
+    hll = op in HLL_FAMILY
+    if hll:
+        dc = 0.0 * dc
     Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
-    cbar = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    cbar = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
     disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
-    lhs = np.sum(_host(Qbar) * dQ) + np.sum(cbar.cpu().numpy() * dc)
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if hll else np.sum(cbar.cpu().numpy() * dc))
     R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
     rhs = np.sum(lam * dR)
     scale = np.sum(np.abs(lam * dR))
@@ -80,6 +99,30 @@ def test_rhs_vjp_dot_product(case, op):
     dQg = disc.new_state()
     disc.ctx.rhs(dQg, Q)
     assert np.max(np.abs(dQg - R)) <= 1e-12 * np.max(np.abs(R))
+
+
+@pytest.mark.parametrize("op", ["strong_hll", "strong_hllc", "split_hllc"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_hll_family_vjp_through_every_branch(dim, op):
+    """HLL and HLLC with a flow that is supersonic in both directions in places (S_L >= 0 and
+    S_R <= 0) and subsonic elsewhere (both signs of the contact speed S*): every branch of the
+    flux is differentiated, against the oracle's dual numbers."""
+    disc = build(dim, 4, (4,) + (2,) * (dim - 1), F.EulerEquation(dim, 1.4), OPERATORS[op]())
+    rng = np.random.default_rng(31 + dim)
+    Q = smooth_euler_state(disc, seed=12)
+    P = disc.equation.vars_cons2prim(Q)
+    P[:, 1] = 2.6 * np.sin(np.pi * disc.coords[:, 0] + 0.4) + 0.1 * P[:, 1]   # |u| up to 2.6 > a ≈ 1.2
+    Q = np.asfortranarray(disc.equation.vars_prim2cons(P))
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = np.ones(disc.mesh.nelements)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    _, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, 0.0 * c)
+    lhs, rhs = np.sum(_host(Qbar) * dQ), np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+    with pytest.raises(F.FlouError):   # HLL/HLLC carry no dissipation scale to differentiate
+        disc.ctx.set_dissipation(c)
 
 
 def _functional_inputs(disc, seed):
@@ -164,7 +207,7 @@ def test_adjoint_against_central_differences():
         assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
 
 
-@pytest.mark.parametrize("op", ["split", "split_stdface"])
+@pytest.mark.parametrize("op", ["split", "split_stdface", "split_hllc"])
 def test_split_rhs_vjp_columns(op):
     """Every column of the transposed Jacobian at once on a small 3D case: (∂R/∂Q)ᵀ λ against
     the dual-number JVPs of all unit directions of one element's nodes."""
@@ -172,11 +215,10 @@ def test_split_rhs_vjp_columns(op):
     disc = _disc(case, op)
     rng = np.random.default_rng(21)
     Q = smooth_euler_state(disc, seed=2, amp=0.3)
-    c = 1.0 + 0.3 * rng.random(disc.mesh.nelements)
-    disc.ctx.set_dissipation(c)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
     lam = rng.standard_normal(Q.shape)
     Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
-    cbar = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    cbar = None if op in HLL_FAMILY else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
     disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
     Qb = _host(Qbar)
     o = oracle_for(disc)
@@ -208,49 +250,51 @@ def _tgv_state(disc, mach, seed):
     return np.asfortranarray(eq.vars_prim2cons(P))
 
 
-@pytest.mark.parametrize("op", ["split", "strong"])
+@pytest.mark.parametrize("op", ["split", "strong", "split_hllc"])
 def test_3d_adjoint_solve_against_dual_numbers(op):
     eq = F.EulerEquation(3, 1.4)
     L = 2 * np.pi
     disc = build(3, 4, (2, 3, 2), eq, OPERATORS[op](), box=((0.0,) * 3, (L,) * 3))
     Q0 = _tgv_state(disc, 0.3, 0)
     rng = np.random.default_rng(13)
-    c = 1.0 + 0.2 * rng.random(disc.mesh.nelements)
-    disc.ctx.set_dissipation(c)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
     rho_t, w = _functional_inputs(disc, 5)
     dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
     nsteps = 10
     g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
-    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
     J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
     o = oracle_for(disc)
     for k in range(3):
         dQ = rng.standard_normal(Q0.shape)
-        dc = rng.standard_normal(c.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
         Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
         assert abs(J - Jo) <= 1e-12 * abs(Jo)
-        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
-def test_split_adjoint_against_central_differences():
+@pytest.mark.parametrize("op", ["split", "split_hllc"])
+def test_split_adjoint_against_central_differences(op):
     eq = F.EulerEquation(3, 1.4)
     L = 2 * np.pi
-    disc = build(3, 5, (3, 3, 3), eq, _split(), box=((0.0,) * 3, (L,) * 3))
+    disc = build(3, 5, (3, 3, 3), eq, OPERATORS[op](), box=((0.0,) * 3, (L,) * 3))
     Q0 = _tgv_state(disc, 0.2, 1)
     rng = np.random.default_rng(17)
-    c = 1.0 + 0.1 * rng.random(disc.mesh.nelements)
-    disc.ctx.set_dissipation(c)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.1 * rng.random(disc.mesh.nelements))
     rho_t, w = _functional_inputs(disc, 8)
     dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
     nsteps = 12
     g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
-    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
     disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 4, _dev(rho_t), _dev(w), g, gc)
     wd, rtd = _dev(w), _dev(rho_t)
 
     def Jof(Q, cc):
-        disc.ctx.set_dissipation(cc)
+        if not hll:
+            disc.ctx.set_dissipation(cc)
         q = _dev(Q)
         disc.ctx.step(q, dt, nsteps)
         r = q[0] - rtd
@@ -259,7 +303,7 @@ def test_split_adjoint_against_central_differences():
     h = 1e-6
     for k in range(3):
         dQ = rng.standard_normal(Q0.shape)
-        dc = rng.standard_normal(c.shape) * 0.1
+        dc = rng.standard_normal(c.shape) * (0.0 if hll else 0.1)
         fd = (Jof(Q0 + h * dQ, c + h * dc) - Jof(Q0 - h * dQ, c - h * dc)) / (2 * h)
-        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
         assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
