@@ -2,6 +2,9 @@
 
 Each translation unit under csrc/ is compiled by its own nvcc process (in parallel), then
 linked into lib/libflou_cuda.so.  Sources are recompiled only when they or a header changed.
+`build(checked=True)` (or `python build.py --checked`) builds lib/libflou_cuda_checked.so with
+-DFLOU_CUDA_CHECKED: every kernel checks its computed indices against the array sizes and
+reports an out-of-range one through the status word (FLOU_ERR_INDEX) instead of accessing it.
 """
 import concurrent.futures
 import glob
@@ -34,8 +37,8 @@ def _newest_header():
     return max(os.path.getmtime(h) for h in hs)
 
 
-def _compile(src, extra):
-    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+def _compile(src, extra, objdir=OBJ):
+    obj = os.path.join(objdir, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _newest_header()):
         return obj, None
     cmd = [nvcc()] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
@@ -45,26 +48,30 @@ def _compile(src, extra):
     return obj, None
 
 
-def build(verbose=False, extra=()):
-    os.makedirs(OBJ, exist_ok=True)
+def build(verbose=False, extra=(), checked=False):
+    objdir = os.path.join(OBJ, "checked") if checked else OBJ
+    lib = os.path.join(LIBDIR, "libflou_cuda_checked.so") if checked else LIB
+    extra = list(extra) + (["-DFLOU_CUDA_CHECKED"] if checked else [])
+    os.makedirs(objdir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     workers = min(len(srcs), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(workers) as ex:
-        results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+        results = list(ex.map(lambda s: _compile(s, extra, objdir), srcs))
     errs = [e for _, e in results if e]
     if errs:
         raise RuntimeError("\n".join(errs))
     objs = [o for o, _ in results]
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), p.stdout, p.stderr))
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, extra=sys.argv[1:])
+    args = [a for a in sys.argv[1:] if a != "--checked"]
+    build(verbose=True, extra=args, checked="--checked" in sys.argv[1:])

@@ -31,6 +31,7 @@ struct BatchArgs {
     const int32_t* nface_items;  // face items per instance
     const int2* items;           // (instance | kind << 30, first face node or element)
     int32_t nitems;
+    int32_t ninst;
     int32_t* counter;            // [0] queue head, [1] abort flag, [2 + k] face items done of instance k
     int32_t* status;             // bit 0 non-physical, bit 1 wait timed out
     int32_t skip_done_inst;      // fault-injection hook: this instance never reports its faces (-1: none)
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(TB, (TB >= 512 ? 1 : 1024 / TB)) batch_stage_k
         if (it >= A.nitems) break;
         const int2 w = A.items[it];
         const int inst = w.x & 0x3fffffff;
+        if (!index_ok(inst, A.ninst, A.status, 0)) continue;
         if ((w.x >> 30) == 0) {
             const FaceParams& fp = A.fp[inst];
             const int64_t gid = (int64_t)w.y + threadIdx.x;
@@ -246,7 +248,10 @@ int upload_params(flou_batch* b) {
         ep[k] = ctx_elem_params(c, Q, Q, U, 1, dt, 0.0, 1.0);
         ep[b->n + k] = ctx_elem_params(c, U, Q, U, 2, dt, 0.75, 0.25);
         ep[2 * b->n + k] = ctx_elem_params(c, U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0);
-        for (int s = 0; s < 3; ++s) ep[s * b->n + k].status = b->d_status;
+        for (int s = 0; s < 3; ++s) {
+            ep[s * b->n + k].status = b->d_status;
+            fp[s * b->n + k].status = b->d_status;
+        }
     }
     BCK(cudaMemcpy(b->d_fp, fp.data(), fp.size() * sizeof(FaceParams), cudaMemcpyHostToDevice), "stage parameters");
     BCK(cudaMemcpy(b->d_ep, ep.data(), ep.size() * sizeof(ElemParams), cudaMemcpyHostToDevice), "stage parameters");
@@ -275,6 +280,7 @@ int launch_stage(flou_batch* b, int s, cudaStream_t st) {
     A.nface_items = b->d_meta + 2 * b->n;
     A.items = b->d_items;
     A.nitems = b->nitems;
+    A.ninst = b->n;
     A.counter = b->d_counter;
     A.status = b->d_status;
     A.skip_done_inst = b->skip_done_inst;
@@ -290,6 +296,9 @@ int check_status(flou_batch* b) {
     if (st[0]) {
         int32_t init[2] = {0, 0x7fffffff};
         cudaMemcpy(b->d_status, init, sizeof(init), cudaMemcpyHostToDevice);
+        if (st[0] & 4)
+            return bfail(b, FLOU_ERR_INDEX, "a device index check failed (element " + std::to_string(st[1]) +
+                                                " of an instance; FLOU_CUDA_CHECKED build)");
         if (st[0] & 2) return bfail(b, FLOU_ERR_TIMEOUT, "a batched element tile waited too long for its face fluxes");
         return bfail(b, FLOU_ERR_NONPHYSICAL, "non-physical or non-finite state in element " + std::to_string(st[1]) +
                                                   " of an instance");

@@ -5,9 +5,10 @@ template <int DIM, int EQ>
 static cudaError_t launch_face_t(bool lgl, const FaceParams& P, cudaStream_t s) {
     int64_t nthreads = (int64_t)P.nfaces * P.nfd;
     if (nthreads == 0) return cudaSuccess;
-    int grid = (int)((nthreads + 255) / 256);
-    if (lgl) face_kernel<DIM, EQ, true><<<grid, 256, 0, s>>>(P);
-    else face_kernel<DIM, EQ, false><<<grid, 256, 0, s>>>(P);
+    const int tb = face_block_size(nthreads);
+    int grid = (int)((nthreads + tb - 1) / tb);
+    if (lgl) face_kernel<DIM, EQ, true><<<grid, tb, 0, s>>>(P);
+    else face_kernel<DIM, EQ, false><<<grid, tb, 0, s>>>(P);
     return cudaGetLastError();
 }
 cudaError_t launch_face(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s) {
@@ -26,9 +27,10 @@ template <int DIM, int EQ>
 static cudaError_t launch_face_curv_t(bool lgl, const FaceParams& P, cudaStream_t s) {
     int64_t nthreads = (int64_t)P.nfaces * P.nfd;
     if (nthreads == 0) return cudaSuccess;
-    int grid = (int)((nthreads + 255) / 256);
-    if (lgl) face_kernel<DIM, EQ, true, true><<<grid, 256, 0, s>>>(P);
-    else face_kernel<DIM, EQ, false, true><<<grid, 256, 0, s>>>(P);
+    const int tb = face_block_size(nthreads);
+    int grid = (int)((nthreads + tb - 1) / tb);
+    if (lgl) face_kernel<DIM, EQ, true, true><<<grid, tb, 0, s>>>(P);
+    else face_kernel<DIM, EQ, false, true><<<grid, tb, 0, s>>>(P);
     return cudaGetLastError();
 }
 cudaError_t launch_face_curv(int dim, int eq, bool lgl, const FaceParams& P, cudaStream_t s) {

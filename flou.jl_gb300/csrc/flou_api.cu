@@ -116,6 +116,7 @@ FaceParams face_params(const flou_ctx* c, const double* Q) {
     P.frames = c->d_frames;
     P.faceJn = c->d_faceJn;
     P.orient = c->d_orient;
+    P.status = c->d_status;
     P.numflux = c->cfg.numflux;
     P.lxf_avg = c->cfg.numflux_avg;
     P.intensity = c->cfg.numflux_intensity;
@@ -237,6 +238,8 @@ int check_status(flou_ctx* c) {
     if (st[0]) {
         int32_t init[2] = {0, 0x7fffffff};
         cudaMemcpy(c->d_status, init, sizeof(init), cudaMemcpyHostToDevice);
+        if (st[0] & 4)
+            return fail(c, FLOU_ERR_INDEX, "a device index check failed (element %d; FLOU_CUDA_CHECKED build)", st[1]);
         return fail(c, FLOU_ERR_NONPHYSICAL, "non-physical or non-finite state in element %d", st[1]);
     }
     return FLOU_OK;

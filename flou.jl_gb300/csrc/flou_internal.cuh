@@ -23,6 +23,25 @@ constexpr int MAXBC = 8;         // boundary conditions per context
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
 
+// Threads per block of the one-thread-per-face-node kernels: 256, halved (down to 32) while the
+// grid would give fewer than 8 blocks per SM.  On small meshes (tens of thousands of face nodes)
+// 256-thread blocks leave most SMs with one block and a few with two, and the kernel lasts two
+// block times; smaller blocks spread the same work evenly.  The SM count is queried once per
+// device (host code; no stream operation, so it is safe during stream capture after the first call).
+inline int face_block_size(int64_t nthreads) {
+    static int sms_of[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    int sms = __atomic_load_n(&sms_of[dev], __ATOMIC_RELAXED);
+    if (sms <= 0) {
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+        __atomic_store_n(&sms_of[dev], sms, __ATOMIC_RELAXED);
+    }
+    int tb = 256;
+    while (tb > 32 && nthreads < (int64_t)8 * sms * tb) tb >>= 1;
+    return tb;
+}
+
 // ---------------------------------------------------------------------------------------
 // Launch parameters (passed by value)
 // ---------------------------------------------------------------------------------------
@@ -46,6 +65,7 @@ struct FaceParams {
     const double* frames;        // [9][nfdofs]: n, t, b of every face node (master ordering)
     const double* faceJn;        // [nfdofs] surface Jacobian of every face node
     const uint8_t* orient;       // [nfaces] master2slave orientation
+    int32_t* status;             // index-check reports (FLOU_CUDA_CHECKED builds)
 };
 
 struct ElemParams {
@@ -109,6 +129,25 @@ __host__ __device__ __forceinline__ int inverse_orientation(int o) {
 // Local face positions follow the reference's face order: 2*dir (left) and 2*dir+1
 // (right); frames of a face are those of its master position (PhysicalRegions.jl:541-696).
 struct FrameTab { double n[3], t[3], b[3]; };
+
+// Device-side index checks, compiled in with -DFLOU_CUDA_CHECKED (build.py --checked, the
+// library libflou_cuda_checked.so): an index outside its array sets bit 2 of the status word
+// (FLOU_ERR_INDEX on the host, with the lowest element involved) and the access is skipped.
+// Nothing traps.  In the default build the checks compile to nothing.
+#ifdef FLOU_CUDA_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
+
+__device__ __forceinline__ bool index_ok(int64_t i, int64_t n, int32_t* status, int64_t elem) {
+    if (!kChecked || (i >= 0 && i < n)) return true;
+    if (status) {
+        atomicOr(status, 4);
+        atomicMin(status + 1, (int32_t)(elem + 1));
+    }
+    return false;
+}
 
 __host__ __device__ inline FrameTab frame_of(int dim, int pos) {
     FrameTab F = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -211,6 +250,15 @@ __device__ __forceinline__ double sqrt_refined(double x) {
     double s0 = x * y;
     double e = fma(-s0, y, 1.0);
     return fma(s0, e * fma(e, 0.375, 0.5), s0);
+}
+
+// 1/√x for a normal x > 0: rsqrt.approx.ftz.f64 refined by the same third-order step,
+// y (1 + e/2 + 3e²/8) with e = 1 - x y².
+__device__ __forceinline__ double rsqrt_refined(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x * y, y, 1.0);
+    return fma(y, e * fma(e, 0.375, 0.5), y);
 }
 
 // Logarithmic mean (src/FlouCommon/Utilities.jl:34-44) of a, b > 0 in sums and differences, given
@@ -398,30 +446,52 @@ struct FrameAxes { int ax[3]; bool neg[3]; };
 
 template <int DIM>
 __device__ __forceinline__ FrameAxes frame_axes(int pos) {
+    // the table of PhysicalRegions.jl:568-696 in closed form (register arithmetic, no switch):
+    // the normal is axis pos / 2, negative on the lower face; the tangents follow cyclically
+    // (2D: t = ±e_other, negative when the normal is positive along y or negative along x)
     FrameAxes A = {{0, 0, 0}, {false, false, false}};
-    if (DIM == 1) { A.neg[0] = (pos == 0); return A; }
+    const int dir = pos >> 1;
+    const bool lower = (pos & 1) == 0;
+    A.ax[0] = dir;
+    A.neg[0] = lower;
     if (DIM == 2) {
-        switch (pos) {
-            case 0: A.ax[0] = 0; A.neg[0] = true; A.ax[1] = 1; A.neg[1] = true; break;
-            case 1: A.ax[0] = 0; A.ax[1] = 1; break;
-            case 2: A.ax[0] = 1; A.neg[0] = true; A.ax[1] = 0; break;
-            default: A.ax[0] = 1; A.ax[1] = 0; A.neg[1] = true; break;
-        }
-        return A;
-    }
-    switch (pos) {
-        case 0: A.ax[0] = 0; A.neg[0] = true; A.ax[1] = 1; A.neg[1] = true; A.ax[2] = 2; break;
-        case 1: A.ax[0] = 0; A.ax[1] = 1; A.ax[2] = 2; break;
-        case 2: A.ax[0] = 1; A.neg[0] = true; A.ax[1] = 2; A.neg[1] = true; A.ax[2] = 0; break;
-        case 3: A.ax[0] = 1; A.ax[1] = 2; A.ax[2] = 0; break;
-        case 4: A.ax[0] = 2; A.neg[0] = true; A.ax[1] = 0; A.neg[1] = true; A.ax[2] = 1; break;
-        default: A.ax[0] = 2; A.ax[1] = 0; A.ax[2] = 1; break;
+        A.ax[1] = 1 - dir;
+        A.neg[1] = lower != (dir == 1);
+    } else if (DIM == 3) {
+        A.ax[1] = dir == 2 ? 0 : dir + 1;
+        A.ax[2] = dir == 0 ? 2 : dir - 1;
+        A.neg[1] = lower;
     }
     return A;
 }
 
 __device__ __forceinline__ double flip(double x, bool neg) {
     return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+}
+
+// Momentum components of a Cartesian face frame without runtime-indexed register arrays (which
+// the compiler would place in local memory): to_face gives a[1 + r] = ±m[A.ax[r]], to_phys puts
+// ±f[1 + r] back on axis A.ax[r]; the selects and sign flips run on the integer units.
+template <int DIM>
+__device__ __forceinline__ void cart_to_face(const double* q, const FrameAxes& A, double* a) {
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        double m = q[1];
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) m = A.ax[r] == k ? q[1 + k] : m;
+        a[1 + r] = flip(m, A.neg[r]);
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void cart_to_phys(const double* f, const FrameAxes& A, double* q) {
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        double m = 0.0;
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) m = A.ax[r] == k ? flip(f[1 + r], A.neg[r]) : m;
+        q[1 + k] = m;
+    }
 }
 
 // StdAverage / LxF(StdAverage) / HLL / HLLC in the face frame with one reciprocal of the
@@ -468,8 +538,12 @@ __device__ __forceinline__ void euler_face_flux_fast(const double* ql, const dou
     double ml = ql[0] * (sl - ul), mr = qr[0] * (sr - ur);
     double ss = fma(ul, ml, (pr - pl) - ur * mr) * rcp_refined(ml - mr);
     bool left = ss >= 0.0;
-    const double* qk = left ? ql : qr;
-    const double* Fk = left ? Fl : Fr;
+    double qk[NV], Fk[NV];   // the star side's state and flux, selected per component (no local memory)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        qk[k] = left ? ql[k] : qr[k];
+        Fk[k] = left ? Fl[k] : Fr[k];
+    }
     double sk = left ? sl : sr, mk = left ? ml : mr, irk = left ? irl : irr, uk = left ? ul : ur,
            pk = left ? pl : pr;
     double R = rcp_refined((sk - ss) * mk);
@@ -543,14 +617,26 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
     int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
     int n = P.n;
     int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
+    if (kChecked) {
+        const int64_t nel = P.ndofs / P.npe;
+        bool ok = index_ok(s0 >> 3, nel, P.status, 0) && index_ok(s0 & 7, 2 * DIM, P.status, s0 >> 3);
+        if (ok && s1 >= 0)
+            ok = index_ok(s1 >> 3, nel, P.status, s0 >> 3) && index_ok(s1 & 7, 2 * DIM, P.status, s1 >> 3) &&
+                 (!CURV || index_ok(master2slave<DIM>(m, P.orient[f], n), P.nfd, P.status, s1 >> 3));
+        if (ok && s1 < 0) ok = index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3);
+        if (!ok) return;
+    }
     auto trace = [&](int32_t s, int mm, double* q) {
         int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
         const double* Qe = P.Q + (int64_t)e * P.npe;
         if (LGL) {
             int node = tp_node<DIM>(n, dir, mm, right ? n - 1 : 0);
+            if (!index_ok(node, P.npe, P.status, e)) node = 0;
+#pragma unroll
             for (int k = 0; k < NV; ++k) q[k] = Qe[k * P.ndofs + node];
         } else {
             const double* lv = P.l + (right ? n : 0);
+#pragma unroll
             for (int k = 0; k < NV; ++k) {
                 double acc = 0.0;
                 for (int p = 0; p < n; ++p) acc = acc + lv[p] * Qe[k * P.ndofs + tp_node<DIM>(n, dir, mm, p)];
@@ -568,7 +654,7 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
             fr.t[c] = P.frames[(3 + c) * P.nfdofs + gid];
             fr.b[c] = P.frames[(6 + c) * P.nfdofs + gid];
         }
-    } else {
+    } else if (EQ != FLOU_EQ_EULER) {   // the Euler path rotates with frame_axes
         fr = frame_of(DIM, s0 & 7);
     }
     if (s1 >= 0) {
@@ -577,8 +663,10 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         int b = P.face_bc[f];
         int kind = P.bc_kind[b];
         if (kind == FLOU_BC_INFLOW) {
+#pragma unroll
             for (int k = 0; k < NV; ++k) qr[k] = P.bc_state[b][k];
         } else if (kind == FLOU_BC_STATE_FIELD) {
+#pragma unroll
             for (int k = 0; k < NV; ++k) qr[k] = P.bc_field[k * P.nfdofs + gid];
         } else if (kind == FLOU_BC_SLIP && EQ == FLOU_EQ_EULER) {
             // EulerSlipBC (Euler.jl:88-94): rotate to the face frame, flip the normal momentum,
@@ -589,11 +677,12 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
                 a[1] = -a[1];
                 rotate_to_phys<DIM>(a, fr, qr);
             } else {
-                for (int k = 0; k < NV; ++k) qr[k] = ql[k];
-                int an = frame_axes<DIM>(s0 & 7).ax[0];
-                qr[1 + an] = -ql[1 + an];
+                const int an = frame_axes<DIM>(s0 & 7).ax[0];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) qr[k] = flip(ql[k], k >= 1 && k <= DIM && k - 1 == an);
             }
         } else {
+#pragma unroll
             for (int k = 0; k < NV; ++k) qr[k] = ql[k];   // outflow
         }
     }
@@ -613,11 +702,8 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
             rotate_to_face<DIM>(qr, fr, b);
         } else {
             a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-#pragma unroll
-            for (int r = 0; r < DIM; ++r) {
-                a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
-                b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
-            }
+            cart_to_face<DIM>(ql, A, a);
+            cart_to_face<DIM>(qr, A, b);
         }
         double Fr[NV];
         euler_numflux<DIM>(a, b, P.numflux, P.lxf_avg, inten, P.gamma, Fr);
@@ -626,8 +712,7 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         } else {
             F[0] = Fr[0];
             F[DIM + 1] = Fr[DIM + 1];
-#pragma unroll
-            for (int r = 0; r < DIM; ++r) F[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]);
+            cart_to_phys<DIM>(Fr, A, F);
         }
     } else if (EQ == FLOU_EQ_LINEAR_ADVECTION) {
         // LinearAdvection.jl:27-39
@@ -645,6 +730,8 @@ __device__ __forceinline__ void face_node(const FaceParams& P, int64_t gid) {
         }
     }
     int64_t o = (int64_t)f * P.nfd + m;
+    if (!index_ok(o, P.nfdofs, P.status, s0 >> 3)) return;
+#pragma unroll
     for (int k = 0; k < NV; ++k) P.Fn[k * P.nfdofs + o] = F[k] * J;
 }
 
@@ -696,6 +783,9 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         }
         int64_t ol = (int64_t)(pl >> 1) * ipow(N, DIM - 1) + linel;
         int64_t orr = (int64_t)(pr >> 1) * ipow(N, DIM - 1) + liner;
+        if (kChecked && !(index_ok(linel, ipow(N, DIM - 1), P.status, e) && index_ok(liner, ipow(N, DIM - 1), P.status, e) &&
+                          index_ok(ol, P.nfdofs, P.status, e) && index_ok(orr, P.nfdofs, P.status, e)))
+            continue;
         double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
         if (LGL && P.lift_ends) {
             // Only the two end nodes of a line take a face flux.  Where pos is the same for a whole
@@ -731,6 +821,7 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         }
     }
     int64_t g = (int64_t)e * ipow(N, DIM) + i;
+    if (!(index_ok(e, P.nelem, P.status, e) && index_ok(g, P.ndofs, P.status, e))) return;
     double invJ = CURV ? P.invJn[g] : P.elem_invJ[e];
     const double dt = P.dtp ? *P.dtp : P.dt;
     const double c = dt * invJ;   // dt/J once per node: q + dt (dq/J) = q + c dq
@@ -1429,17 +1520,15 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                     } else {
                         FrameAxes A = frame_axes<DIM>(2 * dir + 1);
                         a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-#pragma unroll
-                        for (int r = 0; r < DIM; ++r) {
-                            a[1 + r] = flip(ql[1 + A.ax[r]], A.neg[r]);
-                            b[1 + r] = flip(qr[1 + A.ax[r]], A.neg[r]);
-                        }
+                        cart_to_face<DIM>(ql, A, a);
+                        cart_to_face<DIM>(qr, A, b);
                         euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
                         const double Js = P.elem_Ja[e * DIM + dir];
                         Fv[0] = Fr[0] * Js;
                         Fv[DIM + 1] = Fr[DIM + 1] * Js;
+                        cart_to_phys<DIM>(Fr, A, Fv);
 #pragma unroll
-                        for (int r = 0; r < DIM; ++r) Fv[1 + A.ax[r]] = flip(Fr[1 + r], A.neg[r]) * Js;
+                        for (int k = 0; k < DIM; ++k) Fv[1 + k] = Fv[1 + k] * Js;
                     }
                     if constexpr (GAUSS) {   // blended in the scan below
 #pragma unroll

@@ -7,7 +7,11 @@ import ctypes
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libflou_cuda.so")
+# FLOU_CUDA_CHECKED=1 in the environment selects the build with device-side index checks
+# (flou.jl_gb300/build.py --checked): slower, for tests; an out-of-range index is reported as
+# FLOU_ERR_INDEX instead of being accessed.
+CHECKED = os.environ.get("FLOU_CUDA_CHECKED", "") not in ("", "0")
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libflou_cuda_checked.so" if CHECKED else "libflou_cuda.so")
 
 FLOU_OK = 0
 FLOU_ERR_ARG = 1
@@ -17,6 +21,7 @@ FLOU_ERR_TIMEOUT = 4
 FLOU_ERR_OOM = 5
 FLOU_ERR_UNSUPPORTED = 6
 FLOU_ERR_STATE = 7
+FLOU_ERR_INDEX = 8
 
 EQ_LINEAR_ADVECTION, EQ_BURGERS, EQ_EULER = 0, 1, 2
 OP_STRONG, OP_SPLIT, OP_HYBRID = 0, 1, 2
@@ -36,6 +41,7 @@ STATUS_NAMES = {
     FLOU_ERR_OOM: "FLOU_ERR_OOM",
     FLOU_ERR_UNSUPPORTED: "FLOU_ERR_UNSUPPORTED",
     FLOU_ERR_STATE: "FLOU_ERR_STATE",
+    FLOU_ERR_INDEX: "FLOU_ERR_INDEX",
 }
 
 

@@ -36,6 +36,7 @@ extern "C" {
 #define FLOU_ERR_OOM 5          /* device allocation failed                                   */
 #define FLOU_ERR_UNSUPPORTED 6  /* valid in Flou but outside this library                      */
 #define FLOU_ERR_STATE 7        /* call order violated (e.g. rhs before set_mesh)            */
+#define FLOU_ERR_INDEX 8        /* a device index check failed (FLOU_CUDA_CHECKED builds only) */
 
 /* ---- enumerations --------------------------------------------------------------------- */
 /* Equations: LinearAdvection (src/FlouCommon/LinearAdvection.jl:16-26), BurgersEquation
