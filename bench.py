@@ -51,6 +51,12 @@ def replica_throughput(local_ms, local_units, dist=None, device=None):
     return float(tot) / (float(mx) * 1e-3), float(mx)
 
 
+# Fixed dt of the Taylor-Green meshes: TGV_CFL x get_max_dt(U0, 1).  At p = 7 a CFL of 0.2 in
+# get_max_dt's definition (mean node spacing) is unstable with SSP-RK3: the 16^3 p=7 mesh, and
+# the oracle on 4^3 p=7, lose positivity within 50-100 steps; 0.15 is stable over 100 steps.
+TGV_CFL = 0.15
+
+
 def make_tgv(nel, n, mach=0.1):
     import flou_cuda as F
     eq = F.EulerEquation(3, 1.4)
@@ -122,18 +128,19 @@ FULL_NDOFS = 32 ** 3 * 4 ** 3 + 16 ** 3 * 8 ** 3   # 4,194,304 nodes
 
 
 def cpu_oracle_rate(steps, warmup, threads):
-    """The CPU oracle on a bounded sample of the workload: one SSP-RK3 step on a 16³ p=3 mesh
-    and one on an 8³ p=7 mesh (262,144 nodes each) per step.  Returns (rate, seconds, ndofs)."""
+    """The CPU oracle on the workload's own meshes: one SSP-RK3 step of the 32³ p=3 mesh and one
+    of the 16³ p=7 mesh (2,097,152 nodes each) per step, every step from the initial state.
+    Returns (rate, seconds, ndofs)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_ref
     from cases import oracle_for
     L = oracle_ref.lib()
     L.oracle_set_threads(threads)
     samples = []
-    for nel, n in ((16, 4), (8, 8)):
+    for nel, n in ((32, 4), (16, 8)):
         disc, Q0 = make_tgv(nel, n)
         o = oracle_for(disc)
-        dt = 0.2 * o.max_dt(Q0, 1.0, disc.std.omega)
+        dt = TGV_CFL * o.max_dt(Q0, 1.0, disc.std.omega)
         samples.append((o, Q0, dt, disc.ndofs))
     for _ in range(warmup):
         for o, Q0, dt, _n in samples:
@@ -147,6 +154,13 @@ def cpu_oracle_rate(steps, warmup, threads):
     return ndofs * 3 * steps / sec, sec, ndofs
 
 
+def workload_config(world):
+    """The `config` object of both arms (the same workload, the same keys)."""
+    return {"workload": WORKLOAD, "ndofs_per_gpu": FULL_NDOFS, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)",
+            "schedule": "one stream per mesh, steps pipelined per mesh (value and e2e)"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -154,16 +168,15 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     steps = max(args.steps, 1)
     rate, sec, ndofs = cpu_oracle_rate(steps, args.warmup, threads)
+    sample = ("%d SSP-RK3 steps of the workload's two meshes (32^3 p=3 and 16^3 p=7, %d nodes) after %d warm-up "
+              "steps, each from the initial state; the C++ restatement of Flou's residual and SSP-RK3 (Flou's Julia "
+              "path cannot run here: no julia), OpenMP over elements and faces" % (steps, ndofs, args.warmup))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sec / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "ndofs_per_gpu": FULL_NDOFS, "parallelism": "single",
-                   "sample_ndofs": ndofs,
-                   "note": "Flou's Julia path cannot run here (no julia); the C++ restatement of its residual, "
-                           "timed on a bounded sample of the workload (16^3 p=3 + 8^3 p=7 per step)"},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "1 SSP-RK3 step on a 16^3 p=3 and an 8^3 p=7 TGV mesh per step"},
+        "config": workload_config(1),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -239,10 +252,40 @@ def bench_batched(steps, warmup, count=256):
     ms_s = e0.elapsed_time(e1)
     for d in discs:
         d.ctx.set_stream(0)
+    # Where the serial loop's time goes.  The throughput floor: the plain face and element
+    # kernels of each order timed (CUDA events, the three stage modes averaged) on one large
+    # periodic mesh of that order (~1.5 M nodes, many waves: full occupancy, no tail), giving the
+    # cost per node and stage when nothing but the kernels' own work is left; every instance
+    # priced at its order's rate is the time the same tile code needs with no launch, latency
+    # or tail overhead -- what any batching of these kernels can at best reach.
+    orders = sorted({d.std.n for d in discs})
+    per_node = {}
+    by_order = {}
+    eq = discs[0].equation
+    for n in orders:
+        ne = max(8, int(round(math.sqrt(1.5e6) / n)))
+        mesh = F.CartesianMesh((-5.0, -5.0), (5.0, 5.0), (ne, ne))
+        F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"))
+        b = F.LagrangeBasis("GLL", n)
+        big = F.MultielementDisc(mesh, F.StdQuad(b, F.DGSEMrec(b), eq.nvariables), eq,
+                                 F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)), {})
+        qb = torch.from_numpy(np.ascontiguousarray(
+            F.initial.vortex_bump(eq, big.coords, (0.3, -0.2), 3.0, 0.05, period=(10.0, 10.0)).T)).cuda()
+        fms, ems = big.ctx.time_kernels(qb, nrep=3)
+        per_node[n] = (fms + ems) / big.ndofs
+        ks = [k for k, d in enumerate(discs) if d.std.n == n]
+        by_order["p%d" % (n - 1)] = {
+            "instances": len(ks), "ndofs": sum(discs[k].ndofs for k in ks),
+            "floor_ms_per_step": 3 * per_node[n] * sum(discs[k].ndofs for k in ks),
+            "rate_mesh_ndofs": big.ndofs, "ns_per_node_stage": 1e6 * per_node[n]}
+        del big, qb
+    floor_ms = 3 * sum(per_node[d.std.n] * d.ndofs for d in discs)
     vb = ndofs * 3 * steps / (ms_b * 1e-3)
     vs = ndofs * 3 * steps / (ms_s * 1e-3)
     return {"value": vb, "unit": UNIT, "serial_value": vs, "speedup_vs_serial": vb / vs, "instances": count,
             "ndofs": ndofs, "ms_per_step": ms_b / steps, "serial_ms_per_step": ms_s / steps, "autotune": choice,
+            "throughput_floor_ms_per_step": floor_ms, "batched_over_floor": (ms_b / steps) / floor_ms,
+            "speedup_bound_at_floor": (ms_s / steps) / floor_ms, "by_order": by_order,
             "gpu_launches_per_step": 3, "serial_gpu_launches_per_step": 6 * count,
             "workload": "256 x 2D Euler, n~U{8..64}^2 elements, p~U{2..7}, periodic/slip walls, vortex+bump, "
                         "Rusanov, strong form, SSP-RK3"}
@@ -564,7 +607,7 @@ def run_profile(which):
     nel, n = (32, 4) if which == "A" else (16, 8)
     disc, Q0 = make_tgv(nel, n)
     Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
-    dt = 0.2 * disc.ctx.max_dt(Qd, 1.0)
+    dt = TGV_CFL * disc.ctx.max_dt(Qd, 1.0)
     disc.ctx.step(Qd, dt, 2)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": "tgv3d %d^3 p=%d" % (nel, n - 1), "ndofs": disc.ndofs, "steps": 2}))
@@ -606,9 +649,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-curvilinear", action="store_true")
-    ap.add_argument("--adjoint-batch", action="store_true",
-                    help="also run the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; "
-                         "several minutes)")
+    ap.add_argument("--no-adjoint-batch", action="store_true",
+                    help="skip the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; about "
+                         "four minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
     ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G", "H", "I"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
@@ -649,7 +692,7 @@ def main():
         disc, Q0 = make_tgv(nel, n)
         ctx = disc.ctx
         Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
-        dt = 0.2 * ctx.max_dt(Qd, 1.0)   # fixed dt at CFL 0.2 (get_max_dt's definition; p = 7 needs <= 0.2)
+        dt = TGV_CFL * ctx.max_dt(Qd, 1.0)
         meshes.append(dict(name="%dc_p%d" % (nel, n - 1), disc=disc, ctx=ctx, Q0=Q0, Qd=Qd, dt=dt, ndofs=disc.ndofs))
     stream = torch.cuda.current_stream()
     for m in meshes:
@@ -726,25 +769,31 @@ def main():
     prof = load_profile_summary().get(dom, {})
     traffic = prof.get("dram_bytes_per_dof_stage")   # ncu, stage-2 launch of the same kernel
     fp64_ops = prof.get("fp64_flops_per_dof_stage")   # executed FP64 flops (2 per FMA), ncu
+    # The element kernel is bound by the FP64 pipe (2 DFMA lanes per SM per cycle on GB300), not by
+    # HBM: the roofline is the executed FP64 rate (ncu's executed FP64 flops per DOF of the same
+    # kernel, 2 per DFMA, times the DOFs of one launch, over its CUDA-event launch time) against
+    # the DFMA peak measured by the in-run probe (MEASURED_PEAKS.json carries no FP64 figure); the
+    # HBM fraction of the compulsory state traffic is reported beside it.
+    fp64_achieved = (fp64_ops * dk["ndofs"] / (dk["elem_ms"] * 1e-3) / 1e12) if fp64_ops else None
+    fp64_peak_t = fp64_peak / 1e3 if fp64_peak else None
     roofline = {
         "kernel": "elem_split_kernel<3,%d,Euler,Chandrashekar> (%s)" % (int(dom[-1]) + 1, dom),
-        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": (achieved / hbm_peak) if hbm_peak else None,
-        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None,
+        "bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak_t, "unit": "TFLOP/s",
+        "frac": (fp64_achieved / fp64_peak_t) if (fp64_achieved and fp64_peak_t) else None,
+        "peak_source": "in-run FP64 DFMA throughput probe (flou_fp64_peak), measured this run",
+        "flops_source": "profiles/tgv3d_split_elem_kernel.json: ncu executed FP64 flops (2 per DFMA) of the "
+                        "stage-2 launch, per DOF, times the DOFs of one launch",
+        "executed_fp64_flops_per_dof_stage": fp64_ops,
+        "dmma_peak_tflops": dmma_peak / 1e3 if dmma_peak else None,
         "traffic": (traffic * dk["ndofs"]) if traffic else None,
         "traffic_source": "profiles/tgv3d_split_elem_kernel.json: ncu dram__bytes_read+write of the stage-2 launch",
+        "hbm_achieved_gbs": achieved, "hbm_peak_gbs": hbm_peak,
+        "hbm_frac": (achieved / hbm_peak) if hbm_peak else None,
+        "hbm_peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None,
         "algorithmic_bytes_per_launch": algo_bytes,
         "launch_ms": dk["elem_ms"],
-        "fp64": {
-            "peak_gflops": fp64_peak, "peak_source": "DFMA throughput probe (flou_fp64_peak), this run",
-            "dmma_peak_gflops": dmma_peak,
-            "executed_flops_per_dof_stage": fp64_ops,
-            "achieved_gflops": (fp64_ops * dk["ndofs"] / (dk["elem_ms"] * 1e-3) / 1e9) if fp64_ops else None,
-        },
         "kernels": kern,
     }
-    if fp64_ops and fp64_peak:
-        roofline["fp64"]["frac"] = roofline["fp64"]["achieved_gflops"] / fp64_peak
 
     # ---- general geometry: the curvilinear kernels on mesh A's size ----
     curvilinear = None
@@ -820,25 +869,25 @@ def main():
         adjoint = bench_adjoint()
 
     adjoint_batch = None
-    if args.adjoint_batch:
+    if not args.no_adjoint_batch and world == 1:
+        for m in meshes:   # the batched adjoint's budget wants the device memory of the headline meshes back
+            m["ctx"].set_stream(0)
         adjoint_batch = bench_adjoint_batch()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, sec, nd = cpu_oracle_rate(16, 1, threads)
+        rate, sec, nd = cpu_oracle_rate(8, 1, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "16 SSP-RK3 steps on a 16^3 p=3 and an 8^3 p=7 TGV mesh (%d nodes), %.1f s wall" % (nd, sec)}
+               "sample": "8 SSP-RK3 steps of the workload's two meshes (32^3 p=3 and 16^3 p=7, %d nodes), each from "
+                         "the initial state, %.1f s wall" % (nd, sec)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
             "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "ndofs_per_gpu": ndofs, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2: each stage streams ~250 MB per mesh (L2 129 MB)",
-                       "schedule": "one stream per mesh, steps pipelined per mesh (value and e2e)"},
+            "config": workload_config(world),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched, "adjoint": adjoint,
             "adjoint_batch": adjoint_batch, "limiter": limiter, "curvilinear": curvilinear, "operators": operators,
             "gpu_launches": steps * 6 * len(meshes), "clocks": clk,

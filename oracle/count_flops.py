@@ -2,7 +2,7 @@
 oracle -- the CPU restatement of Flou's rhs! -- instantiated with a counting scalar on small
 meshes of the benchmark configurations and prints the counts per node (DOF) as a Markdown table.
 
-    python oracle/count_flops.py > profiles/reference_algorithm_op_count.md
+    python oracle/count_flops.py
 """
 import math
 import os

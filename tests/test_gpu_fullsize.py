@@ -2,8 +2,10 @@
 
 Config 1 (2D vortex, 16² elements, p=4, strong form, Rusanov, 100 SSP-RK3 steps) against the
 oracle; the 3D Taylor-Green meshes (32³ p=3 and 16³ p=7, split form Chandrashekar + HLLC,
-2,097,152 nodes each) through one residual against the oracle and size-independent
-properties: discrete conservation, freestream preservation, bitwise determinism.
+2,097,152 nodes each) through one residual (backward error and relative L-inf against the
+oracle's own conditioning floor) and the configuration's 50 SSP-RK3 steps against the oracle,
+and size-independent properties: discrete conservation, freestream preservation, bitwise
+determinism.
 """
 import math
 
@@ -64,13 +66,38 @@ def test_tgv_residual_against_oracle(tgv):
     assert np.all(err <= 1e-14 * _term_scale(disc, Q0)), (err, _term_scale(disc, Q0))
 
 
-def test_tgv_two_steps_against_oracle(tgv):
+def test_tgv_residual_relative_linf_against_the_oracles_own_spread(tgv):
+    """The relative L-inf error per DOF of one residual, against the oracle.  At Mach 0.1 the
+    residual is ~1e4 times smaller than the terms it sums, so this is held to the larger of 1e-12
+    and four times the oracle's own spread: the change of the oracle's residual when its input
+    moves by one ulp (relative perturbations of 1.1e-16 times a standard normal), the
+    conditioning floor of the problem itself."""
     disc, Q0 = tgv
     Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
-    dt = 0.3 * disc.ctx.max_dt(Qd, 1.0)
-    disc.ctx.step(Qd, dt, 2)
-    ref = oracle_for(disc).ssprk3(Q0, dt, 2)
-    assert rel_linf(Qd.cpu().numpy().T, ref) <= 1e-10
+    dQ = torch.empty_like(Qd)
+    disc.ctx.rhs(dQ, Qd)
+    o = oracle_for(disc)
+    ref = o.rhs(Q0)
+    err = rel_linf(dQ.cpu().numpy().T, ref)
+    rng = np.random.default_rng(0)
+    spread = rel_linf(o.rhs(np.asfortranarray(Q0 * (1 + 1.1e-16 * rng.standard_normal(Q0.shape)))), ref)
+    print("TGV %s residual: relative L-inf %.3e, oracle spread under 1-ulp input changes %.3e"
+          % (disc.mesh.nelements, err, spread))
+    assert err <= max(1e-12, 4.0 * spread), (err, spread)
+
+
+def test_tgv_50_steps_against_oracle(tgv):
+    """The configuration's 50 SSP-RK3 steps at the benchmark's fixed dt (CFL 0.15 in get_max_dt's
+    definition) on the full mesh, against the oracle's 50 steps: relative L-inf <= 1e-10."""
+    import bench
+    disc, Q0 = tgv
+    Qd = torch.from_numpy(np.ascontiguousarray(Q0.T)).cuda()
+    dt = bench.TGV_CFL * disc.ctx.max_dt(Qd, 1.0)
+    disc.ctx.step(Qd, dt, 50)
+    ref = oracle_for(disc).ssprk3(Q0, dt, 50)
+    err = rel_linf(Qd.cpu().numpy().T, ref)
+    print("TGV %s after 50 SSP-RK3 steps: relative L-inf %.3e" % (disc.mesh.nelements, err))
+    assert err <= 1e-10
 
 
 def test_tgv_conservation_freestream_determinism(tgv):

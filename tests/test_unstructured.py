@@ -176,10 +176,13 @@ def test_gmsh41_file():
     assert np.allclose(m.nodes[m.elements[1]], [[1, 0], [2, 0], [2, 1], [1, 1]])
 
 
-REF_MESHES = "/root/reference/test/meshes"
+# The reference's test/meshes folder, named by FLOU_REFERENCE_MESHES (the test is skipped
+# when it is unset or absent).
+REF_MESHES = os.environ.get("FLOU_REFERENCE_MESHES", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="the reference's mesh files are not present")
+@pytest.mark.skipif(not REF_MESHES or not os.path.isdir(REF_MESHES),
+                    reason="FLOU_REFERENCE_MESHES does not name the reference's test/meshes folder")
 @pytest.mark.parametrize("name,dim,nelem,names", [
     ("2D_cylinder", 2, 73, ["Bottom", "Right", "Top", "Left", "Hole"]),
     ("3D_bullet", 3, 295, ["Body", "Interior", "Inlet", "Wall", "Outlet", "Left", "Right"]),
