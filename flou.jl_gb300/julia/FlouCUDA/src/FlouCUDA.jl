@@ -286,8 +286,9 @@ end
 """
     solve_functional(disc, Q0, c, dt, nsteps, ρtarget, w) -> J
 
-J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` SSP-RK3 steps with per-element dissipation scales `c`.
-Differentiable through the `rrule` below (discrete adjoint, binomial checkpointing).
+J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` SSP-RK3 steps with per-element dissipation scales `c`
+(LxF interface fluxes), or `c = nothing` for HLL and HLLC, which have no dissipation scale.
+Differentiable through the `rrule`s below (discrete adjoint, binomial checkpointing).
 Arrays are device pointers wrapped by the caller's GPU array package (e.g. CuArray).
 """
 function solve_functional end
@@ -297,12 +298,26 @@ function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, 
     g = similar(Q0)
     gc = similar(c)
     nf = Ref{Int64}(0)
-    ccall((:flou_set_dissipation, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32), disc.ctx, pointer(c), PTR_DEVICE)
+    check(ccall((:flou_set_dissipation, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32), disc.ctx, pointer(c),
+                PTR_DEVICE), disc.ctx)
     check(ccall((:flou_adjoint_solve, libflou), Int32,
         (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
          Ptr{Float64}, Ref{Int64}),
         disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), pointer(gc), nf), disc.ctx)
     pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, J̄ .* gc, NoTangent(), NoTangent(), NoTangent(), NoTangent())
+    return J[], pullback
+end
+
+# HLL / HLLC interface fluxes: no dissipation scale, so no dJ/dc (the C ABI takes a null dJdc)
+function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, ::Nothing, dt, nsteps, ρt, w; nsnap=20)
+    J = Ref{Float64}(0.0)
+    g = similar(Q0)
+    nf = Ref{Int64}(0)
+    check(ccall((:flou_adjoint_solve, libflou), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ref{Int64}),
+        disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), C_NULL, nf), disc.ctx)
+    pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, NoTangent(), NoTangent(), NoTangent(), NoTangent(), NoTangent())
     return J[], pullback
 end
 
