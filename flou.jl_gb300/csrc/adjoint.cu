@@ -142,9 +142,10 @@ __device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa
     qb[DIM + 1] += kappa * ca;
 }
 
-// Cotangent of one node's primitive variables (ρ, v, β).
+// Cotangent of one node's primitive variables: (ρ, v, β) for the Chandrashekar flux, (ρ, v, p, e)
+// for Kennedy-Gruber (b then holds p̄ and e the cotangent of the specific total energy E/ρ).
 struct PrimBar {
-    double r, v[3], b;
+    double r, v[3], b, e;
 };
 
 // Logarithmic mean (Utilities.jl:34-44) of a = 2 h1, b = 2 h2 given the half sum hs = (a+b)/2,
@@ -252,6 +253,49 @@ __device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, do
     }
     qb[0] += fma(0.5 * vv, pb, fma(-vvb, ir, rb));
     qb[DIM + 1] += pb;
+}
+
+// VJP of the Kennedy-Gruber pair flux along axis D (Kennedy & Gruber 2008, as the forward kernel
+// evaluates it), F = [m, m v̄ + p̄ e_D, m ē + p̄ v̄_D] with m = ρ̄ v̄_D and the arithmetic means
+// ρ̄, v̄, p̄, ē (e = E/ρ).  Inputs are the halved node quantities (rh = ρ/2, vh = v/2, ph = p/2,
+// eh = e/2), so each mean is a sum of two; both nodes receive half of each mean's cotangent.
+template <int DIM, int D>
+__device__ __forceinline__ void kg_pair_vjp(double rh1, const double* vh1, double ph1, double eh1, double rh2,
+                                            const double* vh2, double ph2, double eh2, const double* Fb,
+                                            PrimBar& o1, PrimBar& o2) {
+    const double rho = rh1 + rh2, pm = ph1 + ph2, en = eh1 + eh2;
+    double vm[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vm[k] = vh1[k] + vh2[k];
+    const double m = rho * vm[D];
+    double mb = fma(Fb[DIM + 1], en, Fb[0]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], vm[k], mb);
+    o1.r = o2.r = 0.5 * mb * vm[D];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o1.v[k] = 0.5 * Fb[1 + k] * m;
+    o1.v[D] = fma(0.5 * mb, rho, fma(0.5 * Fb[DIM + 1], pm, o1.v[D]));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o2.v[k] = o1.v[k];
+    o1.b = o2.b = 0.5 * fma(Fb[DIM + 1], vm[D], Fb[1 + D]);
+    o1.e = o2.e = 0.5 * Fb[DIM + 1] * m;
+}
+
+// q̄ += (∂(ρ, v, p, e)/∂q)ᵀ (ρ̄, v̄, p̄, ē) with v = m/ρ, p = (γ-1)(E - ½|m|²/ρ), e = E/ρ:
+//   q̄_ρ += ρ̄ - (v·v̄ + e ē)/ρ + (γ-1)|v|²/2 p̄,  q̄_mk += v̄_k/ρ - (γ-1) v_k p̄,
+//   q̄_E += (γ-1) p̄ + ē/ρ.
+template <int DIM>
+__device__ __forceinline__ void kg_prim_to_cons_vjp(double rho, const double* v, double vv, double E, double g1,
+                                                    const PrimBar& o, double* qb) {
+    const double ir = rcp_refined(rho), e = E * ir, pb = g1 * o.b;
+    double vvb = e * o.e;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vvb = fma(v[k], o.v[k], vvb);
+        qb[1 + k] += fma(o.v[k], ir, -v[k] * pb);
+    }
+    qb[0] += fma(0.5 * vv, pb, fma(-vvb, ir, o.r));
+    qb[DIM + 1] += fma(o.e, ir, pb);
 }
 
 // Cotangents of one side's primitive quantities in the face frame (normal velocity u, tangential
@@ -434,10 +478,80 @@ __device__ __forceinline__ void hll_family_vjp(bool hllc, const double* a, const
     side_prim_vjp<DIM>(pb, g, R, qb);
 }
 
-// KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC.
+// The dissipation vector of ScalarDissipation (Euler.jl:228-301, as the forward face kernel forms
+// it in the face frame), F = A - λ/2 · intensity · D with
+//   D_ρ = ρ_r - ρ_l,  D_m = m_r - m_l (zero in 3D: the reference reads the left momenta from Q_r),
+//   D_E = ½ c₁ (ρ_r - ρ_l) + ½ (ρ_l + ρ_r) c₂,
+//   c₁ = 1/((γ-1) β_ln) + v_l·v_r,  c₂ = ½(|v_r|² - |v_l|²) + (p_r/ρ_r - p_l/ρ_l)/(γ-1),
+// β = ρ/(2p), β_ln the logarithmic mean.  Returns D and adds Dbar·∂D/∂(a, b) to qa, qb (the
+// direct conserved parts) and to L, R (the cotangents of the velocities and pressures).
+template <int DIM>
+__device__ __forceinline__ void sd_jump_vjp(const double* a, const double* b, const Prim& pa, const Prim& pb,
+                                            double g, const double* Db, double* D, double* qa, double* qb,
+                                            SideBar& L, SideBar& R) {
+    constexpr int NV = DIM + 2;
+    const double g1 = g - 1.0, ig1 = 1.0 / g1;
+    const double ipl = rcp_refined(pa.p), ipr = rcp_refined(pb.p);
+    const double bl = 0.5 * pa.rho * ipl, br = 0.5 * pb.rho * ipr;
+    const double hs = 0.5 * (bl + br), hd = 0.5 * (bl - br);
+    double Lb, iLb, dla, dlb;
+    logmean_half(0.5 * bl, 0.5 * br, hs, hd, rcp_refined(hs), Lb, iLb, dla, dlb);
+    double vlr = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vlr = fma(pa.v[k], pb.v[k], vlr);
+    const double c1 = fma(ig1, iLb, vlr);
+    const double c2 = fma(0.5, pb.vv - pa.vv, ig1 * (pb.p * pb.ir - pa.p * pa.ir));
+    const double dr = pb.rho - pa.rho, sr = pa.rho + pb.rho;
+    D[0] = dr;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? 0.0 : b[1 + k] - a[1 + k];
+    D[DIM + 1] = fma(0.5 * c1, dr, 0.5 * sr * c2);
+    // reverse
+    qb[0] += Db[0];
+    qa[0] -= Db[0];
+    if (DIM != 3) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            qb[1 + k] += Db[1 + k];
+            qa[1 + k] -= Db[1 + k];
+        }
+    }
+    const double dE = Db[DIM + 1];
+    const double c1b = 0.5 * dr * dE, c2b = 0.5 * sr * dE;
+    qb[0] += 0.5 * (c1 + c2) * dE;
+    qa[0] += 0.5 * (c2 - c1) * dE;
+    // c1: 1/β_ln and v_l·v_r
+    const double ib = -ig1 * c1b * iLb * iLb;   // cotangent of β_ln
+    const double blb = ib * dla, brb = ib * dlb;
+    // c2: ½(|v_r|² - |v_l|²) and (p/ρ) of both sides
+    const double tr = c2b * ig1 * pb.ir, tl = c2b * ig1 * pa.ir;
+    qb[0] -= tr * pb.p * pb.ir;
+    qa[0] += tl * pa.p * pa.ir;
+    R.p += tr;
+    L.p -= tl;
+    // β = ρ/(2p): ρ̄ += β̄/(2p), p̄ -= β̄ β/p
+    qa[0] += 0.5 * blb * ipl;
+    L.p -= blb * bl * ipl;
+    qb[0] += 0.5 * brb * ipr;
+    R.p -= brb * br * ipr;
+    // velocities (face frame: component 0 normal, then the tangents)
+    const double vlb0 = fma(c1b, pb.v[0], -c2b * pa.v[0]), vrb0 = fma(c1b, pa.v[0], c2b * pb.v[0]);
+    L.u += vlb0;
+    R.u += vrb0;
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        L.vt[k - 1] += fma(c1b, pb.v[k], -c2b * pa.v[k]);
+        R.vt[k - 1] += fma(c1b, pa.v[k], c2b * pb.v[k]);
+    }
+    (void)NV;
+}
+
+// KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC,
+// 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage).
 template <int DIM, int KIND>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
-    constexpr bool CHANDRA = KIND == 1;
+    constexpr bool CHANDRA = KIND == 1 || KIND == 5;
+    constexpr bool SD = KIND >= 4;
     constexpr int NV = DIM + 2;
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
@@ -511,7 +625,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     Prim pb = prim_of<DIM>(bb, g);
     double ab[NV], bbar[NV];
     double Ib = 0.0;
-    if (KIND >= 2) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
+    if (KIND == 2 || KIND == 3) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
 #pragma unroll
         for (int k = 0; k < NV; ++k) ab[k] = bbar[k] = 0.0;
         hll_family_vjp<DIM>(KIND == 3, a, bb, pa, pb, g, fb, ab, bbar);
@@ -520,14 +634,27 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     bool left = lr < ll;   // Base.max(ll, lr)
     double lam = left ? ll : lr;
     double dot = 0.0;
+    SideBar Ls = {}, Rs = {};
+    if (SD) {   // F = A - λ/2 · intensity · D(a, b)
+        double D[NV], Db[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
-    Ib = 0.5 * lam * dot;
+        for (int k = 0; k < NV; ++k) {
+            Db[k] = -0.5 * inten * lam * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        sd_jump_vjp<DIM>(a, bb, pa, pb, g, Db, D, ab, bbar, Ls, Rs);
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        ab[k] = 0.5 * inten * lam * fb[k];
-        bbar[k] = -ab[k];
+        for (int k = 0; k < NV; ++k) dot = fma(-fb[k], D[k], dot);
+    } else {    // F = A + λ/2 · intensity · (a - b)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ab[k] = 0.5 * inten * lam * fb[k];
+            bbar[k] = -ab[k];
+        }
     }
+    Ib = SD ? 0.0 : 0.5 * lam * dot;   // ScalarDissipation takes no per-element scale
     if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
         PrimBar o1, o2;
         double vh1[DIM], vh2[DIM];
@@ -548,6 +675,10 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     double kappa = 0.5 * inten * dot;
     if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
     else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    if (SD) {
+        side_prim_vjp<DIM>(pa, g, Ls, ab);
+        side_prim_vjp<DIM>(pb, g, Rs, bbar);
+    }
     }
     if (s1 < 0) {
         if (bck == FLOU_BC_OUTFLOW) {
@@ -691,12 +822,13 @@ cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
 // the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux;
 // zero on interior LGL nodes) and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved
 // variables.
-template <int DIM, int N>
+template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR>
 struct AdjSplitShape {
     using S = Shape<DIM, N>;
+    static constexpr bool KG = TP == FLOU_TP_KENNEDY_GRUBER;
     static constexpr int NV = DIM + 2;
-    static constexpr int NARR = DIM + 3;                        // rh, vh, bh, vq
-    static constexpr int NPB = DIM + 2;                         // ρ̄, v̄, β̄ per side
+    static constexpr int NARR = DIM + 3;                        // rh, vh, bh, vq (KG: rh, vh, ph, eh)
+    static constexpr int NPB = KG ? DIM + 3 : DIM + 2;          // ρ̄, v̄, β̄ per side (KG: ρ̄, v̄, p̄, ē)
     static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
     static constexpr int NSD = S::EPB * DIM * N * N;           // -Ja_d D♯ per element and direction
     static constexpr size_t SMEM =
@@ -706,12 +838,12 @@ struct AdjSplitShape {
     static constexpr int MINB = (S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
 };
 
-template <int DIM, int N, int D>
+template <int DIM, int N, int D, int TP>
 __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, const double* sJD,
                                                 const double* sprim, const double* sw, double* spb,
                                                 const uint8_t* stab, double cb) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = A::NPT, NPB = A::NPB;
     for (int kp = threadIdx.x; kp < NPT; kp += blockDim.x) {
@@ -734,9 +866,13 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
             v2[k] = sprim[(1 + k) * NN + ib];
         }
         PrimBar o1, o2;
-        chandra_pair_vjp<DIM, D, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
-                                        sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
-                                        Fb, o1, o2);
+        if constexpr (A::KG)
+            kg_pair_vjp<DIM, D>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia], sprim[ib], v2,
+                                sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], Fb, o1, o2);
+        else
+            chandra_pair_vjp<DIM, D, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
+                                            sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
+                                            Fb, o1, o2);
         spb[kp] = o1.r;
         spb[NPB * NPT + kp] = o2.r;
 #pragma unroll
@@ -746,16 +882,20 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
         }
         spb[(1 + DIM) * NPT + kp] = o1.b;
         spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
+        if constexpr (A::KG) {
+            spb[(2 + DIM) * NPT + kp] = o1.e;
+            spb[(NPB + 2 + DIM) * NPT + kp] = o2.e;
+        }
     }
 }
 
-template <int DIM, int N, int D>
+template <int DIM, int N, int D, int TP>
 __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
                                                 const double* Dsh, const double* sw, const double* spb,
                                                 const double* v, double rho, double p, double g1, double* qb,
                                                 PrimBar& acc) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
     constexpr int NV = DIM + 2, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = A::NPT, NPB = A::NPB;
     int pos, line;
@@ -785,6 +925,7 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
 #pragma unroll
         for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
         acc.b += src[(1 + DIM) * NPT + pidx];
+        if constexpr (A::KG) acc.e += src[(2 + DIM) * NPT + pidx];
     }
     if (pos == 0 || pos == N - 1) {
         int32_t pk = P.elem_face[e * 2 * DIM + 2 * D + (pos == 0 ? 0 : 1)];
@@ -797,16 +938,16 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     }
 }
 
-template <int DIM, int N>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::MINB)
+template <int DIM, int N, int TP>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP>::MINB)
     adj_split_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
     constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
     extern __shared__ double smem[];
     double* sops = smem;
-    double* sprim = sops + S::NOPS;   // [NARR][NN]: ρ/2, v/2, β/2, |v|²/4
+    double* sprim = sops + S::NOPS;   // [NARR][NN]: ρ/2, v/2, β/2, |v|²/4 (KG: ρ/2, v/2, p/2, (E/ρ)/2)
     double* sw = sprim + NARR * NN;   // [NV][NN]: w = λ / J
     double* spb = sw + NV * NN;       // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
     double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
@@ -851,8 +992,13 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
         sprim[tid] = 0.5 * rho;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
-        sprim[(1 + DIM) * NN + tid] = (0.25 * rho) * rcp_refined(p);
-        sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
+        if constexpr (A::KG) {
+            sprim[(1 + DIM) * NN + tid] = 0.5 * p;
+            sprim[(2 + DIM) * NN + tid] = 0.5 * (q[DIM + 1] * ir);
+        } else {
+            sprim[(1 + DIM) * NN + tid] = (0.25 * rho) * rcp_refined(p);
+            sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) v[k] = 0.0;
@@ -864,21 +1010,23 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
     PrimBar acc;
     acc.r = 0.0;
     acc.b = 0.0;
+    acc.e = 0.0;
 #pragma unroll
     for (int k = 0; k < NV; ++k) qb[k] = 0.0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
-        if (dir == 0) adj_split_pairs<DIM, N, 0>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0)>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0)>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        if (dir == 0) adj_split_pairs<DIM, N, 0, TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
         __syncthreads();
         if (active) {
-            if (dir == 0) adj_split_nodes<DIM, N, 0>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            if (dir == 0) adj_split_nodes<DIM, N, 0, TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
             else if (dir == 1)
-                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0)>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
-            else adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0)>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            else
+                adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
         }
         __syncthreads();
     }
@@ -886,7 +1034,8 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
     double vv = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
-    prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
+    if constexpr (A::KG) kg_prim_to_cons_vjp<DIM>(rho, v, vv, P.U[(DIM + 1) * P.ndofs + gi], g1, acc, qb);
+    else prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
     for (int k = 0; k < NV; ++k) {
         double ain = P.Ain[k * P.ndofs + gi];
         double o = fma(P.alpha, ain, qb[k]);
@@ -911,35 +1060,42 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N>::M
     }
 }
 
-template <int DIM, int N>
+template <int DIM, int N, int TP>
 cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
-    constexpr size_t smem = AdjSplitShape<DIM, N>::SMEM;
+    constexpr size_t smem = AdjSplitShape<DIM, N, TP>::SMEM;
     static_assert(smem <= 227 * 1024, "split adjoint tile exceeds shared memory");
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_split_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_split_elem_kernel<DIM, N, TP><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int DIM>
-cudaError_t launch_adj_split(int n, const AdjElemParams& P, cudaStream_t s) {
+template <int DIM, int TP>
+cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_split_n<DIM, 2>(P, s);
-        case 3: return launch_adj_split_n<DIM, 3>(P, s);
-        case 4: return launch_adj_split_n<DIM, 4>(P, s);
-        case 5: return launch_adj_split_n<DIM, 5>(P, s);
-        case 6: return launch_adj_split_n<DIM, 6>(P, s);
-        case 7: return launch_adj_split_n<DIM, 7>(P, s);
-        case 8: return launch_adj_split_n<DIM, 8>(P, s);
+        case 2: return launch_adj_split_n<DIM, 2, TP>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3, TP>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4, TP>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5, TP>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6, TP>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7, TP>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8, TP>(P, s);
         default: return cudaErrorInvalidValue;
     }
+}
+
+// The split form's two-point flux: Chandrashekar or Kennedy-Gruber.
+template <int DIM>
+cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
+    return tp == FLOU_TP_KENNEDY_GRUBER ? launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER>(n, P, s)
+                                        : launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR>(n, P, s);
 }
 
 // Terminal functional J = 1/2 Σ w_i (ρ_i - ρt_i)²: seed Ū (density column) and per-block partials.
@@ -977,14 +1133,16 @@ struct AdjBuffers {
 int adj_supported(flou_ctx* c) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
-               (k.volume_op == FLOU_OP_SPLIT && k.twopoint_flux == FLOU_TP_CHANDRASHEKAR);
-    bool nf = (k.numflux == FLOU_NF_LXF &&
+               (k.volume_op == FLOU_OP_SPLIT &&
+                (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER));
+    bool nf = ((k.numflux == FLOU_NF_LXF || k.numflux == FLOU_NF_SCALAR_DISSIPATION) &&
                (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR)) ||
               k.numflux == FLOU_NF_HLL || k.numflux == FLOU_NF_HLLC;
     if (k.equation != FLOU_EQ_EULER || !vol || !nf)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
-                                                 "the Chandrashekar split form, and the LxF(StdAverage), "
-                                                 "LxF(ChandrasekharAverage), HLL or HLLC interface flux");
+                                                 "the Chandrashekar or Kennedy-Gruber split form, and the "
+                                                 "LxF or ScalarDissipation (StdAverage or ChandrasekharAverage), "
+                                                 "HLL or HLLC interface flux");
     if (!c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
     if (c->limiter)
@@ -1050,20 +1208,27 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     int grid = (int)((nth + tb - 1) / tb);
     int dim = c->cfg.dim;
     const int nf = c->cfg.numflux;
-    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
-    switch (dim * 4 + kind) {
-        case 4: adj_face_kernel<1, 0><<<grid, tb, 0, s>>>(F); break;
-        case 5: adj_face_kernel<1, 1><<<grid, tb, 0, s>>>(F); break;
-        case 6: adj_face_kernel<1, 2><<<grid, tb, 0, s>>>(F); break;
-        case 7: adj_face_kernel<1, 3><<<grid, tb, 0, s>>>(F); break;
-        case 8: adj_face_kernel<2, 0><<<grid, tb, 0, s>>>(F); break;
-        case 9: adj_face_kernel<2, 1><<<grid, tb, 0, s>>>(F); break;
-        case 10: adj_face_kernel<2, 2><<<grid, tb, 0, s>>>(F); break;
-        case 11: adj_face_kernel<2, 3><<<grid, tb, 0, s>>>(F); break;
-        case 12: adj_face_kernel<3, 0><<<grid, tb, 0, s>>>(F); break;
-        case 13: adj_face_kernel<3, 1><<<grid, tb, 0, s>>>(F); break;
-        case 14: adj_face_kernel<3, 2><<<grid, tb, 0, s>>>(F); break;
-        default: adj_face_kernel<3, 3><<<grid, tb, 0, s>>>(F); break;
+    const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
+    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch : ch;
+    switch (dim * 8 + kind) {
+        case 8: adj_face_kernel<1, 0><<<grid, tb, 0, s>>>(F); break;
+        case 9: adj_face_kernel<1, 1><<<grid, tb, 0, s>>>(F); break;
+        case 10: adj_face_kernel<1, 2><<<grid, tb, 0, s>>>(F); break;
+        case 11: adj_face_kernel<1, 3><<<grid, tb, 0, s>>>(F); break;
+        case 12: adj_face_kernel<1, 4><<<grid, tb, 0, s>>>(F); break;
+        case 13: adj_face_kernel<1, 5><<<grid, tb, 0, s>>>(F); break;
+        case 16: adj_face_kernel<2, 0><<<grid, tb, 0, s>>>(F); break;
+        case 17: adj_face_kernel<2, 1><<<grid, tb, 0, s>>>(F); break;
+        case 18: adj_face_kernel<2, 2><<<grid, tb, 0, s>>>(F); break;
+        case 19: adj_face_kernel<2, 3><<<grid, tb, 0, s>>>(F); break;
+        case 20: adj_face_kernel<2, 4><<<grid, tb, 0, s>>>(F); break;
+        case 21: adj_face_kernel<2, 5><<<grid, tb, 0, s>>>(F); break;
+        case 24: adj_face_kernel<3, 0><<<grid, tb, 0, s>>>(F); break;
+        case 25: adj_face_kernel<3, 1><<<grid, tb, 0, s>>>(F); break;
+        case 26: adj_face_kernel<3, 2><<<grid, tb, 0, s>>>(F); break;
+        case 27: adj_face_kernel<3, 3><<<grid, tb, 0, s>>>(F); break;
+        case 28: adj_face_kernel<3, 4><<<grid, tb, 0, s>>>(F); break;
+        default: adj_face_kernel<3, 5><<<grid, tb, 0, s>>>(F); break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
@@ -1095,9 +1260,10 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.writeB = writeB;
     P.gamma = c->cfg.gamma;
     if (c->cfg.volume_op == FLOU_OP_SPLIT) {
-        if (dim == 1) e = launch_adj_split<1>(c->n, P, s);
-        else if (dim == 2) e = launch_adj_split<2>(c->n, P, s);
-        else e = launch_adj_split<3>(c->n, P, s);
+        const int tp = c->cfg.twopoint_flux;
+        if (dim == 1) e = launch_adj_split<1>(c->n, tp, P, s);
+        else if (dim == 2) e = launch_adj_split<2>(c->n, tp, P, s);
+        else e = launch_adj_split<3>(c->n, tp, P, s);
     } else {
         if (dim == 1) e = launch_adj_elem<1>(c->n, P, s);
         else if (dim == 2) e = launch_adj_elem<2>(c->n, P, s);

@@ -32,8 +32,9 @@ def _split(face_avg="chandra"):
     return F.SplitDivOperator(F.ChandrasekharAverage(), F.LxF(avg, 1.0))
 
 
-# HLL and HLLC carry no dissipation scale: their contexts take no flou_set_dissipation and no dJ/dc
-HLL_FAMILY = ("split_hllc", "strong_hll", "strong_hllc")
+# HLL, HLLC and ScalarDissipation carry no per-element dissipation scale: their contexts take no
+# flou_set_dissipation and no dJ/dc
+HLL_FAMILY = ("split_hllc", "strong_hll", "strong_hllc", "split_sd", "strong_sd")
 
 
 def _with_c(disc, op, c):
@@ -48,7 +49,11 @@ OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("s
              # the headline configuration's pair: Chandrashekar split form with the HLLC interface flux
              "split_hllc": lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()),
              "strong_hll": lambda: F.StrongDivOperator(F.HLL()),
-             "strong_hllc": lambda: F.StrongDivOperator(F.HLLC())}
+             "strong_hllc": lambda: F.StrongDivOperator(F.HLLC()),
+             "split_kg": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
+             "split_sd": lambda: F.SplitDivOperator(F.ChandrasekharAverage(),
+                                                    F.ScalarDissipation(F.ChandrasekharAverage(), 1.0)),
+             "strong_sd": lambda: F.StrongDivOperator(F.ScalarDissipation(F.StdAverage(), 1.0))}
 
 
 CASES = [
@@ -69,7 +74,8 @@ def _disc(case, op="strong"):
     return d
 
 
-@pytest.mark.parametrize("op", ["strong", "split", "split_stdface", "split_hllc", "strong_hll", "strong_hllc"])
+@pytest.mark.parametrize("op", ["strong", "split", "split_stdface", "split_hllc", "strong_hll", "strong_hllc",
+                                "split_kg", "split_sd", "strong_sd"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
 def test_rhs_vjp_dot_product(case, op):
     disc = _disc(case, op)
@@ -123,6 +129,27 @@ def test_hll_family_vjp_through_every_branch(dim, op):
     assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
     with pytest.raises(F.FlouError):   # HLL/HLLC carry no dissipation scale to differentiate
         disc.ctx.set_dissipation(c)
+
+
+@pytest.mark.parametrize("op", ["split_sd", "strong_sd"])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_scalar_dissipation_vjp_with_jumps(dim, op):
+    """ScalarDissipation (Euler.jl:228-301) on a state whose traces jump at every interface, so the
+    dissipation vector D and the wave-speed factor both act, against the oracle's dual numbers."""
+    disc = build(dim, 4, (3,) * dim, F.EulerEquation(dim, 1.4), OPERATORS[op]())
+    rng = np.random.default_rng(41 + dim)
+    eq = disc.equation
+    P = eq.vars_cons2prim(smooth_euler_state(disc, seed=dim))
+    P += np.repeat(0.05 * rng.standard_normal((disc.mesh.nelements, dim + 2)), disc.std.n ** dim, axis=0)
+    Q = np.asfortranarray(eq.vars_prim2cons(P))
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = np.ones(disc.mesh.nelements)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    _, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, 0.0 * c)
+    lhs, rhs = np.sum(_host(Qbar) * dQ), np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
 
 
 def _functional_inputs(disc, seed):
@@ -207,7 +234,7 @@ def test_adjoint_against_central_differences():
         assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
 
 
-@pytest.mark.parametrize("op", ["split", "split_stdface", "split_hllc"])
+@pytest.mark.parametrize("op", ["split", "split_stdface", "split_hllc", "split_kg"])
 def test_split_rhs_vjp_columns(op):
     """Every column of the transposed Jacobian at once on a small 3D case: (∂R/∂Q)ᵀ λ against
     the dual-number JVPs of all unit directions of one element's nodes."""
@@ -250,7 +277,7 @@ def _tgv_state(disc, mach, seed):
     return np.asfortranarray(eq.vars_prim2cons(P))
 
 
-@pytest.mark.parametrize("op", ["split", "strong", "split_hllc"])
+@pytest.mark.parametrize("op", ["split", "strong", "split_hllc", "split_kg", "split_sd"])
 def test_3d_adjoint_solve_against_dual_numbers(op):
     eq = F.EulerEquation(3, 1.4)
     L = 2 * np.pi
