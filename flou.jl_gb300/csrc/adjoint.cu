@@ -1325,25 +1325,32 @@ struct Schedule {
     }
 };
 
-// Single-instance reverse sweep on two streams.  The forward stream `sf` places snapshots and
-// recomputes the state U^k each reverse step needs into one of two X buffers; the adjoint stream
-// `sa` runs the reverse steps.  Recomputation does not depend on the adjoint, so the forward
-// stream runs one reverse step ahead and both kinds of work overlap on the GPU.  Events hand each
-// X buffer from one stream to the other; snapshots are only touched by the forward stream, and
+// Single-instance reverse sweep on three streams.  The forward stream `sf` places snapshots and
+// recomputes the state U^k each reverse step needs into one of NB X buffers; the stage stream `ss`
+// forms that step's two stage states U^(k,1), U^(k,2) from it; the adjoint stream `sa` runs the
+// three adjoint stages.  Neither recomputation depends on the adjoint, so for reverse step k the
+// forward stream can already be recomputing U^(k-1) and the stage stream the stages of step k
+// while the adjoint stream reverses step k+1: three chains of one-wave kernels share the GPU.
+// Events hand each buffer set from stream to stream (ready: X filled, sready: stages filled,
+// done: the adjoint has consumed them); snapshots are only touched by the forward stream, and
 // each stream has its own stage and face-flux scratch.
 struct Solver {
+    static constexpr int NB = 3;
     flou_ctx* c;
-    cudaStream_t sa = nullptr, sf = nullptr;
+    cudaStream_t sa = nullptr, sf = nullptr, ss = nullptr;
     double dt;
     int nsteps;
     std::vector<double*> slot;          // snapshot states; slot[0] = U^0
     std::vector<int> free_slots;
-    double* X[2] = {nullptr, nullptr};
-    cudaEvent_t ready[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr};
-    bool used[2] = {false, false};
+    double* X[NB] = {};
+    double* SX1[NB] = {};
+    double* SX2[NB] = {};
+    cudaEvent_t ready[NB] = {}, sready[NB] = {}, done[NB] = {};
+    bool used[NB] = {};
     int xi = 0;
     double *F1 = nullptr, *Fnf = nullptr;                          // forward stream: stage, face flux
-    double *S1 = nullptr, *S2 = nullptr, *A = nullptr, *Bacc = nullptr, *T = nullptr;   // adjoint stream
+    double* Fns = nullptr;                                         // stage stream: face flux
+    double *A = nullptr, *Bacc = nullptr, *T = nullptr;            // adjoint stream
     double* cbar = nullptr;
     const double* rho_t;
     const double* w;
@@ -1370,26 +1377,31 @@ struct Solver {
         }
         return FLOU_OK;
     }
-    // U^(i0+k) from snapshot si into the next X buffer, then the reverse step i0+k on it.
+    // U^(i0+k) from snapshot si into the next buffer set, its stage states, then the reverse step
+    // i0+k on them.
     int step_from(int si, int k, int kstep) {
         int r;
         int b = xi;
-        xi ^= 1;
+        xi = (xi + 1) % NB;
         if (used[b] && (r = cuda(cudaStreamWaitEvent(sf, done[b], 0), "event wait"))) return r;
         if ((r = copy(X[b], slot[si]))) return r;
         if ((r = advance(X[b], k))) return r;
         if ((r = cuda(cudaEventRecord(ready[b], sf), "event record"))) return r;
-        if ((r = cuda(cudaStreamWaitEvent(sa, ready[b], 0), "event wait"))) return r;
-        if ((r = backward_step(kstep, X[b]))) return r;
+        // the stage stream: U^(k,1) and U^(k,2) (it waits for ready[b], which the forward stream
+        // records after its own wait for done[b], so the stage buffers are free again)
+        if ((r = cuda(cudaStreamWaitEvent(ss, ready[b], 0), "event wait"))) return r;
+        if ((r = ctx_stage(c, ss, X[b], X[b], SX1[b], 1, dt, 0.0, 1.0, Fns))) return r;
+        if ((r = ctx_stage(c, ss, SX1[b], X[b], SX2[b], 2, dt, 0.75, 0.25, Fns))) return r;
+        if ((r = cuda(cudaEventRecord(sready[b], ss), "event record"))) return r;
+        if ((r = cuda(cudaStreamWaitEvent(sa, sready[b], 0), "event wait"))) return r;
+        if ((r = backward_step(kstep, X[b], SX1[b], SX2[b]))) return r;
         used[b] = true;
         return cuda(cudaEventRecord(done[b], sa), "event record");
     }
-    // Reverse one step from U^k held in Xk: the adjoint of U^(k+1) is in A on entry and that of
-    // U^k on exit (adjoint stream).
-    int backward_step(int k, double* Xk) {
+    // Reverse one step from U^k (Xk) and its stage states (S1, S2): the adjoint of U^(k+1) is in
+    // A on entry and that of U^k on exit (adjoint stream).
+    int backward_step(int k, double* Xk, double* S1, double* S2) {
         int r;
-        if ((r = ctx_stage(c, sa, Xk, Xk, S1, 1, dt, 0.0, 1.0))) return r;             // U1
-        if ((r = ctx_stage(c, sa, S1, Xk, S2, 2, dt, 0.75, 0.25))) return r;          // U2
         if (!seeded) {   // the last step: form U^n, the functional and its gradient seed
             if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
             if ((r = ctx_stage(c, sa, S2, Xk, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;   // U^n
@@ -1603,6 +1615,7 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     int nslots = std::min(nsnap, std::max(nsteps - 1, 0));
     std::vector<double*> owned;
     cudaError_t e = cudaStreamCreateWithFlags(&S.sf, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.ss, cudaStreamNonBlocking);
     auto dalloc = [&](double** p, size_t b) {
         if (e != cudaSuccess) return;
         e = cudaMalloc((void**)p, b);
@@ -1610,12 +1623,19 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     };
     S.slot.assign(nslots + 1, nullptr);
     for (int i = 0; i <= nslots; ++i) dalloc(&S.slot[i], S.bytes);
-    double** bufs[] = {&S.X[0], &S.X[1], &S.F1, &S.S1, &S.S2, &S.Bacc, &S.T};
+    for (int i = 0; i < Solver::NB; ++i) {
+        dalloc(&S.X[i], S.bytes);
+        dalloc(&S.SX1[i], S.bytes);
+        dalloc(&S.SX2[i], S.bytes);
+    }
+    double** bufs[] = {&S.F1, &S.Bacc, &S.T};
     for (double** b : bufs) dalloc(b, S.bytes);
     dalloc(&S.Fnf, (size_t)c->nfdofs * c->nv * sizeof(double));
+    dalloc(&S.Fns, (size_t)c->nfdofs * c->nv * sizeof(double));
     dalloc(&S.partial, S.nblk * sizeof(double));
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    for (int i = 0; i < Solver::NB && e == cudaSuccess; ++i) {
         e = cudaEventCreateWithFlags(&S.ready[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.sready[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.done[i], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&S.h_partial, S.nblk * sizeof(double));
@@ -1644,20 +1664,24 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     }
     if (!rr) rr = S.rev(0, nsteps, nslots, 0);
     cudaError_t e1 = S.sf ? cudaStreamSynchronize(S.sf) : cudaSuccess;
+    cudaError_t e3 = S.ss ? cudaStreamSynchronize(S.ss) : cudaSuccess;
     cudaError_t e2 = cudaStreamSynchronize(S.sa);
+    if (e1 == cudaSuccess) e1 = e3;
     if (!rr && (e1 != cudaSuccess || e2 != cudaSuccess))
         rr = ctx_cuda_fail(c, e1 != cudaSuccess ? e1 : e2, "adjoint solve");
     double Jv = 0.0;
     if (!rr)
         for (int b = 0; b < S.nblk; ++b) Jv += S.h_partial[b];
     free_adj(S.ab);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < Solver::NB; ++i) {
         if (S.ready[i]) cudaEventDestroy(S.ready[i]);
+        if (S.sready[i]) cudaEventDestroy(S.sready[i]);
         if (S.done[i]) cudaEventDestroy(S.done[i]);
     }
     if (S.h_partial) cudaFreeHost(S.h_partial);
     for (double* p : owned) cudaFree(p);
     if (S.sf) cudaStreamDestroy(S.sf);
+    if (S.ss) cudaStreamDestroy(S.ss);
     if (rr) return rr;
     if (J) *J = Jv;
     if (forward_steps) *forward_steps = S.advances;
