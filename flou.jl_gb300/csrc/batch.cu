@@ -3,7 +3,8 @@
 // queue, and the three stages of a step are replayed as one CUDA graph.
 //
 // Work queue of one stage: first every face item of every instance (TB face nodes each), then
-// every element item (one element tile of the instance's order).  Blocks take items with an
+// every element item (G consecutive element tiles of the instance's order, G chosen per order by
+// the autotuner).  Blocks take items with an
 // atomic counter.  An element item needs the face fluxes of its instance; because all face
 // items precede all element items in the queue, they have all been taken by running blocks
 // when an element item is taken, so the wait below always ends.  It is still bounded: after
@@ -29,7 +30,7 @@ struct BatchArgs {
     const int32_t* inst_n;       // nodes per direction
     const int32_t* inst_lgl;     // basis with boundary nodes
     const int32_t* nface_items;  // face items per instance
-    const int2* items;           // (instance | kind << 30, first face node or element)
+    const int2* items;           // (instance | (G - 1) << 27 | kind << 30, first face node or element)
     int32_t nitems;
     int32_t ninst;
     int32_t* counter;            // [0] queue head, [1] abort flag, [2 + k] face items done of instance k
@@ -39,13 +40,20 @@ struct BatchArgs {
 
 // One call per order, not inlined: each order's tile gets its own register allocation instead
 // of the union of all orders (which would limit the persistent kernel to one block per SM).
+// G consecutive tiles of EPB elements each (the last ones may run past the instance's elements).
 template <int DIM, int N, int EQ, int VOL, int TP, int TB>
-__device__ __noinline__ void batch_tile_n(const ElemParams& P, int lgl, int e0, double* smem) {
-    if (VOL == FLOU_OP_STRONG) {
-        if (lgl) strong_tile<DIM, N, EQ, true, TB>(P, e0, smem);
-        else strong_tile<DIM, N, EQ, false, TB>(P, e0, smem);
-    } else {
-        split_tile<DIM, N, EQ, TP, true, TB>(P, e0, smem);
+__device__ __noinline__ void batch_tile_n(const ElemParams& P, int lgl, int e0, int G, double* smem) {
+    constexpr int EPB = Shape<DIM, N, TB>::EPB;
+    for (int g = 0; g < G; ++g) {
+        const int e = e0 + g * EPB;
+        if (e >= P.nelem) break;   // uniform over the block
+        if (g > 0) __syncthreads();   // the previous tile's last phase may still read shared memory
+        if (VOL == FLOU_OP_STRONG) {
+            if (lgl) strong_tile<DIM, N, EQ, true, TB>(P, e, smem);
+            else strong_tile<DIM, N, EQ, false, TB>(P, e, smem);
+        } else {
+            split_tile<DIM, N, EQ, TP, true, TB>(P, e, smem);
+        }
     }
 }
 
@@ -56,15 +64,15 @@ __device__ __noinline__ void batch_face(const FaceParams& P, int64_t gid, int lg
 }
 
 template <int DIM, int EQ, int VOL, int TP, int TB>
-__device__ __forceinline__ void batch_tile(const ElemParams& P, int n, int lgl, int e0, double* smem) {
+__device__ __forceinline__ void batch_tile(const ElemParams& P, int n, int lgl, int e0, int G, double* smem) {
     switch (n) {
-        case 2: batch_tile_n<DIM, 2, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        case 3: batch_tile_n<DIM, 3, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        case 4: batch_tile_n<DIM, 4, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        case 5: batch_tile_n<DIM, 5, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        case 6: batch_tile_n<DIM, 6, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        case 7: batch_tile_n<DIM, 7, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
-        default: batch_tile_n<DIM, 8, EQ, VOL, TP, TB>(P, lgl, e0, smem); break;
+        case 2: batch_tile_n<DIM, 2, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        case 3: batch_tile_n<DIM, 3, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        case 4: batch_tile_n<DIM, 4, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        case 5: batch_tile_n<DIM, 5, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        case 6: batch_tile_n<DIM, 6, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        case 7: batch_tile_n<DIM, 7, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
+        default: batch_tile_n<DIM, 8, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
     }
 }
 
@@ -80,7 +88,7 @@ __global__ void __launch_bounds__(TB, (TB >= 512 ? 1 : 1024 / TB)) batch_stage_k
         __syncthreads();
         if (it >= A.nitems) break;
         const int2 w = A.items[it];
-        const int inst = w.x & 0x3fffffff;
+        const int inst = w.x & 0x07ffffff;
         if (!index_ok(inst, A.ninst, A.status, 0)) continue;
         if ((w.x >> 30) == 0) {
             const FaceParams& fp = A.fp[inst];
@@ -107,7 +115,8 @@ __global__ void __launch_bounds__(TB, (TB >= 512 ? 1 : 1024 / TB)) batch_stage_k
                 __threadfence();
             }
             __syncthreads();
-            batch_tile<DIM, EQ, VOL, TP, TB>(A.ep[inst], A.inst_n[inst], A.inst_lgl[inst], w.y, smem);
+            batch_tile<DIM, EQ, VOL, TP, TB>(A.ep[inst], A.inst_n[inst], A.inst_lgl[inst], w.y,
+                                             ((w.x >> 27) & 7) + 1, smem);
         }
     }
 }
@@ -158,6 +167,7 @@ struct flou_batch {
     std::vector<const BatchKernel*> kernels;   // candidates for this batch's equation/operator
     const BatchKernel* kern = nullptr;
     int blocks_per_sm = 0, order = 0, sms = 0;
+    int tiles[MAXN + 1] = {};   // element tiles per work item for n nodes per direction (0: one)
     std::vector<double*> Q;
     std::vector<double> dt;
     bool have_states = false;
@@ -222,7 +232,8 @@ int build_items(flou_batch* b) {
     for (int k : korder) {
         flou_ctx* c = b->ctxs[k];
         int epb = epb_of(c->npe, b->kern->tb);
-        for (int e = 0; e < c->nelem; e += epb) items.push_back(make_int2(k | (1 << 30), e));
+        int G = std::max(1, std::min(8, b->tiles[c->n]));
+        for (int e = 0; e < c->nelem; e += epb * G) items.push_back(make_int2(k | ((G - 1) << 27) | (1 << 30), e));
     }
     if (items.size() > 0x7fffffff) return bfail(b, FLOU_ERR_ARG, "too many work items");
     if (b->d_items) cudaFree(b->d_items);
@@ -313,7 +324,7 @@ extern "C" {
 const char* flou_batch_last_error(const flou_batch* b) { return b ? b->err.c_str() : "null batch"; }
 
 int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
-    if (!out || n <= 0 || !ctxs) return FLOU_ERR_ARG;
+    if (!out || n <= 0 || n >= (1 << 27) || !ctxs) return FLOU_ERR_ARG;
     *out = nullptr;
     flou_batch* b = new flou_batch();
     b->n = n;
@@ -441,7 +452,10 @@ int32_t flou_batch_step(flou_batch* b, int32_t nsteps) {
 
 // Chooses the block size (elements per tile follow from it: tb / n^d per order), the resident
 // blocks per SM and the element-item order by timing the first stage (which writes only the
-// stage buffers) for every candidate.  out = {threads per block, blocks per SM, order}.
+// stage buffers) for every candidate, then, order by order, how many element tiles one work item
+// holds (1, 2 or 4: larger items take fewer queue operations and face-count checks, smaller ones
+// balance the tail), each against the timing of the current choice.  out = {threads per block,
+// blocks per SM, order}; flou_batch_tiles reads the per-order tiles per item.
 int32_t flou_batch_autotune(flou_batch* b, int32_t* out) {
     if (!b) return FLOU_ERR_ARG;
     if (!b->have_states) return bfail(b, FLOU_ERR_STATE, "flou_batch_set_states has not been called");
@@ -475,16 +489,70 @@ int32_t flou_batch_autotune(flou_batch* b, int32_t* out) {
             }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     b->kern = bk;
     b->blocks_per_sm = bb;
     b->order = bo;
-    int r = build_items(b);
+    // tiles per element item, one order at a time (coordinate search from one tile everywhere)
+    auto time_stage = [&](float* ms_out) -> int {
+        int r = build_items(b);
+        if (r) return r;
+        float tot = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {
+            BCK(cudaEventRecord(e0, b->stream), "event");
+            if ((r = launch_stage(b, 0, b->stream))) return r;
+            BCK(cudaEventRecord(e1, b->stream), "event");
+            BCK(cudaEventSynchronize(e1), "event");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) tot += ms;
+        }
+        *ms_out = tot;
+        return FLOU_OK;
+    };
+    bool present[MAXN + 1] = {};
+    for (flou_ctx* c : b->ctxs) present[c->n] = true;
+    for (int n = 0; n <= MAXN; ++n) b->tiles[n] = 1;
+    float cur = 0.f;
+    int r = time_stage(&cur);
+    if (r) return r;
+    for (int n = 2; n <= MAXN; ++n) {
+        if (!present[n]) continue;
+        int bestG = b->tiles[n];
+        for (int G : {2, 4}) {
+            b->tiles[n] = G;
+            float t = 0.f;
+            if ((r = time_stage(&t))) return r;
+            if (t < cur) { cur = t; bestG = G; }
+        }
+        b->tiles[n] = bestG;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r = build_items(b);
     if (r) return r;
     drop_graph(b);
     if (out) { out[0] = bk->tb; out[1] = bb; out[2] = bo; }
     return check_status(b);
+}
+
+// Element tiles per work item for n = 2..MAXN nodes per direction (tiles[n - 2]; 1 before tuning).
+int32_t flou_batch_tiles(const flou_batch* b, int32_t* tiles) {
+    if (!b || !tiles) return FLOU_ERR_ARG;
+    for (int n = 2; n <= MAXN; ++n) tiles[n - 2] = std::max(1, b->tiles[n]);
+    return FLOU_OK;
+}
+
+// Sets the element tiles per work item of every order (1..8 each) instead of tuning them.
+int32_t flou_batch_set_tiles(flou_batch* b, const int32_t* tiles) {
+    if (!b || !tiles) return FLOU_ERR_ARG;
+    for (int n = 2; n <= MAXN; ++n)
+        if (tiles[n - 2] < 1 || tiles[n - 2] > 8)
+            return bfail(b, FLOU_ERR_ARG, "tiles per work item must be 1..8 (order " + std::to_string(n - 1) + ")");
+    for (int n = 2; n <= MAXN; ++n) b->tiles[n] = tiles[n - 2];
+    int r = build_items(b);
+    if (r) return r;
+    drop_graph(b);
+    return FLOU_OK;
 }
 
 // Fault-injection hook for tests: the face items of instance `inst` never report completion,

@@ -129,6 +129,8 @@ PROTOTYPES = {
     "flou_batch_set_states": [_P, ctypes.POINTER(_P), _D],
     "flou_batch_step": [_P, ctypes.c_int32],
     "flou_batch_autotune": [_P, _I32],
+    "flou_batch_tiles": [_P, _I32],
+    "flou_batch_set_tiles": [_P, _I32],
     "flou_batch_test_skip_faces": [_P, ctypes.c_int32],
 }
 

@@ -51,9 +51,24 @@ class Batch:
         self._check(self._lib.flou_batch_step(self.h, int(nsteps)))
 
     def autotune(self):
+        """Times the candidate launch shapes and keeps the fastest: threads per block (which sets
+        the elements per tile of every order), resident blocks per SM, the element-item order, and
+        per order the number of element tiles one work item holds."""
         out = (ctypes.c_int32 * 3)()
         self._check(self._lib.flou_batch_autotune(self.h, out))
-        return {"threads_per_block": out[0], "blocks_per_sm": out[1], "order": "by_order_desc" if out[2] else "by_instance"}
+        return {"threads_per_block": out[0], "blocks_per_sm": out[1], "order": "by_order_desc" if out[2] else "by_instance",
+                "tiles_per_item": self.tiles_per_item()}
+
+    def set_tiles_per_item(self, tiles):
+        """Fixes the element tiles per work item: an int for every order or {p: tiles}."""
+        t = (ctypes.c_int32 * 7)(*[int(tiles.get(p, 1) if isinstance(tiles, dict) else tiles) for p in range(1, 8)])
+        self._check(self._lib.flou_batch_set_tiles(self.h, t))
+
+    def tiles_per_item(self):
+        """{p: element tiles per work item} for the orders p = 1..7."""
+        t = (ctypes.c_int32 * 7)()
+        self._check(self._lib.flou_batch_tiles(self.h, t))
+        return {n + 1: t[n] for n in range(7)}
 
     def test_skip_faces(self, inst):
         self._check(self._lib.flou_batch_test_skip_faces(self.h, int(inst)))

@@ -354,6 +354,12 @@ int32_t flou_batch_step(flou_batch* b, int32_t nsteps);
 /* Autotuner: times the first stage for every (threads per block, resident blocks per SM,
  * element-item order) candidate and keeps the fastest; out = {threads, blocks/SM, order}. */
 int32_t flou_batch_autotune(flou_batch* b, int32_t* out);
+/* Element tiles per work item the autotuner chose for each order (tiles[n - 2] for n = 2..8 nodes
+ * per direction; 1 before tuning).  No counterpart in the reference. */
+int32_t flou_batch_tiles(const flou_batch* b, int32_t* tiles);
+/* Sets those tiles per work item (1..8 for each of the 7 orders) instead of tuning them.  No
+ * counterpart in the reference. */
+int32_t flou_batch_set_tiles(flou_batch* b, const int32_t* tiles);
 /* Fault-injection hook for tests: instance `inst`'s face items never report completion, so its
  * element tiles run out of their bounded wait; -1 restores normal operation. */
 int32_t flou_batch_test_skip_faces(flou_batch* b, int32_t inst);

@@ -70,9 +70,27 @@ def test_batch_autotune_keeps_results():
     b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
     choice = b.autotune()
     assert choice["threads_per_block"] in (128, 256) and choice["blocks_per_sm"] >= 1
+    assert set(choice["tiles_per_item"].values()) <= {1, 2, 4}
     b.step(2)
     for q, r in zip(states, ref):
         assert torch.equal(q, r)
+
+
+@pytest.mark.parametrize("tiles", [3, 8, {1: 2, 2: 4, 3: 1, 4: 5, 5: 2, 6: 3, 7: 8}])
+def test_batch_tiles_per_item_keep_results(tiles):
+    """Work items of several element tiles (the last tile of an instance may run past its
+    elements) give the serial results bit for bit."""
+    insts = _instances_2d(seed=4, count=6)
+    ref = _serial(insts, 2)
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.set_tiles_per_item(tiles)
+    assert b.tiles_per_item() == ({p: tiles for p in range(1, 8)} if isinstance(tiles, int) else tiles)
+    b.step(2)
+    for q, r in zip(states, ref):
+        assert torch.equal(q, r)
+    with pytest.raises(F.FlouError):
+        b.set_tiles_per_item(9)
 
 
 def test_batch_instance_against_oracle():
