@@ -1325,30 +1325,35 @@ struct Schedule {
     }
 };
 
-// Single-instance reverse sweep on three streams.  The forward stream `sf` places snapshots and
-// recomputes the state U^k each reverse step needs into one of NB X buffers; the stage stream `ss`
-// forms that step's two stage states U^(k,1), U^(k,2) from it; the adjoint stream `sa` runs the
-// three adjoint stages.  Neither recomputation depends on the adjoint, so for reverse step k the
-// forward stream can already be recomputing U^(k-1) and the stage stream the stages of step k
-// while the adjoint stream reverses step k+1: three chains of one-wave kernels share the GPU.
-// Events hand each buffer set from stream to stream (ready: X filled, sready: stages filled,
-// done: the adjoint has consumed them); snapshots are only touched by the forward stream, and
-// each stream has its own stage and face-flux scratch.
+// Single-instance reverse sweep on four streams.  Two forward streams `sf[0..1]` take turns: each
+// places snapshots and recomputes the state U^k that a reverse step needs, into one of NB X
+// buffers; the stage stream `ss` forms that step's two stage states U^(k,1), U^(k,2); the adjoint
+// stream `sa` runs the three adjoint stages.  None of the recomputation depends on the adjoint,
+// so while the adjoint stream reverses step k+1, the stage stream forms the stages of step k and
+// the forward streams recompute U^(k-1) and U^(k-2) side by side: four chains of one-wave kernels
+// share the GPU.  Events order every hand-over: X filled (ready) -> stages filled (sready) ->
+// consumed (done); per snapshot, the event of its last placement (written) and of the last copy
+// each forward stream made from it (read), so a slot is only rewritten after its readers and
+// only read after its writer.  Each stream has its own stage and face-flux scratch.
 struct Solver {
-    static constexpr int NB = 3;
+    static constexpr int NB = 3, NF = 2;
     flou_ctx* c;
-    cudaStream_t sa = nullptr, sf = nullptr, ss = nullptr;
+    cudaStream_t sa = nullptr, ss = nullptr;
+    cudaStream_t sf[NF] = {};
     double dt;
     int nsteps;
     std::vector<double*> slot;          // snapshot states; slot[0] = U^0
     std::vector<int> free_slots;
+    std::vector<cudaEvent_t> written;   // [slot]
+    std::vector<cudaEvent_t> read;      // [slot * NF + f]
     double* X[NB] = {};
     double* SX1[NB] = {};
     double* SX2[NB] = {};
     cudaEvent_t ready[NB] = {}, sready[NB] = {}, done[NB] = {};
     bool used[NB] = {};
-    int xi = 0;
-    double *F1 = nullptr, *Fnf = nullptr;                          // forward stream: stage, face flux
+    int xi = 0, fi = 0;
+    double* F1[NF] = {};                                           // forward streams: stage scratch
+    double* Fnf[NF] = {};                                          // and face fluxes
     double* Fns = nullptr;                                         // stage stream: face flux
     double *A = nullptr, *Bacc = nullptr, *T = nullptr;            // adjoint stream
     double* cbar = nullptr;
@@ -1364,18 +1369,40 @@ struct Solver {
     size_t bytes = 0;
 
     int cuda(cudaError_t e, const char* what) { return e == cudaSuccess ? FLOU_OK : ctx_cuda_fail(c, e, what); }
-    int copy(double* dst, const double* src) {
-        return cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, sf), "state copy");
+    int wait(cudaStream_t s, cudaEvent_t e) { return cuda(cudaStreamWaitEvent(s, e, 0), "event wait"); }
+    int record(cudaEvent_t e, cudaStream_t s) { return cuda(cudaEventRecord(e, s), "event record"); }
+    int next_f() {
+        int f = fi;
+        fi = (fi + 1) % NF;
+        return f;
     }
-    int advance(double* Q, int k) {   // k SSP-RK3 steps in place on the forward stream
+    // dst <- slot si on forward stream f, after the slot's writer; marks the read
+    int copy_from(int f, double* dst, int si) {
+        int r;
+        if ((r = wait(sf[f], written[si]))) return r;
+        if ((r = cuda(cudaMemcpyAsync(dst, slot[si], bytes, cudaMemcpyDeviceToDevice, sf[f]), "state copy"))) return r;
+        return record(read[(size_t)si * NF + f], sf[f]);
+    }
+    int advance(int f, double* Q, int k) {   // k SSP-RK3 steps in place on forward stream f
         for (int i = 0; i < k; ++i) {
             int r;
-            if ((r = ctx_stage(c, sf, Q, Q, F1, 1, dt, 0.0, 1.0, Fnf))) return r;
-            if ((r = ctx_stage(c, sf, F1, Q, F1, 2, dt, 0.75, 0.25, Fnf))) return r;
-            if ((r = ctx_stage(c, sf, F1, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf))) return r;
+            if ((r = ctx_stage(c, sf[f], Q, Q, F1[f], 1, dt, 0.0, 1.0, Fnf[f]))) return r;
+            if ((r = ctx_stage(c, sf[f], F1[f], Q, F1[f], 2, dt, 0.75, 0.25, Fnf[f]))) return r;
+            if ((r = ctx_stage(c, sf[f], F1[f], Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf[f]))) return r;
             ++advances;
         }
         return FLOU_OK;
+    }
+    // slot sj <- U^(i0+m) advanced from slot si (a snapshot placement)
+    int place(int sj, int si, int m) {
+        int r;
+        int f = next_f();
+        for (int g = 0; g < NF; ++g)   // earlier readers of sj, on either forward stream
+            if ((r = wait(sf[f], read[(size_t)sj * NF + g]))) return r;
+        if ((r = wait(sf[f], written[sj]))) return r;
+        if ((r = copy_from(f, slot[sj], si))) return r;
+        if ((r = advance(f, slot[sj], m))) return r;
+        return record(written[sj], sf[f]);
     }
     // U^(i0+k) from snapshot si into the next buffer set, its stage states, then the reverse step
     // i0+k on them.
@@ -1383,20 +1410,21 @@ struct Solver {
         int r;
         int b = xi;
         xi = (xi + 1) % NB;
-        if (used[b] && (r = cuda(cudaStreamWaitEvent(sf, done[b], 0), "event wait"))) return r;
-        if ((r = copy(X[b], slot[si]))) return r;
-        if ((r = advance(X[b], k))) return r;
-        if ((r = cuda(cudaEventRecord(ready[b], sf), "event record"))) return r;
-        // the stage stream: U^(k,1) and U^(k,2) (it waits for ready[b], which the forward stream
-        // records after its own wait for done[b], so the stage buffers are free again)
-        if ((r = cuda(cudaStreamWaitEvent(ss, ready[b], 0), "event wait"))) return r;
+        int f = next_f();
+        if (used[b] && (r = wait(sf[f], done[b]))) return r;
+        if ((r = copy_from(f, X[b], si))) return r;
+        if ((r = advance(f, X[b], k))) return r;
+        if ((r = record(ready[b], sf[f]))) return r;
+        // the stage stream: U^(k,1) and U^(k,2) (ready[b] comes after the forward stream's wait for
+        // done[b], so the stage buffers are free again)
+        if ((r = wait(ss, ready[b]))) return r;
         if ((r = ctx_stage(c, ss, X[b], X[b], SX1[b], 1, dt, 0.0, 1.0, Fns))) return r;
         if ((r = ctx_stage(c, ss, SX1[b], X[b], SX2[b], 2, dt, 0.75, 0.25, Fns))) return r;
-        if ((r = cuda(cudaEventRecord(sready[b], ss), "event record"))) return r;
-        if ((r = cuda(cudaStreamWaitEvent(sa, sready[b], 0), "event wait"))) return r;
+        if ((r = record(sready[b], ss))) return r;
+        if ((r = wait(sa, sready[b]))) return r;
         if ((r = backward_step(kstep, X[b], SX1[b], SX2[b]))) return r;
         used[b] = true;
-        return cuda(cudaEventRecord(done[b], sa), "event record");
+        return record(done[b], sa);
     }
     // Reverse one step from U^k (Xk) and its stage states (S1, S2): the adjoint of U^(k+1) is in
     // A on entry and that of U^k on exit (adjoint stream).
@@ -1432,8 +1460,7 @@ struct Solver {
         if (m < 1 || m >= n) m = n / 2;
         int sj = free_slots.back();
         free_slots.pop_back();
-        if ((r = copy(slot[sj], slot[si]))) return r;
-        if ((r = advance(slot[sj], m))) return r;
+        if ((r = place(sj, si, m))) return r;
         if ((r = rev(i0 + m, n - m, ns - 1, sj))) return r;
         free_slots.push_back(sj);
         return rev(i0, m, ns, si);
@@ -1614,8 +1641,8 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     S.A = dJdQ0;   // the adjoint state lives in the output
     int nslots = std::min(nsnap, std::max(nsteps - 1, 0));
     std::vector<double*> owned;
-    cudaError_t e = cudaStreamCreateWithFlags(&S.sf, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.ss, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&S.ss, cudaStreamNonBlocking);
+    for (int f = 0; f < Solver::NF && e == cudaSuccess; ++f) e = cudaStreamCreateWithFlags(&S.sf[f], cudaStreamNonBlocking);
     auto dalloc = [&](double** p, size_t b) {
         if (e != cudaSuccess) return;
         e = cudaMalloc((void**)p, b);
@@ -1628,10 +1655,19 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
         dalloc(&S.SX1[i], S.bytes);
         dalloc(&S.SX2[i], S.bytes);
     }
-    double** bufs[] = {&S.F1, &S.Bacc, &S.T};
+    double** bufs[] = {&S.Bacc, &S.T};
     for (double** b : bufs) dalloc(b, S.bytes);
-    dalloc(&S.Fnf, (size_t)c->nfdofs * c->nv * sizeof(double));
+    for (int f = 0; f < Solver::NF; ++f) {
+        dalloc(&S.F1[f], S.bytes);
+        dalloc(&S.Fnf[f], (size_t)c->nfdofs * c->nv * sizeof(double));
+    }
     dalloc(&S.Fns, (size_t)c->nfdofs * c->nv * sizeof(double));
+    S.written.assign(nslots + 1, nullptr);
+    S.read.assign((size_t)(nslots + 1) * Solver::NF, nullptr);
+    for (auto& ev : S.written)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (auto& ev : S.read)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     dalloc(&S.partial, S.nblk * sizeof(double));
     for (int i = 0; i < Solver::NB && e == cudaSuccess; ++i) {
         e = cudaEventCreateWithFlags(&S.ready[i], cudaEventDisableTiming);
@@ -1650,20 +1686,26 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     Schedule sch(nsteps, nslots);
     S.sch = &sch;
     for (int i = 1; i <= nslots; ++i) S.free_slots.push_back(i);
-    if (!rr) {   // the forward stream starts after what the caller queued on the context's stream
+    if (!rr) {   // the forward streams start after what the caller queued on the context's stream
         cudaEvent_t ev;
         e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(ev, S.sa);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(S.sf, ev, 0);
+        for (int f = 0; f < Solver::NF && e == cudaSuccess; ++f) e = cudaStreamWaitEvent(S.sf[f], ev, 0);
         if (e == cudaSuccess) cudaEventDestroy(ev);
         if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "stream order");
     }
     if (!rr) {
-        e = cudaMemcpyAsync(S.slot[0], Q0, S.bytes, cudaMemcpyDeviceToDevice, S.sf);
+        e = cudaMemcpyAsync(S.slot[0], Q0, S.bytes, cudaMemcpyDeviceToDevice, S.sf[0]);
+        if (e == cudaSuccess) e = cudaEventRecord(S.written[0], S.sf[0]);
         if (e != cudaSuccess) rr = ctx_cuda_fail(c, e, "state copy");
     }
     if (!rr) rr = S.rev(0, nsteps, nslots, 0);
-    cudaError_t e1 = S.sf ? cudaStreamSynchronize(S.sf) : cudaSuccess;
+    cudaError_t e1 = cudaSuccess;
+    for (int f = 0; f < Solver::NF; ++f)
+        if (S.sf[f]) {
+            cudaError_t ef = cudaStreamSynchronize(S.sf[f]);
+            if (e1 == cudaSuccess) e1 = ef;
+        }
     cudaError_t e3 = S.ss ? cudaStreamSynchronize(S.ss) : cudaSuccess;
     cudaError_t e2 = cudaStreamSynchronize(S.sa);
     if (e1 == cudaSuccess) e1 = e3;
@@ -1678,9 +1720,14 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
         if (S.sready[i]) cudaEventDestroy(S.sready[i]);
         if (S.done[i]) cudaEventDestroy(S.done[i]);
     }
+    for (auto ev : S.written)
+        if (ev) cudaEventDestroy(ev);
+    for (auto ev : S.read)
+        if (ev) cudaEventDestroy(ev);
     if (S.h_partial) cudaFreeHost(S.h_partial);
     for (double* p : owned) cudaFree(p);
-    if (S.sf) cudaStreamDestroy(S.sf);
+    for (int f = 0; f < Solver::NF; ++f)
+        if (S.sf[f]) cudaStreamDestroy(S.sf[f]);
     if (S.ss) cudaStreamDestroy(S.ss);
     if (rr) return rr;
     if (J) *J = Jv;
