@@ -546,12 +546,178 @@ __device__ __forceinline__ void sd_jump_vjp(const double* a, const double* b, co
     (void)NV;
 }
 
+// The matrix-dissipation part of MatrixDissipation (Euler.jl:303-380, in the factorised form the
+// forward face kernel evaluates), F = A + ½ · intensity · o with o = R |Λ| T Rᵀ ΔW:
+//   ΔW = (L_β/(γ-1) + L_ρ - (|v_l|² β_l - |v_r|² β_r), 2(β_l v_l - β_r v_r), -2(β_l - β_r)),
+//   L_x = ln(x_l/x_r), β = ρ/(2p); at the averaged state (ρ_ln, v̄ = (v_l+v_r)/2, p̂, β_ln):
+//   a² = γ p̂/ρ_ln, h = γ/(2(γ-1)β_ln) + ½ v2, v2 = 2|v̄|² - ½(|v_l|² + |v_r|²), u = v̄_1;
+//   y = Rᵀ ΔW, z = |Λ| T y (|u ∓ a| ρ_ln/(2γ), |u| (γ-1) ρ_ln/γ, |u| p̂), o = R z.
+// ob = ½ · intensity · (the flux cotangent).  Adds the cotangents of both sides' densities to
+// qa[0], qb[0] and those of their velocities and pressures to L, R.  |x| differentiates as Base's
+// abs on the dual numbers: -1 when the sign bit is set, else +1.
+template <int DIM>
+__device__ __forceinline__ void md_vjp(const Prim& pa, const Prim& pb, double g, const double* ob, double* qa,
+                                       double* qb, SideBar& L, SideBar& R) {
+    constexpr int NV = DIM + 2, E = DIM + 1;
+    const double g1 = g - 1.0, ig1 = 1.0 / g1, ig = 1.0 / g;
+    const double rl = pa.rho, rr = pb.rho, pl = pa.p, pr = pb.p;
+    const double* vl = pa.v;
+    const double* vr = pb.v;
+    const double vl2 = pa.vv, vr2 = pb.vv;
+    const double ipl = rcp_refined(pl), ipr = rcp_refined(pr);
+    const double bl = 0.5 * rl * ipl, br = 0.5 * rr * ipr;
+    const double sr = rl + rr, sb = bl + br;
+    // logarithmic means with their derivatives (logmean_half takes halved values)
+    double rho, irho, dra, drb, bet, ibet, dba, dbb;
+    logmean_half(0.5 * rl, 0.5 * rr, 0.5 * sr, 0.5 * (rl - rr), rcp_refined(0.5 * sr), rho, irho, dra, drb);
+    logmean_half(0.5 * bl, 0.5 * br, 0.5 * sb, 0.5 * (bl - br), rcp_refined(0.5 * sb), bet, ibet, dba, dbb);
+    const double Lr = log(rl * pb.ir), Lb = log(bl * rcp_refined(br));
+    const double isb = rcp_refined(sb), phat = 0.5 * sr * isb;
+    double vm[3] = {0.0, 0.0, 0.0}, vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vm[k] = 0.5 * (vl[k] + vr[k]);
+        vv = fma(vm[k], vm[k], vv);
+    }
+    const double v2 = fma(2.0, vv, -0.5 * (vl2 + vr2));
+    const double a2 = g * phat * irho, ia = rsqrt_refined(a2), a = a2 * ia;
+    const double h = fma(0.5 * g * ig1, ibet, 0.5 * v2);
+    double dW[NV];
+    dW[0] = fma(Lb, ig1, Lr) - (vl2 * bl - vr2 * br);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) dW[1 + k] = 2.0 * (bl * vl[k] - br * vr[k]);
+    dW[E] = -2.0 * (bl - br);
+    const double u = vm[0];
+    double S = fma(u, dW[1], dW[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) S = fma(vm[k], dW[1 + k], S);
+    double y[NV];
+    y[0] = S - a * dW[1] + (h - u * a) * dW[E];
+    y[E] = S + a * dW[1] + (h + u * a) * dW[E];
+    y[1] = fma(0.5 * v2, dW[E], S);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) y[1 + k] = fma(vm[k], dW[E], dW[1 + k]);
+    const double ta = rho * (0.5 * ig), c1 = g1 * rho * ig;
+    const double um = u - a, up = u + a;
+    const double sm = signbit(um) ? -1.0 : 1.0, sp = signbit(up) ? -1.0 : 1.0, su = signbit(u) ? -1.0 : 1.0;
+    const double aum = fabs(um), aup = fabs(up), au = fabs(u);
+    double z[NV];
+    z[0] = aum * ta * y[0];
+    z[1] = au * c1 * y[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) z[1 + k] = au * phat * y[1 + k];
+    z[E] = aup * ta * y[E];
+    const double zs = z[0] + z[1] + z[E];
+    // reverse: o = R z
+    double vmo = 0.0;   // Σ_{k≥1} v̄_k ō_{1+k}
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vmo = fma(vm[k], ob[1 + k], vmo);
+    double zb[NV];
+    zb[0] = ob[0] + um * ob[1] + (h - u * a) * ob[E] + vmo;
+    zb[1] = ob[0] + u * ob[1] + 0.5 * v2 * ob[E] + vmo;
+    zb[E] = ob[0] + up * ob[1] + (h + u * a) * ob[E] + vmo;
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) zb[1 + k] = fma(vm[k], ob[E], ob[1 + k]);
+    double vmb[3] = {0.0, 0.0, 0.0};
+    double ab_ = ob[1] * (z[E] - z[0]) + ob[E] * u * (z[E] - z[0]);
+    double hb = ob[E] * (z[0] + z[E]);
+    double v2b = 0.5 * ob[E] * z[1];
+    vmb[0] = ob[1] * zs + ob[E] * a * (z[E] - z[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vmb[k] = fma(ob[1 + k], zs, ob[E] * z[1 + k]);
+    // z = |Λ| T y
+    double yb[NV], tab = 0.0, rhob = 0.0, phb = 0.0;
+    yb[0] = zb[0] * aum * ta;
+    vmb[0] += zb[0] * sm * ta * y[0];
+    ab_ -= zb[0] * sm * ta * y[0];
+    tab += zb[0] * aum * y[0];
+    yb[1] = zb[1] * au * c1;
+    vmb[0] += zb[1] * su * c1 * y[1];
+    rhob += zb[1] * au * g1 * ig * y[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        yb[1 + k] = zb[1 + k] * au * phat;
+        vmb[0] += zb[1 + k] * su * phat * y[1 + k];
+        phb += zb[1 + k] * au * y[1 + k];
+    }
+    yb[E] = zb[E] * aup * ta;
+    vmb[0] += zb[E] * sp * ta * y[E];
+    ab_ += zb[E] * sp * ta * y[E];
+    tab += zb[E] * aup * y[E];
+    rhob += tab * 0.5 * ig;
+    // y = Rᵀ ΔW
+    const double Sb = yb[0] + yb[E] + yb[1];
+    double dWb[NV];
+    dWb[0] = Sb;
+    dWb[1] = fma(u, Sb, a * (yb[E] - yb[0]));
+    ab_ += dW[1] * (yb[E] - yb[0]) + u * dW[E] * (yb[E] - yb[0]);
+    hb += dW[E] * (yb[0] + yb[E]);
+    vmb[0] += dW[1] * Sb + a * dW[E] * (yb[E] - yb[0]);
+    dWb[E] = (h - u * a) * yb[0] + (h + u * a) * yb[E] + 0.5 * v2 * yb[1];
+    v2b += 0.5 * dW[E] * yb[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        dWb[E] = fma(vm[k], yb[1 + k], dWb[E]);
+        dWb[1 + k] = fma(vm[k], Sb, yb[1 + k]);
+        vmb[k] += fma(dW[E], yb[1 + k], dW[1 + k] * Sb);
+    }
+    // h, a
+    double ibetb = 0.5 * g * ig1 * hb;
+    v2b += 0.5 * hb;
+    phb += ab_ * g * irho * 0.5 * ia;
+    double irhob = ab_ * g * phat * 0.5 * ia;
+    // ΔW
+    double Lbb = ig1 * dWb[0], Lrb = dWb[0];
+    double vl2b = -dWb[0] * bl, vr2b = dWb[0] * br;
+    double blb = -dWb[0] * vl2 - 2.0 * dWb[E], brb = dWb[0] * vr2 + 2.0 * dWb[E];
+    double vlb[3] = {0.0, 0.0, 0.0}, vrb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        blb = fma(2.0 * dWb[1 + k], vl[k], blb);
+        brb = fma(-2.0 * dWb[1 + k], vr[k], brb);
+        vlb[k] = 2.0 * bl * dWb[1 + k];
+        vrb[k] = -2.0 * br * dWb[1 + k];
+    }
+    // v2 = 2|v̄|² - ½(|v_l|² + |v_r|²), v̄ = (v_l + v_r)/2
+    vl2b -= 0.5 * v2b;
+    vr2b -= 0.5 * v2b;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        const double m = vmb[k] + 4.0 * vm[k] * v2b;   // v̄_k cotangent incl. |v̄|²
+        vlb[k] += fma(0.5, m, 2.0 * vl[k] * vl2b);
+        vrb[k] += fma(0.5, m, 2.0 * vr[k] * vr2b);
+    }
+    // means: p̂ = ½ s_ρ/s_β, 1/ρ_ln, 1/β_ln, and the logarithms
+    rhob -= irhob * irho * irho;
+    const double betb = -ibetb * ibet * ibet;
+    double rlb = fma(rhob, dra, 0.5 * phb * isb) + Lrb / rl;
+    double rrb = fma(rhob, drb, 0.5 * phb * isb) - Lrb / rr;
+    blb += fma(betb, dba, -phb * phat * isb) + Lbb / bl;
+    brb += fma(betb, dbb, -phb * phat * isb) - Lbb / br;
+    // β = ρ/(2p)
+    rlb = fma(0.5 * ipl, blb, rlb);
+    rrb = fma(0.5 * ipr, brb, rrb);
+    L.p -= blb * bl * ipl;
+    R.p -= brb * br * ipr;
+    qa[0] += rlb;
+    qb[0] += rrb;
+    L.u += vlb[0];
+    R.u += vrb[0];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        L.vt[k - 1] += vlb[k];
+        R.vt[k - 1] += vrb[k];
+    }
+}
+
 // KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC,
-// 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage).
+// 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage),
+// 6 MatrixDissipation(StdAverage), 7 MatrixDissipation(ChandrasekharAverage).
 template <int DIM, int KIND>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
-    constexpr bool CHANDRA = KIND == 1 || KIND == 5;
-    constexpr bool SD = KIND >= 4;
+    constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
+    constexpr bool SD = KIND == 4 || KIND == 5;
+    constexpr bool MD = KIND >= 6;
     constexpr int NV = DIM + 2;
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
@@ -635,7 +801,15 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     double lam = left ? ll : lr;
     double dot = 0.0;
     SideBar Ls = {}, Rs = {};
-    if (SD) {   // F = A - λ/2 · intensity · D(a, b)
+    if (MD) {   // F = A + ½ · intensity · R|Λ|TRᵀΔW: no wave-speed maximum
+        double ob[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ob[k] = 0.5 * inten * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        md_vjp<DIM>(pa, pb, g, ob, ab, bbar, Ls, Rs);
+    } else if (SD) {   // F = A - λ/2 · intensity · D(a, b)
         double D[NV], Db[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -654,7 +828,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
             bbar[k] = -ab[k];
         }
     }
-    Ib = SD ? 0.0 : 0.5 * lam * dot;   // ScalarDissipation takes no per-element scale
+    Ib = (SD || MD) ? 0.0 : 0.5 * lam * dot;   // the dissipation fluxes take no per-element scale
     if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
         PrimBar o1, o2;
         double vh1[DIM], vh2[DIM];
@@ -672,10 +846,12 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
         euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
     }
-    double kappa = 0.5 * inten * dot;
-    if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
-    else lambda_vjp<DIM>(pb, g, kappa, bbar);
-    if (SD) {
+    if (!MD) {
+        double kappa = 0.5 * inten * dot;
+        if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
+        else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    }
+    if (SD || MD) {
         side_prim_vjp<DIM>(pa, g, Ls, ab);
         side_prim_vjp<DIM>(pb, g, Rs, bbar);
     }
@@ -1135,13 +1311,14 @@ int adj_supported(flou_ctx* c) {
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                (k.volume_op == FLOU_OP_SPLIT &&
                 (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER));
-    bool nf = ((k.numflux == FLOU_NF_LXF || k.numflux == FLOU_NF_SCALAR_DISSIPATION) &&
+    bool nf = ((k.numflux == FLOU_NF_LXF || k.numflux == FLOU_NF_SCALAR_DISSIPATION ||
+                k.numflux == FLOU_NF_MATRIX_DISSIPATION) &&
                (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR)) ||
               k.numflux == FLOU_NF_HLL || k.numflux == FLOU_NF_HLLC;
     if (k.equation != FLOU_EQ_EULER || !vol || !nf)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
                                                  "the Chandrashekar or Kennedy-Gruber split form, and the "
-                                                 "LxF or ScalarDissipation (StdAverage or ChandrasekharAverage), "
+                                                 "LxF, Scalar- or MatrixDissipation (StdAverage or ChandrasekharAverage), "
                                                  "HLL or HLLC interface flux");
     if (!c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
@@ -1209,7 +1386,8 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     int dim = c->cfg.dim;
     const int nf = c->cfg.numflux;
     const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
-    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch : ch;
+    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch
+                   : nf == FLOU_NF_MATRIX_DISSIPATION ? 6 + ch : ch;
     switch (dim * 8 + kind) {
         case 8: adj_face_kernel<1, 0><<<grid, tb, 0, s>>>(F); break;
         case 9: adj_face_kernel<1, 1><<<grid, tb, 0, s>>>(F); break;
@@ -1217,18 +1395,24 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
         case 11: adj_face_kernel<1, 3><<<grid, tb, 0, s>>>(F); break;
         case 12: adj_face_kernel<1, 4><<<grid, tb, 0, s>>>(F); break;
         case 13: adj_face_kernel<1, 5><<<grid, tb, 0, s>>>(F); break;
+        case 14: adj_face_kernel<1, 6><<<grid, tb, 0, s>>>(F); break;
+        case 15: adj_face_kernel<1, 7><<<grid, tb, 0, s>>>(F); break;
         case 16: adj_face_kernel<2, 0><<<grid, tb, 0, s>>>(F); break;
         case 17: adj_face_kernel<2, 1><<<grid, tb, 0, s>>>(F); break;
         case 18: adj_face_kernel<2, 2><<<grid, tb, 0, s>>>(F); break;
         case 19: adj_face_kernel<2, 3><<<grid, tb, 0, s>>>(F); break;
         case 20: adj_face_kernel<2, 4><<<grid, tb, 0, s>>>(F); break;
         case 21: adj_face_kernel<2, 5><<<grid, tb, 0, s>>>(F); break;
+        case 22: adj_face_kernel<2, 6><<<grid, tb, 0, s>>>(F); break;
+        case 23: adj_face_kernel<2, 7><<<grid, tb, 0, s>>>(F); break;
         case 24: adj_face_kernel<3, 0><<<grid, tb, 0, s>>>(F); break;
         case 25: adj_face_kernel<3, 1><<<grid, tb, 0, s>>>(F); break;
         case 26: adj_face_kernel<3, 2><<<grid, tb, 0, s>>>(F); break;
         case 27: adj_face_kernel<3, 3><<<grid, tb, 0, s>>>(F); break;
         case 28: adj_face_kernel<3, 4><<<grid, tb, 0, s>>>(F); break;
-        default: adj_face_kernel<3, 5><<<grid, tb, 0, s>>>(F); break;
+        case 29: adj_face_kernel<3, 5><<<grid, tb, 0, s>>>(F); break;
+        case 30: adj_face_kernel<3, 6><<<grid, tb, 0, s>>>(F); break;
+        default: adj_face_kernel<3, 7><<<grid, tb, 0, s>>>(F); break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");

@@ -287,8 +287,8 @@ end
     solve_functional(disc, Q0, c, dt, nsteps, ρtarget, w) -> J
 
 J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` SSP-RK3 steps with per-element dissipation scales `c`
-(LxF interface fluxes), or `c = nothing` for HLL, HLLC and ScalarDissipation, which take no
-per-element scale.
+(LxF interface fluxes), or `c = nothing` for HLL, HLLC and the Scalar/MatrixDissipation fluxes,
+which take no per-element scale.
 Differentiable through the `rrule`s below (discrete adjoint, binomial checkpointing).
 Arrays are device pointers wrapped by the caller's GPU array package (e.g. CuArray).
 """
@@ -309,7 +309,7 @@ function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, 
     return J[], pullback
 end
 
-# HLL, HLLC and ScalarDissipation: no per-element scale, so no dJ/dc (the C ABI takes a null dJdc)
+# HLL, HLLC, Scalar/MatrixDissipation: no per-element scale, so no dJ/dc (the C ABI takes a null dJdc)
 function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, ::Nothing, dt, nsteps, ρt, w; nsnap=20)
     J = Ref{Float64}(0.0)
     g = similar(Q0)

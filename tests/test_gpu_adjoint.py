@@ -34,7 +34,7 @@ def _split(face_avg="chandra"):
 
 # HLL, HLLC and ScalarDissipation carry no per-element dissipation scale: their contexts take no
 # flou_set_dissipation and no dJ/dc
-HLL_FAMILY = ("split_hllc", "strong_hll", "strong_hllc", "split_sd", "strong_sd")
+HLL_FAMILY = ("split_hllc", "strong_hll", "strong_hllc", "split_sd", "strong_sd", "split_md", "strong_md")
 
 
 def _with_c(disc, op, c):
@@ -53,7 +53,9 @@ OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("s
              "split_kg": lambda: F.SplitDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0)),
              "split_sd": lambda: F.SplitDivOperator(F.ChandrasekharAverage(),
                                                     F.ScalarDissipation(F.ChandrasekharAverage(), 1.0)),
-             "strong_sd": lambda: F.StrongDivOperator(F.ScalarDissipation(F.StdAverage(), 1.0))}
+             "strong_sd": lambda: F.StrongDivOperator(F.ScalarDissipation(F.StdAverage(), 1.0)),
+             "split_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
+             "strong_md": lambda: F.StrongDivOperator(F.MatrixDissipation(F.StdAverage(), 1.0))}
 
 
 CASES = [
@@ -75,7 +77,7 @@ def _disc(case, op="strong"):
 
 
 @pytest.mark.parametrize("op", ["strong", "split", "split_stdface", "split_hllc", "strong_hll", "strong_hllc",
-                                "split_kg", "split_sd", "strong_sd"])
+                                "split_kg", "split_sd", "strong_sd", "split_md", "strong_md"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
 def test_rhs_vjp_dot_product(case, op):
     disc = _disc(case, op)
@@ -131,11 +133,12 @@ def test_hll_family_vjp_through_every_branch(dim, op):
         disc.ctx.set_dissipation(c)
 
 
-@pytest.mark.parametrize("op", ["split_sd", "strong_sd"])
+@pytest.mark.parametrize("op", ["split_sd", "strong_sd", "split_md", "strong_md"])
 @pytest.mark.parametrize("dim", [1, 2, 3])
-def test_scalar_dissipation_vjp_with_jumps(dim, op):
-    """ScalarDissipation (Euler.jl:228-301) on a state whose traces jump at every interface, so the
-    dissipation vector D and the wave-speed factor both act, against the oracle's dual numbers."""
+def test_dissipation_flux_vjp_with_jumps(dim, op):
+    """ScalarDissipation and MatrixDissipation (Euler.jl:228-380) on a state whose traces jump at
+    every interface, so the dissipation terms (D and the wave-speed factor; R|Λ|TRᵀ applied to the
+    entropy-variable jump) all act, against the oracle's dual numbers."""
     disc = build(dim, 4, (3,) * dim, F.EulerEquation(dim, 1.4), OPERATORS[op]())
     rng = np.random.default_rng(41 + dim)
     eq = disc.equation
@@ -277,7 +280,7 @@ def _tgv_state(disc, mach, seed):
     return np.asfortranarray(eq.vars_prim2cons(P))
 
 
-@pytest.mark.parametrize("op", ["split", "strong", "split_hllc", "split_kg", "split_sd"])
+@pytest.mark.parametrize("op", ["split", "strong", "split_hllc", "split_kg", "split_sd", "split_md"])
 def test_3d_adjoint_solve_against_dual_numbers(op):
     eq = F.EulerEquation(3, 1.4)
     L = 2 * np.pi
