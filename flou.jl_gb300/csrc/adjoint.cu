@@ -1002,9 +1002,12 @@ template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR>
 struct AdjSplitShape {
     using S = Shape<DIM, N>;
     static constexpr bool KG = TP == FLOU_TP_KENNEDY_GRUBER;
+    static constexpr bool STD = TP == FLOU_TP_STD_AVERAGE;
     static constexpr int NV = DIM + 2;
-    static constexpr int NARR = DIM + 3;                        // rh, vh, bh, vq (KG: rh, vh, ph, eh)
-    static constexpr int NPB = KG ? DIM + 3 : DIM + 2;          // ρ̄, v̄, β̄ per side (KG: ρ̄, v̄, p̄, ē)
+    // per node: rh, vh, bh, vq (KG: rh, vh, ph, eh; StdAverage: H, v, |v|²)
+    static constexpr int NARR = DIM + 3;
+    // per side of a pair: ρ̄, v̄, β̄ (KG: ρ̄, v̄, p̄, ē; StdAverage: the conserved cotangent)
+    static constexpr int NPB = KG ? DIM + 3 : DIM + 2;
     static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
     static constexpr int NSD = S::EPB * DIM * N * N;           // -Ja_d D♯ per element and direction
     static constexpr size_t SMEM =
@@ -1042,7 +1045,23 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
             v2[k] = sprim[(1 + k) * NN + ib];
         }
         PrimBar o1, o2;
-        if constexpr (A::KG)
+        if constexpr (A::STD) {   // F♯ = ½ (F(Q_a) + F(Q_b)): each node gets ½ J(Q)ᵀ F̄ in conserved variables
+            const double g1 = P.gamma - 1.0;
+            double qa_[NV], qb_[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qa_[k] = qb_[k] = 0.0;
+            euler_flux_vjp<DIM>(D, v1, sprim[(1 + DIM) * NN + ia], sprim[ia], g1, Fb, 0.5, qa_);
+            euler_flux_vjp<DIM>(D, v2, sprim[(1 + DIM) * NN + ib], sprim[ib], g1, Fb, 0.5, qb_);
+            o1.r = qa_[0];
+            o2.r = qb_[0];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                o1.v[k] = qa_[1 + k];
+                o2.v[k] = qb_[1 + k];
+            }
+            o1.b = qa_[DIM + 1];
+            o2.b = qb_[DIM + 1];
+        } else if constexpr (A::KG)
             kg_pair_vjp<DIM, D>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia], sprim[ib], v2,
                                 sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], Fb, o1, o2);
         else
@@ -1168,7 +1187,12 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         sprim[tid] = 0.5 * rho;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
-        if constexpr (A::KG) {
+        if constexpr (A::STD) {
+            sprim[tid] = (q[DIM + 1] + p) * ir;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = v[k];
+            sprim[(1 + DIM) * NN + tid] = vv;
+        } else if constexpr (A::KG) {
             sprim[(1 + DIM) * NN + tid] = 0.5 * p;
             sprim[(2 + DIM) * NN + tid] = 0.5 * (q[DIM + 1] * ir);
         } else {
@@ -1210,8 +1234,16 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     double vv = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
-    if constexpr (A::KG) kg_prim_to_cons_vjp<DIM>(rho, v, vv, P.U[(DIM + 1) * P.ndofs + gi], g1, acc, qb);
-    else prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
+    if constexpr (A::STD) {   // the pairs' cotangents are already conserved
+        qb[0] += acc.r;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) qb[1 + k] += acc.v[k];
+        qb[DIM + 1] += acc.b;
+    } else if constexpr (A::KG) {
+        kg_prim_to_cons_vjp<DIM>(rho, v, vv, P.U[(DIM + 1) * P.ndofs + gi], g1, acc, qb);
+    } else {
+        prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
+    }
     for (int k = 0; k < NV; ++k) {
         double ain = P.Ain[k * P.ndofs + gi];
         double o = fma(P.alpha, ain, qb[k]);
@@ -1267,11 +1299,12 @@ cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
     }
 }
 
-// The split form's two-point flux: Chandrashekar or Kennedy-Gruber.
+// The split form's two-point flux: Chandrashekar, Kennedy-Gruber or StdAverage.
 template <int DIM>
 cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
-    return tp == FLOU_TP_KENNEDY_GRUBER ? launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER>(n, P, s)
-                                        : launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR>(n, P, s);
+    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER>(n, P, s);
+    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE>(n, P, s);
+    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR>(n, P, s);
 }
 
 // Terminal functional J = 1/2 Σ w_i (ρ_i - ρt_i)²: seed Ū (density column) and per-block partials.
@@ -1310,14 +1343,15 @@ int adj_supported(flou_ctx* c) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                (k.volume_op == FLOU_OP_SPLIT &&
-                (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER));
+                (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER ||
+                 k.twopoint_flux == FLOU_TP_STD_AVERAGE));
     bool nf = ((k.numflux == FLOU_NF_LXF || k.numflux == FLOU_NF_SCALAR_DISSIPATION ||
                 k.numflux == FLOU_NF_MATRIX_DISSIPATION) &&
                (k.numflux_avg == FLOU_NF_STD_AVERAGE || k.numflux_avg == FLOU_NF_CHANDRASHEKAR)) ||
               k.numflux == FLOU_NF_HLL || k.numflux == FLOU_NF_HLLC;
     if (k.equation != FLOU_EQ_EULER || !vol || !nf)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers the Euler equations with the strong form or "
-                                                 "the Chandrashekar or Kennedy-Gruber split form, and the "
+                                                 "the split form (Chandrashekar, Kennedy-Gruber or StdAverage), and the "
                                                  "LxF, Scalar- or MatrixDissipation (StdAverage or ChandrasekharAverage), "
                                                  "HLL or HLLC interface flux");
     if (!c->lift_ends)

@@ -55,6 +55,7 @@ OPERATORS = {"strong": _lxf, "split": _split, "split_stdface": lambda: _split("s
                                                     F.ScalarDissipation(F.ChandrasekharAverage(), 1.0)),
              "strong_sd": lambda: F.StrongDivOperator(F.ScalarDissipation(F.StdAverage(), 1.0)),
              "split_md": lambda: F.SplitDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)),
+             "split_std": lambda: F.SplitDivOperator(F.LxF(F.StdAverage(), 1.0)),
              "strong_md": lambda: F.StrongDivOperator(F.MatrixDissipation(F.StdAverage(), 1.0))}
 
 
@@ -77,7 +78,7 @@ def _disc(case, op="strong"):
 
 
 @pytest.mark.parametrize("op", ["strong", "split", "split_stdface", "split_hllc", "strong_hll", "strong_hllc",
-                                "split_kg", "split_sd", "strong_sd", "split_md", "strong_md"])
+                                "split_kg", "split_sd", "strong_sd", "split_md", "strong_md", "split_std"])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "%dd_n%d" % (c["dim"], c["n"]))
 def test_rhs_vjp_dot_product(case, op):
     disc = _disc(case, op)
@@ -237,7 +238,7 @@ def test_adjoint_against_central_differences():
         assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
 
 
-@pytest.mark.parametrize("op", ["split", "split_stdface", "split_hllc", "split_kg"])
+@pytest.mark.parametrize("op", ["split", "split_stdface", "split_hllc", "split_kg", "split_std"])
 def test_split_rhs_vjp_columns(op):
     """Every column of the transposed Jacobian at once on a small 3D case: (∂R/∂Q)ᵀ λ against
     the dual-number JVPs of all unit directions of one element's nodes."""
@@ -280,7 +281,7 @@ def _tgv_state(disc, mach, seed):
     return np.asfortranarray(eq.vars_prim2cons(P))
 
 
-@pytest.mark.parametrize("op", ["split", "strong", "split_hllc", "split_kg", "split_sd", "split_md"])
+@pytest.mark.parametrize("op", ["split", "strong", "split_hllc", "split_kg", "split_sd", "split_md", "split_std"])
 def test_3d_adjoint_solve_against_dual_numbers(op):
     eq = F.EulerEquation(3, 1.4)
     L = 2 * np.pi
