@@ -1,0 +1,1321 @@
+// adjoint_kernels.cuh -- device side of the discrete adjoint: the parameter blocks, the VJPs of the
+// fluxes (Euler.jl's and Toro's), the face and element VJP kernels and their launch templates.
+// The translation units adjoint_face.cu, adjoint_elem.cu and adjoint_split{1d,2d,3d}.cu instantiate
+// them (compiled in parallel); adjoint.cu holds the host side (stage adjoint, checkpoint schedule,
+// reverse sweeps, C ABI) and calls them through the launchers declared at the end.
+//
+// discrete adjoint (vector-Jacobian products) of the residual and of the
+// SSP-RK3 step for the Euler equations with the strong-form volume term and the LxF
+// (Rusanov, StdAverage) interface flux on LGL nodes, and the checkpointed reverse sweep of
+// a terminal functional.
+//
+// Residual (per element, node i):  dQ_i = (1/J) [ -Σ_d Ja_d Σ_j Ds(i,j) F_d(Q_j) - Σ_faces ∂g·(±Fn) ]
+// (Hyperbolic.jl:31-69 with OpDivergence.jl:42-160, Interfaces.jl:111-136).  Its transpose,
+// applied to a cotangent λ with w = λ/J:
+//   volume:   Q̄_j -= Ja_d (∂F_d/∂Q)(Q_j)ᵀ Σ_i Ds(i,j) w_i           (transposed line contraction)
+//   surface:  F̄(face node) = -∂g_1 w_1 + ∂g_2 w_2  (end nodes of side 1 / side 2)
+//             then the face flux VJP scatters to the two traces and to the dissipation scale.
+// SSP-RK3 step transpose (U1 = U0 + dt L0; U2 = 3/4 U0 + 1/4 (U1 + dt L1); U3 = 1/3 U0 + 2/3 (U2 + dt L2)):
+//   (a) Ū2 = 2/3 Ū3 + VJP(U2; 2/3 dt Ū3),  B = 1/3 Ū3
+//   (b) Ū1 = 1/4 Ū2 + VJP(U1; 1/4 dt Ū2),  B += 3/4 Ū2
+//   (c) Ū0 = Ū1 + B + VJP(U0; dt Ū1)
+// Split form (OpDivergence.jl:200-282 with the Chandrashekar flux of Euler.jl:474-536): the
+// volume term -Ja_d Σ_j D♯(i,j) F♯(Q_i, Q_j) has, for a symmetric pair (a, b) of a line, the
+// flux cotangent F̄ = -Ja_d (D♯(a,b) w_a + D♯(b,a) w_b); its VJP goes to the primitive
+// variables (ρ, v, β = ρ/(2p)) of both nodes and from there to the conserved ones.  The
+// LxF(Chandrashekar) interface flux differentiates the same pair flux (3D keeps the
+// reference's mean of |v|² as written, Euler.jl:216).
+// Non-smooth points follow Julia's Base (what ForwardDiff differentiates on the reference's
+// CPU path): max(a, b) takes b unless b < a; d|u|/du = -1 if u has its sign bit set, else +1.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "flou_ctx.cuh"
+
+namespace flou {
+
+struct AdjFaceParams {
+    int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
+    const double* U;        // state the residual is linearised at
+    const double* Ain;      // adjoint input; λ = s_lam * Ain
+    double s_lam;
+    double* QbL;            // trace cotangent, side 1 [nv][nfdofs]
+    double* QbR;            // trace cotangent, side 2 [nv][nfdofs]
+    double* Ibar;           // cotangent of the face intensity [nfdofs]
+    const int32_t* face_elem;
+    const double* faceJ;
+    const int8_t* face_bc;
+    const double* invJ;
+    const double* ops;      // to read ∂g_l[0], ∂g_r[n-1]
+    const double* elem_c;
+    double intensity, gamma;
+    int64_t ndofs, nfdofs;
+    int32_t nfaces, n, npe, nfd;
+    int32_t bc_kind[MAXBC];
+};
+
+struct AdjElemParams {
+    int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
+    const double* U;
+    const double* Ain;
+    double* Aout;           // alpha Ain + beta B + VJP
+    double* B;              // accumulator: B = gamma_B B + delta_B Ain (when writeB)
+    const double* QbL;
+    const double* QbR;
+    const double* Ibar;
+    double* cbar;           // per element, accumulated (nullable)
+    const int32_t* elem_face;
+    const int32_t* face_elem;
+    const double* invJ;
+    const double* Ja;
+    const double* ops;
+    int64_t ndofs, nfdofs;
+    int32_t nelem;
+    double s_lam, alpha, beta, gamma_B, delta_B;
+    int32_t readB, writeB;
+    double gamma;
+};
+
+// q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
+//   P̄ = ḡ_md + ḡ_E v_d,  s = Σ_k ḡ_mk v_k
+//   q̄_ρ  += -v_d (s + ḡ_E H) + (γ-1) |v|²/2 P̄
+//   q̄_mk += v_d ḡ_mk - (γ-1) v_k P̄ + [k = d] (ḡ_ρ + s + ḡ_E H)
+//   q̄_E  += ḡ_E v_d + (γ-1) P̄
+template <int DIM>
+__device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv, double H, double g1,
+                                               const double* gb, double scale, double* qb) {
+    double Pb = gb[1 + d] + gb[DIM + 1] * v[d];
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) s = fma(gb[1 + k], v[k], s);
+    double t = s + gb[DIM + 1] * H;
+    qb[0] += scale * (fma(0.5 * g1 * vv, Pb, -v[d] * t));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        double r = fma(v[d], gb[1 + k], -g1 * v[k] * Pb);
+        if (k == d) r += gb[0] + t;
+        qb[1 + k] += scale * r;
+    }
+    qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1] * v[d]);
+}
+
+// Primitive quantities of one node with the reciprocals the VJPs reuse (1/ρ, 1/a), from the
+// refined hardware reciprocals (within 1 ulp of the correctly rounded values).
+struct Prim {
+    double rho, v[3], vv, p, H, a, ir, ia;
+};
+
+template <int DIM, bool SOUND = true>
+__device__ __forceinline__ Prim prim_of(const double* q, double g) {
+    Prim P;
+    P.rho = q[0];
+    double ir = rcp_refined(q[0]), ke = 0.0, vv = 0.0;
+    P.ir = ir;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        P.v[k] = q[1 + k] * ir;
+        ke = fma(q[1 + k], P.v[k], ke);
+        vv = fma(P.v[k], P.v[k], vv);
+    }
+    P.vv = vv;
+    P.p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]);
+    P.H = (q[DIM + 1] + P.p) * ir;
+    if (SOUND) {
+        const double a2 = g * P.p * ir;
+        P.ia = rsqrt_refined(a2);
+        P.a = a2 * P.ia;
+    } else {
+        P.a = P.ia = 0.0;
+    }
+    return P;
+}
+
+// q̄ += κ ∇λ, λ = |u_n| + a (face frame, normal momentum first).
+template <int DIM>
+__device__ __forceinline__ void lambda_vjp(const Prim& P, double g, double kappa, double* qb) {
+    double sg = signbit(P.v[0]) ? -1.0 : 1.0;
+    double ir = P.ir;
+    double ca = (0.5 * g * (g - 1.0)) * (P.ia * ir);   // ∂a/∂p · ∂p/∂E
+    qb[0] += kappa * (-sg * P.v[0] * ir + ca * 0.5 * P.vv - P.a * 0.5 * ir);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) qb[1 + k] += kappa * ((k == 0 ? sg * ir : 0.0) - ca * P.v[k]);
+    qb[DIM + 1] += kappa * ca;
+}
+
+// Cotangent of one node's primitive variables: (ρ, v, β) for the Chandrashekar flux, (ρ, v, p, e)
+// for Kennedy-Gruber (b then holds p̄ and e the cotangent of the specific total energy E/ρ).
+struct PrimBar {
+    double r, v[3], b, e;
+};
+
+// Logarithmic mean (Utilities.jl:34-44) of a = 2 h1, b = 2 h2 given the half sum hs = (a+b)/2,
+// the half difference hd = (a-b)/2 and r = 1/hs, with its partial derivatives:
+//   f = (a-b)/(a+b), u = f²;  u < 0.01: L = (a+b)/(2F), F = 1+u/3+u²/5+u³/7, 1/L = F r,
+//     ∂L/∂a = 1/(2F) - 2F'(u) f b/(F²(a+b)),  ∂L/∂b = 1/(2F) + 2F'(u) f a/(F²(a+b));
+//   else L = (a-b)/ℓ, ℓ = ln(a/b):  ∂L/∂a = 1/ℓ - L/(ℓ a),  ∂L/∂b = L/(ℓ b) - 1/ℓ.
+// 1/F takes two Newton steps from 1 - u/3 (relative error (4u²/45)^4 < 1e-20 for u < 0.01).
+__device__ __forceinline__ void logmean_half(double h1, double h2, double hs, double hd, double r, double& L,
+                                             double& iL, double& da, double& db) {
+    double f = hd * r, u = f * f;
+    if (u < 0.01) {
+        double F = fma(u, fma(u, fma(u, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+        double y = fma(-1.0 / 3.0, u, 1.0);
+        y = y * fma(-F, y, 2.0);
+        y = y * fma(-F, y, 2.0);
+        L = hs * y;
+        iL = F * r;
+        double Fp2 = fma(u, fma(u, 6.0 / 7.0, 0.8), 2.0 / 3.0);   // 2 F'(u)
+        double t = Fp2 * f * (y * y) * r;
+        double hy = 0.5 * y;
+        da = fma(-t, h2, hy);
+        db = fma(t, h1, hy);
+    } else {
+        double l = log(h1 / h2), il = 1.0 / l;
+        L = (2.0 * hd) * il;
+        iL = l / (2.0 * hd);
+        double c = 0.5 * L * il;
+        da = il - c / h1;
+        db = c / h2 - il;
+    }
+}
+
+// VJP of the Chandrashekar pair flux along axis D (Euler.jl:474-536 as a function of the
+// primitive variables), F = [m, m v̄ + p̂ e_D, m h] with
+//   m = ρ̂ v̄_D, ρ̂ = ln-mean(ρ), β̂ = ln-mean(β), p̂ = (ρ1+ρ2)/(2(β1+β2)), v̄ = (v1+v2)/2,
+//   h = 1/(2β̂(γ-1)) - S/4 + p̂/ρ̂ + |v̄|²,  S = |v1|² + |v2|²
+// (WL2: S = |v1|² + |v2|² - v2_z² + v1_z², the 3D interface average of Euler.jl:216).
+// Inputs are the halved node quantities rh = ρ/2, vh = v/2, bh = β/2, vq = |v|²/4; one
+// reciprocal 1/(ρ̄ β̄) serves both means and the pressure average.  Cotangents are with
+// respect to (ρ, v, β) of each side.
+template <int DIM, int D, bool WL2>
+__device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, double bh1, double vq1, double rh2,
+                                                 const double* vh2, double bh2, double vq2, double cb,
+                                                 const double* Fb, PrimBar& o1, PrimBar& o2) {
+    double hsr = rh1 + rh2, hdr = rh1 - rh2, hsb = bh1 + bh2, hdb = bh1 - bh2;
+    double R = rcp_refined(hsr * hsb);
+    double rs = hsb * R, rb = hsr * R;   // 1/hsr, 1/hsb
+    double rho, irho, dra, drb, beta, ibeta, dba, dbb;
+    logmean_half(rh1, rh2, hsr, hdr, rs, rho, irho, dra, drb);
+    logmean_half(bh1, bh2, hsb, hdb, rb, beta, ibeta, dba, dbb);
+    double p = 0.5 * hsr * rb;
+    double va[DIM], vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        va[k] = vh1[k] + vh2[k];
+        vv = fma(va[k], va[k], vv);
+    }
+    double S4 = vq1 + vq2;
+    if (WL2 && DIM == 3) S4 = S4 + (vh1[2] * vh1[2] - vh2[2] * vh2[2]);
+    double h = fma(cb, ibeta, -S4) + fma(p, irho, vv);
+    double m = rho * va[D];
+    double mb = fma(Fb[DIM + 1], h, Fb[0]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], va[k], mb);
+    double hb = m * Fb[DIM + 1];
+    double mh = 0.5 * m;
+    double hvab[DIM];   // v̄̄/2: the cotangent of v̄, halved (v̄ = (v1 + v2)/2)
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) hvab[k] = fma(mh, Fb[1 + k], hb * va[k]);
+    hvab[D] = fma(0.5 * mb, rho, hvab[D]);
+    double pb = fma(hb, irho, Fb[1 + D]);
+    double rhob = fma(mb, va[D], -hb * p * (irho * irho));
+    double betab = -hb * cb * (ibeta * ibeta);
+    double pr = 0.25 * pb * rb, pbb = -0.5 * pb * p * rb;
+    o1.r = fma(rhob, dra, pr);
+    o2.r = fma(rhob, drb, pr);
+    o1.b = fma(betab, dba, pbb);
+    o2.b = fma(betab, dbb, pbb);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        o1.v[k] = fma(-hb, vh1[k], hvab[k]);
+        o2.v[k] = fma(-hb, vh2[k], hvab[k]);
+    }
+    if (WL2 && DIM == 3) {
+        o1.v[2] = fma(-hb, vh1[2], o1.v[2]);
+        o2.v[2] = fma(hb, vh2[2], o2.v[2]);
+    }
+}
+
+// q̄ += (∂(ρ, v, β)/∂q)ᵀ (ρ̄, v̄, β̄) with β = ρ/(2p):
+//   ρ̄' = ρ̄ + β̄/(2p),  p̄ = -β̄ β/p,
+//   q̄_ρ += ρ̄' - v·v̄/ρ + (γ-1)|v|²/2 p̄,  q̄_mk += v̄_k/ρ - (γ-1) v_k p̄,  q̄_E += (γ-1) p̄.
+template <int DIM>
+__device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, double vv, double p, double g1,
+                                                 const PrimBar& o, double* qb) {
+    double ip = rcp_refined(p), ir = rcp_refined(rho);
+    double rb = fma(0.5 * ip, o.b, o.r);
+    double pb = -o.b * (0.5 * rho * ip) * ip * g1;   // (γ-1) p̄
+    double vvb = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vvb = fma(v[k], o.v[k], vvb);
+        qb[1 + k] += fma(o.v[k], ir, -v[k] * pb);
+    }
+    qb[0] += fma(0.5 * vv, pb, fma(-vvb, ir, rb));
+    qb[DIM + 1] += pb;
+}
+
+// VJP of the Kennedy-Gruber pair flux along axis D (Kennedy & Gruber 2008, as the forward kernel
+// evaluates it), F = [m, m v̄ + p̄ e_D, m ē + p̄ v̄_D] with m = ρ̄ v̄_D and the arithmetic means
+// ρ̄, v̄, p̄, ē (e = E/ρ).  Inputs are the halved node quantities (rh = ρ/2, vh = v/2, ph = p/2,
+// eh = e/2), so each mean is a sum of two; both nodes receive half of each mean's cotangent.
+template <int DIM, int D>
+__device__ __forceinline__ void kg_pair_vjp(double rh1, const double* vh1, double ph1, double eh1, double rh2,
+                                            const double* vh2, double ph2, double eh2, const double* Fb,
+                                            PrimBar& o1, PrimBar& o2) {
+    const double rho = rh1 + rh2, pm = ph1 + ph2, en = eh1 + eh2;
+    double vm[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vm[k] = vh1[k] + vh2[k];
+    const double m = rho * vm[D];
+    double mb = fma(Fb[DIM + 1], en, Fb[0]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], vm[k], mb);
+    o1.r = o2.r = 0.5 * mb * vm[D];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o1.v[k] = 0.5 * Fb[1 + k] * m;
+    o1.v[D] = fma(0.5 * mb, rho, fma(0.5 * Fb[DIM + 1], pm, o1.v[D]));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o2.v[k] = o1.v[k];
+    o1.b = o2.b = 0.5 * fma(Fb[DIM + 1], vm[D], Fb[1 + D]);
+    o1.e = o2.e = 0.5 * Fb[DIM + 1] * m;
+}
+
+// q̄ += (∂(ρ, v, p, e)/∂q)ᵀ (ρ̄, v̄, p̄, ē) with v = m/ρ, p = (γ-1)(E - ½|m|²/ρ), e = E/ρ:
+//   q̄_ρ += ρ̄ - (v·v̄ + e ē)/ρ + (γ-1)|v|²/2 p̄,  q̄_mk += v̄_k/ρ - (γ-1) v_k p̄,
+//   q̄_E += (γ-1) p̄ + ē/ρ.
+template <int DIM>
+__device__ __forceinline__ void kg_prim_to_cons_vjp(double rho, const double* v, double vv, double E, double g1,
+                                                    const PrimBar& o, double* qb) {
+    const double ir = rcp_refined(rho), e = E * ir, pb = g1 * o.b;
+    double vvb = e * o.e;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vvb = fma(v[k], o.v[k], vvb);
+        qb[1 + k] += fma(o.v[k], ir, -v[k] * pb);
+    }
+    qb[0] += fma(0.5 * vv, pb, fma(-vvb, ir, o.r));
+    qb[DIM + 1] += fma(o.e, ir, pb);
+}
+
+// Cotangents of one side's primitive quantities in the face frame (normal velocity u, tangential
+// velocities, pressure, sound speed), mapped to its conserved variables and added to qb:
+//   p̄' = p̄ + ā γ/(2aρ)   (a = sqrt(γp/ρ)),
+//   q̄_ρ += -ā a/(2ρ) - (ū u + Σ v̄_t v_t)/ρ + (γ-1)|v|²/2 p̄',
+//   q̄_m1 += ū/ρ - (γ-1) u p̄',  q̄_mt += v̄_t/ρ - (γ-1) v_t p̄',  q̄_E += (γ-1) p̄'.
+struct SideBar {
+    double u, vt[2], p, a;
+};
+
+template <int DIM>
+__device__ __forceinline__ void side_prim_vjp(const Prim& P, double g, const SideBar& b, double* qb) {
+    const double g1 = g - 1.0, ir = P.ir;
+    const double pb = fma(b.a * g, 0.5 * ir * P.ia, b.p);
+    double vdot = b.u * P.v[0];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vdot = fma(b.vt[k - 1], P.v[k], vdot);
+    qb[0] += fma(0.5 * g1 * P.vv, pb, -(fma(b.a, 0.5 * P.a, vdot)) * ir);
+    qb[1] += fma(b.u, ir, -g1 * P.v[0] * pb);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) qb[1 + k] += fma(b.vt[k - 1], ir, -g1 * P.v[k] * pb);
+    qb[DIM + 1] += g1 * pb;
+}
+
+// VJP of the physical normal flux F = [m1, m1 u + p, m_t u, (E + p) u] (face frame) with the
+// cotangent gb scaled by sc: the conserved variables it reads directly go to qb, u and p to b.
+template <int DIM>
+__device__ __forceinline__ void normal_flux_vjp(const double* q, const Prim& P, const double* gb, double sc,
+                                                double* qb, SideBar& b) {
+    const double u = P.v[0];
+    double ub = gb[1] * q[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        ub = fma(gb[1 + k], q[1 + k], ub);
+        qb[1 + k] += sc * gb[1 + k] * u;
+    }
+    ub = fma(gb[DIM + 1], q[DIM + 1] + P.p, ub);
+    qb[1] += sc * fma(gb[1], u, gb[0]);
+    qb[DIM + 1] += sc * gb[DIM + 1] * u;
+    b.u += sc * ub;
+    b.p += sc * fma(gb[DIM + 1], u, gb[1]);
+}
+
+// VJP of the HLL (hllc = false) and HLLC interface fluxes in the face frame (no counterpart in
+// Flou; Toro 2009, eqs. 10.21 and 10.37-10.39 with the Davis wave speeds S_L = min(u_L - a_L,
+// u_R - a_R), S_R = max(u_L + a_L, u_R + a_R)).  a, b: the two states; fb: the flux cotangent;
+// qa, qb: the states' cotangents (accumulated).  Branches and ties as the oracle's dual numbers
+// take them: min(x, y) is y only when y < x, max(x, y) is x only when y < x, the supersonic
+// cases when S_L >= 0 or S_R <= 0, the left star state when S* >= 0.
+template <int DIM>
+__device__ __forceinline__ void hll_family_vjp(bool hllc, const double* a, const double* b, const Prim& pa,
+                                               const Prim& pb, double g, const double* fb, double* qa,
+                                               double* qb) {
+    constexpr int NV = DIM + 2;
+    SideBar L = {}, R = {};
+    const double ul = pa.v[0], ur = pb.v[0];
+    const double sl1 = ul - pa.a, sl2 = ur - pb.a, sr1 = ul + pa.a, sr2 = ur + pb.a;
+    const bool slR = sl2 < sl1, srL = sr2 < sr1;
+    const double sl = slR ? sl2 : sl1, sr = srL ? sr1 : sr2;
+    double slb = 0.0, srb = 0.0;
+    if (sl >= 0.0) {
+        normal_flux_vjp<DIM>(a, pa, fb, 1.0, qa, L);
+    } else if (sr <= 0.0) {
+        normal_flux_vjp<DIM>(b, pb, fb, 1.0, qb, R);
+    } else if (!hllc) {
+        double Fl[NV], Fr[NV];
+        euler_normal_flux<DIM>(a, ul, pa.p, Fl);
+        euler_normal_flux<DIM>(b, ur, pb.p, Fr);
+        const double r = rcp_refined(sr - sl), slr = sl * sr * r;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double dq = b[k] - a[k];
+            const double F = (sr * Fl[k] - sl * Fr[k] + sl * sr * dq) * r;
+            srb = fma(fb[k], (Fl[k] + sl * dq - F) * r, srb);
+            slb = fma(fb[k], (F - Fr[k] + sr * dq) * r, slb);
+            qb[k] += fb[k] * slr;
+            qa[k] -= fb[k] * slr;
+        }
+        normal_flux_vjp<DIM>(a, pa, fb, sr * r, qa, L);
+        normal_flux_vjp<DIM>(b, pb, fb, -sl * r, qb, R);
+    } else {
+        const double rl = pa.rho, rr = pb.rho;
+        const double ml = rl * (sl - ul), mr = rr * (sr - ur);
+        const double Dm = ml - mr;
+        const double iDm = rcp_refined(Dm);
+        const double ss = ((pb.p - pa.p) + ul * ml - ur * mr) * iDm;
+        const bool left = ss >= 0.0;
+        // the star side K, selected per component (no local memory); its cotangents are formed in
+        // qkb / K and added to the side they belong to below
+        double qk[NV], qkb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qk[k] = left ? a[k] : b[k];
+            qkb[k] = 0.0;
+        }
+        Prim pk;
+        pk.rho = left ? pa.rho : pb.rho;
+        pk.p = left ? pa.p : pb.p;
+        pk.ir = left ? pa.ir : pb.ir;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) pk.v[k] = left ? pa.v[k] : pb.v[k];
+        SideBar K = {};
+        const double sk = left ? sl : sr, mk = left ? ml : mr, uk = pk.v[0];
+        const double isk = rcp_refined(sk - ss), coef = mk * isk, irk = pk.ir, imk = rcp_refined(mk);
+        const double X = fma(ss - uk, ss + pk.p * imk, qk[DIM + 1] * irk);
+        double Us[NV];
+        Us[0] = coef;
+        Us[1] = coef * ss;
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) Us[1 + k] = coef * pk.v[k];
+        Us[DIM + 1] = coef * X;
+        double skb = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            skb = fma(fb[k], Us[k] - qk[k], skb);
+            qkb[k] -= sk * fb[k];
+        }
+        normal_flux_vjp<DIM>(qk, pk, fb, 1.0, qkb, K);
+        // Us̄ = sk fb
+        double coefb = sk * fma(fb[1], ss, fma(fb[DIM + 1], X, fb[0]));
+#pragma unroll
+        for (int k = 1; k < DIM; ++k) {
+            coefb = fma(sk * fb[1 + k], pk.v[k], coefb);
+            K.vt[k - 1] += sk * fb[1 + k] * coef;
+        }
+        const double Xb = sk * fb[DIM + 1] * coef;
+        double ssb = sk * fb[1] * coef + Xb * ((ss + pk.p * imk) + (ss - uk));
+        qkb[DIM + 1] += Xb * irk;
+        qkb[0] -= Xb * qk[DIM + 1] * irk * irk;
+        K.u -= Xb * (ss + pk.p * imk);
+        K.p += Xb * (ss - uk) * imk;
+        double mkb = -Xb * (ss - uk) * pk.p * imk * imk;
+        // coef = mk / (sk - ss)
+        mkb = fma(coefb, isk, mkb);
+        skb -= coefb * coef * isk;
+        ssb = fma(coefb * coef, isk, ssb);
+        // ss = N / Dm, N = (pr - pl) + ul ml - ur mr, Dm = ml - mr
+        const double Nb = ssb * iDm, Dmb = -ssb * ss * iDm;
+        // the star side's own cotangents go to the side it is
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qa[k] += left ? qkb[k] : 0.0;
+            qb[k] += left ? 0.0 : qkb[k];
+        }
+        L.u += left ? K.u : 0.0;
+        R.u += left ? 0.0 : K.u;
+        L.p += left ? K.p : 0.0;
+        R.p += left ? 0.0 : K.p;
+#pragma unroll
+        for (int k = 0; k < DIM - 1; ++k) {
+            L.vt[k] += left ? K.vt[k] : 0.0;
+            R.vt[k] += left ? 0.0 : K.vt[k];
+        }
+        R.p += Nb;
+        L.p -= Nb;
+        L.u += Nb * ml;
+        R.u -= Nb * mr;
+        double mlb = fma(Nb, ul, Dmb), mrb = -fma(Nb, ur, Dmb);
+        if (left) mlb += mkb;
+        else mrb += mkb;
+        if (left) slb += skb;
+        else srb += skb;
+        // ml = ρl (sl - ul), mr = ρr (sr - ur)
+        qa[0] += mlb * (sl - ul);
+        slb = fma(mlb, rl, slb);
+        L.u -= mlb * rl;
+        qb[0] += mrb * (sr - ur);
+        srb = fma(mrb, rr, srb);
+        R.u -= mrb * rr;
+    }
+    // S_L = min(u_L - a_L, u_R - a_R), S_R = max(u_L + a_L, u_R + a_R)
+    const double slbL = slR ? 0.0 : slb, slbR = slR ? slb : 0.0;
+    const double srbL = srL ? srb : 0.0, srbR = srL ? 0.0 : srb;
+    L.u += slbL + srbL;
+    L.a += srbL - slbL;
+    R.u += slbR + srbR;
+    R.a += srbR - slbR;
+    side_prim_vjp<DIM>(pa, g, L, qa);
+    side_prim_vjp<DIM>(pb, g, R, qb);
+}
+
+// The dissipation vector of ScalarDissipation (Euler.jl:228-301, as the forward face kernel forms
+// it in the face frame), F = A - λ/2 · intensity · D with
+//   D_ρ = ρ_r - ρ_l,  D_m = m_r - m_l (zero in 3D: the reference reads the left momenta from Q_r),
+//   D_E = ½ c₁ (ρ_r - ρ_l) + ½ (ρ_l + ρ_r) c₂,
+//   c₁ = 1/((γ-1) β_ln) + v_l·v_r,  c₂ = ½(|v_r|² - |v_l|²) + (p_r/ρ_r - p_l/ρ_l)/(γ-1),
+// β = ρ/(2p), β_ln the logarithmic mean.  Returns D and adds Dbar·∂D/∂(a, b) to qa, qb (the
+// direct conserved parts) and to L, R (the cotangents of the velocities and pressures).
+template <int DIM>
+__device__ __forceinline__ void sd_jump_vjp(const double* a, const double* b, const Prim& pa, const Prim& pb,
+                                            double g, const double* Db, double* D, double* qa, double* qb,
+                                            SideBar& L, SideBar& R) {
+    constexpr int NV = DIM + 2;
+    const double g1 = g - 1.0, ig1 = 1.0 / g1;
+    const double ipl = rcp_refined(pa.p), ipr = rcp_refined(pb.p);
+    const double bl = 0.5 * pa.rho * ipl, br = 0.5 * pb.rho * ipr;
+    const double hs = 0.5 * (bl + br), hd = 0.5 * (bl - br);
+    double Lb, iLb, dla, dlb;
+    logmean_half(0.5 * bl, 0.5 * br, hs, hd, rcp_refined(hs), Lb, iLb, dla, dlb);
+    double vlr = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vlr = fma(pa.v[k], pb.v[k], vlr);
+    const double c1 = fma(ig1, iLb, vlr);
+    const double c2 = fma(0.5, pb.vv - pa.vv, ig1 * (pb.p * pb.ir - pa.p * pa.ir));
+    const double dr = pb.rho - pa.rho, sr = pa.rho + pb.rho;
+    D[0] = dr;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) D[1 + k] = (DIM == 3) ? 0.0 : b[1 + k] - a[1 + k];
+    D[DIM + 1] = fma(0.5 * c1, dr, 0.5 * sr * c2);
+    // reverse
+    qb[0] += Db[0];
+    qa[0] -= Db[0];
+    if (DIM != 3) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            qb[1 + k] += Db[1 + k];
+            qa[1 + k] -= Db[1 + k];
+        }
+    }
+    const double dE = Db[DIM + 1];
+    const double c1b = 0.5 * dr * dE, c2b = 0.5 * sr * dE;
+    qb[0] += 0.5 * (c1 + c2) * dE;
+    qa[0] += 0.5 * (c2 - c1) * dE;
+    // c1: 1/β_ln and v_l·v_r
+    const double ib = -ig1 * c1b * iLb * iLb;   // cotangent of β_ln
+    const double blb = ib * dla, brb = ib * dlb;
+    // c2: ½(|v_r|² - |v_l|²) and (p/ρ) of both sides
+    const double tr = c2b * ig1 * pb.ir, tl = c2b * ig1 * pa.ir;
+    qb[0] -= tr * pb.p * pb.ir;
+    qa[0] += tl * pa.p * pa.ir;
+    R.p += tr;
+    L.p -= tl;
+    // β = ρ/(2p): ρ̄ += β̄/(2p), p̄ -= β̄ β/p
+    qa[0] += 0.5 * blb * ipl;
+    L.p -= blb * bl * ipl;
+    qb[0] += 0.5 * brb * ipr;
+    R.p -= brb * br * ipr;
+    // velocities (face frame: component 0 normal, then the tangents)
+    const double vlb0 = fma(c1b, pb.v[0], -c2b * pa.v[0]), vrb0 = fma(c1b, pa.v[0], c2b * pb.v[0]);
+    L.u += vlb0;
+    R.u += vrb0;
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        L.vt[k - 1] += fma(c1b, pb.v[k], -c2b * pa.v[k]);
+        R.vt[k - 1] += fma(c1b, pa.v[k], c2b * pb.v[k]);
+    }
+    (void)NV;
+}
+
+// The matrix-dissipation part of MatrixDissipation (Euler.jl:303-380, in the factorised form the
+// forward face kernel evaluates), F = A + ½ · intensity · o with o = R |Λ| T Rᵀ ΔW:
+//   ΔW = (L_β/(γ-1) + L_ρ - (|v_l|² β_l - |v_r|² β_r), 2(β_l v_l - β_r v_r), -2(β_l - β_r)),
+//   L_x = ln(x_l/x_r), β = ρ/(2p); at the averaged state (ρ_ln, v̄ = (v_l+v_r)/2, p̂, β_ln):
+//   a² = γ p̂/ρ_ln, h = γ/(2(γ-1)β_ln) + ½ v2, v2 = 2|v̄|² - ½(|v_l|² + |v_r|²), u = v̄_1;
+//   y = Rᵀ ΔW, z = |Λ| T y (|u ∓ a| ρ_ln/(2γ), |u| (γ-1) ρ_ln/γ, |u| p̂), o = R z.
+// ob = ½ · intensity · (the flux cotangent).  Adds the cotangents of both sides' densities to
+// qa[0], qb[0] and those of their velocities and pressures to L, R.  |x| differentiates as Base's
+// abs on the dual numbers: -1 when the sign bit is set, else +1.
+template <int DIM>
+__device__ __forceinline__ void md_vjp(const Prim& pa, const Prim& pb, double g, const double* ob, double* qa,
+                                       double* qb, SideBar& L, SideBar& R) {
+    constexpr int NV = DIM + 2, E = DIM + 1;
+    const double g1 = g - 1.0, ig1 = 1.0 / g1, ig = 1.0 / g;
+    const double rl = pa.rho, rr = pb.rho, pl = pa.p, pr = pb.p;
+    const double* vl = pa.v;
+    const double* vr = pb.v;
+    const double vl2 = pa.vv, vr2 = pb.vv;
+    const double ipl = rcp_refined(pl), ipr = rcp_refined(pr);
+    const double bl = 0.5 * rl * ipl, br = 0.5 * rr * ipr;
+    const double sr = rl + rr, sb = bl + br;
+    // logarithmic means with their derivatives (logmean_half takes halved values)
+    double rho, irho, dra, drb, bet, ibet, dba, dbb;
+    logmean_half(0.5 * rl, 0.5 * rr, 0.5 * sr, 0.5 * (rl - rr), rcp_refined(0.5 * sr), rho, irho, dra, drb);
+    logmean_half(0.5 * bl, 0.5 * br, 0.5 * sb, 0.5 * (bl - br), rcp_refined(0.5 * sb), bet, ibet, dba, dbb);
+    const double Lr = log(rl * pb.ir), Lb = log(bl * rcp_refined(br));
+    const double isb = rcp_refined(sb), phat = 0.5 * sr * isb;
+    double vm[3] = {0.0, 0.0, 0.0}, vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vm[k] = 0.5 * (vl[k] + vr[k]);
+        vv = fma(vm[k], vm[k], vv);
+    }
+    const double v2 = fma(2.0, vv, -0.5 * (vl2 + vr2));
+    const double a2 = g * phat * irho, ia = rsqrt_refined(a2), a = a2 * ia;
+    const double h = fma(0.5 * g * ig1, ibet, 0.5 * v2);
+    double dW[NV];
+    dW[0] = fma(Lb, ig1, Lr) - (vl2 * bl - vr2 * br);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) dW[1 + k] = 2.0 * (bl * vl[k] - br * vr[k]);
+    dW[E] = -2.0 * (bl - br);
+    const double u = vm[0];
+    double S = fma(u, dW[1], dW[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) S = fma(vm[k], dW[1 + k], S);
+    double y[NV];
+    y[0] = S - a * dW[1] + (h - u * a) * dW[E];
+    y[E] = S + a * dW[1] + (h + u * a) * dW[E];
+    y[1] = fma(0.5 * v2, dW[E], S);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) y[1 + k] = fma(vm[k], dW[E], dW[1 + k]);
+    const double ta = rho * (0.5 * ig), c1 = g1 * rho * ig;
+    const double um = u - a, up = u + a;
+    const double sm = signbit(um) ? -1.0 : 1.0, sp = signbit(up) ? -1.0 : 1.0, su = signbit(u) ? -1.0 : 1.0;
+    const double aum = fabs(um), aup = fabs(up), au = fabs(u);
+    double z[NV];
+    z[0] = aum * ta * y[0];
+    z[1] = au * c1 * y[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) z[1 + k] = au * phat * y[1 + k];
+    z[E] = aup * ta * y[E];
+    const double zs = z[0] + z[1] + z[E];
+    // reverse: o = R z
+    double vmo = 0.0;   // Σ_{k≥1} v̄_k ō_{1+k}
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vmo = fma(vm[k], ob[1 + k], vmo);
+    double zb[NV];
+    zb[0] = ob[0] + um * ob[1] + (h - u * a) * ob[E] + vmo;
+    zb[1] = ob[0] + u * ob[1] + 0.5 * v2 * ob[E] + vmo;
+    zb[E] = ob[0] + up * ob[1] + (h + u * a) * ob[E] + vmo;
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) zb[1 + k] = fma(vm[k], ob[E], ob[1 + k]);
+    double vmb[3] = {0.0, 0.0, 0.0};
+    double ab_ = ob[1] * (z[E] - z[0]) + ob[E] * u * (z[E] - z[0]);
+    double hb = ob[E] * (z[0] + z[E]);
+    double v2b = 0.5 * ob[E] * z[1];
+    vmb[0] = ob[1] * zs + ob[E] * a * (z[E] - z[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) vmb[k] = fma(ob[1 + k], zs, ob[E] * z[1 + k]);
+    // z = |Λ| T y
+    double yb[NV], tab = 0.0, rhob = 0.0, phb = 0.0;
+    yb[0] = zb[0] * aum * ta;
+    vmb[0] += zb[0] * sm * ta * y[0];
+    ab_ -= zb[0] * sm * ta * y[0];
+    tab += zb[0] * aum * y[0];
+    yb[1] = zb[1] * au * c1;
+    vmb[0] += zb[1] * su * c1 * y[1];
+    rhob += zb[1] * au * g1 * ig * y[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        yb[1 + k] = zb[1 + k] * au * phat;
+        vmb[0] += zb[1 + k] * su * phat * y[1 + k];
+        phb += zb[1 + k] * au * y[1 + k];
+    }
+    yb[E] = zb[E] * aup * ta;
+    vmb[0] += zb[E] * sp * ta * y[E];
+    ab_ += zb[E] * sp * ta * y[E];
+    tab += zb[E] * aup * y[E];
+    rhob += tab * 0.5 * ig;
+    // y = Rᵀ ΔW
+    const double Sb = yb[0] + yb[E] + yb[1];
+    double dWb[NV];
+    dWb[0] = Sb;
+    dWb[1] = fma(u, Sb, a * (yb[E] - yb[0]));
+    ab_ += dW[1] * (yb[E] - yb[0]) + u * dW[E] * (yb[E] - yb[0]);
+    hb += dW[E] * (yb[0] + yb[E]);
+    vmb[0] += dW[1] * Sb + a * dW[E] * (yb[E] - yb[0]);
+    dWb[E] = (h - u * a) * yb[0] + (h + u * a) * yb[E] + 0.5 * v2 * yb[1];
+    v2b += 0.5 * dW[E] * yb[1];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        dWb[E] = fma(vm[k], yb[1 + k], dWb[E]);
+        dWb[1 + k] = fma(vm[k], Sb, yb[1 + k]);
+        vmb[k] += fma(dW[E], yb[1 + k], dW[1 + k] * Sb);
+    }
+    // h, a
+    double ibetb = 0.5 * g * ig1 * hb;
+    v2b += 0.5 * hb;
+    phb += ab_ * g * irho * 0.5 * ia;
+    double irhob = ab_ * g * phat * 0.5 * ia;
+    // ΔW
+    double Lbb = ig1 * dWb[0], Lrb = dWb[0];
+    double vl2b = -dWb[0] * bl, vr2b = dWb[0] * br;
+    double blb = -dWb[0] * vl2 - 2.0 * dWb[E], brb = dWb[0] * vr2 + 2.0 * dWb[E];
+    double vlb[3] = {0.0, 0.0, 0.0}, vrb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        blb = fma(2.0 * dWb[1 + k], vl[k], blb);
+        brb = fma(-2.0 * dWb[1 + k], vr[k], brb);
+        vlb[k] = 2.0 * bl * dWb[1 + k];
+        vrb[k] = -2.0 * br * dWb[1 + k];
+    }
+    // v2 = 2|v̄|² - ½(|v_l|² + |v_r|²), v̄ = (v_l + v_r)/2
+    vl2b -= 0.5 * v2b;
+    vr2b -= 0.5 * v2b;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        const double m = vmb[k] + 4.0 * vm[k] * v2b;   // v̄_k cotangent incl. |v̄|²
+        vlb[k] += fma(0.5, m, 2.0 * vl[k] * vl2b);
+        vrb[k] += fma(0.5, m, 2.0 * vr[k] * vr2b);
+    }
+    // means: p̂ = ½ s_ρ/s_β, 1/ρ_ln, 1/β_ln, and the logarithms
+    rhob -= irhob * irho * irho;
+    const double betb = -ibetb * ibet * ibet;
+    double rlb = fma(rhob, dra, 0.5 * phb * isb) + Lrb / rl;
+    double rrb = fma(rhob, drb, 0.5 * phb * isb) - Lrb / rr;
+    blb += fma(betb, dba, -phb * phat * isb) + Lbb / bl;
+    brb += fma(betb, dbb, -phb * phat * isb) - Lbb / br;
+    // β = ρ/(2p)
+    rlb = fma(0.5 * ipl, blb, rlb);
+    rrb = fma(0.5 * ipr, brb, rrb);
+    L.p -= blb * bl * ipl;
+    R.p -= brb * br * ipr;
+    qa[0] += rlb;
+    qb[0] += rrb;
+    L.u += vlb[0];
+    R.u += vrb[0];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        L.vt[k - 1] += vlb[k];
+        R.vt[k - 1] += vrb[k];
+    }
+}
+
+// KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC,
+// 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage),
+// 6 MatrixDissipation(StdAverage), 7 MatrixDissipation(ChandrasekharAverage).
+template <int DIM, int KIND>
+__global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
+    constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
+    constexpr bool SD = KIND == 4 || KIND == 5;
+    constexpr bool MD = KIND >= 6;
+    constexpr int NV = DIM + 2;
+    int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)P.nfaces * P.nfd) return;
+    int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
+    int n = P.n;
+    int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
+    const double* dgl = P.ops + 2 * n * n + 2 * n;
+    const double* dgr = dgl + n;
+    auto endnode = [&](int32_t s, int64_t* g, double* dg) {
+        int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
+        *g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+        *dg = right ? dgr[n - 1] : dgl[0];
+    };
+    int64_t g1i, g2i = 0;
+    double dg1, dg2 = 0.0;
+    if (kChecked && !(index_ok(s0 >> 3, P.ndofs / P.npe, P.status, 0) &&
+                      (s1 < 0 || index_ok(s1 >> 3, P.ndofs / P.npe, P.status, s0 >> 3)) &&
+                      (s1 >= 0 || index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3))))
+        return;
+    endnode(s0, &g1i, &dg1);
+    double qL[NV], qR[NV], Fb[NV];
+    double w1 = P.invJ[s0 >> 3] * P.s_lam;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        qL[k] = P.U[k * P.ndofs + g1i];
+        Fb[k] = -dg1 * (w1 * P.Ain[k * P.ndofs + g1i]);
+    }
+    if (s1 >= 0) {
+        endnode(s1, &g2i, &dg2);
+        double w2 = P.invJ[s1 >> 3] * P.s_lam;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qR[k] = P.U[k * P.ndofs + g2i];
+            Fb[k] = fma(dg2, w2 * P.Ain[k * P.ndofs + g2i], Fb[k]);
+        }
+    }
+    FrameAxes A = frame_axes<DIM>(s0 & 7);
+    double J = P.faceJ[f];
+    // face frame: a = R qL, b = R qR (or the boundary state), F̄ = J R F̄_phys
+    double a[NV], b[NV], fb[NV];
+    a[0] = qL[0];
+    a[DIM + 1] = qL[DIM + 1];
+    fb[0] = J * Fb[0];
+    fb[DIM + 1] = J * Fb[DIM + 1];
+    cart_to_face<DIM>(qL, A, a);
+    {
+        double t[NV];
+        cart_to_face<DIM>(Fb, A, t);
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) fb[1 + r] = J * t[1 + r];
+    }
+    int bck = 0;
+    if (s1 >= 0) {
+        b[0] = qR[0];
+        b[DIM + 1] = qR[DIM + 1];
+        cart_to_face<DIM>(qR, A, b);
+    } else {
+        bck = P.bc_kind[P.face_bc[f]];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) b[k] = a[k];   // outflow; slip flips the normal momentum
+        if (bck == FLOU_BC_SLIP) b[1] = -a[1];
+    }
+    double inten = P.intensity;
+    if (P.elem_c) {
+        int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
+        inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
+    }
+    const double g = P.gamma, g1 = g - 1.0;
+    Prim pa = prim_of<DIM>(a, g);
+    const double* bb = b;
+    Prim pb = prim_of<DIM>(bb, g);
+    double ab[NV], bbar[NV];
+    double Ib = 0.0;
+    if (KIND == 2 || KIND == 3) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
+#pragma unroll
+        for (int k = 0; k < NV; ++k) ab[k] = bbar[k] = 0.0;
+        hll_family_vjp<DIM>(KIND == 3, a, bb, pa, pb, g, fb, ab, bbar);
+    } else {
+    double ll = fabs(pa.v[0]) + pa.a, lr = fabs(pb.v[0]) + pb.a;
+    bool left = lr < ll;   // Base.max(ll, lr)
+    double lam = left ? ll : lr;
+    double dot = 0.0;
+    SideBar Ls = {}, Rs = {};
+    if (MD) {   // F = A + ½ · intensity · R|Λ|TRᵀΔW: no wave-speed maximum
+        double ob[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ob[k] = 0.5 * inten * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        md_vjp<DIM>(pa, pb, g, ob, ab, bbar, Ls, Rs);
+    } else if (SD) {   // F = A - λ/2 · intensity · D(a, b)
+        double D[NV], Db[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            Db[k] = -0.5 * inten * lam * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        sd_jump_vjp<DIM>(a, bb, pa, pb, g, Db, D, ab, bbar, Ls, Rs);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dot = fma(-fb[k], D[k], dot);
+    } else {    // F = A + λ/2 · intensity · (a - b)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ab[k] = 0.5 * inten * lam * fb[k];
+            bbar[k] = -ab[k];
+        }
+    }
+    Ib = (SD || MD) ? 0.0 : 0.5 * lam * dot;   // the dissipation fluxes take no per-element scale
+    if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
+        PrimBar o1, o2;
+        double vh1[DIM], vh2[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            vh1[k] = 0.5 * pa.v[k];
+            vh2[k] = 0.5 * pb.v[k];
+        }
+        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho * rcp_refined(pa.p), 0.25 * pa.vv,
+                                       0.5 * pb.rho, vh2, 0.25 * pb.rho * rcp_refined(pb.p), 0.25 * pb.vv,
+                                       0.5 / g1, fb, o1, o2);
+        prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
+        prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
+    } else {
+        euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
+        euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
+    }
+    if (!MD) {
+        double kappa = 0.5 * inten * dot;
+        if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
+        else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    }
+    if (SD || MD) {
+        side_prim_vjp<DIM>(pa, g, Ls, ab);
+        side_prim_vjp<DIM>(pb, g, Rs, bbar);
+    }
+    }
+    if (s1 < 0) {
+        if (bck == FLOU_BC_OUTFLOW) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) ab[k] += bbar[k];
+        } else if (bck == FLOU_BC_SLIP) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) ab[k] += (k == 1) ? -bbar[k] : bbar[k];
+        }
+    }
+    // back to the physical frame (Rᵀ)
+    double oL[NV], oR[NV];
+    oL[0] = ab[0];
+    oL[DIM + 1] = ab[DIM + 1];
+    oR[0] = bbar[0];
+    oR[DIM + 1] = bbar[DIM + 1];
+    cart_to_phys<DIM>(ab, A, oL);
+    cart_to_phys<DIM>(bbar, A, oR);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        P.QbL[k * P.nfdofs + gid] = oL[k];
+        if (s1 >= 0) P.QbR[k * P.nfdofs + gid] = oR[k];
+    }
+    P.Ibar[gid] = Ib;
+}
+
+template <int DIM, int N>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
+    extern __shared__ double smem[];
+    double* sops = smem;
+    double* sw = sops + S::NOPS;   // [NV][NN]: w = λ / J
+    const int tid = threadIdx.x;
+    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    const int e0 = blockIdx.x * S::EPB;
+    const int el = tid / NPE, i = tid - el * NPE;
+    const int e = e0 + el;
+    const bool active = (tid < NN) && (e < P.nelem);
+    int64_t gi = (int64_t)e * NPE + i;
+    double ain[NV];
+    if (active) {
+        double w = P.invJ[e] * P.s_lam;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ain[k] = P.Ain[k * P.ndofs + gi];
+            sw[k * NN + tid] = w * ain[k];
+        }
+    }
+    __syncthreads();
+    if (!active) return;
+    double q[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
+    Prim pr = prim_of<DIM, false>(q, P.gamma);
+    const double g1 = P.gamma - 1.0;
+    double qb[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) qb[k] = 0.0;
+    const double* Ds = sops;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int pos, line;
+        tp_coords<DIM>(N, i, d, pos, line);
+        double G[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) G[k] = 0.0;
+#pragma unroll
+        for (int r = 0; r < N; ++r) {   // Σ_rows Ds(row, pos) w_row  (transpose)
+            int j = el * NPE + tp_node<DIM>(N, d, line, r);
+            double a = Ds[r + pos * N];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) G[k] = fma(a, sw[k * NN + j], G[k]);
+        }
+        euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
+        // trace cotangents of the faces this node lies on (LGL: the end nodes)
+        if (pos == 0 || pos == N - 1) {
+            int32_t pk = P.elem_face[e * 2 * DIM + 2 * d + (pos == 0 ? 0 : 1)];
+            const double* src = (pk & 1) ? P.QbR : P.QbL;
+            int64_t o = (int64_t)(pk >> 1) * NFD + line;
+            if (!index_ok(o, P.nfdofs, P.status, e)) continue;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qb[k] += __ldcg(src + k * P.nfdofs + o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double o = fma(P.alpha, ain[k], qb[k]);
+        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
+        if (P.writeB) {
+            double b = P.delta_B * ain[k];
+            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
+            P.B[k * P.ndofs + gi] = b;
+        }
+        P.Aout[k * P.ndofs + gi] = o;
+    }
+    if (P.cbar && i == 0) {   // intensity (c1 + c2)/2: each side gets half, a boundary face all
+        double acc = 0.0;
+        for (int fk = 0; fk < 2 * DIM; ++fk) {
+            int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            int fc = pk >> 1;
+            if (!index_ok((int64_t)fc * NFD + NFD - 1, P.nfdofs, P.status, e)) continue;
+            double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+            for (int m = 0; m < NFD; ++m) acc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + m), acc);
+        }
+        P.cbar[e] += acc;
+    }
+}
+
+template <int DIM, int N>
+cudaError_t launch_adj_elem_n(const AdjElemParams& P, cudaStream_t s) {
+    using S = Shape<DIM, N>;
+    constexpr size_t smem = sizeof(double) * (S::NOPS + (DIM + 2) * S::NN);
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    if (attr != cudaSuccess) return attr;
+    int grid = (P.nelem + S::EPB - 1) / S::EPB;
+    adj_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
+    switch (n) {
+        case 2: return launch_adj_elem_n<DIM, 2>(P, s);
+        case 3: return launch_adj_elem_n<DIM, 3>(P, s);
+        case 4: return launch_adj_elem_n<DIM, 4>(P, s);
+        case 5: return launch_adj_elem_n<DIM, 5>(P, s);
+        case 6: return launch_adj_elem_n<DIM, 6>(P, s);
+        case 7: return launch_adj_elem_n<DIM, 7>(P, s);
+        case 8: return launch_adj_elem_n<DIM, 8>(P, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// Split-form element adjoint.  Per direction, a pair phase evaluates every symmetric pair of
+// the block's lines once and keeps the primitive cotangents of both nodes in shared memory;
+// the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux;
+// zero on interior LGL nodes) and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved
+// variables.
+template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR>
+struct AdjSplitShape {
+    using S = Shape<DIM, N>;
+    static constexpr bool KG = TP == FLOU_TP_KENNEDY_GRUBER;
+    static constexpr bool STD = TP == FLOU_TP_STD_AVERAGE;
+    static constexpr int NV = DIM + 2;
+    // per node: rh, vh, bh, vq (KG: rh, vh, ph, eh; StdAverage: H, v, |v|²)
+    static constexpr int NARR = DIM + 3;
+    // per side of a pair: ρ̄, v̄, β̄ (KG: ρ̄, v̄, p̄, ē; StdAverage: the conserved cotangent)
+    static constexpr int NPB = KG ? DIM + 3 : DIM + 2;
+    static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
+    static constexpr int NSD = S::EPB * DIM * N * N;           // -Ja_d D♯ per element and direction
+    static constexpr size_t SMEM =
+        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
+        2 * (S::NPAIR + 1);
+    // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
+    static constexpr int MINB = (S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
+};
+
+template <int DIM, int N, int D, int TP>
+__device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, const double* sJD,
+                                                const double* sprim, const double* sw, double* spb,
+                                                const uint8_t* stab, double cb) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
+    constexpr int NPT = A::NPT, NPB = A::NPB;
+    for (int kp = threadIdx.x; kp < NPT; kp += blockDim.x) {
+        int elp = kp / (NFD * NPAIR);
+        int r = kp - elp * (NFD * NPAIR);
+        int line = r / NPAIR, pp = r - line * NPAIR;
+        if (e0 + elp >= P.nelem) continue;
+        int a = stab[2 * pp], b = stab[2 * pp + 1];
+        int ia = elp * NPE + tp_node<DIM>(N, D, line, a);
+        int ib = elp * NPE + tp_node<DIM>(N, D, line, b);
+        const double* jd = sJD + (elp * DIM + D) * N * N;   // -Ja_D D♯(i, j) = jd[i + j N]
+        double cab = jd[a + b * N], cba = jd[b + a * N];
+        double Fb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fb[k] = fma(cab, sw[k * NN + ia], cba * sw[k * NN + ib]);
+        double v1[DIM], v2[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            v1[k] = sprim[(1 + k) * NN + ia];
+            v2[k] = sprim[(1 + k) * NN + ib];
+        }
+        PrimBar o1, o2;
+        if constexpr (A::STD) {   // F♯ = ½ (F(Q_a) + F(Q_b)): each node gets ½ J(Q)ᵀ F̄ in conserved variables
+            const double g1 = P.gamma - 1.0;
+            double qa_[NV], qb_[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qa_[k] = qb_[k] = 0.0;
+            euler_flux_vjp<DIM>(D, v1, sprim[(1 + DIM) * NN + ia], sprim[ia], g1, Fb, 0.5, qa_);
+            euler_flux_vjp<DIM>(D, v2, sprim[(1 + DIM) * NN + ib], sprim[ib], g1, Fb, 0.5, qb_);
+            o1.r = qa_[0];
+            o2.r = qb_[0];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                o1.v[k] = qa_[1 + k];
+                o2.v[k] = qb_[1 + k];
+            }
+            o1.b = qa_[DIM + 1];
+            o2.b = qb_[DIM + 1];
+        } else if constexpr (A::KG)
+            kg_pair_vjp<DIM, D>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia], sprim[ib], v2,
+                                sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], Fb, o1, o2);
+        else
+            chandra_pair_vjp<DIM, D, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
+                                            sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
+                                            Fb, o1, o2);
+        spb[kp] = o1.r;
+        spb[NPB * NPT + kp] = o2.r;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            spb[(1 + k) * NPT + kp] = o1.v[k];
+            spb[(NPB + 1 + k) * NPT + kp] = o2.v[k];
+        }
+        spb[(1 + DIM) * NPT + kp] = o1.b;
+        spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
+        if constexpr (A::KG) {
+            spb[(2 + DIM) * NPT + kp] = o1.e;
+            spb[(NPB + 2 + DIM) * NPT + kp] = o2.e;
+        }
+    }
+}
+
+template <int DIM, int N, int D, int TP>
+__device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
+                                                const double* Dsh, const double* sw, const double* spb,
+                                                const double* v, double rho, double p, double g1, double* qb,
+                                                PrimBar& acc) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
+    constexpr int NV = DIM + 2, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
+    constexpr int NPT = A::NPT, NPB = A::NPB;
+    int pos, line;
+    tp_coords<DIM>(N, i, D, pos, line);
+    const int tid = threadIdx.x;
+    double dii = Dsh[pos + pos * N];
+    if (dii != 0.0) {   // diagonal: F♯(i, i) = F(Q_i)
+        double G[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) G[k] = dii * sw[k * NN + tid];
+        double vv = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
+        double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) * rcp_refined(rho);
+        euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
+    }
+    int pbase = el * NFD * NPAIR + line * NPAIR;
+    // the N-1 partners of pos, cyclically from pos + 1: every iteration is a pair (a skipped
+    // j == pos would still take its FP64 issue slots as predicated-off instructions)
+#pragma unroll
+    for (int t = 1; t < N; ++t) {
+        const int j = pos + t < N ? pos + t : pos + t - N;
+        int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+        int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+        const double* src = spb + (pos == lo ? 0 : NPB * NPT);
+        acc.r += src[pidx];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
+        acc.b += src[(1 + DIM) * NPT + pidx];
+        if constexpr (A::KG) acc.e += src[(2 + DIM) * NPT + pidx];
+    }
+    if (pos == 0 || pos == N - 1) {
+        int32_t pk = P.elem_face[e * 2 * DIM + 2 * D + (pos == 0 ? 0 : 1)];
+        const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
+        int64_t o = (int64_t)(pk >> 1) * NFD + line;
+        if (index_ok(o, P.nfdofs, P.status, e)) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
+        }
+    }
+}
+
+template <int DIM, int N, int TP>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP>::MINB)
+    adj_split_elem_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
+    constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
+    extern __shared__ double smem[];
+    double* sops = smem;
+    double* sprim = sops + S::NOPS;   // [NARR][NN]: ρ/2, v/2, β/2, |v|²/4 (KG: ρ/2, v/2, p/2, (E/ρ)/2)
+    double* sw = sprim + NARR * NN;   // [NV][NN]: w = λ / J
+    double* spb = sw + NV * NN;       // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
+    double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
+    uint8_t* stab = (uint8_t*)(sJD + A::NSD);
+    const int tid = threadIdx.x;
+    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    for (int t = tid; t < A::NSD; t += blockDim.x) {
+        int q = t / (N * N), ij = t - q * (N * N);
+        int elq = q / DIM, d = q - elq * DIM;
+        int eq_ = blockIdx.x * S::EPB + elq;
+        sJD[t] = eq_ < P.nelem ? -P.Ja[eq_ * DIM + d] * P.ops[N * N + ij] : 0.0;
+    }
+    if (tid == 0) {
+        int c = 0;
+        for (int a = 0; a < N; ++a)
+            for (int b = a + 1; b < N; ++b) { stab[2 * c] = (uint8_t)a; stab[2 * c + 1] = (uint8_t)b; ++c; }
+    }
+    const int e0 = blockIdx.x * S::EPB;
+    const int el = tid / NPE, i = tid - el * NPE;
+    const int e = e0 + el;
+    const bool active = (tid < NN) && (e < P.nelem);
+    const int64_t gi = (int64_t)e * NPE + i;
+    const double g = P.gamma, g1 = g - 1.0;
+    double rho = 1.0, p = 1.0, v[DIM];
+    if (active) {
+        double w = P.invJ[e] * P.s_lam;
+        double q[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sw[k * NN + tid] = w * P.Ain[k * P.ndofs + gi];
+            q[k] = P.U[k * P.ndofs + gi];
+        }
+        rho = q[0];
+        double ir = rcp_refined(rho), ke = 0.0, vv = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            v[k] = q[1 + k] * ir;
+            ke = fma(q[1 + k], v[k], ke);
+            vv = fma(v[k], v[k], vv);
+        }
+        p = g1 * fma(-0.5, ke, q[DIM + 1]);
+        sprim[tid] = 0.5 * rho;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = 0.5 * v[k];
+        if constexpr (A::STD) {
+            sprim[tid] = (q[DIM + 1] + p) * ir;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) sprim[(1 + k) * NN + tid] = v[k];
+            sprim[(1 + DIM) * NN + tid] = vv;
+        } else if constexpr (A::KG) {
+            sprim[(1 + DIM) * NN + tid] = 0.5 * p;
+            sprim[(2 + DIM) * NN + tid] = 0.5 * (q[DIM + 1] * ir);
+        } else {
+            sprim[(1 + DIM) * NN + tid] = (0.25 * rho) * rcp_refined(p);
+            sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) v[k] = 0.0;
+    }
+    __syncthreads();
+    const double* Dsh = sops + N * N;   // D♯(i, j) = Dsh[i + j N]
+    const double cb = 0.5 / g1;
+    double qb[NV];
+    PrimBar acc;
+    acc.r = 0.0;
+    acc.b = 0.0;
+    acc.e = 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) qb[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
+#pragma unroll 1
+    for (int dir = 0; dir < DIM; ++dir) {
+        if (dir == 0) adj_split_pairs<DIM, N, 0, TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        __syncthreads();
+        if (active) {
+            if (dir == 0) adj_split_nodes<DIM, N, 0, TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            else if (dir == 1)
+                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            else
+                adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    double vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
+    if constexpr (A::STD) {   // the pairs' cotangents are already conserved
+        qb[0] += acc.r;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) qb[1 + k] += acc.v[k];
+        qb[DIM + 1] += acc.b;
+    } else if constexpr (A::KG) {
+        kg_prim_to_cons_vjp<DIM>(rho, v, vv, P.U[(DIM + 1) * P.ndofs + gi], g1, acc, qb);
+    } else {
+        prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
+    }
+    for (int k = 0; k < NV; ++k) {
+        double ain = P.Ain[k * P.ndofs + gi];
+        double o = fma(P.alpha, ain, qb[k]);
+        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
+        if (P.writeB) {
+            double b = P.delta_B * ain;
+            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
+            P.B[k * P.ndofs + gi] = b;
+        }
+        P.Aout[k * P.ndofs + gi] = o;
+    }
+    if (P.cbar && i == 0) {
+        double cacc = 0.0;
+        for (int fk = 0; fk < 2 * DIM; ++fk) {
+            int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            int fc = pk >> 1;
+            if (!index_ok((int64_t)fc * S::NFD + S::NFD - 1, P.nfdofs, P.status, e)) continue;
+            double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+            for (int m = 0; m < S::NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * S::NFD + m), cacc);
+        }
+        P.cbar[e] += cacc;
+    }
+}
+
+template <int DIM, int N, int TP>
+cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
+    using S = Shape<DIM, N>;
+    constexpr size_t smem = AdjSplitShape<DIM, N, TP>::SMEM;
+    static_assert(smem <= 227 * 1024, "split adjoint tile exceeds shared memory");
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem);
+    });
+    if (attr != cudaSuccess) return attr;
+    int grid = (P.nelem + S::EPB - 1) / S::EPB;
+    adj_split_elem_kernel<DIM, N, TP><<<grid, S::BLOCK, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int DIM, int TP>
+cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
+    switch (n) {
+        case 2: return launch_adj_split_n<DIM, 2, TP>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3, TP>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4, TP>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5, TP>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6, TP>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7, TP>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8, TP>(P, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// The split form's two-point flux: Chandrashekar, Kennedy-Gruber or StdAverage.
+template <int DIM>
+cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
+    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER>(n, P, s);
+    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE>(n, P, s);
+    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR>(n, P, s);
+}
+
+
+// Launchers, one translation unit each (explicit instantiations of the templates above).
+cudaError_t launch_adj_face(int dim, int kind, int grid, int tb, const AdjFaceParams& F, cudaStream_t s);
+cudaError_t launch_adj_elem_dim(int dim, int n, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s);
+
+}  // namespace flou

@@ -1,0 +1,7 @@
+// Split-form element VJP kernels of the discrete adjoint, 1D (adjoint_kernels.cuh).
+#include "adjoint_kernels.cuh"
+namespace flou {
+cudaError_t launch_adj_split_1d(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
+    return launch_adj_split<1>(n, tp, P, s);
+}
+}  // namespace flou
