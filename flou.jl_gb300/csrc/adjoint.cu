@@ -67,8 +67,6 @@ int adj_supported(flou_ctx* c) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
     if (c->lsrk_s)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint steps with SSP-RK3 (flou_set_integrator 0)");
-    if (c->curv)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint covers Cartesian geometry");
     for (int b = 0; b < c->nbcs; ++b)
         if (c->bc_kind[b] == FLOU_BC_INFLOW || c->bc_kind[b] == FLOU_BC_STATE_FIELD)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint supports periodic, slip and outflow boundaries");
@@ -112,6 +110,10 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     F.invJ = c->d_invJ;
     F.ops = c->d_ops;
     F.elem_c = c->d_c;
+    F.frames = c->d_frames;
+    F.faceJn = c->d_faceJn;
+    F.orient = c->d_orient;
+    F.invJn = c->d_invJn;
     F.intensity = c->cfg.numflux_intensity;
     F.gamma = c->cfg.gamma;
     F.ndofs = c->ndofs;
@@ -129,7 +131,7 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
     const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch
                    : nf == FLOU_NF_MATRIX_DISSIPATION ? 6 + ch : ch;
-    cudaError_t e = launch_adj_face(dim, kind, grid, tb, F, s);
+    cudaError_t e = launch_adj_face(dim, kind, c->curv, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
     memset(&P, 0, sizeof(P));
@@ -146,6 +148,9 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.face_elem = c->d_face_elem;
     P.invJ = c->d_invJ;
     P.Ja = c->d_Ja;
+    P.invJn = c->d_invJn;
+    P.Jan = c->d_Jan;
+    P.orient = c->d_orient;
     P.ops = c->d_ops;
     P.ndofs = c->ndofs;
     P.nfdofs = c->nfdofs;
@@ -159,9 +164,9 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.writeB = writeB;
     P.gamma = c->cfg.gamma;
     if (c->cfg.volume_op == FLOU_OP_SPLIT) {
-        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, P, s);
+        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, P, s);
     } else {
-        e = launch_adj_elem_dim(dim, c->n, P, s);
+        e = launch_adj_elem_dim(dim, c->n, c->curv, P, s);
     }
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint element kernel");
     return FLOU_OK;

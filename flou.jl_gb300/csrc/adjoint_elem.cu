@@ -1,7 +1,8 @@
 // Strong-form element VJP kernels of the discrete adjoint (adjoint_kernels.cuh).
 #include "adjoint_kernels.cuh"
 namespace flou {
-cudaError_t launch_adj_elem_dim(int dim, int n, const AdjElemParams& P, cudaStream_t s) {
+cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s) {
+    if (curv) return dim == 2 ? launch_adj_elem<2, true>(n, P, s) : launch_adj_elem<3, true>(n, P, s);
     if (dim == 1) return launch_adj_elem<1>(n, P, s);
     if (dim == 2) return launch_adj_elem<2>(n, P, s);
     return launch_adj_elem<3>(n, P, s);
@@ -11,7 +12,10 @@ namespace flou {
 cudaError_t launch_adj_split_1d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_2d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s) {
+cudaError_t launch_adj_split_curv2d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_curv3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s) {
+    if (curv) return dim == 2 ? launch_adj_split_curv2d(n, tp, P, s) : launch_adj_split_curv3d(n, tp, P, s);
     if (dim == 1) return launch_adj_split_1d(n, tp, P, s);
     if (dim == 2) return launch_adj_split_2d(n, tp, P, s);
     return launch_adj_split_3d(n, tp, P, s);

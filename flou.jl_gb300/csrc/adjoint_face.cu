@@ -1,7 +1,9 @@
 // Face VJP kernels of the discrete adjoint (adjoint_kernels.cuh), every dimension and flux kind.
 #include "adjoint_kernels.cuh"
 namespace flou {
-cudaError_t launch_adj_face(int dim, int kind, int grid, int tb, const AdjFaceParams& F, cudaStream_t s) {
+cudaError_t launch_adj_face_curv(int dim, int kind, int grid, int tb, const AdjFaceParams& F, cudaStream_t s);
+cudaError_t launch_adj_face(int dim, int kind, bool curv, int grid, int tb, const AdjFaceParams& F, cudaStream_t s) {
+    if (curv) return launch_adj_face_curv(dim, kind, grid, tb, F, s);
     switch (dim * 8 + kind) {
         case 8: adj_face_kernel<1, 0><<<grid, tb, 0, s>>>(F); break;
         case 9: adj_face_kernel<1, 1><<<grid, tb, 0, s>>>(F); break;

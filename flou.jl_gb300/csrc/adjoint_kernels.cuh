@@ -41,6 +41,12 @@ namespace flou {
 
 struct AdjFaceParams {
     int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
+    // general geometry (CURV kernels): per face node frame [9][nfdofs] and surface Jacobian,
+    // per face orientation, per node 1/J
+    const double* frames;
+    const double* faceJn;
+    const uint8_t* orient;
+    const double* invJn;
     const double* U;        // state the residual is linearised at
     const double* Ain;      // adjoint input; λ = s_lam * Ain
     double s_lam;
@@ -61,6 +67,11 @@ struct AdjFaceParams {
 
 struct AdjElemParams {
     int32_t* status;        // index-check reports (FLOU_CUDA_CHECKED builds)
+    // general geometry (CURV kernels): per node 1/J and metric Ja[k][d] at (k + d DIM) * ndofs,
+    // per face orientation
+    const double* invJn;
+    const double* Jan;
+    const uint8_t* orient;
     const double* U;
     const double* Ain;
     double* Aout;           // alpha Ain + beta B + VJP
@@ -102,6 +113,27 @@ __device__ __forceinline__ void euler_flux_vjp(int d, const double* v, double vv
         qb[1 + k] += scale * r;
     }
     qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1] * v[d]);
+}
+
+// The same for the flux along a general direction n (F_n = Σ_d n_d F_d, general geometry), with
+// vn = v·n:  P̄ = Σ_k ḡ_mk n_k + ḡ_E vn,  q̄_ρ += -vn (s + ḡ_E H) + (γ-1)|v|²/2 P̄,
+//   q̄_mk += vn ḡ_mk - (γ-1) v_k P̄ + n_k (ḡ_ρ + s + ḡ_E H),  q̄_E += ḡ_E vn + (γ-1) P̄.
+template <int DIM>
+__device__ __forceinline__ void euler_flux_vjp_n(const double* nrm, const double* v, double vv, double H, double g1,
+                                                 const double* gb, double scale, double* qb) {
+    double vn = 0.0, s = 0.0, Pb = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vn = fma(v[k], nrm[k], vn);
+        s = fma(gb[1 + k], v[k], s);
+        Pb = fma(gb[1 + k], nrm[k], Pb);
+    }
+    Pb = fma(gb[DIM + 1], vn, Pb);
+    double t = s + gb[DIM + 1] * H;
+    qb[0] += scale * (fma(0.5 * g1 * vv, Pb, -vn * t));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) qb[1 + k] += scale * fma(nrm[k], gb[0] + t, fma(vn, gb[1 + k], -g1 * v[k] * Pb));
+    qb[DIM + 1] += scale * fma(g1, Pb, gb[DIM + 1] * vn);
 }
 
 // Primitive quantities of one node with the reciprocals the VJPs reuse (1/ρ, 1/a), from the
@@ -192,10 +224,13 @@ __device__ __forceinline__ void logmean_half(double h1, double h2, double hs, do
 // Inputs are the halved node quantities rh = ρ/2, vh = v/2, bh = β/2, vq = |v|²/4; one
 // reciprocal 1/(ρ̄ β̄) serves both means and the pressure average.  Cotangents are with
 // respect to (ρ, v, β) of each side.
+// D < 0: the flux along the general direction nrm (general geometry), m = ρ̂ v̄·n and p̂ n in the
+// momentum flux.
 template <int DIM, int D, bool WL2>
 __device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, double bh1, double vq1, double rh2,
                                                  const double* vh2, double bh2, double vq2, double cb,
-                                                 const double* Fb, PrimBar& o1, PrimBar& o2) {
+                                                 const double* Fb, PrimBar& o1, PrimBar& o2,
+                                                 const double* nrm = nullptr) {
     double hsr = rh1 + rh2, hdr = rh1 - rh2, hsb = bh1 + bh2, hdb = bh1 - bh2;
     double R = rcp_refined(hsr * hsb);
     double rs = hsb * R, rb = hsr * R;   // 1/hsr, 1/hsb
@@ -212,7 +247,20 @@ __device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, 
     double S4 = vq1 + vq2;
     if (WL2 && DIM == 3) S4 = S4 + (vh1[2] * vh1[2] - vh2[2] * vh2[2]);
     double h = fma(cb, ibeta, -S4) + fma(p, irho, vv);
-    double m = rho * va[D];
+    double vd, fn;   // v̄ along the direction, and the normal component of the momentum cotangent
+    if constexpr (D >= 0) {
+        vd = va[D];
+        fn = Fb[1 + D];
+    } else {
+        vd = 0.0;
+        fn = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            vd = fma(va[k], nrm[k], vd);
+            fn = fma(Fb[1 + k], nrm[k], fn);
+        }
+    }
+    double m = rho * vd;
     double mb = fma(Fb[DIM + 1], h, Fb[0]);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], va[k], mb);
@@ -221,9 +269,14 @@ __device__ __forceinline__ void chandra_pair_vjp(double rh1, const double* vh1, 
     double hvab[DIM];   // v̄̄/2: the cotangent of v̄, halved (v̄ = (v1 + v2)/2)
 #pragma unroll
     for (int k = 0; k < DIM; ++k) hvab[k] = fma(mh, Fb[1 + k], hb * va[k]);
-    hvab[D] = fma(0.5 * mb, rho, hvab[D]);
-    double pb = fma(hb, irho, Fb[1 + D]);
-    double rhob = fma(mb, va[D], -hb * p * (irho * irho));
+    if constexpr (D >= 0) {
+        hvab[D] = fma(0.5 * mb, rho, hvab[D]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) hvab[k] = fma(0.5 * mb * rho, nrm[k], hvab[k]);
+    }
+    double pb = fma(hb, irho, fn);
+    double rhob = fma(mb, vd, -hb * p * (irho * irho));
     double betab = -hb * cb * (ibeta * ibeta);
     double pr = 0.25 * pb * rb, pbb = -0.5 * pb * p * rb;
     o1.r = fma(rhob, dra, pr);
@@ -264,25 +317,45 @@ __device__ __forceinline__ void prim_to_cons_vjp(double rho, const double* v, do
 // evaluates it), F = [m, m v̄ + p̄ e_D, m ē + p̄ v̄_D] with m = ρ̄ v̄_D and the arithmetic means
 // ρ̄, v̄, p̄, ē (e = E/ρ).  Inputs are the halved node quantities (rh = ρ/2, vh = v/2, ph = p/2,
 // eh = e/2), so each mean is a sum of two; both nodes receive half of each mean's cotangent.
+// D < 0: along the general direction nrm, m = ρ̄ v̄·n, F = [m, m v̄ + p̄ n, m ē + p̄ v̄·n].
 template <int DIM, int D>
 __device__ __forceinline__ void kg_pair_vjp(double rh1, const double* vh1, double ph1, double eh1, double rh2,
                                             const double* vh2, double ph2, double eh2, const double* Fb,
-                                            PrimBar& o1, PrimBar& o2) {
+                                            PrimBar& o1, PrimBar& o2, const double* nrm = nullptr) {
     const double rho = rh1 + rh2, pm = ph1 + ph2, en = eh1 + eh2;
     double vm[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; ++k) vm[k] = vh1[k] + vh2[k];
-    const double m = rho * vm[D];
+    double vd, fn;
+    if constexpr (D >= 0) {
+        vd = vm[D];
+        fn = Fb[1 + D];
+    } else {
+        vd = 0.0;
+        fn = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            vd = fma(vm[k], nrm[k], vd);
+            fn = fma(Fb[1 + k], nrm[k], fn);
+        }
+    }
+    const double m = rho * vd;
     double mb = fma(Fb[DIM + 1], en, Fb[0]);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) mb = fma(Fb[1 + k], vm[k], mb);
-    o1.r = o2.r = 0.5 * mb * vm[D];
+    o1.r = o2.r = 0.5 * mb * vd;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) o1.v[k] = 0.5 * Fb[1 + k] * m;
-    o1.v[D] = fma(0.5 * mb, rho, fma(0.5 * Fb[DIM + 1], pm, o1.v[D]));
+    if constexpr (D >= 0) {
+        o1.v[D] = fma(0.5 * mb, rho, fma(0.5 * Fb[DIM + 1], pm, o1.v[D]));
+    } else {
+        const double cn = fma(0.5 * mb, rho, 0.5 * Fb[DIM + 1] * pm);   // the cotangent along n
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) o1.v[k] = fma(cn, nrm[k], o1.v[k]);
+    }
 #pragma unroll
     for (int k = 0; k < DIM; ++k) o2.v[k] = o1.v[k];
-    o1.b = o2.b = 0.5 * fma(Fb[DIM + 1], vm[D], Fb[1 + D]);
+    o1.b = o2.b = 0.5 * fma(Fb[DIM + 1], vd, fn);
     o1.e = o2.e = 0.5 * Fb[DIM + 1] * m;
 }
 
@@ -718,7 +791,10 @@ __device__ __forceinline__ void md_vjp(const Prim& pa, const Prim& pb, double g,
 // KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC,
 // 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage),
 // 6 MatrixDissipation(StdAverage), 7 MatrixDissipation(ChandrasekharAverage).
-template <int DIM, int KIND>
+// CURV: general geometry, the forward face kernel's CURV path transposed: the slave trace at
+// master2slave(m, o), per-node 1/J on both sides, the face-node frame (n, t, b) and surface
+// Jacobian (a = R q, F = J Rᵀ F_face: F̄_face = J R F̄, q̄ = Rᵀ ā).
+template <int DIM, int KIND, bool CURV = false>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
     constexpr bool SD = KIND == 4 || KIND == 5;
@@ -731,9 +807,9 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
     const double* dgl = P.ops + 2 * n * n + 2 * n;
     const double* dgr = dgl + n;
-    auto endnode = [&](int32_t s, int64_t* g, double* dg) {
+    auto endnode = [&](int32_t s, int mm, int64_t* g, double* dg) {
         int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
-        *g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+        *g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, mm, right ? n - 1 : 0);
         *dg = right ? dgr[n - 1] : dgl[0];
     };
     int64_t g1i, g2i = 0;
@@ -742,17 +818,19 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
                       (s1 < 0 || index_ok(s1 >> 3, P.ndofs / P.npe, P.status, s0 >> 3)) &&
                       (s1 >= 0 || index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3))))
         return;
-    endnode(s0, &g1i, &dg1);
+    endnode(s0, m, &g1i, &dg1);
     double qL[NV], qR[NV], Fb[NV];
-    double w1 = P.invJ[s0 >> 3] * P.s_lam;
+    double w1 = (CURV ? P.invJn[g1i] : P.invJ[s0 >> 3]) * P.s_lam;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         qL[k] = P.U[k * P.ndofs + g1i];
         Fb[k] = -dg1 * (w1 * P.Ain[k * P.ndofs + g1i]);
     }
     if (s1 >= 0) {
-        endnode(s1, &g2i, &dg2);
-        double w2 = P.invJ[s1 >> 3] * P.s_lam;
+        const int mm = CURV ? master2slave<DIM>(m, P.orient[f], n) : m;
+        if (CURV && !index_ok(mm, P.nfd, P.status, s1 >> 3)) return;
+        endnode(s1, mm, &g2i, &dg2);
+        double w2 = (CURV ? P.invJn[g2i] : P.invJ[s1 >> 3]) * P.s_lam;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             qR[k] = P.U[k * P.ndofs + g2i];
@@ -760,17 +838,31 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         }
     }
     FrameAxes A = frame_axes<DIM>(s0 & 7);
-    double J = P.faceJ[f];
+    FrameTab fr;
+    if (CURV) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            fr.n[c] = P.frames[c * P.nfdofs + gid];
+            fr.t[c] = P.frames[(3 + c) * P.nfdofs + gid];
+            fr.b[c] = P.frames[(6 + c) * P.nfdofs + gid];
+        }
+    }
+    double J = CURV ? P.faceJn[gid] : P.faceJ[f];
     // face frame: a = R qL, b = R qR (or the boundary state), F̄ = J R F̄_phys
     double a[NV], b[NV], fb[NV];
     a[0] = qL[0];
     a[DIM + 1] = qL[DIM + 1];
     fb[0] = J * Fb[0];
     fb[DIM + 1] = J * Fb[DIM + 1];
-    cart_to_face<DIM>(qL, A, a);
     {
         double t[NV];
-        cart_to_face<DIM>(Fb, A, t);
+        if (CURV) {
+            rotate_to_face<DIM>(qL, fr, a);
+            rotate_to_face<DIM>(Fb, fr, t);
+        } else {
+            cart_to_face<DIM>(qL, A, a);
+            cart_to_face<DIM>(Fb, A, t);
+        }
 #pragma unroll
         for (int r = 0; r < DIM; ++r) fb[1 + r] = J * t[1 + r];
     }
@@ -778,7 +870,8 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     if (s1 >= 0) {
         b[0] = qR[0];
         b[DIM + 1] = qR[DIM + 1];
-        cart_to_face<DIM>(qR, A, b);
+        if (CURV) rotate_to_face<DIM>(qR, fr, b);
+        else cart_to_face<DIM>(qR, A, b);
     } else {
         bck = P.bc_kind[P.face_bc[f]];
 #pragma unroll
@@ -876,8 +969,13 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     oL[DIM + 1] = ab[DIM + 1];
     oR[0] = bbar[0];
     oR[DIM + 1] = bbar[DIM + 1];
-    cart_to_phys<DIM>(ab, A, oL);
-    cart_to_phys<DIM>(bbar, A, oR);
+    if (CURV) {
+        rotate_to_phys<DIM>(ab, fr, oL);
+        rotate_to_phys<DIM>(bbar, fr, oR);
+    } else {
+        cart_to_phys<DIM>(ab, A, oL);
+        cart_to_phys<DIM>(bbar, A, oR);
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         P.QbL[k * P.nfdofs + gid] = oL[k];
@@ -886,7 +984,20 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     P.Ibar[gid] = Ib;
 }
 
-template <int DIM, int N>
+// Face-flux offset of the trace of line `line` of the face at local position fk of element e:
+// a slave reads the master's face dof that master2slave sends onto its line (CURV), as the
+// forward lift does.
+template <int DIM, int N, bool CURV>
+__device__ __forceinline__ int64_t trace_offset(const AdjElemParams& P, int e, int fk, int line) {
+    const int32_t pk = P.elem_face[e * 2 * DIM + fk];
+    int lm = line;
+    if (CURV && (pk & 1)) lm = master2slave<DIM>(line, inverse_orientation<DIM>(P.orient[pk >> 1]), N);
+    return (int64_t)(pk >> 1) * ipow(N, DIM - 1) + lm;
+}
+
+// CURV: general geometry: per-node 1/J, and the contravariant flux F̃_d = Σ_k Ja[k][d] F_k, whose
+// transpose gathers the directions first, G̃_k = Σ_d Ja[k][d] G_d, then takes one flux VJP per k.
+template <int DIM, int N, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
@@ -902,7 +1013,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
     int64_t gi = (int64_t)e * NPE + i;
     double ain[NV];
     if (active) {
-        double w = P.invJ[e] * P.s_lam;
+        double w = (CURV ? P.invJn[gi] : P.invJ[e]) * P.s_lam;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             ain[k] = P.Ain[k * P.ndofs + gi];
@@ -920,6 +1031,11 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
 #pragma unroll
     for (int k = 0; k < NV; ++k) qb[k] = 0.0;
     const double* Ds = sops;
+    double Gt[CURV ? DIM : 1][NV];   // CURV: G̃_k = Σ_d Ja[k][d] G_d
+#pragma unroll
+    for (int k = 0; k < (CURV ? DIM : 1); ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) Gt[k][v] = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         int pos, line;
@@ -934,16 +1050,30 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
 #pragma unroll
             for (int k = 0; k < NV; ++k) G[k] = fma(a, sw[k * NN + j], G[k]);
         }
-        euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
+        if constexpr (CURV) {
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                const double jkd = P.Jan[(k + d * DIM) * P.ndofs + gi];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Gt[k][v] = fma(jkd, G[v], Gt[k][v]);
+            }
+        } else {
+            euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
+        }
         // trace cotangents of the faces this node lies on (LGL: the end nodes)
         if (pos == 0 || pos == N - 1) {
-            int32_t pk = P.elem_face[e * 2 * DIM + 2 * d + (pos == 0 ? 0 : 1)];
+            const int fk = 2 * d + (pos == 0 ? 0 : 1);
+            const int32_t pk = P.elem_face[e * 2 * DIM + fk];
             const double* src = (pk & 1) ? P.QbR : P.QbL;
-            int64_t o = (int64_t)(pk >> 1) * NFD + line;
+            int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
             if (!index_ok(o, P.nfdofs, P.status, e)) continue;
 #pragma unroll
             for (int k = 0; k < NV; ++k) qb[k] += __ldcg(src + k * P.nfdofs + o);
         }
+    }
+    if constexpr (CURV) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) euler_flux_vjp<DIM>(k, pr.v, pr.vv, pr.H, g1, Gt[k], -1.0, qb);
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -969,31 +1099,32 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
     }
 }
 
-template <int DIM, int N>
+template <int DIM, int N, bool CURV = false>
 cudaError_t launch_adj_elem_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
     constexpr size_t smem = sizeof(double) * (S::NOPS + (DIM + 2) * S::NN);
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N, CURV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_elem_kernel<DIM, N><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_elem_kernel<DIM, N, CURV><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int DIM>
+template <int DIM, bool CURV = false>
 cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_elem_n<DIM, 2>(P, s);
-        case 3: return launch_adj_elem_n<DIM, 3>(P, s);
-        case 4: return launch_adj_elem_n<DIM, 4>(P, s);
-        case 5: return launch_adj_elem_n<DIM, 5>(P, s);
-        case 6: return launch_adj_elem_n<DIM, 6>(P, s);
-        case 7: return launch_adj_elem_n<DIM, 7>(P, s);
-        case 8: return launch_adj_elem_n<DIM, 8>(P, s);
+        case 2: return launch_adj_elem_n<DIM, 2, CURV>(P, s);
+        case 3: return launch_adj_elem_n<DIM, 3, CURV>(P, s);
+        case 4: return launch_adj_elem_n<DIM, 4, CURV>(P, s);
+        case 5: return launch_adj_elem_n<DIM, 5, CURV>(P, s);
+        case 6: return launch_adj_elem_n<DIM, 6, CURV>(P, s);
+        case 7: return launch_adj_elem_n<DIM, 7, CURV>(P, s);
+        case 8: return launch_adj_elem_n<DIM, 8, CURV>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -1022,7 +1153,9 @@ struct AdjSplitShape {
     static constexpr int MINB = (S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
 };
 
-template <int DIM, int N, int D, int TP>
+// CURV: the pair flux along the averaged metric column n̄ = (Ja_a + Ja_b)/2 of direction D (the
+// metric terms are in the flux; sJD then holds -D♯ alone).
+template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, const double* sJD,
                                                 const double* sprim, const double* sw, double* spb,
                                                 const uint8_t* stab, double cb) {
@@ -1049,14 +1182,27 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
             v1[k] = sprim[(1 + k) * NN + ia];
             v2[k] = sprim[(1 + k) * NN + ib];
         }
+        constexpr int DD = CURV ? -1 : D;   // the flux direction: the axis, or nrm
+        double nrm[DIM];
+        if constexpr (CURV) {
+            const int64_t ga = (int64_t)e0 * NPE + ia, gb = (int64_t)e0 * NPE + ib;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+                nrm[k] = 0.5 * (P.Jan[(k + D * DIM) * P.ndofs + ga] + P.Jan[(k + D * DIM) * P.ndofs + gb]);
+        }
         PrimBar o1, o2;
         if constexpr (A::STD) {   // F♯ = ½ (F(Q_a) + F(Q_b)): each node gets ½ J(Q)ᵀ F̄ in conserved variables
             const double g1 = P.gamma - 1.0;
             double qa_[NV], qb_[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) qa_[k] = qb_[k] = 0.0;
-            euler_flux_vjp<DIM>(D, v1, sprim[(1 + DIM) * NN + ia], sprim[ia], g1, Fb, 0.5, qa_);
-            euler_flux_vjp<DIM>(D, v2, sprim[(1 + DIM) * NN + ib], sprim[ib], g1, Fb, 0.5, qb_);
+            if constexpr (CURV) {
+                euler_flux_vjp_n<DIM>(nrm, v1, sprim[(1 + DIM) * NN + ia], sprim[ia], g1, Fb, 0.5, qa_);
+                euler_flux_vjp_n<DIM>(nrm, v2, sprim[(1 + DIM) * NN + ib], sprim[ib], g1, Fb, 0.5, qb_);
+            } else {
+                euler_flux_vjp<DIM>(D, v1, sprim[(1 + DIM) * NN + ia], sprim[ia], g1, Fb, 0.5, qa_);
+                euler_flux_vjp<DIM>(D, v2, sprim[(1 + DIM) * NN + ib], sprim[ib], g1, Fb, 0.5, qb_);
+            }
             o1.r = qa_[0];
             o2.r = qb_[0];
 #pragma unroll
@@ -1067,12 +1213,12 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
             o1.b = qa_[DIM + 1];
             o2.b = qb_[DIM + 1];
         } else if constexpr (A::KG)
-            kg_pair_vjp<DIM, D>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia], sprim[ib], v2,
-                                sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], Fb, o1, o2);
+            kg_pair_vjp<DIM, DD>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia], sprim[ib], v2,
+                                 sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], Fb, o1, o2, nrm);
         else
-            chandra_pair_vjp<DIM, D, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
-                                            sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
-                                            Fb, o1, o2);
+            chandra_pair_vjp<DIM, DD, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
+                                             sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
+                                             Fb, o1, o2, nrm);
         spb[kp] = o1.r;
         spb[NPB * NPT + kp] = o2.r;
 #pragma unroll
@@ -1089,7 +1235,9 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
     }
 }
 
-template <int DIM, int N, int D, int TP>
+// CURV: the diagonal term is the contravariant flux of node i (its own metric column), and a slave
+// face reads its trace cotangent through the orientation.
+template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
                                                 const double* Dsh, const double* sw, const double* spb,
                                                 const double* v, double rho, double p, double g1, double* qb,
@@ -1110,7 +1258,14 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
         double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) * rcp_refined(rho);
-        euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
+        if constexpr (CURV) {
+            double nrm[DIM];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
+            euler_flux_vjp_n<DIM>(nrm, v, vv, H, g1, G, -1.0, qb);
+        } else {
+            euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
+        }
     }
     int pbase = el * NFD * NPAIR + line * NPAIR;
     // the N-1 partners of pos, cyclically from pos + 1: every iteration is a pair (a skipped
@@ -1128,9 +1283,10 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         if constexpr (A::KG) acc.e += src[(2 + DIM) * NPT + pidx];
     }
     if (pos == 0 || pos == N - 1) {
-        int32_t pk = P.elem_face[e * 2 * DIM + 2 * D + (pos == 0 ? 0 : 1)];
+        const int fk = 2 * D + (pos == 0 ? 0 : 1);
+        int32_t pk = P.elem_face[e * 2 * DIM + fk];
         const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
-        int64_t o = (int64_t)(pk >> 1) * NFD + line;
+        int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
         if (index_ok(o, P.nfdofs, P.status, e)) {
 #pragma unroll
             for (int k = 0; k < NV; ++k) qb[k] += __ldcg(fsrc + k * P.nfdofs + o);
@@ -1138,7 +1294,7 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     }
 }
 
-template <int DIM, int N, int TP>
+template <int DIM, int N, int TP, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP>::MINB)
     adj_split_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
@@ -1158,7 +1314,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         int q = t / (N * N), ij = t - q * (N * N);
         int elq = q / DIM, d = q - elq * DIM;
         int eq_ = blockIdx.x * S::EPB + elq;
-        sJD[t] = eq_ < P.nelem ? -P.Ja[eq_ * DIM + d] * P.ops[N * N + ij] : 0.0;
+        sJD[t] = eq_ < P.nelem ? -(CURV ? 1.0 : P.Ja[eq_ * DIM + d]) * P.ops[N * N + ij] : 0.0;
     }
     if (tid == 0) {
         int c = 0;
@@ -1173,7 +1329,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     const double g = P.gamma, g1 = g - 1.0;
     double rho = 1.0, p = 1.0, v[DIM];
     if (active) {
-        double w = P.invJ[e] * P.s_lam;
+        double w = (CURV ? P.invJn[gi] : P.invJ[e]) * P.s_lam;
         double q[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -1222,16 +1378,18 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
-        if (dir == 0) adj_split_pairs<DIM, N, 0, TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0), TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0), TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
         __syncthreads();
         if (active) {
-            if (dir == 0) adj_split_nodes<DIM, N, 0, TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            if (dir == 0) adj_split_nodes<DIM, N, 0, TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
             else if (dir == 1)
-                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0), TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb,
+                                                                     acc);
             else
-                adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0), TP>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+                adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0), TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb,
+                                                                     acc);
         }
         __syncthreads();
     }
@@ -1273,7 +1431,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     }
 }
 
-template <int DIM, int N, int TP>
+template <int DIM, int N, int TP, bool CURV = false>
 cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
     constexpr size_t smem = AdjSplitShape<DIM, N, TP>::SMEM;
@@ -1281,41 +1439,42 @@ cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem);
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP, CURV>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_split_elem_kernel<DIM, N, TP><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_split_elem_kernel<DIM, N, TP, CURV><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int DIM, int TP>
+template <int DIM, int TP, bool CURV = false>
 cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_split_n<DIM, 2, TP>(P, s);
-        case 3: return launch_adj_split_n<DIM, 3, TP>(P, s);
-        case 4: return launch_adj_split_n<DIM, 4, TP>(P, s);
-        case 5: return launch_adj_split_n<DIM, 5, TP>(P, s);
-        case 6: return launch_adj_split_n<DIM, 6, TP>(P, s);
-        case 7: return launch_adj_split_n<DIM, 7, TP>(P, s);
-        case 8: return launch_adj_split_n<DIM, 8, TP>(P, s);
+        case 2: return launch_adj_split_n<DIM, 2, TP, CURV>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3, TP, CURV>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4, TP, CURV>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5, TP, CURV>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6, TP, CURV>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7, TP, CURV>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8, TP, CURV>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 // The split form's two-point flux: Chandrashekar, Kennedy-Gruber or StdAverage.
-template <int DIM>
+template <int DIM, bool CURV = false>
 cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
-    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER>(n, P, s);
-    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE>(n, P, s);
-    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR>(n, P, s);
+    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER, CURV>(n, P, s);
+    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE, CURV>(n, P, s);
+    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV>(n, P, s);
 }
 
 
 // Launchers, one translation unit each (explicit instantiations of the templates above).
-cudaError_t launch_adj_face(int dim, int kind, int grid, int tb, const AdjFaceParams& F, cudaStream_t s);
-cudaError_t launch_adj_elem_dim(int dim, int n, const AdjElemParams& P, cudaStream_t s);
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s);
+// curv: the general-geometry kernels (2D and 3D).
+cudaError_t launch_adj_face(int dim, int kind, bool curv, int grid, int tb, const AdjFaceParams& F, cudaStream_t s);
+cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s);
 
 }  // namespace flou

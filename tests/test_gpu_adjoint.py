@@ -263,6 +263,97 @@ def test_split_rhs_vjp_columns(op):
             assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
 
 
+def _general(dim, n, op, walls, seed=5):
+    """A perturbed box whose elements are randomly rotated (every master2slave orientation occurs
+    in 3D) and whose interior nodes are displaced: J, the metric, the face frames and the surface
+    Jacobians vary per node.  Walls: slip on the odd boundaries, outflow on the even ones."""
+    from test_unstructured import _std
+    eq = F.EulerEquation(dim, 1.4)
+    mesh = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=seed)
+    bcs = {str(k): (F.EulerSlipBC() if walls and k % 2 else F.EulerOutflowBC()) for k in range(1, 2 * dim + 1)}
+    return F.MultielementDisc(mesh, _std(dim, n, dim + 2, "GLL"), eq, OPERATORS[op](), bcs)
+
+
+GENERAL_OPS = ["strong", "split", "split_stdface", "split_hllc", "strong_hllc", "strong_hll", "split_kg", "split_std",
+               "split_sd", "split_md", "strong_md"]
+
+
+@pytest.mark.parametrize("op", GENERAL_OPS)
+@pytest.mark.parametrize("dim,n,walls", [(2, 4, False), (2, 5, True), (3, 3, True), (3, 4, False)])
+def test_general_geometry_rhs_vjp_dot_product(dim, n, walls, op):
+    """The residual VJP on general geometry (the CURV kernels: contravariant fluxes with the
+    per-node metric, pair fluxes along the averaged metric columns, slave traces through the
+    orientation, per-node face frames), against the oracle's dual numbers."""
+    from test_unstructured import _state
+    disc = _general(dim, n, op, walls)
+    if dim == 3:
+        assert len(set(disc.mesh.orientation.tolist())) == 8
+    rng = np.random.default_rng(40 + dim + n)
+    Q = _state(disc, seed=dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    hll = op in HLL_FAMILY
+    dc = 0.0 * c if hll else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if hll else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op", ["split", "strong", "split_kg", "split_std"])
+def test_general_geometry_rhs_vjp_columns(op):
+    """Every column of one element's transposed Jacobian on a rotated 3D mesh, against the
+    dual-number JVPs of the unit directions (catches a cotangent sent to the wrong slave node)."""
+    from test_unstructured import _state
+    disc = _general(3, 3, op, walls=True, seed=8)
+    rng = np.random.default_rng(23)
+    Q = _state(disc, seed=4)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if op in HLL_FAMILY else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 3
+    e = 13   # the middle element: all its faces are interior
+    for v in range(Q.shape[1]):
+        for i in range(e * npe, (e + 1) * npe):
+            dQ = np.zeros_like(Q)
+            dQ[i, v] = 1.0
+            _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+            col = np.sum(lam * dR)
+            assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+@pytest.mark.parametrize("op", ["split_hllc", "strong", "split_kg"])
+def test_general_geometry_adjoint_solve_against_dual_numbers(op):
+    from test_unstructured import _state
+    disc = _general(3, 4, op, walls=True)
+    Q0 = _state(disc, seed=9)
+    rng = np.random.default_rng(29)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 5)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 8
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
 def _tgv_state(disc, mach, seed):
     """Taylor-Green vortex with a small random smooth perturbation of every primitive variable.
     The plain vortex is symmetric: interface wave speeds tie exactly (|u_L| + a_L = |u_R| + a_R)
