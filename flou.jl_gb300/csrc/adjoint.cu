@@ -36,6 +36,12 @@ __global__ void functional_kernel(const double* Q, const double* rho_t, const do
     }
 }
 
+// y = a x (the first reverse stage of a 2N-storage step: k̄ = B_s Ū)
+__global__ void scale_kernel(double* y, const double* x, double a, int64_t n) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < n) y[g] = a * x[g];
+}
+
 }  // namespace flou
 
 using namespace flou;
@@ -46,7 +52,8 @@ struct AdjBuffers {
     double *QbL = nullptr, *QbR = nullptr, *Ibar = nullptr;
 };
 
-int adj_supported(flou_ctx* c) {
+// ssp_only: the batched adjoint, whose lockstep sweep steps with SSP-RK3 only.
+int adj_supported(flou_ctx* c, bool ssp_only = false) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                (k.volume_op == FLOU_OP_SPLIT &&
@@ -65,11 +72,8 @@ int adj_supported(flou_ctx* c) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
-    if (c->lsrk_s)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint steps with SSP-RK3 (flou_set_integrator 0)");
-    for (int b = 0; b < c->nbcs; ++b)
-        if (c->bc_kind[b] == FLOU_BC_INFLOW || c->bc_kind[b] == FLOU_BC_STATE_FIELD)
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint supports periodic, slip and outflow boundaries");
+    if (ssp_only && c->lsrk_s)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint steps with SSP-RK3 (flou_set_integrator 0)");
     return FLOU_OK;
 }
 
@@ -94,7 +98,7 @@ void free_adj(AdjBuffers& B) {
 //   cbar += (∂L/∂c)ᵀ (s_lam Ain)
 int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, const double* Ain, double* Aout,
               double* Bacc, double* cbar, double s_lam, double alpha, double beta, int readB, int writeB,
-              double gamma_B, double delta_B) {
+              double gamma_B, double delta_B, double* K = nullptr, double kA = 0.0, double kB = 0.0) {
     AdjFaceParams F;
     memset(&F, 0, sizeof(F));
     F.status = c->d_status;
@@ -122,7 +126,11 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     F.n = c->n;
     F.npe = c->npe;
     F.nfd = c->nfd;
-    for (int b = 0; b < MAXBC; ++b) F.bc_kind[b] = c->bc_kind[b];
+    for (int b = 0; b < MAXBC; ++b) {
+        F.bc_kind[b] = c->bc_kind[b];
+        for (int k = 0; k < 5; ++k) F.bc_state[b][k] = c->bc_state[b][k];
+    }
+    F.bc_field = c->d_bcfield;
     int64_t nth = (int64_t)c->nfaces * c->nfd;
     const int tb = face_block_size(nth);
     int grid = (int)((nth + tb - 1) / tb);
@@ -163,6 +171,9 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.readB = readB;
     P.writeB = writeB;
     P.gamma = c->cfg.gamma;
+    P.K = K;
+    P.kA = kA;
+    P.kB = kB;
     if (c->cfg.volume_op == FLOU_OP_SPLIT) {
         e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, P, s);
     } else {
@@ -246,8 +257,10 @@ struct Solver {
     std::vector<cudaEvent_t> written;   // [slot]
     std::vector<cudaEvent_t> read;      // [slot * NF + f]
     double* X[NB] = {};
-    double* SX1[NB] = {};
-    double* SX2[NB] = {};
+    // stage states of a reverse step: SSP-RK3 U^(k,1), U^(k,2); a 2N-storage method u_1 .. u_(s-1)
+    std::vector<double*> SX[NB];
+    int lsrk = 0;                     // stages of the 2N-storage method (0: SSP-RK3)
+    double* Kss = nullptr;            // the stage stream's 2N register
     cudaEvent_t ready[NB] = {}, sready[NB] = {}, done[NB] = {};
     bool used[NB] = {};
     int xi = 0, fi = 0;
@@ -282,12 +295,21 @@ struct Solver {
         if ((r = cuda(cudaMemcpyAsync(dst, slot[si], bytes, cudaMemcpyDeviceToDevice, sf[f]), "state copy"))) return r;
         return record(read[(size_t)si * NF + f], sf[f]);
     }
-    int advance(int f, double* Q, int k) {   // k SSP-RK3 steps in place on forward stream f
+    // One 2N-storage stage (0-based st) from u on stream s: k = A_st k + dt L(u) in K, out = u + B_st k.
+    int lsrk_stage(cudaStream_t s, const double* u, double* K, double* out, int st, double* Fn) {
+        return ctx_stage(c, s, u, K, out, 3, dt, st == 0 ? 0.0 : c->lsrk_A[st], c->lsrk_B[st], Fn);
+    }
+    int advance(int f, double* Q, int k) {   // k steps in place on forward stream f
         for (int i = 0; i < k; ++i) {
             int r;
-            if ((r = ctx_stage(c, sf[f], Q, Q, F1[f], 1, dt, 0.0, 1.0, Fnf[f]))) return r;
-            if ((r = ctx_stage(c, sf[f], F1[f], Q, F1[f], 2, dt, 0.75, 0.25, Fnf[f]))) return r;
-            if ((r = ctx_stage(c, sf[f], F1[f], Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf[f]))) return r;
+            if (lsrk) {   // F1[f] is the stream's 2N register
+                for (int st = 0; st < lsrk; ++st)
+                    if ((r = lsrk_stage(sf[f], Q, F1[f], Q, st, Fnf[f]))) return r;
+            } else {
+                if ((r = ctx_stage(c, sf[f], Q, Q, F1[f], 1, dt, 0.0, 1.0, Fnf[f]))) return r;
+                if ((r = ctx_stage(c, sf[f], F1[f], Q, F1[f], 2, dt, 0.75, 0.25, Fnf[f]))) return r;
+                if ((r = ctx_stage(c, sf[f], F1[f], Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf[f]))) return r;
+            }
             ++advances;
         }
         return FLOU_OK;
@@ -314,14 +336,25 @@ struct Solver {
         if ((r = copy_from(f, X[b], si))) return r;
         if ((r = advance(f, X[b], k))) return r;
         if ((r = record(ready[b], sf[f]))) return r;
-        // the stage stream: U^(k,1) and U^(k,2) (ready[b] comes after the forward stream's wait for
-        // done[b], so the stage buffers are free again)
+        // the stage stream: U^(k,1) and U^(k,2), or u_1 .. u_(s-1) (ready[b] comes after the forward
+        // stream's wait for done[b], so the stage buffers are free again)
         if ((r = wait(ss, ready[b]))) return r;
-        if ((r = ctx_stage(c, ss, X[b], X[b], SX1[b], 1, dt, 0.0, 1.0, Fns))) return r;
-        if ((r = ctx_stage(c, ss, SX1[b], X[b], SX2[b], 2, dt, 0.75, 0.25, Fns))) return r;
+        if (lsrk) {
+            const double* u = X[b];
+            for (int st = 0; st + 1 < lsrk; ++st) {
+                if ((r = lsrk_stage(ss, u, Kss, SX[b][st], st, Fns))) return r;
+                u = SX[b][st];
+            }
+            // the last step: U^n, which the functional reads, from the same register (the adjoint
+            // stream has not used T yet)
+            if (kstep == nsteps - 1 && !seeded && (r = lsrk_stage(ss, u, Kss, T, lsrk - 1, Fns))) return r;
+        } else {
+            if ((r = ctx_stage(c, ss, X[b], X[b], SX[b][0], 1, dt, 0.0, 1.0, Fns))) return r;
+            if ((r = ctx_stage(c, ss, SX[b][0], X[b], SX[b][1], 2, dt, 0.75, 0.25, Fns))) return r;
+        }
         if ((r = record(sready[b], ss))) return r;
         if ((r = wait(sa, sready[b]))) return r;
-        if ((r = backward_step(kstep, X[b], SX1[b], SX2[b]))) return r;
+        if ((r = (lsrk ? backward_step_2n(kstep, b) : backward_step(kstep, X[b], SX[b][0], SX[b][1])))) return r;
         used[b] = true;
         return record(done[b], sa);
     }
@@ -343,6 +376,33 @@ struct Solver {
             return r;
         if ((r = adj_stage(c, ab, sa, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
         if ((r = adj_stage(c, ab, sa, Xk, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
+        return FLOU_OK;
+    }
+    // The same for a 2N-storage step (Williamson form; stage i from u_i: k_i = A_i k_(i-1) +
+    // dt L(u_i), u_(i+1) = u_i + B_i k_i, A_0 = 0).  Reverse stage i with k̄ = k̄_i + B_i Ū(i+1) in T:
+    //   Ū_i = Ū_(i+1) + dt (∂L/∂u)(u_i)ᵀ k̄,  then T = A_i k̄ + B_(i-1) Ū_i for stage i-1
+    // (the element kernel's epilogue forms the next k̄ in place).  The last stage starts from
+    // k̄ = B_(s-1) Ū; A_0 = 0 leaves nothing to carry into the previous step.
+    int backward_step_2n(int k, int b) {
+        int r;
+        if (!seeded) {   // U^n was formed in T by the stage stream
+            if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
+            functional_kernel<<<nblk, 256, 0, sa>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
+            if ((r = cuda(cudaGetLastError(), "functional"))) return r;
+            if ((r = cuda(cudaMemcpyAsync(h_partial, partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, sa),
+                          "functional")))
+                return r;
+            seeded = true;
+        }
+        const int64_t n = c->ndofs * c->nv;
+        scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, sa>>>(T, A, c->lsrk_B[lsrk - 1], n);
+        if ((r = cuda(cudaGetLastError(), "adjoint register"))) return r;
+        for (int i = lsrk - 1; i >= 0; --i) {
+            const double* u = i == 0 ? X[b] : SX[b][i - 1];
+            if ((r = adj_stage(c, ab, sa, u, T, A, A, cbar, dt, 0.0, 1.0, 1, 0, 0.0, 0.0, i > 0 ? T : nullptr,
+                               c->lsrk_A[i], i > 0 ? c->lsrk_B[i - 1] : 0.0)))
+                return r;
+        }
         return FLOU_OK;
     }
     // U^i0 is in slot[si]; ns free snapshot slots may be used; reverses steps i0 .. i0+n-1.
@@ -549,11 +609,14 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     };
     S.slot.assign(nslots + 1, nullptr);
     for (int i = 0; i <= nslots; ++i) dalloc(&S.slot[i], S.bytes);
+    S.lsrk = c->lsrk_s;
+    const int nst = S.lsrk ? S.lsrk - 1 : 2;
     for (int i = 0; i < Solver::NB; ++i) {
         dalloc(&S.X[i], S.bytes);
-        dalloc(&S.SX1[i], S.bytes);
-        dalloc(&S.SX2[i], S.bytes);
+        S.SX[i].assign(nst, nullptr);
+        for (int j = 0; j < nst; ++j) dalloc(&S.SX[i][j], S.bytes);
     }
+    if (S.lsrk) dalloc(&S.Kss, S.bytes);
     double** bufs[] = {&S.Bacc, &S.T};
     for (double** b : bufs) dalloc(b, S.bytes);
     for (int f = 0; f < Solver::NF; ++f) {
@@ -651,7 +714,7 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
     for (int i = 0; i < n; ++i) {
         flou_ctx* c = ctxs[i];
         int r = ctx_prepare(c);
-        if (!r) r = adj_supported(c);
+        if (!r) r = adj_supported(c, true);
         if (!r && (!Q0[i] || !rho_target[i] || !weights[i] || !dJdQ0[i] || !std::isfinite(dt[i])))
             r = ctx_fail(c, FLOU_ERR_ARG, "invalid arguments");
         if (!r && dJdc && dJdc[i] && !c->d_c)

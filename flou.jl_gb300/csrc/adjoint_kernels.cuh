@@ -63,6 +63,10 @@ struct AdjFaceParams {
     int64_t ndofs, nfdofs;
     int32_t nfaces, n, npe, nfd;
     int32_t bc_kind[MAXBC];
+    // external states of FLOU_BC_INFLOW (per boundary) and FLOU_BC_STATE_FIELD ([nv][nfdofs]
+    // per face node), in the physical frame; constants, so their cotangents are dropped
+    double bc_state[MAXBC][5];
+    const double* bc_field;
 };
 
 struct AdjElemParams {
@@ -90,6 +94,10 @@ struct AdjElemParams {
     double s_lam, alpha, beta, gamma_B, delta_B;
     int32_t readB, writeB;
     double gamma;
+    // 2N-storage reverse stages: K = kA Ain + kB Aout per node (nullable; K may alias Ain, whose
+    // other readers are done: the face kernel ran before, and a block reads only its own nodes)
+    double* K;
+    double kA, kB;
 };
 
 // q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
@@ -873,10 +881,22 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         if (CURV) rotate_to_face<DIM>(qR, fr, b);
         else cart_to_face<DIM>(qR, A, b);
     } else {
-        bck = P.bc_kind[P.face_bc[f]];
+        const int bi = P.face_bc[f];
+        bck = P.bc_kind[bi];
+        if (bck == FLOU_BC_INFLOW || bck == FLOU_BC_STATE_FIELD) {   // a fixed external state
+            double qe[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) b[k] = a[k];   // outflow; slip flips the normal momentum
-        if (bck == FLOU_BC_SLIP) b[1] = -a[1];
+            for (int k = 0; k < NV; ++k)
+                qe[k] = bck == FLOU_BC_INFLOW ? P.bc_state[bi][k] : P.bc_field[k * P.nfdofs + gid];
+            b[0] = qe[0];
+            b[DIM + 1] = qe[DIM + 1];
+            if (CURV) rotate_to_face<DIM>(qe, fr, b);
+            else cart_to_face<DIM>(qe, A, b);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) b[k] = a[k];   // outflow; slip flips the normal momentum
+            if (bck == FLOU_BC_SLIP) b[1] = -a[1];
+        }
     }
     double inten = P.intensity;
     if (P.elem_c) {
@@ -1085,6 +1105,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
             P.B[k * P.ndofs + gi] = b;
         }
         P.Aout[k * P.ndofs + gi] = o;
+        if (P.K) P.K[k * P.ndofs + gi] = fma(P.kA, ain[k], P.kB * o);
     }
     if (P.cbar && i == 0) {   // intensity (c1 + c2)/2: each side gets half, a boundary face all
         double acc = 0.0;
@@ -1417,6 +1438,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
             P.B[k * P.ndofs + gi] = b;
         }
         P.Aout[k * P.ndofs + gi] = o;
+        if (P.K) P.K[k * P.ndofs + gi] = fma(P.kA, ain, P.kB * o);
     }
     if (P.cbar && i == 0) {
         double cacc = 0.0;

@@ -237,16 +237,24 @@ function LowStorageGPU(solver)
     return LowStorageGPU(vcat(0.0, collect(tab.A2end)), vcat(tab.B1, collect(tab.B2end)))
 end
 
-function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, solver::LowStorageGPU, tfinal; dt,
-                            kwargs...)
+# runs f() with the context stepping by `integrator` (SSP-RK3 again afterwards)
+with_integrator(f, disc::GPUDisc, ::SSPRK3GPU) = f()
+function with_integrator(f, disc::GPUDisc, solver::LowStorageGPU)
     A, B = solver.A, solver.B
     GC.@preserve A B check(ccall((:flou_set_integrator, libflou), Int32,
         (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}), disc.ctx, length(B), A, B), disc.ctx)
     try
-        return Flou.timeintegrate(Q0, disc, equation, SSPRK3GPU(), tfinal; dt=dt, kwargs...)
+        return f()
     finally
         ccall((:flou_set_integrator, libflou), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}),
               disc.ctx, 0, C_NULL, C_NULL)
+    end
+end
+
+function Flou.timeintegrate(Q0::Matrix{Float64}, disc::GPUDisc, equation, solver::LowStorageGPU, tfinal; dt,
+                            kwargs...)
+    return with_integrator(disc, solver) do
+        Flou.timeintegrate(Q0, disc, equation, SSPRK3GPU(), tfinal; dt=dt, kwargs...)
     end
 end
 
@@ -286,38 +294,46 @@ end
 """
     solve_functional(disc, Q0, c, dt, nsteps, ρtarget, w) -> J
 
-J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` SSP-RK3 steps with per-element dissipation scales `c`
-(LxF interface fluxes), or `c = nothing` for HLL, HLLC and the Scalar/MatrixDissipation fluxes,
-which take no per-element scale.
+J = 1/2 Σ w (ρ(T) - ρt)² after `nsteps` steps with per-element dissipation scales `c` (LxF
+interface fluxes), or `c = nothing` for HLL, HLLC and the Scalar/MatrixDissipation fluxes, which
+take no per-element scale.  The keyword `integrator` (SSPRK3GPU() or a LowStorageGPU method)
+selects the time stepping that is differentiated.
 Differentiable through the `rrule`s below (discrete adjoint, binomial checkpointing).
 Arrays are device pointers wrapped by the caller's GPU array package (e.g. CuArray).
 """
 function solve_functional end
 
-function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, dt, nsteps, ρt, w; nsnap=20)
+function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, c, dt, nsteps, ρt, w; nsnap=20,
+                              integrator=SSPRK3GPU())
     J = Ref{Float64}(0.0)
     g = similar(Q0)
     gc = similar(c)
     nf = Ref{Int64}(0)
     check(ccall((:flou_set_dissipation, libflou), Int32, (Ptr{Cvoid}, Ptr{Float64}, Int32), disc.ctx, pointer(c),
                 PTR_DEVICE), disc.ctx)
-    check(ccall((:flou_adjoint_solve, libflou), Int32,
-        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
-         Ptr{Float64}, Ref{Int64}),
-        disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), pointer(gc), nf), disc.ctx)
+    with_integrator(disc, integrator) do
+        check(ccall((:flou_adjoint_solve, libflou), Int32,
+            (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
+             Ptr{Float64}, Ref{Int64}),
+            disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), pointer(gc), nf),
+            disc.ctx)
+    end
     pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, J̄ .* gc, NoTangent(), NoTangent(), NoTangent(), NoTangent())
     return J[], pullback
 end
 
 # HLL, HLLC, Scalar/MatrixDissipation: no per-element scale, so no dJ/dc (the C ABI takes a null dJdc)
-function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, ::Nothing, dt, nsteps, ρt, w; nsnap=20)
+function ChainRulesCore.rrule(::typeof(solve_functional), disc::GPUDisc, Q0, ::Nothing, dt, nsteps, ρt, w; nsnap=20,
+                              integrator=SSPRK3GPU())
     J = Ref{Float64}(0.0)
     g = similar(Q0)
     nf = Ref{Int64}(0)
-    check(ccall((:flou_adjoint_solve, libflou), Int32,
-        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
-         Ptr{Float64}, Ref{Int64}),
-        disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), C_NULL, nf), disc.ctx)
+    with_integrator(disc, integrator) do
+        check(ccall((:flou_adjoint_solve, libflou), Int32,
+            (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ref{Float64}, Ptr{Float64},
+             Ptr{Float64}, Ref{Int64}),
+            disc.ctx, pointer(Q0), dt, nsteps, nsnap, pointer(ρt), pointer(w), J, pointer(g), C_NULL, nf), disc.ctx)
+    end
     pullback(J̄) = (NoTangent(), NoTangent(), J̄ .* g, NoTangent(), NoTangent(), NoTangent(), NoTangent(), NoTangent())
     return J[], pullback
 end

@@ -31,6 +31,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace oracle {
@@ -1500,14 +1501,17 @@ inline void ssprk3_step_limited(const Disc& g, double* Q, double dt, double t, W
 // tests and examples step with (test/tests.jl:19,56,93,139; examples/src/3D_Euler.jl:77):
 //   k = dt L(u); u = u + B_1 k;   for i = 2..s: k = A_i k + dt L(u, t + c_i dt); u = u + B_i k.
 // The stage limiter, when `omega` is given, acts on u after every stage.
-inline void lsrk2n_step(const Disc& g, double* Q, double dt, double t, Workspace<double>& ws,
-                        std::vector<double>& K, std::vector<double>& L, int s, const double* A, const double* B,
-                        const double* c, double minval = 0.0, const std::vector<double>* omega = nullptr) {
+// T = Dual (forward-mode derivatives, with the per-element dissipation scales celem) takes no
+// limiter.
+template <class T>
+void lsrk2n_step(const Disc& g, T* Q, double dt, double t, Workspace<T>& ws, std::vector<T>& K, std::vector<T>& L,
+                 int s, const double* A, const double* B, const double* c, double minval = 0.0,
+                 const std::vector<double>* omega = nullptr, const T* celem = nullptr) {
     long N = g.ndofs() * g.cfg.nv;
     K.resize(N);
     L.resize(N);
     for (int st = 0; st < s; ++st) {
-        rhs(g, L.data(), Q, t + c[st] * dt, ws);
+        rhs(g, L.data(), Q, t + c[st] * dt, ws, celem);
         if (st == 0) {
 #pragma omp parallel for schedule(static)
             for (long i = 0; i < N; ++i) K[i] = dt * L[i];
@@ -1517,7 +1521,9 @@ inline void lsrk2n_step(const Disc& g, double* Q, double dt, double t, Workspace
         }
 #pragma omp parallel for schedule(static)
         for (long i = 0; i < N; ++i) Q[i] = Q[i] + B[st] * K[i];
-        if (omega) zhang_shu(g, Q, minval, *omega);
+        if constexpr (std::is_same_v<T, double>) {
+            if (omega) zhang_shu(g, Q, minval, *omega);
+        }
     }
 }
 

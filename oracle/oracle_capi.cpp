@@ -439,6 +439,30 @@ void oracle_solve_jvp(void* hp, const double* Q0, const double* dQ0, const doubl
     *dJ = acc.d;
 }
 
+// The same for nsteps steps of a 2N-storage method (nstages, A, B, c as oracle_lsrk2n).
+void oracle_solve_jvp_lsrk(void* hp, const double* Q0, const double* dQ0, const double* c, const double* dc,
+                           double dt, int nsteps, const double* rho_t, const double* w, int nstages, const double* A,
+                           const double* B, const double* cst, double* J, double* dJ) {
+    Handle* h = (Handle*)hp;
+    long nd = h->g.ndofs(), N = nd * h->g.cfg.nv;
+    std::vector<Dual> q(N), ce, K, L;
+    for (long i = 0; i < N; ++i) q[i] = Dual(Q0[i], dQ0 ? dQ0[i] : 0.0);
+    if (c) {
+        ce.resize(h->g.nelem);
+        for (int e = 0; e < h->g.nelem; ++e) ce[e] = Dual(c[e], dc ? dc[e] : 0.0);
+    }
+    Workspace<Dual> ws;
+    for (int s = 0; s < nsteps; ++s)
+        lsrk2n_step(h->g, q.data(), dt, s * dt, ws, K, L, nstages, A, B, cst, 0.0, nullptr, c ? ce.data() : nullptr);
+    Dual acc(0.0);
+    for (long i = 0; i < nd; ++i) {
+        Dual r = q[i] - rho_t[i];
+        acc = acc + (0.5 * w[i]) * (r * r);
+    }
+    *J = acc.v;
+    *dJ = acc.d;
+}
+
 // Operation count of one residual evaluation (single thread).  out = {add, mul, div, sqrt,
 // log, cmp}.
 void oracle_count_rhs(void* hp, const double* Q, double t, long long* out) {

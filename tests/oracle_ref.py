@@ -52,6 +52,8 @@ def lib():
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
         _lib.oracle_solve_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D, D, D]
+        _lib.oracle_solve_jvp_lsrk.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D,
+                                               ctypes.c_int, D, D, D, D, D]
     return _lib
 
 
@@ -214,6 +216,19 @@ class Disc:
         p = lambda a: _d(a) if a is not None else None
         self.L.oracle_solve_jvp(self.h, _d(Q0), _d(dQ0), p(args[0]), p(args[1]), dt, nsteps, p(args[2]),
                                 p(args[3]), ctypes.byref(J), ctypes.byref(dJ))
+        return J.value, dJ.value
+
+    def solve_jvp_lsrk(self, Q0, dQ0, c, dc, dt, nsteps, rho_t, w, A, B, cst):
+        """solve_jvp for nsteps steps of the 2N-storage method (A, B, c)."""
+        Q0 = np.asfortranarray(Q0, dtype=np.float64)
+        dQ0 = np.asfortranarray(dQ0, dtype=np.float64)
+        J, dJ = ctypes.c_double(), ctypes.c_double()
+        args = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
+                for x in (c, dc, rho_t, w, A, B, cst)]
+        p = lambda a: _d(a) if a is not None else None
+        self.L.oracle_solve_jvp_lsrk(self.h, _d(Q0), _d(dQ0), p(args[0]), p(args[1]), dt, nsteps, p(args[2]),
+                                     p(args[3]), len(args[5]), p(args[4]), p(args[5]), p(args[6]),
+                                     ctypes.byref(J), ctypes.byref(dJ))
         return J.value, dJ.value
 
     def count(self, Q, t=0.0):

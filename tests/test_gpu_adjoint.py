@@ -354,6 +354,150 @@ def test_general_geometry_adjoint_solve_against_dual_numbers(op):
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
+def _fixed_state_bcs(dim, eq, field):
+    """Boundary 1: an inflow state; boundary 2: a state that varies along the boundary (a
+    boundary-state field, flou_set_bc_field) or an outflow; slip and outflow walls elsewhere."""
+    Pin = np.zeros(dim + 2)
+    Pin[0], Pin[1], Pin[-1] = 1.05, 0.25, 1.1
+    bcs = {"1": F.EulerInflowBC(eq.vars_prim2cons(Pin)), "2": F.EulerOutflowBC()}
+    if field:
+        def qext(_q, x, _f, _t, _e):
+            P = np.zeros(dim + 2)
+            P[0], P[1], P[-1] = 1.0 + 0.2 * np.sin(2 * np.pi * x[1]), 0.3, 1.0 + 0.1 * x[1]
+            if dim > 1:
+                P[2] = 0.1 * np.cos(2 * np.pi * x[1])
+            return eq.vars_prim2cons(P)
+        bcs["2"] = F.GenericBC(qext)
+    for k in range(3, 2 * dim + 1):
+        bcs[str(k)] = F.EulerSlipBC() if k % 2 else F.EulerOutflowBC()
+    return bcs
+
+
+@pytest.mark.parametrize("op", ["strong", "split", "split_hllc", "strong_hll", "split_md", "split_kg"])
+@pytest.mark.parametrize("dim,general,field", [(2, False, True), (3, False, False), (2, True, True),
+                                               (3, True, True)])
+def test_rhs_vjp_with_inflow_and_state_field_boundaries(dim, general, field, op):
+    """Fixed external states (an inflow boundary, and a boundary-state field that varies along
+    the boundary) enter the face flux as constants: only the interior trace's cotangent remains."""
+    from test_unstructured import _state, _std
+    eq = F.EulerEquation(dim, 1.4)
+    bcs = _fixed_state_bcs(dim, eq, field)
+    if general:
+        mesh = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=6)
+        disc = F.MultielementDisc(mesh, _std(dim, 4, dim + 2, "GLL"), eq, OPERATORS[op](), bcs)
+        Q = _state(disc, seed=3)
+    else:
+        disc = build(dim, 4, (3,) * dim, eq, OPERATORS[op](), periodic=(), bcs=bcs,
+                     box=((0.0,) * dim, (1.0,) * dim))
+        Q = smooth_euler_state(disc, seed=5)
+    if field:
+        assert any(isinstance(b, F.equations.StateFieldBC) for b in disc.bcs)
+    rng = np.random.default_rng(50 + dim)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    hll = op in HLL_FAMILY
+    dc = 0.0 * c if hll else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if hll else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+def test_adjoint_solve_with_inflow_and_state_field_boundaries():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 4, (4, 3), eq, OPERATORS["split_hllc"](), periodic=(), bcs=_fixed_state_bcs(2, eq, True),
+                 box=((0.0, 0.0), (1.0, 1.0)))
+    Q0 = smooth_euler_state(disc, seed=12)
+    rng = np.random.default_rng(33)
+    rho_t, w = _functional_inputs(disc, 7)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 10
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, None)
+    o = oracle_for(disc)
+    c1 = np.ones(disc.mesh.nelements)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c1, 0.0 * c1, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ)
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+@pytest.mark.parametrize("solver", ["ORK256", "CarpenterKennedy2N54"])
+@pytest.mark.parametrize("op,dim", [("strong", 2), ("split_hllc", 2), ("split", 3), ("split_kg", 3)])
+def test_lowstorage_adjoint_solve_against_dual_numbers(solver, op, dim):
+    """The discrete adjoint of the 2N-storage methods (flou_set_integrator): each reverse stage
+    Ū_i = Ū_(i+1) + dt (∂L/∂u)(u_i)ᵀ k̄ with k̄ carried as A_i k̄ + B_(i-1) Ū_i, against the oracle's
+    dual numbers through the same method, with snapshots and recomputation."""
+    eq = F.EulerEquation(dim, 1.4)
+    if dim == 2:
+        disc = build(2, 4, (4, 3), eq, OPERATORS[op](), box=((-5.0, -5.0), (5.0, 5.0)))
+        Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.3, -0.4), 4.0, 0.05, period=(10.0, 10.0)))
+    else:
+        disc = build(3, 4, (2, 3, 2), eq, OPERATORS[op](), box=((0.0,) * 3, (2 * np.pi,) * 3))
+        Q0 = _tgv_state(disc, 0.3, 2)
+    m = getattr(F, solver)()
+    disc.ctx.set_integrator(m.A, m.B)
+    rng = np.random.default_rng(61)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 3)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 9
+    o = oracle_for(disc)
+    for nsnap in (2, 8):
+        g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+        gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+        J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, nsnap, _dev(rho_t), _dev(w), g, gc)
+        for k in range(2):
+            dQ = rng.standard_normal(Q0.shape)
+            dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
+            Jo, dJo = o.solve_jvp_lsrk(Q0, dQ, c, dc, dt, nsteps, rho_t, w, m.A, m.B, m.c)
+            assert abs(J - Jo) <= 1e-12 * abs(Jo)
+            ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
+            assert abs(ours - dJo) <= 1e-10 * abs(dJo), (nsnap, ours, dJo)
+    disc.ctx.set_integrator(None)
+
+
+def test_lowstorage_adjoint_against_central_differences():
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 5, (6, 6), eq, _lxf(), box=((-5.0, -5.0), (5.0, 5.0)))
+    Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.5, 0.1), 5.0, 0.08, period=(10.0, 10.0)))
+    m = F.ORK256()
+    disc.ctx.set_integrator(m.A, m.B)
+    rng = np.random.default_rng(19)
+    c = 1.0 + 0.1 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 8)
+    dt = 0.4 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 12
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    wd, rtd = _dev(w), _dev(rho_t)
+
+    def Jof(Q, cc):
+        disc.ctx.set_dissipation(cc)
+        q = _dev(Q)
+        disc.ctx.step(q, dt, nsteps)
+        r = q[0] - rtd
+        return float(0.5 * torch.sum(wd * r * r))
+
+    h = 1e-6
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * 0.1
+        fd = (Jof(Q0 + h * dQ, c + h * dc) - Jof(Q0 - h * dQ, c - h * dc)) / (2 * h)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
+    disc.ctx.set_integrator(None)
+
+
 def _tgv_state(disc, mach, seed):
     """Taylor-Green vortex with a small random smooth perturbation of every primitive variable.
     The plain vortex is symmetric: interface wave speeds tie exactly (|u_L| + a_L = |u_R| + a_R)
