@@ -68,8 +68,10 @@ int adj_supported(flou_ctx* c, bool ssp_only = false) {
                                                  "the split form (Chandrashekar, Kennedy-Gruber or StdAverage), and the "
                                                  "LxF, Scalar- or MatrixDissipation (StdAverage or ChandrasekharAverage), "
                                                  "HLL or HLLC interface flux");
-    if (!c->lift_ends)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint needs a basis with boundary nodes (LGL) and the DGSEM lift");
+    if (k.volume_op == FLOU_OP_SPLIT && !c->lift_ends)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs a basis with boundary nodes "
+                                                 "(LGL) and the DGSEM lift (the Gauss-node entropy projection is not "
+                                                 "differentiated)");
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
     if (ssp_only && c->lsrk_s)
@@ -139,7 +141,9 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
     const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch
                    : nf == FLOU_NF_MATRIX_DISSIPATION ? 6 + ch : ch;
-    cudaError_t e = launch_adj_face(dim, kind, c->curv, grid, tb, F, s);
+    // the strong form on a basis without exact end-node injection: interpolated traces, full lift
+    const bool gauss = c->cfg.volume_op == FLOU_OP_STRONG && !c->lgl;
+    cudaError_t e = launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
     memset(&P, 0, sizeof(P));
@@ -177,7 +181,7 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     if (c->cfg.volume_op == FLOU_OP_SPLIT) {
         e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, P, s);
     } else {
-        e = launch_adj_elem_dim(dim, c->n, c->curv, P, s);
+        e = launch_adj_elem_dim(dim, c->n, c->curv, gauss, P, s);
     }
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint element kernel");
     return FLOU_OK;

@@ -1,7 +1,9 @@
 // Strong-form element VJP kernels of the discrete adjoint (adjoint_kernels.cuh).
 #include "adjoint_kernels.cuh"
 namespace flou {
-cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s) {
+cudaError_t launch_adj_elem_gauss(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, bool gauss, const AdjElemParams& P, cudaStream_t s) {
+    if (gauss) return launch_adj_elem_gauss(dim, n, curv, P, s);
     if (curv) return dim == 2 ? launch_adj_elem<2, true>(n, P, s) : launch_adj_elem<3, true>(n, P, s);
     if (dim == 1) return launch_adj_elem<1>(n, P, s);
     if (dim == 2) return launch_adj_elem<2>(n, P, s);

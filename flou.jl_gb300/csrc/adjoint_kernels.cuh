@@ -802,7 +802,11 @@ __device__ __forceinline__ void md_vjp(const Prim& pa, const Prim& pb, double g,
 // CURV: general geometry, the forward face kernel's CURV path transposed: the slave trace at
 // master2slave(m, o), per-node 1/J on both sides, the face-node frame (n, t, b) and surface
 // Jacobian (a = R q, F = J Rᵀ F_face: F̄_face = J R F̄, q̄ = Rᵀ ā).
-template <int DIM, int KIND, bool CURV = false>
+// G: a basis without exact end-node injection (Gauss nodes; the strong form only): the traces
+// are the interpolations Σ_p l[p] U_p along the line, and the lift reaches every node of it, so
+// the flux cotangent gathers -Σ_p ∂g[p] w_p over the line (the element kernel scatters the trace
+// cotangents back with l).
+template <int DIM, int KIND, bool CURV = false, bool G = false>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
     constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
     constexpr bool SD = KIND == 4 || KIND == 5;
@@ -820,29 +824,60 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         *g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, mm, right ? n - 1 : 0);
         *dg = right ? dgr[n - 1] : dgl[0];
     };
-    int64_t g1i, g2i = 0;
-    double dg1, dg2 = 0.0;
+    // G: the trace of side s (interpolated with l) and the lift transpose Σ_p ∂g[p] (w λ)_p
+    auto line_sums = [&](int32_t s, int mm, double* q, double* fl) {
+        int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
+        const double* lv = P.ops + 2 * n * n + (right ? n : 0);
+        const double* dg = right ? dgr : dgl;
+#pragma unroll
+        for (int k = 0; k < DIM + 2; ++k) q[k] = fl[k] = 0.0;
+        for (int p = 0; p < n; ++p) {
+            const int64_t g = (int64_t)e * P.npe + tp_node<DIM>(n, dir, mm, p);
+            const double wl = (CURV ? P.invJn[g] : P.invJ[e]) * P.s_lam * dg[p];
+#pragma unroll
+            for (int k = 0; k < DIM + 2; ++k) {
+                q[k] = fma(lv[p], P.U[k * P.ndofs + g], q[k]);
+                fl[k] = fma(wl, P.Ain[k * P.ndofs + g], fl[k]);
+            }
+        }
+    };
+    int64_t g1i = 0, g2i = 0;
+    double dg1 = 0.0, dg2 = 0.0;
     if (kChecked && !(index_ok(s0 >> 3, P.ndofs / P.npe, P.status, 0) &&
                       (s1 < 0 || index_ok(s1 >> 3, P.ndofs / P.npe, P.status, s0 >> 3)) &&
                       (s1 >= 0 || index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3))))
         return;
-    endnode(s0, m, &g1i, &dg1);
     double qL[NV], qR[NV], Fb[NV];
-    double w1 = (CURV ? P.invJn[g1i] : P.invJ[s0 >> 3]) * P.s_lam;
+    if constexpr (G) {
+        double fl[NV];
+        line_sums(s0, m, qL, fl);
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        qL[k] = P.U[k * P.ndofs + g1i];
-        Fb[k] = -dg1 * (w1 * P.Ain[k * P.ndofs + g1i]);
+        for (int k = 0; k < NV; ++k) Fb[k] = -fl[k];
+    } else {
+        endnode(s0, m, &g1i, &dg1);
+        double w1 = (CURV ? P.invJn[g1i] : P.invJ[s0 >> 3]) * P.s_lam;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            qL[k] = P.U[k * P.ndofs + g1i];
+            Fb[k] = -dg1 * (w1 * P.Ain[k * P.ndofs + g1i]);
+        }
     }
     if (s1 >= 0) {
         const int mm = CURV ? master2slave<DIM>(m, P.orient[f], n) : m;
         if (CURV && !index_ok(mm, P.nfd, P.status, s1 >> 3)) return;
-        endnode(s1, mm, &g2i, &dg2);
-        double w2 = (CURV ? P.invJn[g2i] : P.invJ[s1 >> 3]) * P.s_lam;
+        if constexpr (G) {
+            double fl[NV];
+            line_sums(s1, mm, qR, fl);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            qR[k] = P.U[k * P.ndofs + g2i];
-            Fb[k] = fma(dg2, w2 * P.Ain[k * P.ndofs + g2i], Fb[k]);
+            for (int k = 0; k < NV; ++k) Fb[k] += fl[k];
+        } else {
+            endnode(s1, mm, &g2i, &dg2);
+            double w2 = (CURV ? P.invJn[g2i] : P.invJ[s1 >> 3]) * P.s_lam;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                qR[k] = P.U[k * P.ndofs + g2i];
+                Fb[k] = fma(dg2, w2 * P.Ain[k * P.ndofs + g2i], Fb[k]);
+            }
         }
     }
     FrameAxes A = frame_axes<DIM>(s0 & 7);
@@ -1017,7 +1052,9 @@ __device__ __forceinline__ int64_t trace_offset(const AdjElemParams& P, int e, i
 
 // CURV: general geometry: per-node 1/J, and the contravariant flux F̃_d = Σ_k Ja[k][d] F_k, whose
 // transpose gathers the directions first, G̃_k = Σ_d Ja[k][d] G_d, then takes one flux VJP per k.
-template <int DIM, int N, bool CURV = false>
+// G: a basis without exact end-node injection (the strong form on Gauss nodes): every node of a
+// line takes l_l[pos] and l_r[pos] of the trace cotangents of the line's two faces.
+template <int DIM, int N, bool CURV = false, bool G = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
@@ -1081,7 +1118,19 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
             euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
         }
         // trace cotangents of the faces this node lies on (LGL: the end nodes)
-        if (pos == 0 || pos == N - 1) {
+        if constexpr (G) {
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int fk = 2 * d + side;
+                const int32_t pk = P.elem_face[e * 2 * DIM + fk];
+                const double* src = (pk & 1) ? P.QbR : P.QbL;
+                const double lw = sops[2 * N * N + side * N + pos];
+                int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
+                if (!index_ok(o, P.nfdofs, P.status, e)) continue;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) qb[k] = fma(lw, __ldcg(src + k * P.nfdofs + o), qb[k]);
+            }
+        } else if (pos == 0 || pos == N - 1) {
             const int fk = 2 * d + (pos == 0 ? 0 : 1);
             const int32_t pk = P.elem_face[e * 2 * DIM + fk];
             const double* src = (pk & 1) ? P.QbR : P.QbL;
@@ -1120,32 +1169,32 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
     }
 }
 
-template <int DIM, int N, bool CURV = false>
+template <int DIM, int N, bool CURV = false, bool G = false>
 cudaError_t launch_adj_elem_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
     constexpr size_t smem = sizeof(double) * (S::NOPS + (DIM + 2) * S::NN);
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N, CURV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        attr = cudaFuncSetAttribute(adj_elem_kernel<DIM, N, CURV, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_elem_kernel<DIM, N, CURV><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_elem_kernel<DIM, N, CURV, G><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int DIM, bool CURV = false>
+template <int DIM, bool CURV = false, bool G = false>
 cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_elem_n<DIM, 2, CURV>(P, s);
-        case 3: return launch_adj_elem_n<DIM, 3, CURV>(P, s);
-        case 4: return launch_adj_elem_n<DIM, 4, CURV>(P, s);
-        case 5: return launch_adj_elem_n<DIM, 5, CURV>(P, s);
-        case 6: return launch_adj_elem_n<DIM, 6, CURV>(P, s);
-        case 7: return launch_adj_elem_n<DIM, 7, CURV>(P, s);
-        case 8: return launch_adj_elem_n<DIM, 8, CURV>(P, s);
+        case 2: return launch_adj_elem_n<DIM, 2, CURV, G>(P, s);
+        case 3: return launch_adj_elem_n<DIM, 3, CURV, G>(P, s);
+        case 4: return launch_adj_elem_n<DIM, 4, CURV, G>(P, s);
+        case 5: return launch_adj_elem_n<DIM, 5, CURV, G>(P, s);
+        case 6: return launch_adj_elem_n<DIM, 6, CURV, G>(P, s);
+        case 7: return launch_adj_elem_n<DIM, 7, CURV, G>(P, s);
+        case 8: return launch_adj_elem_n<DIM, 8, CURV, G>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -1494,9 +1543,11 @@ cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t
 
 
 // Launchers, one translation unit each (explicit instantiations of the templates above).
-// curv: the general-geometry kernels (2D and 3D).
-cudaError_t launch_adj_face(int dim, int kind, bool curv, int grid, int tb, const AdjFaceParams& F, cudaStream_t s);
-cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s);
+// curv: the general-geometry kernels (2D and 3D); gauss: the interpolated traces and full-line
+// lift of a basis without exact end-node injection (strong form).
+cudaError_t launch_adj_face(int dim, int kind, bool curv, bool gauss, int grid, int tb, const AdjFaceParams& F,
+                            cudaStream_t s);
+cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, bool gauss, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s);
 
 }  // namespace flou

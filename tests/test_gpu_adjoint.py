@@ -428,6 +428,108 @@ def test_adjoint_solve_with_inflow_and_state_field_boundaries():
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
+GAUSS_OPS = ["strong", "strong_hll", "strong_hllc", "strong_sd", "strong_md"]
+
+
+@pytest.mark.parametrize("op", GAUSS_OPS)
+@pytest.mark.parametrize("dim,n,general,walls", [(1, 5, False, True), (2, 4, False, False), (2, 5, False, True),
+                                                 (3, 3, False, True), (2, 4, True, True), (3, 4, True, False)])
+def test_gauss_nodes_strong_rhs_vjp_dot_product(dim, n, general, walls, op):
+    """The strong form on Gauss nodes: the traces are interpolations Σ l_p U_p and the lift
+    reaches every node of a line, so the face VJP gathers the whole line and the element VJP
+    scatters the trace cotangents back through l."""
+    from test_unstructured import _state, _std
+    eq = F.EulerEquation(dim, 1.4)
+    if general:
+        mesh = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=7)
+        bcs = _fixed_state_bcs(dim, eq, True) if walls else \
+            {str(k): F.EulerOutflowBC() for k in range(1, 2 * dim + 1)}
+        disc = F.MultielementDisc(mesh, _std(dim, n, dim + 2, "GL"), eq, OPERATORS[op](), bcs)
+        Q = _state(disc, seed=dim + n)
+    else:
+        bcs = None
+        if walls:
+            bcs = {str(k): (F.EulerSlipBC() if k % 2 else F.EulerOutflowBC()) for k in range(1, 2 * dim + 1)}
+        disc = build(dim, n, (3,) * dim, eq, OPERATORS[op](), periodic=() if walls else True, bcs=bcs, basis="GL")
+        Q = smooth_euler_state(disc, seed=dim + n)
+        if walls:
+            P = eq.vars_cons2prim(Q)
+            P[:, 1:1 + dim] *= 0.2
+            Q = np.asfortranarray(eq.vars_prim2cons(P))
+    rng = np.random.default_rng(70 + dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    hll = op in HLL_FAMILY
+    dc = 0.0 * c if hll else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if hll else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+def test_gauss_nodes_strong_rhs_vjp_columns():
+    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), _lxf(), basis="GL")
+    rng = np.random.default_rng(24)
+    Q = smooth_euler_state(disc, seed=5, amp=0.3)
+    c = _with_c(disc, "strong", 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 2
+    e = 4
+    for v in range(Q.shape[1]):
+        for i in range(e * npe, (e + 1) * npe):
+            dQ = np.zeros_like(Q)
+            dQ[i, v] = 1.0
+            _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+            col = np.sum(lam * dR)
+            assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+@pytest.mark.parametrize("op,dim", [("strong", 2), ("strong_hllc", 3)])
+def test_gauss_nodes_adjoint_solve_against_dual_numbers(op, dim):
+    eq = F.EulerEquation(dim, 1.4)
+    if dim == 2:
+        disc = build(2, 5, (4, 3), eq, OPERATORS[op](), box=((-5.0, -5.0), (5.0, 5.0)), basis="GL")
+        Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.3, -0.4), 4.0, 0.05, period=(10.0, 10.0)))
+    else:
+        disc = build(3, 4, (2, 3, 2), eq, OPERATORS[op](), box=((0.0,) * 3, (2 * np.pi,) * 3), basis="GL")
+        Q0 = _tgv_state(disc, 0.3, 4)
+    rng = np.random.default_rng(41)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 9)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 8
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+def test_gauss_nodes_split_form_is_not_differentiated():
+    from flou_cuda import _lib as L
+    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), _split(), basis="GL")
+    Q = _dev(smooth_euler_state(disc, seed=1))
+    g = torch.empty_like(Q)
+    with pytest.raises(F.FlouError) as ei:
+        disc.ctx.rhs_vjp(g, None, Q, Q)
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+
+
 @pytest.mark.parametrize("solver", ["ORK256", "CarpenterKennedy2N54"])
 @pytest.mark.parametrize("op,dim", [("strong", 2), ("split_hllc", 2), ("split", 3), ("split_kg", 3)])
 def test_lowstorage_adjoint_solve_against_dual_numbers(solver, op, dim):
