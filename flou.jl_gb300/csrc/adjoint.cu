@@ -68,10 +68,15 @@ int adj_supported(flou_ctx* c, bool ssp_only = false) {
                                                  "the split form (Chandrashekar, Kennedy-Gruber or StdAverage), and the "
                                                  "LxF, Scalar- or MatrixDissipation (StdAverage or ChandrasekharAverage), "
                                                  "HLL or HLLC interface flux");
-    if (k.volume_op == FLOU_OP_SPLIT && !c->lift_ends)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs a basis with boundary nodes "
-                                                 "(LGL) and the DGSEM lift (the Gauss-node entropy projection is not "
-                                                 "differentiated)");
+    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && c->curv)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form on Gauss nodes covers Cartesian "
+                                                 "geometry");
+    if (k.volume_op == FLOU_OP_SPLIT && c->bnodes && !c->lift_ends)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs the DGSEM lift on a basis "
+                                                 "with boundary nodes");
+    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_gauss_fits(k.dim, c->n, k.twopoint_flux))
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile of the Kennedy-Gruber flux at "
+                                                 "3D p=7 exceeds shared memory");
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
     if (ssp_only && c->lsrk_s)
@@ -141,8 +146,9 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
     const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch
                    : nf == FLOU_NF_MATRIX_DISSIPATION ? 6 + ch : ch;
-    // the strong form on a basis without exact end-node injection: interpolated traces, full lift
-    const bool gauss = c->cfg.volume_op == FLOU_OP_STRONG && !c->lgl;
+    // interpolated traces and the full-line lift: the strong form on a basis without exact end-node
+    // injection, the split form on a basis without boundary nodes (the forward's general paths)
+    const bool gauss = c->cfg.volume_op == FLOU_OP_STRONG ? !c->lgl : !c->bnodes;
     cudaError_t e = launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
@@ -179,7 +185,7 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.kA = kA;
     P.kB = kB;
     if (c->cfg.volume_op == FLOU_OP_SPLIT) {
-        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, P, s);
+        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss, P, s);
     } else {
         e = launch_adj_elem_dim(dim, c->n, c->curv, gauss, P, s);
     }

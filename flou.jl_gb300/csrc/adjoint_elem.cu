@@ -16,7 +16,11 @@ cudaError_t launch_adj_split_2d(int n, int tp, const AdjElemParams& P, cudaStrea
 cudaError_t launch_adj_split_3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_curv2d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_curv3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s) {
+cudaError_t launch_adj_split_gauss(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_gauss3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, const AdjElemParams& P,
+                                 cudaStream_t s) {
+    if (gauss) return dim == 3 ? launch_adj_split_gauss3d(n, tp, P, s) : launch_adj_split_gauss(dim, n, tp, P, s);
     if (curv) return dim == 2 ? launch_adj_split_curv2d(n, tp, P, s) : launch_adj_split_curv3d(n, tp, P, s);
     if (dim == 1) return launch_adj_split_1d(n, tp, P, s);
     if (dim == 2) return launch_adj_split_2d(n, tp, P, s);

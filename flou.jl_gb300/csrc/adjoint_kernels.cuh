@@ -1204,7 +1204,7 @@ cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
 // the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux;
 // zero on interior LGL nodes) and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved
 // variables.
-template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR>
+template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR, bool G = false>
 struct AdjSplitShape {
     using S = Shape<DIM, N>;
     static constexpr bool KG = TP == FLOU_TP_KENNEDY_GRUBER;
@@ -1216,12 +1216,280 @@ struct AdjSplitShape {
     static constexpr int NPB = KG ? DIM + 3 : DIM + 2;
     static constexpr int NPT = S::EPB * S::NFD * S::NPAIR;
     static constexpr int NSD = S::EPB * DIM * N * N;           // -Ja_d D♯ per element and direction
+    // G (Gauss nodes): per line side the cotangent of its projected entropy variables, and per node
+    // the cotangents of its two projected-state pair fluxes
+    static constexpr int NPROJ = G ? 2 * S::EPB * S::NFD : 0;
+    static constexpr int NGX = G ? NV * NPROJ + NPB * S::NN : 0;
     static constexpr size_t SMEM =
-        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
+        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD + NGX) +
         2 * (S::NPAIR + 1);
     // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
-    static constexpr int MINB = (S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
+    // (G: one, for the projection's registers)
+    static constexpr int MINB = (!G && S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
 };
+
+// Per-node quantities the split adjoint keeps for a state q (p its pressure): Chandrashekar
+// ρ/2, v/2, β/2, |v|²/4; Kennedy-Gruber ρ/2, v/2, p/2, e/2; StdAverage H, v, |v|².
+template <int DIM, int TP>
+__device__ __forceinline__ void split_node_values(const double* q, double p, double* o) {
+    const double rho = q[0], ir = rcp_refined(rho);
+    double v[DIM], vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        v[k] = q[1 + k] * ir;
+        vv = fma(v[k], v[k], vv);
+    }
+    if constexpr (TP == FLOU_TP_STD_AVERAGE) {
+        o[0] = (q[DIM + 1] + p) * ir;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) o[1 + k] = v[k];
+        o[1 + DIM] = vv;
+    } else {
+        o[0] = 0.5 * rho;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) o[1 + k] = 0.5 * v[k];
+        if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) {
+            o[1 + DIM] = 0.5 * p;
+            o[2 + DIM] = 0.5 * (q[DIM + 1] * ir);
+        } else {
+            o[1 + DIM] = (0.25 * rho) * rcp_refined(p);
+            o[2 + DIM] = 0.25 * vv;
+        }
+    }
+}
+
+// The two-point flux VJP of the split form along axis D for two nodes given by their
+// split_node_values A and B: cotangents in the format the node phase sums (PrimBar; StdAverage:
+// conserved).
+template <int DIM, int D, int TP>
+__device__ __forceinline__ void split_pair_vjp(const double* A, const double* B, const double* Fb, double cb,
+                                               double g1, PrimBar& o1, PrimBar& o2) {
+    constexpr int NV = DIM + 2;
+    if constexpr (TP == FLOU_TP_STD_AVERAGE) {
+        double qa_[NV], qb_[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qa_[k] = qb_[k] = 0.0;
+        euler_flux_vjp<DIM>(D, A + 1, A[1 + DIM], A[0], g1, Fb, 0.5, qa_);
+        euler_flux_vjp<DIM>(D, B + 1, B[1 + DIM], B[0], g1, Fb, 0.5, qb_);
+        o1.r = qa_[0];
+        o2.r = qb_[0];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            o1.v[k] = qa_[1 + k];
+            o2.v[k] = qb_[1 + k];
+        }
+        o1.b = qa_[DIM + 1];
+        o2.b = qb_[DIM + 1];
+        o1.e = o2.e = 0.0;
+    } else if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) {
+        kg_pair_vjp<DIM, D>(A[0], A + 1, A[1 + DIM], A[2 + DIM], B[0], B + 1, B[1 + DIM], B[2 + DIM], Fb, o1, o2);
+    } else {
+        chandra_pair_vjp<DIM, D, false>(A[0], A + 1, A[1 + DIM], A[2 + DIM], B[0], B + 1, B[1 + DIM], B[2 + DIM], cb,
+                                        Fb, o1, o2);
+        o1.e = o2.e = 0.0;
+    }
+}
+
+// Conserved cotangent of a state from the node-format cotangent o (split_node_values' format).
+template <int DIM, int TP>
+__device__ __forceinline__ void split_node_to_cons(const double* q, double p, double g1, const PrimBar& o,
+                                                   double* qb) {
+    if constexpr (TP == FLOU_TP_STD_AVERAGE) {
+        qb[0] += o.r;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) qb[1 + k] += o.v[k];
+        qb[DIM + 1] += o.b;
+    } else {
+        const double ir = rcp_refined(q[0]);
+        double v[DIM], vv = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            v[k] = q[1 + k] * ir;
+            vv = fma(v[k], v[k], vv);
+        }
+        if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) kg_prim_to_cons_vjp<DIM>(q[0], v, vv, q[DIM + 1], g1, o, qb);
+        else prim_to_cons_vjp<DIM>(q[0], v, vv, p, g1, o, qb);
+    }
+}
+
+// Entropy variables W(q) = ((γ - s)/(γ-1) - ρ|v|²/(2p), ρv/p, -ρ/p), s = ln p - γ ln ρ
+// (FlouCommon/Euler.jl:273-307), and the state of given entropy variables (Euler.jl:309-334).
+template <int DIM>
+__device__ __forceinline__ void entropy_of(const double* q, double g, double* w) {
+    const double ir = rcp_refined(q[0]);
+    double ke = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k] * ir, ke);
+    const double p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]), ip = rcp_refined(p);
+    const double sv = log(p) - g * log(q[0]);
+    w[0] = (g - sv) * rcp_refined(g - 1.0) - ke * ip * 0.5;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) w[1 + k] = q[1 + k] * ip;
+    w[DIM + 1] = -q[0] * ip;
+}
+
+template <int DIM>
+__device__ __forceinline__ double state_of_entropy(const double* w, double g, double* q) {
+    const double wl = w[DIM + 1], iwl = rcp_refined(wl), ig1 = rcp_refined(g - 1.0);
+    double vp[DIM], vv = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vp[k] = -w[1 + k] * iwl;
+        vv = fma(vp[k], vp[k], vv);
+    }
+    const double sv = g - (g - 1.0) * (w[0] - wl * vv * 0.5);
+    const double pp = exp(-fma(g, log(-wl), sv) * ig1);
+    const double rho = -pp * wl;
+    q[0] = rho;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) q[1 + k] = rho * vp[k];
+    q[DIM + 1] = fma(pp, ig1, 0.5 * rho * vv);
+    return pp;
+}
+
+// w̄ = (∂q/∂W)ᵀ q̄ = A₀ q̄, A₀ the symmetric Jacobian of the conserved variables with respect to
+// the entropy variables: rows (ρ, ρv, E), (ρv_k, ρ v_k v + p e_k, ρH v_k), (E, ρH v, ρH² - γp²/((γ-1)ρ)).
+template <int DIM>
+__device__ __forceinline__ void entropy_jacobian_apply(const double* q, double p, double g, const double* qb,
+                                                       double* wb) {
+    const double rho = q[0], ir = rcp_refined(rho), E = q[DIM + 1], rH = E + p;
+    double v[DIM], mq = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        v[k] = q[1 + k] * ir;
+        mq = fma(q[1 + k], qb[1 + k], mq);   // ρ v·q̄_m
+    }
+    const double vm = mq * ir;               // v·q̄_m
+    wb[0] = fma(rho, qb[0], fma(E, qb[DIM + 1], mq));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wb[1 + k] = fma(q[1 + k], fma(rH * ir, qb[DIM + 1], qb[0] + vm), p * qb[1 + k]);
+    const double eE = rH * rH * ir - g * p * p * ir * rcp_refined(g - 1.0);
+    wb[DIM + 1] = fma(E, qb[0], fma(rH, vm, eE * qb[DIM + 1]));
+}
+
+// q̄ += (∂W/∂q)ᵀ w̄ for the entropy variables of q (pressure p):
+//   p̄ = (-a/(γ-1) + (aρ|v|²/2 - ρ v·b + cρ)/p)/p   with w̄ = (a, b, c),
+//   q̄_ρ += a(γ/((γ-1)ρ) + |v|²/(2p)) - c/p + (γ-1)|v|²/2 p̄,  q̄_m += (b - a v)/p - (γ-1) v p̄,
+//   q̄_E += (γ-1) p̄.
+template <int DIM>
+__device__ __forceinline__ void entropy_vjp(const double* q, double p, double g, const double* wb, double* qb) {
+    const double rho = q[0], ir = rcp_refined(rho), ip = rcp_refined(p), g1 = g - 1.0, ig1 = rcp_refined(g1);
+    const double a = wb[0], c = wb[DIM + 1];
+    double v[DIM], vv = 0.0, vb = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        v[k] = q[1 + k] * ir;
+        vv = fma(v[k], v[k], vv);
+        vb = fma(v[k], wb[1 + k], vb);
+    }
+    const double pb = fma(rho * ip, fma(0.5 * a, vv, c - vb), -a * ig1) * ip;
+    qb[0] += fma(a, fma(g * ig1, ir, 0.5 * vv * ip), fma(0.5 * g1 * vv, pb, -c * ip));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) qb[1 + k] += fma(wb[1 + k] - a * v[k], ip, -g1 * v[k] * pb);
+    qb[DIM + 1] += g1 * pb;
+}
+
+// G (Gauss nodes, Cartesian): the entropy-projected coupling of each line transposed, one thread
+// per line.  The forward adds to node i the flux differences
+//   Ja (∂g_l[i] (F♯(Q_i, Q̃_l) - Σ_j l_j F♯(Q_j, Q̃_l)) - ∂g_r[i] (F♯(Q_i, Q̃_r) - Σ_j r_j F♯(Q_j, Q̃_r)))
+// with Q̃ = q(Σ_j l_j W(Q_j)).  With w = λ/J and T = Σ_i ∂g[i] w_i, the pair F♯(Q_j, Q̃) has the
+// cotangent ±Ja (∂g[j] w_j - l_j T); its node-side cotangents go to snode, and its Q̃ side, summed
+// over the line, is taken to the projected entropy variables (sWb), which the node phase spreads
+// back with l.
+template <int DIM, int N, int D, int TP>
+__device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int e0, const double* sops,
+                                                     const double* sprim, const double* sw, double* snode,
+                                                     double* sWb, double cb) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP, true>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR, NPB = A::NPB;
+    constexpr int NPROJ = A::NPROJ;
+    const double g = P.gamma, g1 = g - 1.0;
+    const double* lv = sops + 2 * N * N;   // l_l, then l_r
+    const double* dgl = lv + 2 * N;        // ∂g_l, then ∂g_r
+    for (int t = threadIdx.x; t < S::EPB * NFD; t += blockDim.x) {
+        const int elp = t / NFD, line = t - elp * NFD;
+        const int e = e0 + elp;
+        if (e >= P.nelem) continue;
+        const double Ja = P.Ja[e * DIM + D];
+        double wt[2][NV], T[2][NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) wt[0][k] = wt[1][k] = T[0][k] = T[1][k] = 0.0;
+        for (int pos = 0; pos < N; ++pos) {
+            const int j = elp * NPE + tp_node<DIM>(N, D, line, pos);
+            double q[NV], w[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
+            entropy_of<DIM>(q, g, w);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                wt[0][k] = fma(lv[pos], w[k], wt[0][k]);
+                wt[1][k] = fma(lv[N + pos], w[k], wt[1][k]);
+                T[0][k] = fma(dgl[pos], sw[k * NN + j], T[0][k]);
+                T[1][k] = fma(dgl[N + pos], sw[k * NN + j], T[1][k]);
+            }
+        }
+        double qt[2][NV], pt[2], vt[2][NARR];
+#pragma unroll
+        for (int sd = 0; sd < 2; ++sd) {
+            pt[sd] = state_of_entropy<DIM>(wt[sd], g, qt[sd]);
+            split_node_values<DIM, TP>(qt[sd], pt[sd], vt[sd]);
+        }
+        PrimBar ot[2];
+#pragma unroll
+        for (int sd = 0; sd < 2; ++sd) {
+            ot[sd].r = ot[sd].b = ot[sd].e = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ot[sd].v[k] = 0.0;
+        }
+        for (int pos = 0; pos < N; ++pos) {
+            const int j = elp * NPE + tp_node<DIM>(N, D, line, pos);
+            double vj[NARR];
+#pragma unroll
+            for (int k = 0; k < NARR; ++k) vj[k] = sprim[k * NN + j];
+            PrimBar on;
+            on.r = on.b = on.e = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) on.v[k] = 0.0;
+#pragma unroll
+            for (int sd = 0; sd < 2; ++sd) {
+                const double sg = sd == 0 ? Ja : -Ja;
+                const double dg = dgl[sd * N + pos], lj = lv[sd * N + pos];
+                double Fb[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) Fb[k] = sg * fma(dg, sw[k * NN + j], -lj * T[sd][k]);
+                PrimBar o1, o2;
+                split_pair_vjp<DIM, D, TP>(vj, vt[sd], Fb, cb, g1, o1, o2);
+                on.r += o1.r;
+                on.b += o1.b;
+                on.e += o1.e;
+                ot[sd].r += o2.r;
+                ot[sd].b += o2.b;
+                ot[sd].e += o2.e;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) {
+                    on.v[k] += o1.v[k];
+                    ot[sd].v[k] += o2.v[k];
+                }
+            }
+            snode[j] = on.r;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) snode[(1 + k) * NN + j] = on.v[k];
+            snode[(1 + DIM) * NN + j] = on.b;
+            if constexpr (NPB > DIM + 2) snode[(2 + DIM) * NN + j] = on.e;
+        }
+#pragma unroll
+        for (int sd = 0; sd < 2; ++sd) {   // Q̃'s cotangent -> conserved -> entropy variables
+            double qbt[NV], wbt[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qbt[k] = 0.0;
+            split_node_to_cons<DIM, TP>(qt[sd], pt[sd], g1, ot[sd], qbt);
+            entropy_jacobian_apply<DIM>(qt[sd], pt[sd], g, qbt, wbt);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sWb[k * NPROJ + 2 * t + sd] = wbt[k];
+        }
+    }
+}
 
 // CURV: the pair flux along the averaged metric column n̄ = (Ja_a + Ja_b)/2 of direction D (the
 // metric terms are in the flux; sJD then holds -D♯ alone).
@@ -1307,13 +1575,16 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
 
 // CURV: the diagonal term is the contravariant flux of node i (its own metric column), and a slave
 // face reads its trace cotangent through the orientation.
-template <int DIM, int N, int D, int TP, bool CURV = false>
+// G: also the node's projected-state pair cotangents (snode), the spread of the projected
+// entropy-variable cotangents (into wb), and the trace cotangents through l at every node.
+template <int DIM, int N, int D, int TP, bool CURV = false, bool G = false>
 __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
                                                 const double* Dsh, const double* sw, const double* spb,
                                                 const double* v, double rho, double p, double g1, double* qb,
-                                                PrimBar& acc) {
+                                                PrimBar& acc, const double* snode = nullptr,
+                                                const double* sWb = nullptr, double* wb = nullptr) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N, TP>;
+    using A = AdjSplitShape<DIM, N, TP, G>;
     constexpr int NV = DIM + 2, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
     constexpr int NPT = A::NPT, NPB = A::NPB;
     int pos, line;
@@ -1352,7 +1623,29 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         acc.b += src[(1 + DIM) * NPT + pidx];
         if constexpr (A::KG) acc.e += src[(2 + DIM) * NPT + pidx];
     }
-    if (pos == 0 || pos == N - 1) {
+    if constexpr (G) {
+        const int tid = threadIdx.x;
+        acc.r += snode[tid];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) acc.v[k] += snode[(1 + k) * NN + tid];
+        acc.b += snode[(1 + DIM) * NN + tid];
+        if constexpr (A::KG) acc.e += snode[(2 + DIM) * NN + tid];
+        const double* lv = Dsh + N * N;   // l_l, l_r follow D♯
+        const int c0 = 2 * (el * NFD + line);
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            wb[k] = fma(lv[pos], sWb[k * A::NPROJ + c0], fma(lv[N + pos], sWb[k * A::NPROJ + c0 + 1], wb[k]));
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int fk = 2 * D + side;
+            int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
+            int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
+            if (!index_ok(o, P.nfdofs, P.status, e)) continue;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qb[k] = fma(lv[side * N + pos], __ldcg(fsrc + k * P.nfdofs + o), qb[k]);
+        }
+    } else if (pos == 0 || pos == N - 1) {
         const int fk = 2 * D + (pos == 0 ? 0 : 1);
         int32_t pk = P.elem_face[e * 2 * DIM + fk];
         const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
@@ -1364,11 +1657,11 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     }
 }
 
-template <int DIM, int N, int TP, bool CURV = false>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP>::MINB)
+template <int DIM, int N, int TP, bool CURV = false, bool G = false>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP, G>::MINB)
     adj_split_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N, TP>;
+    using A = AdjSplitShape<DIM, N, TP, G>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
     constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
     extern __shared__ double smem[];
@@ -1377,7 +1670,9 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     double* sw = sprim + NARR * NN;   // [NV][NN]: w = λ / J
     double* spb = sw + NV * NN;       // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
     double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
-    uint8_t* stab = (uint8_t*)(sJD + A::NSD);
+    double* sWb = sJD + A::NSD;          // G: [NV][NPROJ] projected entropy-variable cotangents
+    double* snode = sWb + NV * A::NPROJ; // G: [NPB][NN] projected-state pair cotangents per node
+    uint8_t* stab = (uint8_t*)(sJD + A::NSD + A::NGX);
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
     for (int t = tid; t < A::NSD; t += blockDim.x) {
@@ -1446,20 +1741,31 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     for (int k = 0; k < NV; ++k) qb[k] = 0.0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) acc.v[k] = 0.0;
+    double wb[NV];   // G: cotangent of the node's entropy variables
+#pragma unroll
+    for (int k = 0; k < NV; ++k) wb[k] = 0.0;
+    constexpr int D1 = DIM > 1 ? 1 : 0, D2 = DIM > 2 ? 2 : 0;
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
         if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else if (dir == 1) adj_split_pairs<DIM, N, (DIM > 1 ? 1 : 0), TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else adj_split_pairs<DIM, N, (DIM > 2 ? 2 : 0), TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        if constexpr (G) {
+            if (dir == 0) adj_split_projection<DIM, N, 0, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            else if (dir == 1) adj_split_projection<DIM, N, D1, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            else adj_split_projection<DIM, N, D2, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
+        }
         __syncthreads();
         if (active) {
-            if (dir == 0) adj_split_nodes<DIM, N, 0, TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc);
+            if (dir == 0)
+                adj_split_nodes<DIM, N, 0, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
+                                                        sWb, wb);
             else if (dir == 1)
-                adj_split_nodes<DIM, N, (DIM > 1 ? 1 : 0), TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb,
-                                                                     acc);
+                adj_split_nodes<DIM, N, D1, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
+                                                         sWb, wb);
             else
-                adj_split_nodes<DIM, N, (DIM > 2 ? 2 : 0), TP, CURV>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb,
-                                                                     acc);
+                adj_split_nodes<DIM, N, D2, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
+                                                         sWb, wb);
         }
         __syncthreads();
     }
@@ -1476,6 +1782,12 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         kg_prim_to_cons_vjp<DIM>(rho, v, vv, P.U[(DIM + 1) * P.ndofs + gi], g1, acc, qb);
     } else {
         prim_to_cons_vjp<DIM>(rho, v, vv, p, g1, acc, qb);
+    }
+    if constexpr (G) {   // the projections' entropy variables of this node
+        double q[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
+        entropy_vjp<DIM>(q, p, g, wb, qb);
     }
     for (int k = 0; k < NV; ++k) {
         double ain = P.Ain[k * P.ndofs + gi];
@@ -1502,43 +1814,53 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     }
 }
 
-template <int DIM, int N, int TP, bool CURV = false>
+template <int DIM, int N, int TP, bool CURV = false, bool G = false>
 cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
-    constexpr size_t smem = AdjSplitShape<DIM, N, TP>::SMEM;
-    static_assert(smem <= 227 * 1024, "split adjoint tile exceeds shared memory");
+    constexpr size_t smem = AdjSplitShape<DIM, N, TP, G>::SMEM;
+    if constexpr (smem > 227 * 1024) {   // G: the Kennedy-Gruber 3D p=7 tile (checked on the host first)
+        return cudaErrorInvalidValue;
+    } else {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP, CURV>,
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP, CURV, G>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_split_elem_kernel<DIM, N, TP, CURV><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_split_elem_kernel<DIM, N, TP, CURV, G><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
+    }
 }
 
-template <int DIM, int TP, bool CURV = false>
+template <int DIM, int TP, bool CURV = false, bool G = false>
 cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_split_n<DIM, 2, TP, CURV>(P, s);
-        case 3: return launch_adj_split_n<DIM, 3, TP, CURV>(P, s);
-        case 4: return launch_adj_split_n<DIM, 4, TP, CURV>(P, s);
-        case 5: return launch_adj_split_n<DIM, 5, TP, CURV>(P, s);
-        case 6: return launch_adj_split_n<DIM, 6, TP, CURV>(P, s);
-        case 7: return launch_adj_split_n<DIM, 7, TP, CURV>(P, s);
-        case 8: return launch_adj_split_n<DIM, 8, TP, CURV>(P, s);
+        case 2: return launch_adj_split_n<DIM, 2, TP, CURV, G>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3, TP, CURV, G>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4, TP, CURV, G>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5, TP, CURV, G>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6, TP, CURV, G>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7, TP, CURV, G>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8, TP, CURV, G>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 // The split form's two-point flux: Chandrashekar, Kennedy-Gruber or StdAverage.
-template <int DIM, bool CURV = false>
+template <int DIM, bool CURV = false, bool G = false>
 cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
-    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER, CURV>(n, P, s);
-    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE, CURV>(n, P, s);
-    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV>(n, P, s);
+    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER, CURV, G>(n, P, s);
+    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE, CURV, G>(n, P, s);
+    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV, G>(n, P, s);
+}
+
+// Whether the Gauss-node split adjoint tile fits in shared memory (all but the Kennedy-Gruber 3D
+// p=7 tile do).
+inline bool adj_split_gauss_fits(int dim, int n, int tp) {
+    return !(dim == 3 && n == 8 && tp == FLOU_TP_KENNEDY_GRUBER) ||
+           AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, true>::SMEM <= 227 * 1024;
 }
 
 
@@ -1548,6 +1870,8 @@ cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t
 cudaError_t launch_adj_face(int dim, int kind, bool curv, bool gauss, int grid, int tb, const AdjFaceParams& F,
                             cudaStream_t s);
 cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, bool gauss, const AdjElemParams& P, cudaStream_t s);
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s);
+// gauss: the split form on a basis without boundary nodes (the entropy-projected coupling; Cartesian)
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, const AdjElemParams& P,
+                                 cudaStream_t s);
 
 }  // namespace flou

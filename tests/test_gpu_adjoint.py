@@ -520,13 +520,107 @@ def test_gauss_nodes_adjoint_solve_against_dual_numbers(op, dim):
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
-def test_gauss_nodes_split_form_is_not_differentiated():
+GAUSS_SPLIT_OPS = ["split", "split_stdface", "split_hllc", "split_kg", "split_std", "split_md", "split_sd"]
+
+
+@pytest.mark.parametrize("op", GAUSS_SPLIT_OPS)
+@pytest.mark.parametrize("dim,n,walls", [(1, 4, True), (2, 4, False), (2, 5, True), (3, 3, False), (3, 4, True)])
+def test_gauss_nodes_split_rhs_vjp_dot_product(dim, n, walls, op):
+    """The split form on Gauss nodes: the entropy-projected coupling (OpDivergence.jl:301-437)
+    transposed -- the pair fluxes of every node with its line's two projected states, the
+    projections' sums, the state of the projected entropy variables and the entropy variables of
+    every node -- against the oracle's dual numbers."""
+    eq = F.EulerEquation(dim, 1.4)
+    bcs = None
+    if walls:
+        bcs = {str(k): (F.EulerSlipBC() if k % 2 else F.EulerOutflowBC()) for k in range(1, 2 * dim + 1)}
+    disc = build(dim, n, (3,) * dim, eq, OPERATORS[op](), periodic=() if walls else True, bcs=bcs, basis="GL")
+    Q = smooth_euler_state(disc, seed=dim + n)
+    if walls:
+        P = eq.vars_cons2prim(Q)
+        P[:, 1:1 + dim] *= 0.2
+        Q = np.asfortranarray(eq.vars_prim2cons(P))
+    rng = np.random.default_rng(80 + dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    hll = op in HLL_FAMILY
+    dc = 0.0 * c if hll else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if hll else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op", ["split", "split_kg", "split_std"])
+def test_gauss_nodes_split_rhs_vjp_columns(op):
+    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), OPERATORS[op](), basis="GL")
+    rng = np.random.default_rng(26)
+    Q = smooth_euler_state(disc, seed=6, amp=0.3)
+    c = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 2
+    e = 4
+    for v in range(Q.shape[1]):
+        for i in range(e * npe, (e + 1) * npe):
+            dQ = np.zeros_like(Q)
+            dQ[i, v] = 1.0
+            _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+            col = np.sum(lam * dR)
+            assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+@pytest.mark.parametrize("op", ["split_hllc", "split_kg"])
+def test_gauss_nodes_split_adjoint_solve_against_dual_numbers(op):
+    eq = F.EulerEquation(3, 1.4)
+    disc = build(3, 4, (2, 3, 2), eq, OPERATORS[op](), box=((0.0,) * 3, (2 * np.pi,) * 3), basis="GL")
+    Q0 = _tgv_state(disc, 0.3, 5)
+    rng = np.random.default_rng(43)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 10)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 6
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 2, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+def test_gauss_nodes_split_adjoint_limits():
+    """Not covered: the split form on Gauss nodes on general geometry, and the Kennedy-Gruber 3D
+    p=7 tile (beyond shared memory)."""
     from flou_cuda import _lib as L
-    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), _split(), basis="GL")
-    Q = _dev(smooth_euler_state(disc, seed=1))
+    from test_unstructured import _std
+    eq = F.EulerEquation(2, 1.4)
+    mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=3)
+    disc = F.MultielementDisc(mesh, _std(2, 4, 4, "GL"), eq, _split(),
+                              {str(k): F.EulerOutflowBC() for k in range(1, 5)})
+    from test_unstructured import _state
+    Q = _dev(_state(disc, seed=1))
     g = torch.empty_like(Q)
     with pytest.raises(F.FlouError) as ei:
         disc.ctx.rhs_vjp(g, None, Q, Q)
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+    kg = build(3, 8, (1, 1, 1), F.EulerEquation(3, 1.4), OPERATORS["split_kg"](), basis="GL")
+    Q = _dev(smooth_euler_state(kg, seed=1))
+    g = torch.empty_like(Q)
+    with pytest.raises(F.FlouError) as ei:
+        kg.ctx.rhs_vjp(g, None, Q, Q)
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
 
 
