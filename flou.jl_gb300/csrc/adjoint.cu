@@ -52,11 +52,25 @@ struct AdjBuffers {
     double *QbL = nullptr, *QbR = nullptr, *Ibar = nullptr;
 };
 
+// The flux kind of adj_face_kernel / numflux_vjp for an interface flux (numflux, central part),
+// -1 for one the adjoint does not differentiate.
+int flux_kind(int nf, int avg) {
+    const int ch = avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
+    if (nf == FLOU_NF_HLLC) return 3;
+    if (nf == FLOU_NF_HLL) return 2;
+    if (avg != FLOU_NF_STD_AVERAGE && avg != FLOU_NF_CHANDRASHEKAR) return -1;
+    if (nf == FLOU_NF_SCALAR_DISSIPATION) return 4 + ch;
+    if (nf == FLOU_NF_MATRIX_DISSIPATION) return 6 + ch;
+    if (nf == FLOU_NF_LXF) return ch;
+    return -1;
+}
+int fv_kind(const flou_ctx* c) { return flux_kind(c->fvflux, c->fvavg); }
+
 // ssp_only: the batched adjoint, whose lockstep sweep steps with SSP-RK3 only.
 int adj_supported(flou_ctx* c, bool ssp_only = false) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
-               (k.volume_op == FLOU_OP_SPLIT &&
+               ((k.volume_op == FLOU_OP_SPLIT || k.volume_op == FLOU_OP_HYBRID) &&
                 (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER ||
                  k.twopoint_flux == FLOU_TP_STD_AVERAGE));
     bool nf = ((k.numflux == FLOU_NF_LXF || k.numflux == FLOU_NF_SCALAR_DISSIPATION ||
@@ -74,9 +88,21 @@ int adj_supported(flou_ctx* c, bool ssp_only = false) {
     if (k.volume_op == FLOU_OP_SPLIT && c->bnodes && !c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs the DGSEM lift on a basis "
                                                  "with boundary nodes");
-    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_gauss_fits(k.dim, c->n, k.twopoint_flux))
+    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, false))
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile of the Kennedy-Gruber flux at "
                                                  "3D p=7 exceeds shared memory");
+    if (k.volume_op == FLOU_OP_HYBRID) {
+        if (!c->bnodes || !c->lift_ends || c->curv)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto nodes "
+                                                     "and Cartesian geometry");
+        if (fv_kind(c) < 0)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator's subcell flux must be LxF, "
+                                                     "Scalar- or MatrixDissipation (StdAverage or "
+                                                     "ChandrasekharAverage), HLL or HLLC for the adjoint");
+        if (!adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, true))
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid adjoint tile of the Kennedy-Gruber flux at 3D p=7 "
+                                                     "exceeds shared memory");
+    }
     if (c->limiter)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
     if (ssp_only && c->lsrk_s)
@@ -142,10 +168,7 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     const int tb = face_block_size(nth);
     int grid = (int)((nth + tb - 1) / tb);
     int dim = c->cfg.dim;
-    const int nf = c->cfg.numflux;
-    const int ch = c->cfg.numflux_avg == FLOU_NF_CHANDRASHEKAR ? 1 : 0;
-    const int kind = nf == FLOU_NF_HLLC ? 3 : nf == FLOU_NF_HLL ? 2 : nf == FLOU_NF_SCALAR_DISSIPATION ? 4 + ch
-                   : nf == FLOU_NF_MATRIX_DISSIPATION ? 6 + ch : ch;
+    const int kind = flux_kind(c->cfg.numflux, c->cfg.numflux_avg);
     // interpolated traces and the full-line lift: the strong form on a basis without exact end-node
     // injection, the split form on a basis without boundary nodes (the forward's general paths)
     const bool gauss = c->cfg.volume_op == FLOU_OP_STRONG ? !c->lgl : !c->bnodes;
@@ -184,8 +207,15 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.K = K;
     P.kA = kA;
     P.kB = kB;
-    if (c->cfg.volume_op == FLOU_OP_SPLIT) {
-        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss, P, s);
+    P.omega1 = c->d_omega1;
+    P.fvkind = c->cfg.volume_op == FLOU_OP_HYBRID ? fv_kind(c) : 0;
+    P.fvflux = c->fvflux;
+    P.fvavg = c->fvavg;
+    P.fvintensity = c->fvintensity;
+    P.blend = c->blend;
+    if (c->cfg.volume_op != FLOU_OP_STRONG) {
+        e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss,
+                                 c->cfg.volume_op == FLOU_OP_HYBRID, P, s);
     } else {
         e = launch_adj_elem_dim(dim, c->n, c->curv, gauss, P, s);
     }

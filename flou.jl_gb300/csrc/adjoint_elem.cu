@@ -18,8 +18,11 @@ cudaError_t launch_adj_split_curv2d(int n, int tp, const AdjElemParams& P, cudaS
 cudaError_t launch_adj_split_curv3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_gauss(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s);
 cudaError_t launch_adj_split_gauss3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, const AdjElemParams& P,
+cudaError_t launch_adj_hybrid(int dim, int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_hybrid3d(int n, int tp, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, bool hybrid, const AdjElemParams& P,
                                  cudaStream_t s) {
+    if (hybrid) return dim == 3 ? launch_adj_hybrid3d(n, tp, P, s) : launch_adj_hybrid(dim, n, tp, P, s);
     if (gauss) return dim == 3 ? launch_adj_split_gauss3d(n, tp, P, s) : launch_adj_split_gauss(dim, n, tp, P, s);
     if (curv) return dim == 2 ? launch_adj_split_curv2d(n, tp, P, s) : launch_adj_split_curv3d(n, tp, P, s);
     if (dim == 1) return launch_adj_split_1d(n, tp, P, s);

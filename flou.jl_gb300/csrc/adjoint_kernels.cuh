@@ -98,6 +98,11 @@ struct AdjElemParams {
     // other readers are done: the face kernel ran before, and a block reads only its own nodes)
     double* K;
     double kA, kB;
+    // hybrid operator: 1D quadrature weights, the subcell FV flux (numflux_vjp kind) and its
+    // intensity, the blending constant
+    const double* omega1;
+    int32_t fvkind, fvflux, fvavg;   // numflux_vjp kind; the forward's numflux and central part
+    double fvintensity, blend;
 };
 
 // q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
@@ -796,21 +801,102 @@ __device__ __forceinline__ void md_vjp(const Prim& pa, const Prim& pb, double g,
     }
 }
 
+// VJP of the numerical flux of kind KIND (adj_face_kernel's list) in the face frame: a, b the
+// two states, fb the flux cotangent; ab, bbar receive the states' cotangents (overwritten).
+// Returns the cotangent of the dissipation intensity (LxF only).
+template <int DIM, int KIND>
+__device__ __forceinline__ double numflux_vjp(const double* a, const double* b, double inten, double g,
+                                              const double* fb, double* ab, double* bbar) {
+    constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
+    constexpr bool SD = KIND == 4 || KIND == 5;
+    constexpr bool MD = KIND >= 6;
+    constexpr int NV = DIM + 2;
+    const double g1 = g - 1.0;
+    Prim pa = prim_of<DIM>(a, g);
+    const double* bb = b;
+    Prim pb = prim_of<DIM>(bb, g);
+    double Ib = 0.0;
+    if (KIND == 2 || KIND == 3) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
+#pragma unroll
+        for (int k = 0; k < NV; ++k) ab[k] = bbar[k] = 0.0;
+        hll_family_vjp<DIM>(KIND == 3, a, bb, pa, pb, g, fb, ab, bbar);
+    } else {
+    double ll = fabs(pa.v[0]) + pa.a, lr = fabs(pb.v[0]) + pb.a;
+    bool left = lr < ll;   // Base.max(ll, lr)
+    double lam = left ? ll : lr;
+    double dot = 0.0;
+    SideBar Ls = {}, Rs = {};
+    if (MD) {   // F = A + ½ · intensity · R|Λ|TRᵀΔW: no wave-speed maximum
+        double ob[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ob[k] = 0.5 * inten * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        md_vjp<DIM>(pa, pb, g, ob, ab, bbar, Ls, Rs);
+    } else if (SD) {   // F = A - λ/2 · intensity · D(a, b)
+        double D[NV], Db[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            Db[k] = -0.5 * inten * lam * fb[k];
+            ab[k] = bbar[k] = 0.0;
+        }
+        sd_jump_vjp<DIM>(a, bb, pa, pb, g, Db, D, ab, bbar, Ls, Rs);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dot = fma(-fb[k], D[k], dot);
+    } else {    // F = A + λ/2 · intensity · (a - b)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ab[k] = 0.5 * inten * lam * fb[k];
+            bbar[k] = -ab[k];
+        }
+    }
+    Ib = (SD || MD) ? 0.0 : 0.5 * lam * dot;   // the dissipation fluxes take no per-element scale
+    if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
+        PrimBar o1, o2;
+        double vh1[DIM], vh2[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            vh1[k] = 0.5 * pa.v[k];
+            vh2[k] = 0.5 * pb.v[k];
+        }
+        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho * rcp_refined(pa.p), 0.25 * pa.vv,
+                                       0.5 * pb.rho, vh2, 0.25 * pb.rho * rcp_refined(pb.p), 0.25 * pb.vv,
+                                       0.5 / g1, fb, o1, o2);
+        prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
+        prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
+    } else {
+        euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
+        euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
+    }
+    if (!MD) {
+        double kappa = 0.5 * inten * dot;
+        if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
+        else lambda_vjp<DIM>(pb, g, kappa, bbar);
+    }
+    if (SD || MD) {
+        side_prim_vjp<DIM>(pa, g, Ls, ab);
+        side_prim_vjp<DIM>(pb, g, Rs, bbar);
+    }
+    }
+    return Ib;
+}
+
 // KIND: 0 LxF(StdAverage), 1 LxF(ChandrasekharAverage), 2 HLL, 3 HLLC,
 // 4 ScalarDissipation(StdAverage), 5 ScalarDissipation(ChandrasekharAverage),
 // 6 MatrixDissipation(StdAverage), 7 MatrixDissipation(ChandrasekharAverage).
 // CURV: general geometry, the forward face kernel's CURV path transposed: the slave trace at
 // master2slave(m, o), per-node 1/J on both sides, the face-node frame (n, t, b) and surface
 // Jacobian (a = R q, F = J Rᵀ F_face: F̄_face = J R F̄, q̄ = Rᵀ ā).
-// G: a basis without exact end-node injection (Gauss nodes; the strong form only): the traces
-// are the interpolations Σ_p l[p] U_p along the line, and the lift reaches every node of it, so
+// G: the forward's general trace path (the strong form without exact end-node injection, the
+// split form on Gauss nodes): the traces are the interpolations Σ_p l[p] U_p along the line, and
+// the lift reaches every node of it, so
 // the flux cotangent gathers -Σ_p ∂g[p] w_p over the line (the element kernel scatters the trace
 // cotangents back with l).
 template <int DIM, int KIND, bool CURV = false, bool G = false>
 __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
-    constexpr bool CHANDRA = KIND == 1 || KIND == 5 || KIND == 7;
-    constexpr bool SD = KIND == 4 || KIND == 5;
-    constexpr bool MD = KIND >= 6;
     constexpr int NV = DIM + 2;
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
@@ -938,77 +1024,8 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
         inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
     }
-    const double g = P.gamma, g1 = g - 1.0;
-    Prim pa = prim_of<DIM>(a, g);
-    const double* bb = b;
-    Prim pb = prim_of<DIM>(bb, g);
     double ab[NV], bbar[NV];
-    double Ib = 0.0;
-    if (KIND == 2 || KIND == 3) {   // HLL / HLLC: no dissipation scale, so no intensity cotangent
-#pragma unroll
-        for (int k = 0; k < NV; ++k) ab[k] = bbar[k] = 0.0;
-        hll_family_vjp<DIM>(KIND == 3, a, bb, pa, pb, g, fb, ab, bbar);
-    } else {
-    double ll = fabs(pa.v[0]) + pa.a, lr = fabs(pb.v[0]) + pb.a;
-    bool left = lr < ll;   // Base.max(ll, lr)
-    double lam = left ? ll : lr;
-    double dot = 0.0;
-    SideBar Ls = {}, Rs = {};
-    if (MD) {   // F = A + ½ · intensity · R|Λ|TRᵀΔW: no wave-speed maximum
-        double ob[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            ob[k] = 0.5 * inten * fb[k];
-            ab[k] = bbar[k] = 0.0;
-        }
-        md_vjp<DIM>(pa, pb, g, ob, ab, bbar, Ls, Rs);
-    } else if (SD) {   // F = A - λ/2 · intensity · D(a, b)
-        double D[NV], Db[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            Db[k] = -0.5 * inten * lam * fb[k];
-            ab[k] = bbar[k] = 0.0;
-        }
-        sd_jump_vjp<DIM>(a, bb, pa, pb, g, Db, D, ab, bbar, Ls, Rs);
-#pragma unroll
-        for (int k = 0; k < NV; ++k) dot = fma(-fb[k], D[k], dot);
-    } else {    // F = A + λ/2 · intensity · (a - b)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) dot = fma(fb[k], a[k] - bb[k], dot);
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            ab[k] = 0.5 * inten * lam * fb[k];
-            bbar[k] = -ab[k];
-        }
-    }
-    Ib = (SD || MD) ? 0.0 : 0.5 * lam * dot;   // the dissipation fluxes take no per-element scale
-    if (CHANDRA) {   // LxF(ChandrasekharAverage): the pair flux of the two traces
-        PrimBar o1, o2;
-        double vh1[DIM], vh2[DIM];
-#pragma unroll
-        for (int k = 0; k < DIM; ++k) {
-            vh1[k] = 0.5 * pa.v[k];
-            vh2[k] = 0.5 * pb.v[k];
-        }
-        chandra_pair_vjp<DIM, 0, true>(0.5 * pa.rho, vh1, 0.25 * pa.rho * rcp_refined(pa.p), 0.25 * pa.vv,
-                                       0.5 * pb.rho, vh2, 0.25 * pb.rho * rcp_refined(pb.p), 0.25 * pb.vv,
-                                       0.5 / g1, fb, o1, o2);
-        prim_to_cons_vjp<DIM>(pa.rho, pa.v, pa.vv, pa.p, g1, o1, ab);
-        prim_to_cons_vjp<DIM>(pb.rho, pb.v, pb.vv, pb.p, g1, o2, bbar);
-    } else {
-        euler_flux_vjp<DIM>(0, pa.v, pa.vv, pa.H, g1, fb, 0.5, ab);
-        euler_flux_vjp<DIM>(0, pb.v, pb.vv, pb.H, g1, fb, 0.5, bbar);
-    }
-    if (!MD) {
-        double kappa = 0.5 * inten * dot;
-        if (left) lambda_vjp<DIM>(pa, g, kappa, ab);
-        else lambda_vjp<DIM>(pb, g, kappa, bbar);
-    }
-    if (SD || MD) {
-        side_prim_vjp<DIM>(pa, g, Ls, ab);
-        side_prim_vjp<DIM>(pb, g, Rs, bbar);
-    }
-    }
+    const double Ib = numflux_vjp<DIM, KIND>(a, b, inten, P.gamma, fb, ab, bbar);
     if (s1 < 0) {
         if (bck == FLOU_BC_OUTFLOW) {
 #pragma unroll
@@ -1204,7 +1221,7 @@ cudaError_t launch_adj_elem(int n, const AdjElemParams& P, cudaStream_t s) {
 // the node phase then sums its pairs, adds the diagonal term D♯(i,i) F(Q_i) (the physical flux;
 // zero on interior LGL nodes) and the face traces, and finally maps (ρ̄, v̄, β̄) to the conserved
 // variables.
-template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR, bool G = false>
+template <int DIM, int N, int TP = FLOU_TP_CHANDRASHEKAR, bool G = false, bool H = false>
 struct AdjSplitShape {
     using S = Shape<DIM, N>;
     static constexpr bool KG = TP == FLOU_TP_KENNEDY_GRUBER;
@@ -1219,13 +1236,14 @@ struct AdjSplitShape {
     // G (Gauss nodes): per line side the cotangent of its projected entropy variables, and per node
     // the cotangents of its two projected-state pair fluxes
     static constexpr int NPROJ = G ? 2 * S::EPB * S::NFD : 0;
-    static constexpr int NGX = G ? NV * NPROJ + NPB * S::NN : 0;
+    // H (hybrid operator): per node the subcell-flux values, then their cotangents
+    static constexpr int NGX = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0);
     static constexpr size_t SMEM =
         sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD + NGX) +
         2 * (S::NPAIR + 1);
     // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
     // (G: one, for the projection's registers)
-    static constexpr int MINB = (!G && S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
+    static constexpr int MINB = (!G && !H && S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
 };
 
 // Per-node quantities the split adjoint keeps for a state q (p its pressure): Chandrashekar
@@ -1491,6 +1509,272 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
     }
 }
 
+// The Euler flux along axis D of a conserved state.
+template <int DIM, int D>
+__device__ __forceinline__ void euler_flux_axis(const double* q, double g, double* F) {
+    const double ir = rcp_refined(q[0]);
+    double ke = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k] * ir, ke);
+    const double p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]), vd = q[1 + D] * ir;
+    F[0] = q[1 + D];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) F[1 + k] = fma(q[1 + k], vd, k == D ? p : 0.0);
+    F[DIM + 1] = (q[DIM + 1] + p) * vd;
+}
+
+// The split form's two-point flux along axis D (the forward of split_pair_vjp) from the nodes'
+// split_node_values A, B; StdAverage takes the conserved states qa, qb.
+template <int DIM, int D, int TP>
+__device__ __forceinline__ void split_pair_flux(const double* A, const double* B, const double* qa, const double* qb,
+                                                double g, double* F) {
+    constexpr int NV = DIM + 2;
+    if constexpr (TP == FLOU_TP_STD_AVERAGE) {
+        double Fa[NV], Fc[NV];
+        euler_flux_axis<DIM, D>(qa, g, Fa);
+        euler_flux_axis<DIM, D>(qb, g, Fc);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = 0.5 * (Fa[k] + Fc[k]);
+    } else if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) {
+        const double rho = A[0] + B[0], pm = A[1 + DIM] + B[1 + DIM], en = A[2 + DIM] + B[2 + DIM];
+        double vm[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) vm[k] = A[1 + k] + B[1 + k];
+        const double m = rho * vm[D];
+        F[0] = m;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, vm[k], k == D ? pm : 0.0);
+        F[DIM + 1] = fma(m, en, pm * vm[D]);
+    } else {
+        const double hsr = A[0] + B[0], hdr = A[0] - B[0], hsb = A[1 + DIM] + B[1 + DIM],
+                     hdb = A[1 + DIM] - B[1 + DIM];
+        const double R = rcp_refined(hsr * hsb), rs = hsb * R, rb = hsr * R;
+        double rho, irho, beta, ibeta, d1, d2;
+        logmean_half(A[0], B[0], hsr, hdr, rs, rho, irho, d1, d2);
+        logmean_half(A[1 + DIM], B[1 + DIM], hsb, hdb, rb, beta, ibeta, d1, d2);
+        const double p = 0.5 * hsr * rb;
+        double va[DIM], vv = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            va[k] = A[1 + k] + B[1 + k];
+            vv = fma(va[k], va[k], vv);
+        }
+        const double h = fma(0.5 * rcp_refined(g - 1.0), ibeta, -(A[2 + DIM] + B[2 + DIM])) + fma(p, irho, vv);
+        const double m = rho * va[D];
+        F[0] = m;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], k == D ? p : 0.0);
+        F[DIM + 1] = m * h;
+    }
+}
+
+// numflux_vjp for a kind known at run time (the hybrid operator's subcell FV flux).
+template <int DIM>
+__device__ __noinline__ void numflux_vjp_any(int kind, const double* a, const double* b, double inten, double g,
+                                             const double* fb, double* ab, double* bbar) {
+    switch (kind) {
+        case 0: numflux_vjp<DIM, 0>(a, b, inten, g, fb, ab, bbar); break;
+        case 1: numflux_vjp<DIM, 1>(a, b, inten, g, fb, ab, bbar); break;
+        case 2: numflux_vjp<DIM, 2>(a, b, inten, g, fb, ab, bbar); break;
+        case 3: numflux_vjp<DIM, 3>(a, b, inten, g, fb, ab, bbar); break;
+        case 4: numflux_vjp<DIM, 4>(a, b, inten, g, fb, ab, bbar); break;
+        case 5: numflux_vjp<DIM, 5>(a, b, inten, g, fb, ab, bbar); break;
+        case 6: numflux_vjp<DIM, 6>(a, b, inten, g, fb, ab, bbar); break;
+        default: numflux_vjp<DIM, 7>(a, b, inten, g, fb, ab, bbar); break;
+    }
+}
+
+// H (HybridDivOperator on Gauss-Lobatto nodes, Cartesian; OpDivergence.jl:553-604 with the
+// blending of :781-801), one direction D.  Forward: the high-order subcell fluxes F̄_p =
+// Σ_{r<p} ω_r Ja (Σ_j D♯_rj F♯_rj) (recomputed: pair fluxes, node sums, exclusive scan), the FV
+// fluxes Fv_p = Ja Fv(Q_(p-1), Q_p) along the axis, b = (W_p - W_(p-1))·(F̄_p - Fv_p),
+// δ = max(1 - b/√(b²+c), ½), F_p = Fv_p + δ (F̄_p - Fv_p), dQ_p += (F_p - F_(p+1))/ω_p (F_0 = F_N =
+// 0).  Reverse, with w = λ/J: F̄b_p = w_p/ω_p - w_(p-1)/ω_(p-1); δ̄ = F̄b·(F̄ - Fv), b̄ = -δ̄ c/√(b²+c)³
+// on the unclipped branch; the cotangent of F̄_p is δ F̄b + b̄ ΔW, that of Fv (1-δ) F̄b - b̄ ΔW (through
+// the FV flux VJP to both nodes), ΔW's b̄ (F̄ - Fv) goes through W's VJP; the suffix sums of the F̄
+// cotangents give each node's pair weight w'_r = -ω_r Σ_(p>r) F̄̄_p, left in sH for the split-form
+// pair and node phases.  A node's contribution from the interface on its right is handed over in
+// spb (free between the phases); the node's own goes to qb.
+template <int DIM, int N, int D, int TP>
+__device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
+                                               const double* sops, const double* sprim, const double* sw, double* sH,
+                                               double* spb, const uint8_t* stab, double* qb) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP, false, true>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR, NARR = A::NARR;
+    constexpr int NPT = A::NPT;
+    const double g = P.gamma;
+    const double* Dsh = sops + N * N;
+    const int tid = threadIdx.x;
+    // forward pair fluxes into spb as [NV][NPT]
+    for (int kp = tid; kp < NPT; kp += blockDim.x) {
+        const int elp = kp / (NFD * NPAIR);
+        const int r = kp - elp * (NFD * NPAIR);
+        const int line = r / NPAIR, pp = r - line * NPAIR;
+        if (e0 + elp >= P.nelem) continue;
+        const int ia = elp * NPE + tp_node<DIM>(N, D, line, stab[2 * pp]);
+        const int ib = elp * NPE + tp_node<DIM>(N, D, line, stab[2 * pp + 1]);
+        double Av[NARR], Bv[NARR], qa[NV], qc[NV], F[NV];
+#pragma unroll
+        for (int k = 0; k < NARR; ++k) {
+            Av[k] = sprim[k * NN + ia];
+            Bv[k] = sprim[k * NN + ib];
+        }
+        if constexpr (TP == FLOU_TP_STD_AVERAGE) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                qa[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + ia];
+                qc[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + ib];
+            }
+        }
+        split_pair_flux<DIM, D, TP>(Av, Bv, qa, qc, g, F);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) spb[k * NPT + kp] = F[k];
+    }
+    __syncthreads();
+    const int e = e0 + el;
+    int pos = 0, line = 0;
+    tp_coords<DIM>(N, i, D, pos, line);
+    const int64_t gi = (int64_t)e * NPE + i;
+    const double Ja = active ? P.Ja[e * DIM + D] : 0.0;
+    if (active) {   // ω_p Ja Σ_j D♯_pj F♯_pj (with the diagonal D♯_pp F(Q_p))
+        double q[NV], acc[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
+        euler_flux_axis<DIM, D>(q, g, acc);
+        const double dii = Dsh[pos + pos * N];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] *= dii;
+        const int pbase = el * NFD * NPAIR + line * NPAIR;
+#pragma unroll
+        for (int t = 1; t < N; ++t) {
+            const int j = pos + t < N ? pos + t : pos + t - N;
+            const int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+            const int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+            const double a = Dsh[pos + j * N];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] = fma(a, spb[k * NPT + pidx], acc[k]);
+        }
+        const double wq = P.omega1[pos] * Ja;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sH[k * NN + tid] = wq * acc[k];
+    }
+    __syncthreads();
+    for (int t = tid; t < S::EPB * NFD; t += blockDim.x) {   // F̄_p: exclusive scan along each line
+        const int elp = t / NFD, ln = t - elp * NFD;
+        if (e0 + elp >= P.nelem) continue;
+        double run[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) run[k] = 0.0;
+        for (int pp = 0; pp < N; ++pp) {
+            const int j = elp * NPE + tp_node<DIM>(N, D, ln, pp);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double x = sH[k * NN + j];
+                sH[k * NN + j] = run[k];
+                run[k] += x;
+            }
+        }
+    }
+    __syncthreads();
+    if (active && pos > 0) {   // the subcell interface between pos-1 and pos
+        const int il = el * NPE + tp_node<DIM>(N, D, line, pos - 1);
+        const int64_t gl = (int64_t)e0 * NPE + il;
+        double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV], wl[NV], wr[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ql[k] = P.U[k * P.ndofs + gl];
+            qr[k] = P.U[k * P.ndofs + gi];
+        }
+        const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
+        a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+        cart_to_face<DIM>(ql, Ax, a);
+        cart_to_face<DIM>(qr, Ax, b);
+        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+        Fv[0] = Fr[0] * Ja;
+        Fv[DIM + 1] = Fr[DIM + 1] * Ja;
+        cart_to_phys<DIM>(Fr, Ax, Fv);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) Fv[1 + k] *= Ja;
+        entropy_of<DIM>(ql, g, wl);
+        entropy_of<DIM>(qr, g, wr);
+        double bb = 0.0, dW[NV], Fh[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            dW[k] = wr[k] - wl[k];
+            Fh[k] = sH[k * NN + tid];
+            bb = fma(dW[k], Fh[k] - Fv[k], bb);
+        }
+        const double dl = sqrt_refined(fma(bb, bb, P.blend)), idl = rcp_refined(dl);
+        const double draw = (dl - bb) * idl;
+        const bool free_ = 0.5 < draw;   // Base.max(draw, 0.5) takes draw only above 0.5
+        const double dlt = free_ ? draw : 0.5;
+        const double iwp = rcp_refined(P.omega1[pos]), iwm = rcp_refined(P.omega1[pos - 1]);
+        double Fb[NV], db = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            Fb[k] = fma(sw[k * NN + tid], iwp, -sw[k * NN + il] * iwm);
+            db = fma(Fb[k], Fh[k] - Fv[k], db);
+        }
+        const double bbar = free_ ? -db * P.blend * idl * idl * idl : 0.0;
+        double Fvb[NV], wbar[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sH[k * NN + tid] = fma(dlt, Fb[k], bbar * dW[k]);   // the cotangent of F̄_p
+            Fvb[k] = fma(1.0 - dlt, Fb[k], -bbar * dW[k]);
+            wbar[k] = bbar * (Fh[k] - Fv[k]);
+        }
+        double Frb[NV], ab[NV], bbr[NV], t[NV], ol[NV], orr[NV];
+        Frb[0] = Ja * Fvb[0];
+        Frb[DIM + 1] = Ja * Fvb[DIM + 1];
+        cart_to_face<DIM>(Fvb, Ax, t);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) Frb[1 + k] = Ja * t[1 + k];
+        numflux_vjp_any<DIM>(P.fvkind, a, b, P.fvintensity, g, Frb, ab, bbr);
+        ol[0] = ab[0]; ol[DIM + 1] = ab[DIM + 1]; orr[0] = bbr[0]; orr[DIM + 1] = bbr[DIM + 1];
+        cart_to_phys<DIM>(ab, Ax, ol);
+        cart_to_phys<DIM>(bbr, Ax, orr);
+        auto pressure = [&](const double* q) {
+            double ke = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k], ke);
+            return (g - 1.0) * fma(-0.5, ke * rcp_refined(q[0]), q[DIM + 1]);
+        };
+        const double pr = pressure(qr), plv = pressure(ql);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qb[k] += orr[k];
+        entropy_vjp<DIM>(qr, pr, g, wbar, qb);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) wbar[k] = -wbar[k];
+        entropy_vjp<DIM>(ql, plv, g, wbar, ol);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) spb[k * NN + il] = ol[k];
+    }
+    __syncthreads();
+    for (int t = tid; t < S::EPB * NFD; t += blockDim.x) {   // w'_r = -ω_r Σ_(p>r) F̄̄_p, in place
+        const int elp = t / NFD, ln = t - elp * NFD;
+        if (e0 + elp >= P.nelem) continue;
+        double run[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) run[k] = 0.0;
+        for (int pp = N - 1; pp >= 0; --pp) {
+            const int j = elp * NPE + tp_node<DIM>(N, D, ln, pp);
+            const double wq = -P.omega1[pp];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double x = pp > 0 ? sH[k * NN + j] : 0.0;
+                sH[k * NN + j] = wq * run[k];
+                run[k] += x;
+            }
+        }
+    }
+    if (active && pos < N - 1) {   // the cotangent from the interface on this node's right
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qb[k] += spb[k * NN + tid];
+    }
+    __syncthreads();
+}
+
 // CURV: the pair flux along the averaged metric column n̄ = (Ja_a + Ja_b)/2 of direction D (the
 // metric terms are in the flux; sJD then holds -D♯ alone).
 template <int DIM, int N, int D, int TP, bool CURV = false>
@@ -1657,11 +1941,12 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     }
 }
 
-template <int DIM, int N, int TP, bool CURV = false, bool G = false>
-__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP, G>::MINB)
+// H: the hybrid operator (adj_hybrid_dir gives the pair weights of each direction).
+template <int DIM, int N, int TP, bool CURV = false, bool G = false, bool H = false>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP, G, H>::MINB)
     adj_split_elem_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N, TP, G>;
+    using A = AdjSplitShape<DIM, N, TP, G, H>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
     constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
     extern __shared__ double smem[];
@@ -1672,6 +1957,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
     double* sWb = sJD + A::NSD;          // G: [NV][NPROJ] projected entropy-variable cotangents
     double* snode = sWb + NV * A::NPROJ; // G: [NPB][NN] projected-state pair cotangents per node
+    double* sHy = snode + (G ? NPB * NN : 0);   // H: [NV][NN] subcell fluxes, then the pair weights
     uint8_t* stab = (uint8_t*)(sJD + A::NSD + A::NGX);
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
@@ -1745,11 +2031,17 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
 #pragma unroll
     for (int k = 0; k < NV; ++k) wb[k] = 0.0;
     constexpr int D1 = DIM > 1 ? 1 : 0, D2 = DIM > 2 ? 2 : 0;
+    const double* swd = H ? sHy : sw;   // the pair weights
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
-        if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
-        else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, sw, spb, stab, cb);
+        if constexpr (H) {
+            if (dir == 0) adj_hybrid_dir<DIM, N, 0, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+            else if (dir == 1) adj_hybrid_dir<DIM, N, D1, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+            else adj_hybrid_dir<DIM, N, D2, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+        }
+        if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
+        else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
+        else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         if constexpr (G) {
             if (dir == 0) adj_split_projection<DIM, N, 0, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
             else if (dir == 1) adj_split_projection<DIM, N, D1, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
@@ -1758,14 +2050,14 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         __syncthreads();
         if (active) {
             if (dir == 0)
-                adj_split_nodes<DIM, N, 0, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
+                adj_split_nodes<DIM, N, 0, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc, snode,
                                                         sWb, wb);
             else if (dir == 1)
-                adj_split_nodes<DIM, N, D1, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
-                                                         sWb, wb);
+                adj_split_nodes<DIM, N, D1, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
+                                                         snode, sWb, wb);
             else
-                adj_split_nodes<DIM, N, D2, TP, CURV, G>(P, e, el, i, gi, Dsh, sw, spb, v, rho, p, g1, qb, acc, snode,
-                                                         sWb, wb);
+                adj_split_nodes<DIM, N, D2, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
+                                                         snode, sWb, wb);
         }
         __syncthreads();
     }
@@ -1814,53 +2106,54 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     }
 }
 
-template <int DIM, int N, int TP, bool CURV = false, bool G = false>
+template <int DIM, int N, int TP, bool CURV = false, bool G = false, bool H = false>
 cudaError_t launch_adj_split_n(const AdjElemParams& P, cudaStream_t s) {
     using S = Shape<DIM, N>;
-    constexpr size_t smem = AdjSplitShape<DIM, N, TP, G>::SMEM;
-    if constexpr (smem > 227 * 1024) {   // G: the Kennedy-Gruber 3D p=7 tile (checked on the host first)
+    constexpr size_t smem = AdjSplitShape<DIM, N, TP, G, H>::SMEM;
+    if constexpr (smem > 227 * 1024) {   // G, H: the Kennedy-Gruber 3D p=7 tile (checked on the host first)
         return cudaErrorInvalidValue;
     } else {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP, CURV, G>,
+        attr = cudaFuncSetAttribute(adj_split_elem_kernel<DIM, N, TP, CURV, G, H>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
     if (attr != cudaSuccess) return attr;
     int grid = (P.nelem + S::EPB - 1) / S::EPB;
-    adj_split_elem_kernel<DIM, N, TP, CURV, G><<<grid, S::BLOCK, smem, s>>>(P);
+    adj_split_elem_kernel<DIM, N, TP, CURV, G, H><<<grid, S::BLOCK, smem, s>>>(P);
     return cudaGetLastError();
     }
 }
 
-template <int DIM, int TP, bool CURV = false, bool G = false>
+template <int DIM, int TP, bool CURV = false, bool G = false, bool H = false>
 cudaError_t launch_adj_split_tp(int n, const AdjElemParams& P, cudaStream_t s) {
     switch (n) {
-        case 2: return launch_adj_split_n<DIM, 2, TP, CURV, G>(P, s);
-        case 3: return launch_adj_split_n<DIM, 3, TP, CURV, G>(P, s);
-        case 4: return launch_adj_split_n<DIM, 4, TP, CURV, G>(P, s);
-        case 5: return launch_adj_split_n<DIM, 5, TP, CURV, G>(P, s);
-        case 6: return launch_adj_split_n<DIM, 6, TP, CURV, G>(P, s);
-        case 7: return launch_adj_split_n<DIM, 7, TP, CURV, G>(P, s);
-        case 8: return launch_adj_split_n<DIM, 8, TP, CURV, G>(P, s);
+        case 2: return launch_adj_split_n<DIM, 2, TP, CURV, G, H>(P, s);
+        case 3: return launch_adj_split_n<DIM, 3, TP, CURV, G, H>(P, s);
+        case 4: return launch_adj_split_n<DIM, 4, TP, CURV, G, H>(P, s);
+        case 5: return launch_adj_split_n<DIM, 5, TP, CURV, G, H>(P, s);
+        case 6: return launch_adj_split_n<DIM, 6, TP, CURV, G, H>(P, s);
+        case 7: return launch_adj_split_n<DIM, 7, TP, CURV, G, H>(P, s);
+        case 8: return launch_adj_split_n<DIM, 8, TP, CURV, G, H>(P, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 // The split form's two-point flux: Chandrashekar, Kennedy-Gruber or StdAverage.
-template <int DIM, bool CURV = false, bool G = false>
+template <int DIM, bool CURV = false, bool G = false, bool H = false>
 cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t s) {
-    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER, CURV, G>(n, P, s);
-    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE, CURV, G>(n, P, s);
-    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV, G>(n, P, s);
+    if (tp == FLOU_TP_KENNEDY_GRUBER) return launch_adj_split_tp<DIM, FLOU_TP_KENNEDY_GRUBER, CURV, G, H>(n, P, s);
+    if (tp == FLOU_TP_STD_AVERAGE) return launch_adj_split_tp<DIM, FLOU_TP_STD_AVERAGE, CURV, G, H>(n, P, s);
+    return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV, G, H>(n, P, s);
 }
 
-// Whether the Gauss-node split adjoint tile fits in shared memory (all but the Kennedy-Gruber 3D
-// p=7 tile do).
-inline bool adj_split_gauss_fits(int dim, int n, int tp) {
-    return !(dim == 3 && n == 8 && tp == FLOU_TP_KENNEDY_GRUBER) ||
-           AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, true>::SMEM <= 227 * 1024;
+// Whether the Gauss-node split (G) or hybrid (H) adjoint tile fits in shared memory (all but the
+// Kennedy-Gruber 3D p=7 tile do).
+inline bool adj_split_tile_fits(int dim, int n, int tp, bool hybrid) {
+    if (!(dim == 3 && n == 8 && tp == FLOU_TP_KENNEDY_GRUBER)) return true;
+    return hybrid ? AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, false, true>::SMEM <= 227 * 1024
+                  : AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, true>::SMEM <= 227 * 1024;
 }
 
 
@@ -1870,8 +2163,9 @@ inline bool adj_split_gauss_fits(int dim, int n, int tp) {
 cudaError_t launch_adj_face(int dim, int kind, bool curv, bool gauss, int grid, int tb, const AdjFaceParams& F,
                             cudaStream_t s);
 cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, bool gauss, const AdjElemParams& P, cudaStream_t s);
-// gauss: the split form on a basis without boundary nodes (the entropy-projected coupling; Cartesian)
-cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, const AdjElemParams& P,
+// gauss: the split form on a basis without boundary nodes (the entropy-projected coupling;
+// Cartesian); hybrid: the hybrid operator on Gauss-Lobatto nodes (Cartesian)
+cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, bool hybrid, const AdjElemParams& P,
                                  cudaStream_t s);
 
 }  // namespace flou

@@ -263,15 +263,20 @@ int32_t flou_fp64_dmma_peak(double* gflops);
 int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_err);
 
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
- * Covers the Euler equations with the strong-form volume term or the split form with the
- * Chandrashekar, Kennedy-Gruber or StdAverage two-point flux; the LxF, ScalarDissipation or
- * MatrixDissipation interface flux with the StdAverage or ChandrasekharAverage central part,
- * HLL and HLLC; on Gauss-Lobatto or Gauss nodes, Cartesian or general geometry (the split form
- * on Gauss nodes: Cartesian), with periodic, slip-wall, outflow,
- * inflow and boundary-state-field boundaries (fixed external states: constants of the
- * differentiation); flou_adjoint_solve differentiates SSP-RK3 or the 2N-storage method set by
- * flou_set_integrator (flou_adjoint_solve_batch: SSP-RK3).  Other contexts return
- * FLOU_ERR_UNSUPPORTED (the hybrid operator, the limiter).
+ * Covers the Euler equations with
+ *  - the strong form, the split form (Chandrashekar, Kennedy-Gruber or StdAverage two-point
+ *    flux) and the hybrid operator (Gauss-Lobatto nodes and Cartesian geometry; any interface
+ *    flux below as its subcell flux);
+ *  - the LxF, ScalarDissipation or MatrixDissipation interface flux (StdAverage or
+ *    ChandrasekharAverage central part), HLL and HLLC;
+ *  - Gauss-Lobatto or Gauss nodes, Cartesian or general geometry (the split form on Gauss
+ *    nodes: Cartesian geometry);
+ *  - periodic, slip-wall, outflow, inflow and boundary-state-field boundaries (fixed external
+ *    states are constants of the differentiation);
+ *  - SSP-RK3 or the 2N-storage method set by flou_set_integrator (flou_adjoint_solve_batch:
+ *    SSP-RK3).
+ * Other contexts (a limiter; the Kennedy-Gruber 3D p=7 tile of the Gauss-node split and hybrid
+ * forms) return FLOU_ERR_UNSUPPORTED.
  * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):
  * max(a, b) takes b unless b < a; d|u|/du = -1 for a set sign bit, else +1. */
 

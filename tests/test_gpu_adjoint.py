@@ -624,6 +624,122 @@ def test_gauss_nodes_split_adjoint_limits():
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
 
 
+HYBRID_OPS = {
+    # blend 0.5 with HLLC: the δ = ½ clip is active at some interfaces and not at others
+    "hybrid_hllc": lambda: F.HybridDivOperator(F.ChandrasekharAverage(), F.HLLC(),
+                                               F.LxF(F.ChandrasekharAverage(), 1.0), 0.5),
+    "hybrid_md": lambda: F.HybridDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), 1.0),
+    "hybrid_kg": lambda: F.HybridDivOperator(F.KennedyGruberAverage(), F.LxF(F.StdAverage(), 1.0), 1e-3),
+    "hybrid_std_hll": lambda: F.HybridDivOperator(F.StdAverage(), F.HLL(), F.HLL(), 0.1),
+}
+
+
+def _hybrid_disc(dim, n, op, walls, seed):
+    eq = F.EulerEquation(dim, 1.4)
+    bcs = None
+    if walls:
+        bcs = {str(k): (F.EulerSlipBC() if k % 2 else F.EulerOutflowBC()) for k in range(1, 2 * dim + 1)}
+    disc = build(dim, n, (3,) * dim, eq, HYBRID_OPS[op](), periodic=() if walls else True, bcs=bcs)
+    Q = smooth_euler_state(disc, seed=seed, amp=0.3)
+    if walls:
+        P = eq.vars_cons2prim(Q)
+        P[:, 1:1 + dim] *= 0.2
+        Q = np.asfortranarray(eq.vars_prim2cons(P))
+    return disc, Q
+
+
+def _hybrid_c(disc, op, c):
+    """Sets the per-element dissipation scale where the interface flux has one (LxF)."""
+    if op in ("hybrid_kg",):
+        disc.ctx.set_dissipation(c)
+        return c, False
+    return np.ones_like(c), True
+
+
+@pytest.mark.parametrize("op", sorted(HYBRID_OPS))
+@pytest.mark.parametrize("dim,n,walls", [(1, 5, True), (2, 4, False), (2, 5, True), (3, 3, True), (3, 4, False)])
+def test_hybrid_rhs_vjp_dot_product(dim, n, walls, op):
+    """HybridDivOperator on Gauss-Lobatto nodes: the blended subcell fluxes transposed (the FV
+    flux VJP, Fisher's indicator through the entropy variables, the ½ clip, the telescoped
+    high-order subcell fluxes as weighted split-form pairs), against the oracle's dual numbers."""
+    disc, Q = _hybrid_disc(dim, n, op, walls, seed=dim + n)
+    rng = np.random.default_rng(90 + dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _hybrid_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op", ["hybrid_hllc", "hybrid_md"])
+def test_hybrid_rhs_vjp_columns(op):
+    disc, Q = _hybrid_disc(2, 4, op, False, seed=7)
+    rng = np.random.default_rng(27)
+    c, _ = _hybrid_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 2
+    e = 4
+    for v in range(Q.shape[1]):
+        for i in range(e * npe, (e + 1) * npe):
+            dQ = np.zeros_like(Q)
+            dQ[i, v] = 1.0
+            _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+            col = np.sum(lam * dR)
+            assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+@pytest.mark.parametrize("op", ["hybrid_hllc", "hybrid_kg"])
+def test_hybrid_adjoint_solve_against_dual_numbers(op):
+    eq = F.EulerEquation(3, 1.4)
+    disc = build(3, 4, (2, 3, 2), eq, HYBRID_OPS[op](), box=((0.0,) * 3, (2 * np.pi,) * 3))
+    Q0 = _tgv_state(disc, 0.3, 6)
+    rng = np.random.default_rng(47)
+    c, noc = _hybrid_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 11)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 6
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 2, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if noc else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if noc else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
+def test_hybrid_adjoint_limits():
+    """Not covered: the hybrid operator on Gauss nodes and on general geometry."""
+    from flou_cuda import _lib as L
+    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), HYBRID_OPS["hybrid_hllc"](), basis="GL")
+    Q = _dev(smooth_euler_state(disc, seed=1))
+    g = torch.empty_like(Q)
+    with pytest.raises(F.FlouError) as ei:
+        disc.ctx.rhs_vjp(g, None, Q, Q)
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+    from test_gpu_unstructured import _disc as _udisc
+    from test_unstructured import _state
+    u = _udisc(2, 4, "hybrid_hllc")
+    Q = _dev(_state(u, seed=2))
+    g = torch.empty_like(Q)
+    with pytest.raises(F.FlouError) as ei:
+        u.ctx.rhs_vjp(g, None, Q, Q)
+    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+
+
 @pytest.mark.parametrize("solver", ["ORK256", "CarpenterKennedy2N54"])
 @pytest.mark.parametrize("op,dim", [("strong", 2), ("split_hllc", 2), ("split", 3), ("split_kg", 3)])
 def test_lowstorage_adjoint_solve_against_dual_numbers(solver, op, dim):
