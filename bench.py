@@ -639,6 +639,71 @@ def bench_operators(nel=16, n=8):
     return out
 
 
+def bench_adjoint_operators(nel=12, n=6, nsteps=10):
+    """Adjoint/forward time of the operator variants the adjoint differentiates, on one 3D
+    Taylor-Green mesh of nel³ hexahedra at p = n-1 (Mach 0.1, periodic; the general-geometry
+    case: a perturbed box of rotated hexahedra with outflow boundaries): `nsteps` steps forward
+    (flou_step) against the adjoint solve with every state kept (nsnap = nsteps - 1, so the
+    ratio is the cost of the stage recomputation and the adjoint stages, not of the schedule)."""
+    import torch
+    import flou_cuda as F
+    eq = F.EulerEquation(3, 1.4)
+    md = F.MatrixDissipation(F.ChandrasekharAverage(), 1.0)
+    cases = [
+        ("split_hllc_GLL", "GLL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), False, None),
+        ("split_hllc_GL", "GL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), False, None),
+        ("strong_hllc_GL", "GL", lambda: F.StrongDivOperator(F.HLLC()), False, None),
+        ("hybrid_md_GLL", "GLL", lambda: F.HybridDivOperator(md, 1.0), False, None),
+        ("split_hllc_general", "GLL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), True, None),
+        ("split_hllc_GLL_ORK256", "GLL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), False,
+         F.ORK256()),
+    ]
+    out = {}
+    for name, basis, op, general, lsrk in cases:
+        b = F.LagrangeBasis(basis, n)
+        std = F.StdHex(b, F.DGSEMrec(b), 5)
+        if general:
+            mesh = F.perturbed_box(3, nel, (0.0,) * 3, (2 * math.pi,) * 3, amp=0.1, seed=3)
+            disc = F.MultielementDisc(mesh, std, eq, op(), {str(k): F.EulerOutflowBC() for k in range(1, 7)})
+        else:
+            mesh = F.CartesianMesh((0.0,) * 3, (2 * math.pi,) * 3, (nel,) * 3)
+            F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
+            disc = F.MultielementDisc(mesh, std, eq, op(), {})
+        q0 = torch.from_numpy(np.ascontiguousarray(F.initial.taylor_green(eq, disc.coords, mach=0.1).T)).cuda()
+        if lsrk is not None:
+            disc.ctx.set_integrator(lsrk.A, lsrk.B)
+        dt = TGV_CFL * disc.ctx.max_dt(q0, 1.0)
+        rho_t = (q0[0] * 1.01).contiguous()
+        w = torch.from_numpy(np.tile(disc.std.omega, disc.mesh.nelements) * disc.J).cuda()
+        g = torch.empty_like(q0)
+
+        def forward():
+            q = q0.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            disc.ctx.step(q, dt, nsteps)
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t0) * 1e3
+
+        def adjoint():
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            disc.ctx.adjoint_solve(q0, dt, nsteps, nsteps - 1, rho_t, w, g)
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t0) * 1e3
+
+        forward(), adjoint()   # warm-up (graph capture, allocations)
+        fms = min(forward() for _ in range(3))
+        ams = min(adjoint() for _ in range(3))
+        out[name] = {"forward_ms": fms, "adjoint_ms": ams, "ratio": ams / fms, "ndofs": disc.ndofs}
+        if lsrk is not None:
+            disc.ctx.set_integrator(None)
+        del disc, q0, g
+    out["workload"] = ("3D TGV M0.1, %d^3 hexahedra at p=%d (general: perturbed rotated hexahedra, outflow), "
+                       "split Chandrashekar + HLLC unless named, %d steps, every state kept" % (nel, n - 1, nsteps))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -809,6 +874,11 @@ def main():
             operators = bench_operators()
         except Exception as exc:   # reported, not fatal to the bench line
             operators = {"error": str(exc)}
+        if not args.no_adjoint:
+            try:
+                operators["adjoint"] = bench_adjoint_operators()
+            except Exception as exc:   # reported, not fatal to the bench line
+                operators["adjoint"] = {"error": str(exc)}
 
     # ---- cost of the Zhang-Shu stage limiter (minval 1e-10, as examples/src/3D_Euler.jl:76) ----
     limiter = None
