@@ -66,8 +66,8 @@ int flux_kind(int nf, int avg) {
 }
 int fv_kind(const flou_ctx* c) { return flux_kind(c->fvflux, c->fvavg); }
 
-// ssp_only: the batched adjoint, whose lockstep sweep steps with SSP-RK3 only.
-int adj_supported(flou_ctx* c, bool ssp_only = false) {
+// batched: the batched adjoint, whose lockstep sweep steps with SSP-RK3 and no limiter.
+int adj_supported(flou_ctx* c, bool batched = false) {
     const flou_config& k = c->cfg;
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                ((k.volume_op == FLOU_OP_SPLIT || k.volume_op == FLOU_OP_HYBRID) &&
@@ -103,9 +103,10 @@ int adj_supported(flou_ctx* c, bool ssp_only = false) {
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid adjoint tile of the Kennedy-Gruber flux at 3D p=7 "
                                                      "exceeds shared memory");
     }
-    if (c->limiter)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint does not differentiate the limiter (flou_set_limiter 0)");
-    if (ssp_only && c->lsrk_s)
+    if (batched && c->limiter)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint does not differentiate the limiter "
+                                                 "(flou_set_limiter 0)");
+    if (batched && c->lsrk_s)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint steps with SSP-RK3 (flou_set_integrator 0)");
     return FLOU_OK;
 }
@@ -300,6 +301,9 @@ struct Solver {
     // stage states of a reverse step: SSP-RK3 U^(k,1), U^(k,2); a 2N-storage method u_1 .. u_(s-1)
     std::vector<double*> SX[NB];
     int lsrk = 0;                     // stages of the 2N-storage method (0: SSP-RK3)
+    // the Zhang-Shu stage limiter: the stage states come in pairs, before (V) and after (U) the
+    // limiter: SSP-RK3 {U1, U2, V1, V2, V3}; 2N-storage {u_1 .. u_(s-1), v_1 .. v_s}
+    bool lim = false;
     double* Kss = nullptr;            // the stage stream's 2N register
     cudaEvent_t ready[NB] = {}, sready[NB] = {}, done[NB] = {};
     bool used[NB] = {};
@@ -339,20 +343,31 @@ struct Solver {
     int lsrk_stage(cudaStream_t s, const double* u, double* K, double* out, int st, double* Fn) {
         return ctx_stage(c, s, u, K, out, 3, dt, st == 0 ? 0.0 : c->lsrk_A[st], c->lsrk_B[st], Fn);
     }
+    int limit(cudaStream_t s, double* Q) { return lim ? ctx_limit(c, s, Q) : FLOU_OK; }
     int advance(int f, double* Q, int k) {   // k steps in place on forward stream f
         for (int i = 0; i < k; ++i) {
             int r;
             if (lsrk) {   // F1[f] is the stream's 2N register
-                for (int st = 0; st < lsrk; ++st)
+                for (int st = 0; st < lsrk; ++st) {
                     if ((r = lsrk_stage(sf[f], Q, F1[f], Q, st, Fnf[f]))) return r;
+                    if ((r = limit(sf[f], Q))) return r;
+                }
             } else {
                 if ((r = ctx_stage(c, sf[f], Q, Q, F1[f], 1, dt, 0.0, 1.0, Fnf[f]))) return r;
+                if ((r = limit(sf[f], F1[f]))) return r;
                 if ((r = ctx_stage(c, sf[f], F1[f], Q, F1[f], 2, dt, 0.75, 0.25, Fnf[f]))) return r;
+                if ((r = limit(sf[f], F1[f]))) return r;
                 if ((r = ctx_stage(c, sf[f], F1[f], Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf[f]))) return r;
+                if ((r = limit(sf[f], Q))) return r;
             }
             ++advances;
         }
         return FLOU_OK;
+    }
+    // dst <- the limited copy of src on stream s
+    int limited_copy(cudaStream_t s, double* dst, const double* src) {
+        int r = cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s), "stage copy");
+        return r ? r : limit(s, dst);
     }
     // slot sj <- U^(i0+m) advanced from slot si (a snapshot placement)
     int place(int sj, int si, int m) {
@@ -379,7 +394,19 @@ struct Solver {
         // the stage stream: U^(k,1) and U^(k,2), or u_1 .. u_(s-1) (ready[b] comes after the forward
         // stream's wait for done[b], so the stage buffers are free again)
         if ((r = wait(ss, ready[b]))) return r;
-        if (lsrk) {
+        const bool seed = kstep == nsteps - 1 && !seeded;
+        if (lsrk && lim) {   // v_(i+1) from u_i, u_(i+1) its limited copy
+            const double* u = X[b];
+            for (int st = 0; st < lsrk; ++st) {
+                double* v = SX[b][lsrk - 1 + st];
+                if ((r = lsrk_stage(ss, u, Kss, v, st, Fns))) return r;
+                if (st + 1 < lsrk && (r = limited_copy(ss, SX[b][st], v))) return r;
+                u = SX[b][st];
+            }
+            // the last step: U^n = L(v_s), which the functional reads (the adjoint stream has not
+            // used T yet)
+            if (seed && (r = limited_copy(ss, T, SX[b][2 * lsrk - 2]))) return r;
+        } else if (lsrk) {
             const double* u = X[b];
             for (int st = 0; st + 1 < lsrk; ++st) {
                 if ((r = lsrk_stage(ss, u, Kss, SX[b][st], st, Fns))) return r;
@@ -387,24 +414,36 @@ struct Solver {
             }
             // the last step: U^n, which the functional reads, from the same register (the adjoint
             // stream has not used T yet)
-            if (kstep == nsteps - 1 && !seeded && (r = lsrk_stage(ss, u, Kss, T, lsrk - 1, Fns))) return r;
+            if (seed && (r = lsrk_stage(ss, u, Kss, T, lsrk - 1, Fns))) return r;
+        } else if (lim) {   // V1, U1 = L(V1), V2, U2 = L(V2), V3
+            if ((r = ctx_stage(c, ss, X[b], X[b], SX[b][2], 1, dt, 0.0, 1.0, Fns))) return r;
+            if ((r = limited_copy(ss, SX[b][0], SX[b][2]))) return r;
+            if ((r = ctx_stage(c, ss, SX[b][0], X[b], SX[b][3], 2, dt, 0.75, 0.25, Fns))) return r;
+            if ((r = limited_copy(ss, SX[b][1], SX[b][3]))) return r;
+            if ((r = ctx_stage(c, ss, SX[b][1], X[b], SX[b][4], 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fns))) return r;
         } else {
             if ((r = ctx_stage(c, ss, X[b], X[b], SX[b][0], 1, dt, 0.0, 1.0, Fns))) return r;
             if ((r = ctx_stage(c, ss, SX[b][0], X[b], SX[b][1], 2, dt, 0.75, 0.25, Fns))) return r;
         }
         if ((r = record(sready[b], ss))) return r;
         if ((r = wait(sa, sready[b]))) return r;
-        if ((r = (lsrk ? backward_step_2n(kstep, b) : backward_step(kstep, X[b], SX[b][0], SX[b][1])))) return r;
+        if ((r = (lsrk ? backward_step_2n(kstep, b) : backward_step(kstep, b)))) return r;
         used[b] = true;
         return record(done[b], sa);
     }
-    // Reverse one step from U^k (Xk) and its stage states (S1, S2): the adjoint of U^(k+1) is in
-    // A on entry and that of U^k on exit (adjoint stream).
-    int backward_step(int k, double* Xk, double* S1, double* S2) {
+    // Reverse one step from U^k (X[b]) and its stage states: the adjoint of U^(k+1) is in A on
+    // entry and that of U^k on exit (adjoint stream).  With the limiter, each stage's adjoint first
+    // goes through the limiter's VJP at that stage's state before the limiter.
+    int backward_step(int k, int b) {
         int r;
+        double *Xk = X[b], *S1 = SX[b][0], *S2 = SX[b][1];
         if (!seeded) {   // the last step: form U^n, the functional and its gradient seed
             if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
-            if ((r = ctx_stage(c, sa, S2, Xk, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) return r;   // U^n
+            if (lim) {
+                if ((r = limited_copy(sa, T, SX[b][4]))) return r;   // U^n = L(V3)
+            } else if ((r = ctx_stage(c, sa, S2, Xk, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) {
+                return r;   // U^n
+            }
             functional_kernel<<<nblk, 256, 0, sa>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
             if ((r = cuda(cudaGetLastError(), "functional"))) return r;
             if ((r = cuda(cudaMemcpyAsync(h_partial, partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, sa),
@@ -412,9 +451,12 @@ struct Solver {
                 return r;
             seeded = true;
         }
+        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][4], A, nullptr, 0.0, 0.0))) return r;
         if ((r = adj_stage(c, ab, sa, S2, A, T, Bacc, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
             return r;
+        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][3], T, nullptr, 0.0, 0.0))) return r;
         if ((r = adj_stage(c, ab, sa, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
+        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][2], A, nullptr, 0.0, 0.0))) return r;
         if ((r = adj_stage(c, ab, sa, Xk, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
         return FLOU_OK;
     }
@@ -422,7 +464,9 @@ struct Solver {
     // dt L(u_i), u_(i+1) = u_i + B_i k_i, A_0 = 0).  Reverse stage i with k̄ = k̄_i + B_i Ū(i+1) in T:
     //   Ū_i = Ū_(i+1) + dt (∂L/∂u)(u_i)ᵀ k̄,  then T = A_i k̄ + B_(i-1) Ū_i for stage i-1
     // (the element kernel's epilogue forms the next k̄ in place).  The last stage starts from
-    // k̄ = B_(s-1) Ū; A_0 = 0 leaves nothing to carry into the previous step.
+    // k̄ = B_(s-1) Ū; A_0 = 0 leaves nothing to carry into the previous step.  With the limiter
+    // (u_(i+1) = L(v_(i+1))), Ū_(i+1) first becomes V̄_(i+1) through the limiter's VJP, which also
+    // adds B_i V̄_(i+1) to the register (the epilogue then carries A_i k̄ alone).
     int backward_step_2n(int k, int b) {
         int r;
         if (!seeded) {   // U^n was formed in T by the stage stream
@@ -434,13 +478,19 @@ struct Solver {
                 return r;
             seeded = true;
         }
-        const int64_t n = c->ndofs * c->nv;
-        scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, sa>>>(T, A, c->lsrk_B[lsrk - 1], n);
-        if ((r = cuda(cudaGetLastError(), "adjoint register"))) return r;
+        if (lim) {
+            if ((r = ctx_limit_vjp(c, sa, SX[b][2 * lsrk - 2], A, T, 0.0, c->lsrk_B[lsrk - 1]))) return r;
+        } else {
+            const int64_t n = c->ndofs * c->nv;
+            scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, sa>>>(T, A, c->lsrk_B[lsrk - 1], n);
+            if ((r = cuda(cudaGetLastError(), "adjoint register"))) return r;
+        }
         for (int i = lsrk - 1; i >= 0; --i) {
             const double* u = i == 0 ? X[b] : SX[b][i - 1];
             if ((r = adj_stage(c, ab, sa, u, T, A, A, cbar, dt, 0.0, 1.0, 1, 0, 0.0, 0.0, i > 0 ? T : nullptr,
-                               c->lsrk_A[i], i > 0 ? c->lsrk_B[i - 1] : 0.0)))
+                               c->lsrk_A[i], (i > 0 && !lim) ? c->lsrk_B[i - 1] : 0.0)))
+                return r;
+            if (lim && i > 0 && (r = ctx_limit_vjp(c, sa, SX[b][lsrk - 2 + i], A, T, 1.0, c->lsrk_B[i - 1])))
                 return r;
         }
         return FLOU_OK;
@@ -650,7 +700,8 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     S.slot.assign(nslots + 1, nullptr);
     for (int i = 0; i <= nslots; ++i) dalloc(&S.slot[i], S.bytes);
     S.lsrk = c->lsrk_s;
-    const int nst = S.lsrk ? S.lsrk - 1 : 2;
+    S.lim = c->limiter == FLOU_LIMITER_ZHANG_SHU;
+    const int nst = S.lsrk ? (S.lim ? 2 * S.lsrk - 1 : S.lsrk - 1) : (S.lim ? 5 : 2);
     for (int i = 0; i < Solver::NB; ++i) {
         dalloc(&S.X[i], S.bytes);
         S.SX[i].assign(nst, nullptr);

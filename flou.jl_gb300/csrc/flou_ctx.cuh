@@ -107,6 +107,9 @@ int ctx_stage(flou_ctx* c, cudaStream_t s, const double* Q, const double* Q0, do
 int ctx_check_status(flou_ctx* c);
 // limiter.cu: the stage limiter on Q (no-op when off) and the per-step monitor record
 int ctx_limit(flou_ctx* c, cudaStream_t s, double* Q);
+// The limiter's VJP at the pre-limiter state V: A (cotangent of the limited state) becomes that of
+// V; with K set, K = kK K + kb A afterwards.
+int ctx_limit_vjp(flou_ctx* c, cudaStream_t s, const double* V, double* A, double* K, double kK, double kb);
 int ctx_record_monitors(flou_ctx* c, cudaStream_t s, const double* Q);
 void ctx_free_limiter(flou_ctx* c);
 void drop_step_graph(flou_ctx* c);   // settings that change the captured step

@@ -141,6 +141,211 @@ __global__ void __launch_bounds__(256) zhang_shu_kernel(LimParams P) {
 
 // Partial sums over blocks of nodes of Jω f(Q): [0] kinetic energy |ρv|²/(2ρ) (FlouCommon/Euler.jl:162-175),
 // [1] mathematical entropy -ρ s/(γ-1), s = log p - γ log ρ (FlouCommon/Euler.jl:202-217).
+// The limiter's VJP (reverse mode through zhang_shu_kernel, for the discrete adjoint of a limited
+// time step), one warp per element.  V is the state before the limiter; A holds the cotangent of
+// the limited state on entry and that of V on exit.  The forward quantities are recomputed from V:
+// the mean Q̄, the first minimal density node, θ₁ = |N₁/D₁| (N₁ = ρ̄ - min(minval, ρ̄), D₁ = ρ̄ -
+// ρ_min), the pressures of the density-limited nodes, their mean and first minimal node, θ₂.  In
+// reverse: Q'' = Q̄ + θ₂ (Q' - Q̄) gives Q̄' = θ₂ Ā, Q̄̄ += (1-θ₂) Σ Ā and θ̄₂ = Σ Ā·(Q' - Q̄); θ₂'s
+// derivative (sign-bit convention for |·|) reaches p̄ and p_min when m = minval (when m = p̄ the
+// numerator is identically zero); the pressures take their cotangents to (ρ', m, E); the density
+// step is reversed the same way, and the mean's cotangent spreads back with Jω/vol.  Elements the
+// limiter leaves alone (the forward's fast exit, or neither θ ≤ 1) pass A through.  With K set,
+// K = kK K + kb A after A is formed (the 2N-storage register of the reverse sweep), every node.
+struct LimVjpParams {
+    const double* V;
+    double* A;
+    double* K;
+    double kK, kb;
+    const double* J;
+    const double* Jn;
+    const double* w;
+    int64_t ndofs;
+    int nelem, npe;
+    double minval, gamma;
+};
+
+__device__ __forceinline__ void warp_argmin(double& v, int& idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ov < v || (ov == v && oi < idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) zhang_shu_vjp_kernel(LimVjpParams P) {
+    constexpr int NV = DIM + 2;
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
+    const double g1 = P.gamma - 1.0;
+    auto sgn = [](double x) { return signbit(x) ? -1.0 : 1.0; };
+    for (int e = warp; e < P.nelem; e += nwarps) {
+        const double Je = P.J[e];
+        const int64_t b = (int64_t)e * P.npe;
+        bool clear = true;   // the forward's fast exit, on the same state
+        for (int i = lane; i < P.npe; i += 32) {
+            double r = P.V[b + i];
+            double ke = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                double mk = P.V[(1 + k) * P.ndofs + b + i];
+                ke = fma(mk, mk, ke);
+            }
+            double E = P.V[(DIM + 1) * P.ndofs + b + i];
+            double lhs = 2.0 * r * fma(g1, E, -P.minval), rhs = g1 * ke;
+            double tol = 1e-12 * (fabs(2.0 * r * g1 * E) + fabs(2.0 * r * P.minval) + rhs);
+            clear = clear && r > 0.0 && (r - P.minval > 1e-12 * fabs(P.minval) + 1e-300) && (lhs - rhs > tol);
+        }
+        bool pass = __all_sync(0xffffffffu, clear);
+        double S[NV], vol = 0.0, rmin = INFINITY, Qm[NV];
+        int i1 = P.npe, j2 = P.npe;
+        double th1 = 2.0, th2 = 2.0, r1 = 0.0, r2 = 0.0, N1 = 0.0, D1 = 1.0, N2 = 0.0, D2 = 1.0;
+        bool l1 = false, l2 = false, mmean1 = false, mmean2 = false;
+        if (!pass) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) S[k] = 0.0;
+            for (int i = lane; i < P.npe; i += 32) {
+                double jw = (P.Jn ? P.Jn[b + i] : Je) * P.w[i];
+                vol += jw;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) S[k] = fma(jw, P.V[k * P.ndofs + b + i], S[k]);
+                if (P.V[b + i] < rmin) {
+                    rmin = P.V[b + i];
+                    i1 = i;
+                }
+            }
+            vol = warp_sum(vol);
+            warp_argmin(rmin, i1);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) Qm[k] = warp_sum(S[k]) / vol;
+            const double m = fmin(P.minval, Qm[0]);
+            mmean1 = Qm[0] < P.minval;
+            N1 = Qm[0] - m;
+            D1 = Qm[0] - rmin;
+            r1 = N1 / D1;
+            th1 = fabs(r1);
+            l1 = th1 <= 1.0;
+            double ps = 0.0, pmin = INFINITY;
+            for (int i = lane; i < P.npe; i += 32) {
+                double r = P.V[b + i];
+                if (l1) r = th1 * (r - Qm[0]) + Qm[0];
+                double p = node_pressure<DIM>(r, P.V, P.ndofs, b + i, g1);
+                ps = fma((P.Jn ? P.Jn[b + i] : Je) * P.w[i], p, ps);
+                if (p < pmin) {
+                    pmin = p;
+                    j2 = i;
+                }
+            }
+            const double pbar = warp_sum(ps) / vol;
+            warp_argmin(pmin, j2);
+            const double m2 = fmin(P.minval, pbar);
+            mmean2 = pbar < P.minval;
+            N2 = pbar - m2;
+            D2 = pbar - pmin;
+            r2 = N2 / D2;
+            th2 = fabs(r2);
+            l2 = th2 <= 1.0;
+            pass = !l1 && !l2;
+        }
+        if (pass) {
+            if (P.K)
+                for (int i = lane; i < P.npe; i += 32)
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) {
+                        const int64_t o = k * P.ndofs + b + i;
+                        P.K[o] = fma(P.kK, P.K[o], P.kb * P.A[o]);
+                    }
+            continue;
+        }
+        // pressure step: the sums of Ā and Ā·(Q' - Q̄)
+        double sA[NV], t2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sA[k] = 0.0;
+        if (l2) {
+            for (int i = lane; i < P.npe; i += 32) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    double q = P.V[k * P.ndofs + b + i];
+                    if (k == 0 && l1) q = th1 * (q - Qm[0]) + Qm[0];
+                    const double a = P.A[k * P.ndofs + b + i];
+                    sA[k] += a;
+                    t2 = fma(a, q - Qm[k], t2);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sA[k] = warp_sum(sA[k]);
+            t2 = warp_sum(t2);
+        }
+        const double rb2 = l2 ? t2 * sgn(r2) : 0.0;
+        const double pbb = (l2 && !mmean2) ? rb2 * (1.0 / D2 - N2 / (D2 * D2)) : 0.0;
+        const double pmb = (l2 && !mmean2) ? rb2 * N2 / (D2 * D2) : 0.0;
+        double Qmb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Qmb[k] = l2 ? (1.0 - th2) * sA[k] : 0.0;
+        // Q̄' (with the pressures' cotangents), then the density step
+        double sR = 0.0, t1 = 0.0;
+        for (int i = lane; i < P.npe; i += 32) {
+            double qb[NV], q[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                q[k] = P.V[k * P.ndofs + b + i];
+                const double a = P.A[k * P.ndofs + b + i];
+                qb[k] = l2 ? th2 * a : a;
+            }
+            const double rho0 = q[0];
+            const double rp = l1 ? th1 * (q[0] - Qm[0]) + Qm[0] : q[0];
+            const double jw = (P.Jn ? P.Jn[b + i] : Je) * P.w[i];
+            const double pb = pbb * jw / vol + (i == j2 ? pmb : 0.0);
+            if (pb != 0.0) {   // p = (γ-1)(E - |m|²/(2ρ'))
+                double ke = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k], ke);
+                const double ir = 1.0 / rp;
+                qb[0] = fma(pb * g1 * 0.5 * ke, ir * ir, qb[0]);
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) qb[1 + k] = fma(-pb * g1 * ir, q[1 + k], qb[1 + k]);
+                qb[DIM + 1] = fma(pb, g1, qb[DIM + 1]);
+            }
+            if (l1) {
+                sR += qb[0];
+                t1 = fma(qb[0], rho0 - Qm[0], t1);
+                qb[0] *= th1;
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) P.A[k * P.ndofs + b + i] = qb[k];
+        }
+        double rminb = 0.0;
+        if (l1) {
+            sR = warp_sum(sR);
+            t1 = warp_sum(t1);
+            const double rb1 = t1 * sgn(r1);
+            Qmb[0] = fma(1.0 - th1, sR, Qmb[0]);
+            if (!mmean1) {
+                Qmb[0] = fma(rb1, 1.0 / D1 - N1 / (D1 * D1), Qmb[0]);
+                rminb = rb1 * N1 / (D1 * D1);
+            }
+        }
+        for (int i = lane; i < P.npe; i += 32) {   // the mean's cotangent, the minimal node's
+            const double sj = (P.Jn ? P.Jn[b + i] : Je) * P.w[i] / vol;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const int64_t o = k * P.ndofs + b + i;
+                double a = fma(Qmb[k], sj, P.A[o]);
+                if (k == 0 && i == i1) a += rminb;
+                P.A[o] = a;
+                if (P.K) P.K[o] = fma(P.kK, P.K[o], P.kb * a);
+            }
+        }
+    }
+}
+
+
 template <int DIM>
 __global__ void __launch_bounds__(256) monitor_partial_kernel(const double* Q, const double* J, const double* Jn,
                                                               const double* w, int64_t ndofs, int npe, double gamma,
@@ -324,6 +529,29 @@ int ctx_limit(flou_ctx* c, cudaStream_t s, double* Q) {
     else if (d == 2) zhang_shu_kernel<2><<<grid, 256, 0, s>>>(P);
     else zhang_shu_kernel<3><<<grid, 256, 0, s>>>(P);
     return lcuda(c, cudaGetLastError(), "limiter kernel");
+}
+
+int ctx_limit_vjp(flou_ctx* c, cudaStream_t s, const double* V, double* A, double* K, double kK, double kb) {
+    LimVjpParams P;
+    P.V = V;
+    P.A = A;
+    P.K = K;
+    P.kK = kK;
+    P.kb = kb;
+    P.J = c->d_Jel;
+    P.Jn = c->curv ? c->d_Jn : nullptr;
+    P.w = c->d_wtp;
+    P.ndofs = c->ndofs;
+    P.nelem = c->nelem;
+    P.npe = c->npe;
+    P.minval = c->lim_min;
+    P.gamma = c->cfg.gamma;
+    int grid = (c->nelem + 7) / 8;
+    int d = c->cfg.dim;
+    if (d == 1) zhang_shu_vjp_kernel<1><<<grid, 256, 0, s>>>(P);
+    else if (d == 2) zhang_shu_vjp_kernel<2><<<grid, 256, 0, s>>>(P);
+    else zhang_shu_vjp_kernel<3><<<grid, 256, 0, s>>>(P);
+    return lcuda(c, cudaGetLastError(), "limiter VJP kernel");
 }
 
 int ctx_record_monitors(flou_ctx* c, cudaStream_t s, const double* Q) {

@@ -1409,11 +1409,16 @@ template <class T> void ssprk3_step(const Disc& g, T* Q, double dt, double t, Wo
 // density-limited nodes gives p̄ = Σ Jω p / vol and θ = |(p̄ - m)/(p̄ - p_min)|, m = min(minval,
 // p̄), and when θ <= 1 every variable is scaled toward the mean Q̄ taken before the density
 // step.  `omega` holds the tensor-product quadrature weights per element node.
-inline void zhang_shu(const Disc& g, double* Q, double minval, const std::vector<double>& omega) {
+// T = Dual: forward-mode derivatives through the means, the minima (the first minimal node, as
+// Julia's min keeps), the absolute values and the θ <= 1 branches.
+template <class T>
+void zhang_shu(const Disc& g, T* Q, double minval, const std::vector<double>& omega) {
+    using std::min; using std::fabs;
     const Config& c = g.cfg;
     long nd = g.ndofs();
     int nv = c.nv, npe = g.npe;
-    std::vector<double> Jw(npe), p(npe);
+    std::vector<double> Jw(npe);
+    std::vector<T> p(npe);
     for (int e = 0; e < g.nelem; ++e) {
         long b = (long)e * npe;
         double vol = 0.0;
@@ -1421,27 +1426,27 @@ inline void zhang_shu(const Disc& g, double* Q, double minval, const std::vector
             Jw[i] = g.J[b + i] * omega[i];
             vol = vol + Jw[i];
         }
-        Vec<double> Qm{};
+        Vec<T> Qm{};
         for (int k = 0; k < nv; ++k) {
-            double acc = 0.0;
+            T acc = T(0.0);
             for (int i = 0; i < npe; ++i) acc = acc + Jw[i] * Q[k * nd + b + i];
             Qm[k] = acc / vol;
         }
-        double m = std::min(minval, Qm[0]);
-        double rmin = INFINITY;
-        for (int i = 0; i < npe; ++i) rmin = std::min(rmin, Q[b + i]);
-        double th = std::fabs((Qm[0] - m) / (Qm[0] - rmin));
+        T m = min(T(minval), Qm[0]);
+        T rmin = T(INFINITY);
+        for (int i = 0; i < npe; ++i) rmin = min(rmin, Q[b + i]);
+        T th = fabs((Qm[0] - m) / (Qm[0] - rmin));
         if (th <= 1.0)
             for (int i = 0; i < npe; ++i) Q[b + i] = th * (Q[b + i] - Qm[0]) + Qm[0];
-        double ps = 0.0, pmin = INFINITY;
+        T ps = T(0.0), pmin = T(INFINITY);
         for (int i = 0; i < npe; ++i) {
             p[i] = pressure(getv(Q, nd, b + i, nv), c.dim, c.gamma);
             ps = ps + Jw[i] * p[i];
-            pmin = std::min(pmin, p[i]);
+            pmin = min(pmin, p[i]);
         }
-        double pbar = ps / vol;
-        m = std::min(minval, pbar);
-        th = std::fabs((pbar - m) / (pbar - pmin));
+        T pbar = ps / vol;
+        m = min(T(minval), pbar);
+        th = fabs((pbar - m) / (pbar - pmin));
         if (th <= 1.0)
             for (int i = 0; i < npe; ++i)
                 for (int k = 0; k < nv; ++k) Q[k * nd + b + i] = th * (Q[k * nd + b + i] - Qm[k]) + Qm[k];
@@ -1479,19 +1484,20 @@ inline double monitor(const Disc& g, const double* Q, int which, const std::vect
 
 // SSP-RK3 with the limiter as OrdinaryDiffEq's stage_limiter! (FlouTime.jl:136-148): applied
 // to U1, U2 and the new state.
-inline void ssprk3_step_limited(const Disc& g, double* Q, double dt, double t, Workspace<double>& ws,
-                                std::vector<double>& U, std::vector<double>& L, double minval,
-                                const std::vector<double>& omega) {
+template <class T>
+void ssprk3_step_limited(const Disc& g, T* Q, double dt, double t, Workspace<T>& ws, std::vector<T>& U,
+                         std::vector<T>& L, double minval, const std::vector<double>& omega,
+                         const T* celem = nullptr) {
     long N = g.ndofs() * g.cfg.nv;
     U.resize(N);
     L.resize(N);
-    rhs(g, L.data(), Q, t, ws);
+    rhs(g, L.data(), Q, t, ws, celem);
     for (long i = 0; i < N; ++i) U[i] = Q[i] + dt * L[i];
     zhang_shu(g, U.data(), minval, omega);
-    rhs(g, L.data(), U.data(), t + dt, ws);
+    rhs(g, L.data(), U.data(), t + dt, ws, celem);
     for (long i = 0; i < N; ++i) U[i] = 0.75 * Q[i] + 0.25 * (U[i] + dt * L[i]);
     zhang_shu(g, U.data(), minval, omega);
-    rhs(g, L.data(), U.data(), t + 0.5 * dt, ws);
+    rhs(g, L.data(), U.data(), t + 0.5 * dt, ws, celem);
     for (long i = 0; i < N; ++i) Q[i] = (1.0 / 3.0) * Q[i] + (2.0 / 3.0) * (U[i] + dt * L[i]);
     zhang_shu(g, Q, minval, omega);
 }
@@ -1501,8 +1507,7 @@ inline void ssprk3_step_limited(const Disc& g, double* Q, double dt, double t, W
 // tests and examples step with (test/tests.jl:19,56,93,139; examples/src/3D_Euler.jl:77):
 //   k = dt L(u); u = u + B_1 k;   for i = 2..s: k = A_i k + dt L(u, t + c_i dt); u = u + B_i k.
 // The stage limiter, when `omega` is given, acts on u after every stage.
-// T = Dual (forward-mode derivatives, with the per-element dissipation scales celem) takes no
-// limiter.
+// T = Dual: forward-mode derivatives, with the per-element dissipation scales celem.
 template <class T>
 void lsrk2n_step(const Disc& g, T* Q, double dt, double t, Workspace<T>& ws, std::vector<T>& K, std::vector<T>& L,
                  int s, const double* A, const double* B, const double* c, double minval = 0.0,
@@ -1521,9 +1526,7 @@ void lsrk2n_step(const Disc& g, T* Q, double dt, double t, Workspace<T>& ws, std
         }
 #pragma omp parallel for schedule(static)
         for (long i = 0; i < N; ++i) Q[i] = Q[i] + B[st] * K[i];
-        if constexpr (std::is_same_v<T, double>) {
-            if (omega) zhang_shu(g, Q, minval, *omega);
-        }
+        if (omega) zhang_shu(g, Q, minval, *omega);
     }
 }
 

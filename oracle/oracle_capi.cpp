@@ -439,10 +439,12 @@ void oracle_solve_jvp(void* hp, const double* Q0, const double* dQ0, const doubl
     *dJ = acc.d;
 }
 
-// The same for nsteps steps of a 2N-storage method (nstages, A, B, c as oracle_lsrk2n).
+// The same for nsteps steps of a 2N-storage method (nstages, A, B, c as oracle_lsrk2n; nstages = 0:
+// SSP-RK3), with the Zhang-Shu stage limiter when omega_tp is given.
 void oracle_solve_jvp_lsrk(void* hp, const double* Q0, const double* dQ0, const double* c, const double* dc,
                            double dt, int nsteps, const double* rho_t, const double* w, int nstages, const double* A,
-                           const double* B, const double* cst, double* J, double* dJ) {
+                           const double* B, const double* cst, double* J, double* dJ, double minval = 0.0,
+                           const double* omega_tp = nullptr) {
     Handle* h = (Handle*)hp;
     long nd = h->g.ndofs(), N = nd * h->g.cfg.nv;
     std::vector<Dual> q(N), ce, K, L;
@@ -452,8 +454,17 @@ void oracle_solve_jvp_lsrk(void* hp, const double* Q0, const double* dQ0, const 
         for (int e = 0; e < h->g.nelem; ++e) ce[e] = Dual(c[e], dc ? dc[e] : 0.0);
     }
     Workspace<Dual> ws;
-    for (int s = 0; s < nsteps; ++s)
-        lsrk2n_step(h->g, q.data(), dt, s * dt, ws, K, L, nstages, A, B, cst, 0.0, nullptr, c ? ce.data() : nullptr);
+    std::vector<double> om;
+    if (omega_tp) om.assign(omega_tp, omega_tp + h->g.npe);
+    for (int s = 0; s < nsteps; ++s) {
+        if (nstages == 0 && omega_tp)
+            ssprk3_step_limited(h->g, q.data(), dt, s * dt, ws, K, L, minval, om, c ? ce.data() : nullptr);
+        else if (nstages == 0)
+            ssprk3_step(h->g, q.data(), dt, s * dt, ws, K, L, c ? ce.data() : nullptr);
+        else
+            lsrk2n_step(h->g, q.data(), dt, s * dt, ws, K, L, nstages, A, B, cst, minval, omega_tp ? &om : nullptr,
+                        c ? ce.data() : nullptr);
+    }
     Dual acc(0.0);
     for (long i = 0; i < nd; ++i) {
         Dual r = q[i] - rho_t[i];

@@ -53,7 +53,7 @@ def lib():
         _lib.oracle_rhs_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, D, D]
         _lib.oracle_solve_jvp.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D, D, D]
         _lib.oracle_solve_jvp_lsrk.argtypes = [ctypes.c_void_p, D, D, D, D, ctypes.c_double, ctypes.c_int, D, D,
-                                               ctypes.c_int, D, D, D, D, D]
+                                               ctypes.c_int, D, D, D, D, D, ctypes.c_double, D]
     return _lib
 
 
@@ -218,17 +218,20 @@ class Disc:
                                 p(args[3]), ctypes.byref(J), ctypes.byref(dJ))
         return J.value, dJ.value
 
-    def solve_jvp_lsrk(self, Q0, dQ0, c, dc, dt, nsteps, rho_t, w, A, B, cst):
-        """solve_jvp for nsteps steps of the 2N-storage method (A, B, c)."""
+    def solve_jvp_lsrk(self, Q0, dQ0, c, dc, dt, nsteps, rho_t, w, A=None, B=None, cst=None, minval=None,
+                       omega_tp=None):
+        """solve_jvp for nsteps steps of the 2N-storage method (A, B, c), or of SSP-RK3 when A is
+        None; with the Zhang-Shu stage limiter when minval is given."""
         Q0 = np.asfortranarray(Q0, dtype=np.float64)
         dQ0 = np.asfortranarray(dQ0, dtype=np.float64)
         J, dJ = ctypes.c_double(), ctypes.c_double()
         args = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
-                for x in (c, dc, rho_t, w, A, B, cst)]
+                for x in (c, dc, rho_t, w, A, B, cst, omega_tp if minval is not None else None)]
         p = lambda a: _d(a) if a is not None else None
         self.L.oracle_solve_jvp_lsrk(self.h, _d(Q0), _d(dQ0), p(args[0]), p(args[1]), dt, nsteps, p(args[2]),
-                                     p(args[3]), len(args[5]), p(args[4]), p(args[5]), p(args[6]),
-                                     ctypes.byref(J), ctypes.byref(dJ))
+                                     p(args[3]), 0 if A is None else len(args[5]), p(args[4]), p(args[5]),
+                                     p(args[6]), ctypes.byref(J), ctypes.byref(dJ),
+                                     0.0 if minval is None else float(minval), p(args[7]))
         return J.value, dJ.value
 
     def count(self, Q, t=0.0):

@@ -740,6 +740,87 @@ def test_hybrid_adjoint_limits():
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("integrator", ["SSPRK3", "ORK256"])
+@pytest.mark.parametrize("op,dim", [("strong", 2), ("split", 2), ("split_hllc", 3), ("strong", 1)])
+def test_limited_adjoint_solve_against_dual_numbers(integrator, op, dim):
+    """The Zhang-Shu stage limiter (after every stage, as Flou's stage_limiter!) differentiated:
+    a state with a density dip and a pressure dip and minval = 0.5 keep two elements limited
+    through the solve; against the oracle's dual numbers through the same limited method."""
+    from flou_cuda import _lib as L
+    from test_oracle_kat import _dipped_state
+    eq = F.EulerEquation(dim, 1.4)
+    disc = build(dim, 4, (3,) * dim, eq, OPERATORS[op]())
+    Q0 = _dipped_state(disc, seed=10 + dim)
+    minval = 0.5
+    disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, minval)
+    m = None if integrator == "SSPRK3" else F.ORK256()
+    if m is not None:
+        disc.ctx.set_integrator(m.A, m.B)
+    rng = np.random.default_rng(71)
+    hll = op in HLL_FAMILY
+    c = _with_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 4)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 6
+    o = oracle_for(disc)
+    args = () if m is None else (m.A, m.B, m.c)
+    # the limiter acts along this trajectory
+    J0, _ = o.solve_jvp_lsrk(Q0, 0 * Q0, c, 0 * c, dt, nsteps, rho_t, w, *args)
+    J1, _ = o.solve_jvp_lsrk(Q0, 0 * Q0, c, 0 * c, dt, nsteps, rho_t, w, *args, minval=minval,
+                             omega_tp=disc.std.omega)
+    assert not np.isfinite(J0) or abs(J1 - J0) > 1e-6 * abs(J0)   # (unlimited, some runs break down)
+    for nsnap in (2, nsteps - 1):
+        g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+        gc = None if hll else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+        J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, nsnap, _dev(rho_t), _dev(w), g, gc)
+        assert abs(J - J1) <= 1e-12 * abs(J1)
+        for k in range(2):
+            dQ = rng.standard_normal(Q0.shape)
+            dc = rng.standard_normal(c.shape) * (0.0 if hll else 1.0)
+            Jo, dJo = o.solve_jvp_lsrk(Q0, dQ, c, dc, dt, nsteps, rho_t, w, *args, minval=minval,
+                                       omega_tp=disc.std.omega)
+            ours = np.sum(_host(g) * dQ) + (0.0 if hll else np.sum(gc.cpu().numpy() * dc))
+            assert abs(ours - dJo) <= 1e-10 * abs(dJo), (nsnap, ours, dJo)
+    disc.ctx.set_limiter(L.LIMITER_NONE)
+    if m is not None:
+        disc.ctx.set_integrator(None)
+
+
+def test_limited_adjoint_against_central_differences():
+    from flou_cuda import _lib as L
+    from test_oracle_kat import _dipped_state
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 5, (4, 4), eq, _lxf())
+    Q0 = _dipped_state(disc, seed=21)
+    disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.5)
+    rng = np.random.default_rng(81)
+    c = 1.0 + 0.1 * rng.random(disc.mesh.nelements)
+    disc.ctx.set_dissipation(c)
+    rho_t, w = _functional_inputs(disc, 8)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 8
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    wd, rtd = _dev(w), _dev(rho_t)
+
+    def Jof(Q, cc):
+        disc.ctx.set_dissipation(cc)
+        q = _dev(Q)
+        disc.ctx.step(q, dt, nsteps)
+        r = q[0] - rtd
+        return float(0.5 * torch.sum(wd * r * r))
+
+    h = 1e-6
+    for k in range(3):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * 0.1
+        fd = (Jof(Q0 + h * dQ, c + h * dc) - Jof(Q0 - h * dQ, c - h * dc)) / (2 * h)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
+    disc.ctx.set_limiter(L.LIMITER_NONE)
+
+
 @pytest.mark.parametrize("solver", ["ORK256", "CarpenterKennedy2N54"])
 @pytest.mark.parametrize("op,dim", [("strong", 2), ("split_hllc", 2), ("split", 3), ("split_kg", 3)])
 def test_lowstorage_adjoint_solve_against_dual_numbers(solver, op, dim):
