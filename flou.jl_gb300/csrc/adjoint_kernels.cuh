@@ -1242,8 +1242,9 @@ struct AdjSplitShape {
         sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD + NGX) +
         2 * (S::NPAIR + 1);
     // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
-    // (G: one, for the projection's registers)
-    static constexpr int MINB = (!G && !H && S::BLOCK * 2 * 128 <= 65536) ? 2 : 1;
+    // (G, H: two where that still leaves 144 registers, else one, for the projection's registers)
+    static constexpr int MINB = (!G && !H) ? ((S::BLOCK * 2 * 128 <= 65536) ? 2 : 1)
+                                           : ((S::BLOCK * 2 * 144 <= 65536) ? 2 : 1);
 };
 
 // Per-node quantities the split adjoint keeps for a state q (p its pressure): Chandrashekar
@@ -1407,13 +1408,17 @@ __device__ __forceinline__ void entropy_vjp(const double* q, double p, double g,
     qb[DIM + 1] += g1 * pb;
 }
 
-// G (Gauss nodes, Cartesian): the entropy-projected coupling of each line transposed, one thread
-// per line.  The forward adds to node i the flux differences
+// G (Gauss nodes, Cartesian): the entropy-projected coupling of each line transposed.  The forward
+// adds to node i the flux differences
 //   Ja (∂g_l[i] (F♯(Q_i, Q̃_l) - Σ_j l_j F♯(Q_j, Q̃_l)) - ∂g_r[i] (F♯(Q_i, Q̃_r) - Σ_j r_j F♯(Q_j, Q̃_r)))
 // with Q̃ = q(Σ_j l_j W(Q_j)).  With w = λ/J and T = Σ_i ∂g[i] w_i, the pair F♯(Q_j, Q̃) has the
 // cotangent ±Ja (∂g[j] w_j - l_j T); its node-side cotangents go to snode, and its Q̃ side, summed
 // over the line, is taken to the projected entropy variables (sWb), which the node phase spreads
-// back with l.
+// back with l.  One group of 8 lanes per line side (N <= 8), one lane per node: the sums over the
+// line (W̃, T and the Q̃ cotangent) are butterfly shuffles within the group, which leave the same
+// bits in every lane; each lane then takes its node's pair.  A node receives one cotangent from
+// each side of its line, added into snode (zeroed first) in either order: two addends onto zero
+// give the same sum.
 template <int DIM, int N, int D, int TP>
 __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int e0, const double* sops,
                                                      const double* sprim, const double* sw, double* snode,
@@ -1421,90 +1426,86 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, true>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR, NPB = A::NPB;
-    constexpr int NPROJ = A::NPROJ;
+    constexpr int NPROJ = A::NPROJ;   // line sides of the block: the groups
+    static_assert(N <= 8, "one lane per node of a line within a group of 8");
     const double g = P.gamma, g1 = g - 1.0;
     const double* lv = sops + 2 * N * N;   // l_l, then l_r
     const double* dgl = lv + 2 * N;        // ∂g_l, then ∂g_r
-    for (int t = threadIdx.x; t < S::EPB * NFD; t += blockDim.x) {
-        const int elp = t / NFD, line = t - elp * NFD;
-        const int e = e0 + elp;
-        if (e >= P.nelem) continue;
-        const double Ja = P.Ja[e * DIM + D];
-        double wt[2][NV], T[2][NV];
+    for (int t = threadIdx.x; t < NPB * NN; t += blockDim.x) snode[t] = 0.0;
+    __syncthreads();
+    auto gsum = [](double v) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) wt[0][k] = wt[1][k] = T[0][k] = T[1][k] = 0.0;
-        for (int pos = 0; pos < N; ++pos) {
-            const int j = elp * NPE + tp_node<DIM>(N, D, line, pos);
-            double q[NV], w[NV];
+        for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    };
+    constexpr int TOTAL = ((NPROJ * 8 + 31) / 32) * 32;   // whole warps, so every shuffle has its partners
+    for (int t = threadIdx.x; t < TOTAL; t += blockDim.x) {
+        const int grp = t >> 3, pos = t & 7;
+        const int elp = grp / (2 * NFD), rr = grp - elp * 2 * NFD, line = rr >> 1, sd = rr & 1;
+        const bool on = grp < NPROJ && e0 + elp < P.nelem && pos < N;
+        const int j = on ? elp * NPE + tp_node<DIM>(N, D, line, pos) : 0;
+        double wt[NV], T[NV];
+        if (on) {
+            double q[NV], wj[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
-            entropy_of<DIM>(q, g, w);
+            entropy_of<DIM>(q, g, wj);
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                wt[0][k] = fma(lv[pos], w[k], wt[0][k]);
-                wt[1][k] = fma(lv[N + pos], w[k], wt[1][k]);
-                T[0][k] = fma(dgl[pos], sw[k * NN + j], T[0][k]);
-                T[1][k] = fma(dgl[N + pos], sw[k * NN + j], T[1][k]);
+                wt[k] = lv[sd * N + pos] * wj[k];
+                T[k] = dgl[sd * N + pos] * sw[k * NN + j];
             }
-        }
-        double qt[2][NV], pt[2], vt[2][NARR];
+        } else {
 #pragma unroll
-        for (int sd = 0; sd < 2; ++sd) {
-            pt[sd] = state_of_entropy<DIM>(wt[sd], g, qt[sd]);
-            split_node_values<DIM, TP>(qt[sd], pt[sd], vt[sd]);
+            for (int k = 0; k < NV; ++k) wt[k] = T[k] = 0.0;
         }
-        PrimBar ot[2];
 #pragma unroll
-        for (int sd = 0; sd < 2; ++sd) {
-            ot[sd].r = ot[sd].b = ot[sd].e = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) ot[sd].v[k] = 0.0;
+        for (int k = 0; k < NV; ++k) {
+            wt[k] = gsum(wt[k]);
+            T[k] = gsum(T[k]);
         }
-        for (int pos = 0; pos < N; ++pos) {
-            const int j = elp * NPE + tp_node<DIM>(N, D, line, pos);
-            double vj[NARR];
+        PrimBar o2;
+        o2.r = o2.b = o2.e = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) o2.v[k] = 0.0;
+        double qt[NV], pt = 1.0;
+        const bool grp_on = grp < NPROJ && e0 + elp < P.nelem;
+        if (grp_on) {
+            pt = state_of_entropy<DIM>(wt, g, qt);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qt[k] = k == 0 || k == DIM + 1 ? 1.0 : 0.0;
+        }
+        if (on) {
+            double vt[NARR], vj[NARR], Fb[NV];
+            split_node_values<DIM, TP>(qt, pt, vt);
 #pragma unroll
             for (int k = 0; k < NARR; ++k) vj[k] = sprim[k * NN + j];
-            PrimBar on;
-            on.r = on.b = on.e = 0.0;
+            const double Ja = P.Ja[(e0 + elp) * DIM + D], sg = sd == 0 ? Ja : -Ja;
+            const double dg = dgl[sd * N + pos], lj = lv[sd * N + pos];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) on.v[k] = 0.0;
+            for (int k = 0; k < NV; ++k) Fb[k] = sg * fma(dg, sw[k * NN + j], -lj * T[k]);
+            PrimBar o1;
+            split_pair_vjp<DIM, D, TP>(vj, vt, Fb, cb, g1, o1, o2);
+            atomicAdd(snode + j, o1.r);
 #pragma unroll
-            for (int sd = 0; sd < 2; ++sd) {
-                const double sg = sd == 0 ? Ja : -Ja;
-                const double dg = dgl[sd * N + pos], lj = lv[sd * N + pos];
-                double Fb[NV];
-#pragma unroll
-                for (int k = 0; k < NV; ++k) Fb[k] = sg * fma(dg, sw[k * NN + j], -lj * T[sd][k]);
-                PrimBar o1, o2;
-                split_pair_vjp<DIM, D, TP>(vj, vt[sd], Fb, cb, g1, o1, o2);
-                on.r += o1.r;
-                on.b += o1.b;
-                on.e += o1.e;
-                ot[sd].r += o2.r;
-                ot[sd].b += o2.b;
-                ot[sd].e += o2.e;
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) {
-                    on.v[k] += o1.v[k];
-                    ot[sd].v[k] += o2.v[k];
-                }
-            }
-            snode[j] = on.r;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) snode[(1 + k) * NN + j] = on.v[k];
-            snode[(1 + DIM) * NN + j] = on.b;
-            if constexpr (NPB > DIM + 2) snode[(2 + DIM) * NN + j] = on.e;
+            for (int k = 0; k < DIM; ++k) atomicAdd(snode + (1 + k) * NN + j, o1.v[k]);
+            atomicAdd(snode + (1 + DIM) * NN + j, o1.b);
+            if constexpr (NPB > DIM + 2) atomicAdd(snode + (2 + DIM) * NN + j, o1.e);
         }
+        o2.r = gsum(o2.r);
+        o2.b = gsum(o2.b);
+        o2.e = gsum(o2.e);
 #pragma unroll
-        for (int sd = 0; sd < 2; ++sd) {   // Q̃'s cotangent -> conserved -> entropy variables
+        for (int k = 0; k < DIM; ++k) o2.v[k] = gsum(o2.v[k]);
+        if (grp_on && pos == 0) {   // Q̃'s cotangent -> conserved -> entropy variables
             double qbt[NV], wbt[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k) qbt[k] = 0.0;
-            split_node_to_cons<DIM, TP>(qt[sd], pt[sd], g1, ot[sd], qbt);
-            entropy_jacobian_apply<DIM>(qt[sd], pt[sd], g, qbt, wbt);
+            split_node_to_cons<DIM, TP>(qt, pt, g1, o2, qbt);
+            entropy_jacobian_apply<DIM>(qt, pt, g, qbt, wbt);
 #pragma unroll
-            for (int k = 0; k < NV; ++k) sWb[k * NPROJ + 2 * t + sd] = wbt[k];
+            for (int k = 0; k < NV; ++k) sWb[k * NPROJ + grp] = wbt[k];
         }
     }
 }
