@@ -82,9 +82,6 @@ int adj_supported(flou_ctx* c, bool batched = false) {
                                                  "the split form (Chandrashekar, Kennedy-Gruber or StdAverage), and the "
                                                  "LxF, Scalar- or MatrixDissipation (StdAverage or ChandrasekharAverage), "
                                                  "HLL or HLLC interface flux");
-    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && c->curv)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form on Gauss nodes covers Cartesian "
-                                                 "geometry");
     if (k.volume_op == FLOU_OP_SPLIT && c->bnodes && !c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs the DGSEM lift on a basis "
                                                  "with boundary nodes");
@@ -92,9 +89,8 @@ int adj_supported(flou_ctx* c, bool batched = false) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile of the Kennedy-Gruber flux at "
                                                  "3D p=7 exceeds shared memory");
     if (k.volume_op == FLOU_OP_HYBRID) {
-        if (!c->bnodes || !c->lift_ends || c->curv)
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto nodes "
-                                                     "and Cartesian geometry");
+        if (!c->bnodes || !c->lift_ends)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto nodes");
         if (fv_kind(c) < 0)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator's subcell flux must be LxF, "
                                                      "Scalar- or MatrixDissipation (StdAverage or "
@@ -214,6 +210,8 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.fvavg = c->fvavg;
     P.fvintensity = c->fvintensity;
     P.blend = c->blend;
+    P.subfr = c->d_subfr;
+    P.subJ = c->d_subJ;
     if (c->cfg.volume_op != FLOU_OP_STRONG) {
         e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss,
                                  c->cfg.volume_op == FLOU_OP_HYBRID, P, s);

@@ -103,6 +103,10 @@ struct AdjElemParams {
     const double* omega1;
     int32_t fvkind, fvflux, fvavg;   // numflux_vjp kind; the forward's numflux and central part
     double fvintensity, blend;
+    // general geometry, hybrid and Gauss-node forms: the subcell interfaces' frames [9][ns] and
+    // surface Jacobians, at ((e DIM + dir) n^(d-1) + line)(n+1) + s
+    const double* subfr;
+    const double* subJ;
 };
 
 // q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
@@ -1280,16 +1284,22 @@ __device__ __forceinline__ void split_node_values(const double* q, double p, dou
 // The two-point flux VJP of the split form along axis D for two nodes given by their
 // split_node_values A and B: cotangents in the format the node phase sums (PrimBar; StdAverage:
 // conserved).
+// D < 0: along the general direction nrm (general geometry).
 template <int DIM, int D, int TP>
 __device__ __forceinline__ void split_pair_vjp(const double* A, const double* B, const double* Fb, double cb,
-                                               double g1, PrimBar& o1, PrimBar& o2) {
+                                               double g1, PrimBar& o1, PrimBar& o2, const double* nrm = nullptr) {
     constexpr int NV = DIM + 2;
     if constexpr (TP == FLOU_TP_STD_AVERAGE) {
         double qa_[NV], qb_[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) qa_[k] = qb_[k] = 0.0;
-        euler_flux_vjp<DIM>(D, A + 1, A[1 + DIM], A[0], g1, Fb, 0.5, qa_);
-        euler_flux_vjp<DIM>(D, B + 1, B[1 + DIM], B[0], g1, Fb, 0.5, qb_);
+        if constexpr (D >= 0) {
+            euler_flux_vjp<DIM>(D, A + 1, A[1 + DIM], A[0], g1, Fb, 0.5, qa_);
+            euler_flux_vjp<DIM>(D, B + 1, B[1 + DIM], B[0], g1, Fb, 0.5, qb_);
+        } else {
+            euler_flux_vjp_n<DIM>(nrm, A + 1, A[1 + DIM], A[0], g1, Fb, 0.5, qa_);
+            euler_flux_vjp_n<DIM>(nrm, B + 1, B[1 + DIM], B[0], g1, Fb, 0.5, qb_);
+        }
         o1.r = qa_[0];
         o2.r = qb_[0];
 #pragma unroll
@@ -1301,10 +1311,11 @@ __device__ __forceinline__ void split_pair_vjp(const double* A, const double* B,
         o2.b = qb_[DIM + 1];
         o1.e = o2.e = 0.0;
     } else if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) {
-        kg_pair_vjp<DIM, D>(A[0], A + 1, A[1 + DIM], A[2 + DIM], B[0], B + 1, B[1 + DIM], B[2 + DIM], Fb, o1, o2);
+        kg_pair_vjp<DIM, D>(A[0], A + 1, A[1 + DIM], A[2 + DIM], B[0], B + 1, B[1 + DIM], B[2 + DIM], Fb, o1, o2,
+                            nrm);
     } else {
         chandra_pair_vjp<DIM, D, false>(A[0], A + 1, A[1 + DIM], A[2 + DIM], B[0], B + 1, B[1 + DIM], B[2 + DIM], cb,
-                                        Fb, o1, o2);
+                                        Fb, o1, o2, nrm);
         o1.e = o2.e = 0.0;
     }
 }
@@ -1419,7 +1430,11 @@ __device__ __forceinline__ void entropy_vjp(const double* q, double p, double g,
 // bits in every lane; each lane then takes its node's pair.  A node receives one cotangent from
 // each side of its line, added into snode (zeroed first) in either order: two addends onto zero
 // give the same sum.
-template <int DIM, int N, int D, int TP>
+// CURV: the pair of node j with a projected state is along n̄ = (Ja_j + n Js)/2, Ja_j the node's
+// metric column of direction D and n Js the line end's subcell interface normal times its surface
+// Jacobian (the forward's metric of the projected states); the metric is in the fluxes, so the
+// cotangent carries ±1 instead of ±Ja.
+template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int e0, const double* sops,
                                                      const double* sprim, const double* sw, double* snode,
                                                      double* sWb, double cb) {
@@ -1481,12 +1496,24 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
             split_node_values<DIM, TP>(qt, pt, vt);
 #pragma unroll
             for (int k = 0; k < NARR; ++k) vj[k] = sprim[k * NN + j];
-            const double Ja = P.Ja[(e0 + elp) * DIM + D], sg = sd == 0 ? Ja : -Ja;
+            const double Ja = CURV ? 1.0 : P.Ja[(e0 + elp) * DIM + D], sg = sd == 0 ? Ja : -Ja;
             const double dg = dgl[sd * N + pos], lj = lv[sd * N + pos];
 #pragma unroll
             for (int k = 0; k < NV; ++k) Fb[k] = sg * fma(dg, sw[k * NN + j], -lj * T[k]);
             PrimBar o1;
-            split_pair_vjp<DIM, D, TP>(vj, vt, Fb, cb, g1, o1, o2);
+            if constexpr (CURV) {
+                const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+                const int64_t si = (((int64_t)(e0 + elp) * DIM + D) * NFD + line) * (N + 1) + (sd ? N : 0);
+                const int64_t gj = (int64_t)e0 * NPE + j;
+                const double js = P.subJ[si];
+                double nrm[DIM];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                    nrm[k] = 0.5 * fma(P.subfr[k * ns + si], js, P.Jan[(k + D * DIM) * P.ndofs + gj]);
+                split_pair_vjp<DIM, -1, TP>(vj, vt, Fb, cb, g1, o1, o2, nrm);
+            } else {
+                split_pair_vjp<DIM, D, TP>(vj, vt, Fb, cb, g1, o1, o2);
+            }
             atomicAdd(snode + j, o1.r);
 #pragma unroll
             for (int k = 0; k < DIM; ++k) atomicAdd(snode + (1 + k) * NN + j, o1.v[k]);
@@ -1524,16 +1551,53 @@ __device__ __forceinline__ void euler_flux_axis(const double* q, double g, doubl
     F[DIM + 1] = (q[DIM + 1] + p) * vd;
 }
 
+// The Euler flux along a general direction n: [ρ v·n, ρ v v·n + p n, (E+p) v·n].
+template <int DIM>
+__device__ __forceinline__ void euler_flux_n(const double* q, const double* n, double g, double* F) {
+    const double ir = rcp_refined(q[0]);
+    double ke = 0.0, mn = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        ke = fma(q[1 + k], q[1 + k] * ir, ke);
+        mn = fma(q[1 + k], n[k], mn);
+    }
+    const double p = (g - 1.0) * fma(-0.5, ke, q[DIM + 1]), vn = mn * ir;
+    F[0] = mn;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) F[1 + k] = fma(q[1 + k], vn, p * n[k]);
+    F[DIM + 1] = (q[DIM + 1] + p) * vn;
+}
+
 // The split form's two-point flux along axis D (the forward of split_pair_vjp) from the nodes'
-// split_node_values A, B; StdAverage takes the conserved states qa, qb.
+// split_node_values A, B; StdAverage takes the conserved states qa, qb.  D < 0: along the
+// general direction nrm.
 template <int DIM, int D, int TP>
 __device__ __forceinline__ void split_pair_flux(const double* A, const double* B, const double* qa, const double* qb,
-                                                double g, double* F) {
+                                                double g, double* F, const double* nrm = nullptr) {
     constexpr int NV = DIM + 2;
+    auto along = [&](const double* v) {   // v·(the direction)
+        if constexpr (D >= 0) {
+            return v[D];
+        } else {
+            double x = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) x = fma(v[k], nrm[k], x);
+            return x;
+        }
+    };
+    auto dir = [&](int k) {   // the direction's component k
+        if constexpr (D >= 0) return k == D ? 1.0 : 0.0;
+        else return nrm[k];
+    };
     if constexpr (TP == FLOU_TP_STD_AVERAGE) {
         double Fa[NV], Fc[NV];
-        euler_flux_axis<DIM, D>(qa, g, Fa);
-        euler_flux_axis<DIM, D>(qb, g, Fc);
+        if constexpr (D >= 0) {
+            euler_flux_axis<DIM, D>(qa, g, Fa);
+            euler_flux_axis<DIM, D>(qb, g, Fc);
+        } else {
+            euler_flux_n<DIM>(qa, nrm, g, Fa);
+            euler_flux_n<DIM>(qb, nrm, g, Fc);
+        }
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = 0.5 * (Fa[k] + Fc[k]);
     } else if constexpr (TP == FLOU_TP_KENNEDY_GRUBER) {
@@ -1541,11 +1605,11 @@ __device__ __forceinline__ void split_pair_flux(const double* A, const double* B
         double vm[DIM];
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vm[k] = A[1 + k] + B[1 + k];
-        const double m = rho * vm[D];
+        const double vd = along(vm), m = rho * vd;
         F[0] = m;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, vm[k], k == D ? pm : 0.0);
-        F[DIM + 1] = fma(m, en, pm * vm[D]);
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, vm[k], pm * dir(k));
+        F[DIM + 1] = fma(m, en, pm * vd);
     } else {
         const double hsr = A[0] + B[0], hdr = A[0] - B[0], hsb = A[1 + DIM] + B[1 + DIM],
                      hdb = A[1 + DIM] - B[1 + DIM];
@@ -1561,10 +1625,10 @@ __device__ __forceinline__ void split_pair_flux(const double* A, const double* B
             vv = fma(va[k], va[k], vv);
         }
         const double h = fma(0.5 * rcp_refined(g - 1.0), ibeta, -(A[2 + DIM] + B[2 + DIM])) + fma(p, irho, vv);
-        const double m = rho * va[D];
+        const double m = rho * along(va);
         F[0] = m;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], k == D ? p : 0.0);
+        for (int k = 0; k < DIM; ++k) F[1 + k] = fma(m, va[k], p * dir(k));
         F[DIM + 1] = m * h;
     }
 }
@@ -1596,7 +1660,10 @@ __device__ __noinline__ void numflux_vjp_any(int kind, const double* a, const do
 // cotangents give each node's pair weight w'_r = -ω_r Σ_(p>r) F̄̄_p, left in sH for the split-form
 // pair and node phases.  A node's contribution from the interface on its right is handed over in
 // spb (free between the phases); the node's own goes to qb.
-template <int DIM, int N, int D, int TP>
+// CURV (general geometry): the pair fluxes along the averaged metric columns, the node's own
+// column in the diagonal term, ω_p alone as the node-sum weight (the metric is in the fluxes), and
+// each subcell interface's uploaded frame and surface Jacobian for the FV flux.
+template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
                                                const double* sops, const double* sprim, const double* sw, double* sH,
                                                double* spb, const uint8_t* stab, double* qb) {
@@ -1628,7 +1695,16 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
                 qc[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + ib];
             }
         }
-        split_pair_flux<DIM, D, TP>(Av, Bv, qa, qc, g, F);
+        if constexpr (CURV) {
+            const int64_t ga = (int64_t)e0 * NPE + ia, gb = (int64_t)e0 * NPE + ib;
+            double nrm[DIM];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+                nrm[k] = 0.5 * (P.Jan[(k + D * DIM) * P.ndofs + ga] + P.Jan[(k + D * DIM) * P.ndofs + gb]);
+            split_pair_flux<DIM, -1, TP>(Av, Bv, qa, qc, g, F, nrm);
+        } else {
+            split_pair_flux<DIM, D, TP>(Av, Bv, qa, qc, g, F);
+        }
 #pragma unroll
         for (int k = 0; k < NV; ++k) spb[k * NPT + kp] = F[k];
     }
@@ -1637,12 +1713,19 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
     int pos = 0, line = 0;
     tp_coords<DIM>(N, i, D, pos, line);
     const int64_t gi = (int64_t)e * NPE + i;
-    const double Ja = active ? P.Ja[e * DIM + D] : 0.0;
+    const double Ja = active ? (CURV ? 1.0 : P.Ja[e * DIM + D]) : 0.0;
     if (active) {   // ω_p Ja Σ_j D♯_pj F♯_pj (with the diagonal D♯_pp F(Q_p))
         double q[NV], acc[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
-        euler_flux_axis<DIM, D>(q, g, acc);
+        if constexpr (CURV) {
+            double nrm[DIM];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
+            euler_flux_n<DIM>(q, nrm, g, acc);
+        } else {
+            euler_flux_axis<DIM, D>(q, g, acc);
+        }
         const double dii = Dsh[pos + pos * N];
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] *= dii;
@@ -1688,15 +1771,37 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
             qr[k] = P.U[k * P.ndofs + gi];
         }
         const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
-        a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-        cart_to_face<DIM>(ql, Ax, a);
-        cart_to_face<DIM>(qr, Ax, b);
-        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
-        Fv[0] = Fr[0] * Ja;
-        Fv[DIM + 1] = Fr[DIM + 1] * Ja;
-        cart_to_phys<DIM>(Fr, Ax, Fv);
+        FrameTab fr;   // CURV: the subcell interface's frame and surface Jacobian
+        double Js = Ja;
+        if constexpr (CURV) {
+            const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+            const int64_t si = (((int64_t)e * DIM + D) * NFD + line) * (N + 1) + pos;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) Fv[1 + k] *= Ja;
+            for (int r = 0; r < 3; ++r) {
+                fr.n[r] = P.subfr[r * ns + si];
+                fr.t[r] = P.subfr[(3 + r) * ns + si];
+                fr.b[r] = P.subfr[(6 + r) * ns + si];
+            }
+            Js = P.subJ[si];
+            rotate_to_face<DIM>(ql, fr, a);
+            rotate_to_face<DIM>(qr, fr, b);
+        } else {
+            a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+            cart_to_face<DIM>(ql, Ax, a);
+            cart_to_face<DIM>(qr, Ax, b);
+        }
+        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+        if constexpr (CURV) {
+            rotate_to_phys<DIM>(Fr, fr, Fv);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) Fv[k] *= Js;
+        } else {
+            Fv[0] = Fr[0] * Js;
+            Fv[DIM + 1] = Fr[DIM + 1] * Js;
+            cart_to_phys<DIM>(Fr, Ax, Fv);
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) Fv[1 + k] *= Js;
+        }
         entropy_of<DIM>(ql, g, wl);
         entropy_of<DIM>(qr, g, wr);
         double bb = 0.0, dW[NV], Fh[NV];
@@ -1726,15 +1831,26 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
             wbar[k] = bbar * (Fh[k] - Fv[k]);
         }
         double Frb[NV], ab[NV], bbr[NV], t[NV], ol[NV], orr[NV];
-        Frb[0] = Ja * Fvb[0];
-        Frb[DIM + 1] = Ja * Fvb[DIM + 1];
-        cart_to_face<DIM>(Fvb, Ax, t);
+        if constexpr (CURV) {
+            rotate_to_face<DIM>(Fvb, fr, t);
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) Frb[1 + k] = Ja * t[1 + k];
+            for (int k = 0; k < NV; ++k) Frb[k] = Js * t[k];
+        } else {
+            Frb[0] = Js * Fvb[0];
+            Frb[DIM + 1] = Js * Fvb[DIM + 1];
+            cart_to_face<DIM>(Fvb, Ax, t);
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) Frb[1 + k] = Js * t[1 + k];
+        }
         numflux_vjp_any<DIM>(P.fvkind, a, b, P.fvintensity, g, Frb, ab, bbr);
-        ol[0] = ab[0]; ol[DIM + 1] = ab[DIM + 1]; orr[0] = bbr[0]; orr[DIM + 1] = bbr[DIM + 1];
-        cart_to_phys<DIM>(ab, Ax, ol);
-        cart_to_phys<DIM>(bbr, Ax, orr);
+        if constexpr (CURV) {
+            rotate_to_phys<DIM>(ab, fr, ol);
+            rotate_to_phys<DIM>(bbr, fr, orr);
+        } else {
+            ol[0] = ab[0]; ol[DIM + 1] = ab[DIM + 1]; orr[0] = bbr[0]; orr[DIM + 1] = bbr[DIM + 1];
+            cart_to_phys<DIM>(ab, Ax, ol);
+            cart_to_phys<DIM>(bbr, Ax, orr);
+        }
         auto pressure = [&](const double* q) {
             double ke = 0.0;
 #pragma unroll
@@ -2036,17 +2152,20 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
         if constexpr (H) {
-            if (dir == 0) adj_hybrid_dir<DIM, N, 0, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
-            else if (dir == 1) adj_hybrid_dir<DIM, N, D1, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
-            else adj_hybrid_dir<DIM, N, D2, TP>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+            if (dir == 0)
+                adj_hybrid_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+            else if (dir == 1)
+                adj_hybrid_dir<DIM, N, D1, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+            else
+                adj_hybrid_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
         }
         if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         if constexpr (G) {
-            if (dir == 0) adj_split_projection<DIM, N, 0, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
-            else if (dir == 1) adj_split_projection<DIM, N, D1, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
-            else adj_split_projection<DIM, N, D2, TP>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            if (dir == 0) adj_split_projection<DIM, N, 0, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            else if (dir == 1) adj_split_projection<DIM, N, D1, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            else adj_split_projection<DIM, N, D2, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
         }
         __syncthreads();
         if (active) {

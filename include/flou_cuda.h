@@ -265,12 +265,11 @@ int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
  * Covers the Euler equations with
  *  - the strong form, the split form (Chandrashekar, Kennedy-Gruber or StdAverage two-point
- *    flux) and the hybrid operator (Gauss-Lobatto nodes and Cartesian geometry; any interface
- *    flux below as its subcell flux);
+ *    flux) and the hybrid operator (Gauss-Lobatto nodes; any interface flux below as its
+ *    subcell flux);
  *  - the LxF, ScalarDissipation or MatrixDissipation interface flux (StdAverage or
  *    ChandrasekharAverage central part), HLL and HLLC;
- *  - Gauss-Lobatto or Gauss nodes, Cartesian or general geometry (the split form on Gauss
- *    nodes: Cartesian geometry);
+ *  - Gauss-Lobatto or Gauss nodes, Cartesian or general geometry;
  *  - periodic, slip-wall, outflow, inflow and boundary-state-field boundaries (fixed external
  *    states are constants of the differentiation);
  *  - SSP-RK3 or the 2N-storage method set by flou_set_integrator, with or without the Zhang-Shu

@@ -602,20 +602,8 @@ def test_gauss_nodes_split_adjoint_solve_against_dual_numbers(op):
 
 
 def test_gauss_nodes_split_adjoint_limits():
-    """Not covered: the split form on Gauss nodes on general geometry, and the Kennedy-Gruber 3D
-    p=7 tile (beyond shared memory)."""
+    """Not covered: the Kennedy-Gruber 3D p=7 tile (beyond shared memory)."""
     from flou_cuda import _lib as L
-    from test_unstructured import _std
-    eq = F.EulerEquation(2, 1.4)
-    mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=3)
-    disc = F.MultielementDisc(mesh, _std(2, 4, 4, "GL"), eq, _split(),
-                              {str(k): F.EulerOutflowBC() for k in range(1, 5)})
-    from test_unstructured import _state
-    Q = _dev(_state(disc, seed=1))
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        disc.ctx.rhs_vjp(g, None, Q, Q)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
     kg = build(3, 8, (1, 1, 1), F.EulerEquation(3, 1.4), OPERATORS["split_kg"](), basis="GL")
     Q = _dev(smooth_euler_state(kg, seed=1))
     g = torch.empty_like(Q)
@@ -722,7 +710,7 @@ def test_hybrid_adjoint_solve_against_dual_numbers(op):
 
 
 def test_hybrid_adjoint_limits():
-    """Not covered: the hybrid operator on Gauss nodes and on general geometry."""
+    """Not covered: the hybrid operator on Gauss nodes."""
     from flou_cuda import _lib as L
     disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), HYBRID_OPS["hybrid_hllc"](), basis="GL")
     Q = _dev(smooth_euler_state(disc, seed=1))
@@ -730,14 +718,68 @@ def test_hybrid_adjoint_limits():
     with pytest.raises(F.FlouError) as ei:
         disc.ctx.rhs_vjp(g, None, Q, Q)
     assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+
+
+def _maybe_c(disc, c):
+    """The per-element dissipation scale where the interface flux takes one (LxF): (c, False);
+    else (ones, True)."""
+    try:
+        disc.ctx.set_dissipation(c)
+        return c, False
+    except F.FlouError:
+        return np.ones_like(c), True
+
+
+@pytest.mark.parametrize("op,basis", [("split_chandra_lxfc", "GL"), ("split_kg_lxf", "GL"), ("split_std_lxf", "GL"),
+                                      ("split_chandra_md", "GL"), ("hybrid_hllc", "GLL"), ("hybrid_md", "GLL"),
+                                      ("hybrid_kg", "GLL")])
+@pytest.mark.parametrize("dim,n", [(2, 4), (3, 3), (3, 4)])
+def test_general_geometry_gauss_split_and_hybrid_rhs_vjp(dim, n, op, basis):
+    """General geometry for the split form on Gauss nodes (the projected states' pairs along
+    (Ja_j + n Js)/2 with the line end's subcell normal) and for the hybrid operator (the subcell
+    FV fluxes in the uploaded subcell frames), against the oracle's dual numbers."""
     from test_gpu_unstructured import _disc as _udisc
     from test_unstructured import _state
-    u = _udisc(2, 4, "hybrid_hllc")
-    Q = _dev(_state(u, seed=2))
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        u.ctx.rhs_vjp(g, None, Q, Q)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+    disc = _udisc(dim, n, op, basis=basis)
+    if dim == 3:
+        assert len(set(disc.mesh.orientation.tolist())) == 8
+    rng = np.random.default_rng(100 + dim + n)
+    Q = _state(disc, seed=dim * 3 + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _maybe_c(disc, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op,basis", [("split_chandra_lxfc", "GL"), ("hybrid_hllc", "GLL")])
+def test_general_geometry_gauss_split_and_hybrid_adjoint_solve(op, basis):
+    from test_gpu_unstructured import _disc as _udisc
+    from test_unstructured import _state
+    disc = _udisc(3, 4, op, basis=basis)
+    Q0 = _state(disc, seed=5)
+    rng = np.random.default_rng(53)
+    c, noc = _maybe_c(disc, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 12)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 5
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 2, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if noc else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if noc else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
 @pytest.mark.parametrize("integrator", ["SSPRK3", "ORK256"])
