@@ -66,9 +66,30 @@ int flux_kind(int nf, int avg) {
 }
 int fv_kind(const flou_ctx* c) { return flux_kind(c->fvflux, c->fvavg); }
 
+// The scalar equations (linear advection, Burgers): the strong form on either node set or the
+// split form with the arithmetic-mean two-point flux, the LxF or central interface flux,
+// Cartesian geometry.
+int adj_supported_scalar(flou_ctx* c, bool batched) {
+    const flou_config& k = c->cfg;
+    const bool vol = k.volume_op == FLOU_OP_STRONG ||
+                     (k.volume_op == FLOU_OP_SPLIT && k.twopoint_flux == FLOU_TP_STD_AVERAGE);
+    const bool nf = k.numflux == FLOU_NF_STD_AVERAGE ||
+                    (k.numflux == FLOU_NF_LXF && k.numflux_avg == FLOU_NF_STD_AVERAGE);
+    if (!vol || !nf)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the scalar equations covers the strong form and the "
+                                                 "split form with the StdAverage two-point flux, with the LxF or "
+                                                 "StdAverage interface flux");
+    if (c->curv)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the scalar equations covers Cartesian geometry");
+    if (batched && c->lsrk_s)
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint steps with SSP-RK3 (flou_set_integrator 0)");
+    return FLOU_OK;
+}
+
 // batched: the batched adjoint, whose lockstep sweep steps with SSP-RK3 and no limiter.
 int adj_supported(flou_ctx* c, bool batched = false) {
     const flou_config& k = c->cfg;
+    if (k.equation != FLOU_EQ_EULER) return adj_supported_scalar(c, batched);
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                ((k.volume_op == FLOU_OP_SPLIT || k.volume_op == FLOU_OP_HYBRID) &&
                 (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER ||
@@ -169,7 +190,10 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     // interpolated traces and the full-line lift: the strong form on a basis without exact end-node
     // injection, the split form on a basis without boundary nodes (the forward's general paths)
     const bool gauss = c->cfg.volume_op == FLOU_OP_STRONG ? !c->lgl : !c->bnodes;
-    cudaError_t e = launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
+    const bool scalar = c->cfg.equation != FLOU_EQ_EULER;
+    for (int d = 0; d < 3; ++d) F.adv[d] = c->cfg.advection[d];
+    F.lxf = c->cfg.numflux == FLOU_NF_LXF ? 1 : 0;
+    cudaError_t e = scalar ? cudaSuccess : launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
     memset(&P, 0, sizeof(P));
@@ -212,6 +236,12 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.blend = c->blend;
     P.subfr = c->d_subfr;
     P.subJ = c->d_subJ;
+    for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
+    if (scalar) {
+        e = launch_adj_scalar(dim, c->cfg.equation, c->n, c->cfg.volume_op == FLOU_OP_SPLIT, gauss, grid, tb, F, P, s);
+        if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint kernels (scalar equation)");
+        return FLOU_OK;
+    }
     if (c->cfg.volume_op != FLOU_OP_STRONG) {
         e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss,
                                  c->cfg.volume_op == FLOU_OP_HYBRID, P, s);

@@ -67,6 +67,8 @@ struct AdjFaceParams {
     // per face node), in the physical frame; constants, so their cotangents are dropped
     double bc_state[MAXBC][5];
     const double* bc_field;
+    double adv[3];          // linear advection velocity (scalar equations)
+    int32_t lxf;            // scalar equations: LxF dissipation (else the central flux)
 };
 
 struct AdjElemParams {
@@ -107,6 +109,7 @@ struct AdjElemParams {
     // surface Jacobians, at ((e DIM + dir) n^(d-1) + line)(n+1) + s
     const double* subfr;
     const double* subJ;
+    double adv[3];          // linear advection velocity (scalar equations)
 };
 
 // q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
@@ -2276,6 +2279,187 @@ inline bool adj_split_tile_fits(int dim, int n, int tp, bool hybrid) {
                   : AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, true>::SMEM <= 227 * 1024;
 }
 
+
+// ---- the scalar equations: linear advection (LinearAdvection.jl) and Burgers (Burgers.jl) ----
+// Face VJP.  The flux is F = J (an (q_l + q_r)/2 + [LxF] |an| (q_l - q_r)/2 c) for linear
+// advection (an = a·n), and F = J ((q_l² + q_r²)/4 n + [LxF] λ (q_l - q_r)/2 c) with
+// λ = max(|q_l|, |q_r|) for Burgers (1D); the face normal n is the master side's.  Its cotangent
+// comes from the lift as for the Euler face VJP (G: the interpolated traces and the full-line
+// lift).  A fixed boundary state (Dirichlet, a state field) takes no cotangent; outflow passes
+// the ghost's to the trace.  The intensity cotangent feeds dJ/dc.
+template <int DIM, int EQ, bool G = false>
+__global__ void __launch_bounds__(256) adj_face_scalar_kernel(AdjFaceParams P) {
+    int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)P.nfaces * P.nfd) return;
+    const int f = (int)(gid / P.nfd), m = (int)(gid - (int64_t)f * P.nfd);
+    const int n = P.n;
+    const int32_t s0 = P.face_elem[2 * f], s1 = P.face_elem[2 * f + 1];
+    if (kChecked && !(index_ok(s0 >> 3, P.ndofs / P.npe, P.status, 0) &&
+                      (s1 < 0 || index_ok(s1 >> 3, P.ndofs / P.npe, P.status, s0 >> 3)) &&
+                      (s1 >= 0 || index_ok(P.face_bc[f], MAXBC, P.status, s0 >> 3))))
+        return;
+    const double* lvb = P.ops + 2 * n * n;
+    const double* dgl = lvb + 2 * n;
+    const double* dgr = dgl + n;
+    // the trace of side s and the lift transpose Σ ∂g (w λ) over its line (LGL: the end node)
+    auto side = [&](int32_t s, double& q, double& fl) {
+        const int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
+        const double wj = P.invJ[e] * P.s_lam;
+        if constexpr (G) {
+            const double* lv = lvb + (right ? n : 0);
+            const double* dg = right ? dgr : dgl;
+            q = fl = 0.0;
+            for (int p = 0; p < n; ++p) {
+                const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, p);
+                q = fma(lv[p], P.U[gg], q);
+                fl = fma(wj * dg[p], P.Ain[gg], fl);
+            }
+        } else {
+            const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+            q = P.U[gg];
+            fl = (right ? dgr[n - 1] : dgl[0]) * wj * P.Ain[gg];
+        }
+    };
+    double ql, qr = 0.0, f1, f2 = 0.0;
+    side(s0, ql, f1);
+    double Fb = -f1;
+    int bck = 0;
+    if (s1 >= 0) {
+        side(s1, qr, f2);
+        Fb += f2;
+    } else {
+        const int bi = P.face_bc[f];
+        bck = P.bc_kind[bi];
+        qr = bck == FLOU_BC_INFLOW ? P.bc_state[bi][0] : bck == FLOU_BC_STATE_FIELD ? P.bc_field[gid] : ql;
+    }
+    Fb *= P.faceJ[f];
+    double inten = P.intensity;
+    if (P.elem_c) {
+        const int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
+        inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
+    }
+    const FrameTab fr = frame_of(DIM, s0 & 7);
+    double ab, bb, Ib = 0.0;
+    if constexpr (EQ == FLOU_EQ_LINEAR_ADVECTION) {
+        double an = P.adv[0] * fr.n[0];
+        if (DIM > 1) an = an + P.adv[1] * fr.n[1];
+        if (DIM > 2) an = an + P.adv[2] * fr.n[2];
+        ab = bb = 0.5 * an * Fb;
+        if (P.lxf) {
+            const double d = 0.5 * fabs(an) * inten * Fb;
+            ab += d;
+            bb -= d;
+            Ib = 0.5 * fabs(an) * (ql - qr) * Fb;
+        }
+    } else {   // Burgers
+        ab = 0.5 * ql * fr.n[0] * Fb;
+        bb = 0.5 * qr * fr.n[0] * Fb;
+        if (P.lxf) {
+            const double al = fabs(ql), ar = fabs(qr);
+            const bool left = ar < al;   // Base.max(|q_l|, |q_r|)
+            const double lam = left ? al : ar;
+            const double d = 0.5 * lam * inten * Fb;
+            ab += d;
+            bb -= d;
+            const double lb = 0.5 * (ql - qr) * inten * Fb;   // the cotangent of λ
+            if (left) ab += lb * (signbit(ql) ? -1.0 : 1.0);
+            else bb += lb * (signbit(qr) ? -1.0 : 1.0);
+            Ib = 0.5 * lam * (ql - qr) * Fb;
+        }
+    }
+    if (s1 < 0 && bck != FLOU_BC_INFLOW && bck != FLOU_BC_STATE_FIELD) ab += bb;   // the ghost is the trace
+    P.QbL[gid] = ab;
+    if (s1 >= 0) P.QbR[gid] = bb;
+    P.Ibar[gid] = Ib;
+}
+
+// Element VJP of the scalar equations (Cartesian): per direction, with f'(u) = a_d (linear
+// advection) or u (Burgers), the strong form F̃ = Ja f(u) gives ū += -Ja f'(u) Σ_r Ds(r, pos) w_r;
+// the split form with the arithmetic-mean two-point flux F♯ = (f(u_i) + f(u_j))/2 gives
+// ū_i += -Ja f'(u_i) (½ Σ_(j≠i) (D♯_ij w_i + D♯_ji w_j) + D♯_ii w_i).  Then the trace cotangents
+// (G: through l at every node), the stage combination and dJ/dc as for the Euler kernels.
+template <int DIM, int N, int EQ, bool SPLIT, bool G = false>
+__global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_scalar_kernel(AdjElemParams P) {
+    using S = Shape<DIM, N>;
+    constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD;
+    extern __shared__ double smem[];
+    double* sops = smem;
+    double* sw = sops + S::NOPS;
+    const int tid = threadIdx.x;
+    for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
+    const int e0 = blockIdx.x * S::EPB;
+    const int el = tid / NPE, i = tid - el * NPE;
+    const int e = e0 + el;
+    const bool active = (tid < NN) && (e < P.nelem);
+    const int64_t gi = (int64_t)e * NPE + i;
+    double ain = 0.0;
+    if (active) {
+        ain = P.Ain[gi];
+        sw[tid] = P.invJ[e] * P.s_lam * ain;
+    }
+    __syncthreads();
+    if (!active) return;
+    const double u = P.U[gi];
+    const double* Ds = sops;
+    const double* Dsh = sops + N * N;
+    const double* lv = sops + 2 * N * N;
+    double qb = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int pos, line;
+        tp_coords<DIM>(N, i, d, pos, line);
+        double Gs = 0.0;
+        if constexpr (SPLIT) {
+            const double wi = sw[tid];
+            double acc = 0.0;
+#pragma unroll
+            for (int r = 0; r < N; ++r) {
+                if (r == pos) continue;
+                const int j = el * NPE + tp_node<DIM>(N, d, line, r);
+                acc = fma(Dsh[pos + r * N], wi, fma(Dsh[r + pos * N], sw[j], acc));
+            }
+            Gs = fma(Dsh[pos + pos * N], wi, 0.5 * acc);
+        } else {
+#pragma unroll
+            for (int r = 0; r < N; ++r) Gs = fma(Ds[r + pos * N], sw[el * NPE + tp_node<DIM>(N, d, line, r)], Gs);
+        }
+        const double fp = EQ == FLOU_EQ_LINEAR_ADVECTION ? P.adv[d] : u;
+        qb = fma(-P.Ja[e * DIM + d] * fp, Gs, qb);
+#pragma unroll
+        for (int sd = 0; sd < 2; ++sd) {
+            if (!G && pos != (sd ? N - 1 : 0)) continue;
+            const int fk = 2 * d + sd;
+            const int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            const double* src = (pk & 1) ? P.QbR : P.QbL;
+            const int64_t o = (int64_t)(pk >> 1) * NFD + line;
+            if (!index_ok(o, P.nfdofs, P.status, e)) continue;
+            qb = fma(G ? lv[sd * N + pos] : 1.0, __ldcg(src + o), qb);
+        }
+    }
+    double o = fma(P.alpha, ain, qb);
+    if (P.readB) o = fma(P.beta, P.B[gi], o);
+    if (P.writeB) {
+        double b = P.delta_B * ain;
+        if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[gi], b);
+        P.B[gi] = b;
+    }
+    P.Aout[gi] = o;
+    if (P.K) P.K[gi] = fma(P.kA, ain, P.kB * o);
+    if (P.cbar && i == 0) {   // intensity (c1 + c2)/2: each side gets half, a boundary face all
+        double acc = 0.0;
+        for (int fk = 0; fk < 2 * DIM; ++fk) {
+            const int fc = P.elem_face[e * 2 * DIM + fk] >> 1;
+            if (!index_ok((int64_t)fc * NFD + NFD - 1, P.nfdofs, P.status, e)) continue;
+            const double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+            for (int mm = 0; mm < NFD; ++mm) acc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * NFD + mm), acc);
+        }
+        P.cbar[e] += acc;
+    }
+}
+
+// Scalar equations: eq FLOU_EQ_LINEAR_ADVECTION (1D-3D) or FLOU_EQ_BURGERS (1D).
+cudaError_t launch_adj_scalar(int dim, int eq, int n, bool split, bool gauss, int grid, int tb, const AdjFaceParams& F,
+                              const AdjElemParams& P, cudaStream_t s);
 
 // Launchers, one translation unit each (explicit instantiations of the templates above).
 // curv: the general-geometry kernels (2D and 3D); gauss: the interpolated traces and full-line

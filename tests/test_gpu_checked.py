@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 SUITES = ["tests/test_gpu_parity.py", "tests/test_gpu_unstructured.py", "tests/test_gpu_batch.py",
-          "tests/test_gpu_adjoint.py", "tests/test_gpu_adjoint_batch.py", "tests/test_gpu_limiter.py",
+          "tests/test_gpu_adjoint.py", "tests/test_gpu_adjoint_scalar.py", "tests/test_gpu_adjoint_batch.py", "tests/test_gpu_limiter.py",
           "tests/test_gpu_cfl.py", "tests/test_gpu_lowstorage.py", "tests/test_zz_no_alloc.py"]
 
 
