@@ -69,7 +69,7 @@ int fv_kind(const flou_ctx* c) { return flux_kind(c->fvflux, c->fvavg); }
 // The scalar equations (linear advection, Burgers): the strong form on either node set or the
 // split form with the arithmetic-mean two-point flux, the LxF or central interface flux,
 // Cartesian geometry.
-int adj_supported_scalar(flou_ctx* c, bool batched) {
+int adj_supported_scalar(flou_ctx* c) {
     const flou_config& k = c->cfg;
     const bool vol = k.volume_op == FLOU_OP_STRONG ||
                      (k.volume_op == FLOU_OP_SPLIT && k.twopoint_flux == FLOU_TP_STD_AVERAGE);
@@ -81,15 +81,12 @@ int adj_supported_scalar(flou_ctx* c, bool batched) {
                                                  "StdAverage interface flux");
     if (c->curv)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the scalar equations covers Cartesian geometry");
-    if (batched && c->lsrk_s)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint steps with SSP-RK3 (flou_set_integrator 0)");
     return FLOU_OK;
 }
 
-// batched: the batched adjoint, whose lockstep sweep steps with SSP-RK3 and no limiter.
-int adj_supported(flou_ctx* c, bool batched = false) {
+int adj_supported(flou_ctx* c) {
     const flou_config& k = c->cfg;
-    if (k.equation != FLOU_EQ_EULER) return adj_supported_scalar(c, batched);
+    if (k.equation != FLOU_EQ_EULER) return adj_supported_scalar(c);
     bool vol = k.volume_op == FLOU_OP_STRONG ||
                ((k.volume_op == FLOU_OP_SPLIT || k.volume_op == FLOU_OP_HYBRID) &&
                 (k.twopoint_flux == FLOU_TP_CHANDRASHEKAR || k.twopoint_flux == FLOU_TP_KENNEDY_GRUBER ||
@@ -120,11 +117,6 @@ int adj_supported(flou_ctx* c, bool batched = false) {
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid adjoint tile of the Kennedy-Gruber flux at 3D p=7 "
                                                      "exceeds shared memory");
     }
-    if (batched && c->limiter)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint does not differentiate the limiter "
-                                                 "(flou_set_limiter 0)");
-    if (batched && c->lsrk_s)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the batched adjoint steps with SSP-RK3 (flou_set_integrator 0)");
     return FLOU_OK;
 }
 
@@ -304,6 +296,137 @@ struct Schedule {
     }
 };
 
+// ---- one time step, forward and reverse, for both solvers ----
+// SSP-RK3 (Shu-Osher) or the context's 2N-storage method; with the Zhang-Shu limiter after every
+// stage when the context has it.  A reverse step keeps the step's stage states: SSP-RK3 U1, U2
+// (with the limiter also the states before it, V1, V2, V3); a 2N-storage method u_1 .. u_(s-1)
+// (with the limiter also v_1 .. v_s).
+bool has_limiter(const flou_ctx* c) { return c->limiter == FLOU_LIMITER_ZHANG_SHU; }
+
+int stage_count(const flou_ctx* c) {
+    const int s = c->lsrk_s;
+    return s ? (has_limiter(c) ? 2 * s - 1 : s - 1) : (has_limiter(c) ? 5 : 2);
+}
+
+// One 2N-storage stage (0-based st) from u: k = A_st k + dt L(u) in K, out = u + B_st k.
+int lsrk_stage(flou_ctx* c, cudaStream_t s, double dt, const double* u, double* K, double* out, int st, double* Fn) {
+    return ctx_stage(c, s, u, K, out, 3, dt, st == 0 ? 0.0 : c->lsrk_A[st], c->lsrk_B[st], Fn);
+}
+
+int limit_if(flou_ctx* c, cudaStream_t s, double* Q) { return has_limiter(c) ? ctx_limit(c, s, Q) : FLOU_OK; }
+
+// dst <- the limited copy of src
+int limited_copy(flou_ctx* c, cudaStream_t s, double* dst, const double* src) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, (size_t)c->ndofs * c->nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return ctx_cuda_fail(c, e, "stage copy");
+    return limit_if(c, s, dst);
+}
+
+// k steps in place; R is a state-sized register (the SSP-RK3 stage, the 2N-storage k).
+int advance_steps(flou_ctx* c, cudaStream_t s, double dt, double* Q, double* R, double* Fn, int k) {
+    for (int i = 0; i < k; ++i) {
+        int r;
+        if (c->lsrk_s) {
+            for (int st = 0; st < c->lsrk_s; ++st) {
+                if ((r = lsrk_stage(c, s, dt, Q, R, Q, st, Fn))) return r;
+                if ((r = limit_if(c, s, Q))) return r;
+            }
+        } else {
+            if ((r = ctx_stage(c, s, Q, Q, R, 1, dt, 0.0, 1.0, Fn))) return r;
+            if ((r = limit_if(c, s, R))) return r;
+            if ((r = ctx_stage(c, s, R, Q, R, 2, dt, 0.75, 0.25, Fn))) return r;
+            if ((r = limit_if(c, s, R))) return r;
+            if ((r = ctx_stage(c, s, R, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fn))) return r;
+            if ((r = limit_if(c, s, Q))) return r;
+        }
+    }
+    return FLOU_OK;
+}
+
+// The stage states of the step from X into SX (stage_count buffers) with the register K; for a
+// 2N-storage method and seedT set, also the step's result U^n (the functional's state).
+int stage_states(flou_ctx* c, cudaStream_t s, double dt, const double* X, double* const* SX, double* K, double* Fn,
+                 double* seedT) {
+    int r;
+    const int ns = c->lsrk_s;
+    if (ns && has_limiter(c)) {   // v_(i+1) from u_i, u_(i+1) its limited copy
+        const double* u = X;
+        for (int st = 0; st < ns; ++st) {
+            double* v = SX[ns - 1 + st];
+            if ((r = lsrk_stage(c, s, dt, u, K, v, st, Fn))) return r;
+            if (st + 1 < ns && (r = limited_copy(c, s, SX[st], v))) return r;
+            u = SX[st];
+        }
+        if (seedT && (r = limited_copy(c, s, seedT, SX[2 * ns - 2]))) return r;
+    } else if (ns) {
+        const double* u = X;
+        for (int st = 0; st + 1 < ns; ++st) {
+            if ((r = lsrk_stage(c, s, dt, u, K, SX[st], st, Fn))) return r;
+            u = SX[st];
+        }
+        if (seedT && (r = lsrk_stage(c, s, dt, u, K, seedT, ns - 1, Fn))) return r;
+    } else if (has_limiter(c)) {   // V1, U1 = L(V1), V2, U2 = L(V2), V3
+        if ((r = ctx_stage(c, s, X, X, SX[2], 1, dt, 0.0, 1.0, Fn))) return r;
+        if ((r = limited_copy(c, s, SX[0], SX[2]))) return r;
+        if ((r = ctx_stage(c, s, SX[0], X, SX[3], 2, dt, 0.75, 0.25, Fn))) return r;
+        if ((r = limited_copy(c, s, SX[1], SX[3]))) return r;
+        if ((r = ctx_stage(c, s, SX[1], X, SX[4], 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fn))) return r;
+    } else {
+        if ((r = ctx_stage(c, s, X, X, SX[0], 1, dt, 0.0, 1.0, Fn))) return r;
+        if ((r = ctx_stage(c, s, SX[0], X, SX[1], 2, dt, 0.75, 0.25, Fn))) return r;
+    }
+    return FLOU_OK;
+}
+
+// SSP-RK3: the step's result U^n into T from its stage states (the 2N-storage methods form it in
+// stage_states).
+int final_state(flou_ctx* c, cudaStream_t s, double dt, const double* X, double* const* SX, double* T, double* Fn) {
+    if (has_limiter(c)) return limited_copy(c, s, T, SX[4]);   // U^n = L(V3)
+    return ctx_stage(c, s, SX[1], X, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fn);
+}
+
+// The adjoint of one step: A holds Ū^(k+1) on entry and Ū^k on exit; T and B are scratch.
+// SSP-RK3 (Ū2 = ⅔V̄3 + VJP(U2; ⅔dt V̄3), B = ⅓V̄3; Ū1 = ¼V̄2 + VJP(U1; ¼dt V̄2), B += ¾V̄2;
+// Ū0 = V̄1 + B + VJP(U0; dt V̄1), with V̄ = Ū without the limiter, its VJP at V with it).
+// A 2N-storage step (Williamson form; stage i from u_i: k_i = A_i k_(i-1) + dt L(u_i),
+// u_(i+1) = u_i + B_i k_i, A_0 = 0), reverse stage i with k̄ = k̄_i + B_i Ū(i+1) in T:
+//   Ū_i = Ū_(i+1) + dt (∂L/∂u)(u_i)ᵀ k̄,  then T = A_i k̄ + B_(i-1) Ū_i for stage i-1
+// (the element kernel's epilogue forms the next k̄ in place); the last stage starts from
+// k̄ = B_(s-1) Ū; A_0 = 0 leaves nothing to carry into the previous step.  With the limiter
+// (u_(i+1) = L(v_(i+1))), Ū_(i+1) first becomes V̄_(i+1) through the limiter's VJP, which also
+// adds B_i V̄_(i+1) to the register (the epilogue then carries A_i k̄ alone).
+int reverse_stages(flou_ctx* c, AdjBuffers& ab, cudaStream_t s, double dt, const double* X, double* const* SX,
+                   double* A, double* T, double* B, double* cbar) {
+    int r;
+    const bool lim = has_limiter(c);
+    const int ns = c->lsrk_s;
+    if (ns) {
+        if (lim) {
+            if ((r = ctx_limit_vjp(c, s, SX[2 * ns - 2], A, T, 0.0, c->lsrk_B[ns - 1]))) return r;
+        } else {
+            const int64_t n = c->ndofs * c->nv;
+            scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(T, A, c->lsrk_B[ns - 1], n);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint register");
+        }
+        for (int i = ns - 1; i >= 0; --i) {
+            const double* u = i == 0 ? X : SX[i - 1];
+            if ((r = adj_stage(c, ab, s, u, T, A, A, cbar, dt, 0.0, 1.0, 1, 0, 0.0, 0.0, i > 0 ? T : nullptr,
+                               c->lsrk_A[i], (i > 0 && !lim) ? c->lsrk_B[i - 1] : 0.0)))
+                return r;
+            if (lim && i > 0 && (r = ctx_limit_vjp(c, s, SX[ns - 2 + i], A, T, 1.0, c->lsrk_B[i - 1]))) return r;
+        }
+        return FLOU_OK;
+    }
+    if (lim && (r = ctx_limit_vjp(c, s, SX[4], A, nullptr, 0.0, 0.0))) return r;
+    if ((r = adj_stage(c, ab, s, SX[1], A, T, B, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
+        return r;
+    if (lim && (r = ctx_limit_vjp(c, s, SX[3], T, nullptr, 0.0, 0.0))) return r;
+    if ((r = adj_stage(c, ab, s, SX[0], T, A, B, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
+    if (lim && (r = ctx_limit_vjp(c, s, SX[2], A, nullptr, 0.0, 0.0))) return r;
+    return adj_stage(c, ab, s, X, A, A, B, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0);
+}
+
 // Single-instance reverse sweep on four streams.  Two forward streams `sf[0..1]` take turns: each
 // places snapshots and recomputes the state U^k that a reverse step needs, into one of NB X
 // buffers; the stage stream `ss` forms that step's two stage states U^(k,1), U^(k,2); the adjoint
@@ -328,10 +451,6 @@ struct Solver {
     double* X[NB] = {};
     // stage states of a reverse step: SSP-RK3 U^(k,1), U^(k,2); a 2N-storage method u_1 .. u_(s-1)
     std::vector<double*> SX[NB];
-    int lsrk = 0;                     // stages of the 2N-storage method (0: SSP-RK3)
-    // the Zhang-Shu stage limiter: the stage states come in pairs, before (V) and after (U) the
-    // limiter: SSP-RK3 {U1, U2, V1, V2, V3}; 2N-storage {u_1 .. u_(s-1), v_1 .. v_s}
-    bool lim = false;
     double* Kss = nullptr;            // the stage stream's 2N register
     cudaEvent_t ready[NB] = {}, sready[NB] = {}, done[NB] = {};
     bool used[NB] = {};
@@ -367,35 +486,10 @@ struct Solver {
         if ((r = cuda(cudaMemcpyAsync(dst, slot[si], bytes, cudaMemcpyDeviceToDevice, sf[f]), "state copy"))) return r;
         return record(read[(size_t)si * NF + f], sf[f]);
     }
-    // One 2N-storage stage (0-based st) from u on stream s: k = A_st k + dt L(u) in K, out = u + B_st k.
-    int lsrk_stage(cudaStream_t s, const double* u, double* K, double* out, int st, double* Fn) {
-        return ctx_stage(c, s, u, K, out, 3, dt, st == 0 ? 0.0 : c->lsrk_A[st], c->lsrk_B[st], Fn);
-    }
-    int limit(cudaStream_t s, double* Q) { return lim ? ctx_limit(c, s, Q) : FLOU_OK; }
-    int advance(int f, double* Q, int k) {   // k steps in place on forward stream f
-        for (int i = 0; i < k; ++i) {
-            int r;
-            if (lsrk) {   // F1[f] is the stream's 2N register
-                for (int st = 0; st < lsrk; ++st) {
-                    if ((r = lsrk_stage(sf[f], Q, F1[f], Q, st, Fnf[f]))) return r;
-                    if ((r = limit(sf[f], Q))) return r;
-                }
-            } else {
-                if ((r = ctx_stage(c, sf[f], Q, Q, F1[f], 1, dt, 0.0, 1.0, Fnf[f]))) return r;
-                if ((r = limit(sf[f], F1[f]))) return r;
-                if ((r = ctx_stage(c, sf[f], F1[f], Q, F1[f], 2, dt, 0.75, 0.25, Fnf[f]))) return r;
-                if ((r = limit(sf[f], F1[f]))) return r;
-                if ((r = ctx_stage(c, sf[f], F1[f], Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fnf[f]))) return r;
-                if ((r = limit(sf[f], Q))) return r;
-            }
-            ++advances;
-        }
-        return FLOU_OK;
-    }
-    // dst <- the limited copy of src on stream s
-    int limited_copy(cudaStream_t s, double* dst, const double* src) {
-        int r = cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s), "stage copy");
-        return r ? r : limit(s, dst);
+    int advance(int f, double* Q, int k) {   // k steps in place on forward stream f (F1[f]: its register)
+        int r = advance_steps(c, sf[f], dt, Q, F1[f], Fnf[f], k);
+        advances += k;
+        return r;
     }
     // slot sj <- U^(i0+m) advanced from slot si (a snapshot placement)
     int place(int sj, int si, int m) {
@@ -419,59 +513,25 @@ struct Solver {
         if ((r = copy_from(f, X[b], si))) return r;
         if ((r = advance(f, X[b], k))) return r;
         if ((r = record(ready[b], sf[f]))) return r;
-        // the stage stream: U^(k,1) and U^(k,2), or u_1 .. u_(s-1) (ready[b] comes after the forward
-        // stream's wait for done[b], so the stage buffers are free again)
+        // the stage stream (ready[b] comes after the forward stream's wait for done[b], so the stage
+        // buffers are free again); for the last step of a 2N-storage method also U^n, into T, which
+        // the adjoint stream has not used yet
         if ((r = wait(ss, ready[b]))) return r;
         const bool seed = kstep == nsteps - 1 && !seeded;
-        if (lsrk && lim) {   // v_(i+1) from u_i, u_(i+1) its limited copy
-            const double* u = X[b];
-            for (int st = 0; st < lsrk; ++st) {
-                double* v = SX[b][lsrk - 1 + st];
-                if ((r = lsrk_stage(ss, u, Kss, v, st, Fns))) return r;
-                if (st + 1 < lsrk && (r = limited_copy(ss, SX[b][st], v))) return r;
-                u = SX[b][st];
-            }
-            // the last step: U^n = L(v_s), which the functional reads (the adjoint stream has not
-            // used T yet)
-            if (seed && (r = limited_copy(ss, T, SX[b][2 * lsrk - 2]))) return r;
-        } else if (lsrk) {
-            const double* u = X[b];
-            for (int st = 0; st + 1 < lsrk; ++st) {
-                if ((r = lsrk_stage(ss, u, Kss, SX[b][st], st, Fns))) return r;
-                u = SX[b][st];
-            }
-            // the last step: U^n, which the functional reads, from the same register (the adjoint
-            // stream has not used T yet)
-            if (seed && (r = lsrk_stage(ss, u, Kss, T, lsrk - 1, Fns))) return r;
-        } else if (lim) {   // V1, U1 = L(V1), V2, U2 = L(V2), V3
-            if ((r = ctx_stage(c, ss, X[b], X[b], SX[b][2], 1, dt, 0.0, 1.0, Fns))) return r;
-            if ((r = limited_copy(ss, SX[b][0], SX[b][2]))) return r;
-            if ((r = ctx_stage(c, ss, SX[b][0], X[b], SX[b][3], 2, dt, 0.75, 0.25, Fns))) return r;
-            if ((r = limited_copy(ss, SX[b][1], SX[b][3]))) return r;
-            if ((r = ctx_stage(c, ss, SX[b][1], X[b], SX[b][4], 2, dt, 1.0 / 3.0, 2.0 / 3.0, Fns))) return r;
-        } else {
-            if ((r = ctx_stage(c, ss, X[b], X[b], SX[b][0], 1, dt, 0.0, 1.0, Fns))) return r;
-            if ((r = ctx_stage(c, ss, SX[b][0], X[b], SX[b][1], 2, dt, 0.75, 0.25, Fns))) return r;
-        }
+        if ((r = stage_states(c, ss, dt, X[b], SX[b].data(), Kss, Fns, seed && c->lsrk_s ? T : nullptr))) return r;
         if ((r = record(sready[b], ss))) return r;
         if ((r = wait(sa, sready[b]))) return r;
-        if ((r = (lsrk ? backward_step_2n(kstep, b) : backward_step(kstep, b)))) return r;
+        if ((r = backward_step(kstep, b))) return r;
         used[b] = true;
         return record(done[b], sa);
     }
     // Reverse one step from U^k (X[b]) and its stage states: the adjoint of U^(k+1) is in A on
-    // entry and that of U^k on exit (adjoint stream).  With the limiter, each stage's adjoint first
-    // goes through the limiter's VJP at that stage's state before the limiter.
+    // entry and that of U^k on exit (adjoint stream).
     int backward_step(int k, int b) {
         int r;
-        double *Xk = X[b], *S1 = SX[b][0], *S2 = SX[b][1];
-        if (!seeded) {   // the last step: form U^n, the functional and its gradient seed
+        if (!seeded) {   // the last step: U^n, the functional and its gradient seed
             if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
-            if (lim) {
-                if ((r = limited_copy(sa, T, SX[b][4]))) return r;   // U^n = L(V3)
-            } else if ((r = ctx_stage(c, sa, S2, Xk, T, 2, dt, 1.0 / 3.0, 2.0 / 3.0))) {
-                return r;   // U^n
-            }
+            if (!c->lsrk_s && (r = final_state(c, sa, dt, X[b], SX[b].data(), T, nullptr))) return r;
             functional_kernel<<<nblk, 256, 0, sa>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
             if ((r = cuda(cudaGetLastError(), "functional"))) return r;
             if ((r = cuda(cudaMemcpyAsync(h_partial, partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, sa),
@@ -479,49 +539,7 @@ struct Solver {
                 return r;
             seeded = true;
         }
-        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][4], A, nullptr, 0.0, 0.0))) return r;
-        if ((r = adj_stage(c, ab, sa, S2, A, T, Bacc, cbar, (2.0 / 3.0) * dt, 2.0 / 3.0, 0.0, 0, 1, 0.0, 1.0 / 3.0)))
-            return r;
-        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][3], T, nullptr, 0.0, 0.0))) return r;
-        if ((r = adj_stage(c, ab, sa, S1, T, A, Bacc, cbar, 0.25 * dt, 0.25, 0.0, 0, 1, 1.0, 0.75))) return r;
-        if (lim && (r = ctx_limit_vjp(c, sa, SX[b][2], A, nullptr, 0.0, 0.0))) return r;
-        if ((r = adj_stage(c, ab, sa, Xk, A, A, Bacc, cbar, dt, 1.0, 1.0, 1, 0, 0.0, 0.0))) return r;
-        return FLOU_OK;
-    }
-    // The same for a 2N-storage step (Williamson form; stage i from u_i: k_i = A_i k_(i-1) +
-    // dt L(u_i), u_(i+1) = u_i + B_i k_i, A_0 = 0).  Reverse stage i with k̄ = k̄_i + B_i Ū(i+1) in T:
-    //   Ū_i = Ū_(i+1) + dt (∂L/∂u)(u_i)ᵀ k̄,  then T = A_i k̄ + B_(i-1) Ū_i for stage i-1
-    // (the element kernel's epilogue forms the next k̄ in place).  The last stage starts from
-    // k̄ = B_(s-1) Ū; A_0 = 0 leaves nothing to carry into the previous step.  With the limiter
-    // (u_(i+1) = L(v_(i+1))), Ū_(i+1) first becomes V̄_(i+1) through the limiter's VJP, which also
-    // adds B_i V̄_(i+1) to the register (the epilogue then carries A_i k̄ alone).
-    int backward_step_2n(int k, int b) {
-        int r;
-        if (!seeded) {   // U^n was formed in T by the stage stream
-            if (k != nsteps - 1) return ctx_fail(c, FLOU_ERR_STATE, "adjoint schedule out of order");
-            functional_kernel<<<nblk, 256, 0, sa>>>(T, rho_t, w, c->ndofs, c->nv, A, partial);
-            if ((r = cuda(cudaGetLastError(), "functional"))) return r;
-            if ((r = cuda(cudaMemcpyAsync(h_partial, partial, nblk * sizeof(double), cudaMemcpyDeviceToHost, sa),
-                          "functional")))
-                return r;
-            seeded = true;
-        }
-        if (lim) {
-            if ((r = ctx_limit_vjp(c, sa, SX[b][2 * lsrk - 2], A, T, 0.0, c->lsrk_B[lsrk - 1]))) return r;
-        } else {
-            const int64_t n = c->ndofs * c->nv;
-            scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, sa>>>(T, A, c->lsrk_B[lsrk - 1], n);
-            if ((r = cuda(cudaGetLastError(), "adjoint register"))) return r;
-        }
-        for (int i = lsrk - 1; i >= 0; --i) {
-            const double* u = i == 0 ? X[b] : SX[b][i - 1];
-            if ((r = adj_stage(c, ab, sa, u, T, A, A, cbar, dt, 0.0, 1.0, 1, 0, 0.0, 0.0, i > 0 ? T : nullptr,
-                               c->lsrk_A[i], (i > 0 && !lim) ? c->lsrk_B[i - 1] : 0.0)))
-                return r;
-            if (lim && i > 0 && (r = ctx_limit_vjp(c, sa, SX[b][lsrk - 2 + i], A, T, 1.0, c->lsrk_B[i - 1])))
-                return r;
-        }
-        return FLOU_OK;
+        return reverse_stages(c, ab, sa, dt, X[b], SX[b].data(), A, T, Bacc, cbar);
     }
     // U^i0 is in slot[si]; ns free snapshot slots may be used; reverses steps i0 .. i0+n-1.
     int rev(int i0, int n, int ns, int si) {
@@ -551,10 +569,12 @@ struct Solver {
 // ordered, while instances on other streams overlap with it.  The step scratch (X, S1, S2, T, B
 // and the face cotangents) is per stream, sized for the largest instance on that stream; the
 // adjoint state of instance i lives in the caller's gradient buffer and its initial state is
-// read from the caller's Q0 (snapshot 0).
+// read from the caller's Q0 (snapshot 0).  Each instance steps with its own context's method
+// (SSP-RK3 or its 2N-storage method, with or without the limiter).
 struct BatchSolver {
     struct Scratch {
-        double *X = nullptr, *S1 = nullptr, *S2 = nullptr, *T = nullptr, *B = nullptr;
+        double *X = nullptr, *T = nullptr, *B = nullptr, *K = nullptr;   // K: the stepping register
+        std::vector<double*> SX;                                          // stage states
         AdjBuffers ab;
     };
     int n = 0, nsteps = 0;
@@ -592,16 +612,8 @@ struct BatchSolver {
         return e == cudaSuccess ? FLOU_OK : fail_at(i, ctx_cuda_fail(c[i], e, "state copy"));
     }
     int advance(double* Q, int k, int i) {
-        flou_ctx* ci = c[i];
-        double* S1 = W(i).S1;
-        cudaStream_t s = S(i);
-        for (int j = 0; j < k; ++j) {
-            int r;
-            if ((r = ctx_stage(ci, s, Q, Q, S1, 1, dt[i], 0.0, 1.0))) return fail_at(i, r);
-            if ((r = ctx_stage(ci, s, S1, Q, S1, 2, dt[i], 0.75, 0.25))) return fail_at(i, r);
-            if ((r = ctx_stage(ci, s, S1, Q, Q, 2, dt[i], 1.0 / 3.0, 2.0 / 3.0))) return fail_at(i, r);
-        }
-        return FLOU_OK;
+        int r = advance_steps(c[i], S(i), dt[i], Q, W(i).K, nullptr, k);
+        return r ? fail_at(i, r) : FLOU_OK;
     }
     // U^k of instance i is in its stream's X; A[i] holds the adjoint of U^(k+1) on entry and
     // that of U^k on exit.
@@ -611,11 +623,12 @@ struct BatchSolver {
         cudaStream_t s = S(i);
         double h = dt[i];
         int r;
-        if ((r = ctx_stage(ci, s, w_.X, w_.X, w_.S1, 1, h, 0.0, 1.0))) return fail_at(i, r);
-        if ((r = ctx_stage(ci, s, w_.S1, w_.X, w_.S2, 2, h, 0.75, 0.25))) return fail_at(i, r);
-        if (!seeded[i]) {
+        const bool seed = !seeded[i];
+        if ((r = stage_states(ci, s, h, w_.X, w_.SX.data(), w_.K, nullptr, seed && ci->lsrk_s ? w_.T : nullptr)))
+            return fail_at(i, r);
+        if (seed) {
             if (k != nsteps - 1) return fail_at(i, ctx_fail(ci, FLOU_ERR_STATE, "adjoint schedule out of order"));
-            if ((r = ctx_stage(ci, s, w_.S2, w_.X, w_.T, 2, h, 1.0 / 3.0, 2.0 / 3.0))) return fail_at(i, r);
+            if (!ci->lsrk_s && (r = final_state(ci, s, h, w_.X, w_.SX.data(), w_.T, nullptr))) return fail_at(i, r);
             functional_kernel<<<nblk[i], 256, 0, s>>>(w_.T, rho_t[i], w[i], ci->ndofs, ci->nv, A[i], partial + poff[i]);
             cudaError_t e = cudaGetLastError();
             if (e == cudaSuccess)
@@ -624,13 +637,7 @@ struct BatchSolver {
             if (e != cudaSuccess) return fail_at(i, ctx_cuda_fail(ci, e, "functional"));
             seeded[i] = 1;
         }
-        if ((r = adj_stage(ci, w_.ab, s, w_.S2, A[i], w_.T, w_.B, cbar[i], (2.0 / 3.0) * h, 2.0 / 3.0, 0.0, 0, 1,
-                           0.0, 1.0 / 3.0)))
-            return fail_at(i, r);
-        if ((r = adj_stage(ci, w_.ab, s, w_.S1, w_.T, A[i], w_.B, cbar[i], 0.25 * h, 0.25, 0.0, 0, 1, 1.0, 0.75)))
-            return fail_at(i, r);
-        if ((r = adj_stage(ci, w_.ab, s, w_.X, A[i], A[i], w_.B, cbar[i], h, 1.0, 1.0, 1, 0, 0.0, 0.0)))
-            return fail_at(i, r);
+        if ((r = reverse_stages(ci, w_.ab, s, h, w_.X, w_.SX.data(), A[i], w_.T, w_.B, cbar[i]))) return fail_at(i, r);
         return FLOU_OK;
     }
     // Every instance's U^i0 is in snapshot si; ns free snapshots; reverses steps i0 .. i0+m-1.
@@ -727,15 +734,13 @@ int32_t flou_adjoint_solve(flou_ctx* c, const double* Q0, double dt, int32_t nst
     };
     S.slot.assign(nslots + 1, nullptr);
     for (int i = 0; i <= nslots; ++i) dalloc(&S.slot[i], S.bytes);
-    S.lsrk = c->lsrk_s;
-    S.lim = c->limiter == FLOU_LIMITER_ZHANG_SHU;
-    const int nst = S.lsrk ? (S.lim ? 2 * S.lsrk - 1 : S.lsrk - 1) : (S.lim ? 5 : 2);
+    const int nst = stage_count(c);
     for (int i = 0; i < Solver::NB; ++i) {
         dalloc(&S.X[i], S.bytes);
         S.SX[i].assign(nst, nullptr);
         for (int j = 0; j < nst; ++j) dalloc(&S.SX[i][j], S.bytes);
     }
-    if (S.lsrk) dalloc(&S.Kss, S.bytes);
+    if (c->lsrk_s) dalloc(&S.Kss, S.bytes);
     double** bufs[] = {&S.Bacc, &S.T};
     for (double** b : bufs) dalloc(b, S.bytes);
     for (int f = 0; f < Solver::NF; ++f) {
@@ -833,7 +838,7 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
     for (int i = 0; i < n; ++i) {
         flou_ctx* c = ctxs[i];
         int r = ctx_prepare(c);
-        if (!r) r = adj_supported(c, true);
+        if (!r) r = adj_supported(c);
         if (!r && (!Q0[i] || !rho_target[i] || !weights[i] || !dJdQ0[i] || !std::isfinite(dt[i])))
             r = ctx_fail(c, FLOU_ERR_ARG, "invalid arguments");
         if (!r && dJdc && dJdc[i] && !c->d_c)
@@ -867,7 +872,8 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
     for (int i = 0; i < n; ++i) order[i] = i;
     std::sort(order.begin(), order.end(), [&](int a, int b) { return B.bytes[a] > B.bytes[b]; });
     std::vector<double> load(S, 0.0);
-    std::vector<size_t> maxb(S, 0), maxf(S, 0), maxfd(S, 0);
+    std::vector<size_t> maxb(S, 0), maxf(S, 0), maxfd(S, 0), maxst(S, 0);
+    std::vector<char> any2n(S, 0);   // a stream with a 2N-storage instance needs its own register
     B.stream_of.assign(n, 0);
     for (int i : order) {
         int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
@@ -876,9 +882,12 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
         maxb[s] = std::max(maxb[s], B.bytes[i]);
         maxf[s] = std::max(maxf[s], (size_t)ctxs[i]->nfdofs * ctxs[i]->nv);
         maxfd[s] = std::max(maxfd[s], (size_t)ctxs[i]->nfdofs);
+        maxst[s] = std::max(maxst[s], (size_t)stage_count(ctxs[i]));
+        if (ctxs[i]->lsrk_s) any2n[s] = 1;
     }
     size_t fixed = npart * sizeof(double);
-    for (int s = 0; s < S; ++s) fixed += 5 * maxb[s] + (2 * maxf[s] + maxfd[s]) * sizeof(double);
+    for (int s = 0; s < S; ++s)
+        fixed += (3 + maxst[s] + any2n[s]) * maxb[s] + (2 * maxf[s] + maxfd[s]) * sizeof(double);
     if (budget_bytes < 0 || (size_t)budget_bytes < fixed)
         return fail_all(FLOU_ERR_ARG, "device-memory budget below the " + std::to_string(fixed) +
                                           " bytes of step scratch the batch needs");
@@ -895,8 +904,14 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
     B.scr.resize(S);
     for (int s = 0; s < S; ++s) {
         BatchSolver::Scratch& w = B.scr[s];
-        double** bufs[] = {&w.X, &w.S1, &w.S2, &w.T, &w.B};
+        double** bufs[] = {&w.X, &w.T, &w.B};
         for (double** b : bufs) dalloc((void**)b, maxb[s]);
+        w.SX.assign(maxst[s], nullptr);
+        for (double*& b : w.SX) dalloc((void**)&b, maxb[s]);
+        // SSP-RK3 steps and forms its stage states one after the other on the stream, so its
+        // stepping register can be the first stage state; a 2N-storage register lives on
+        if (any2n[s]) dalloc((void**)&w.K, maxb[s]);
+        else w.K = w.SX[0];
         dalloc((void**)&w.ab.QbL, maxf[s] * sizeof(double));
         dalloc((void**)&w.ab.QbR, maxf[s] * sizeof(double));
         dalloc((void**)&w.ab.Ibar, std::max<size_t>(maxfd[s], 1) * sizeof(double));

@@ -275,7 +275,7 @@ int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_
  *  - periodic, slip-wall, outflow, inflow and boundary-state-field boundaries (fixed external
  *    states are constants of the differentiation);
  *  - SSP-RK3 or the 2N-storage method set by flou_set_integrator, with or without the Zhang-Shu
- *    stage limiter (flou_adjoint_solve_batch: SSP-RK3 without limiter).
+ *    stage limiter (in flou_adjoint_solve_batch each instance with its own).
  * Other contexts (the Kennedy-Gruber 3D p=7 tile of the Gauss-node split and hybrid forms)
  * return FLOU_ERR_UNSUPPORTED.
  * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import flou_cuda as F
-from cases import build, oracle_for
+from cases import build, oracle_for, smooth_euler_state
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -93,3 +93,55 @@ def test_budget_sets_the_snapshots():
         assert J0[k] == J1[k] == J2[k]
         assert torch.equal(g0[k], g1[k]) and torch.equal(g0[k], g2[k])
         assert torch.equal(gc0[k], gc1[k]) and torch.equal(gc0[k], gc2[k])
+
+
+def test_batched_adjoint_with_2n_storage_and_limiter_instances():
+    """Instances stepping with ORK256, with the Zhang-Shu limiter, with both, and plain SSP-RK3
+    in one lockstep sweep (a stream holding a 2N-storage instance keeps its own register): each
+    gradient is bit-identical to its single solve, and the limited 2N-storage one agrees with the
+    dual-number oracle through the same limited method."""
+    from flou_cuda import _lib as L
+    from test_oracle_kat import _dipped_state
+    inst = _instances()
+    m = F.ORK256()
+    eq = F.EulerEquation(2, 1.4)
+    extra = []
+    for k, (lsrk, lim) in enumerate([(True, False), (False, True), (True, True)]):
+        disc = build(2, 4, (3, 3), eq, _lxf())
+        Q0 = _dipped_state(disc, seed=30 + k) if lim else smooth_euler_state(disc, seed=30 + k)
+        c = 1.0 + 0.1 * np.random.default_rng(60 + k).random(disc.mesh.nelements)
+        disc.ctx.set_dissipation(c)
+        if lsrk:
+            disc.ctx.set_integrator(m.A, m.B)
+        if lim:
+            disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.5)
+        rho_t, w = _functional_inputs(disc, 70 + k)
+        dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+        extra.append(dict(disc=disc, Q0=Q0, c=c, rho_t=rho_t, w=w, dt=dt, lsrk=lsrk, lim=lim))
+    inst = inst[:2] + extra
+    nsteps = 6
+    for budget in (8 << 30, None):
+        if budget is None:   # two snapshots: recomputation through the limited / 2N-storage steps
+            with pytest.raises(F.FlouError) as ei:
+                _run_batch(inst, nsteps, 0)
+            budget = int(re.search(r"below the (\d+) bytes", str(ei.value)).group(1)) + 2 * _snap_bytes(inst)
+        J, g, gc, nf, ns = _run_batch(inst, nsteps, budget)
+        for k, x in enumerate(inst):
+            d = x["disc"]
+            g1 = torch.empty_like(g[k])
+            gc1 = torch.empty_like(gc[k])
+            J1, _ = d.ctx.adjoint_solve(_dev(x["Q0"]), x["dt"], nsteps, 3, _dev(x["rho_t"]), _dev(x["w"]), g1, gc1)
+            assert J[k] == J1
+            assert torch.equal(g[k], g1) and torch.equal(gc[k], gc1)
+    x = inst[-1]
+    rng = np.random.default_rng(2)
+    dQ = rng.standard_normal(x["Q0"].shape)
+    dc = rng.standard_normal(x["c"].shape)
+    Jo, dJo = oracle_for(x["disc"]).solve_jvp_lsrk(x["Q0"], dQ, x["c"], dc, x["dt"], nsteps, x["rho_t"], x["w"],
+                                                   m.A, m.B, m.c, minval=0.5, omega_tp=x["disc"].std.omega)
+    ours = np.sum(_host(g[-1]) * dQ) + np.sum(gc[-1].cpu().numpy() * dc)
+    assert abs(J[-1] - Jo) <= 1e-12 * abs(Jo)
+    assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+    for x in extra:
+        x["disc"].ctx.set_limiter(L.LIMITER_NONE)
+        x["disc"].ctx.set_integrator(None)

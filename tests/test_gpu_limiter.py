@@ -115,15 +115,11 @@ def test_flou_style_callbacks():
 
 
 def test_limiter_is_rejected_where_it_is_not_run():
-    """The batched launch and the batched adjoint run no limiter; the single adjoint solve
-    differentiates it (test_gpu_adjoint.py)."""
+    """The batched launch runs no limiter (the adjoint solves differentiate it:
+    test_gpu_adjoint.py, test_gpu_adjoint_batch.py)."""
     disc = _disc(2, op=F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
     disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.1)
     Q = torch.from_numpy(np.ascontiguousarray(_dipped_state(disc, seed=1).T)).cuda()
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        F.adjoint_solve_batch([disc], [Q], [1e-3], 2, 1 << 30, [Q[0].clone()], [Q[0].clone()], [g])
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
     with pytest.raises(F.FlouError):
         F.Batch([disc], [Q], [1e-3])
     adv = build(1, 4, (3,), F.LinearAdvection(1.0), F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))

@@ -93,19 +93,15 @@ def test_shockwave2d_golden_on_device():
     assert rel_linf(Q, ref) <= max(STEP_TOL, 10 * spread)
 
 
-def test_batched_paths_reject_lowstorage():
-    """The batched launch and the batched adjoint step with SSP-RK3 only; the single adjoint
-    solve differentiates the 2N-storage methods (test_gpu_adjoint.py)."""
+def test_batched_launch_rejects_lowstorage():
+    """The batched launch steps with SSP-RK3 only (the single and the batched adjoint solves
+    differentiate the 2N-storage methods: test_gpu_adjoint.py, test_gpu_adjoint_batch.py)."""
     torch = pytest.importorskip("torch")
     from flou_cuda import _lib as L
     disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
     m = F.ORK256()
     disc.ctx.set_integrator(m.A, m.B)
     Q = torch.from_numpy(np.ascontiguousarray(smooth_euler_state(disc, seed=2).T)).cuda()
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        F.adjoint_solve_batch([disc], [Q], [1e-3], 2, 1 << 30, [Q[0].clone()], [Q[0].clone()], [g])
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
     with pytest.raises(F.FlouError):
         F.Batch([disc], [Q], [1e-3])
     with pytest.raises(F.FlouError) as ei:
