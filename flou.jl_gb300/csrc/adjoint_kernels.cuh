@@ -1121,25 +1121,25 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_kernel(AdjElemP
     for (int d = 0; d < DIM; ++d) {
         int pos, line;
         tp_coords<DIM>(N, i, d, pos, line);
-        double G[NV];
+        double Gd[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) G[k] = 0.0;
+        for (int k = 0; k < NV; ++k) Gd[k] = 0.0;
 #pragma unroll
         for (int r = 0; r < N; ++r) {   // Σ_rows Ds(row, pos) w_row  (transpose)
             int j = el * NPE + tp_node<DIM>(N, d, line, r);
             double a = Ds[r + pos * N];
 #pragma unroll
-            for (int k = 0; k < NV; ++k) G[k] = fma(a, sw[k * NN + j], G[k]);
+            for (int k = 0; k < NV; ++k) Gd[k] = fma(a, sw[k * NN + j], Gd[k]);
         }
         if constexpr (CURV) {
 #pragma unroll
             for (int k = 0; k < DIM; ++k) {
                 const double jkd = P.Jan[(k + d * DIM) * P.ndofs + gi];
 #pragma unroll
-                for (int v = 0; v < NV; ++v) Gt[k][v] = fma(jkd, G[v], Gt[k][v]);
+                for (int v = 0; v < NV; ++v) Gt[k][v] = fma(jkd, Gd[v], Gt[k][v]);
             }
         } else {
-            euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, G, -P.Ja[e * DIM + d], qb);
+            euler_flux_vjp<DIM>(d, pr.v, pr.vv, pr.H, g1, Gd, -P.Ja[e * DIM + d], qb);
         }
         // trace cotangents of the faces this node lies on (LGL: the end nodes)
         if constexpr (G) {
@@ -1996,9 +1996,9 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     const int tid = threadIdx.x;
     double dii = Dsh[pos + pos * N];
     if (dii != 0.0) {   // diagonal: F♯(i, i) = F(Q_i)
-        double G[NV];
+        double Gd[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) G[k] = dii * sw[k * NN + tid];
+        for (int k = 0; k < NV; ++k) Gd[k] = dii * sw[k * NN + tid];
         double vv = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
@@ -2007,9 +2007,9 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
             double nrm[DIM];
 #pragma unroll
             for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
-            euler_flux_vjp_n<DIM>(nrm, v, vv, H, g1, G, -1.0, qb);
+            euler_flux_vjp_n<DIM>(nrm, v, vv, H, g1, Gd, -1.0, qb);
         } else {
-            euler_flux_vjp<DIM>(D, v, vv, H, g1, G, -P.Ja[e * DIM + D], qb);
+            euler_flux_vjp<DIM>(D, v, vv, H, g1, Gd, -P.Ja[e * DIM + D], qb);
         }
     }
     int pbase = el * NFD * NPAIR + line * NPAIR;
