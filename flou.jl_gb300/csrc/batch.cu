@@ -1,6 +1,8 @@
 // batch.cu -- many independent discretizations (uneven element counts and orders) advanced
-// together: one persistent launch per SSP-RK3 stage serves every instance from one work
-// queue, and the three stages of a step are replayed as one CUDA graph.
+// together: one persistent launch per stage (SSP-RK3's three, or the instances' common
+// 2N-storage method's) serves every instance from one work queue, and the stages of a step are
+// replayed as one CUDA graph; an instance with the Zhang-Shu limiter gets it after every stage
+// (its own launch in the graph).
 //
 // Work queue of one stage: first every face item of every instance (TB face nodes each), then
 // every element item (G consecutive element tiles of the instance's order, G chosen per order by
@@ -168,6 +170,11 @@ struct flou_batch {
     const BatchKernel* kern = nullptr;
     int blocks_per_sm = 0, order = 0, sms = 0;
     int tiles[MAXN + 1] = {};   // element tiles per work item for n nodes per direction (0: one)
+    // stages of a step: SSP-RK3's three, or the instances' common 2N-storage method; the
+    // parameter sets hold one per stage and instance, then a timing set (the first SSP-RK3 stage,
+    // which writes only the stage buffer) for the autotuner
+    int nst = 3;
+    bool any_limiter = false;
     std::vector<double*> Q;
     std::vector<double> dt;
     bool have_states = false;
@@ -246,20 +253,30 @@ int build_items(flou_batch* b) {
 }
 
 int upload_params(flou_batch* b) {
-    std::vector<FaceParams> fp(3 * b->n);
-    std::vector<ElemParams> ep(3 * b->n);
+    const int ns = b->nst;
+    std::vector<FaceParams> fp((ns + 1) * b->n);
+    std::vector<ElemParams> ep((ns + 1) * b->n);
     for (int k = 0; k < b->n; ++k) {
         flou_ctx* c = b->ctxs[k];
         double* Q = b->Q[k];
         double* U = c->d_U;
         double dt = b->dt[k];
-        fp[k] = ctx_face_params(c, Q);
-        fp[b->n + k] = ctx_face_params(c, U);
-        fp[2 * b->n + k] = ctx_face_params(c, U);
-        ep[k] = ctx_elem_params(c, Q, Q, U, 1, dt, 0.0, 1.0);
-        ep[b->n + k] = ctx_elem_params(c, U, Q, U, 2, dt, 0.75, 0.25);
-        ep[2 * b->n + k] = ctx_elem_params(c, U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0);
-        for (int s = 0; s < 3; ++s) {
+        if (c->lsrk_s) {   // 2N-storage: every stage in place on Q, the register in U
+            for (int st = 0; st < ns; ++st) {
+                fp[st * b->n + k] = ctx_face_params(c, Q);
+                ep[st * b->n + k] = ctx_elem_params(c, Q, U, Q, 3, dt, st ? c->lsrk_A[st] : 0.0, c->lsrk_B[st]);
+            }
+        } else {
+            fp[k] = ctx_face_params(c, Q);
+            fp[b->n + k] = ctx_face_params(c, U);
+            fp[2 * b->n + k] = ctx_face_params(c, U);
+            ep[k] = ctx_elem_params(c, Q, Q, U, 1, dt, 0.0, 1.0);
+            ep[b->n + k] = ctx_elem_params(c, U, Q, U, 2, dt, 0.75, 0.25);
+            ep[2 * b->n + k] = ctx_elem_params(c, U, Q, Q, 2, dt, 1.0 / 3.0, 2.0 / 3.0);
+        }
+        fp[ns * b->n + k] = ctx_face_params(c, Q);   // the timing set
+        ep[ns * b->n + k] = ctx_elem_params(c, Q, Q, U, 1, dt, 0.0, 1.0);
+        for (int s = 0; s <= ns; ++s) {
             ep[s * b->n + k].status = b->d_status;
             fp[s * b->n + k].status = b->d_status;
         }
@@ -297,6 +314,20 @@ int launch_stage(flou_batch* b, int s, cudaStream_t st) {
     A.skip_done_inst = b->skip_done_inst;
     b->kern->fn<<<grid, b->kern->tb, b->kern->smem, st>>>(A);
     BCK(cudaGetLastError(), "batch kernel launch");
+    return FLOU_OK;
+}
+
+// The limiter after stage s of every instance that has one (OrdinaryDiffEq's stage_limiter!):
+// on the stage buffer after the first two SSP-RK3 stages, on the state otherwise.
+int limit_stage(flou_batch* b, int s, cudaStream_t st) {
+    if (!b->any_limiter) return FLOU_OK;
+    for (int k = 0; k < b->n; ++k) {
+        flou_ctx* c = b->ctxs[k];
+        if (!c->limiter) continue;
+        double* q = (!c->lsrk_s && s < 2) ? c->d_U : b->Q[k];
+        int r = ctx_limit(c, st, q);
+        if (r) return bfail(b, r, "instance " + std::to_string(k) + ": " + c->err);
+    }
     return FLOU_OK;
 }
 
@@ -354,13 +385,22 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
             delete b;
             return r;
         }
-        if (c->limiter || c->mon_mask || c->curv || c->lsrk_s ||
-            (c->cfg.volume_op != FLOU_OP_STRONG && !c->bnodes)) {   // the persistent launch runs none of these
-            c->err = "the batched launch covers Cartesian geometry, SSP-RK3, without limiter or monitors, and "
-                     "the split form on Gauss-Lobatto nodes";
+        if (c->mon_mask || c->curv || (c->cfg.volume_op != FLOU_OP_STRONG && !c->bnodes)) {
+            c->err = "the batched launch covers Cartesian geometry without monitors, and the split form on "
+                     "Gauss-Lobatto nodes";
             delete b;
             return FLOU_ERR_UNSUPPORTED;
         }
+        // one stage sequence for all: SSP-RK3 everywhere, or one 2N-storage method everywhere
+        bool same = c->lsrk_s == c0->lsrk_s;
+        for (int st = 0; same && st < c->lsrk_s; ++st)
+            same = c->lsrk_A[st] == c0->lsrk_A[st] && c->lsrk_B[st] == c0->lsrk_B[st];
+        if (!same) {
+            c->err = "the instances of a batch step with the same time integrator";
+            delete b;
+            return FLOU_ERR_ARG;
+        }
+        if (c->limiter) b->any_limiter = true;
         maxnpe = std::max(maxnpe, c->npe);
     }
     std::vector<const BatchKernel*> fit;
@@ -376,8 +416,9 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_fp, 3 * n * sizeof(FaceParams));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_ep, 3 * n * sizeof(ElemParams));
+    b->nst = c0->lsrk_s ? c0->lsrk_s : 3;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_fp, (size_t)(b->nst + 1) * n * sizeof(FaceParams));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_ep, (size_t)(b->nst + 1) * n * sizeof(ElemParams));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_meta, 3 * n * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counter, (2 + n) * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_status, 2 * sizeof(int32_t));
@@ -438,7 +479,10 @@ int32_t flou_batch_step(flou_batch* b, int32_t nsteps) {
     if (!b->gexec) {
         BCK(cudaStreamBeginCapture(b->own_stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         int rr = FLOU_OK;
-        for (int s = 0; s < 3 && !rr; ++s) rr = launch_stage(b, s, b->own_stream);
+        for (int s = 0; s < b->nst && !rr; ++s) {
+            rr = launch_stage(b, s, b->own_stream);
+            if (!rr) rr = limit_stage(b, s, b->own_stream);
+        }
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(b->own_stream, &g);
         if (rr) { if (g) cudaGraphDestroy(g); return rr; }
@@ -478,7 +522,7 @@ int32_t flou_batch_autotune(flou_batch* b, int32_t* out) {
                 float tot = 0.f;
                 for (int rep = 0; rep < 3; ++rep) {
                     BCK(cudaEventRecord(e0, b->stream), "event");
-                    if ((r = launch_stage(b, 0, b->stream))) return r;
+                    if ((r = launch_stage(b, b->nst, b->stream))) return r;
                     BCK(cudaEventRecord(e1, b->stream), "event");
                     BCK(cudaEventSynchronize(e1), "event");
                     float ms = 0.f;
@@ -499,7 +543,7 @@ int32_t flou_batch_autotune(flou_batch* b, int32_t* out) {
         float tot = 0.f;
         for (int rep = 0; rep < 3; ++rep) {
             BCK(cudaEventRecord(e0, b->stream), "event");
-            if ((r = launch_stage(b, 0, b->stream))) return r;
+            if ((r = launch_stage(b, b->nst, b->stream))) return r;
             BCK(cudaEventRecord(e1, b->stream), "event");
             BCK(cudaEventSynchronize(e1), "event");
             float ms = 0.f;

@@ -833,10 +833,12 @@ __device__ __forceinline__ void surface_and_update(const ElemParams& P, const do
         else if (P.mode == 1) o = fma(c, dq[k], q[k]);
         else if (P.mode == 2) o = fma(P.a0, P.Q0[k * P.ndofs + g], P.a1 * fma(c, dq[k], q[k]));
         else {
+            // explicit FMAs, as in the other modes: every instantiation (the plain kernels, the
+            // batched tiles) rounds alike
             double kk = c * dq[k];
-            if (P.a0 != 0.0) kk = P.a0 * P.aux[k * P.ndofs + g] + kk;   // first stage: k is not read
+            if (P.a0 != 0.0) kk = fma(P.a0, P.aux[k * P.ndofs + g], kk);   // first stage: k is not read
             P.aux[k * P.ndofs + g] = kk;
-            o = q[k] + P.a1 * kk;
+            o = fma(P.a1, kk, q[k]);
         }
         bad |= !isfinite(o);
         P.out[k * P.ndofs + g] = o;

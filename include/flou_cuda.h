@@ -347,11 +347,13 @@ int32_t flou_take_monitors_timed(flou_ctx* ctx, double* out, double* times, int3
 
 /* ---- batched mode (no counterpart in the reference: Flou solves one problem at a time) ----
  * Many independent discretizations with uneven element counts and orders advance together:
- * one persistent launch per SSP-RK3 stage serves every instance from one work queue of face
- * items and element tiles, and the three stages of a step replay as one CUDA graph.  A batch is
- * built from contexts whose set-up is complete; they must outlive the batch and share the
- * dimension, equation and volume operator (2D Euler strong form, or 3D Euler split form with
- * the Chandrashekar flux).  States are device pointers, one per instance. */
+ * one persistent launch per stage serves every instance from one work queue of face items and
+ * element tiles, and the stages of a step replay as one CUDA graph.  A batch is built from
+ * contexts whose set-up is complete; they must outlive the batch and share the dimension,
+ * equation and volume operator (2D Euler strong form, or 3D Euler split form with the
+ * Chandrashekar flux) and the time integrator (SSP-RK3, or one 2N-storage method for all); an
+ * instance with the Zhang-Shu limiter gets it after every stage.  Cartesian geometry, no
+ * monitors.  States are device pointers, one per instance. */
 typedef struct flou_batch flou_batch;
 int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out);
 int32_t flou_batch_destroy(flou_batch* b);
@@ -359,7 +361,7 @@ const char* flou_batch_last_error(const flou_batch* b);
 int32_t flou_batch_set_stream(flou_batch* b, void* stream);
 /* Q[k]: device state of instance k (advanced in place); dt[k]: its fixed time step. */
 int32_t flou_batch_set_states(flou_batch* b, double* const* Q, const double* dt);
-/* nsteps SSP-RK3 steps of every instance.  FLOU_ERR_TIMEOUT if a bounded device-side wait ran
+/* nsteps steps of every instance.  FLOU_ERR_TIMEOUT if a bounded device-side wait ran
  * out (the results of that call are then invalid; the batch stays usable). */
 int32_t flou_batch_step(flou_batch* b, int32_t nsteps);
 /* Autotuner: times the first stage for every (threads per block, resident blocks per SM,

@@ -142,3 +142,72 @@ def test_batch_rejects_mixed_operators():
     qa, qc = _device(smooth_euler_state(a)), _device(smooth_euler_state(c))
     with pytest.raises(F.FlouError):
         F.Batch([a, c], [qa, qc], [1e-3, 1e-3])
+
+
+@pytest.mark.parametrize("method", ["ORK256", "CarpenterKennedy2N54"])
+def test_batch_2n_storage_matches_serial_bitwise(method):
+    """Instances stepping with a 2N-storage method: one persistent launch per stage, every stage
+    in place with the register in the stage buffer, bit for bit the serial steps; the autotuner
+    times its own set (the first SSP-RK3 stage) and leaves the states alone."""
+    insts = _instances_2d(seed=5, count=6)
+    m = getattr(F, method)()
+    for d, _, _ in insts:
+        d.ctx.set_integrator(m.A, m.B)
+    try:
+        ref = _serial(insts, 3)
+        states = [_device(Q) for _, Q, _ in insts]
+        b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+        b.autotune()
+        for q, (_, Q, _) in zip(states, insts):
+            assert torch.equal(q, _device(Q))
+        b.step(3)
+        for q, r in zip(states, ref):
+            assert torch.equal(q, r)
+    finally:
+        for d, _, _ in insts:
+            d.ctx.set_integrator(None)
+
+
+def test_batch_limiter_matches_serial_bitwise():
+    """Instances with the Zhang-Shu stage limiter (some with it, some without), with SSP-RK3 and
+    with ORK256: the limiter runs after every stage of the limited instances, bit for bit the
+    serial steps, and it acts."""
+    from test_oracle_kat import _dipped_state
+    eq = F.EulerEquation(2, 1.4)
+    op = lambda: F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0))
+    for method in (None, F.ORK256()):
+        insts = []
+        for k in range(4):
+            disc = build(2, 4 + k % 2, (3, 3), eq, op())
+            Q = _dipped_state(disc, seed=40 + k)
+            if k % 2 == 0:
+                disc.ctx.set_limiter(_lib.LIMITER_ZHANG_SHU, 0.5)
+            if method is not None:
+                disc.ctx.set_integrator(method.A, method.B)
+            insts.append((disc, Q, 0.2 * disc.ctx.max_dt(Q, 1.0)))
+        ref = _serial(insts[::2], 3)
+        states = [_device(Q) for _, Q, _ in insts[::2]]
+        b = F.Batch([d for d, _, _ in insts[::2]], states, [dt for _, _, dt in insts[::2]])
+        b.step(3)
+        for q, r in zip(states, ref):
+            assert torch.equal(q, r)
+        d0, Q0, dt0 = insts[0]
+        o = oracle_for(d0)
+        lim = (o.ssprk3_limited(Q0, dt0, 3, 0.5, d0.std.omega) if method is None else
+               o.lsrk2n(Q0, dt0, 3, method.A, method.B, method.c, minval=0.5, omega_tp=d0.std.omega))
+        assert rel_linf(states[0].cpu().numpy().T, lim) <= 1e-10
+        for d, _, _ in insts:
+            d.ctx.set_limiter(_lib.LIMITER_NONE)
+            d.ctx.set_integrator(None)
+
+
+def test_batch_rejects_mixed_integrators():
+    eq = F.EulerEquation(2, 1.4)
+    a = build(2, 4, (2, 2), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    c = build(2, 4, (2, 2), eq, F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
+    m = F.ORK256()
+    c.ctx.set_integrator(m.A, m.B)
+    qa, qc = _device(smooth_euler_state(a)), _device(smooth_euler_state(c))
+    with pytest.raises(F.FlouError):
+        F.Batch([a, c], [qa, qc], [1e-3, 1e-3])
+    c.ctx.set_integrator(None)

@@ -93,17 +93,11 @@ def test_shockwave2d_golden_on_device():
     assert rel_linf(Q, ref) <= max(STEP_TOL, 10 * spread)
 
 
-def test_batched_launch_rejects_lowstorage():
-    """The batched launch steps with SSP-RK3 only (the single and the batched adjoint solves
-    differentiate the 2N-storage methods: test_gpu_adjoint.py, test_gpu_adjoint_batch.py)."""
-    torch = pytest.importorskip("torch")
+def test_integrator_rejects_too_many_stages():
+    """(The batched launch and both adjoint solves step with the 2N-storage methods too:
+    test_gpu_batch.py, test_gpu_adjoint.py, test_gpu_adjoint_batch.py.)"""
     from flou_cuda import _lib as L
     disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
-    m = F.ORK256()
-    disc.ctx.set_integrator(m.A, m.B)
-    Q = torch.from_numpy(np.ascontiguousarray(smooth_euler_state(disc, seed=2).T)).cuda()
-    with pytest.raises(F.FlouError):
-        F.Batch([disc], [Q], [1e-3])
     with pytest.raises(F.FlouError) as ei:
         disc.ctx.set_integrator([0.0] * 17, [0.1] * 17)
     assert ei.value.status == L.FLOU_ERR_ARG
