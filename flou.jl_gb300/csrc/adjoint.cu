@@ -67,8 +67,7 @@ int flux_kind(int nf, int avg) {
 int fv_kind(const flou_ctx* c) { return flux_kind(c->fvflux, c->fvavg); }
 
 // The scalar equations (linear advection, Burgers): the strong form on either node set or the
-// split form with the arithmetic-mean two-point flux, the LxF or central interface flux,
-// Cartesian geometry.
+// split form with the arithmetic-mean two-point flux, the LxF or central interface flux.
 int adj_supported_scalar(flou_ctx* c) {
     const flou_config& k = c->cfg;
     const bool vol = k.volume_op == FLOU_OP_STRONG ||
@@ -79,8 +78,6 @@ int adj_supported_scalar(flou_ctx* c) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the scalar equations covers the strong form and the "
                                                  "split form with the StdAverage two-point flux, with the LxF or "
                                                  "StdAverage interface flux");
-    if (c->curv)
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the scalar equations covers Cartesian geometry");
     return FLOU_OK;
 }
 
@@ -230,7 +227,8 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     P.subJ = c->d_subJ;
     for (int d = 0; d < 3; ++d) P.adv[d] = c->cfg.advection[d];
     if (scalar) {
-        e = launch_adj_scalar(dim, c->cfg.equation, c->n, c->cfg.volume_op == FLOU_OP_SPLIT, gauss, grid, tb, F, P, s);
+        e = launch_adj_scalar(dim, c->cfg.equation, c->n, c->cfg.volume_op == FLOU_OP_SPLIT, gauss, c->curv, grid, tb,
+                              F, P, s);
         if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint kernels (scalar equation)");
         return FLOU_OK;
     }

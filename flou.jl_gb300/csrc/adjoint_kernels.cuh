@@ -2287,7 +2287,9 @@ inline bool adj_split_tile_fits(int dim, int n, int tp, bool hybrid) {
 // comes from the lift as for the Euler face VJP (G: the interpolated traces and the full-line
 // lift).  A fixed boundary state (Dirichlet, a state field) takes no cotangent; outflow passes
 // the ghost's to the trace.  The intensity cotangent feeds dJ/dc.
-template <int DIM, int EQ, bool G = false>
+// CURV (linear advection on general geometry): the slave trace through the orientation, per-node
+// 1/J, the face node's normal and surface Jacobian.
+template <int DIM, int EQ, bool G = false, bool CURV = false>
 __global__ void __launch_bounds__(256) adj_face_scalar_kernel(AdjFaceParams P) {
     int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)P.nfaces * P.nfd) return;
@@ -2302,43 +2304,50 @@ __global__ void __launch_bounds__(256) adj_face_scalar_kernel(AdjFaceParams P) {
     const double* dgl = lvb + 2 * n;
     const double* dgr = dgl + n;
     // the trace of side s and the lift transpose Σ ∂g (w λ) over its line (LGL: the end node)
-    auto side = [&](int32_t s, double& q, double& fl) {
+    auto side = [&](int32_t s, int mm, double& q, double& fl) {
         const int e = s >> 3, pos = s & 7, dir = pos >> 1, right = pos & 1;
-        const double wj = P.invJ[e] * P.s_lam;
         if constexpr (G) {
             const double* lv = lvb + (right ? n : 0);
             const double* dg = right ? dgr : dgl;
             q = fl = 0.0;
             for (int p = 0; p < n; ++p) {
-                const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, p);
+                const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, mm, p);
+                const double wj = (CURV ? P.invJn[gg] : P.invJ[e]) * P.s_lam;
                 q = fma(lv[p], P.U[gg], q);
                 fl = fma(wj * dg[p], P.Ain[gg], fl);
             }
         } else {
-            const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, m, right ? n - 1 : 0);
+            const int64_t gg = (int64_t)e * P.npe + tp_node<DIM>(n, dir, mm, right ? n - 1 : 0);
+            const double wj = (CURV ? P.invJn[gg] : P.invJ[e]) * P.s_lam;
             q = P.U[gg];
             fl = (right ? dgr[n - 1] : dgl[0]) * wj * P.Ain[gg];
         }
     };
     double ql, qr = 0.0, f1, f2 = 0.0;
-    side(s0, ql, f1);
+    side(s0, m, ql, f1);
     double Fb = -f1;
     int bck = 0;
     if (s1 >= 0) {
-        side(s1, qr, f2);
+        const int mm = CURV ? master2slave<DIM>(m, P.orient[f], n) : m;
+        if (CURV && !index_ok(mm, P.nfd, P.status, s1 >> 3)) return;
+        side(s1, mm, qr, f2);
         Fb += f2;
     } else {
         const int bi = P.face_bc[f];
         bck = P.bc_kind[bi];
         qr = bck == FLOU_BC_INFLOW ? P.bc_state[bi][0] : bck == FLOU_BC_STATE_FIELD ? P.bc_field[gid] : ql;
     }
-    Fb *= P.faceJ[f];
+    Fb *= CURV ? P.faceJn[gid] : P.faceJ[f];
     double inten = P.intensity;
     if (P.elem_c) {
         const int e1 = s0 >> 3, e2 = s1 >= 0 ? (s1 >> 3) : e1;
         inten = (P.elem_c[e1] + P.elem_c[e2]) * 0.5;
     }
-    const FrameTab fr = frame_of(DIM, s0 & 7);
+    FrameTab fr = frame_of(DIM, s0 & 7);
+    if constexpr (CURV) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fr.n[c] = P.frames[c * P.nfdofs + gid];
+    }
     double ab, bb, Ib = 0.0;
     if constexpr (EQ == FLOU_EQ_LINEAR_ADVECTION) {
         double an = P.adv[0] * fr.n[0];
@@ -2378,7 +2387,10 @@ __global__ void __launch_bounds__(256) adj_face_scalar_kernel(AdjFaceParams P) {
 // the split form with the arithmetic-mean two-point flux F♯ = (f(u_i) + f(u_j))/2 gives
 // ū_i += -Ja f'(u_i) (½ Σ_(j≠i) (D♯_ij w_i + D♯_ji w_j) + D♯_ii w_i).  Then the trace cotangents
 // (G: through l at every node), the stage combination and dJ/dc as for the Euler kernels.
-template <int DIM, int N, int EQ, bool SPLIT, bool G = false>
+// CURV (linear advection on general geometry): per-node 1/J; the strong form's flux derivative is
+// the contravariant a·Ja_d of the node, the split form's pair (i, j) runs along a·(Ja_i + Ja_j)/2
+// and its diagonal along a·Ja_i, and the slave traces are read through the orientation.
+template <int DIM, int N, int EQ, bool SPLIT, bool G = false, bool CURV = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_scalar_kernel(AdjElemParams P) {
     using S = Shape<DIM, N>;
     constexpr int NPE = S::NPE, NN = S::NN, NFD = S::NFD;
@@ -2395,7 +2407,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_scalar_kernel(A
     double ain = 0.0;
     if (active) {
         ain = P.Ain[gi];
-        sw[tid] = P.invJ[e] * P.s_lam * ain;
+        sw[tid] = (CURV ? P.invJn[gi] : P.invJ[e]) * P.s_lam * ain;
     }
     __syncthreads();
     if (!active) return;
@@ -2408,30 +2420,51 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_scalar_kernel(A
     for (int d = 0; d < DIM; ++d) {
         int pos, line;
         tp_coords<DIM>(N, i, d, pos, line);
-        double Gs = 0.0;
-        if constexpr (SPLIT) {
-            const double wi = sw[tid];
+        auto a_dot_Ja = [&](int64_t g) {   // a·Ja[:, d] of node g
+            double x = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) x = fma(P.adv[k], P.Jan[(k + d * DIM) * P.ndofs + g], x);
+            return x;
+        };
+        if constexpr (CURV && SPLIT) {
+            const double wi = sw[tid], ai = a_dot_Ja(gi);
             double acc = 0.0;
 #pragma unroll
             for (int r = 0; r < N; ++r) {
                 if (r == pos) continue;
                 const int j = el * NPE + tp_node<DIM>(N, d, line, r);
-                acc = fma(Dsh[pos + r * N], wi, fma(Dsh[r + pos * N], sw[j], acc));
+                const double aij = 0.5 * (ai + a_dot_Ja((int64_t)e0 * NPE + j));
+                acc = fma(aij, fma(Dsh[pos + r * N], wi, Dsh[r + pos * N] * sw[j]), acc);
             }
-            Gs = fma(Dsh[pos + pos * N], wi, 0.5 * acc);
+            qb -= fma(Dsh[pos + pos * N] * ai, wi, 0.5 * acc);
         } else {
+            double Gs = 0.0;
+            if constexpr (SPLIT) {
+                const double wi = sw[tid];
+                double acc = 0.0;
 #pragma unroll
-            for (int r = 0; r < N; ++r) Gs = fma(Ds[r + pos * N], sw[el * NPE + tp_node<DIM>(N, d, line, r)], Gs);
+                for (int r = 0; r < N; ++r) {
+                    if (r == pos) continue;
+                    const int j = el * NPE + tp_node<DIM>(N, d, line, r);
+                    acc = fma(Dsh[pos + r * N], wi, fma(Dsh[r + pos * N], sw[j], acc));
+                }
+                Gs = fma(Dsh[pos + pos * N], wi, 0.5 * acc);
+            } else {
+#pragma unroll
+                for (int r = 0; r < N; ++r) Gs = fma(Ds[r + pos * N], sw[el * NPE + tp_node<DIM>(N, d, line, r)], Gs);
+            }
+            double fp;
+            if constexpr (CURV) fp = a_dot_Ja(gi);
+            else fp = (EQ == FLOU_EQ_LINEAR_ADVECTION ? P.adv[d] : u) * P.Ja[e * DIM + d];
+            qb = fma(-fp, Gs, qb);
         }
-        const double fp = EQ == FLOU_EQ_LINEAR_ADVECTION ? P.adv[d] : u;
-        qb = fma(-P.Ja[e * DIM + d] * fp, Gs, qb);
 #pragma unroll
         for (int sd = 0; sd < 2; ++sd) {
             if (!G && pos != (sd ? N - 1 : 0)) continue;
             const int fk = 2 * d + sd;
             const int32_t pk = P.elem_face[e * 2 * DIM + fk];
             const double* src = (pk & 1) ? P.QbR : P.QbL;
-            const int64_t o = (int64_t)(pk >> 1) * NFD + line;
+            const int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
             if (!index_ok(o, P.nfdofs, P.status, e)) continue;
             qb = fma(G ? lv[sd * N + pos] : 1.0, __ldcg(src + o), qb);
         }
@@ -2457,9 +2490,10 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK) adj_elem_scalar_kernel(A
     }
 }
 
-// Scalar equations: eq FLOU_EQ_LINEAR_ADVECTION (1D-3D) or FLOU_EQ_BURGERS (1D).
-cudaError_t launch_adj_scalar(int dim, int eq, int n, bool split, bool gauss, int grid, int tb, const AdjFaceParams& F,
-                              const AdjElemParams& P, cudaStream_t s);
+// Scalar equations: eq FLOU_EQ_LINEAR_ADVECTION (1D-3D; general geometry in 2D and 3D) or
+// FLOU_EQ_BURGERS (1D).
+cudaError_t launch_adj_scalar(int dim, int eq, int n, bool split, bool gauss, bool curv, int grid, int tb,
+                              const AdjFaceParams& F, const AdjElemParams& P, cudaStream_t s);
 
 // Launchers, one translation unit each (explicit instantiations of the templates above).
 // curv: the general-geometry kernels (2D and 3D); gauss: the interpolated traces and full-line

@@ -263,9 +263,9 @@ int32_t flou_fp64_dmma_peak(double* gflops);
 int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_err);
 
 /* ---- discrete adjoint (no counterpart in the reference; Flou differentiates nothing) ----
- * Covers linear advection (1D-3D) and Burgers (1D) with the strong form (either node set) or the
- * split form with the StdAverage two-point flux, the LxF or StdAverage interface flux, on
- * Cartesian geometry; and the Euler equations with
+ * Covers linear advection (1D-3D, Cartesian or general geometry) and Burgers (1D) with the strong
+ * form (either node set) or the split form with the StdAverage two-point flux, the LxF or
+ * StdAverage interface flux; and the Euler equations with
  *  - the strong form, the split form (Chandrashekar, Kennedy-Gruber or StdAverage two-point
  *    flux) and the hybrid operator (Gauss-Lobatto nodes; any interface flux below as its
  *    subcell flux);

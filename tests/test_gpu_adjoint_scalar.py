@@ -4,7 +4,6 @@ import numpy as np
 import pytest
 
 import flou_cuda as F
-from flou_cuda import _lib as L
 from cases import build, oracle_for
 
 pytestmark = pytest.mark.gpu
@@ -124,14 +123,57 @@ def test_scalar_adjoint_against_central_differences():
         assert abs(ours - fd) <= 1e-6 * abs(fd), (ours, fd)
 
 
-def test_scalar_adjoint_limits():
-    """Not covered: general geometry for the scalar equations."""
+def _general(dim, n, op, basis, walls):
     from test_unstructured import _std
-    mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=1)
-    adv = F.MultielementDisc(mesh, _std(2, 4, 1), F.LinearAdvection(1.0, 0.5), OPS["strong_lxf"](),
-                             {str(k): F.DirichletBC([1.0]) for k in range(1, 5)})
-    Q = torch.ones((1, adv.ndofs), dtype=torch.float64, device="cuda")
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        adv.ctx.rhs_vjp(g, None, Q, Q)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+    mesh = F.perturbed_box(dim, 3, (0.0,) * dim, (1.0,) * dim, amp=0.12, seed=4 + dim)
+    bcs = {str(k): (F.DirichletBC([0.5 + 0.1 * k]) if walls and k % 2 else F.OutflowBC())
+           for k in range(1, 2 * dim + 1)}
+    disc = F.MultielementDisc(mesh, _std(dim, n, 1, basis), F.LinearAdvection(*([1.0, -0.6, 0.4][:dim])),
+                              OPS[op](), bcs)
+    X = disc.coords
+    Q = 1.0 + 0.5 * np.prod([np.cos(3.0 * X[:, d] + d) for d in range(dim)], axis=0)
+    return disc, np.asfortranarray(Q[:, None])
+
+
+@pytest.mark.parametrize("op,basis", [("strong_lxf", "GLL"), ("strong_central", "GLL"), ("split_lxf", "GLL"),
+                                      ("strong_lxf", "GL")])
+@pytest.mark.parametrize("dim,n,walls", [(2, 4, True), (2, 5, False), (3, 3, True), (3, 4, False)])
+def test_scalar_general_geometry_rhs_vjp(dim, n, walls, op, basis):
+    """Linear advection on perturbed, rotated elements (every orientation in 3D): contravariant
+    fluxes with the node's metric, pairs along the averaged columns, the face nodes' normals and
+    surface Jacobians, slave traces through the orientation."""
+    disc, Q = _general(dim, n, op, basis, walls)
+    if dim == 3:
+        assert len(set(disc.mesh.orientation.tolist())) == 8
+    rng = np.random.default_rng(110 + dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _with_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+def test_scalar_general_geometry_adjoint_solve():
+    disc, Q0 = _general(3, 4, "split_lxf", "GLL", True)
+    rng = np.random.default_rng(93)
+    c, _ = _with_c(disc, "split_lxf", 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 5)
+    dt = 0.3 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 8
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 3, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + np.sum(gc.cpu().numpy() * dc)
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
