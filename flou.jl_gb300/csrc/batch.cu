@@ -2,7 +2,8 @@
 // together: one persistent launch per stage (SSP-RK3's three, or the instances' common
 // 2N-storage method's) serves every instance from one work queue, and the stages of a step are
 // replayed as one CUDA graph; an instance with the Zhang-Shu limiter gets it after every stage
-// (its own launch in the graph).
+// and one with monitors records them after every step (its own launches in the graph).  A batch
+// is all Cartesian or all on general geometry (batch_curv.cu instantiates the latter).
 //
 // Work queue of one stage: first every face item of every instance (TB face nodes each), then
 // every element item (G consecutive element tiles of the instance's order, G chosen per order by
@@ -20,138 +21,18 @@
 #include <string>
 #include <vector>
 
-#include "flou_ctx.cuh"
+#include "batch_kernels.cuh"
 
 namespace flou {
 
-constexpr long long kWaitCycles = 200000000LL;   // per wait, ~0.1 s at 2 GHz
-
-struct BatchArgs {
-    const FaceParams* fp;        // [ninst], this stage
-    const ElemParams* ep;        // [ninst], this stage
-    const int32_t* inst_n;       // nodes per direction
-    const int32_t* inst_lgl;     // basis with boundary nodes
-    const int32_t* nface_items;  // face items per instance
-    const int2* items;           // (instance | (G - 1) << 27 | kind << 30, first face node or element)
-    int32_t nitems;
-    int32_t ninst;
-    int32_t* counter;            // [0] queue head, [1] abort flag, [2 + k] face items done of instance k
-    int32_t* status;             // bit 0 non-physical, bit 1 wait timed out
-    int32_t skip_done_inst;      // fault-injection hook: this instance never reports its faces (-1: none)
-};
-
-// One call per order, not inlined: each order's tile gets its own register allocation instead
-// of the union of all orders (which would limit the persistent kernel to one block per SM).
-// G consecutive tiles of EPB elements each (the last ones may run past the instance's elements).
-template <int DIM, int N, int EQ, int VOL, int TP, int TB>
-__device__ __noinline__ void batch_tile_n(const ElemParams& P, int lgl, int e0, int G, double* smem) {
-    constexpr int EPB = Shape<DIM, N, TB>::EPB;
-    for (int g = 0; g < G; ++g) {
-        const int e = e0 + g * EPB;
-        if (e >= P.nelem) break;   // uniform over the block
-        if (g > 0) __syncthreads();   // the previous tile's last phase may still read shared memory
-        if (VOL == FLOU_OP_STRONG) {
-            if (lgl) strong_tile<DIM, N, EQ, true, TB>(P, e, smem);
-            else strong_tile<DIM, N, EQ, false, TB>(P, e, smem);
-        } else {
-            split_tile<DIM, N, EQ, TP, true, TB>(P, e, smem);
-        }
-    }
-}
-
-template <int DIM, int EQ>
-__device__ __noinline__ void batch_face(const FaceParams& P, int64_t gid, int lgl) {
-    if (lgl) face_node<DIM, EQ, true>(P, gid);
-    else face_node<DIM, EQ, false>(P, gid);
-}
-
-template <int DIM, int EQ, int VOL, int TP, int TB>
-__device__ __forceinline__ void batch_tile(const ElemParams& P, int n, int lgl, int e0, int G, double* smem) {
-    switch (n) {
-        case 2: batch_tile_n<DIM, 2, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        case 3: batch_tile_n<DIM, 3, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        case 4: batch_tile_n<DIM, 4, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        case 5: batch_tile_n<DIM, 5, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        case 6: batch_tile_n<DIM, 6, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        case 7: batch_tile_n<DIM, 7, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-        default: batch_tile_n<DIM, 8, EQ, VOL, TP, TB>(P, lgl, e0, G, smem); break;
-    }
-}
-
-template <int DIM, int EQ, int VOL, int TP, int TB>
-__global__ void __launch_bounds__(TB, (TB >= 512 ? 1 : 1024 / TB)) batch_stage_kernel(BatchArgs A) {
-    extern __shared__ double smem[];
-    __shared__ int s_item;
-    int32_t* done = A.counter + 2;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
-        __syncthreads();
-        const int it = s_item;
-        __syncthreads();
-        if (it >= A.nitems) break;
-        const int2 w = A.items[it];
-        const int inst = w.x & 0x07ffffff;
-        if (!index_ok(inst, A.ninst, A.status, 0)) continue;
-        if ((w.x >> 30) == 0) {
-            const FaceParams& fp = A.fp[inst];
-            const int64_t gid = (int64_t)w.y + threadIdx.x;
-            batch_face<DIM, EQ>(fp, gid, A.inst_lgl[inst]);
-            __threadfence();   // this thread's face fluxes are visible device-wide ...
-            __syncthreads();   // ... for every thread of the block before the count goes up
-            if (threadIdx.x == 0 && inst != A.skip_done_inst) atomicAdd(done + inst, 1);
-        } else {
-            if (threadIdx.x == 0) {
-                const volatile int32_t* d = done + inst;
-                const volatile int32_t* abort_flag = A.counter + 1;
-                const int32_t target = A.nface_items[inst];
-                const long long t0 = clock64();
-                while (*d < target) {
-                    if (*abort_flag) break;
-                    if (clock64() - t0 > kWaitCycles) {
-                        atomicExch(A.counter + 1, 1);
-                        atomicOr(A.status, 2);
-                        break;
-                    }
-                    __nanosleep(64);
-                }
-                __threadfence();
-            }
-            __syncthreads();
-            batch_tile<DIM, EQ, VOL, TP, TB>(A.ep[inst], A.inst_n[inst], A.inst_lgl[inst], w.y,
-                                             ((w.x >> 27) & 7) + 1, smem);
-        }
-    }
-}
-
-template <int DIM, int EQ, int VOL, int TP, int TB>
-constexpr size_t batch_smem_bytes() {
-    size_t m = 0;
-    m = std::max(m, elem_smem_bytes<DIM, 2, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 3, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 4, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 5, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 6, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 7, EQ, VOL, TP, TB>());
-    m = std::max(m, elem_smem_bytes<DIM, 8, EQ, VOL, TP, TB>());
-    return (m + 15) & ~size_t(15);
-}
-
-// The instantiated batch kernels: 2D Euler strong form (the batched configuration) with 128 or
-// 256 threads per block, 3D Euler split form with the Chandrashekar flux with 512.
-struct BatchKernel {
-    int dim, eq, vol, tp, tb;
-    void (*fn)(BatchArgs);
-    size_t smem;
-};
-
 static const BatchKernel kBatchKernels[] = {
-    {2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 128,
+    {2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 128, false,
      batch_stage_kernel<2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 128>,
      batch_smem_bytes<2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 128>()},
-    {2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 256,
+    {2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 256, false,
      batch_stage_kernel<2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 256>,
      batch_smem_bytes<2, FLOU_EQ_EULER, FLOU_OP_STRONG, FLOU_TP_STD_AVERAGE, 256>()},
-    {3, FLOU_EQ_EULER, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, 512,
+    {3, FLOU_EQ_EULER, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, 512, false,
      batch_stage_kernel<3, FLOU_EQ_EULER, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, 512>,
      batch_smem_bytes<3, FLOU_EQ_EULER, FLOU_OP_SPLIT, FLOU_TP_CHANDRASHEKAR, 512>()},
 };
@@ -174,7 +55,7 @@ struct flou_batch {
     // parameter sets hold one per stage and instance, then a timing set (the first SSP-RK3 stage,
     // which writes only the stage buffer) for the autotuner
     int nst = 3;
-    bool any_limiter = false;
+    bool any_limiter = false, any_monitors = false;
     std::vector<double*> Q;
     std::vector<double> dt;
     bool have_states = false;
@@ -331,6 +212,18 @@ int limit_stage(flou_batch* b, int s, cudaStream_t st) {
     return FLOU_OK;
 }
 
+// The monitors of every instance that records them, after each step (Flou's monitor callback).
+int record_monitors(flou_batch* b, cudaStream_t st) {
+    if (!b->any_monitors) return FLOU_OK;
+    for (int k = 0; k < b->n; ++k) {
+        flou_ctx* c = b->ctxs[k];
+        if (!c->mon_mask) continue;
+        int r = ctx_record_monitors(c, st, b->Q[k]);
+        if (r) return bfail(b, r, "instance " + std::to_string(k) + ": " + c->err);
+    }
+    return FLOU_OK;
+}
+
 int check_status(flou_batch* b) {
     int32_t st[2];
     BCK(cudaMemcpyAsync(st, b->d_status, sizeof(st), cudaMemcpyDeviceToHost, b->stream), "status read");
@@ -366,8 +259,13 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
     b->eq = c0->cfg.equation;
     b->vol = c0->cfg.volume_op;
     b->tp = b->vol == FLOU_OP_SPLIT ? c0->cfg.twopoint_flux : FLOU_TP_STD_AVERAGE;
-    for (const BatchKernel& k : kBatchKernels)
+    // Cartesian or general geometry: one kernel list or the other, for the whole batch
+    const BatchKernel* list = c0->curv ? kBatchKernelsCurv : kBatchKernels;
+    const int nlist = c0->curv ? kNumBatchKernelsCurv : (int)(sizeof(kBatchKernels) / sizeof(kBatchKernels[0]));
+    for (int i = 0; i < nlist; ++i) {
+        const BatchKernel& k = list[i];
         if (k.dim == b->dim && k.eq == b->eq && k.vol == b->vol && k.tp == b->tp) b->kernels.push_back(&k);
+    }
     if (b->kernels.empty()) {
         delete b;
         return FLOU_ERR_UNSUPPORTED;
@@ -385,12 +283,17 @@ int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out) {
             delete b;
             return r;
         }
-        if (c->mon_mask || c->curv || (c->cfg.volume_op != FLOU_OP_STRONG && !c->bnodes)) {
-            c->err = "the batched launch covers Cartesian geometry without monitors, and the split form on "
-                     "Gauss-Lobatto nodes";
+        if (c->cfg.volume_op != FLOU_OP_STRONG && !c->bnodes) {
+            c->err = "the batched launch covers the split form on Gauss-Lobatto nodes";
             delete b;
             return FLOU_ERR_UNSUPPORTED;
         }
+        if (c->curv != c0->curv) {
+            c->err = "the instances of a batch are all on Cartesian or all on general geometry";
+            delete b;
+            return FLOU_ERR_ARG;
+        }
+        if (c->mon_mask) b->any_monitors = true;
         // one stage sequence for all: SSP-RK3 everywhere, or one 2N-storage method everywhere
         bool same = c->lsrk_s == c0->lsrk_s;
         for (int st = 0; same && st < c->lsrk_s; ++st)
@@ -483,6 +386,7 @@ int32_t flou_batch_step(flou_batch* b, int32_t nsteps) {
             rr = launch_stage(b, s, b->own_stream);
             if (!rr) rr = limit_stage(b, s, b->own_stream);
         }
+        if (!rr) rr = record_monitors(b, b->own_stream);
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(b->own_stream, &g);
         if (rr) { if (g) cudaGraphDestroy(g); return rr; }

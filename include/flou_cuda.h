@@ -351,9 +351,10 @@ int32_t flou_take_monitors_timed(flou_ctx* ctx, double* out, double* times, int3
  * element tiles, and the stages of a step replay as one CUDA graph.  A batch is built from
  * contexts whose set-up is complete; they must outlive the batch and share the dimension,
  * equation and volume operator (2D Euler strong form, or 3D Euler split form with the
- * Chandrashekar flux) and the time integrator (SSP-RK3, or one 2N-storage method for all); an
- * instance with the Zhang-Shu limiter gets it after every stage.  Cartesian geometry, no
- * monitors.  States are device pointers, one per instance. */
+ * Chandrashekar flux), the time integrator (SSP-RK3, or one 2N-storage method for all) and the
+ * kind of geometry (all Cartesian or all general); an instance with the Zhang-Shu limiter gets
+ * it after every stage, one with monitors records them after every step.  States are device
+ * pointers, one per instance. */
 typedef struct flou_batch flou_batch;
 int32_t flou_batch_create(int32_t n, flou_ctx* const* ctxs, flou_batch** out);
 int32_t flou_batch_destroy(flou_batch* b);

@@ -211,3 +211,40 @@ def test_batch_rejects_mixed_integrators():
     with pytest.raises(F.FlouError):
         F.Batch([a, c], [qa, qc], [1e-3, 1e-3])
     c.ctx.set_integrator(None)
+
+
+def test_batch_general_geometry_matches_serial_bitwise():
+    """Instances on perturbed, rotated meshes (the general-geometry tiles and face nodes of the
+    persistent kernel): 2D strong form of uneven orders, and 3D split form."""
+    from test_gpu_unstructured import _disc as _udisc
+    from test_unstructured import _state
+    for dim, cases in ((2, [(3, "strong_lxf"), (5, "strong_lxf"), (4, "strong_lxf"), (7, "strong_lxf")]),
+                       (3, [(3, "split_chandra_lxfc"), (4, "split_chandra_lxfc"), (5, "split_chandra_lxfc")])):
+        insts = []
+        for k, (n, op) in enumerate(cases):
+            disc = _udisc(dim, n, op, nel=2 + k % 2, seed=3 + k)
+            Q = _state(disc, seed=k)
+            insts.append((disc, Q, 0.2 * disc.ctx.max_dt(Q, 1.0)))
+        ref = _serial(insts, 3)
+        states = [_device(Q) for _, Q, _ in insts]
+        b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+        b.step(3)
+        for q, r in zip(states, ref):
+            assert torch.equal(q, r)
+
+
+def test_batch_records_monitors_like_serial():
+    insts = _instances_2d(seed=7, count=4)
+    for d, _, _ in insts[::2]:
+        d.ctx.set_monitors(_lib.MONITOR_KINETIC_ENERGY | _lib.MONITOR_ENTROPY)
+    ref_states = _serial(insts, 3)
+    ref = [d.ctx.take_monitors() for d, _, _ in insts[::2]]
+    states = [_device(Q) for _, Q, _ in insts]
+    b = F.Batch([d for d, _, _ in insts], states, [dt for _, _, dt in insts])
+    b.step(3)
+    for q, r in zip(states, ref_states):
+        assert torch.equal(q, r)
+    for (d, _, _), r in zip(insts[::2], ref):
+        got = d.ctx.take_monitors()
+        assert got.shape == (3, 2) and np.array_equal(got, r)
+        d.ctx.set_monitors(0)

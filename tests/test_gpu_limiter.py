@@ -114,16 +114,8 @@ def test_flou_style_callbacks():
     assert np.allclose(mvals.value, ents, rtol=1e-11)
 
 
-def test_limiter_and_monitors_are_rejected_where_they_are_not_run():
-    """The batched launch records no monitors (it runs the limiter: test_gpu_batch.py), and the
-    limiter applies to the Euler equations only."""
-    disc = _disc(2, op=F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
-    disc.ctx.set_monitors(L.MONITOR_KINETIC_ENERGY)
-    Q = torch.from_numpy(np.ascontiguousarray(_dipped_state(disc, seed=1).T)).cuda()
-    with pytest.raises(F.FlouError) as ei:
-        F.Batch([disc], [Q], [1e-3])
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
-    disc.ctx.set_monitors(0)
+def test_limiter_applies_to_the_euler_equations_only():
+    """(The batched launch runs the limiter and the monitors too: test_gpu_batch.py.)"""
     adv = build(1, 4, (3,), F.LinearAdvection(1.0), F.StrongDivOperator(F.LxF(F.StdAverage(), 1.0)))
     with pytest.raises(F.FlouError) as ei:
         adv.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.1)

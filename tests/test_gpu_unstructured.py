@@ -7,7 +7,7 @@ import pytest
 
 import flou_cuda as F
 from flou_cuda import _lib as L
-from cases import oracle_for, rel_linf
+from cases import build, oracle_for, rel_linf
 from test_unstructured import _state, _std
 
 pytestmark = pytest.mark.gpu
@@ -173,10 +173,14 @@ def test_unstructured_limiter_and_monitors():
 
 
 def test_general_geometry_is_rejected_where_not_covered():
+    # a batch is all Cartesian or all on general geometry
     disc = _disc(2, 4, "strong_lxf")
     Q = torch.from_numpy(np.ascontiguousarray(_state(disc).T)).cuda()
+    cart = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), _ops()["strong_lxf"]())
+    Qc = torch.from_numpy(np.ascontiguousarray(_state(cart).T)).cuda()
     with pytest.raises(F.FlouError) as ei:
-        F.Batch([disc], [Q], [1e-3])
+        F.Batch([disc, cart], [Q, Qc], [1e-3, 1e-3])
+    assert ei.value.status == L.FLOU_ERR_ARG
     # the adjoint covers general geometry, but not the hybrid operator on Gauss nodes
     hyb = _disc(2, 4, "hybrid_hllc", basis="GL")
     Qh = torch.from_numpy(np.ascontiguousarray(_state(hyb).T)).cuda()
