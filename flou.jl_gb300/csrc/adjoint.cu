@@ -50,7 +50,15 @@ namespace {
 
 struct AdjBuffers {
     double *QbL = nullptr, *QbR = nullptr, *Ibar = nullptr;
+    // the hybrid operator on Gauss nodes: the forward face fluxes at U, their cotangents by side
+    // of the face, and the first element pass's partial node cotangents
+    double *Fn = nullptr, *FbS = nullptr, *Tq = nullptr;
 };
+
+// The hybrid operator on a basis without boundary nodes: its stage takes two element passes.
+bool hybrid_gauss(const flou_ctx* c) {
+    return c->cfg.equation == FLOU_EQ_EULER && c->cfg.volume_op == FLOU_OP_HYBRID && !c->bnodes;
+}
 
 // The flux kind of adj_face_kernel / numflux_vjp for an interface flux (numflux, central part),
 // -1 for one the adjoint does not differentiate.
@@ -100,19 +108,25 @@ int adj_supported(flou_ctx* c) {
     if (k.volume_op == FLOU_OP_SPLIT && c->bnodes && !c->lift_ends)
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs the DGSEM lift on a basis "
                                                  "with boundary nodes");
-    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, false))
+    if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, true, false))
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile of the Kennedy-Gruber flux at "
                                                  "3D p=7 exceeds shared memory");
     if (k.volume_op == FLOU_OP_HYBRID) {
-        if (!c->bnodes || !c->lift_ends)
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto nodes");
+        if (c->bnodes && !c->lift_ends)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto and "
+                                                     "Gauss nodes");
+        if (!c->bnodes && c->curv)
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator on Gauss nodes covers "
+                                                     "Cartesian elements");
         if (fv_kind(c) < 0)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator's subcell flux must be LxF, "
                                                      "Scalar- or MatrixDissipation (StdAverage or "
                                                      "ChandrasekharAverage), HLL or HLLC for the adjoint");
-        if (!adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, true))
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid adjoint tile of the Kennedy-Gruber flux at 3D p=7 "
-                                                     "exceeds shared memory");
+        if (!adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, !c->bnodes, true))
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, c->bnodes ? "the hybrid adjoint tile of the Kennedy-Gruber flux at "
+                                                                 "3D p=7 exceeds shared memory"
+                                                               : "the Gauss-node hybrid adjoint tile at 3D p=7 exceeds "
+                                                                 "shared memory");
     }
     return FLOU_OK;
 }
@@ -122,6 +136,11 @@ int alloc_adj(flou_ctx* c, AdjBuffers& B) {
     cudaError_t e = cudaMalloc((void**)&B.QbL, nf * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&B.QbR, nf * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&B.Ibar, (size_t)c->nfdofs * sizeof(double));
+    if (hybrid_gauss(c)) {
+        if (e == cudaSuccess) e = cudaMalloc((void**)&B.Fn, nf * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&B.FbS, 2 * nf * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&B.Tq, (size_t)c->ndofs * c->nv * sizeof(double));
+    }
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint buffers");
     return FLOU_OK;
 }
@@ -130,6 +149,9 @@ void free_adj(AdjBuffers& B) {
     if (B.QbL) cudaFree(B.QbL);
     if (B.QbR) cudaFree(B.QbR);
     if (B.Ibar) cudaFree(B.Ibar);
+    if (B.Fn) cudaFree(B.Fn);
+    if (B.FbS) cudaFree(B.FbS);
+    if (B.Tq) cudaFree(B.Tq);
     B = AdjBuffers();
 }
 
@@ -182,7 +204,8 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     const bool scalar = c->cfg.equation != FLOU_EQ_EULER;
     for (int d = 0; d < 3; ++d) F.adv[d] = c->cfg.advection[d];
     F.lxf = c->cfg.numflux == FLOU_NF_LXF ? 1 : 0;
-    cudaError_t e = scalar ? cudaSuccess : launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
+    const bool hg = hybrid_gauss(c);
+    cudaError_t e = scalar || hg ? cudaSuccess : launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
     memset(&P, 0, sizeof(P));
@@ -232,7 +255,23 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
         if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint kernels (scalar equation)");
         return FLOU_OK;
     }
-    if (c->cfg.volume_op != FLOU_OP_STRONG) {
+    if (hg) {   // forward face fluxes, element pass 1, the face VJP with its cotangents, pass 2
+        FaceParams fp = ctx_face_params(c, U);
+        fp.Fn = Bf.Fn;
+        e = c->curv ? launch_face_curv(dim, c->cfg.equation, c->lgl, fp, s)
+                    : launch_face(dim, c->cfg.equation, c->lgl, fp, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(Bf.FbS, 0, 2 * (size_t)c->nfdofs * c->nv * sizeof(double), s);
+        if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint forward face fluxes");
+        P.FnU = Bf.Fn;
+        P.FbS = Bf.FbS;
+        P.Tq = Bf.Tq;
+        e = launch_adj_hybrid_gauss(dim, c->n, c->cfg.twopoint_flux, c->curv, P, s);
+        if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint element kernel");
+        F.FbS = Bf.FbS;
+        e = launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
+        if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
+        e = launch_adj_hybrid_gauss_finish(dim, c->n, c->curv, P, s);
+    } else if (c->cfg.volume_op != FLOU_OP_STRONG) {
         e = launch_adj_split_dim(dim, c->n, c->cfg.twopoint_flux, c->curv, gauss,
                                  c->cfg.volume_op == FLOU_OP_HYBRID, P, s);
     } else {

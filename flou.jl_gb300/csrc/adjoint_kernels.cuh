@@ -69,6 +69,9 @@ struct AdjFaceParams {
     const double* bc_field;
     double adv[3];          // linear advection velocity (scalar equations)
     int32_t lxf;            // scalar equations: LxF dissipation (else the central flux)
+    // the hybrid operator on Gauss nodes: the face fluxes' cotangents come from the elements
+    // ([2][nv][nfdofs], master and slave side), instead of the lift's transpose (nullable)
+    const double* FbS;
 };
 
 struct AdjElemParams {
@@ -110,6 +113,12 @@ struct AdjElemParams {
     const double* subfr;
     const double* subJ;
     double adv[3];          // linear advection velocity (scalar equations)
+    // the hybrid operator on Gauss nodes (a stage in two element passes around the face VJP):
+    // the forward face fluxes at U, the face-flux cotangents [2][nv][nfdofs] the first pass
+    // writes, and its partial node cotangents (state-sized), which the second pass completes
+    const double* FnU;
+    double* FbS;
+    double* Tq;
 };
 
 // q̄ += (∂F_d/∂q)ᵀ ḡ for the Euler flux along axis d, with v = m/ρ, p, H = (E+p)/ρ:
@@ -945,7 +954,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
         double fl[NV];
         line_sums(s0, m, qL, fl);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) Fb[k] = -fl[k];
+        for (int k = 0; k < NV; ++k) Fb[k] = P.FbS ? P.FbS[k * P.nfdofs + gid] : -fl[k];
     } else {
         endnode(s0, m, &g1i, &dg1);
         double w1 = (CURV ? P.invJn[g1i] : P.invJ[s0 >> 3]) * P.s_lam;
@@ -962,7 +971,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(AdjFaceParams P) {
             double fl[NV];
             line_sums(s1, mm, qR, fl);
 #pragma unroll
-            for (int k = 0; k < NV; ++k) Fb[k] += fl[k];
+            for (int k = 0; k < NV; ++k) Fb[k] += P.FbS ? P.FbS[(NV + k) * P.nfdofs + gid] : fl[k];
         } else {
             endnode(s1, mm, &g2i, &dg2);
             double w2 = (CURV ? P.invJn[g2i] : P.invJ[s1 >> 3]) * P.s_lam;
@@ -1243,8 +1252,11 @@ struct AdjSplitShape {
     // G (Gauss nodes): per line side the cotangent of its projected entropy variables, and per node
     // the cotangents of its two projected-state pair fluxes
     static constexpr int NPROJ = G ? 2 * S::EPB * S::NFD : 0;
-    // H (hybrid operator): per node the subcell-flux values, then their cotangents
-    static constexpr int NGX = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0);
+    // H (hybrid operator): per node the subcell-flux values, then their cotangents; G and H (the
+    // hybrid operator on Gauss nodes): also the projected-state flux differences of both line
+    // sides per node, later the entropy-jump cotangents and the hand-over to the left neighbour
+    static constexpr int NGX = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0) +
+                               (G && H ? 2 * NV * S::NN : 0);
     static constexpr size_t SMEM =
         sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD + NGX) +
         2 * (S::NPAIR + 1);
@@ -1437,7 +1449,9 @@ __device__ __forceinline__ void entropy_vjp(const double* q, double p, double g,
 // metric column of direction D and n Js the line end's subcell interface normal times its surface
 // Jacobian (the forward's metric of the projected states); the metric is in the fluxes, so the
 // cotangent carries ±1 instead of ±Ja.
-template <int DIM, int N, int D, int TP, bool CURV = false>
+// HG (the hybrid operator on Gauss nodes): sw holds the pair weights w' and ∂g[j] becomes
+// l[j]/ω_j (the projected-state pairs enter the node increments through l).
+template <int DIM, int N, int D, int TP, bool CURV = false, bool HG = false>
 __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int e0, const double* sops,
                                                      const double* sprim, const double* sw, double* snode,
                                                      double* sWb, double cb) {
@@ -1468,10 +1482,11 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
 #pragma unroll
             for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
             entropy_of<DIM>(q, g, wj);
+            const double cf = HG ? lv[sd * N + pos] * rcp_refined(P.omega1[pos]) : dgl[sd * N + pos];
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 wt[k] = lv[sd * N + pos] * wj[k];
-                T[k] = dgl[sd * N + pos] * sw[k * NN + j];
+                T[k] = cf * sw[k * NN + j];
             }
         } else {
 #pragma unroll
@@ -1500,7 +1515,8 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
 #pragma unroll
             for (int k = 0; k < NARR; ++k) vj[k] = sprim[k * NN + j];
             const double Ja = CURV ? 1.0 : P.Ja[(e0 + elp) * DIM + D], sg = sd == 0 ? Ja : -Ja;
-            const double dg = dgl[sd * N + pos], lj = lv[sd * N + pos];
+            const double lj = lv[sd * N + pos];
+            const double dg = HG ? lj * rcp_refined(P.omega1[pos]) : dgl[sd * N + pos];
 #pragma unroll
             for (int k = 0; k < NV; ++k) Fb[k] = sg * fma(dg, sw[k * NN + j], -lj * T[k]);
             PrimBar o1;
@@ -1652,32 +1668,104 @@ __device__ __noinline__ void numflux_vjp_any(int kind, const double* a, const do
     }
 }
 
-// H (HybridDivOperator on Gauss-Lobatto nodes, Cartesian; OpDivergence.jl:553-604 with the
-// blending of :781-801), one direction D.  Forward: the high-order subcell fluxes F̄_p =
-// Σ_{r<p} ω_r Ja (Σ_j D♯_rj F♯_rj) (recomputed: pair fluxes, node sums, exclusive scan), the FV
-// fluxes Fv_p = Ja Fv(Q_(p-1), Q_p) along the axis, b = (W_p - W_(p-1))·(F̄_p - Fv_p),
-// δ = max(1 - b/√(b²+c), ½), F_p = Fv_p + δ (F̄_p - Fv_p), dQ_p += (F_p - F_(p+1))/ω_p (F_0 = F_N =
-// 0).  Reverse, with w = λ/J: F̄b_p = w_p/ω_p - w_(p-1)/ω_(p-1); δ̄ = F̄b·(F̄ - Fv), b̄ = -δ̄ c/√(b²+c)³
-// on the unclipped branch; the cotangent of F̄_p is δ F̄b + b̄ ΔW, that of Fv (1-δ) F̄b - b̄ ΔW (through
-// the FV flux VJP to both nodes), ΔW's b̄ (F̄ - Fv) goes through W's VJP; the suffix sums of the F̄
-// cotangents give each node's pair weight w'_r = -ω_r Σ_(p>r) F̄̄_p, left in sH for the split-form
-// pair and node phases.  A node's contribution from the interface on its right is handed over in
-// spb (free between the phases); the node's own goes to qb.
-// CURV (general geometry): the pair fluxes along the averaged metric columns, the node's own
-// column in the diagonal term, ω_p alone as the node-sum weight (the metric is in the fluxes), and
-// each subcell interface's uploaded frame and surface Jacobian for the FV flux.
-template <int DIM, int N, int D, int TP, bool CURV = false>
-__device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
-                                               const double* sops, const double* sprim, const double* sw, double* sH,
-                                               double* spb, const uint8_t* stab, double* qb) {
+// One subcell interface of direction D (between positions pos-1 and pos of a line): the rotated
+// states a, b and, on general geometry, the interface's uploaded frame and surface Jacobian
+// (Cartesian: the positive axis and Ja_DD).
+template <int DIM>
+struct SubcellFace {
+    double a[DIM + 2], b[DIM + 2];
+    FrameTab fr;
+    double Js;
+};
+
+// The interface's frame and the states in it.
+template <int DIM, int N, int D, bool CURV>
+__device__ __forceinline__ void subcell_face(const AdjElemParams& P, int e, int line, int pos, double Ja,
+                                             const double* ql, const double* qr, SubcellFace<DIM>& sf) {
+    constexpr int NFD = Shape<DIM, N>::NFD;
+    sf.Js = Ja;
+    if constexpr (CURV) {
+        const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+        const int64_t si = (((int64_t)e * DIM + D) * NFD + line) * (N + 1) + pos;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            sf.fr.n[r] = P.subfr[r * ns + si];
+            sf.fr.t[r] = P.subfr[(3 + r) * ns + si];
+            sf.fr.b[r] = P.subfr[(6 + r) * ns + si];
+        }
+        sf.Js = P.subJ[si];
+        rotate_to_face<DIM>(ql, sf.fr, sf.a);
+        rotate_to_face<DIM>(qr, sf.fr, sf.b);
+    } else {
+        const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
+        sf.a[0] = ql[0]; sf.b[0] = qr[0]; sf.a[DIM + 1] = ql[DIM + 1]; sf.b[DIM + 1] = qr[DIM + 1];
+        cart_to_face<DIM>(ql, Ax, sf.a);
+        cart_to_face<DIM>(qr, Ax, sf.b);
+    }
+}
+
+// The subcell FV flux Fv = Js Fv(ql, qr) in physical components (PhysicalRegions.jl:68-300).
+template <int DIM, int N, int D, bool CURV>
+__device__ __forceinline__ void subcell_fv(const AdjElemParams& P, int e, int line, int pos, double Ja,
+                                           const double* ql, const double* qr, SubcellFace<DIM>& sf, double* Fv) {
+    constexpr int NV = DIM + 2;
+    double Fr[NV];
+    subcell_face<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf);
+    euler_numflux<DIM>(sf.a, sf.b, P.fvflux, P.fvavg, P.fvintensity, P.gamma, Fr);
+    if constexpr (CURV) {
+        rotate_to_phys<DIM>(Fr, sf.fr, Fv);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fv[k] *= sf.Js;
+    } else {
+        const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
+        Fv[0] = Fr[0] * sf.Js;
+        Fv[DIM + 1] = Fr[DIM + 1] * sf.Js;
+        cart_to_phys<DIM>(Fr, Ax, Fv);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) Fv[1 + k] *= sf.Js;
+    }
+}
+
+// The transpose of subcell_fv: the cotangent Fvb of Fv onto the two states (ol: the left one).
+template <int DIM, int D, bool CURV>
+__device__ __forceinline__ void subcell_fv_vjp(const AdjElemParams& P, const SubcellFace<DIM>& sf, const double* Fvb,
+                                               double* ol, double* orr) {
+    constexpr int NV = DIM + 2;
+    const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
+    double Frb[NV], ab[NV], bbr[NV], t[NV];
+    if constexpr (CURV) {
+        rotate_to_face<DIM>(Fvb, sf.fr, t);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Frb[k] = sf.Js * t[k];
+    } else {
+        Frb[0] = sf.Js * Fvb[0];
+        Frb[DIM + 1] = sf.Js * Fvb[DIM + 1];
+        cart_to_face<DIM>(Fvb, Ax, t);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) Frb[1 + k] = sf.Js * t[1 + k];
+    }
+    numflux_vjp_any<DIM>(P.fvkind, sf.a, sf.b, P.fvintensity, P.gamma, Frb, ab, bbr);
+    if constexpr (CURV) {
+        rotate_to_phys<DIM>(ab, sf.fr, ol);
+        rotate_to_phys<DIM>(bbr, sf.fr, orr);
+    } else {
+        ol[0] = ab[0]; ol[DIM + 1] = ab[DIM + 1]; orr[0] = bbr[0]; orr[DIM + 1] = bbr[DIM + 1];
+        cart_to_phys<DIM>(ab, Ax, ol);
+        cart_to_phys<DIM>(bbr, Ax, orr);
+    }
+}
+
+// The hybrid operators' forward pair fluxes F♯(Q_a, Q_b) of direction D, every pair of the block
+// once, into spb as [NV][NPT] (CURV: along the averaged metric column).
+template <int DIM, int N, int D, int TP, bool CURV>
+__device__ __forceinline__ void hybrid_pair_fluxes(const AdjElemParams& P, int e0, const double* sprim, double* spb,
+                                                   const uint8_t* stab) {
     using S = Shape<DIM, N>;
-    using A = AdjSplitShape<DIM, N, TP, false, true>;
+    using A = AdjSplitShape<DIM, N, TP>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR, NARR = A::NARR;
     constexpr int NPT = A::NPT;
     const double g = P.gamma;
-    const double* Dsh = sops + N * N;
     const int tid = threadIdx.x;
-    // forward pair fluxes into spb as [NV][NPT]
     for (int kp = tid; kp < NPT; kp += blockDim.x) {
         const int elp = kp / (NFD * NPAIR);
         const int r = kp - elp * (NFD * NPAIR);
@@ -1711,6 +1799,76 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
 #pragma unroll
         for (int k = 0; k < NV; ++k) spb[k * NPT + kp] = F[k];
     }
+}
+
+// Σ_j D♯_pj F♯_pj of node gi (position pos on its line) from the pair fluxes in spb, with the
+// diagonal D♯_pp F(Q_p) (CURV: the node's contravariant flux).
+template <int DIM, int N, int D, int TP, bool CURV>
+__device__ __forceinline__ void hybrid_node_sum(const AdjElemParams& P, int64_t gi, int el, int pos, int line,
+                                                const double* Dsh, const double* spb, double* acc) {
+    using S = Shape<DIM, N>;
+    constexpr int NV = DIM + 2, NFD = S::NFD, NPAIR = S::NPAIR;
+    constexpr int NPT = AdjSplitShape<DIM, N, TP>::NPT;
+    const double g = P.gamma;
+    double q[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
+    if constexpr (CURV) {
+        double nrm[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
+        euler_flux_n<DIM>(q, nrm, g, acc);
+    } else {
+        euler_flux_axis<DIM, D>(q, g, acc);
+    }
+    const double dii = Dsh[pos + pos * N];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] *= dii;
+    const int pbase = el * NFD * NPAIR + line * NPAIR;
+#pragma unroll
+    for (int t = 1; t < N; ++t) {
+        const int j = pos + t < N ? pos + t : pos + t - N;
+        const int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
+        const int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+        const double a = Dsh[pos + j * N];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = fma(a, spb[k * NPT + pidx], acc[k]);
+    }
+}
+
+// The pressure of a conserved state.
+template <int DIM>
+__device__ __forceinline__ double pressure_of(const double* q, double g) {
+    double ke = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k], ke);
+    return (g - 1.0) * fma(-0.5, ke * rcp_refined(q[0]), q[DIM + 1]);
+}
+
+// H (HybridDivOperator on Gauss-Lobatto nodes, Cartesian; OpDivergence.jl:553-604 with the
+// blending of :781-801), one direction D.  Forward: the high-order subcell fluxes F̄_p =
+// Σ_{r<p} ω_r Ja (Σ_j D♯_rj F♯_rj) (recomputed: pair fluxes, node sums, exclusive scan), the FV
+// fluxes Fv_p = Ja Fv(Q_(p-1), Q_p) along the axis, b = (W_p - W_(p-1))·(F̄_p - Fv_p),
+// δ = max(1 - b/√(b²+c), ½), F_p = Fv_p + δ (F̄_p - Fv_p), dQ_p += (F_p - F_(p+1))/ω_p (F_0 = F_N =
+// 0).  Reverse, with w = λ/J: F̄b_p = w_p/ω_p - w_(p-1)/ω_(p-1); δ̄ = F̄b·(F̄ - Fv), b̄ = -δ̄ c/√(b²+c)³
+// on the unclipped branch; the cotangent of F̄_p is δ F̄b + b̄ ΔW, that of Fv (1-δ) F̄b - b̄ ΔW (through
+// the FV flux VJP to both nodes), ΔW's b̄ (F̄ - Fv) goes through W's VJP; the suffix sums of the F̄
+// cotangents give each node's pair weight w'_r = -ω_r Σ_(p>r) F̄̄_p, left in sH for the split-form
+// pair and node phases.  A node's contribution from the interface on its right is handed over in
+// spb (free between the phases); the node's own goes to qb.
+// CURV (general geometry): the pair fluxes along the averaged metric columns, the node's own
+// column in the diagonal term, ω_p alone as the node-sum weight (the metric is in the fluxes), and
+// each subcell interface's uploaded frame and surface Jacobian for the FV flux.
+template <int DIM, int N, int D, int TP, bool CURV = false>
+__device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
+                                               const double* sops, const double* sprim, const double* sw, double* sH,
+                                               double* spb, const uint8_t* stab, double* qb) {
+    using S = Shape<DIM, N>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
+    const double g = P.gamma;
+    const double* Dsh = sops + N * N;
+    const int tid = threadIdx.x;
+    hybrid_pair_fluxes<DIM, N, D, TP, CURV>(P, e0, sprim, spb, stab);
     __syncthreads();
     const int e = e0 + el;
     int pos = 0, line = 0;
@@ -1718,30 +1876,8 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
     const int64_t gi = (int64_t)e * NPE + i;
     const double Ja = active ? (CURV ? 1.0 : P.Ja[e * DIM + D]) : 0.0;
     if (active) {   // ω_p Ja Σ_j D♯_pj F♯_pj (with the diagonal D♯_pp F(Q_p))
-        double q[NV], acc[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
-        if constexpr (CURV) {
-            double nrm[DIM];
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
-            euler_flux_n<DIM>(q, nrm, g, acc);
-        } else {
-            euler_flux_axis<DIM, D>(q, g, acc);
-        }
-        const double dii = Dsh[pos + pos * N];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) acc[k] *= dii;
-        const int pbase = el * NFD * NPAIR + line * NPAIR;
-#pragma unroll
-        for (int t = 1; t < N; ++t) {
-            const int j = pos + t < N ? pos + t : pos + t - N;
-            const int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
-            const int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
-            const double a = Dsh[pos + j * N];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) acc[k] = fma(a, spb[k * NPT + pidx], acc[k]);
-        }
+        double acc[NV];
+        hybrid_node_sum<DIM, N, D, TP, CURV>(P, gi, el, pos, line, Dsh, spb, acc);
         const double wq = P.omega1[pos] * Ja;
 #pragma unroll
         for (int k = 0; k < NV; ++k) sH[k * NN + tid] = wq * acc[k];
@@ -1767,44 +1903,14 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
     if (active && pos > 0) {   // the subcell interface between pos-1 and pos
         const int il = el * NPE + tp_node<DIM>(N, D, line, pos - 1);
         const int64_t gl = (int64_t)e0 * NPE + il;
-        double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV], wl[NV], wr[NV];
+        double ql[NV], qr[NV], Fv[NV], wl[NV], wr[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             ql[k] = P.U[k * P.ndofs + gl];
             qr[k] = P.U[k * P.ndofs + gi];
         }
-        const FrameAxes Ax = frame_axes<DIM>(2 * D + 1);
-        FrameTab fr;   // CURV: the subcell interface's frame and surface Jacobian
-        double Js = Ja;
-        if constexpr (CURV) {
-            const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
-            const int64_t si = (((int64_t)e * DIM + D) * NFD + line) * (N + 1) + pos;
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                fr.n[r] = P.subfr[r * ns + si];
-                fr.t[r] = P.subfr[(3 + r) * ns + si];
-                fr.b[r] = P.subfr[(6 + r) * ns + si];
-            }
-            Js = P.subJ[si];
-            rotate_to_face<DIM>(ql, fr, a);
-            rotate_to_face<DIM>(qr, fr, b);
-        } else {
-            a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-            cart_to_face<DIM>(ql, Ax, a);
-            cart_to_face<DIM>(qr, Ax, b);
-        }
-        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
-        if constexpr (CURV) {
-            rotate_to_phys<DIM>(Fr, fr, Fv);
-#pragma unroll
-            for (int k = 0; k < NV; ++k) Fv[k] *= Js;
-        } else {
-            Fv[0] = Fr[0] * Js;
-            Fv[DIM + 1] = Fr[DIM + 1] * Js;
-            cart_to_phys<DIM>(Fr, Ax, Fv);
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) Fv[1 + k] *= Js;
-        }
+        SubcellFace<DIM> sf;
+        subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
         entropy_of<DIM>(ql, g, wl);
         entropy_of<DIM>(qr, g, wr);
         double bb = 0.0, dW[NV], Fh[NV];
@@ -1833,34 +1939,9 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
             Fvb[k] = fma(1.0 - dlt, Fb[k], -bbar * dW[k]);
             wbar[k] = bbar * (Fh[k] - Fv[k]);
         }
-        double Frb[NV], ab[NV], bbr[NV], t[NV], ol[NV], orr[NV];
-        if constexpr (CURV) {
-            rotate_to_face<DIM>(Fvb, fr, t);
-#pragma unroll
-            for (int k = 0; k < NV; ++k) Frb[k] = Js * t[k];
-        } else {
-            Frb[0] = Js * Fvb[0];
-            Frb[DIM + 1] = Js * Fvb[DIM + 1];
-            cart_to_face<DIM>(Fvb, Ax, t);
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) Frb[1 + k] = Js * t[1 + k];
-        }
-        numflux_vjp_any<DIM>(P.fvkind, a, b, P.fvintensity, g, Frb, ab, bbr);
-        if constexpr (CURV) {
-            rotate_to_phys<DIM>(ab, fr, ol);
-            rotate_to_phys<DIM>(bbr, fr, orr);
-        } else {
-            ol[0] = ab[0]; ol[DIM + 1] = ab[DIM + 1]; orr[0] = bbr[0]; orr[DIM + 1] = bbr[DIM + 1];
-            cart_to_phys<DIM>(ab, Ax, ol);
-            cart_to_phys<DIM>(bbr, Ax, orr);
-        }
-        auto pressure = [&](const double* q) {
-            double ke = 0.0;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) ke = fma(q[1 + k], q[1 + k], ke);
-            return (g - 1.0) * fma(-0.5, ke * rcp_refined(q[0]), q[DIM + 1]);
-        };
-        const double pr = pressure(qr), plv = pressure(ql);
+        double ol[NV], orr[NV];
+        subcell_fv_vjp<DIM, D, CURV>(P, sf, Fvb, ol, orr);
+        const double pr = pressure_of<DIM>(qr, g), plv = pressure_of<DIM>(ql, g);
 #pragma unroll
         for (int k = 0; k < NV; ++k) qb[k] += orr[k];
         entropy_vjp<DIM>(qr, pr, g, wbar, qb);
@@ -1888,6 +1969,267 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
             }
         }
     }
+    if (active && pos < N - 1) {   // the cotangent from the interface on this node's right
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qb[k] += spb[k * NN + tid];
+    }
+    __syncthreads();
+}
+
+// G and H (HybridDivOperator on Gauss nodes, OpDivergence.jl:633-780), one direction D, in the first
+// of the stage's two element passes.  Forward (recomputed): per line the entropy-projected states
+// Q̃_l, Q̃_r and every node's pair with them, Fl_i = F♯(Q_i, Q̃_l) - Σ_j l_l[j] F♯(Q_j, Q̃_l) (Fr
+// alike), the element's side values of its line's face fluxes fls = ±Fn_left, frs = ±Fn_right, the
+// node increments sH_i = ω_i Ja Σ_j D♯_ij F♯_ij - l_l[i] (Ja Fl_i - fls) + l_r[i] (Ja Fr_i + frs),
+// the FV fluxes Fv_p (p = 1..N-1) and the blended scan F_0 = -fls, X_p = F_(p-1) + sH_(p-1),
+// F_p = Fv_p + δ_p (X_p - Fv_p), δ_p from b_p = (W_p - W_(p-1))·(X_p - Fv_p); dQ_i += (F_i -
+// F_(i+1))/ω_i with F_N = frs.  Reverse: one thread per line runs the scan backwards (the
+// cotangent of F_p is w_p/ω_p - w_(p-1)/ω_(p-1) plus what X_(p+1) hands back), leaving per
+// interface the cotangents of Fv_p and of the entropy jump, the pair weights w'_i = -ω_i s̄H_i in
+// sH (s̄H_(N-1) = 0: the last increment closes on frs, not on the scan), and the cotangents of fls
+// (-w_0/ω_0 - X̄_1 + Σ l_l s̄H) and of frs (-w_(N-1)/ω_(N-1) + Σ l_r s̄H), which the end nodes
+// write to FbS for the face VJP.  The projected-state pairs take l_s[i] w'_i/ω_i as their
+// coefficients in adj_split_projection.
+// Shared memory: sF2 [2][NV][NN] (the projected pairs of both sides, then per interface Fv and
+// X - Fv, then their cotangents), scl (the projection's [NV][NPROJ], free until it runs: the line
+// reductions Σ_j l_s[j] F♯(Q_j, Q̃_s)), sdW (the projection's node array, zeroed when it runs:
+// the entropy jumps, then the face-flux cotangents at the end nodes).
+template <int DIM, int N, int D, int TP, bool CURV = false>
+__device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
+                                                     const double* sops, const double* sprim, const double* sw,
+                                                     double* sH, double* spb, const uint8_t* stab, double* sF2,
+                                                     double* scl, double* sdW, double* qb) {
+    using S = Shape<DIM, N>;
+    using A = AdjSplitShape<DIM, N, TP, true, true>;
+    constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR;
+    constexpr int NPROJ = A::NPROJ;
+    static_assert(N <= 8, "one lane per node of a line within a group of 8");
+    const double g = P.gamma;
+    const double* Dsh = sops + N * N;
+    const double* lv = sops + 2 * N * N;   // l_l, then l_r
+    const int tid = threadIdx.x;
+    hybrid_pair_fluxes<DIM, N, D, TP, CURV>(P, e0, sprim, spb, stab);
+    auto gsum = [](double v) {
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    };
+    // the projected states and their pairs with every node of the line: one group of 8 lanes per
+    // line side, one lane per node (the line sums are butterfly shuffles within the group)
+    constexpr int TOTAL = ((NPROJ * 8 + 31) / 32) * 32;
+    for (int t = tid; t < TOTAL; t += blockDim.x) {
+        const int grp = t >> 3, pos = t & 7;
+        const int elp = grp / (2 * NFD), rr = grp - elp * 2 * NFD, line = rr >> 1, sd = rr & 1;
+        const bool grp_on = grp < NPROJ && e0 + elp < P.nelem;
+        const bool on = grp_on && pos < N;
+        const int j = on ? elp * NPE + tp_node<DIM>(N, D, line, pos) : 0;
+        double q[NV], wt[NV];
+        if (on) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
+            entropy_of<DIM>(q, g, wt);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) wt[k] *= lv[sd * N + pos];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) wt[k] = 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) wt[k] = gsum(wt[k]);
+        double qt[NV], pt = 1.0;
+        if (grp_on) {
+            pt = state_of_entropy<DIM>(wt, g, qt);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qt[k] = k == 0 || k == DIM + 1 ? 1.0 : 0.0;
+        }
+        double cl[NV];
+        if (on) {
+            double vt[NARR], vj[NARR], F[NV];
+            split_node_values<DIM, TP>(qt, pt, vt);
+#pragma unroll
+            for (int k = 0; k < NARR; ++k) vj[k] = sprim[k * NN + j];
+            if constexpr (CURV) {
+                const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+                const int64_t si = (((int64_t)(e0 + elp) * DIM + D) * NFD + line) * (N + 1) + (sd ? N : 0);
+                const int64_t gj = (int64_t)e0 * NPE + j;
+                const double js = P.subJ[si];
+                double nrm[DIM];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                    nrm[k] = 0.5 * fma(P.subfr[k * ns + si], js, P.Jan[(k + D * DIM) * P.ndofs + gj]);
+                split_pair_flux<DIM, -1, TP>(vj, vt, q, qt, g, F, nrm);
+            } else {
+                split_pair_flux<DIM, D, TP>(vj, vt, q, qt, g, F);
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                sF2[(sd * NV + k) * NN + j] = F[k];
+                cl[k] = lv[sd * N + pos] * F[k];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) cl[k] = 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) cl[k] = gsum(cl[k]);
+        if (grp_on && pos == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) scl[k * NPROJ + grp] = cl[k];
+        }
+    }
+    __syncthreads();
+    const int e = e0 + el;
+    int pos = 0, line = 0;
+    tp_coords<DIM>(N, i, D, pos, line);
+    const int64_t gi = (int64_t)e * NPE + i;
+    const double Ja = active ? (CURV ? 1.0 : P.Ja[e * DIM + D]) : 0.0;
+    int32_t pl = 0, pr = 0;
+    int64_t ofl = 0, ofr = 0;   // the face dofs of the line's two ends
+    if (active) {
+        pl = P.elem_face[e * 2 * DIM + 2 * D];
+        pr = P.elem_face[e * 2 * DIM + 2 * D + 1];
+        ofl = trace_offset<DIM, N, CURV>(P, e, 2 * D, line);
+        ofr = trace_offset<DIM, N, CURV>(P, e, 2 * D + 1, line);
+        if (!index_ok(ofl, P.nfdofs, P.status, e)) ofl = 0;
+        if (!index_ok(ofr, P.nfdofs, P.status, e)) ofr = 0;
+        const double sl = (pl & 1) ? -1.0 : 1.0, sr = (pr & 1) ? -1.0 : 1.0;
+        double acc[NV];
+        hybrid_node_sum<DIM, N, D, TP, CURV>(P, gi, el, pos, line, Dsh, spb, acc);
+        const int c0 = 2 * (el * NFD + line);
+        const double wq = P.omega1[pos] * Ja;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double fls = sl * __ldcg(P.FnU + k * P.nfdofs + ofl);
+            const double frs = sr * __ldcg(P.FnU + k * P.nfdofs + ofr);
+            const double Fl = sF2[k * NN + tid] - scl[k * NPROJ + c0];
+            const double Fr = sF2[(NV + k) * NN + tid] - scl[k * NPROJ + c0 + 1];
+            sH[k * NN + tid] = wq * acc[k] - lv[pos] * fma(Ja, Fl, -fls) + lv[N + pos] * fma(Ja, Fr, frs);
+            if (pos == 0) sF2[k * NN + tid] = -fls;   // F_0, read by the line's scan
+        }
+    }
+    if (active && pos > 0) {   // the FV flux of the interface on the node's left, and the entropy jump
+        const int64_t gl = (int64_t)e0 * NPE + el * NPE + tp_node<DIM>(N, D, line, pos - 1);
+        double ql[NV], qr[NV], Fv[NV], wl[NV], wr[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ql[k] = P.U[k * P.ndofs + gl];
+            qr[k] = P.U[k * P.ndofs + gi];
+        }
+        SubcellFace<DIM> sf;
+        subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
+        entropy_of<DIM>(ql, g, wl);
+        entropy_of<DIM>(qr, g, wr);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sF2[k * NN + tid] = Fv[k];
+            sdW[k * NN + tid] = wr[k] - wl[k];
+        }
+    }
+    __syncthreads();
+    for (int t = tid; t < S::EPB * NFD; t += blockDim.x) {   // the scan, forward then reverse
+        const int elp = t / NFD, ln = t - elp * NFD;
+        if (e0 + elp >= P.nelem) continue;
+        const int j0 = elp * NPE + tp_node<DIM>(N, D, ln, 0);
+        double Fb[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fb[k] = sF2[k * NN + j0];
+        int jp = j0;
+        for (int pp = 1; pp < N; ++pp) {
+            const int jn = elp * NPE + tp_node<DIM>(N, D, ln, pp);
+            double d[NV], bb = 0.0;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                d[k] = (Fb[k] + sH[k * NN + jp]) - sF2[k * NN + jn];
+                bb = fma(sdW[k * NN + jn], d[k], bb);
+            }
+            const double dl = sqrt_refined(fma(bb, bb, P.blend));
+            const double dlt = fmax((dl - bb) * rcp_refined(dl), 0.5);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                Fb[k] = fma(dlt, d[k], sF2[k * NN + jn]);
+                sF2[(NV + k) * NN + jn] = d[k];
+            }
+            jp = jn;
+        }
+        double carry[NV], sl_[NV], sr_[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) carry[k] = sl_[k] = sr_[k] = 0.0;
+        int jn = jp;   // the line's last node
+        for (int pp = N - 1; pp >= 1; --pp) {
+            jp = elp * NPE + tp_node<DIM>(N, D, ln, pp - 1);
+            const double iwp = rcp_refined(P.omega1[pp]), iwm = rcp_refined(P.omega1[pp - 1]);
+            double Gb[NV], d[NV], dW[NV], bb = 0.0, db = 0.0;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                Gb[k] = fma(sw[k * NN + jn], iwp, -sw[k * NN + jp] * iwm) + carry[k];
+                d[k] = sF2[(NV + k) * NN + jn];
+                dW[k] = sdW[k * NN + jn];
+                bb = fma(dW[k], d[k], bb);
+                db = fma(Gb[k], d[k], db);
+            }
+            const double dl = sqrt_refined(fma(bb, bb, P.blend)), idl = rcp_refined(dl);
+            const double draw = (dl - bb) * idl;
+            const bool free_ = 0.5 < draw;   // Base.max(draw, 0.5) takes draw only above 0.5
+            const double dlt = free_ ? draw : 0.5;
+            const double bbar = free_ ? -db * P.blend * idl * idl * idl : 0.0;
+            const double wm = P.omega1[pp - 1];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double xb = fma(dlt, Gb[k], bbar * dW[k]);   // the cotangent of X_pp
+                sF2[k * NN + jn] = fma(1.0 - dlt, Gb[k], -bbar * dW[k]);
+                sF2[(NV + k) * NN + jn] = bbar * d[k];
+                sH[k * NN + jp] = -wm * xb;
+                sl_[k] = fma(lv[pp - 1], xb, sl_[k]);
+                sr_[k] = fma(lv[N + pp - 1], xb, sr_[k]);
+                carry[k] = xb;
+            }
+            jn = jp;
+        }
+        const int jl = elp * NPE + tp_node<DIM>(N, D, ln, N - 1);
+        const double iw0 = rcp_refined(P.omega1[0]), iwl = rcp_refined(P.omega1[N - 1]);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sH[k * NN + jl] = 0.0;
+            sdW[k * NN + j0] = sl_[k] - fma(sw[k * NN + j0], iw0, carry[k]);
+            sdW[k * NN + jl] = fma(-sw[k * NN + jl], iwl, sr_[k]);
+        }
+    }
+    __syncthreads();
+    if (active && pos > 0) {   // the FV flux and the entropy jump transposed
+        const int il = el * NPE + tp_node<DIM>(N, D, line, pos - 1);
+        const int64_t gl = (int64_t)e0 * NPE + il;
+        double ql[NV], qr[NV], Fvb[NV], wbar[NV], ol[NV], orr[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            ql[k] = P.U[k * P.ndofs + gl];
+            qr[k] = P.U[k * P.ndofs + gi];
+            Fvb[k] = sF2[k * NN + tid];
+            wbar[k] = sF2[(NV + k) * NN + tid];
+        }
+        SubcellFace<DIM> sf;
+        subcell_face<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf);
+        subcell_fv_vjp<DIM, D, CURV>(P, sf, Fvb, ol, orr);
+        const double prr = pressure_of<DIM>(qr, g), plv = pressure_of<DIM>(ql, g);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) qb[k] += orr[k];
+        entropy_vjp<DIM>(qr, prr, g, wbar, qb);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) wbar[k] = -wbar[k];
+        entropy_vjp<DIM>(ql, plv, g, wbar, ol);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) spb[k * NN + il] = ol[k];
+    }
+    if (active && (pos == 0 || pos == N - 1)) {   // the face-flux cotangents, by side of the face
+        const bool left = pos == 0;
+        const int32_t pk = left ? pl : pr;
+        const int64_t o = left ? ofl : ofr;
+        const double sg = (pk & 1) ? -1.0 : 1.0;
+        double* dst = P.FbS + (int64_t)(pk & 1) * NV * P.nfdofs;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dst[k * P.nfdofs + o] = sg * sdW[k * NN + tid];
+    }
+    __syncthreads();
     if (active && pos < N - 1) {   // the cotangent from the interface on this node's right
 #pragma unroll
         for (int k = 0; k < NV; ++k) qb[k] += spb[k * NN + tid];
@@ -1980,8 +2322,9 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
 // CURV: the diagonal term is the contravariant flux of node i (its own metric column), and a slave
 // face reads its trace cotangent through the orientation.
 // G: also the node's projected-state pair cotangents (snode), the spread of the projected
-// entropy-variable cotangents (into wb), and the trace cotangents through l at every node.
-template <int DIM, int N, int D, int TP, bool CURV = false, bool G = false>
+// entropy-variable cotangents (into wb), and the trace cotangents through l at every node (G and
+// H: not yet known; the stage's second element pass adds them).
+template <int DIM, int N, int D, int TP, bool CURV = false, bool G = false, bool H = false>
 __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
                                                 const double* Dsh, const double* sw, const double* spb,
                                                 const double* v, double rho, double p, double g1, double* qb,
@@ -2002,14 +2345,14 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         double vv = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) vv = fma(v[k], v[k], vv);
-        double H = (P.U[(DIM + 1) * P.ndofs + gi] + p) * rcp_refined(rho);
+        double Hq = (P.U[(DIM + 1) * P.ndofs + gi] + p) * rcp_refined(rho);
         if constexpr (CURV) {
             double nrm[DIM];
 #pragma unroll
             for (int k = 0; k < DIM; ++k) nrm[k] = P.Jan[(k + D * DIM) * P.ndofs + gi];
-            euler_flux_vjp_n<DIM>(nrm, v, vv, H, g1, Gd, -1.0, qb);
+            euler_flux_vjp_n<DIM>(nrm, v, vv, Hq, g1, Gd, -1.0, qb);
         } else {
-            euler_flux_vjp<DIM>(D, v, vv, H, g1, Gd, -P.Ja[e * DIM + D], qb);
+            euler_flux_vjp<DIM>(D, v, vv, Hq, g1, Gd, -P.Ja[e * DIM + D], qb);
         }
     }
     int pbase = el * NFD * NPAIR + line * NPAIR;
@@ -2040,7 +2383,7 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         for (int k = 0; k < NV; ++k)
             wb[k] = fma(lv[pos], sWb[k * A::NPROJ + c0], fma(lv[N + pos], sWb[k * A::NPROJ + c0 + 1], wb[k]));
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
+        for (int side = 0; side < (H ? 0 : 2); ++side) {
             const int fk = 2 * D + side;
             int32_t pk = P.elem_face[e * 2 * DIM + fk];
             const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
@@ -2061,6 +2404,39 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
     }
 }
 
+// The adjoint stage combination at node gi with its transposed residual qb.
+template <int DIM>
+__device__ __forceinline__ void adj_node_epilogue(const AdjElemParams& P, int64_t gi, const double* qb) {
+    constexpr int NV = DIM + 2;
+    for (int k = 0; k < NV; ++k) {
+        double ain = P.Ain[k * P.ndofs + gi];
+        double o = fma(P.alpha, ain, qb[k]);
+        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
+        if (P.writeB) {
+            double b = P.delta_B * ain;
+            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
+            P.B[k * P.ndofs + gi] = b;
+        }
+        P.Aout[k * P.ndofs + gi] = o;
+        if (P.K) P.K[k * P.ndofs + gi] = fma(P.kA, ain, P.kB * o);
+    }
+}
+
+// cbar[e] += the element's share of its faces' intensity cotangents (interior faces half each).
+template <int DIM, int N>
+__device__ __forceinline__ void adj_elem_cbar(const AdjElemParams& P, int e) {
+    using S = Shape<DIM, N>;
+    double cacc = 0.0;
+    for (int fk = 0; fk < 2 * DIM; ++fk) {
+        int32_t pk = P.elem_face[e * 2 * DIM + fk];
+        int fc = pk >> 1;
+        if (!index_ok((int64_t)fc * S::NFD + S::NFD - 1, P.nfdofs, P.status, e)) continue;
+        double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
+        for (int m = 0; m < S::NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * S::NFD + m), cacc);
+    }
+    P.cbar[e] += cacc;
+}
+
 // H: the hybrid operator (adj_hybrid_dir gives the pair weights of each direction).
 template <int DIM, int N, int TP, bool CURV = false, bool G = false, bool H = false>
 __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP, G, H>::MINB)
@@ -2078,6 +2454,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     double* sWb = sJD + A::NSD;          // G: [NV][NPROJ] projected entropy-variable cotangents
     double* snode = sWb + NV * A::NPROJ; // G: [NPB][NN] projected-state pair cotangents per node
     double* sHy = snode + (G ? NPB * NN : 0);   // H: [NV][NN] subcell fluxes, then the pair weights
+    double* sF2 = sHy + (H ? NV * NN : 0);      // G and H: [2][NV][NN] (adj_hybrid_gauss_dir)
     uint8_t* stab = (uint8_t*)(sJD + A::NSD + A::NGX);
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
@@ -2154,7 +2531,17 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     const double* swd = H ? sHy : sw;   // the pair weights
 #pragma unroll 1
     for (int dir = 0; dir < DIM; ++dir) {
-        if constexpr (H) {
+        if constexpr (G && H) {
+            if (dir == 0)
+                adj_hybrid_gauss_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
+                                                          sWb, snode, qb);
+            else if (dir == 1)
+                adj_hybrid_gauss_dir<DIM, N, D1, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
+                                                           sWb, snode, qb);
+            else
+                adj_hybrid_gauss_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
+                                                           sWb, snode, qb);
+        } else if constexpr (H) {
             if (dir == 0)
                 adj_hybrid_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
             else if (dir == 1)
@@ -2166,21 +2553,21 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         if constexpr (G) {
-            if (dir == 0) adj_split_projection<DIM, N, 0, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
-            else if (dir == 1) adj_split_projection<DIM, N, D1, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
-            else adj_split_projection<DIM, N, D2, TP, CURV>(P, e0, sops, sprim, sw, snode, sWb, cb);
+            if (dir == 0) adj_split_projection<DIM, N, 0, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
+            else if (dir == 1) adj_split_projection<DIM, N, D1, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
+            else adj_split_projection<DIM, N, D2, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
         }
         __syncthreads();
         if (active) {
             if (dir == 0)
-                adj_split_nodes<DIM, N, 0, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc, snode,
-                                                        sWb, wb);
+                adj_split_nodes<DIM, N, 0, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
+                                                           snode, sWb, wb);
             else if (dir == 1)
-                adj_split_nodes<DIM, N, D1, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
-                                                         snode, sWb, wb);
+                adj_split_nodes<DIM, N, D1, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
+                                                            snode, sWb, wb);
             else
-                adj_split_nodes<DIM, N, D2, TP, CURV, G>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
-                                                         snode, sWb, wb);
+                adj_split_nodes<DIM, N, D2, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
+                                                            snode, sWb, wb);
         }
         __syncthreads();
     }
@@ -2204,28 +2591,12 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + gi];
         entropy_vjp<DIM>(q, p, g, wb, qb);
     }
-    for (int k = 0; k < NV; ++k) {
-        double ain = P.Ain[k * P.ndofs + gi];
-        double o = fma(P.alpha, ain, qb[k]);
-        if (P.readB) o = fma(P.beta, P.B[k * P.ndofs + gi], o);
-        if (P.writeB) {
-            double b = P.delta_B * ain;
-            if (P.gamma_B != 0.0) b = fma(P.gamma_B, P.B[k * P.ndofs + gi], b);
-            P.B[k * P.ndofs + gi] = b;
-        }
-        P.Aout[k * P.ndofs + gi] = o;
-        if (P.K) P.K[k * P.ndofs + gi] = fma(P.kA, ain, P.kB * o);
-    }
-    if (P.cbar && i == 0) {
-        double cacc = 0.0;
-        for (int fk = 0; fk < 2 * DIM; ++fk) {
-            int32_t pk = P.elem_face[e * 2 * DIM + fk];
-            int fc = pk >> 1;
-            if (!index_ok((int64_t)fc * S::NFD + S::NFD - 1, P.nfdofs, P.status, e)) continue;
-            double wgt = P.face_elem[2 * fc + 1] < 0 ? 1.0 : 0.5;
-            for (int m = 0; m < S::NFD; ++m) cacc = fma(wgt, __ldcg(P.Ibar + (int64_t)fc * S::NFD + m), cacc);
-        }
-        P.cbar[e] += cacc;
+    if constexpr (G && H) {   // the traces' cotangents follow the face VJP
+#pragma unroll
+        for (int k = 0; k < NV; ++k) P.Tq[k * P.ndofs + gi] = qb[k];
+    } else {
+        adj_node_epilogue<DIM>(P, gi, qb);
+        if (P.cbar && i == 0) adj_elem_cbar<DIM, N>(P, e);
     }
 }
 
@@ -2271,14 +2642,69 @@ cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t
     return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV, G, H>(n, P, s);
 }
 
-// Whether the Gauss-node split (G) or hybrid (H) adjoint tile fits in shared memory (all but the
-// Kennedy-Gruber 3D p=7 tile do).
-inline bool adj_split_tile_fits(int dim, int n, int tp, bool hybrid) {
-    if (!(dim == 3 && n == 8 && tp == FLOU_TP_KENNEDY_GRUBER)) return true;
-    return hybrid ? AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, false, true>::SMEM <= 227 * 1024
-                  : AdjSplitShape<3, 8, FLOU_TP_KENNEDY_GRUBER, true>::SMEM <= 227 * 1024;
+// Whether the split adjoint tile (G: Gauss nodes, H: the hybrid operator) fits in shared memory:
+// all but the 3D p=7 tiles of the Gauss-node forms (the split form's with the Kennedy-Gruber flux,
+// the hybrid operator's with every two-point flux) do.
+template <int TP>
+constexpr size_t adj_split_smem_3d8(bool G, bool H) {
+    return G && H ? AdjSplitShape<3, 8, TP, true, true>::SMEM
+                  : (G ? AdjSplitShape<3, 8, TP, true, false>::SMEM : AdjSplitShape<3, 8, TP, false, true>::SMEM);
+}
+inline bool adj_split_tile_fits(int dim, int n, int tp, bool gauss, bool hybrid) {
+    if (!(dim == 3 && n == 8)) return true;
+    const size_t smem = tp == FLOU_TP_KENNEDY_GRUBER ? adj_split_smem_3d8<FLOU_TP_KENNEDY_GRUBER>(gauss, hybrid)
+                        : tp == FLOU_TP_STD_AVERAGE  ? adj_split_smem_3d8<FLOU_TP_STD_AVERAGE>(gauss, hybrid)
+                                                     : adj_split_smem_3d8<FLOU_TP_CHANDRASHEKAR>(gauss, hybrid);
+    return smem <= 227 * 1024;
 }
 
+// The second element pass of a hybrid stage on Gauss nodes: the first pass's partial node
+// cotangents Tq, plus every node's l_l[pos] and l_r[pos] shares of its lines' trace cotangents
+// (from the face VJP), then the stage combination and cbar.  One thread per node.
+template <int DIM, int N, bool CURV = false>
+__global__ void __launch_bounds__(256) adj_hybrid_gauss_finish_kernel(AdjElemParams P) {
+    constexpr int NV = DIM + 2, NPE = Shape<DIM, N>::NPE;
+    const int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= P.ndofs) return;
+    const int e = (int)(gi / NPE), i = (int)(gi - (int64_t)e * NPE);
+    const double* lv = P.ops + 2 * N * N;
+    double qb[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) qb[k] = P.Tq[k * P.ndofs + gi];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int pos, line;
+        tp_coords<DIM>(N, i, d, pos, line);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int fk = 2 * d + side;
+            const int32_t pk = P.elem_face[e * 2 * DIM + fk];
+            const double* fsrc = (pk & 1) ? P.QbR : P.QbL;
+            const int64_t o = trace_offset<DIM, N, CURV>(P, e, fk, line);
+            if (!index_ok(o, P.nfdofs, P.status, e)) continue;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) qb[k] = fma(lv[side * N + pos], __ldcg(fsrc + k * P.nfdofs + o), qb[k]);
+        }
+    }
+    adj_node_epilogue<DIM>(P, gi, qb);
+    if (P.cbar && i == 0) adj_elem_cbar<DIM, N>(P, e);
+}
+
+template <int DIM, bool CURV = false>
+cudaError_t launch_adj_hybrid_gauss_finish_t(int n, const AdjElemParams& P, cudaStream_t s) {
+    const int grid = (int)((P.ndofs + 255) / 256);
+    switch (n) {
+        case 2: adj_hybrid_gauss_finish_kernel<DIM, 2, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 3: adj_hybrid_gauss_finish_kernel<DIM, 3, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 4: adj_hybrid_gauss_finish_kernel<DIM, 4, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 5: adj_hybrid_gauss_finish_kernel<DIM, 5, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 6: adj_hybrid_gauss_finish_kernel<DIM, 6, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 7: adj_hybrid_gauss_finish_kernel<DIM, 7, CURV><<<grid, 256, 0, s>>>(P); break;
+        case 8: adj_hybrid_gauss_finish_kernel<DIM, 8, CURV><<<grid, 256, 0, s>>>(P); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 // ---- the scalar equations: linear advection (LinearAdvection.jl) and Burgers (Burgers.jl) ----
 // Face VJP.  The flux is F = J (an (q_l + q_r)/2 + [LxF] |an| (q_l - q_r)/2 c) for linear
@@ -2501,8 +2927,11 @@ cudaError_t launch_adj_scalar(int dim, int eq, int n, bool split, bool gauss, bo
 cudaError_t launch_adj_face(int dim, int kind, bool curv, bool gauss, int grid, int tb, const AdjFaceParams& F,
                             cudaStream_t s);
 cudaError_t launch_adj_elem_dim(int dim, int n, bool curv, bool gauss, const AdjElemParams& P, cudaStream_t s);
-// gauss: the split form on a basis without boundary nodes (the entropy-projected coupling;
-// Cartesian); hybrid: the hybrid operator on Gauss-Lobatto nodes (Cartesian)
+// The hybrid operator on Gauss nodes: the first element pass (before the face VJP) and the second.
+cudaError_t launch_adj_hybrid_gauss(int dim, int n, int tp, bool curv, const AdjElemParams& P, cudaStream_t s);
+cudaError_t launch_adj_hybrid_gauss_finish(int dim, int n, bool curv, const AdjElemParams& P, cudaStream_t s);
+// gauss: the split form on a basis without boundary nodes (the entropy-projected coupling);
+// hybrid: the hybrid operator on Gauss-Lobatto nodes (curv: general geometry in both)
 cudaError_t launch_adj_split_dim(int dim, int n, int tp, bool curv, bool gauss, bool hybrid, const AdjElemParams& P,
                                  cudaStream_t s);
 

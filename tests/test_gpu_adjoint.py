@@ -622,12 +622,12 @@ HYBRID_OPS = {
 }
 
 
-def _hybrid_disc(dim, n, op, walls, seed):
+def _hybrid_disc(dim, n, op, walls, seed, basis="GLL"):
     eq = F.EulerEquation(dim, 1.4)
     bcs = None
     if walls:
         bcs = {str(k): (F.EulerSlipBC() if k % 2 else F.EulerOutflowBC()) for k in range(1, 2 * dim + 1)}
-    disc = build(dim, n, (3,) * dim, eq, HYBRID_OPS[op](), periodic=() if walls else True, bcs=bcs)
+    disc = build(dim, n, (3,) * dim, eq, HYBRID_OPS[op](), periodic=() if walls else True, bcs=bcs, basis=basis)
     Q = smooth_euler_state(disc, seed=seed, amp=0.3)
     if walls:
         P = eq.vars_cons2prim(Q)
@@ -709,10 +709,78 @@ def test_hybrid_adjoint_solve_against_dual_numbers(op):
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
+@pytest.mark.parametrize("dim,n,walls,op",
+                         [(d, n, w, op) for op in sorted(HYBRID_OPS)
+                          for d, n, w in [(1, 5, True), (2, 4, False), (2, 5, True), (3, 3, True), (3, 4, False)]] +
+                         [(3, 7, False, "hybrid_hllc"), (2, 8, True, "hybrid_kg")])
+def test_gauss_nodes_hybrid_rhs_vjp_dot_product(dim, n, walls, op):
+    """HybridDivOperator on Gauss nodes: the blended scan that starts from the element's own face
+    flux, run backwards (the face-flux cotangents handed to the face VJP), the projected-state
+    pairs weighted by l/ω, the FV fluxes and Fisher's indicator, against the oracle's dual
+    numbers."""
+    disc, Q = _hybrid_disc(dim, n, op, walls, seed=dim + n, basis="GL")
+    rng = np.random.default_rng(190 + dim + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _hybrid_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op", ["hybrid_hllc", "hybrid_std_hll"])
+def test_gauss_nodes_hybrid_rhs_vjp_columns(op):
+    disc, Q = _hybrid_disc(2, 4, op, True, seed=8, basis="GL")
+    rng = np.random.default_rng(28)
+    c, _ = _hybrid_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    lam = rng.standard_normal(Q.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, None, _dev(Q), _dev(lam))
+    Qb = _host(Qbar)
+    o = oracle_for(disc)
+    npe = disc.std.n ** 2
+    for e in (0, 4):
+        for v in range(Q.shape[1]):
+            for i in range(e * npe, (e + 1) * npe):
+                dQ = np.zeros_like(Q)
+                dQ[i, v] = 1.0
+                _, dR = o.rhs_jvp(Q, dQ, c, 0.0 * c)
+                col = np.sum(lam * dR)
+                assert abs(Qb[i, v] - col) <= 1e-12 * max(1.0, np.sum(np.abs(lam * dR))), (v, i, Qb[i, v], col)
+
+
+@pytest.mark.parametrize("op", ["hybrid_hllc", "hybrid_kg"])
+def test_gauss_nodes_hybrid_adjoint_solve_against_dual_numbers(op):
+    eq = F.EulerEquation(3, 1.4)
+    disc = build(3, 4, (2, 3, 2), eq, HYBRID_OPS[op](), box=((0.0,) * 3, (2 * np.pi,) * 3), basis="GL")
+    Q0 = _tgv_state(disc, 0.3, 7)
+    rng = np.random.default_rng(48)
+    c, noc = _hybrid_c(disc, op, 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+    rho_t, w = _functional_inputs(disc, 13)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 6
+    g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+    gc = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, 2, _dev(rho_t), _dev(w), g, gc)
+    o = oracle_for(disc)
+    for k in range(2):
+        dQ = rng.standard_normal(Q0.shape)
+        dc = rng.standard_normal(c.shape) * (0.0 if noc else 1.0)
+        Jo, dJo = o.solve_jvp(Q0, dQ, c, dc, dt, nsteps, rho_t, w)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ) + (0.0 if noc else np.sum(gc.cpu().numpy() * dc))
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
+
+
 def test_hybrid_adjoint_limits():
-    """Not covered: the hybrid operator on Gauss nodes."""
+    """Not covered: the hybrid operator on Gauss nodes at 3D p=7 (beyond shared memory)."""
     from flou_cuda import _lib as L
-    disc = build(2, 4, (3, 3), F.EulerEquation(2, 1.4), HYBRID_OPS["hybrid_hllc"](), basis="GL")
+    disc = build(3, 8, (1, 1, 1), F.EulerEquation(3, 1.4), HYBRID_OPS["hybrid_hllc"](), basis="GL")
     Q = _dev(smooth_euler_state(disc, seed=1))
     g = torch.empty_like(Q)
     with pytest.raises(F.FlouError) as ei:

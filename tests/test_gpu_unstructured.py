@@ -181,7 +181,7 @@ def test_general_geometry_is_rejected_where_not_covered():
     with pytest.raises(F.FlouError) as ei:
         F.Batch([disc, cart], [Q, Qc], [1e-3, 1e-3])
     assert ei.value.status == L.FLOU_ERR_ARG
-    # the adjoint covers general geometry, but not the hybrid operator on Gauss nodes
+    # the adjoint covers general geometry, but not the hybrid operator on Gauss nodes there
     hyb = _disc(2, 4, "hybrid_hllc", basis="GL")
     Qh = torch.from_numpy(np.ascontiguousarray(_state(hyb).T)).cuda()
     g = torch.empty_like(Qh)
