@@ -115,9 +115,6 @@ int adj_supported(flou_ctx* c) {
         if (c->bnodes && !c->lift_ends)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto and "
                                                      "Gauss nodes");
-        if (!c->bnodes && c->curv)
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator on Gauss nodes covers "
-                                                     "Cartesian elements");
         if (fv_kind(c) < 0)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid operator's subcell flux must be LxF, "
                                                      "Scalar- or MatrixDissipation (StdAverage or "

@@ -800,12 +800,14 @@ def _maybe_c(disc, c):
 
 @pytest.mark.parametrize("op,basis", [("split_chandra_lxfc", "GL"), ("split_kg_lxf", "GL"), ("split_std_lxf", "GL"),
                                       ("split_chandra_md", "GL"), ("hybrid_hllc", "GLL"), ("hybrid_md", "GLL"),
-                                      ("hybrid_kg", "GLL")])
+                                      ("hybrid_kg", "GLL"), ("hybrid_hllc", "GL"), ("hybrid_md", "GL"),
+                                      ("hybrid_kg", "GL")])
 @pytest.mark.parametrize("dim,n", [(2, 4), (3, 3), (3, 4)])
 def test_general_geometry_gauss_split_and_hybrid_rhs_vjp(dim, n, op, basis):
     """General geometry for the split form on Gauss nodes (the projected states' pairs along
     (Ja_j + n Js)/2 with the line end's subcell normal) and for the hybrid operator (the subcell
-    FV fluxes in the uploaded subcell frames), against the oracle's dual numbers."""
+    FV fluxes in the uploaded subcell frames; on Gauss nodes also the face fluxes' cotangents to
+    a slave side through the orientation), against the oracle's dual numbers."""
     from test_gpu_unstructured import _disc as _udisc
     from test_unstructured import _state
     disc = _udisc(dim, n, op, basis=basis)
@@ -826,7 +828,7 @@ def test_general_geometry_gauss_split_and_hybrid_rhs_vjp(dim, n, op, basis):
     assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
 
 
-@pytest.mark.parametrize("op,basis", [("split_chandra_lxfc", "GL"), ("hybrid_hllc", "GLL")])
+@pytest.mark.parametrize("op,basis", [("split_chandra_lxfc", "GL"), ("hybrid_hllc", "GLL"), ("hybrid_hllc", "GL")])
 def test_general_geometry_gauss_split_and_hybrid_adjoint_solve(op, basis):
     from test_gpu_unstructured import _disc as _udisc
     from test_unstructured import _state

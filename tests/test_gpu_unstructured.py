@@ -181,13 +181,6 @@ def test_general_geometry_is_rejected_where_not_covered():
     with pytest.raises(F.FlouError) as ei:
         F.Batch([disc, cart], [Q, Qc], [1e-3, 1e-3])
     assert ei.value.status == L.FLOU_ERR_ARG
-    # the adjoint covers general geometry, but not the hybrid operator on Gauss nodes there
-    hyb = _disc(2, 4, "hybrid_hllc", basis="GL")
-    Qh = torch.from_numpy(np.ascontiguousarray(_state(hyb).T)).cuda()
-    g = torch.empty_like(Qh)
-    with pytest.raises(F.FlouError) as ei:
-        hyb.ctx.adjoint_solve(Qh, 1e-3, 2, 1, Qh[0].clone(), Qh[0].clone(), g)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
     # the split form of a scalar equation has no Gauss-node form (no entropy variables)
     mesh = F.perturbed_box(2, 3, (0.0, 0.0), (1.0, 1.0), amp=0.1, seed=1)
     b = F.LagrangeBasis("GL", 4)
