@@ -654,6 +654,7 @@ def bench_adjoint_operators(nel=12, n=6, nsteps=10):
         ("split_hllc_GL", "GL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), False, None),
         ("strong_hllc_GL", "GL", lambda: F.StrongDivOperator(F.HLLC()), False, None),
         ("hybrid_md_GLL", "GLL", lambda: F.HybridDivOperator(md, 1.0), False, None),
+        ("hybrid_md_GL", "GL", lambda: F.HybridDivOperator(md, 1.0), False, None),
         ("split_hllc_general", "GLL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), True, None),
         ("split_hllc_GLL_ORK256", "GLL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()), False,
          F.ORK256()),

@@ -267,8 +267,7 @@ int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_
  * form (either node set) or the split form with the StdAverage two-point flux, the LxF or
  * StdAverage interface flux; and the Euler equations with
  *  - the strong form, the split form (Chandrashekar, Kennedy-Gruber or StdAverage two-point
- *    flux) and the hybrid operator (Gauss-Lobatto nodes; any interface flux below as its
- *    subcell flux);
+ *    flux) and the hybrid operator (any interface flux below as its subcell flux);
  *  - the LxF, ScalarDissipation or MatrixDissipation interface flux (StdAverage or
  *    ChandrasekharAverage central part), HLL and HLLC;
  *  - Gauss-Lobatto or Gauss nodes, Cartesian or general geometry;
@@ -276,8 +275,9 @@ int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_
  *    states are constants of the differentiation);
  *  - SSP-RK3 or the 2N-storage method set by flou_set_integrator, with or without the Zhang-Shu
  *    stage limiter (in flou_adjoint_solve_batch each instance with its own).
- * Other contexts (the Kennedy-Gruber 3D p=7 tile of the Gauss-node split and hybrid forms)
- * return FLOU_ERR_UNSUPPORTED.
+ * Other contexts (the 3D p=7 tiles beyond shared memory: the Gauss-node hybrid operator, and the
+ * Kennedy-Gruber flux in the Gauss-node split form and the Gauss-Lobatto hybrid operator) return
+ * FLOU_ERR_UNSUPPORTED.
  * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):
  * max(a, b) takes b unless b < a; d|u|/du = -1 for a set sign bit, else +1. */
 
