@@ -48,28 +48,50 @@ def _compile(src, extra, objdir=OBJ):
     return obj, None
 
 
-def build(verbose=False, extra=(), checked=False):
-    objdir = os.path.join(OBJ, "checked") if checked else OBJ
-    lib = os.path.join(LIBDIR, "libflou_cuda_checked.so") if checked else LIB
-    extra = list(extra) + (["-DFLOU_CUDA_CHECKED"] if checked else [])
-    os.makedirs(objdir, exist_ok=True)
+def _weight(src):
+    """Rough compile cost of a translation unit, so that the slowest start first."""
+    name = os.path.basename(src)
+    for prefix, w in (("adjoint_hybrid", 4), ("adjoint_split", 3), ("elem_", 2), ("batch", 2), ("adjoint", 1)):
+        if name.startswith(prefix):
+            return w
+    return 0
+
+
+def build_set(variants, verbose=False):
+    """Builds one library per (extra flags, checked) variant, compiling every variant's
+    translation units in one worker pool, slowest first; returns the library paths."""
+    plans = []
+    for extra, checked in variants:
+        objdir = os.path.join(OBJ, "checked") if checked else OBJ
+        lib = os.path.join(LIBDIR, "libflou_cuda_checked.so") if checked else LIB
+        flags = list(extra) + (["-DFLOU_CUDA_CHECKED"] if checked else [])
+        os.makedirs(objdir, exist_ok=True)
+        plans.append((objdir, lib, flags))
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    workers = min(len(srcs), os.cpu_count() or 4)
+    jobs = sorted(((k, s) for k in range(len(plans)) for s in srcs), key=lambda j: -_weight(j[1]))
+    workers = min(len(jobs), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(workers) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra, objdir), srcs))
+        results = list(ex.map(lambda j: _compile(j[1], plans[j[0]][2], plans[j[0]][0]), jobs))
     errs = [e for _, e in results if e]
     if errs:
         raise RuntimeError("\n".join(errs))
-    objs = [o for o, _ in results]
-    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
-        p = subprocess.run(cmd, capture_output=True, text=True)
-        if p.returncode != 0:
-            raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), p.stdout, p.stderr))
-    if verbose:
-        print("built", lib)
-    return lib
+    libs = []
+    for k, (objdir, lib, _) in enumerate(plans):
+        objs = sorted(o for (kk, _), (o, _) in zip(jobs, results) if kk == k)
+        if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+            cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
+            p = subprocess.run(cmd, capture_output=True, text=True)
+            if p.returncode != 0:
+                raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), p.stdout, p.stderr))
+        if verbose:
+            print("built", lib)
+        libs.append(lib)
+    return libs
+
+
+def build(verbose=False, extra=(), checked=False):
+    return build_set([(extra, checked)], verbose)[0]
 
 
 if __name__ == "__main__":
