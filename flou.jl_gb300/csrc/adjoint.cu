@@ -202,6 +202,8 @@ int adj_stage(flou_ctx* c, AdjBuffers& Bf, cudaStream_t s, const double* U, cons
     for (int d = 0; d < 3; ++d) F.adv[d] = c->cfg.advection[d];
     F.lxf = c->cfg.numflux == FLOU_NF_LXF ? 1 : 0;
     const bool hg = hybrid_gauss(c);
+    if (hg && !(Bf.Fn && Bf.FbS && Bf.Tq))
+        return ctx_fail(c, FLOU_ERR_STATE, "the Gauss-node hybrid adjoint stage has no face-flux buffers");
     cudaError_t e = scalar || hg ? cudaSuccess : launch_adj_face(dim, kind, c->curv, gauss, grid, tb, F, s);
     if (e != cudaSuccess) return ctx_cuda_fail(c, e, "adjoint face kernel");
     AdjElemParams P;
@@ -908,6 +910,7 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
     std::vector<double> load(S, 0.0);
     std::vector<size_t> maxb(S, 0), maxf(S, 0), maxfd(S, 0), maxst(S, 0);
     std::vector<char> any2n(S, 0);   // a stream with a 2N-storage instance needs its own register
+    std::vector<char> anyhg(S, 0);   // and one with a Gauss-node hybrid instance its face-flux buffers
     B.stream_of.assign(n, 0);
     for (int i : order) {
         int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
@@ -918,10 +921,12 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
         maxfd[s] = std::max(maxfd[s], (size_t)ctxs[i]->nfdofs);
         maxst[s] = std::max(maxst[s], (size_t)stage_count(ctxs[i]));
         if (ctxs[i]->lsrk_s) any2n[s] = 1;
+        if (hybrid_gauss(ctxs[i])) anyhg[s] = 1;
     }
     size_t fixed = npart * sizeof(double);
     for (int s = 0; s < S; ++s)
-        fixed += (3 + maxst[s] + any2n[s]) * maxb[s] + (2 * maxf[s] + maxfd[s]) * sizeof(double);
+        fixed += (3 + maxst[s] + any2n[s] + anyhg[s]) * maxb[s] + ((2 + 3 * anyhg[s]) * maxf[s] + maxfd[s]) *
+                                                                   sizeof(double);
     if (budget_bytes < 0 || (size_t)budget_bytes < fixed)
         return fail_all(FLOU_ERR_ARG, "device-memory budget below the " + std::to_string(fixed) +
                                           " bytes of step scratch the batch needs");
@@ -949,6 +954,11 @@ int32_t flou_adjoint_solve_batch(int32_t n, flou_ctx* const* ctxs, double* const
         dalloc((void**)&w.ab.QbL, maxf[s] * sizeof(double));
         dalloc((void**)&w.ab.QbR, maxf[s] * sizeof(double));
         dalloc((void**)&w.ab.Ibar, std::max<size_t>(maxfd[s], 1) * sizeof(double));
+        if (anyhg[s]) {
+            dalloc((void**)&w.ab.Fn, maxf[s] * sizeof(double));
+            dalloc((void**)&w.ab.FbS, 2 * maxf[s] * sizeof(double));
+            dalloc((void**)&w.ab.Tq, maxb[s]);
+        }
     }
     dalloc((void**)&B.partial, npart * sizeof(double));
     B.slot.assign(nslots + 1, nullptr);

@@ -145,3 +145,43 @@ def test_batched_adjoint_with_2n_storage_and_limiter_instances():
     for x in extra:
         x["disc"].ctx.set_limiter(L.LIMITER_NONE)
         x["disc"].ctx.set_integrator(None)
+
+
+def test_batched_adjoint_mixes_operators_and_node_sets():
+    """One lockstep reverse sweep over the hybrid operator on Gauss nodes (two element passes a
+    stage), the hybrid operator on Gauss-Lobatto nodes and the Gauss-node split form: every
+    instance bitwise its own single solve, the Gauss hybrid one also against the dual numbers."""
+    from test_gpu_adjoint import HYBRID_OPS, _hybrid_c
+    L = 2 * np.pi
+    specs = [(4, (2, 2, 2), "GL", HYBRID_OPS["hybrid_md"]), (3, (3, 2, 2), "GL", HYBRID_OPS["hybrid_kg"]),
+             (4, (2, 3, 2), "GLL", HYBRID_OPS["hybrid_hllc"]),
+             (4, (2, 2, 2), "GL", lambda: F.SplitDivOperator(F.ChandrasekharAverage(), F.HLLC()))]
+    inst = []
+    for k, (n, ne, basis, op) in enumerate(specs):
+        disc = build(3, n, ne, F.EulerEquation(3, 1.4), op(), box=((0.0,) * 3, (L,) * 3), basis=basis)
+        Q0 = _tgv_state(disc, 0.2 + 0.05 * k, 60 + k)
+        rng = np.random.default_rng(70 + k)
+        c, noc = _hybrid_c(disc, "hybrid_kg" if k == 1 else "", 1.0 + 0.2 * rng.random(disc.mesh.nelements))
+        rho_t, w = _functional_inputs(disc, 80 + k)
+        inst.append(dict(disc=disc, Q0=Q0, c=c, noc=noc, rho_t=rho_t, w=w, dt=0.2 * disc.ctx.max_dt(Q0, 1.0)))
+    nsteps = 6
+    g = [torch.empty(x["Q0"].shape[::-1], dtype=torch.float64, device="cuda") for x in inst]
+    gc = [None if x["noc"] else torch.empty(x["disc"].mesh.nelements, dtype=torch.float64, device="cuda")
+          for x in inst]
+    J, nf, ns = F.adjoint_solve_batch([x["disc"] for x in inst], [_dev(x["Q0"]) for x in inst],
+                                      [x["dt"] for x in inst], nsteps, 8 << 30, [_dev(x["rho_t"]) for x in inst],
+                                      [_dev(x["w"]) for x in inst], g, gc, nstreams=2)
+    for k, x in enumerate(inst):
+        g1 = torch.empty_like(g[k])
+        gc1 = None if gc[k] is None else torch.empty_like(gc[k])
+        J1, _ = x["disc"].ctx.adjoint_solve(_dev(x["Q0"]), x["dt"], nsteps, 2, _dev(x["rho_t"]), _dev(x["w"]), g1,
+                                            gc1)
+        assert J[k] == J1
+        assert torch.equal(g[k], g1) and (gc1 is None or torch.equal(gc[k], gc1))
+    x = inst[0]
+    dQ = np.random.default_rng(3).standard_normal(x["Q0"].shape)
+    Jo, dJo = oracle_for(x["disc"]).solve_jvp(x["Q0"], dQ, x["c"], 0.0 * x["c"], x["dt"], nsteps, x["rho_t"],
+                                              x["w"])
+    ours = np.sum(_host(g[0]) * dQ)
+    assert abs(J[0] - Jo) <= 1e-12 * abs(Jo)
+    assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
