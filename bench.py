@@ -587,6 +587,24 @@ def run_profile(which):
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "tgv3d 32^3 p=3 + limiter", "ndofs": disc.ndofs, "steps": 2}))
         return 0
+    if which == "J":   # the hybrid operator's adjoint on Gauss nodes: 12^3 p=5 TGV, 3 steps, every state kept
+        import flou_cuda as F
+        eq = F.EulerEquation(3, 1.4)
+        mesh = F.CartesianMesh((0.0,) * 3, (2 * math.pi,) * 3, (12,) * 3)
+        F.apply_periodicBCs(mesh, ("1", "2"), ("3", "4"), ("5", "6"))
+        b = F.LagrangeBasis("GL", 6)
+        op = F.HybridDivOperator(F.MatrixDissipation(F.ChandrasekharAverage(), 1.0), 1.0)
+        disc = F.MultielementDisc(mesh, F.StdHex(b, F.DGSEMrec(b), 5), eq, op, {})
+        Qd = torch.from_numpy(np.ascontiguousarray(F.initial.taylor_green(eq, disc.coords, mach=0.1).T)).cuda()
+        dt = TGV_CFL * disc.ctx.max_dt(Qd, 1.0)
+        rho_t = (Qd[0] * 1.01).contiguous()
+        w = torch.from_numpy(np.tile(disc.std.omega, disc.mesh.nelements) * disc.J).cuda()
+        g = torch.empty_like(Qd)
+        J, nf = disc.ctx.adjoint_solve(Qd, dt, 3, 2, rho_t, w, g)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "adjoint J: hybrid MatrixDissipation on Gauss nodes", "ndofs": disc.ndofs,
+                          "steps": 3, "recomputed": nf, "J": J}))
+        return 0
     if which in ("H", "I"):   # mesh B, MatrixDissipation (Shockwave2D's flux): H the hybrid operator on
         import flou_cuda as F    # Gauss-Lobatto nodes, I the split form on Gauss nodes
         eq = F.EulerEquation(3, 1.4)
@@ -719,12 +737,13 @@ def main():
                     help="skip the batched-adjoint configuration (64 3D instances, 200 steps, 120 GB budget; about "
                          "four minutes)")
     ap.add_argument("--adjoint-batch-only", action="store_true", help="run only the batched-adjoint configuration")
-    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G", "H", "I"], default=None,
+    ap.add_argument("--profile", choices=["A", "B", "C", "D", "E", "F", "G", "H", "I", "J"], default=None,
                     help="profiling case: two SSP-RK3 steps of mesh A (32^3 p=3), B (16^3 p=7) or the batched "
                          "configuration C (256 instances, one persistent launch per stage, default tiling); "
                          "adjoint solves D (2D 64^2 p=4, 20 steps) and E (3D split 16^3 p=4, 10 steps); F: mesh A with the "
                          "Zhang-Shu stage limiter; G: the FP64 DFMA and DMMA throughput probes; H: mesh B with the "
-                         "hybrid operator and MatrixDissipation")
+                         "hybrid operator and MatrixDissipation, I: the same on Gauss nodes with the split form; J: "
+                         "the hybrid operator's adjoint on Gauss nodes (3D 12^3 p=5, 3 steps)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1255,11 +1255,16 @@ struct AdjSplitShape {
     // H (hybrid operator): per node the subcell-flux values, then their cotangents; G and H (the
     // hybrid operator on Gauss nodes): also the projected-state flux differences of both line
     // sides per node, later the entropy-jump cotangents and the hand-over to the left neighbour
-    static constexpr int NGX = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0) +
-                               (G && H ? 2 * NV * S::NN : 0);
-    static constexpr size_t SMEM =
-        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD + NGX) +
+    static constexpr int NGX0 = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0) +
+                                (G && H ? 2 * NV * S::NN : 0);
+    static constexpr size_t BASE =
+        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
         2 * (S::NPAIR + 1);
+    // G: every node's entropy variables, evaluated once per block where the tile has room for them
+    // (all Gauss-node tiles but the 3D p=7 ones); else each use evaluates them again
+    static constexpr bool WC = G && BASE + sizeof(double) * ((size_t)NGX0 + (size_t)NV * S::NN) <= 227 * 1024;
+    static constexpr int NGX = NGX0 + (WC ? NV * S::NN : 0);
+    static constexpr size_t SMEM = BASE + sizeof(double) * (size_t)NGX;
     // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
     // (G, H: two where that still leaves 144 registers, else one, for the projection's registers)
     static constexpr int MINB = (!G && !H) ? ((S::BLOCK * 2 * 128 <= 65536) ? 2 : 1)
@@ -1451,10 +1456,10 @@ __device__ __forceinline__ void entropy_vjp(const double* q, double p, double g,
 // cotangent carries ±1 instead of ±Ja.
 // HG (the hybrid operator on Gauss nodes): sw holds the pair weights w' and ∂g[j] becomes
 // l[j]/ω_j (the projected-state pairs enter the node increments through l).
-template <int DIM, int N, int D, int TP, bool CURV = false, bool HG = false>
+template <int DIM, int N, int D, int TP, bool CURV = false, bool HG = false, bool WC = false>
 __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int e0, const double* sops,
                                                      const double* sprim, const double* sw, double* snode,
-                                                     double* sWb, double cb) {
+                                                     double* sWb, double cb, const double* sWn) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, true>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR, NPB = A::NPB;
@@ -1478,10 +1483,16 @@ __device__ __forceinline__ void adj_split_projection(const AdjElemParams& P, int
         const int j = on ? elp * NPE + tp_node<DIM>(N, D, line, pos) : 0;
         double wt[NV], T[NV];
         if (on) {
-            double q[NV], wj[NV];
+            double wj[NV];
+            if constexpr (WC) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
-            entropy_of<DIM>(q, g, wj);
+                for (int k = 0; k < NV; ++k) wj[k] = sWn[k * NN + j];
+            } else {
+                double q[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
+                entropy_of<DIM>(q, g, wj);
+            }
             const double cf = HG ? lv[sd * N + pos] * rcp_refined(P.omega1[pos]) : dgl[sd * N + pos];
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
@@ -1998,9 +2009,10 @@ template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
                                                      const double* sops, const double* sprim, const double* sw,
                                                      double* sH, double* spb, const uint8_t* stab, double* sF2,
-                                                     double* scl, double* sdW, double* qb) {
+                                                     double* scl, double* sdW, const double* sWn, double* qb) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, true, true>;
+    static_assert(A::WC, "the Gauss-node hybrid tiles keep the entropy variables");
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR;
     constexpr int NPROJ = A::NPROJ;
     static_assert(N <= 8, "one lane per node of a line within a group of 8");
@@ -2026,10 +2038,10 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         double q[NV], wt[NV];
         if (on) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
-            entropy_of<DIM>(q, g, wt);
-#pragma unroll
-            for (int k = 0; k < NV; ++k) wt[k] *= lv[sd * N + pos];
+            for (int k = 0; k < NV; ++k) {
+                q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
+                wt[k] = sWn[k * NN + j] * lv[sd * N + pos];
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < NV; ++k) wt[k] = 0.0;
@@ -2109,8 +2121,9 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         }
     }
     if (active && pos > 0) {   // the FV flux of the interface on the node's left, and the entropy jump
-        const int64_t gl = (int64_t)e0 * NPE + el * NPE + tp_node<DIM>(N, D, line, pos - 1);
-        double ql[NV], qr[NV], Fv[NV], wl[NV], wr[NV];
+        const int il = el * NPE + tp_node<DIM>(N, D, line, pos - 1);
+        const int64_t gl = (int64_t)e0 * NPE + il;
+        double ql[NV], qr[NV], Fv[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             ql[k] = P.U[k * P.ndofs + gl];
@@ -2118,12 +2131,10 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         }
         SubcellFace<DIM> sf;
         subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
-        entropy_of<DIM>(ql, g, wl);
-        entropy_of<DIM>(qr, g, wr);
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             sF2[k * NN + tid] = Fv[k];
-            sdW[k * NN + tid] = wr[k] - wl[k];
+            sdW[k * NN + tid] = sWn[k * NN + tid] - sWn[k * NN + il];
         }
     }
     __syncthreads();
@@ -2455,6 +2466,7 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     double* snode = sWb + NV * A::NPROJ; // G: [NPB][NN] projected-state pair cotangents per node
     double* sHy = snode + (G ? NPB * NN : 0);   // H: [NV][NN] subcell fluxes, then the pair weights
     double* sF2 = sHy + (H ? NV * NN : 0);      // G and H: [2][NV][NN] (adj_hybrid_gauss_dir)
+    double* sWn = sF2 + (G && H ? 2 * NV * NN : 0);   // A::WC: [NV][NN] the nodes' entropy variables
     uint8_t* stab = (uint8_t*)(sJD + A::NSD + A::NGX);
     const int tid = threadIdx.x;
     for (int t = tid; t < S::NOPS; t += blockDim.x) sops[t] = P.ops[t];
@@ -2508,6 +2520,12 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
             sprim[(1 + DIM) * NN + tid] = (0.25 * rho) * rcp_refined(p);
             sprim[(2 + DIM) * NN + tid] = 0.25 * vv;
         }
+        if constexpr (A::WC) {
+            double wn[NV];
+            entropy_of<DIM>(q, g, wn);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) sWn[k * NN + tid] = wn[k];
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) v[k] = 0.0;
@@ -2534,13 +2552,13 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         if constexpr (G && H) {
             if (dir == 0)
                 adj_hybrid_gauss_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
-                                                          sWb, snode, qb);
+                                                          sWb, snode, sWn, qb);
             else if (dir == 1)
                 adj_hybrid_gauss_dir<DIM, N, D1, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
-                                                           sWb, snode, qb);
+                                                           sWb, snode, sWn, qb);
             else
                 adj_hybrid_gauss_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sF2,
-                                                           sWb, snode, qb);
+                                                           sWb, snode, sWn, qb);
         } else if constexpr (H) {
             if (dir == 0)
                 adj_hybrid_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
@@ -2553,9 +2571,13 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
         else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         if constexpr (G) {
-            if (dir == 0) adj_split_projection<DIM, N, 0, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
-            else if (dir == 1) adj_split_projection<DIM, N, D1, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
-            else adj_split_projection<DIM, N, D2, TP, CURV, H>(P, e0, sops, sprim, swd, snode, sWb, cb);
+            constexpr bool WC = A::WC;
+            if (dir == 0)
+                adj_split_projection<DIM, N, 0, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
+            else if (dir == 1)
+                adj_split_projection<DIM, N, D1, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
+            else
+                adj_split_projection<DIM, N, D2, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
         }
         __syncthreads();
         if (active) {
