@@ -1260,9 +1260,9 @@ struct AdjSplitShape {
     static constexpr size_t BASE =
         sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
         2 * (S::NPAIR + 1);
-    // G: every node's entropy variables, evaluated once per block where the tile has room for them
-    // (all Gauss-node tiles but the 3D p=7 ones); else each use evaluates them again
-    static constexpr bool WC = G && BASE + sizeof(double) * ((size_t)NGX0 + (size_t)NV * S::NN) <= 227 * 1024;
+    // G, H: every node's entropy variables, evaluated once per block where the tile has room for
+    // them (all but the Gauss-node 3D p=7 tiles); else each use evaluates them again
+    static constexpr bool WC = (G || H) && BASE + sizeof(double) * ((size_t)NGX0 + (size_t)NV * S::NN) <= 227 * 1024;
     static constexpr int NGX = NGX0 + (WC ? NV * S::NN : 0);
     static constexpr size_t SMEM = BASE + sizeof(double) * (size_t)NGX;
     // two resident blocks where the register file allows 64K / (2 * BLOCK) >= 128 registers
@@ -1873,7 +1873,8 @@ __device__ __forceinline__ double pressure_of(const double* q, double g) {
 template <int DIM, int N, int D, int TP, bool CURV = false>
 __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, bool active, int el, int i,
                                                const double* sops, const double* sprim, const double* sw, double* sH,
-                                               double* spb, const uint8_t* stab, double* qb) {
+                                               double* spb, const uint8_t* stab, const double* sWn, double* qb) {
+    constexpr bool WC = AdjSplitShape<DIM, N, TP, false, true>::WC;
     using S = Shape<DIM, N>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD;
     const double g = P.gamma;
@@ -1922,8 +1923,16 @@ __device__ __forceinline__ void adj_hybrid_dir(const AdjElemParams& P, int e0, b
         }
         SubcellFace<DIM> sf;
         subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
-        entropy_of<DIM>(ql, g, wl);
-        entropy_of<DIM>(qr, g, wr);
+        if constexpr (WC) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                wl[k] = sWn[k * NN + il];
+                wr[k] = sWn[k * NN + tid];
+            }
+        } else {
+            entropy_of<DIM>(ql, g, wl);
+            entropy_of<DIM>(qr, g, wr);
+        }
         double bb = 0.0, dW[NV], Fh[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -2561,11 +2570,14 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
                                                            sWb, snode, sWn, qb);
         } else if constexpr (H) {
             if (dir == 0)
-                adj_hybrid_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+                adj_hybrid_dir<DIM, N, 0, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sWn,
+                                                    qb);
             else if (dir == 1)
-                adj_hybrid_dir<DIM, N, D1, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+                adj_hybrid_dir<DIM, N, D1, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sWn,
+                                                     qb);
             else
-                adj_hybrid_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, qb);
+                adj_hybrid_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sWn,
+                                                     qb);
         }
         if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
         else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
