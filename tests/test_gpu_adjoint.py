@@ -777,6 +777,47 @@ def test_gauss_nodes_hybrid_adjoint_solve_against_dual_numbers(op):
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
+@pytest.mark.parametrize("integrator,limited", [("SSPRK3", True), ("ORK256", True), ("CarpenterKennedy2N54", False)])
+def test_gauss_nodes_hybrid_adjoint_through_limiter_and_2n_storage(integrator, limited):
+    """The Gauss-node hybrid operator's two-pass adjoint stage inside the limited SSP-RK3 and
+    2N-storage reverse sweeps, against the oracle's dual numbers through the same method."""
+    from flou_cuda import _lib as L
+    eq = F.EulerEquation(2, 1.4)
+    disc = build(2, 4, (4, 3), eq, HYBRID_OPS["hybrid_hllc"](), box=((-5.0, -5.0), (5.0, 5.0)), basis="GL")
+    if limited:   # a smooth state (a one-node dip's entropy variables extrapolate to a
+        # non-physical line-end state on Gauss nodes), limited where ρ or p is below 0.82
+        Q0 = smooth_euler_state(disc, seed=14, amp=0.2)
+        disc.ctx.set_limiter(L.LIMITER_ZHANG_SHU, 0.82)
+    else:
+        Q0 = np.asfortranarray(F.initial.vortex_bump(eq, disc.coords, (0.3, -0.4), 4.0, 0.05, period=(10.0, 10.0)))
+    m = None if integrator == "SSPRK3" else getattr(F, integrator)()
+    if m is not None:
+        disc.ctx.set_integrator(m.A, m.B)
+    c = np.ones(disc.mesh.nelements)
+    rho_t, w = _functional_inputs(disc, 9)
+    dt = 0.2 * disc.ctx.max_dt(Q0, 1.0)
+    nsteps = 6
+    o = oracle_for(disc)
+    args = () if m is None else (m.A, m.B, m.c)
+    lim = dict(minval=0.82, omega_tp=disc.std.omega) if limited else {}
+    if limited:   # the limiter acts along this trajectory
+        J0, _ = o.solve_jvp_lsrk(Q0, 0 * Q0, c, 0 * c, dt, nsteps, rho_t, w, *args)
+        J1, _ = o.solve_jvp_lsrk(Q0, 0 * Q0, c, 0 * c, dt, nsteps, rho_t, w, *args, **lim)
+        assert abs(J1 - J0) > 1e-6 * abs(J0)
+    rng = np.random.default_rng(72)
+    for nsnap in (2, nsteps - 1):
+        g = torch.empty(Q0.shape[::-1], dtype=torch.float64, device="cuda")
+        J, nfwd = disc.ctx.adjoint_solve(_dev(Q0), dt, nsteps, nsnap, _dev(rho_t), _dev(w), g)
+        dQ = rng.standard_normal(Q0.shape)
+        Jo, dJo = o.solve_jvp_lsrk(Q0, dQ, c, 0 * c, dt, nsteps, rho_t, w, *args, **lim)
+        assert abs(J - Jo) <= 1e-12 * abs(Jo)
+        ours = np.sum(_host(g) * dQ)
+        assert abs(ours - dJo) <= 1e-10 * abs(dJo), (nsnap, ours, dJo)
+    disc.ctx.set_limiter(L.LIMITER_NONE)
+    if m is not None:
+        disc.ctx.set_integrator(None)
+
+
 def test_hybrid_adjoint_limits():
     """Not covered: the hybrid operator on Gauss nodes at 3D p=7 (beyond shared memory)."""
     from flou_cuda import _lib as L
