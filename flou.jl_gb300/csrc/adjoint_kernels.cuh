@@ -1257,11 +1257,18 @@ struct AdjSplitShape {
     // sides per node, later the entropy-jump cotangents and the hand-over to the left neighbour
     static constexpr int NGX0 = (G ? NV * NPROJ + NPB * S::NN : 0) + (H ? NV * S::NN : 0) +
                                 (G && H ? 2 * NV * S::NN : 0);
-    static constexpr size_t BASE =
-        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + 2 * (size_t)NPB * NPT + NSD) +
-        2 * (S::NPAIR + 1);
+    static constexpr size_t FIXED =
+        sizeof(double) * (S::NOPS + (size_t)NARR * S::NN + (size_t)NV * S::NN + NSD) + 2 * (S::NPAIR + 1);
+    // The pair cotangents of a direction in CH chunks of its lines (one element per block): two
+    // where all of them at once would not fit in shared memory (the 3D p=7 tiles of the
+    // Gauss-node and Kennedy-Gruber hybrid forms), each chunk's pairs then its nodes.
+    static constexpr int CH =
+        (FIXED + sizeof(double) * (2 * (size_t)NPB * NPT + NGX0) > 227 * 1024 && S::EPB == 1 && S::NFD % 2 == 0) ? 2
+                                                                                                              : 1;
+    static constexpr int NPTC = NPT / CH;   // pairs of one chunk
+    static constexpr size_t BASE = FIXED + sizeof(double) * 2 * (size_t)NPB * NPTC;
     // G, H: every node's entropy variables, evaluated once per block where the tile has room for
-    // them (all but the Gauss-node 3D p=7 tiles); else each use evaluates them again
+    // them (all but some 3D p=7 tiles); else each use evaluates them again
     static constexpr bool WC = (G || H) && BASE + sizeof(double) * ((size_t)NGX0 + (size_t)NV * S::NN) <= 227 * 1024;
     static constexpr int NGX = NGX0 + (WC ? NV * S::NN : 0);
     static constexpr size_t SMEM = BASE + sizeof(double) * (size_t)NGX;
@@ -2021,7 +2028,6 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
                                                      double* scl, double* sdW, const double* sWn, double* qb) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, true, true>;
-    static_assert(A::WC, "the Gauss-node hybrid tiles keep the entropy variables");
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NARR = A::NARR;
     constexpr int NPROJ = A::NPROJ;
     static_assert(N <= 8, "one lane per node of a line within a group of 8");
@@ -2047,10 +2053,15 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         double q[NV], wt[NV];
         if (on) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
-                wt[k] = sWn[k * NN + j] * lv[sd * N + pos];
+            for (int k = 0; k < NV; ++k) q[k] = P.U[k * P.ndofs + (int64_t)e0 * NPE + j];
+            if constexpr (A::WC) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) wt[k] = sWn[k * NN + j];
+            } else {
+                entropy_of<DIM>(q, g, wt);
             }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) wt[k] *= lv[sd * N + pos];
         } else {
 #pragma unroll
             for (int k = 0; k < NV; ++k) wt[k] = 0.0;
@@ -2140,10 +2151,21 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         }
         SubcellFace<DIM> sf;
         subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
+        double wl[NV], wr[NV];
+        if constexpr (A::WC) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                wl[k] = sWn[k * NN + il];
+                wr[k] = sWn[k * NN + tid];
+            }
+        } else {
+            entropy_of<DIM>(ql, g, wl);
+            entropy_of<DIM>(qr, g, wr);
+        }
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             sF2[k * NN + tid] = Fv[k];
-            sdW[k * NN + tid] = sWn[k * NN + tid] - sWn[k * NN + il];
+            sdW[k * NN + tid] = wr[k] - wl[k];
         }
     }
     __syncthreads();
@@ -2259,15 +2281,16 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
 
 // CURV: the pair flux along the averaged metric column n̄ = (Ja_a + Ja_b)/2 of direction D (the
 // metric terms are in the flux; sJD then holds -D♯ alone).
-template <int DIM, int N, int D, int TP, bool CURV = false>
+template <int DIM, int N, int D, int TP, bool CURV = false, int CH = 1>
 __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, const double* sJD,
                                                 const double* sprim, const double* sw, double* spb,
-                                                const uint8_t* stab, double cb) {
+                                                const uint8_t* stab, double cb, int chunk = 0) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
-    constexpr int NPT = A::NPT, NPB = A::NPB;
-    for (int kp = threadIdx.x; kp < NPT; kp += blockDim.x) {
+    constexpr int NPB = A::NPB, NPTC = A::NPT / CH;   // CH > 1: this chunk's pairs, spb holds them alone
+    for (int kq = threadIdx.x; kq < NPTC; kq += blockDim.x) {
+        const int kp = chunk * NPTC + kq;
         int elp = kp / (NFD * NPAIR);
         int r = kp - elp * (NFD * NPAIR);
         int line = r / NPAIR, pp = r - line * NPAIR;
@@ -2323,18 +2346,18 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
             chandra_pair_vjp<DIM, DD, false>(sprim[ia], v1, sprim[(1 + DIM) * NN + ia], sprim[(2 + DIM) * NN + ia],
                                              sprim[ib], v2, sprim[(1 + DIM) * NN + ib], sprim[(2 + DIM) * NN + ib], cb,
                                              Fb, o1, o2, nrm);
-        spb[kp] = o1.r;
-        spb[NPB * NPT + kp] = o2.r;
+        spb[kq] = o1.r;
+        spb[NPB * NPTC + kq] = o2.r;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) {
-            spb[(1 + k) * NPT + kp] = o1.v[k];
-            spb[(NPB + 1 + k) * NPT + kp] = o2.v[k];
+            spb[(1 + k) * NPTC + kq] = o1.v[k];
+            spb[(NPB + 1 + k) * NPTC + kq] = o2.v[k];
         }
-        spb[(1 + DIM) * NPT + kp] = o1.b;
-        spb[(NPB + 1 + DIM) * NPT + kp] = o2.b;
+        spb[(1 + DIM) * NPTC + kq] = o1.b;
+        spb[(NPB + 1 + DIM) * NPTC + kq] = o2.b;
         if constexpr (A::KG) {
-            spb[(2 + DIM) * NPT + kp] = o1.e;
-            spb[(NPB + 2 + DIM) * NPT + kp] = o2.e;
+            spb[(2 + DIM) * NPTC + kq] = o1.e;
+            spb[(NPB + 2 + DIM) * NPTC + kq] = o2.e;
         }
     }
 }
@@ -2344,18 +2367,19 @@ __device__ __forceinline__ void adj_split_pairs(const AdjElemParams& P, int e0, 
 // G: also the node's projected-state pair cotangents (snode), the spread of the projected
 // entropy-variable cotangents (into wb), and the trace cotangents through l at every node (G and
 // H: not yet known; the stage's second element pass adds them).
-template <int DIM, int N, int D, int TP, bool CURV = false, bool G = false, bool H = false>
+template <int DIM, int N, int D, int TP, bool CURV = false, bool G = false, bool H = false, int CH = 1>
 __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, int el, int i, int64_t gi,
                                                 const double* Dsh, const double* sw, const double* spb,
                                                 const double* v, double rho, double p, double g1, double* qb,
                                                 PrimBar& acc, const double* snode = nullptr,
-                                                const double* sWb = nullptr, double* wb = nullptr) {
+                                                const double* sWb = nullptr, double* wb = nullptr, int chunk = 0) {
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, G>;
     constexpr int NV = DIM + 2, NN = S::NN, NFD = S::NFD, NPAIR = S::NPAIR;
-    constexpr int NPT = A::NPT, NPB = A::NPB;
+    constexpr int NPB = A::NPB, NPTC = A::NPT / CH;
     int pos, line;
     tp_coords<DIM>(N, i, D, pos, line);
+    if (CH > 1 && line / (NFD / CH) != chunk) return;   // the node's line is in another chunk
     const int tid = threadIdx.x;
     double dii = Dsh[pos + pos * N];
     if (dii != 0.0) {   // diagonal: F♯(i, i) = F(Q_i)
@@ -2375,7 +2399,7 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
             euler_flux_vjp<DIM>(D, v, vv, Hq, g1, Gd, -P.Ja[e * DIM + D], qb);
         }
     }
-    int pbase = el * NFD * NPAIR + line * NPAIR;
+    int pbase = el * NFD * NPAIR + line * NPAIR - chunk * NPTC;
     // the N-1 partners of pos, cyclically from pos + 1: every iteration is a pair (a skipped
     // j == pos would still take its FP64 issue slots as predicated-off instructions)
 #pragma unroll
@@ -2383,12 +2407,12 @@ __device__ __forceinline__ void adj_split_nodes(const AdjElemParams& P, int e, i
         const int j = pos + t < N ? pos + t : pos + t - N;
         int lo = j < pos ? j : pos, hi = j < pos ? pos : j;
         int pidx = pbase + lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
-        const double* src = spb + (pos == lo ? 0 : NPB * NPT);
+        const double* src = spb + (pos == lo ? 0 : NPB * NPTC);
         acc.r += src[pidx];
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPT + pidx];
-        acc.b += src[(1 + DIM) * NPT + pidx];
-        if constexpr (A::KG) acc.e += src[(2 + DIM) * NPT + pidx];
+        for (int k = 0; k < DIM; ++k) acc.v[k] += src[(1 + k) * NPTC + pidx];
+        acc.b += src[(1 + DIM) * NPTC + pidx];
+        if constexpr (A::KG) acc.e += src[(2 + DIM) * NPTC + pidx];
     }
     if constexpr (G) {
         const int tid = threadIdx.x;
@@ -2464,13 +2488,13 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
     using S = Shape<DIM, N>;
     using A = AdjSplitShape<DIM, N, TP, G, H>;
     constexpr int NV = DIM + 2, NPE = S::NPE, NN = S::NN;
-    constexpr int NPT = A::NPT, NPB = A::NPB, NARR = A::NARR;
+    constexpr int NPB = A::NPB, NARR = A::NARR;
     extern __shared__ double smem[];
     double* sops = smem;
     double* sprim = sops + S::NOPS;   // [NARR][NN]: ρ/2, v/2, β/2, |v|²/4 (KG: ρ/2, v/2, p/2, (E/ρ)/2)
     double* sw = sprim + NARR * NN;   // [NV][NN]: w = λ / J
-    double* spb = sw + NV * NN;       // [2][NPB][NPT]: side-1 / side-2 cotangents of each pair
-    double* sJD = spb + 2 * NPB * NPT;   // [EPB][DIM][N*N]: -Ja_d D♯
+    double* spb = sw + NV * NN;       // [2][NPB][NPTC]: side-1 / side-2 cotangents of each pair (of a chunk)
+    double* sJD = spb + 2 * NPB * A::NPTC;   // [EPB][DIM][N*N]: -Ja_d D♯
     double* sWb = sJD + A::NSD;          // G: [NV][NPROJ] projected entropy-variable cotangents
     double* snode = sWb + NV * A::NPROJ; // G: [NPB][NN] projected-state pair cotangents per node
     double* sHy = snode + (G ? NPB * NN : 0);   // H: [NV][NN] subcell fluxes, then the pair weights
@@ -2579,31 +2603,39 @@ __global__ void __launch_bounds__(Shape<DIM, N>::BLOCK, AdjSplitShape<DIM, N, TP
                 adj_hybrid_dir<DIM, N, D2, TP, CURV>(P, e0, active, el, i, sops, sprim, sw, sHy, spb, stab, sWn,
                                                      qb);
         }
-        if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
-        else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
-        else adj_split_pairs<DIM, N, D2, TP, CURV>(P, e0, sJD, sprim, swd, spb, stab, cb);
-        if constexpr (G) {
-            constexpr bool WC = A::WC;
-            if (dir == 0)
-                adj_split_projection<DIM, N, 0, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
-            else if (dir == 1)
-                adj_split_projection<DIM, N, D1, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
-            else
-                adj_split_projection<DIM, N, D2, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
+        constexpr int CH = A::CH;
+#pragma unroll 1
+        for (int ch = 0; ch < CH; ++ch) {   // CH > 1: the lines in chunks, each its pairs then its nodes
+            if (dir == 0) adj_split_pairs<DIM, N, 0, TP, CURV, CH>(P, e0, sJD, sprim, swd, spb, stab, cb, ch);
+            else if (dir == 1) adj_split_pairs<DIM, N, D1, TP, CURV, CH>(P, e0, sJD, sprim, swd, spb, stab, cb, ch);
+            else adj_split_pairs<DIM, N, D2, TP, CURV, CH>(P, e0, sJD, sprim, swd, spb, stab, cb, ch);
+            if constexpr (G) {
+                constexpr bool WC = A::WC;
+                if (ch == 0) {
+                    if (dir == 0)
+                        adj_split_projection<DIM, N, 0, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb, sWn);
+                    else if (dir == 1)
+                        adj_split_projection<DIM, N, D1, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb,
+                                                                         sWn);
+                    else
+                        adj_split_projection<DIM, N, D2, TP, CURV, H, WC>(P, e0, sops, sprim, swd, snode, sWb, cb,
+                                                                         sWn);
+                }
+            }
+            __syncthreads();
+            if (active) {
+                if (dir == 0)
+                    adj_split_nodes<DIM, N, 0, TP, CURV, G, H, CH>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb,
+                                                                   acc, snode, sWb, wb, ch);
+                else if (dir == 1)
+                    adj_split_nodes<DIM, N, D1, TP, CURV, G, H, CH>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb,
+                                                                    acc, snode, sWb, wb, ch);
+                else
+                    adj_split_nodes<DIM, N, D2, TP, CURV, G, H, CH>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb,
+                                                                    acc, snode, sWb, wb, ch);
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        if (active) {
-            if (dir == 0)
-                adj_split_nodes<DIM, N, 0, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
-                                                           snode, sWb, wb);
-            else if (dir == 1)
-                adj_split_nodes<DIM, N, D1, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
-                                                            snode, sWb, wb);
-            else
-                adj_split_nodes<DIM, N, D2, TP, CURV, G, H>(P, e, el, i, gi, Dsh, swd, spb, v, rho, p, g1, qb, acc,
-                                                            snode, sWb, wb);
-        }
-        __syncthreads();
     }
     if (!active) return;
     double vv = 0.0;
@@ -2676,9 +2708,8 @@ cudaError_t launch_adj_split(int n, int tp, const AdjElemParams& P, cudaStream_t
     return launch_adj_split_tp<DIM, FLOU_TP_CHANDRASHEKAR, CURV, G, H>(n, P, s);
 }
 
-// Whether the split adjoint tile (G: Gauss nodes, H: the hybrid operator) fits in shared memory:
-// all but the 3D p=7 tiles of the Gauss-node forms (the split form's with the Kennedy-Gruber flux,
-// the hybrid operator's with every two-point flux) do.
+// Whether the split adjoint tile (G: Gauss nodes, H: the hybrid operator) fits in shared memory
+// (with the pairs in two chunks of lines where all of them at once do not: every tile does).
 template <int TP>
 constexpr size_t adj_split_smem_3d8(bool G, bool H) {
     return G && H ? AdjSplitShape<3, 8, TP, true, true>::SMEM

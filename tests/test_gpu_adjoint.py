@@ -601,15 +601,23 @@ def test_gauss_nodes_split_adjoint_solve_against_dual_numbers(op):
         assert abs(ours - dJo) <= 1e-10 * abs(dJo), (ours, dJo)
 
 
-def test_gauss_nodes_split_adjoint_limits():
-    """Not covered: the Kennedy-Gruber 3D p=7 tile (beyond shared memory)."""
-    from flou_cuda import _lib as L
-    kg = build(3, 8, (1, 1, 1), F.EulerEquation(3, 1.4), OPERATORS["split_kg"](), basis="GL")
-    Q = _dev(smooth_euler_state(kg, seed=1))
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        kg.ctx.rhs_vjp(g, None, Q, Q)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+def test_gauss_nodes_split_adjoint_3d_p7_kennedy_gruber():
+    """The Kennedy-Gruber 3D p=7 tile on Gauss nodes, whose pair cotangents go in two chunks of
+    lines (all at once they exceed shared memory), against the oracle's dual numbers."""
+    disc = build(3, 8, (2, 2, 1), F.EulerEquation(3, 1.4), OPERATORS["split_kg"](), basis="GL")
+    Q = smooth_euler_state(disc, seed=31, amp=0.2)
+    rng = np.random.default_rng(131)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c = _with_c(disc, "split_kg", 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + np.sum(cbar.cpu().numpy() * dc)
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
 
 
 HYBRID_OPS = {
@@ -818,15 +826,28 @@ def test_gauss_nodes_hybrid_adjoint_through_limiter_and_2n_storage(integrator, l
         disc.ctx.set_integrator(None)
 
 
-def test_hybrid_adjoint_limits():
-    """Not covered: the hybrid operator on Gauss nodes at 3D p=7 (beyond shared memory)."""
-    from flou_cuda import _lib as L
-    disc = build(3, 8, (1, 1, 1), F.EulerEquation(3, 1.4), HYBRID_OPS["hybrid_hllc"](), basis="GL")
-    Q = _dev(smooth_euler_state(disc, seed=1))
-    g = torch.empty_like(Q)
-    with pytest.raises(F.FlouError) as ei:
-        disc.ctx.rhs_vjp(g, None, Q, Q)
-    assert ei.value.status == L.FLOU_ERR_UNSUPPORTED
+@pytest.mark.parametrize("op,basis", [("hybrid_hllc", "GL"), ("hybrid_kg", "GL"), ("hybrid_std_hll", "GL"),
+                                      ("hybrid_kg", "GLL"), ("hybrid_md", "GLL")])
+def test_hybrid_adjoint_3d_p7(op, basis):
+    """The 3D p=7 hybrid tiles: on Gauss nodes (every two-point flux) and with the Kennedy-Gruber
+    flux the pair cotangents go in two chunks of lines; the MatrixDissipation tile on Gauss-Lobatto
+    nodes keeps the nodes' entropy variables in the last 198 bytes of shared memory.  Against the
+    oracle's dual numbers."""
+    eq = F.EulerEquation(3, 1.4)
+    disc = build(3, 8, (2, 2, 1), eq, HYBRID_OPS[op](), basis=basis)
+    Q = smooth_euler_state(disc, seed=32, amp=0.3)
+    rng = np.random.default_rng(132)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _hybrid_c(disc, op, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
 
 
 def _maybe_c(disc, c):
@@ -856,6 +877,28 @@ def test_general_geometry_gauss_split_and_hybrid_rhs_vjp(dim, n, op, basis):
         assert len(set(disc.mesh.orientation.tolist())) == 8
     rng = np.random.default_rng(100 + dim + n)
     Q = _state(disc, seed=dim * 3 + n)
+    lam = rng.standard_normal(Q.shape)
+    dQ = rng.standard_normal(Q.shape)
+    c, noc = _maybe_c(disc, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
+    dc = 0.0 * c if noc else rng.standard_normal(c.shape)
+    Qbar = torch.empty(Q.shape[::-1], dtype=torch.float64, device="cuda")
+    cbar = None if noc else torch.empty(disc.mesh.nelements, dtype=torch.float64, device="cuda")
+    disc.ctx.rhs_vjp(Qbar, cbar, _dev(Q), _dev(lam))
+    lhs = np.sum(_host(Qbar) * dQ) + (0.0 if noc else np.sum(cbar.cpu().numpy() * dc))
+    R, dR = oracle_for(disc).rhs_jvp(Q, dQ, c, dc)
+    rhs = np.sum(lam * dR)
+    assert abs(lhs - rhs) <= 1e-12 * np.sum(np.abs(lam * dR)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("op,basis", [("split_kg_lxf", "GL"), ("hybrid_hllc", "GL"), ("hybrid_kg", "GLL")])
+def test_general_geometry_3d_p7_tiles_rhs_vjp(op, basis):
+    """The chunked 3D p=7 tiles on rotated general elements (every orientation), against the
+    oracle's dual numbers."""
+    from test_gpu_unstructured import _disc as _udisc
+    from test_unstructured import _state
+    disc = _udisc(3, 8, op, basis=basis, nel=2)
+    rng = np.random.default_rng(140)
+    Q = _state(disc, seed=41)
     lam = rng.standard_normal(Q.shape)
     dQ = rng.standard_normal(Q.shape)
     c, noc = _maybe_c(disc, 1.0 + 0.3 * rng.random(disc.mesh.nelements))
