@@ -274,10 +274,9 @@ int32_t flou_check_refined_math(int64_t nsamples, double* rcp_err, double* sqrt_
  *  - periodic, slip-wall, outflow, inflow and boundary-state-field boundaries (fixed external
  *    states are constants of the differentiation);
  *  - SSP-RK3 or the 2N-storage method set by flou_set_integrator, with or without the Zhang-Shu
- *    stage limiter (in flou_adjoint_solve_batch each instance with its own).
- * Other contexts (the 3D p=7 tiles beyond shared memory: the Gauss-node hybrid operator, and the
- * Kennedy-Gruber flux in the Gauss-node split form and the Gauss-Lobatto hybrid operator) return
- * FLOU_ERR_UNSUPPORTED.
+ *    stage limiter (in flou_adjoint_solve_batch each instance with its own);
+ *  - every order p = 1..7.
+ * Other contexts return FLOU_ERR_UNSUPPORTED.
  * Non-smooth points follow Julia's Base (ForwardDiff on the reference's CPU path):
  * max(a, b) takes b unless b < a; d|u|/du = -1 for a set sign bit, else +1. */
 
