@@ -47,7 +47,7 @@ def test_connectivity_bit_exact(dim, start, finish, n):
             assert m.bdmap.get(bid, 0) == o["bdindex_of_id"][bid - 1]
 
 
-def test_face_counts_of_survey_configs():
+def test_face_counts_of_the_vortex_and_tgv_meshes():
     m = F.CartesianMesh((-5, -5), (5, 5), (16, 16))
     assert m.nfaces == 17 * 16 * 2 == 544
     F.apply_periodicBCs(m, ("1", "2"), ("3", "4"))
