@@ -1484,66 +1484,73 @@ __device__ __forceinline__ void split_tile(const ElemParams& P, int e0, double* 
                 }
                 __syncthreads();
             }
-            if (active) {
-                int pos, line;
-                tp_coords<DIM>(N, i, dir, pos, line);
-                if (pos > 0) {   // the subcell interface between positions pos-1 and pos
-                    const int il = el * NPE + tp_node<DIM>(N, dir, line, pos - 1);
-                    double Fh[NV];
+            // One thread per subcell interface (between positions pos-1 and pos, pos = 1..N-1), the
+            // block's interfaces numbered consecutively: the threads beyond them (one in N) leave
+            // whole warps idle instead of one lane in every warp.  The result goes to the slot of
+            // the interface's right node.
+            constexpr int NFV = S::EPB * NFD * (N - 1);
+            for (int t = tid; t < NFV; t += blockDim.x) {
+                const int elp = t / (NFD * (N - 1));
+                const int rr = t - elp * (NFD * (N - 1));
+                const int line = rr / (N - 1), pos = 1 + (rr - line * (N - 1));
+                const int ef = e0 + elp;
+                if (ef >= P.nelem) continue;
+                const int jn = elp * NPE + tp_node<DIM>(N, dir, line, pos);
+                const int il = elp * NPE + tp_node<DIM>(N, dir, line, pos - 1);
+                double Fh[NV];
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) Fh[k] = GAUSS ? 0.0 : sH[k * NN + tid];
-                    // FV flux in the subcell interface's frame times its surface Jacobian
-                    // (PhysicalRegions.jl:68-300): the positive axis and Ja_dd on a Cartesian
-                    // element, the uploaded subgrid geometry on a general one
-                    double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV];
-                    const int64_t gl = (int64_t)e * NPE + (il - el * NPE);
+                for (int k = 0; k < NV; ++k) Fh[k] = GAUSS ? 0.0 : sH[k * NN + jn];
+                // FV flux in the subcell interface's frame times its surface Jacobian
+                // (PhysicalRegions.jl:68-300): the positive axis and Ja_dd on a Cartesian
+                // element, the uploaded subgrid geometry on a general one
+                double ql[NV], qr[NV], a[NV], b[NV], Fr[NV], Fv[NV];
+                const int64_t gl = (int64_t)e0 * NPE + il, gr = (int64_t)e0 * NPE + jn;
 #pragma unroll
-                    for (int k = 0; k < NV; ++k) {
-                        ql[k] = P.Q[k * P.ndofs + gl];
-                        qr[k] = q[k];
+                for (int k = 0; k < NV; ++k) {
+                    ql[k] = P.Q[k * P.ndofs + gl];
+                    qr[k] = P.Q[k * P.ndofs + gr];
+                }
+                if constexpr (CURV) {
+                    const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
+                    const int64_t si = (((int64_t)ef * DIM + dir) * NFD + line) * (N + 1) + pos;
+                    FrameTab fr;
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        fr.n[r] = P.subfr[r * ns + si];
+                        fr.t[r] = P.subfr[(3 + r) * ns + si];
+                        fr.b[r] = P.subfr[(6 + r) * ns + si];
                     }
-                    if constexpr (CURV) {
-                        const int64_t ns = (int64_t)P.nelem * DIM * NFD * (N + 1);
-                        const int64_t si = (((int64_t)e * DIM + dir) * NFD + line) * (N + 1) + pos;
-                        FrameTab fr;
+                    rotate_to_face<DIM>(ql, fr, a);
+                    rotate_to_face<DIM>(qr, fr, b);
+                    euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                    rotate_to_phys<DIM>(Fr, fr, Fv);
+                    const double Js = P.subJ[si];
 #pragma unroll
-                        for (int r = 0; r < 3; ++r) {
-                            fr.n[r] = P.subfr[r * ns + si];
-                            fr.t[r] = P.subfr[(3 + r) * ns + si];
-                            fr.b[r] = P.subfr[(6 + r) * ns + si];
-                        }
-                        rotate_to_face<DIM>(ql, fr, a);
-                        rotate_to_face<DIM>(qr, fr, b);
-                        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
-                        rotate_to_phys<DIM>(Fr, fr, Fv);
-                        const double Js = P.subJ[si];
+                    for (int k = 0; k < NV; ++k) Fv[k] = Fv[k] * Js;
+                } else {
+                    FrameAxes A = frame_axes<DIM>(2 * dir + 1);
+                    a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
+                    cart_to_face<DIM>(ql, A, a);
+                    cart_to_face<DIM>(qr, A, b);
+                    euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
+                    const double Js = P.elem_Ja[ef * DIM + dir];
+                    Fv[0] = Fr[0] * Js;
+                    Fv[DIM + 1] = Fr[DIM + 1] * Js;
+                    cart_to_phys<DIM>(Fr, A, Fv);
 #pragma unroll
-                        for (int k = 0; k < NV; ++k) Fv[k] = Fv[k] * Js;
-                    } else {
-                        FrameAxes A = frame_axes<DIM>(2 * dir + 1);
-                        a[0] = ql[0]; b[0] = qr[0]; a[DIM + 1] = ql[DIM + 1]; b[DIM + 1] = qr[DIM + 1];
-                        cart_to_face<DIM>(ql, A, a);
-                        cart_to_face<DIM>(qr, A, b);
-                        euler_numflux<DIM>(a, b, P.fvflux, P.fvavg, P.fvintensity, g, Fr);
-                        const double Js = P.elem_Ja[e * DIM + dir];
-                        Fv[0] = Fr[0] * Js;
-                        Fv[DIM + 1] = Fr[DIM + 1] * Js;
-                        cart_to_phys<DIM>(Fr, A, Fv);
+                    for (int k = 0; k < DIM; ++k) Fv[1 + k] = Fv[1 + k] * Js;
+                }
+                if constexpr (GAUSS) {   // blended in the scan below
 #pragma unroll
-                        for (int k = 0; k < DIM; ++k) Fv[1 + k] = Fv[1 + k] * Js;
-                    }
-                    if constexpr (GAUSS) {   // blended in the scan below
+                    for (int k = 0; k < NV; ++k) sFb[k * NN + jn] = Fv[k];
+                } else {
+                    double bb = 0.0;
 #pragma unroll
-                        for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = Fv[k];
-                    } else {
-                        double bb = 0.0;
+                    for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + jn] - sW[k * NN + il], Fh[k] - Fv[k], bb);
+                    double dl = sqrt_refined(fma(bb, bb, P.blend));
+                    dl = fmax((dl - bb) * rcp_refined(dl), 0.5);
 #pragma unroll
-                        for (int k = 0; k < NV; ++k) bb = fma(sW[k * NN + tid] - sW[k * NN + il], Fh[k] - Fv[k], bb);
-                        double dl = sqrt_refined(fma(bb, bb, P.blend));
-                        dl = fmax((dl - bb) * rcp_refined(dl), 0.5);
-#pragma unroll
-                        for (int k = 0; k < NV; ++k) sFb[k * NN + tid] = fma(dl, Fh[k] - Fv[k], Fv[k]);
-                    }
+                    for (int k = 0; k < NV; ++k) sFb[k * NN + jn] = fma(dl, Fh[k] - Fv[k], Fv[k]);
                 }
             }
             __syncthreads();
