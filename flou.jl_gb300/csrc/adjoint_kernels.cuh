@@ -2140,23 +2140,34 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
             if (pos == 0) sF2[k * NN + tid] = -fls;   // F_0, read by the line's scan
         }
     }
-    if (active && pos > 0) {   // the FV flux of the interface on the node's left, and the entropy jump
-        const int il = el * NPE + tp_node<DIM>(N, D, line, pos - 1);
-        const int64_t gl = (int64_t)e0 * NPE + il;
+    __syncthreads();   // the node phase has read sF2, whose interface slots the FV phase writes
+    // the FV flux and the entropy jump of every subcell interface, one thread per interface (the
+    // block's interfaces numbered consecutively: the spare threads are whole idle warps), into
+    // the slot of the interface's right node
+    constexpr int NFV = S::EPB * NFD * (N - 1);
+    for (int t = tid; t < NFV; t += blockDim.x) {
+        const int elp = t / (NFD * (N - 1));
+        const int rr = t - elp * (NFD * (N - 1));
+        const int ln = rr / (N - 1), ps = 1 + (rr - ln * (N - 1));
+        const int ef = e0 + elp;
+        if (ef >= P.nelem) continue;
+        const int jn = elp * NPE + tp_node<DIM>(N, D, ln, ps);
+        const int il = elp * NPE + tp_node<DIM>(N, D, ln, ps - 1);
+        const int64_t gl = (int64_t)e0 * NPE + il, gr = (int64_t)e0 * NPE + jn;
         double ql[NV], qr[NV], Fv[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             ql[k] = P.U[k * P.ndofs + gl];
-            qr[k] = P.U[k * P.ndofs + gi];
+            qr[k] = P.U[k * P.ndofs + gr];
         }
         SubcellFace<DIM> sf;
-        subcell_fv<DIM, N, D, CURV>(P, e, line, pos, Ja, ql, qr, sf, Fv);
+        subcell_fv<DIM, N, D, CURV>(P, ef, ln, ps, CURV ? 1.0 : P.Ja[ef * DIM + D], ql, qr, sf, Fv);
         double wl[NV], wr[NV];
         if constexpr (A::WC) {
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 wl[k] = sWn[k * NN + il];
-                wr[k] = sWn[k * NN + tid];
+                wr[k] = sWn[k * NN + jn];
             }
         } else {
             entropy_of<DIM>(ql, g, wl);
@@ -2164,8 +2175,8 @@ __device__ __forceinline__ void adj_hybrid_gauss_dir(const AdjElemParams& P, int
         }
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            sF2[k * NN + tid] = Fv[k];
-            sdW[k * NN + tid] = wr[k] - wl[k];
+            sF2[k * NN + jn] = Fv[k];
+            sdW[k * NN + jn] = wr[k] - wl[k];
         }
     }
     __syncthreads();
