@@ -2,8 +2,8 @@
 //
 // CPU restatement of Flou.jl's DGSEM residual `rhs!` and its set-up (Cartesian mesh
 // connectivity with periodic stitching, Lagrange operators, Cartesian geometry), plus the
-// Shu-Osher SSP-RK3 integrator and the CFL time step.  It is the checker that the CUDA
-// library is compared against; nothing in the product links, imports or runs it.
+// Shu-Osher SSP-RK3 integrator and the CFL time step.  The CUDA library is compared against
+// it; nothing in the product links, imports or runs it.
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
 //
 // Parity status of this oracle (pinning):

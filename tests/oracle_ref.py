@@ -1,6 +1,6 @@
 """ctypes front-end of the CPU oracle (oracle/liboracle.so) for the tests.
 
-Test infrastructure: the oracle is the checker the CUDA library is compared against.
+Test infrastructure: the oracle the CUDA library is compared against.
 """
 import ctypes
 import os

@@ -1,6 +1,6 @@
 """The benchmark configurations at full size.
 
-Config 1 (2D vortex, 16² elements, p=4, strong form, Rusanov, 100 SSP-RK3 steps) against the
+The 2D vortex (16² elements, p=4, strong form, Rusanov, 100 SSP-RK3 steps) against the
 oracle; the 3D Taylor-Green meshes (32³ p=3 and 16³ p=7, split form Chandrashekar + HLLC,
 2,097,152 nodes each) through one residual (backward error and relative L-inf against the
 oracle's own conditioning floor) and the configuration's 50 SSP-RK3 steps against the oracle,

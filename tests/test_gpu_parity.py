@@ -1,6 +1,6 @@
 """GPU parity: libflou_cuda against the CPU oracle on the same inputs, through the C ABI.
 
-Bars (north-star): one residual to <= 1e-12 relative L-inf per variable, N SSP-RK3 steps to
+Bars: one residual to <= 1e-12 relative L-inf per variable, N SSP-RK3 steps to
 <= 1e-10; connectivity/index work is bit-exact (set-up tests).  Relative L-inf is
 max_v max_i |a - b| / max_i |b| per variable.
 """
