@@ -109,8 +109,7 @@ int adj_supported(flou_ctx* c) {
         return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the split form needs the DGSEM lift on a basis "
                                                  "with boundary nodes");
     if (k.volume_op == FLOU_OP_SPLIT && !c->bnodes && !adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, true, false))
-        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile of the Kennedy-Gruber flux at "
-                                                 "3D p=7 exceeds shared memory");
+        return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the Gauss-node split adjoint tile exceeds shared memory");
     if (k.volume_op == FLOU_OP_HYBRID) {
         if (c->bnodes && !c->lift_ends)
             return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the adjoint of the hybrid operator covers Gauss-Lobatto and "
@@ -120,10 +119,7 @@ int adj_supported(flou_ctx* c) {
                                                      "Scalar- or MatrixDissipation (StdAverage or "
                                                      "ChandrasekharAverage), HLL or HLLC for the adjoint");
         if (!adj_split_tile_fits(k.dim, c->n, k.twopoint_flux, !c->bnodes, true))
-            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, c->bnodes ? "the hybrid adjoint tile of the Kennedy-Gruber flux at "
-                                                                 "3D p=7 exceeds shared memory"
-                                                               : "the Gauss-node hybrid adjoint tile at 3D p=7 exceeds "
-                                                                 "shared memory");
+            return ctx_fail(c, FLOU_ERR_UNSUPPORTED, "the hybrid adjoint tile exceeds shared memory");
     }
     return FLOU_OK;
 }
